@@ -1,0 +1,227 @@
+/*
+ * yukawa.h -- C ABI of libyukawa_gb300.so, the GB300-native Langevin hot path
+ * of the 2-D Yukawa model of Matteo294/YukawaColouredNoise.
+ *
+ * The reference exposes no plugin/FFI API; its boundaries are the in-process
+ * C++ classes DiracOP, CGsolver, FermionicDrift, ColouredNoise, the `Run`
+ * kernel, the input.toml schema and the `./out input.toml` CLI.  Each entry
+ * point below names the reference interface it replaces (paths relative to
+ * the reference project).
+ *
+ * Conventions
+ *   - Every function returns a yk_status (YK_OK == 0); yk_last_error() gives
+ *     the message of the last failure on the calling thread.
+ *   - Buffers passed as `void*`/`double*` to operator calls are DEVICE
+ *     pointers unless the name says host.  Spinors are 4 complex per site
+ *     ([f1s1, f1s2, f2s1, f2s2], interleaved re/im, code/src/Spinor.cuh:7-16),
+ *     site n = t*Nx + x (code/src/Lattice.cu:16-18).
+ *   - All work is ordered on the context's stream (yk_ctx_set_stream); calls
+ *     that return host values synchronise that stream.
+ *   - One context per host thread; a context is not thread-safe.
+ */
+#ifndef YUKAWA_GB300_H
+#define YUKAWA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum yk_status {
+    YK_OK = 0,
+    YK_EINVAL = 1,    /* bad argument, size or unsupported combination      */
+    YK_ENOCONV = 2,   /* CG reached its iteration cap without converging     */
+    YK_ENAN = 3,      /* NaN/Inf met in a residual, drift or field           */
+    YK_ETIMEOUT = 4,  /* a bounded device-side wait gave up                  */
+    YK_ECUDA = 5,     /* CUDA runtime error                                  */
+    YK_ENOMEM = 6,    /* device allocation failed                            */
+    YK_EIO = 7        /* file could not be read or written                   */
+} yk_status;
+
+enum { YK_NORMAL = 0, YK_DAGGER = 1 };          /* MatrixType, code/src/params.h:8 */
+enum { YK_FP64 = 0, YK_FP32 = 1, YK_MIXED = 2 }; /* arithmetic of a call           */
+enum { YK_TOL_ABS = 0, YK_TOL_REL = 1 };         /* CG stopping rule               */
+enum { YK_INIT_DRAND48 = 0, YK_INIT_PHILOX = 1, YK_INIT_NONE = 2 };
+
+/*
+ * Run parameters: the reference's input.toml keys (code/input.toml:1-28, read
+ * at code/src/main.cu:112-170), the lattice size that the reference fixes at
+ * compile time (code/src/params.h:28, patched by runs.py:80-85), and the
+ * [gpu] extension keys.  yk_params_default() gives the reference's defaults:
+ * compile-time tolerance 1e-8 absolute and IterMax 1000 (code/src/params.h:13-15).
+ */
+typedef struct yk_params {
+    /* [physics] */
+    int use_mass;              /* useMass == "true"                              */
+    double mass;               /* m^2 when use_mass                              */
+    double g;                  /* lambda when use_mass                           */
+    double kappa;              /* hopping parameter when !use_mass               */
+    double lambda;             /* lattice lambda when !use_mass                  */
+    double cut_fraction;       /* cutFraction s: keep |p| <= sqrt(2) pi s        */
+    /* [langevin] */
+    double average_epsilon;
+    double max_langevin_time;
+    double export_time;
+    int burn_count;
+    int measure_drift_count;
+    /* [random] */
+    int64_t seed;
+    /* [fermions] */
+    double yukawa_coupling;
+    double fermion_mass;
+    int drift_mode;            /* 0 normal, 1 rescaled by cutFraction^2          */
+    double wilson_param;
+    /* [lattice] */
+    int Nt, Nx;
+    /* [gpu] extensions (not in the reference) */
+    int precision;             /* YK_FP64 or YK_MIXED for the CG of each step     */
+    int n_rhs;                 /* stochastic right-hand sides per step (1 = ref) */
+    int cg_tol_mode;           /* YK_TOL_ABS (reference) or YK_TOL_REL            */
+    double cg_tol;             /* 1e-8 (reference)                                */
+    int cg_max_iter;           /* 1000 (reference)                                */
+    int reliable_every;        /* mixed precision: FP64 residual every N iters    */
+    double fixed_dt;           /* > 0: fixed Euler step instead of adaptive eps   */
+    int init;                  /* YK_INIT_DRAND48 (reference), YK_INIT_PHILOX     */
+} yk_params;
+
+/* Parameters after the reference's conversion (main.cu:58-63, 113-170). */
+typedef struct yk_action {
+    double m2, lambda, kappa, sq2kappa, g, m0, r, cut_fraction, eps_bar;
+    int drift_mode, use_mass;
+} yk_action;
+
+typedef struct yk_solve_stats {
+    int iterations;            /* CG iterations (summed over right-hand sides)   */
+    int reliable_updates;      /* FP64 residual recomputations (mixed)           */
+    double rr;                 /* final |r|^2 of the solver                      */
+    double rr0;                /* |b|^2                                          */
+    int converged;             /* 1 if every system met its stopping rule        */
+} yk_solve_stats;
+
+/* Per-chain observables of the last step (langevin_gpu_v2.cu:65-118,
+ * reductions.cu:106-140, 200-233). */
+typedef struct yk_obs {
+    double t;                  /* Langevin time accumulated by yk_langevin_step  */
+    double eps;                /* step size of the last step                      */
+    double max_drift;          /* clamped max |drift| of the last step            */
+    double sum_phi;            /* sum_n sigma_n after the step                   */
+    double sum_phi2;           /* sum_n sigma_n^2                                 */
+    double sum_force;          /* sum_n F_n of the step's fermion force          */
+    int64_t steps;             /* steps taken by this chain                       */
+    int cg_iterations;         /* CG iterations of the last step                  */
+    int status;                /* yk_status of the last step                      */
+} yk_obs;
+
+typedef struct yk_ctx yk_ctx;
+
+const char* yk_last_error(void);
+const char* yk_version(void);
+
+/* ---------------------------------------------------------------- params */
+/* Defaults of code/input.toml and code/src/params.h. */
+void yk_params_default(yk_params* p);
+/* Parse an input.toml (code/src/main.cu:112-170; [lattice] and [gpu] optional). */
+int yk_params_from_toml(const char* path, yk_params* p);
+/* main.cu:58-63 FindKappa and main.cu:113-170 conversion. */
+int yk_derive_action(const yk_params* p, yk_action* a);
+
+/* --------------------------------------------------------------- context */
+/* One context holds n_chains independent chains (each with its own size and
+ * couplings, params[c]).  Replaces the reference's global __constant__
+ * parameter set (main.cu:268-278) and the objects built at main.cu:172-242. */
+int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** ctx);
+int yk_ctx_destroy(yk_ctx* ctx);
+int yk_ctx_set_stream(yk_ctx* ctx, void* cuda_stream);
+/* Waits for the context's stream; reports device-side wait timeouts. */
+int yk_ctx_synchronize(yk_ctx* ctx);
+int yk_ctx_n_chains(const yk_ctx* ctx);
+int yk_ctx_volume(const yk_ctx* ctx, int chain);
+int yk_ctx_shape(const yk_ctx* ctx, int chain, int* Nt, int* Nx);
+/* Scalar field sigma of a chain (main.cu:92-95 initial field).  Host pointers. */
+int yk_set_field_host(yk_ctx* ctx, int chain, const double* phi);
+int yk_get_field_host(yk_ctx* ctx, int chain, double* phi);
+/* Device pointer of the chain's field (V doubles), owned by the context. */
+int yk_field_device(yk_ctx* ctx, int chain, double** phi);
+
+/* ------------------------------------------------------------- operators */
+/* DiracOP<double>::applyD(in, out, MatrixType) (code/src/Dirac.cuh:22,
+ * Dirac.cu:23-35): out = D in or D^dag in with sigma = the chain's field.
+ * precision YK_FP64: double2 buffers; YK_FP32: float2 buffers. */
+int yk_dirac_apply(yk_ctx* ctx, int chain, const void* in, void* out, int dagger, int precision);
+
+/* CGsolver::solve(in, out, D, MatrixType) (code/src/CGsolver.cuh:36,
+ * CGsolver.cu:42-59): solve A x = b with A = D^dag D (YK_DAGGER) or D D^dag
+ * (YK_NORMAL), x0 = 0.  b and x are FP64 complex.  precision YK_FP64 runs the
+ * reference's plain CG; YK_MIXED runs FP32 iterations with FP64 reliable
+ * updates and an FP64 final residual check.  Returns YK_ENOCONV if the cap
+ * is hit (the reference stops silently, CGsolver.cu:107). */
+int yk_cg_solve(yk_ctx* ctx, int chain, const void* b, void* x, int mtype, double tol,
+                int tol_mode, int max_iter, int precision, yk_solve_stats* stats);
+
+/* FermionicDrift::getForce (code/src/FermionicDrift.cuh:15, FermionicDrift.cu:57-100):
+ * F_n = -g Re sum_c conj(chi_{n,c}) eta_{n,c}, chi = D (D^dag D)^-1 eta, averaged
+ * over the chain's n_rhs right-hand sides; eta (n_rhs * 4V FP64 complex, device)
+ * may be NULL, then it is drawn from Philox at the chain's current step.
+ * F: V doubles, device. */
+int yk_fermion_force(yk_ctx* ctx, int chain, const void* eta, double* F, yk_solve_stats* stats);
+
+/* ColouredNoise::operator() (code/src/colouredNoise.h:33, colouredNoise.cpp:155-178):
+ * xi = Z2D(mask * D2Z(w)) with the sharp cutoff mask.  white: V doubles
+ * (device) or NULL to draw w from Philox at the chain's current step. */
+int yk_coloured_noise(yk_ctx* ctx, int chain, const double* white, double* xi);
+
+/* n_steps Langevin steps of every chain (main.cu:370-381: noise, force,
+ * Run kernel langevin_gpu_v2.cu:65-118), fully on the device; the step
+ * graph is captured once and replayed. */
+int yk_langevin_step(yk_ctx* ctx, int n_steps);
+
+/* The Run kernel (code/src/langevin_gpu_v2.cu:65-118, launched at main.cu:377)
+ * on injected inputs: drift = force + phi (m^2 + lambda/6 phi^2) - Lap phi,
+ * eps = epsBar*30/clamp(max|drift|) (or fixed_dt), phi -= eps drift +
+ * sqrt(2 eps) xi.  force, xi: V doubles (device).  Advances the chain's step
+ * counter and Langevin time like yk_langevin_step; obs may be NULL. */
+int yk_euler_update(yk_ctx* ctx, int chain, const double* force, const double* xi, yk_obs* obs);
+
+/* Host copy of a chain's last-step observables (synchronises the stream). */
+int yk_observables(yk_ctx* ctx, int chain, yk_obs* obs);
+
+/* gpuTimeSlices (reductions.cu:65-104): slices[t] = sum_x sigma(t, x); host out (Nt). */
+int yk_time_slices(yk_ctx* ctx, int chain, double* slices_host);
+
+/* Point-source fermion correlator (main.cu:441-469 + reductions.cu:176-191):
+ * y = D^dag (D D^dag)^-1 e0 with e0 = (1,1,0,0) at site 0, corr[t] = sum_x sum_c Re y;
+ * host out (Nt). */
+int yk_correlator(yk_ctx* ctx, int chain, double* corr_host, yk_solve_stats* stats);
+
+/* Condensate of main.cu:471-483: a fresh force estimate, tr = sum_n F_n / g
+ * (0 when g == 0); returns tr / V in *cond. */
+int yk_condensate(yk_ctx* ctx, int chain, double* cond, yk_solve_stats* stats);
+
+/* Langevin time-step control of main.cu:325-352: set the averageEpsilon used
+ * by the adaptive rule eps = epsBar * 30 / max|drift|. */
+int yk_set_eps_bar(yk_ctx* ctx, int chain, double eps_bar);
+int yk_get_step(yk_ctx* ctx, int chain, int64_t* step);
+int yk_set_step(yk_ctx* ctx, int chain, int64_t step);
+int yk_set_time(yk_ctx* ctx, int chain, double t);
+
+/* Checkpoint / resume of one chain: field, Philox step counter, Langevin time
+ * and epsBar in a small binary file.  The reference parses io.startFileName
+ * and io.resume (main.cu:146-157) but never reads or writes a configuration. */
+int yk_checkpoint_save(yk_ctx* ctx, int chain, const char* path, double eps_bar);
+int yk_checkpoint_load(yk_ctx* ctx, int chain, const char* path, double* eps_bar);
+
+/* --------------------------------------------------------------- analysis */
+/* Wolff Gamma-method (analysis/AutoCorrelation/ac.cpp:73-181, Wrapper :183-190):
+ * out = {mean, error, error of error, tau_int, tau_int error}; host buffers. */
+int yk_gamma_method(const double* data, int64_t n, double stau, double* out5);
+
+/* The full reference run protocol of main.cu:73-516 (burn-in, epsBar
+ * measurement, export loop, slice.dat / data.csv / traces.csv and stdout)
+ * from an input.toml; files are written into out_dir. */
+int yk_run_toml(const char* toml_path, const char* out_dir);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* YUKAWA_GB300_H */

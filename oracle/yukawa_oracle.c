@@ -1,0 +1,606 @@
+/*
+ * yukawa_oracle.c -- CPU FP64 restatement of the Langevin hot path of
+ * Matteo294/YukawaColouredNoise.  Every function cites the reference lines it
+ * follows (paths relative to the reference project).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+ * baseline.  The product library never links or calls this file.
+ *
+ * The reference has no CPU path (all of it is CUDA on managed memory); this is
+ * a restatement of its arithmetic in plain C with OpenMP over sites.  Complex
+ * numbers are interleaved (re, im) doubles, as thrust::complex<double> is laid
+ * out in the reference.
+ */
+#include "yukawa_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+int yko_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------- */
+/* Parameters: main.cu:58-63 (FindKappa), main.cu:113-170 (conversion).       */
+/* ------------------------------------------------------------------------- */
+static double find_kappa(double m2, double lambda0)
+{
+    /* main.cu:58-63, nDim = 2 */
+    const double nd2 = 2.0 * 2.0;
+    const double delta = (nd2 + m2) * (nd2 + m2) + 4.0 * lambda0 / 3.0;
+    return (-(nd2 + m2) + sqrt(delta)) / (2.0 * lambda0 / 3.0);
+}
+
+void yko_derive(int use_mass, double mass, double g_phys, double kappa, double lambda_in,
+                double yukawa_in, double fermion_mass, double wilson, double cut_fraction,
+                double average_epsilon, int drift_mode, yko_action* out)
+{
+    memset(out, 0, sizeof(*out));
+    if (use_mass) {
+        /* main.cu:117-122: m2 = mass, lambda = g, kappa from FindKappa */
+        out->m2 = mass;
+        out->lambda = g_phys;
+        out->kappa = find_kappa(mass, g_phys);
+    } else {
+        /* main.cu:123-129 */
+        out->kappa = kappa;
+        out->m2 = (1.0 - 2.0 * lambda_in) / kappa - 2.0 * 2.0;
+        out->lambda = 6.0 * lambda_in / (kappa * kappa);
+    }
+    out->sq2kappa = sqrt(2.0 * out->kappa);                         /* main.cu:130 */
+    out->g = use_mass ? yukawa_in : yukawa_in / out->sq2kappa;       /* main.cu:166-169 */
+    out->m0 = fermion_mass;                                          /* main.cu:163 */
+    out->r = wilson;                                                 /* main.cu:164 */
+    out->cut_fraction = cut_fraction;                                /* main.cu:131 */
+    out->eps_bar = average_epsilon;                                  /* main.cu:137 */
+    out->drift_mode = drift_mode;                                    /* main.cu:170 */
+    out->use_mass = use_mass;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Wilson-Dirac operator: Dirac.cu:37-70 (zero, diagonal) + :144-190 (hops).  */
+/* ------------------------------------------------------------------------- */
+void yko_dirac(int Nt, int Nx, const yko_action* a, const double* sigma,
+               const double* in, double* out, int dagger)
+{
+    const double r = a->r;
+    const int V = Nt * Nx;
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n < V; ++n) {
+        const int t = n / Nx, x = n % Nx;                      /* Lattice.cu:26-30 */
+        const int tu = ((t + 1) % Nt) * Nx + x;                /* Dirac.cu:10-21   */
+        const int td = ((t - 1 + Nt) % Nt) * Nx + x;
+        const int xu = t * Nx + (x + 1) % Nx;
+        const int xd = t * Nx + (x - 1 + Nx) % Nx;
+        /* antiperiodic time: Dirac.cu:161-162 */
+        const double s0 = (t == Nt - 1) ? -1.0 : 1.0;   /* hop to n + t   */
+        const double s1 = (t == 0) ? -1.0 : 1.0;        /* hop to n - t   */
+        const double diag = 2.0 * r + a->m0 + a->g * sigma[n];  /* Dirac.cu:52-69 */
+        for (int f = 0; f < 2; ++f) {
+            for (int k = 0; k < 2; ++k) {   /* k: real / imaginary plane */
+#define U(m) in[((m) * 4 + 2 * f + 0) * 2 + k]
+#define Dn(m) in[((m) * 4 + 2 * f + 1) * 2 + k]
+                double hu, hd;
+                if (!dagger) {
+                    /* Dirac.cu:165-174 */
+                    hu = -s1 * 0.5 * (r + 1.0) * U(td) - s0 * 0.5 * (r - 1.0) * U(tu)
+                         - 0.5 * (r * U(xu) - Dn(xu)) - 0.5 * (r * U(xd) + Dn(xd));
+                    hd = -s1 * 0.5 * (r - 1.0) * Dn(td) - s0 * 0.5 * (r + 1.0) * Dn(tu)
+                         + 0.5 * (U(xu) - r * Dn(xu)) - 0.5 * (U(xd) + r * Dn(xd));
+                } else {
+                    /* Dirac.cu:175-185 */
+                    hu = -s0 * 0.5 * (r + 1.0) * U(tu) - s1 * 0.5 * (r - 1.0) * U(td)
+                         - 0.5 * (r * U(xd) - Dn(xd)) - 0.5 * (r * U(xu) + Dn(xu));
+                    hd = -s0 * 0.5 * (r - 1.0) * Dn(tu) - s1 * 0.5 * (r + 1.0) * Dn(td)
+                         + 0.5 * (U(xd) - r * Dn(xd)) - 0.5 * (U(xu) + r * Dn(xu));
+                }
+                out[(n * 4 + 2 * f + 0) * 2 + k] = diag * U(n) + hu;
+                out[(n * 4 + 2 * f + 1) * 2 + k] = diag * Dn(n) + hd;
+#undef U
+#undef Dn
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* CG on D^dag D: CGsolver.cu:72-170, gpuSumSpinors :172-177,                 */
+/* gpuDotProduct reductions.cu:145-174.                                        */
+/* ------------------------------------------------------------------------- */
+static void cdot(int64_t n, const double* a, const double* b, double* re, double* im)
+{
+    /* sum conj(a_i) b_i over n complex */
+    double sr = 0.0, si = 0.0;
+#pragma omp parallel for reduction(+ : sr, si) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const double ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
+        sr += ar * br + ai * bi;
+        si += ar * bi - ai * br;
+    }
+    *re = sr;
+    *im = si;
+}
+
+/* res = s1 + c * s2 (complex c) */
+static void csum(int64_t n, const double* s1, const double* s2, double* res, double cr, double ci)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        const double xr = s2[2 * i], xi = s2[2 * i + 1];
+        const double pr = cr * xr - ci * xi, pi = cr * xi + ci * xr;
+        res[2 * i] = s1[2 * i] + pr;
+        res[2 * i + 1] = s1[2 * i + 1] + pi;
+    }
+}
+
+static void cdiv(double a, double b, double c, double d, double* re, double* im)
+{
+    /* (a+ib)/(c+id), Smith's algorithm */
+    if (fabs(c) >= fabs(d)) {
+        const double q = d / c, den = c + d * q;
+        *re = (a + b * q) / den;
+        *im = (b - a * q) / den;
+    } else {
+        const double q = c / d, den = c * q + d;
+        *re = (a * q + b) / den;
+        *im = (b * q - a) / den;
+    }
+}
+
+int yko_cg(int Nt, int Nx, const yko_action* a, const double* sigma, const double* b,
+           double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr)
+{
+    const int64_t n = (int64_t)Nt * Nx * 4;   /* complex entries */
+    double* r = (double*)malloc(sizeof(double) * 2 * n);
+    double* p = (double*)malloc(sizeof(double) * 2 * n);
+    double* t1 = (double*)malloc(sizeof(double) * 2 * n);
+    double* t2 = (double*)malloc(sizeof(double) * 2 * n);
+    memset(x, 0, sizeof(double) * 2 * n);            /* CGsolver.cu:83 */
+    memcpy(r, b, sizeof(double) * 2 * n);            /* :90 */
+    memcpy(p, b, sizeof(double) * 2 * n);            /* :92 */
+    double re, im;
+    cdot(n, r, r, &re, &im);
+    double rmodsq = hypot(re, im);                   /* :100 abs(dot) */
+    const double stop = (tol_mode == 0) ? tol : tol * sqrt(rmodsq);
+    /* Mtype = Dagger (1): first D, then D^dag, i.e. A = D^dag D (:113-125) */
+    const int first = (mtype == 1) ? 0 : 1;
+    const int second = (mtype == 1) ? 1 : 0;
+    int k;
+    for (k = 0; k < max_iter && sqrt(rmodsq) > stop; ++k) {
+        yko_dirac(Nt, Nx, a, sigma, p, t2, first);
+        yko_dirac(Nt, Nx, a, sigma, t2, t1, second);
+        cdot(n, p, t1, &re, &im);                    /* :133 */
+        double ar, ai;
+        cdiv(rmodsq, 0.0, re, im, &ar, &ai);         /* :137 alpha = rmodsq / <p,Ap> */
+        csum(n, x, p, x, ar, ai);                    /* :143 x += alpha p */
+        csum(n, r, t1, r, -ar, -ai);                 /* :148 r -= alpha Ap */
+        cdot(n, r, r, &re, &im);                     /* :152 */
+        const double rr = hypot(re, im);
+        const double beta = rr / rmodsq;             /* :156 */
+        rmodsq = rr;
+        csum(n, r, p, p, beta, 0.0);                 /* :162 p = r + beta p */
+    }
+    if (final_rr) *final_rr = rmodsq;
+    free(r); free(p); free(t1); free(t2);
+    return k;
+}
+
+/* FermionicDrift.cu:57-80 (getForce) and :83-100 (computeDrift). */
+int yko_force(int Nt, int Nx, const yko_action* a, const double* sigma, const double* eta,
+              int n_rhs, double tol, int tol_mode, int max_iter, double* F)
+{
+    const int V = Nt * Nx;
+    const int64_t n = (int64_t)V * 4;
+    double* xs = (double*)malloc(sizeof(double) * 2 * n);
+    double* chi = (double*)malloc(sizeof(double) * 2 * n);
+    const double scale = (a->drift_mode == 1) ? a->cut_fraction * a->cut_fraction : 1.0;
+    int iters = 0;
+    for (int i = 0; i < V; ++i) F[i] = 0.0;
+    for (int j = 0; j < n_rhs; ++j) {
+        const double* e = eta + (int64_t)j * 2 * n;
+        iters += yko_cg(Nt, Nx, a, sigma, e, xs, 1, tol, tol_mode, max_iter, NULL);
+        yko_dirac(Nt, Nx, a, sigma, xs, chi, 0);     /* chi = D x */
+        for (int i = 0; i < V; ++i) {
+            double s = 0.0;
+            for (int c = 0; c < 4; ++c) {
+                const int64_t q = (int64_t)(4 * i + c) * 2;
+                s += chi[q] * e[q] + chi[q + 1] * e[q + 1];   /* Re conj(chi) eta */
+            }
+            F[i] += -(scale * a->g) * s;
+        }
+    }
+    if (n_rhs > 1)
+        for (int i = 0; i < V; ++i) F[i] /= (double)n_rhs;
+    free(xs); free(chi);
+    return iters;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Coloured noise: colouredNoise.cpp:5-29 (momenta), :138-145 (mask),         */
+/* :155-178 (RNG -> D2Z -> mask -> Z2D).                                       */
+/* ------------------------------------------------------------------------- */
+/* p^2 of mode (kt, kx) in the reference's operation order (:16-29). */
+static double momentum_sq(int kt, int kx, int Nt, int Nx)
+{
+    const int sizes[2] = {Nt, Nx};
+    const int coo[2] = {kt, kx};
+    double msq = 0.0;
+    for (int d = 0; d < 2; ++d) {
+        const int L = sizes[d];
+        const double tmp = (coo[d] <= (L / 2) ? coo[d] : coo[d] - L) * 2.0 * M_PI / L;
+        msq += tmp * tmp;
+    }
+    return msq;
+}
+
+static double cut_sq(double cut_fraction)
+{
+    const double momentum_cut = sqrt(2.0) * M_PI * cut_fraction;  /* :139 */
+    return momentum_cut * momentum_cut;
+}
+
+void yko_mask_half(int Nt, int Nx, double cut_fraction, double* mask)
+{
+    const double csq = cut_sq(cut_fraction);
+    const int Nh = Nx / 2 + 1;
+    const double inv = 1.0 / (double)(Nt * Nx);
+    for (int kt = 0; kt < Nt; ++kt)
+        for (int kx = 0; kx < Nh; ++kx)
+            mask[kt * Nh + kx] = (momentum_sq(kt, kx, Nt, Nx) <= csq) ? inv : 0.0;
+}
+
+int yko_mask_all_kept(int Nt, int Nx, double cut_fraction)
+{
+    const double csq = cut_sq(cut_fraction);
+    for (int kt = 0; kt < Nt; ++kt)
+        for (int kx = 0; kx <= Nx / 2; ++kx)
+            if (!(momentum_sq(kt, kx, Nt, Nx) <= csq)) return 0;
+    return 1;
+}
+
+static void fft1(int n, double* re, double* im, int sign)
+{
+    /* iterative radix-2 for powers of two, direct DFT otherwise */
+    if ((n & (n - 1)) == 0) {
+        for (int i = 1, j = 0; i < n; ++i) {
+            int bit = n >> 1;
+            for (; j & bit; bit >>= 1) j ^= bit;
+            j ^= bit;
+            if (i < j) {
+                double tr = re[i]; re[i] = re[j]; re[j] = tr;
+                double ti = im[i]; im[i] = im[j]; im[j] = ti;
+            }
+        }
+        for (int len = 2; len <= n; len <<= 1) {
+            const int h = len / 2;
+            for (int i = 0; i < n; i += len) {
+                for (int k = 0; k < h; ++k) {
+                    const double ang = sign * 2.0 * M_PI * k / len;
+                    const double wr = cos(ang), wi = sin(ang);
+                    const double ur = re[i + k], ui = im[i + k];
+                    const double vr = re[i + k + h] * wr - im[i + k + h] * wi;
+                    const double vi = re[i + k + h] * wi + im[i + k + h] * wr;
+                    re[i + k] = ur + vr; im[i + k] = ui + vi;
+                    re[i + k + h] = ur - vr; im[i + k + h] = ui - vi;
+                }
+            }
+        }
+    } else {
+        double* tr = (double*)malloc(sizeof(double) * n);
+        double* ti = (double*)malloc(sizeof(double) * n);
+        for (int k = 0; k < n; ++k) {
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < n; ++j) {
+                const double ang = sign * 2.0 * M_PI * (double)(((int64_t)j * k) % n) / n;
+                sr += re[j] * cos(ang) - im[j] * sin(ang);
+                si += re[j] * sin(ang) + im[j] * cos(ang);
+            }
+            tr[k] = sr; ti[k] = si;
+        }
+        memcpy(re, tr, sizeof(double) * n);
+        memcpy(im, ti, sizeof(double) * n);
+        free(tr); free(ti);
+    }
+}
+
+void yko_fft2(int Nt, int Nx, double* data, int sign)
+{
+    const int L = Nt > Nx ? Nt : Nx;
+    double* re = (double*)malloc(sizeof(double) * L);
+    double* im = (double*)malloc(sizeof(double) * L);
+    for (int t = 0; t < Nt; ++t) {
+        for (int x = 0; x < Nx; ++x) { re[x] = data[2 * (t * Nx + x)]; im[x] = data[2 * (t * Nx + x) + 1]; }
+        fft1(Nx, re, im, sign);
+        for (int x = 0; x < Nx; ++x) { data[2 * (t * Nx + x)] = re[x]; data[2 * (t * Nx + x) + 1] = im[x]; }
+    }
+    for (int x = 0; x < Nx; ++x) {
+        for (int t = 0; t < Nt; ++t) { re[t] = data[2 * (t * Nx + x)]; im[t] = data[2 * (t * Nx + x) + 1]; }
+        fft1(Nt, re, im, sign);
+        for (int t = 0; t < Nt; ++t) { data[2 * (t * Nx + x)] = re[t]; data[2 * (t * Nx + x) + 1] = im[t]; }
+    }
+    free(re); free(im);
+}
+
+void yko_coloured_noise(int Nt, int Nx, double cut_fraction, const double* white, double* xi)
+{
+    const int V = Nt * Nx;
+    if (yko_mask_all_kept(Nt, Nx, cut_fraction)) {
+        /* every mode kept: Z2D(D2Z(w)/V) is w up to rounding */
+        memcpy(xi, white, sizeof(double) * V);
+        return;
+    }
+    const double csq = cut_sq(cut_fraction);
+    const double inv = 1.0 / (double)V;
+    double* c = (double*)malloc(sizeof(double) * 2 * V);
+    for (int i = 0; i < V; ++i) { c[2 * i] = white[i]; c[2 * i + 1] = 0.0; }
+    yko_fft2(Nt, Nx, c, -1);
+    /* full-spectrum mask: the half-spectrum rule extended by k -> -k symmetry */
+    for (int kt = 0; kt < Nt; ++kt)
+        for (int kx = 0; kx < Nx; ++kx) {
+            const int kxh = (kx <= Nx / 2) ? kx : Nx - kx;
+            const int kth = (kx <= Nx / 2) ? kt : (Nt - kt) % Nt;
+            const double m = (momentum_sq(kth, kxh, Nt, Nx) <= csq) ? inv : 0.0;
+            c[2 * (kt * Nx + kx)] *= m;
+            c[2 * (kt * Nx + kx) + 1] *= m;
+        }
+    yko_fft2(Nt, Nx, c, +1);
+    for (int i = 0; i < V; ++i) xi[i] = c[2 * i];
+    free(c);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Bosonic drift and Euler update: langevin_gpu_v2.cu:9-37, 41-63, 65-118;    */
+/* Laplacian CSR (sorted columns, diag -2d): Laplace.cu:61-100.               */
+/* ------------------------------------------------------------------------- */
+static int cmp_int(const void* a, const void* b)
+{
+    const int x = *(const int*)a, y = *(const int*)b;
+    return (x > y) - (x < y);
+}
+
+void yko_bosonic_drift(int Nt, int Nx, double m2, double lambda, const double* phi, double* drift)
+{
+    const int V = Nt * Nx;
+    const double my_lambda = lambda / 6.0;                 /* langevin_gpu_v2.cu:13 */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < V; ++i) {
+        const double v = phi[i];
+        drift[i] += v * (m2 + my_lambda * (v * v));        /* :15-24 */
+        const int t = i / Nx, x = i % Nx;
+        int cols[5] = {i, ((t + 1) % Nt) * Nx + x, ((t - 1 + Nt) % Nt) * Nx + x,
+                       t * Nx + (x + 1) % Nx, t * Nx + (x - 1 + Nx) % Nx};
+        qsort(cols, 5, sizeof(int), cmp_int);               /* Laplace.cu:88 */
+        double out = 0.0;
+        for (int j = 0; j < 5; ++j)                         /* :52-59 */
+            out += (cols[j] != i ? 1.0 : -4.0) * phi[cols[j]];
+        drift[i] -= out;
+    }
+}
+
+double yko_euler_update(int V, double eps_bar, double fixed_dt, double* phi, const double* drift,
+                        const double* noise, double* max_drift)
+{
+    double eps;
+    double m = 0.0;
+    for (int i = 0; i < V; ++i) {                           /* reductions.cu:30-63 */
+        const double v = fabs(drift[i]);
+        m = v > m ? v : m;
+    }
+    if (m > 1e5) m = 1e5;                                   /* langevin_gpu_v2.cu:83-91 */
+    else if (m < 1e-5) m = 1e-5;
+    if (max_drift) *max_drift = m;
+    if (fixed_dt > 0.0)
+        eps = fixed_dt;
+    else
+        eps = eps_bar * 30.0 / m;                           /* :71, :112 */
+    const double fact = sqrt(2.0 * eps);                    /* :32 */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < V; ++i)
+        phi[i] -= eps * drift[i] + fact * noise[i];         /* :34 */
+    return eps;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Observables: reductions.cu:65-140, 176-191, 200-233.                       */
+/* ------------------------------------------------------------------------- */
+double yko_sum(int n, const double* v)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += v[i];
+    return s;
+}
+
+void yko_time_slices(int Nt, int Nx, const double* phi, double* slices)
+{
+    for (int t = 0; t < Nt; ++t) {
+        double s = 0.0;
+        for (int x = 0; x < Nx; ++x) s += phi[t * Nx + x];
+        slices[t] = s;
+    }
+}
+
+void yko_time_slices_spinor(int Nt, int Nx, const double* psi, double* corr)
+{
+    for (int t = 0; t < Nt; ++t) {
+        double s = 0.0;
+        for (int x = 0; x < Nx; ++x)
+            for (int c = 0; c < 4; ++c) s += psi[((t * Nx + x) * 4 + c) * 2];
+        corr[t] = s;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Philox4x32-10 (Salmon et al., SC'11) and Box-Muller.                        */
+/* ------------------------------------------------------------------------- */
+void yko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int round = 0; round < 10; ++round) {
+        if (round > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* 52 random bits -> (0,1), exactly representable */
+static double u52(uint32_t hi, uint32_t lo)
+{
+    const uint64_t m = ((uint64_t)hi << 20) | (lo >> 12);
+    return ((double)m + 0.5) * 0x1p-52;
+}
+
+static void scheme_key_ctr(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind,
+                           uint32_t rhs, uint32_t key[2], uint32_t ctr[4])
+{
+    key[0] = (uint32_t)seed;
+    key[1] = (uint32_t)(seed >> 32) ^ chain;
+    ctr[1] = (uint32_t)step;
+    ctr[2] = (uint32_t)(step >> 32);
+    ctr[3] = (kind << 24) | (rhs & 0xFFFFFFu);
+}
+
+void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
+                 int64_t n, double* out)
+{
+    uint32_t key[2], ctr0[4];
+    scheme_key_ctr(seed, chain, step, kind, rhs, key, ctr0);
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (n + 1) / 2; ++e) {
+        uint32_t ctr[4] = {(uint32_t)e, ctr0[1], ctr0[2], ctr0[3]}, o[4];
+        yko_philox4x32_10(ctr, key, o);
+        const double u1 = u52(o[0], o[1]), u2 = u52(o[2], o[3]);
+        const double R = sqrt(-2.0 * log(u1));
+        const double th = 2.0 * M_PI * u2;
+        out[2 * e] = R * cos(th);
+        if (2 * e + 1 < n) out[2 * e + 1] = R * sin(th);
+    }
+}
+
+void yko_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out)
+{
+    uint32_t key[2], ctr0[4];
+    scheme_key_ctr(seed, chain, 0, 0u, 0u, key, ctr0);
+    for (int64_t e = 0; e < (n + 1) / 2; ++e) {
+        uint32_t ctr[4] = {(uint32_t)e, ctr0[1], ctr0[2], ctr0[3]}, o[4];
+        yko_philox4x32_10(ctr, key, o);
+        out[2 * e] = 1.0 - 2.0 * u52(o[0], o[1]);
+        if (2 * e + 1 < n) out[2 * e + 1] = 1.0 - 2.0 * u52(o[2], o[3]);
+    }
+}
+
+void yko_drand48_field(int64_t n, double* out)
+{
+    /* POSIX drand48: X <- (a X + c) mod 2^48, a = 0x5DEECE66D, c = 0xB; glibc's
+       state starts at X = 0 when no seeding call is made; value X / 2^48. */
+    uint64_t X = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        X = (0x5DEECE66DULL * X + 0xBULL) & ((1ULL << 48) - 1);
+        out[i] = 1.0 - 2.0 * ((double)X * 0x1p-48);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* One full Langevin step (main.cu:370-381): noise, force, bosonic drift,     */
+/* update.                                                                    */
+/* ------------------------------------------------------------------------- */
+double yko_langevin_step(int Nt, int Nx, const yko_action* a, uint64_t seed, uint32_t chain,
+                         uint64_t step, int n_rhs, double tol, int tol_mode, int max_iter,
+                         double fixed_dt, double* phi, double* obs)
+{
+    const int V = Nt * Nx;
+    double* w = (double*)malloc(sizeof(double) * V);
+    double* xi = (double*)malloc(sizeof(double) * V);
+    double* F = (double*)malloc(sizeof(double) * V);
+    double* drift = (double*)malloc(sizeof(double) * V);
+    yko_normals(seed, chain, step, 1u, 0u, V, w);
+    yko_coloured_noise(Nt, Nx, a->cut_fraction, w, xi);
+    int iters = 0;
+    if (a->g != 0.0) {
+        const int64_t n = (int64_t)V * 4;
+        double* eta = (double*)calloc((size_t)(2 * n * n_rhs), sizeof(double));
+        double* re = (double*)malloc(sizeof(double) * n);
+        for (int j = 0; j < n_rhs; ++j) {
+            yko_normals(seed, chain, step, 2u, (uint32_t)j, n, re);
+            for (int64_t i = 0; i < n; ++i) eta[(int64_t)j * 2 * n + 2 * i] = re[i];
+        }
+        iters = yko_force(Nt, Nx, a, phi, eta, n_rhs, tol, tol_mode, max_iter, F);
+        free(eta); free(re);
+    } else {
+        for (int i = 0; i < V; ++i) F[i] = 0.0;
+    }
+    memcpy(drift, F, sizeof(double) * V);
+    yko_bosonic_drift(Nt, Nx, a->m2, a->lambda, phi, drift);
+    double maxd;
+    const double eps = yko_euler_update(V, a->eps_bar, fixed_dt, phi, drift, xi, &maxd);
+    if (obs) {
+        double s2 = 0.0;
+        for (int i = 0; i < V; ++i) s2 += phi[i] * phi[i];
+        obs[0] = eps; obs[1] = maxd; obs[2] = yko_sum(V, phi); obs[3] = yko_sum(V, F);
+        obs[4] = (double)iters; obs[5] = s2;
+    }
+    free(w); free(xi); free(F); free(drift);
+    return eps;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Gamma-method, restated from U. Wolff, CPC 156 (2004) 143, eqs. (31)-(52);   */
+/* the reference wraps the same method in analysis/AutoCorrelation/ac.cpp.    */
+/* ------------------------------------------------------------------------- */
+void yko_gamma_method(const double* data, int64_t n, double stau, double out[5])
+{
+    double mean = 0.0;
+    for (int64_t i = 0; i < n; ++i) mean += data[i];
+    mean /= (double)n;
+    out[0] = mean; out[1] = out[2] = out[3] = out[4] = 0.0;
+    if (n < 2) return;
+    const int64_t tmax = n / 2;
+    double* gam = (double*)calloc((size_t)tmax + 1, sizeof(double));
+    for (int64_t t = 0; t <= tmax; ++t) {
+        double s = 0.0;
+        for (int64_t i = 0; i + t < n; ++i) s += (data[i] - mean) * (data[i + t] - mean);
+        gam[t] = s / (double)(n - t);
+    }
+    if (gam[0] == 0.0) { free(gam); return; }
+    int64_t W = tmax;
+    double gint = 0.0;
+    int found = 0;
+    for (int64_t t = 1; t <= tmax; ++t) {
+        gint += gam[t] / gam[0];
+        const double tauw = (gint <= 0.0) ? 1e-5 : stau / log((gint + 1.0) / gint);
+        const double gw = exp(-(double)t / tauw) - tauw / sqrt((double)t * (double)n);
+        if (gw < 0.0) { W = t; found = 1; break; }
+    }
+    (void)found;
+    double cf = gam[0];
+    for (int64_t t = 1; t <= W; ++t) cf += 2.0 * gam[t];
+    for (int64_t t = 0; t <= tmax; ++t) gam[t] += cf / (double)n;   /* bias correction */
+    double cf2 = gam[0], acc = gam[0];
+    for (int64_t t = 1; t <= W; ++t) { cf2 += 2.0 * gam[t]; acc += gam[t]; }
+    const double tau = acc / gam[0] - 0.5;
+    out[1] = sqrt(cf2 / (double)n);
+    out[2] = out[1] * sqrt(((double)W + 0.5) / (double)n);
+    out[3] = tau;
+    out[4] = tau * 2.0 * sqrt(((double)W - tau + 0.5) / (double)n);
+    free(gam);
+}

@@ -1,0 +1,303 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances: FP64 operator applications 1e-13 relative; FP32 Dirac 2e-6
+relative; CG solutions to the oracle's FP64 solution at the stated
+tolerances; Langevin steps 1e-9 absolute on the field after the CG has
+converged to a relative residual of 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+S_HALF_PI = 0.35355339059327373   # cutFraction for Lambda = pi/2
+
+
+def params(yk, Nt, Nx, **kw):
+    base = dict(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=0.1, wilson_param=1.0,
+                cut_fraction=S_HALF_PI, Nt=Nt, Nx=Nx, cg_tol=1e-12, cg_tol_mode=yk.YK_TOL_REL, seed=1234,
+                init=yk.YK_INIT_PHILOX)
+    base.update(kw)
+    return yk.Params.default(**base)
+
+
+def act(p):
+    return O.action(m2=p.mass, lam=p.g, g=p.yukawa_coupling, m0=p.fermion_mass, r=p.wilson_param,
+                    cut_fraction=p.cut_fraction, eps_bar=p.average_epsilon, drift_mode=p.drift_mode)
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def rand_spinor(rng, V):
+    return rng.normal(size=(V, 4)) + 1j * rng.normal(size=(V, 4))
+
+
+@pytest.mark.parametrize("Nt,Nx,r", [(8, 4, 1.0), (16, 16, 0.5), (6, 10, 1.0), (64, 32, 1.0), (2, 8, 0.0)])
+def test_dirac_fp64(ylib, cuda, Nt, Nx, r):
+    yk = ylib
+    p = params(yk, Nt, Nx, wilson_param=r)
+    rng = np.random.default_rng(1)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        psi = rand_spinor(rng, Nt * Nx)
+        x = dev(cuda, psi)
+        y = cuda.empty_like(x)
+        for dag in (False, True):
+            yk.DiracOP(ctx).applyD(x, y, yk.MatrixType.Dagger if dag else yk.MatrixType.Normal)
+            ctx.synchronize()
+            want = O.dirac(Nt, Nx, act(p), sig, psi, dag)
+            err = np.abs(host(y) - want).max() / np.abs(want).max()
+            assert err < 1e-13, (dag, err)
+
+
+def test_dirac_fp32(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 32, 16
+    p = params(yk, Nt, Nx)
+    rng = np.random.default_rng(2)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        psi = rand_spinor(rng, Nt * Nx).astype(np.complex64)
+        x = dev(cuda, psi)
+        y = cuda.empty_like(x)
+        ctx.dirac_apply(x, y, dagger=False, precision=yk.YK_FP32)
+        ctx.synchronize()
+        want = O.dirac(Nt, Nx, act(p), sig, psi.astype(np.complex128))
+        assert np.abs(host(y) - want).max() / np.abs(want).max() < 2e-6
+
+
+@pytest.mark.parametrize("mtype", [0, 1])
+@pytest.mark.parametrize("Nt,Nx", [(8, 4), (32, 32), (6, 10)])
+def test_cg_fp64(ylib, cuda, Nt, Nx, mtype):
+    yk = ylib
+    p = params(yk, Nt, Nx)
+    rng = np.random.default_rng(3)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        b = rand_spinor(rng, Nt * Nx)
+        bd, xd = dev(cuda, b), dev(cuda, np.zeros_like(b))
+        st = ctx.cg_solve(bd, xd, mtype=mtype, tol=1e-12, tol_mode=yk.YK_TOL_REL)
+        want, it, _ = O.cg(Nt, Nx, act(p), sig, b, mtype=mtype, tol=1e-12, tol_mode=1)
+        x = host(xd)
+        assert np.abs(x - want).max() / np.abs(want).max() < 1e-9
+        assert abs(st.iterations - it) <= 1 and st.converged == 1
+        # reference stopping rule (absolute 1e-8, IterMax 1000)
+        st2 = yk.CGsolver(ctx).solve(bd, xd, None, yk.MatrixType(mtype))
+        want2, it2, _ = O.cg(Nt, Nx, act(p), sig, b, mtype=mtype)
+        assert abs(st2.iterations - it2) <= 1
+        assert np.abs(host(xd) - want2).max() / np.abs(want2).max() < 1e-7
+
+
+def test_cg_mixed_reaches_fp64_residual(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 64, 64
+    p = params(yk, Nt, Nx)
+    rng = np.random.default_rng(4)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        b = rand_spinor(rng, Nt * Nx)
+        bd, xd = dev(cuda, b), dev(cuda, np.zeros_like(b))
+        st = ctx.cg_solve(bd, xd, tol=1e-10, tol_mode=yk.YK_TOL_REL, precision=yk.YK_MIXED)
+        x = host(xd)
+        a = act(p)
+        r = b - O.dirac(Nt, Nx, a, sig, O.dirac(Nt, Nx, a, sig, x), True)
+        assert np.linalg.norm(r) <= 1.05e-10 * np.linalg.norm(b), np.linalg.norm(r) / np.linalg.norm(b)
+        assert st.converged == 1 and st.reliable_updates >= 1
+        want, it, _ = O.cg(Nt, Nx, a, sig, b, tol=1e-10, tol_mode=1)
+        assert np.abs(x - want).max() / np.abs(want).max() < 1e-7
+        assert st.iterations <= 1.5 * it + 60
+
+
+def test_cg_iteration_cap_reports_noconv(ylib, cuda):
+    yk = ylib
+    p = params(yk, 16, 16)
+    rng = np.random.default_rng(5)
+    with yk.Context(p) as ctx:
+        ctx.set_field(rng.uniform(-1, 1, 256))
+        b = dev(cuda, rand_spinor(rng, 256))
+        x = cuda.zeros_like(b)
+        with pytest.raises(yk.YukawaError) as e:
+            ctx.cg_solve(b, x, tol=1e-14, tol_mode=yk.YK_TOL_REL, max_iter=3)
+        assert e.value.status == yk.YK_ENOCONV
+        st = ctx.cg_solve(b, x, tol=1e-14, tol_mode=yk.YK_TOL_REL, max_iter=3, allow_noconv=True)
+        assert st.iterations == 3 and st.converged == 0
+        z = cuda.zeros_like(b)
+        st0 = ctx.cg_solve(z, x)
+        assert st0.iterations == 0 and np.abs(host(x)).max() == 0.0
+
+
+@pytest.mark.parametrize("n_rhs,drift_mode", [(1, 0), (2, 0), (1, 1)])
+def test_force_injected_eta(ylib, cuda, n_rhs, drift_mode):
+    yk = ylib
+    Nt, Nx = 16, 8
+    p = params(yk, Nt, Nx, n_rhs=n_rhs, drift_mode=drift_mode, cut_fraction=0.5)
+    rng = np.random.default_rng(6)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        eta = np.zeros((n_rhs, Nt * Nx, 4), complex)
+        eta.real = rng.normal(size=eta.shape)
+        F = cuda.empty(Nt * Nx, dtype=cuda.float64, device="cuda")
+        ctx.fermion_force(F, dev(cuda, eta))
+        want, _ = O.force(Nt, Nx, act(p), sig, eta, tol=1e-12, tol_mode=1)
+        assert np.abs(host(F) - want).max() < 1e-9
+
+
+def test_force_philox_eta(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 16, 16
+    p = params(yk, Nt, Nx)
+    with yk.Context(p) as ctx:
+        sig = ctx.get_field()
+        F = cuda.empty(Nt * Nx, dtype=cuda.float64, device="cuda")
+        yk.FermionicDrift(ctx).getForce(F)
+        eta = O.fermion_eta(1234, 0, 0, Nt, Nx)
+        want, _ = O.force(Nt, Nx, act(p), sig, eta, tol=1e-12, tol_mode=1)
+        assert np.abs(host(F) - want).max() < 1e-9
+
+
+@pytest.mark.parametrize("Nt,Nx,s", [(16, 16, S_HALF_PI), (8, 4, 0.25), (6, 10, 0.3), (32, 64, 0.2),
+                                     (16, 16, 1.0), (256, 8, 0.3)])
+def test_coloured_noise(ylib, cuda, Nt, Nx, s):
+    yk = ylib
+    p = params(yk, Nt, Nx, cut_fraction=s)
+    rng = np.random.default_rng(7)
+    with yk.Context(p) as ctx:
+        w = rng.normal(size=Nt * Nx)
+        xi = cuda.empty(Nt * Nx, dtype=cuda.float64, device="cuda")
+        yk.ColouredNoise(ctx, xi)(dev(cuda, w))
+        ctx.synchronize()
+        assert np.abs(host(xi) - O.coloured_noise(Nt, Nx, s, w)).max() < 1e-13
+        # Philox white noise at step 0 of chain 0
+        yk.ColouredNoise(ctx, xi)()
+        ctx.synchronize()
+        w0 = O.normals(1234, 0, 0, 1, 0, Nt * Nx)
+        assert np.abs(host(xi) - O.coloured_noise(Nt, Nx, s, w0)).max() < 1e-13
+
+
+def test_euler_update_injected(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 16, 32
+    p = params(yk, Nt, Nx)
+    rng = np.random.default_rng(8)
+    with yk.Context(p) as ctx:
+        phi = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(phi)
+        F, xi = rng.normal(size=Nt * Nx) * 0.3, rng.normal(size=Nt * Nx)
+        obs = ctx.euler_update(dev(cuda, F), dev(cuda, xi))
+        drift = O.bosonic_drift(Nt, Nx, p.mass, p.g, phi, F)
+        want, eps, m = O.euler_update(phi, drift, xi, p.average_epsilon)
+        assert abs(obs.eps - eps) <= 1e-15 * eps and abs(obs.max_drift - m) <= 1e-15 * m
+        assert np.abs(ctx.get_field() - want).max() < 1e-14
+        assert abs(obs.sum_phi - want.sum()) < 1e-10 and obs.steps == 1
+
+
+@pytest.mark.parametrize("fixed_dt", [0.0, 0.01])
+@pytest.mark.parametrize("Nt,Nx,s", [(16, 16, S_HALF_PI), (8, 12, 1.0)])
+def test_langevin_steps_match_oracle(ylib, cuda, Nt, Nx, s, fixed_dt):
+    yk = ylib
+    p = params(yk, Nt, Nx, cut_fraction=s, fixed_dt=fixed_dt)
+    a = act(p)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        assert np.array_equal(phi, O.uniform_field(1234, 0, Nt * Nx))
+        for step in range(4):
+            ctx.step(1)
+            obs = ctx.observables()
+            phi, ro = O.langevin_step(Nt, Nx, a, phi, 1234, 0, step, tol=1e-12, tol_mode=1, fixed_dt=fixed_dt)
+            got = ctx.get_field()
+            assert np.abs(got - phi).max() < 1e-9, step
+            assert abs(obs.eps - ro.eps) < 1e-12 * ro.eps
+            assert abs(obs.cg_iterations - ro.cg_iters) <= 2
+            phi = got   # keep the chains identical to the last bit of the GPU field
+        assert ctx.get_step() == 4 and obs.steps == 4
+
+
+def test_langevin_mixed_precision_step(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 32, 32
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    a = act(p)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        ctx.step(1)
+        want, ro = O.langevin_step(Nt, Nx, a, phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+        assert np.abs(ctx.get_field() - want).max() < 1e-8
+        assert ctx.observables().status == 0
+
+
+def test_batched_chains_equal_single_chains(ylib, cuda):
+    yk = ylib
+    specs = [(16, 16, 0.1, 0.5, S_HALF_PI), (32, 8, 0.25, 0.3, 0.2), (8, 8, 0.05, 0.8, 1.0)]
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, cut_fraction=s, n_rhs=2)
+          for nt, nx, m0, g, s in specs]
+    with yk.Context(ps) as ctx:
+        ctx.step(3)
+        batched = [ctx.get_field(c) for c in range(len(ps))]
+        obs_b = [ctx.observables(c) for c in range(len(ps))]
+    for c, p in enumerate(ps):
+        # the Philox key of a chain includes its chain index c
+        phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+        for step in range(3):
+            phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=2, tol=1e-12, tol_mode=1)
+        assert np.abs(batched[c] - phi).max() < 1e-9, c
+        assert obs_b[c].steps == 3
+
+
+def test_deterministic(ylib, cuda):
+    yk = ylib
+    p = params(yk, 32, 32)
+    out = []
+    for _ in range(2):
+        with yk.Context(p) as ctx:
+            ctx.step(3)
+            out.append(ctx.get_field())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_observables(ylib, cuda):
+    yk = ylib
+    Nt, Nx = 16, 8
+    p = params(yk, Nt, Nx)
+    with yk.Context(p) as ctx:
+        ctx.step(2)
+        phi = ctx.get_field()
+        assert np.abs(ctx.time_slices() - O.time_slices(Nt, Nx, phi)).max() < 1e-12
+        corr, st = ctx.correlator()
+        a = act(p)
+        src = np.zeros((Nt * Nx, 4), complex)
+        src[0, 0] = src[0, 1] = 1.0
+        x, _, _ = O.cg(Nt, Nx, a, phi, src, mtype=0, tol=1e-12, tol_mode=1)
+        y = O.dirac(Nt, Nx, a, phi, x, True)
+        assert np.abs(corr - O.time_slices_spinor(Nt, Nx, y)).max() < 1e-9
+        cond, _ = ctx.condensate()
+        eta = O.fermion_eta(1234, 0, 2, Nt, Nx, kind=3)
+        F, _ = O.force(Nt, Nx, a, phi, eta, tol=1e-12, tol_mode=1)
+        assert abs(cond - F.sum() / p.yukawa_coupling / (Nt * Nx)) < 1e-9
+
+
+def test_checkpoint_roundtrip(ylib, cuda, tmp_path):
+    yk = ylib
+    p = params(yk, 16, 16)
+    with yk.Context(p) as ctx:
+        ctx.step(2)
+        ctx.checkpoint_save(tmp_path / "c.ckpt", 0.03)
+        ctx.step(2)
+        f4 = ctx.get_field()
+    with yk.Context(p) as ctx2:
+        assert ctx2.checkpoint_load(tmp_path / "c.ckpt") == 0.03
+        assert ctx2.get_step() == 2
+        ctx2.step(2)
+        assert np.array_equal(ctx2.get_field(), f4)

@@ -1,0 +1,215 @@
+"""CPU oracle pins: published known-answer tests, dense linear algebra, numpy FFTs,
+analytic free-fermion spectrum, and the Gamma-method.  No GPU."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32, 10 rounds (Salmon et al. SC'11)
+    kat = [
+        (([0, 0, 0, 0], [0, 0]), [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+        (([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2), [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+        (([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]),
+         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+    ]
+    for (ctr, key), want in kat:
+        assert list(O.philox(ctr, key)) == want
+
+
+def test_drand48_matches_libc():
+    libc = ctypes.CDLL("libc.so.6")
+    libc.drand48.restype = ctypes.c_double
+    # a fresh process-wide state is not guaranteed here, so compare the recurrence
+    # from an explicit seed-free start against the documented LCG instead
+    x = 0
+    vals = []
+    for _ in range(5):
+        x = (0x5DEECE66D * x + 0xB) % (1 << 48)
+        vals.append(1.0 - 2.0 * x / 2.0**48)
+    assert np.array_equal(np.array(vals), O.drand48_field(5))
+
+
+def test_normals_statistics():
+    z = O.normals(1234, 0, 7, 1, 0, 400_000)
+    assert abs(z.mean()) < 5e-3 and abs(z.var() - 1.0) < 1e-2
+    # distinct streams are distinct
+    assert not np.allclose(z[:100], O.normals(1234, 0, 8, 1, 0, 100))
+    assert not np.allclose(z[:100], O.normals(1234, 1, 7, 1, 0, 100))
+    assert not np.allclose(z[:100], O.normals(1234, 0, 7, 2, 0, 100))
+
+
+def _dense(Nt, Nx, a, sig, dagger=False):
+    V = Nt * Nx
+    n = 4 * V
+    M = np.zeros((n, n), complex)
+    for i in range(n):
+        e = np.zeros(n, complex)
+        e[i] = 1
+        M[:, i] = O.dirac(Nt, Nx, a, sig, e.reshape(V, 4), dagger).ravel()
+    return M
+
+
+@pytest.mark.parametrize("Nt,Nx,r", [(4, 6, 1.0), (6, 4, 0.5), (2, 5, 0.0)])
+def test_dirac_adjoint_and_dagger(Nt, Nx, r):
+    a = O.action(g=0.5, m0=0.1, r=r)
+    rng = np.random.default_rng(3)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    D = _dense(Nt, Nx, a, sig)
+    Dd = _dense(Nt, Nx, a, sig, True)
+    assert np.abs(Dd - D.conj().T).max() < 1e-14
+
+
+def test_free_wilson_spectrum():
+    """Constant sigma: D is diagonal in momentum space with antiperiodic time
+    momenta; eigenvalues M + r sum(1 - cos p) +- i sqrt(sum sin^2 p)."""
+    Nt, Nx, r, m0, g, s0 = 6, 4, 1.0, 0.3, 0.5, 0.4
+    a = O.action(g=g, m0=m0, r=r)
+    D = _dense(Nt, Nx, a, np.full(Nt * Nx, s0))
+    ev = np.linalg.eigvals(D)
+    M = m0 + g * s0
+    want = []
+    for kt in range(Nt):
+        pt = (2 * kt + 1) * np.pi / Nt
+        for kx in range(Nx):
+            px = 2 * np.pi * kx / Nx
+            re = M + r * (2 - np.cos(pt) - np.cos(px))
+            im = np.sqrt(np.sin(pt) ** 2 + np.sin(px) ** 2)
+            want += [re + 1j * im, re - 1j * im] * 2   # two flavours
+    key = lambda z: sorted(z, key=lambda v: (round(v.real, 9), round(v.imag, 9)))
+    assert np.abs(np.array(key(ev)) - np.array(key(np.array(want)))).max() < 1e-10
+
+
+@pytest.mark.parametrize("mtype", [0, 1])
+def test_cg_matches_dense_solve(mtype):
+    Nt, Nx = 8, 4
+    a = O.action(g=0.5, m0=0.1)
+    rng = np.random.default_rng(5)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    b = rng.normal(size=(Nt * Nx, 4)) + 1j * rng.normal(size=(Nt * Nx, 4))
+    D = _dense(Nt, Nx, a, sig)
+    A = D.conj().T @ D if mtype == 1 else D @ D.conj().T
+    x, it, rr = O.cg(Nt, Nx, a, sig, b, mtype=mtype, tol=1e-13, tol_mode=1)
+    xd = np.linalg.solve(A, b.ravel())
+    assert np.abs(x.ravel() - xd).max() / np.abs(xd).max() < 1e-11
+    assert 0 < it < 400 and np.sqrt(rr) <= 1e-13 * np.linalg.norm(b)
+
+
+def test_cg_reference_stopping_rule():
+    Nt, Nx = 8, 4
+    a = O.action(g=0.5, m0=0.1)
+    rng = np.random.default_rng(6)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    b = rng.normal(size=(Nt * Nx, 4)) + 0j
+    x, it, rr = O.cg(Nt, Nx, a, sig, b)             # absolute 1e-8, IterMax 1000
+    assert np.sqrt(rr) <= 1e-8
+    _, it0, _ = O.cg(Nt, Nx, a, sig, np.zeros_like(b))
+    assert it0 == 0
+    _, itc, _ = O.cg(Nt, Nx, a, sig, b, max_iter=3)
+    assert itc == 3
+
+
+def test_force_matches_dense():
+    Nt, Nx = 4, 6
+    a = O.action(g=0.7, m0=0.2)
+    rng = np.random.default_rng(7)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    eta = np.zeros((1, Nt * Nx, 4), complex)
+    eta.real = rng.normal(size=(1, Nt * Nx, 4))
+    F, _ = O.force(Nt, Nx, a, sig, eta, tol=1e-14, tol_mode=1)
+    D = _dense(Nt, Nx, a, sig)
+    chi = np.linalg.solve(D.conj().T, eta[0].ravel()).reshape(-1, 4)
+    want = -0.7 * np.real(np.sum(np.conj(chi) * eta[0], axis=1))
+    assert np.abs(F - want).max() < 1e-10
+
+
+def test_fft_matches_numpy():
+    rng = np.random.default_rng(8)
+    for Nt, Nx in [(8, 16), (6, 10), (4, 4)]:
+        z = rng.normal(size=(Nt, Nx)) + 1j * rng.normal(size=(Nt, Nx))
+        assert np.abs(O.fft2(Nt, Nx, z) - np.fft.fft2(z)).max() < 1e-12
+        assert np.abs(O.fft2(Nt, Nx, z, +1) - np.fft.ifft2(z) * Nt * Nx).max() < 1e-12
+
+
+@pytest.mark.parametrize("Nt,Nx,s", [(16, 16, 0.35355339059327373), (8, 4, 0.25), (6, 10, 0.3), (16, 8, 1.0)])
+def test_coloured_noise_matches_numpy_r2c(Nt, Nx, s):
+    rng = np.random.default_rng(9)
+    w = rng.normal(size=Nt * Nx)
+    mh = O.mask_half(Nt, Nx, s)
+    want = np.fft.irfft2(np.fft.rfft2(w.reshape(Nt, Nx)) * mh * (Nt * Nx), s=(Nt, Nx)).ravel()
+    got = O.coloured_noise(Nt, Nx, s, w)
+    assert np.abs(got - want).max() < 1e-13
+
+
+def test_mask_rule():
+    # |p|^2 <= 2 pi^2 s^2 with p = 2 pi k / L, k folded into (-L/2, L/2]
+    Nt, Nx, s = 16, 12, 0.3
+    mh = O.mask_half(Nt, Nx, s)
+    for kt in range(Nt):
+        for kx in range(Nx // 2 + 1):
+            ft = kt if kt <= Nt // 2 else kt - Nt
+            p2 = (2 * np.pi * ft / Nt) ** 2 + (2 * np.pi * kx / Nx) ** 2
+            keep = p2 <= 2 * np.pi**2 * s**2
+            assert (mh[kt, kx] > 0) == keep
+    assert O.mask_all_kept(Nt, Nx, 1.0) and not O.mask_all_kept(Nt, Nx, 0.5)
+
+
+def test_bosonic_drift_matches_numpy():
+    Nt, Nx = 6, 8
+    rng = np.random.default_rng(10)
+    phi = rng.uniform(-1, 1, Nt * Nx)
+    got = O.bosonic_drift(Nt, Nx, -0.5, 1.0, phi)
+    p = phi.reshape(Nt, Nx)
+    lap = np.roll(p, 1, 0) + np.roll(p, -1, 0) + np.roll(p, 1, 1) + np.roll(p, -1, 1) - 4 * p
+    want = (p * (-0.5 + 1.0 / 6.0 * p * p) - lap).ravel()
+    assert np.abs(got - want).max() < 1e-14
+
+
+def test_euler_update_rules():
+    rng = np.random.default_rng(11)
+    phi, d, xi = rng.uniform(-1, 1, 64), rng.normal(size=64), rng.normal(size=64)
+    new, eps, m = O.euler_update(phi, d, xi, 0.02)
+    assert m == np.abs(d).max() and eps == 0.02 * 30.0 / m
+    assert np.abs(new - (phi - (eps * d + np.sqrt(2 * eps) * xi))).max() < 1e-15
+    _, eps2, m2 = O.euler_update(phi, d * 1e7, xi, 0.02)
+    assert m2 == 1e5 and eps2 == 0.02 * 30.0 / 1e5
+    _, eps3, _ = O.euler_update(phi, d, xi, 0.02, fixed_dt=0.01)
+    assert eps3 == 0.01
+
+
+def _gamma_py(a, stau=1.5):
+    n = len(a)
+    m = a.mean()
+    d = a - m
+    tmax = n // 2
+    gam = np.array([np.dot(d[: n - t], d[t:]) / (n - t) for t in range(tmax + 1)])
+    W, gint = tmax, 0.0
+    for t in range(1, tmax + 1):
+        gint += gam[t] / gam[0]
+        tau = 1e-5 if gint <= 0 else stau / np.log((gint + 1) / gint)
+        if np.exp(-t / tau) - tau / np.sqrt(t * n) < 0:
+            W = t
+            break
+    cf = gam[0] + 2 * gam[1: W + 1].sum()
+    gam = gam + cf / n
+    cf2 = gam[0] + 2 * gam[1: W + 1].sum()
+    tau = (gam[0] + gam[1: W + 1].sum()) / gam[0] - 0.5
+    err = np.sqrt(cf2 / n)
+    return np.array([m, err, err * np.sqrt((W + 0.5) / n), tau, tau * 2 * np.sqrt((W - tau + 0.5) / n)])
+
+
+def test_gamma_method():
+    rng = np.random.default_rng(12)
+    rho, n = 0.8, 20000
+    x = np.empty(n)
+    x[0] = 0
+    e = rng.normal(size=n)
+    for i in range(1, n):
+        x[i] = rho * x[i - 1] + e[i]
+    got = O.gamma_method(x)
+    assert np.allclose(got, _gamma_py(x), rtol=1e-10, atol=1e-12)
+    tau_exact = 0.5 * (1 + rho) / (1 - rho)
+    assert abs(got[3] - tau_exact) < 4 * got[4] + 0.3

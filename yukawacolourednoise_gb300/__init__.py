@@ -1,0 +1,377 @@
+"""GB300-native Langevin hot path of the 2-D Yukawa model (Matteo294/YukawaColouredNoise).
+
+The product is the C-ABI library ``lib/libyukawa_gb300.so`` (include/yukawa.h);
+this module binds it with ctypes and mirrors the reference's host classes so
+that code written against the reference reads the same:
+
+    reference (code/src/)                         here
+    DiracOP<double>::applyD(in, out, MatrixType)  DiracOP(ctx).applyD(in, out, MatrixType.Normal)
+    CGsolver::solve(in, out, D, MatrixType)       CGsolver(ctx).solve(in, out, D, MatrixType.Dagger)
+    FermionicDrift::getForce(out, D, CG, ...)     FermionicDrift(ctx).getForce(out, D, CG)
+    ColouredNoise::operator()()                   ColouredNoise(ctx)()
+    ./out input.toml                              run("input.toml")   /  lib/yk_run input.toml
+
+Device buffers are passed as objects with ``data_ptr()`` (torch tensors) or
+raw integer addresses.  There is no CPU fallback: importing without the
+built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libyukawa_gb300.so"
+
+YK_OK, YK_EINVAL, YK_ENOCONV, YK_ENAN, YK_ETIMEOUT, YK_ECUDA, YK_ENOMEM, YK_EIO = range(8)
+YK_NORMAL, YK_DAGGER = 0, 1
+YK_FP64, YK_FP32, YK_MIXED = 0, 1, 2
+YK_TOL_ABS, YK_TOL_REL = 0, 1
+YK_INIT_DRAND48, YK_INIT_PHILOX, YK_INIT_NONE = 0, 1, 2
+
+
+class MatrixType(enum.IntEnum):
+    """code/src/params.h:8"""
+    Normal = YK_NORMAL
+    Dagger = YK_DAGGER
+
+
+class YukawaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[status {status}] {msg}")
+        self.status = status
+
+
+class Params(C.Structure):
+    """yk_params: input.toml keys + [lattice] + [gpu] extensions."""
+    _fields_ = [
+        ("use_mass", C.c_int), ("mass", C.c_double), ("g", C.c_double), ("kappa", C.c_double),
+        ("lam", C.c_double), ("cut_fraction", C.c_double),
+        ("average_epsilon", C.c_double), ("max_langevin_time", C.c_double), ("export_time", C.c_double),
+        ("burn_count", C.c_int), ("measure_drift_count", C.c_int),
+        ("seed", C.c_int64),
+        ("yukawa_coupling", C.c_double), ("fermion_mass", C.c_double), ("drift_mode", C.c_int),
+        ("wilson_param", C.c_double),
+        ("Nt", C.c_int), ("Nx", C.c_int),
+        ("precision", C.c_int), ("n_rhs", C.c_int), ("cg_tol_mode", C.c_int), ("cg_tol", C.c_double),
+        ("cg_max_iter", C.c_int), ("reliable_every", C.c_int), ("fixed_dt", C.c_double), ("init", C.c_int),
+    ]
+
+    @classmethod
+    def default(cls, **kw) -> "Params":
+        p = cls()
+        lib().yk_params_default(C.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+    @classmethod
+    def from_toml(cls, path) -> "Params":
+        p = cls()
+        _check(lib().yk_params_from_toml(str(path).encode(), C.byref(p)))
+        return p
+
+    def action(self) -> "Action":
+        a = Action()
+        _check(lib().yk_derive_action(C.byref(self), C.byref(a)))
+        return a
+
+    def copy(self, **kw) -> "Params":
+        p = Params()
+        C.pointer(p)[0] = self
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+class Action(C.Structure):
+    _fields_ = [("m2", C.c_double), ("lam", C.c_double), ("kappa", C.c_double), ("sq2kappa", C.c_double),
+                ("g", C.c_double), ("m0", C.c_double), ("r", C.c_double), ("cut_fraction", C.c_double),
+                ("eps_bar", C.c_double), ("drift_mode", C.c_int), ("use_mass", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("reliable_updates", C.c_int), ("rr", C.c_double),
+                ("rr0", C.c_double), ("converged", C.c_int)]
+
+
+class Obs(C.Structure):
+    _fields_ = [("t", C.c_double), ("eps", C.c_double), ("max_drift", C.c_double), ("sum_phi", C.c_double),
+                ("sum_phi2", C.c_double), ("sum_force", C.c_double), ("steps", C.c_int64),
+                ("cg_iterations", C.c_int), ("status", C.c_int)]
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "yk_last_error": (C.c_char_p, []),
+    "yk_version": (C.c_char_p, []),
+    "yk_params_default": (None, [C.POINTER(Params)]),
+    "yk_params_from_toml": (C.c_int, [C.c_char_p, C.POINTER(Params)]),
+    "yk_derive_action": (C.c_int, [C.POINTER(Params), C.POINTER(Action)]),
+    "yk_ctx_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),
+    "yk_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "yk_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "yk_ctx_synchronize": (C.c_int, [C.c_void_p]),
+    "yk_ctx_n_chains": (C.c_int, [C.c_void_p]),
+    "yk_ctx_volume": (C.c_int, [C.c_void_p, C.c_int]),
+    "yk_ctx_shape": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "yk_set_field_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "yk_get_field_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "yk_field_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "yk_dirac_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "yk_cg_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
+                              C.c_int, C.c_int, C.POINTER(SolveStats)]),
+    "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
+    "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "yk_euler_update": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(Obs)]),
+    "yk_observables": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Obs)]),
+    "yk_time_slices": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "yk_correlator": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(SolveStats)]),
+    "yk_condensate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(SolveStats)]),
+    "yk_set_eps_bar": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "yk_get_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]),
+    "yk_set_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int64]),
+    "yk_set_time": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "yk_checkpoint_save": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_double]),
+    "yk_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]),
+    "yk_gamma_method": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    "yk_run_toml": (C.c_int, [C.c_char_p, C.c_char_p]),
+}
+
+
+def lib():
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        _lib = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(_lib, name)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _check(rc: int, ok=(YK_OK,)):
+    if rc not in ok:
+        raise YukawaError(rc, lib().yk_last_error().decode())
+    return rc
+
+
+def _ptr(buf) -> int:
+    if buf is None:
+        return None
+    if isinstance(buf, int):
+        return buf
+    if hasattr(buf, "data_ptr"):
+        return buf.data_ptr()
+    raise TypeError(f"expected a device buffer (data_ptr()) or an address, got {type(buf)}")
+
+
+class Context:
+    """yk_ctx: one or more independent chains on the current CUDA device."""
+
+    def __init__(self, params, n_chains: int | None = None):
+        if isinstance(params, Params):
+            params = [params] * (n_chains or 1)
+        arr = (Params * len(params))(*params)
+        h = C.c_void_p()
+        _check(lib().yk_ctx_create(arr, len(params), C.byref(h)))
+        self.h = h
+        self.params = list(params)
+
+    def close(self):
+        if self.h:
+            lib().yk_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def n_chains(self) -> int:
+        return lib().yk_ctx_n_chains(self.h)
+
+    def volume(self, chain=0) -> int:
+        return lib().yk_ctx_volume(self.h, chain)
+
+    def shape(self, chain=0):
+        nt, nx = C.c_int(), C.c_int()
+        _check(lib().yk_ctx_shape(self.h, chain, C.byref(nt), C.byref(nx)))
+        return nt.value, nx.value
+
+    def set_stream(self, stream_handle: int):
+        _check(lib().yk_ctx_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def synchronize(self):
+        _check(lib().yk_ctx_synchronize(self.h))
+
+    def set_field(self, phi, chain=0):
+        import numpy as np
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        assert a.size == self.volume(chain)
+        _check(lib().yk_set_field_host(self.h, chain, a.ctypes.data_as(C.c_void_p)))
+
+    def get_field(self, chain=0):
+        import numpy as np
+        a = np.empty(self.volume(chain))
+        _check(lib().yk_get_field_host(self.h, chain, a.ctypes.data_as(C.c_void_p)))
+        return a
+
+    def field_ptr(self, chain=0) -> int:
+        p = C.c_void_p()
+        _check(lib().yk_field_device(self.h, chain, C.byref(p)))
+        return p.value
+
+    def dirac_apply(self, inp, out, dagger=False, precision=YK_FP64, chain=0):
+        _check(lib().yk_dirac_apply(self.h, chain, _ptr(inp), _ptr(out), int(bool(dagger)), precision))
+
+    def cg_solve(self, b, x, mtype=YK_DAGGER, tol=1e-8, tol_mode=YK_TOL_ABS, max_iter=1000, precision=YK_FP64,
+                 chain=0, allow_noconv=False) -> SolveStats:
+        st = SolveStats()
+        ok = (YK_OK, YK_ENOCONV) if allow_noconv else (YK_OK,)
+        _check(lib().yk_cg_solve(self.h, chain, _ptr(b), _ptr(x), int(mtype), tol, tol_mode, max_iter, precision,
+                                 C.byref(st)), ok)
+        return st
+
+    def fermion_force(self, F, eta=None, chain=0) -> SolveStats:
+        st = SolveStats()
+        _check(lib().yk_fermion_force(self.h, chain, _ptr(eta), _ptr(F), C.byref(st)))
+        return st
+
+    def coloured_noise(self, xi, white=None, chain=0):
+        _check(lib().yk_coloured_noise(self.h, chain, _ptr(white), _ptr(xi)))
+
+    def step(self, n=1):
+        _check(lib().yk_langevin_step(self.h, n))
+
+    def euler_update(self, force, xi, chain=0) -> Obs:
+        o = Obs()
+        _check(lib().yk_euler_update(self.h, chain, _ptr(force), _ptr(xi), C.byref(o)))
+        return o
+
+    def observables(self, chain=0) -> Obs:
+        o = Obs()
+        _check(lib().yk_observables(self.h, chain, C.byref(o)))
+        return o
+
+    def time_slices(self, chain=0):
+        import numpy as np
+        nt, _ = self.shape(chain)
+        out = np.empty(nt)
+        _check(lib().yk_time_slices(self.h, chain, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def correlator(self, chain=0):
+        import numpy as np
+        nt, _ = self.shape(chain)
+        out = np.empty(nt)
+        st = SolveStats()
+        _check(lib().yk_correlator(self.h, chain, out.ctypes.data_as(C.c_void_p), C.byref(st)))
+        return out, st
+
+    def condensate(self, chain=0):
+        v = C.c_double()
+        st = SolveStats()
+        _check(lib().yk_condensate(self.h, chain, C.byref(v), C.byref(st)))
+        return v.value, st
+
+    def set_eps_bar(self, eps_bar, chain=0):
+        _check(lib().yk_set_eps_bar(self.h, chain, eps_bar))
+
+    def get_step(self, chain=0) -> int:
+        v = C.c_int64()
+        _check(lib().yk_get_step(self.h, chain, C.byref(v)))
+        return v.value
+
+    def set_step(self, step, chain=0):
+        _check(lib().yk_set_step(self.h, chain, step))
+
+    def checkpoint_save(self, path, eps_bar, chain=0):
+        _check(lib().yk_checkpoint_save(self.h, chain, str(path).encode(), eps_bar))
+
+    def checkpoint_load(self, path, chain=0) -> float:
+        e = C.c_double()
+        _check(lib().yk_checkpoint_load(self.h, chain, str(path).encode(), C.byref(e)))
+        return e.value
+
+
+# ---------------------------------------------------------------------------
+# Mirrors of the reference's host classes (code/src/*.cuh).
+# ---------------------------------------------------------------------------
+class DiracOP:
+    """DiracOP<double> (code/src/Dirac.cuh:16-27); sigma is the chain's field."""
+
+    def __init__(self, ctx: Context, chain=0):
+        self.ctx, self.chain = ctx, chain
+
+    def applyD(self, inp, out, MType=MatrixType.Normal, precision=YK_FP64):
+        self.ctx.dirac_apply(inp, out, MType == MatrixType.Dagger, precision, self.chain)
+
+
+class CGsolver:
+    """CGsolver (code/src/CGsolver.cuh:32-53); tolerance and IterMax default to params.h:13-15."""
+
+    def __init__(self, ctx: Context, chain=0, tol=1e-8, tol_mode=YK_TOL_ABS, max_iter=1000, precision=YK_FP64):
+        self.ctx, self.chain = ctx, chain
+        self.tol, self.tol_mode, self.max_iter, self.precision = tol, tol_mode, max_iter, precision
+        self.last = None
+
+    def solve(self, inVec, outVec, D: DiracOP | None = None, Mtype=MatrixType.Dagger) -> SolveStats:
+        self.last = self.ctx.cg_solve(inVec, outVec, int(Mtype), self.tol, self.tol_mode, self.max_iter,
+                                      self.precision, self.chain, allow_noconv=True)
+        return self.last
+
+
+class FermionicDrift:
+    """FermionicDrift (code/src/FermionicDrift.cuh:11-32): Philox noise instead of per-element XORWOW states."""
+
+    def __init__(self, ctx: Context, chain=0):
+        self.ctx, self.chain = ctx, chain
+
+    def getForce(self, outVec, D: DiracOP | None = None, CG: CGsolver | None = None, eta=None) -> SolveStats:
+        return self.ctx.fermion_force(outVec, eta, self.chain)
+
+
+class ColouredNoise:
+    """ColouredNoise (code/src/colouredNoise.h:26-51): xi = filtered white noise."""
+
+    def __init__(self, ctx: Context, noise, chain=0):
+        self.ctx, self.noise, self.chain = ctx, noise, chain
+
+    def __call__(self, white=None):
+        self.ctx.coloured_noise(self.noise, white, self.chain)
+
+
+def gamma_method(data, stau=1.5):
+    """Wolff Gamma-method: (mean, error, error of error, tau_int, tau_int error)."""
+    import numpy as np
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    out = np.zeros(5)
+    _check(lib().yk_gamma_method(d.ctypes.data_as(C.c_void_p), d.size, stau, out.ctypes.data_as(C.c_void_p)))
+    return tuple(out)
+
+
+def run(toml_path, out_dir="."):
+    """The reference's `./out input.toml` protocol (main.cu:73-516)."""
+    _check(lib().yk_run_toml(str(toml_path).encode(), str(out_dir).encode()))

@@ -1,0 +1,1035 @@
+// yk_api.cu -- the context runtime behind include/yukawa.h.
+//
+// A context owns every chain's device buffers in one allocation, the device
+// tables that let each kernel serve all chains at once (CG systems and tiles,
+// site tiles, noise block tables), and the captured CUDA graph of one
+// Langevin step.  The reference's equivalents are process-global
+// __constant__ parameters (code/src/main.cu:268-278) and per-object managed
+// buffers with a device synchronisation after every launch.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "yk_host.h"
+#include "yk_kernels.h"
+
+using namespace yk;
+
+#define YK_CK(call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            set_error("%s failed: %s", #call, cudaGetErrorString(e_));                      \
+            return YK_ECUDA;                                                                 \
+        }                                                                                    \
+    } while (0)
+
+namespace {
+
+// Bump allocator over one device allocation.
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0, used = 0;
+    size_t reserve(size_t bytes)
+    {
+        const size_t off = (used + 255) & ~(size_t)255;
+        used = off + bytes;
+        return off;
+    }
+    template <typename T>
+    T* at(size_t off)
+    {
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
+// Complex (K = 2) workspace of one chain for operator-level calls with
+// caller-provided complex buffers.
+struct Workspace {
+    bool ready = false;
+    int R = 0;                  // systems
+    void* mem = nullptr;
+    SysDev* d_sys = nullptr;
+    int2* d_tiles = nullptr;
+    CGState* d_state = nullptr;
+    double2* d_partial = nullptr;
+    ChainDev* d_chain = nullptr;   // chain copy whose sys0 = 0 refers to d_sys
+    int2* d_site_tiles = nullptr;
+    std::vector<SysDev> h_sys;
+    double* point = nullptr;    // point source (K = 2)
+    double* work = nullptr;     // K = 2 spinor scratch
+    double* corr = nullptr;     // Nt
+};
+
+struct Chain {
+    yk_params p;
+    yk_action a;
+    int Nt, Nx, V;
+    int filter;
+    int n_rhs_step;             // CG systems per step (0 when g == 0)
+    int sys0 = 0, cg_tile0 = 0, cg_tile1 = 0;
+    int site_tile0 = 0, nsite_tiles = 0;
+    int row0 = 0, nrows = 0, col0 = 0, ncols = 0, white0 = 0, nwhite = 0;
+    double *phi, *drift, *xi, *force, *slices;
+    double2* spec;
+    uint8_t* keep;
+    double2 *tw_t, *tw_x;
+    Workspace ws;
+};
+
+}  // namespace
+
+struct yk_ctx {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<Chain> ch;
+    void* mem = nullptr;
+    // step tables
+    ChainDev* d_chains = nullptr;
+    std::vector<ChainDev> h_chains;
+    SysDev* d_sys = nullptr;
+    int nsys = 0;
+    int2* d_sys_tiles = nullptr;
+    int n_sys_tiles = 0;
+    CGState* d_state = nullptr;
+    double2* d_partial = nullptr;
+    GridBarrier* d_bar = nullptr;
+    int* d_err = nullptr;
+    int* d_nactive = nullptr;
+    int* d_anyru = nullptr;
+    int2* d_site_tiles = nullptr;
+    int n_site_tiles = 0;
+    double* d_tile_max = nullptr;
+    double2* d_tile_sum = nullptr;
+    double* d_tile_sum2 = nullptr;
+    int2 *d_rows = nullptr, *d_cols = nullptr, *d_white = nullptr;
+    int nrows = 0, ncols = 0, nwhite = 0;
+    int max_nx = 1, max_cols = 1;
+    // solver settings (shared by all chains of a context)
+    int precision = YK_FP64, tol_mode = YK_TOL_ABS, max_iter = 1000, reliable_every = 50;
+    double tol = 1e-8;
+    // step graph
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_failed = false;
+    int cg_grid = 0;
+};
+
+namespace {
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+int check_params(const yk_params& p, int c)
+{
+    if (p.Nt < 2 || p.Nx < 2) {
+        set_error("chain %d: lattice %dx%d too small (need Nt, Nx >= 2)", c, p.Nt, p.Nx);
+        return YK_EINVAL;
+    }
+    if ((int64_t)p.Nt * p.Nx > (1LL << 27)) {
+        set_error("chain %d: lattice %dx%d too large", c, p.Nt, p.Nx);
+        return YK_EINVAL;
+    }
+    if (!all_modes_kept(p.Nt, p.Nx, p.cut_fraction)) {
+        const bool okt = (is_pow2(p.Nt) && p.Nt <= kMaxFFT) || p.Nt <= kMaxDFT;
+        const bool okx = (is_pow2(p.Nx) && p.Nx <= kMaxFFT) || p.Nx <= kMaxDFT;
+        if (!okt || !okx) {
+            set_error("chain %d: coloured noise needs Nt, Nx powers of two <= %d or <= %d (got %dx%d)", c,
+                      kMaxFFT, kMaxDFT, p.Nt, p.Nx);
+            return YK_EINVAL;
+        }
+    }
+    if (p.n_rhs < 1 || p.n_rhs > 64) {
+        set_error("chain %d: n_rhs = %d outside [1, 64]", c, p.n_rhs);
+        return YK_EINVAL;
+    }
+    if (p.precision != YK_FP64 && p.precision != YK_MIXED) {
+        set_error("chain %d: precision must be YK_FP64 or YK_MIXED", c);
+        return YK_EINVAL;
+    }
+    if (p.cg_max_iter < 0 || p.cg_max_iter > 1000000) {
+        set_error("chain %d: cg_max_iter out of range", c);
+        return YK_EINVAL;
+    }
+    return YK_OK;
+}
+
+int ntiles_of(int V) { return (V + kTile - 1) / kTile; }
+
+int chain_ok(const yk_ctx* ctx, int c)
+{
+    if (!ctx || c < 0 || c >= (int)ctx->ch.size()) {
+        set_error("invalid context or chain index %d", c);
+        return YK_EINVAL;
+    }
+    return YK_OK;
+}
+
+int status_of_err(yk_ctx* ctx)
+{
+    int e = 0;
+    YK_CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (e) {
+        set_error("a bounded device wait gave up (status %d)", e);
+        return YK_ETIMEOUT;
+    }
+    return YK_OK;
+}
+
+CGArgs base_args(yk_ctx* ctx)
+{
+    CGArgs a = {};
+    a.bar = ctx->d_bar;
+    a.err = ctx->d_err;
+    a.n_active = ctx->d_nactive;
+    a.any_ru = ctx->d_anyru;
+    a.max_iter = ctx->max_iter;
+    a.tol_mode = ctx->tol_mode;
+    a.tol = ctx->tol;
+    a.reliable_every = ctx->reliable_every;
+    a.mtype = YK_DAGGER;
+    return a;
+}
+
+StepArgs step_args(yk_ctx* ctx)
+{
+    StepArgs s = {};
+    s.ch = ctx->d_chains;
+    s.nch = (int)ctx->ch.size();
+    s.tiles = ctx->d_site_tiles;
+    s.ntiles = ctx->n_site_tiles;
+    s.tile_max = ctx->d_tile_max;
+    s.tile_sum = ctx->d_tile_sum;
+    s.tile_sum2 = ctx->d_tile_sum2;
+    return s;
+}
+
+// Enqueues one Langevin step of every chain.
+int enqueue_step(yk_ctx* ctx)
+{
+    NoiseTables nt = {ctx->d_rows, ctx->nrows, ctx->d_cols, ctx->ncols, ctx->d_white, ctx->nwhite};
+    YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
+    if (ctx->nsys > 0) {
+        CGArgs a = base_args(ctx);
+        a.sys = ctx->d_sys;
+        a.sys_first = 0;
+        a.sys_count = ctx->nsys;
+        a.tiles = ctx->d_sys_tiles;
+        a.tile_begin = 0;
+        a.tile_end = ctx->n_sys_tiles;
+        a.eta_kind = 2;
+        a.st = ctx->d_state;
+        a.partial = ctx->d_partial;
+        YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
+    }
+    StepArgs s = step_args(ctx);
+    YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream));
+    YK_CK(launch_update(s, ctx->d_state, ctx->stream));
+    return YK_OK;
+}
+
+// Complex (K = 2) workspace with R systems for chain c.
+int ensure_ws(yk_ctx* ctx, int c, int R)
+{
+    Chain& C = ctx->ch[c];
+    Workspace& w = C.ws;
+    if (w.ready && w.R >= R) return YK_OK;
+    if (w.mem) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(w.mem);
+        w = Workspace();
+    }
+    const int V = C.V, nt = ntiles_of(V);
+    const size_t v64 = sizeof(double) * 8 * (size_t)V, v32 = sizeof(float) * 8 * (size_t)V;
+    Arena ar;
+    const size_t o_sys = ar.reserve(sizeof(SysDev) * R);
+    const size_t o_tiles = ar.reserve(sizeof(int2) * (size_t)R * nt);
+    const size_t o_state = ar.reserve(sizeof(CGState) * R);
+    const size_t o_part = ar.reserve(sizeof(double2) * (size_t)R * nt);
+    const size_t o_chain = ar.reserve(sizeof(ChainDev));
+    const size_t o_stile = ar.reserve(sizeof(int2) * nt);
+    const size_t o_point = ar.reserve(v64);
+    const size_t o_work = ar.reserve(v64);
+    const size_t o_corr = ar.reserve(sizeof(double) * C.Nt);
+    std::vector<size_t> o_vec(R * 12);
+    for (int j = 0; j < R; ++j) {
+        for (int q = 0; q < 6; ++q) o_vec[j * 12 + q] = ar.reserve(v64);       // x r p0 p1 t Ap
+        for (int q = 6; q < 12; ++q) o_vec[j * 12 + q] = ar.reserve(v32);      // r p0 p1 t Ap xs
+    }
+    void* mem = nullptr;
+    if (cudaMalloc(&mem, ar.used) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("workspace allocation of %zu bytes failed", ar.used);
+        return YK_ENOMEM;
+    }
+    ar.base = (char*)mem;
+    w.mem = mem;
+    w.R = R;
+    w.d_sys = ar.at<SysDev>(o_sys);
+    w.d_tiles = ar.at<int2>(o_tiles);
+    w.d_state = ar.at<CGState>(o_state);
+    w.d_partial = ar.at<double2>(o_part);
+    w.d_chain = ar.at<ChainDev>(o_chain);
+    w.d_site_tiles = ar.at<int2>(o_stile);
+    w.point = ar.at<double>(o_point);
+    w.work = ar.at<double>(o_work);
+    w.corr = ar.at<double>(o_corr);
+    w.h_sys.assign(R, SysDev());
+    std::vector<int2> tiles((size_t)R * nt);
+    for (int j = 0; j < R; ++j) {
+        SysDev& S = w.h_sys[j];
+        std::memset(&S, 0, sizeof(S));
+        S.chain = c;
+        S.rhs = j;
+        S.Nt = C.Nt;
+        S.Nx = C.Nx;
+        S.V = V;
+        S.tile0 = j * nt;
+        S.ntiles = nt;
+        S.m0 = C.a.m0;
+        S.g = C.a.g;
+        S.r = C.a.r;
+        S.sigma = C.phi;
+        S.x = ar.at<double>(o_vec[j * 12 + 0]);
+        S.r64 = ar.at<double>(o_vec[j * 12 + 1]);
+        S.p64[0] = ar.at<double>(o_vec[j * 12 + 2]);
+        S.p64[1] = ar.at<double>(o_vec[j * 12 + 3]);
+        S.t64 = ar.at<double>(o_vec[j * 12 + 4]);
+        S.Ap64 = ar.at<double>(o_vec[j * 12 + 5]);
+        S.r32 = ar.at<float>(o_vec[j * 12 + 6]);
+        S.p32[0] = ar.at<float>(o_vec[j * 12 + 7]);
+        S.p32[1] = ar.at<float>(o_vec[j * 12 + 8]);
+        S.t32 = ar.at<float>(o_vec[j * 12 + 9]);
+        S.Ap32 = ar.at<float>(o_vec[j * 12 + 10]);
+        S.xs32 = ar.at<float>(o_vec[j * 12 + 11]);
+        S.gen_eta = 0;
+        for (int t = 0; t < nt; ++t) tiles[(size_t)j * nt + t] = make_int2(j, t * kTile);
+    }
+    std::vector<int2> stiles(nt);
+    for (int t = 0; t < nt; ++t) stiles[t] = make_int2(0, t * kTile);
+    YK_CK(cudaMemcpyAsync(w.d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    YK_CK(cudaMemcpyAsync(w.d_site_tiles, stiles.data(), sizeof(int2) * nt, cudaMemcpyHostToDevice,
+                          ctx->stream));
+    YK_CK(cudaMemsetAsync(w.d_state, 0, sizeof(CGState) * R, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    w.ready = true;
+    return YK_OK;
+}
+
+// Solves the first `count` systems of chain c's complex workspace.
+int ws_solve(yk_ctx* ctx, int c, int count, int mtype, double tol, int tol_mode, int max_iter, int precision,
+             yk_solve_stats* stats)
+{
+    Chain& C = ctx->ch[c];
+    Workspace& w = C.ws;
+    YK_CK(cudaMemcpyAsync(w.d_sys, w.h_sys.data(), sizeof(SysDev) * count, cudaMemcpyHostToDevice, ctx->stream));
+    CGArgs a = base_args(ctx);
+    a.sys = w.d_sys;
+    a.sys_first = 0;
+    a.sys_count = count;
+    a.tiles = w.d_tiles;
+    a.tile_begin = 0;
+    a.tile_end = count * ntiles_of(C.V);
+    a.eta_kind = 0;
+    a.st = w.d_state;
+    a.partial = w.d_partial;
+    a.mtype = mtype;
+    a.tol = tol;
+    a.tol_mode = tol_mode;
+    a.max_iter = max_iter;
+    YK_CK(launch_cg(a, 2, precision == YK_MIXED, ctx->stream, nullptr));
+    std::vector<CGState> st(count);
+    YK_CK(cudaMemcpyAsync(st.data(), w.d_state, sizeof(CGState) * count, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = status_of_err(ctx);
+    if (rc) return rc;
+    yk_solve_stats s = {};
+    s.converged = 1;
+    int status = 0;
+    for (int j = 0; j < count; ++j) {
+        s.iterations += st[j].iters;
+        s.reliable_updates += st[j].n_ru;
+        s.rr += st[j].rr;
+        s.rr0 += st[j].rr0;
+        if (!st[j].converged) s.converged = 0;
+        if (!status && st[j].status) status = st[j].status;
+    }
+    if (stats) *stats = s;
+    if (status) {
+        set_error("CG: status %d after %d iterations (|r|^2 = %g)", status, s.iterations, s.rr);
+        return status;
+    }
+    return YK_OK;
+}
+
+// Runs the CG of chain c's step systems (K = 1) with Philox right-hand sides
+// of stream `kind` at the chain's current step.
+int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
+{
+    Chain& C = ctx->ch[c];
+    if (C.n_rhs_step == 0) {
+        if (stats) *stats = yk_solve_stats{0, 0, 0.0, 0.0, 1};
+        return YK_OK;
+    }
+    CGArgs a = base_args(ctx);
+    a.sys = ctx->d_sys;
+    a.sys_first = C.sys0;
+    a.sys_count = C.n_rhs_step;
+    a.tiles = ctx->d_sys_tiles;
+    a.tile_begin = C.cg_tile0;
+    a.tile_end = C.cg_tile1;
+    a.eta_kind = kind;
+    a.st = ctx->d_state;
+    a.partial = ctx->d_partial;
+    YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, nullptr));
+    std::vector<CGState> st(C.n_rhs_step);
+    YK_CK(cudaMemcpyAsync(st.data(), ctx->d_state + C.sys0, sizeof(CGState) * C.n_rhs_step,
+                          cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = status_of_err(ctx);
+    if (rc) return rc;
+    yk_solve_stats s = {};
+    s.converged = 1;
+    int status = 0;
+    for (auto& q : st) {
+        s.iterations += q.iters;
+        s.reliable_updates += q.n_ru;
+        s.rr += q.rr;
+        s.rr0 += q.rr0;
+        if (!q.converged) s.converged = 0;
+        if (!status && q.status) status = q.status;
+    }
+    if (stats) *stats = s;
+    if (status) {
+        set_error("CG: status %d after %d iterations", status, s.iterations);
+        return status;
+    }
+    return YK_OK;
+}
+
+StepArgs chain_step_args(yk_ctx* ctx, int c)
+{
+    StepArgs s = step_args(ctx);
+    s.tiles = ctx->d_site_tiles + ctx->ch[c].site_tile0;
+    s.ntiles = ctx->ch[c].nsite_tiles;
+    s.tile_base = ctx->ch[c].site_tile0;
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
+{
+    if (!params || n_chains < 1 || !out) {
+        set_error("yk_ctx_create: bad arguments");
+        return YK_EINVAL;
+    }
+    *out = nullptr;
+    for (int c = 0; c < n_chains; ++c) {
+        int rc = check_params(params[c], c);
+        if (rc) return rc;
+    }
+    const yk_params& p0 = params[0];
+    for (int c = 1; c < n_chains; ++c) {
+        const yk_params& p = params[c];
+        if (p.precision != p0.precision || p.cg_tol_mode != p0.cg_tol_mode || p.cg_tol != p0.cg_tol ||
+            p.cg_max_iter != p0.cg_max_iter || p.reliable_every != p0.reliable_every) {
+            set_error("chains of one context must share precision and CG settings");
+            return YK_EINVAL;
+        }
+    }
+    std::unique_ptr<yk_ctx> ctx(new yk_ctx());
+    YK_CK(cudaGetDevice(&ctx->dev));
+    YK_CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    ctx->own_stream = true;
+    ctx->precision = p0.precision;
+    ctx->tol_mode = p0.cg_tol_mode;
+    ctx->tol = p0.cg_tol;
+    ctx->max_iter = p0.cg_max_iter;
+    ctx->reliable_every = p0.reliable_every;
+    const bool mixed = ctx->precision == YK_MIXED;
+    // occupancy queries and kernel attributes before any stream capture
+    cg_max_grid(1, mixed);
+    cg_max_grid(2, false);
+    cg_max_grid(2, true);
+    noise_init_attributes();
+
+    ctx->ch.resize(n_chains);
+    int nsys = 0, nsys_tiles = 0, nsite_tiles = 0, nrows = 0, ncols = 0, nwhite = 0;
+    for (int c = 0; c < n_chains; ++c) {
+        Chain& C = ctx->ch[c];
+        C.p = params[c];
+        yk_derive_action(&C.p, &C.a);
+        C.Nt = C.p.Nt;
+        C.Nx = C.p.Nx;
+        C.V = C.Nt * C.Nx;
+        C.filter = all_modes_kept(C.Nt, C.Nx, C.p.cut_fraction) ? 0 : 1;
+        C.n_rhs_step = (C.a.g != 0.0) ? C.p.n_rhs : 0;
+        const int nt = ntiles_of(C.V);
+        C.sys0 = nsys;
+        C.cg_tile0 = nsys_tiles;
+        nsys += C.n_rhs_step;
+        nsys_tiles += C.n_rhs_step * nt;
+        C.cg_tile1 = nsys_tiles;
+        C.site_tile0 = nsite_tiles;
+        C.nsite_tiles = nt;
+        nsite_tiles += nt;
+        if (C.filter) {
+            C.row0 = nrows;
+            C.nrows = C.Nt;
+            nrows += C.Nt;
+            const int cw = noise_strip(C.Nt);
+            C.col0 = ncols;
+            C.ncols = (C.Nx + cw - 1) / cw;
+            ncols += C.ncols;
+            if (C.Nx > ctx->max_nx) ctx->max_nx = C.Nx;
+            const int ce = C.Nt * (cw < C.Nx ? cw : C.Nx);
+            if (ce > ctx->max_cols) ctx->max_cols = ce;
+        } else {
+            C.white0 = nwhite;
+            C.nwhite = nt;
+            nwhite += nt;
+        }
+    }
+    ctx->nsys = nsys;
+    ctx->n_sys_tiles = nsys_tiles;
+    ctx->n_site_tiles = nsite_tiles;
+    ctx->nrows = nrows;
+    ctx->ncols = ncols;
+    ctx->nwhite = nwhite;
+
+    // ---- one arena for everything
+    Arena ar;
+    struct COff {
+        size_t phi, drift, xi, force, slices, spec, keep, twt, twx;
+    };
+    std::vector<COff> co(n_chains);
+    struct SOff {
+        size_t b, x, r64, p0, p1, t64, ap64, r32, q0, q1, t32, ap32, xs;
+    };
+    std::vector<SOff> so(nsys);
+    for (int c = 0; c < n_chains; ++c) {
+        Chain& C = ctx->ch[c];
+        const size_t V = C.V;
+        co[c].phi = ar.reserve(8 * V);
+        co[c].drift = ar.reserve(8 * V);
+        co[c].xi = ar.reserve(8 * V);
+        co[c].force = ar.reserve(8 * V);
+        co[c].slices = ar.reserve(8 * (size_t)C.Nt);
+        if (C.filter) {
+            co[c].spec = ar.reserve(16 * V);
+            co[c].keep = ar.reserve(V);
+            co[c].twt = ar.reserve(16 * (size_t)C.Nt);
+            co[c].twx = ar.reserve(16 * (size_t)C.Nx);
+        }
+        for (int j = 0; j < C.n_rhs_step; ++j) {
+            SOff& o = so[C.sys0 + j];
+            const size_t d = 8 * 4 * V, f = 4 * 4 * V;
+            o.b = ar.reserve(d);
+            o.x = ar.reserve(d);
+            o.t64 = ar.reserve(d);
+            if (mixed) {
+                o.r32 = ar.reserve(f);
+                o.q0 = ar.reserve(f);
+                o.q1 = ar.reserve(f);
+                o.t32 = ar.reserve(f);
+                o.ap32 = ar.reserve(f);
+                o.xs = ar.reserve(f);
+            } else {
+                o.r64 = ar.reserve(d);
+                o.p0 = ar.reserve(d);
+                o.p1 = ar.reserve(d);
+                o.ap64 = ar.reserve(d);
+            }
+        }
+    }
+    const size_t o_chains = ar.reserve(sizeof(ChainDev) * n_chains);
+    const size_t o_sys = ar.reserve(sizeof(SysDev) * (nsys > 0 ? nsys : 1));
+    const size_t o_systiles = ar.reserve(sizeof(int2) * (nsys_tiles > 0 ? nsys_tiles : 1));
+    const size_t o_state = ar.reserve(sizeof(CGState) * (nsys > 0 ? nsys : 1));
+    const size_t o_partial = ar.reserve(sizeof(double2) * (nsys_tiles > 0 ? nsys_tiles : 1));
+    const size_t o_bar = ar.reserve(sizeof(GridBarrier));
+    const size_t o_err = ar.reserve(sizeof(int) * 4);
+    const size_t o_sitetiles = ar.reserve(sizeof(int2) * nsite_tiles);
+    const size_t o_tmax = ar.reserve(sizeof(double) * nsite_tiles);
+    const size_t o_tsum = ar.reserve(sizeof(double2) * nsite_tiles);
+    const size_t o_tsum2 = ar.reserve(sizeof(double) * nsite_tiles);
+    const size_t o_rows = ar.reserve(sizeof(int2) * (nrows > 0 ? nrows : 1));
+    const size_t o_cols = ar.reserve(sizeof(int2) * (ncols > 0 ? ncols : 1));
+    const size_t o_white = ar.reserve(sizeof(int2) * (nwhite > 0 ? nwhite : 1));
+    if (cudaMalloc(&ctx->mem, ar.used) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("context allocation of %zu bytes failed", ar.used);
+        cudaStreamDestroy(ctx->stream);
+        return YK_ENOMEM;
+    }
+    ar.base = (char*)ctx->mem;
+    YK_CK(cudaMemsetAsync(ctx->mem, 0, ar.used, ctx->stream));
+
+    ctx->d_chains = ar.at<ChainDev>(o_chains);
+    ctx->d_sys = ar.at<SysDev>(o_sys);
+    ctx->d_sys_tiles = ar.at<int2>(o_systiles);
+    ctx->d_state = ar.at<CGState>(o_state);
+    ctx->d_partial = ar.at<double2>(o_partial);
+    ctx->d_bar = ar.at<GridBarrier>(o_bar);
+    ctx->d_err = ar.at<int>(o_err);
+    ctx->d_nactive = ctx->d_err + 1;
+    ctx->d_anyru = ctx->d_err + 2;
+    ctx->d_site_tiles = ar.at<int2>(o_sitetiles);
+    ctx->d_tile_max = ar.at<double>(o_tmax);
+    ctx->d_tile_sum = ar.at<double2>(o_tsum);
+    ctx->d_tile_sum2 = ar.at<double>(o_tsum2);
+    ctx->d_rows = ar.at<int2>(o_rows);
+    ctx->d_cols = ar.at<int2>(o_cols);
+    ctx->d_white = ar.at<int2>(o_white);
+
+    std::vector<SysDev> hs(nsys);
+    std::vector<int2> sys_tiles, site_tiles, rows, cols, white;
+    ctx->h_chains.assign(n_chains, ChainDev());
+    int64_t drand_skip = 0;
+    for (int c = 0; c < n_chains; ++c) {
+        Chain& C = ctx->ch[c];
+        const COff& o = co[c];
+        C.phi = ar.at<double>(o.phi);
+        C.drift = ar.at<double>(o.drift);
+        C.xi = ar.at<double>(o.xi);
+        C.force = ar.at<double>(o.force);
+        C.slices = ar.at<double>(o.slices);
+        C.spec = C.filter ? ar.at<double2>(o.spec) : nullptr;
+        C.keep = C.filter ? ar.at<uint8_t>(o.keep) : nullptr;
+        C.tw_t = C.filter ? ar.at<double2>(o.twt) : nullptr;
+        C.tw_x = C.filter ? ar.at<double2>(o.twx) : nullptr;
+        const int nt = ntiles_of(C.V);
+        for (int t = 0; t < nt; ++t) site_tiles.push_back(make_int2(c, t * kTile));
+        for (int j = 0; j < C.n_rhs_step; ++j) {
+            const SOff& q = so[C.sys0 + j];
+            SysDev& S = hs[C.sys0 + j];
+            std::memset(&S, 0, sizeof(S));
+            S.chain = c;
+            S.rhs = j;
+            S.Nt = C.Nt;
+            S.Nx = C.Nx;
+            S.V = C.V;
+            S.tile0 = (int)sys_tiles.size();
+            S.ntiles = nt;
+            S.m0 = C.a.m0;
+            S.g = C.a.g;
+            S.r = C.a.r;
+            S.sigma = C.phi;
+            S.b = ar.at<double>(q.b);
+            S.x = ar.at<double>(q.x);
+            S.t64 = ar.at<double>(q.t64);
+            if (mixed) {
+                S.r32 = ar.at<float>(q.r32);
+                S.p32[0] = ar.at<float>(q.q0);
+                S.p32[1] = ar.at<float>(q.q1);
+                S.t32 = ar.at<float>(q.t32);
+                S.Ap32 = ar.at<float>(q.ap32);
+                S.xs32 = ar.at<float>(q.xs);
+            } else {
+                S.r64 = ar.at<double>(q.r64);
+                S.p64[0] = ar.at<double>(q.p0);
+                S.p64[1] = ar.at<double>(q.p1);
+                S.Ap64 = ar.at<double>(q.ap64);
+            }
+            S.gen_eta = 1;
+            S.seed = (uint64_t)C.p.seed;
+            S.step = &ctx->d_chains[c].step;
+            for (int t = 0; t < nt; ++t) sys_tiles.push_back(make_int2(C.sys0 + j, t * kTile));
+        }
+        if (C.filter) {
+            for (int t = 0; t < C.Nt; ++t) rows.push_back(make_int2(c, t));
+            const int cw = noise_strip(C.Nt);
+            for (int x0 = 0; x0 < C.Nx; x0 += cw) cols.push_back(make_int2(c, x0));
+            std::vector<uint8_t> keep;
+            momentum_keep(C.Nt, C.Nx, C.p.cut_fraction, keep);
+            std::vector<double> twt, twx;
+            twiddles(C.Nt, twt);
+            twiddles(C.Nx, twx);
+            YK_CK(cudaMemcpy(C.keep, keep.data(), keep.size(), cudaMemcpyHostToDevice));
+            YK_CK(cudaMemcpy(C.tw_t, twt.data(), sizeof(double) * twt.size(), cudaMemcpyHostToDevice));
+            YK_CK(cudaMemcpy(C.tw_x, twx.data(), sizeof(double) * twx.size(), cudaMemcpyHostToDevice));
+        } else {
+            for (int t = 0; t < nt; ++t) white.push_back(make_int2(c, t * kTile));
+        }
+        // initial field (main.cu:92-95)
+        std::vector<double> phi(C.V, 0.0);
+        if (C.p.init == YK_INIT_DRAND48) {
+            drand48_field(drand_skip, C.V, phi.data());
+            drand_skip += C.V;
+        } else if (C.p.init == YK_INIT_PHILOX) {
+            // 1 - 2u, u uniform in (0, 1) from Philox stream kind 0 of (seed, chain)
+            philox_uniform_field((uint64_t)C.p.seed, (uint32_t)c, C.V, phi.data());
+        }
+        YK_CK(cudaMemcpy(C.phi, phi.data(), sizeof(double) * C.V, cudaMemcpyHostToDevice));
+
+        ChainDev& H = ctx->h_chains[c];
+        std::memset(&H, 0, sizeof(H));
+        H.Nt = C.Nt;
+        H.Nx = C.Nx;
+        H.V = C.V;
+        H.n_rhs = C.n_rhs_step;
+        H.sys0 = C.sys0;
+        H.tile0 = C.site_tile0;
+        H.ntiles = C.nsite_tiles;
+        H.m2 = C.a.m2;
+        H.lambda = C.a.lambda;
+        H.g = C.a.g;
+        H.m0 = C.a.m0;
+        H.r = C.a.r;
+        H.cut = C.a.cut_fraction;
+        H.eps_bar = C.a.eps_bar;
+        H.fixed_dt = C.p.fixed_dt;
+        H.drift_mode = C.a.drift_mode;
+        H.filter = C.filter;
+        H.seed = (uint64_t)C.p.seed;
+        H.chain_id = (uint32_t)c;
+        H.phi = C.phi;
+        H.drift = C.drift;
+        H.xi = C.xi;
+        H.white = nullptr;
+        H.spec = C.spec;
+        H.keep = C.keep;
+        H.tw_t = C.tw_t;
+        H.tw_x = C.tw_x;
+        H.step = 0;
+        H.time = 0.0;
+    }
+    YK_CK(cudaMemcpyAsync(ctx->d_chains, ctx->h_chains.data(), sizeof(ChainDev) * n_chains,
+                          cudaMemcpyHostToDevice, ctx->stream));
+    if (nsys > 0) {
+        YK_CK(cudaMemcpyAsync(ctx->d_sys, hs.data(), sizeof(SysDev) * nsys, cudaMemcpyHostToDevice, ctx->stream));
+        YK_CK(cudaMemcpyAsync(ctx->d_sys_tiles, sys_tiles.data(), sizeof(int2) * sys_tiles.size(),
+                              cudaMemcpyHostToDevice, ctx->stream));
+    }
+    YK_CK(cudaMemcpyAsync(ctx->d_site_tiles, site_tiles.data(), sizeof(int2) * site_tiles.size(),
+                          cudaMemcpyHostToDevice, ctx->stream));
+    if (!rows.empty()) {
+        YK_CK(cudaMemcpyAsync(ctx->d_rows, rows.data(), sizeof(int2) * rows.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+        YK_CK(cudaMemcpyAsync(ctx->d_cols, cols.data(), sizeof(int2) * cols.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    }
+    if (!white.empty())
+        YK_CK(cudaMemcpyAsync(ctx->d_white, white.data(), sizeof(int2) * white.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    *out = ctx.release();
+    return YK_OK;
+}
+
+int yk_ctx_destroy(yk_ctx* ctx)
+{
+    if (!ctx) return YK_OK;
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (auto& C : ctx->ch)
+        if (C.ws.mem) cudaFree(C.ws.mem);
+    if (ctx->mem) cudaFree(ctx->mem);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return YK_OK;
+}
+
+int yk_ctx_set_stream(yk_ctx* ctx, void* stream)
+{
+    if (!ctx) return YK_EINVAL;
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    return YK_OK;
+}
+
+int yk_ctx_synchronize(yk_ctx* ctx)
+{
+    if (!ctx) return YK_EINVAL;
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return status_of_err(ctx);
+}
+
+int yk_ctx_n_chains(const yk_ctx* ctx) { return ctx ? (int)ctx->ch.size() : 0; }
+
+int yk_ctx_volume(const yk_ctx* ctx, int chain)
+{
+    if (!ctx || chain < 0 || chain >= (int)ctx->ch.size()) return 0;
+    return ctx->ch[chain].V;
+}
+
+int yk_ctx_shape(const yk_ctx* ctx, int c, int* Nt, int* Nx)
+{
+    if (!ctx || c < 0 || c >= (int)ctx->ch.size()) return YK_EINVAL;
+    if (Nt) *Nt = ctx->ch[c].Nt;
+    if (Nx) *Nx = ctx->ch[c].Nx;
+    return YK_OK;
+}
+
+int yk_set_field_host(yk_ctx* ctx, int c, const double* phi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    YK_CK(cudaMemcpyAsync(ctx->ch[c].phi, phi, sizeof(double) * ctx->ch[c].V, cudaMemcpyHostToDevice, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_get_field_host(yk_ctx* ctx, int c, double* phi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    YK_CK(cudaMemcpyAsync(phi, ctx->ch[c].phi, sizeof(double) * ctx->ch[c].V, cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_field_device(yk_ctx* ctx, int c, double** phi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    *phi = ctx->ch[c].phi;
+    return YK_OK;
+}
+
+int yk_dirac_apply(yk_ctx* ctx, int c, const void* in, void* out, int dagger, int precision)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!in || !out || (precision != YK_FP64 && precision != YK_FP32)) {
+        set_error("yk_dirac_apply: bad buffers or precision");
+        return YK_EINVAL;
+    }
+    if (in == out) {
+        set_error("yk_dirac_apply: in and out must not alias");
+        return YK_EINVAL;
+    }
+    const Chain& C = ctx->ch[c];
+    YK_CK(launch_dirac(in, out, C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r, dagger ? 1 : 0, precision, 2,
+                       ctx->stream));
+    return YK_OK;
+}
+
+int yk_cg_solve(yk_ctx* ctx, int c, const void* b, void* x, int mtype, double tol, int tol_mode, int max_iter,
+                int precision, yk_solve_stats* stats)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!b || !x || b == x || (precision != YK_FP64 && precision != YK_MIXED) || max_iter < 0 ||
+        (mtype != YK_NORMAL && mtype != YK_DAGGER) || !(tol >= 0.0)) {
+        set_error("yk_cg_solve: bad arguments");
+        return YK_EINVAL;
+    }
+    if (int rc = ensure_ws(ctx, c, 1)) return rc;
+    Workspace& w = ctx->ch[c].ws;
+    w.h_sys[0].b = (double*)b;
+    w.h_sys[0].x = (double*)x;
+    int rc = ws_solve(ctx, c, 1, mtype, tol, tol_mode, max_iter, precision, stats);
+    w.h_sys[0].b = nullptr;
+    return rc;
+}
+
+int yk_fermion_force(yk_ctx* ctx, int c, const void* eta, double* F, yk_solve_stats* stats)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!F) {
+        set_error("yk_fermion_force: F is null");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    if (eta) {
+        const int R = C.p.n_rhs;
+        if (int rc = ensure_ws(ctx, c, R)) return rc;
+        Workspace& w = C.ws;
+        for (int j = 0; j < R; ++j) w.h_sys[j].b = (double*)eta + (size_t)j * 8 * C.V;
+        int rc = YK_OK;
+        if (C.a.g != 0.0) rc = ws_solve(ctx, c, R, YK_DAGGER, ctx->tol, ctx->tol_mode, ctx->max_iter, YK_FP64, stats);
+        else if (stats) *stats = yk_solve_stats{0, 0, 0.0, 0.0, 1};
+        if (rc && rc != YK_ENOCONV) return rc;
+        ChainDev H = ctx->h_chains[c];
+        H.sys0 = 0;
+        H.n_rhs = (C.a.g != 0.0) ? R : 0;
+        H.drift = F;
+        H.tile0 = 0;
+        YK_CK(cudaMemcpyAsync(w.d_chain, &H, sizeof(ChainDev), cudaMemcpyHostToDevice, ctx->stream));
+        StepArgs s = step_args(ctx);
+        s.ch = w.d_chain;
+        s.nch = 1;
+        s.tiles = w.d_site_tiles;
+        s.ntiles = ntiles_of(C.V);
+        YK_CK(launch_force_drift(s, w.d_sys, 1, 2, ctx->stream));
+        YK_CK(cudaStreamSynchronize(ctx->stream));
+        return rc;
+    }
+    int rc = chain_solve(ctx, c, 2, stats);
+    if (rc && rc != YK_ENOCONV) return rc;
+    StepArgs s = chain_step_args(ctx, c);
+    YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
+    YK_CK(cudaMemcpyAsync(F, C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return rc;
+}
+
+int yk_coloured_noise(yk_ctx* ctx, int c, const double* white, double* xi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!xi) {
+        set_error("yk_coloured_noise: xi is null");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    NoiseTables nt = {ctx->d_rows + C.row0, C.nrows, ctx->d_cols + C.col0, C.ncols, ctx->d_white + C.white0,
+                      C.nwhite};
+    YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, white, ctx->stream));
+    YK_CK(cudaMemcpyAsync(xi, C.xi, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream));
+    return YK_OK;
+}
+
+int yk_langevin_step(yk_ctx* ctx, int n_steps)
+{
+    if (!ctx || n_steps < 0) {
+        set_error("yk_langevin_step: bad arguments");
+        return YK_EINVAL;
+    }
+    if (!ctx->gexec && !ctx->graph_failed && ctx->stream) {
+        cudaGraph_t g = nullptr;
+        bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            const int rc = enqueue_step(ctx);
+            const bool end_ok = cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess;
+            ok = (rc == YK_OK) && end_ok && g;
+            if (ok) ok = cudaGraphInstantiate(&ctx->gexec, g, 0) == cudaSuccess;
+            if (g) cudaGraphDestroy(g);
+        }
+        if (!ok) {
+            cudaGetLastError();
+            ctx->gexec = nullptr;
+            ctx->graph_failed = true;
+        }
+    }
+    for (int i = 0; i < n_steps; ++i) {
+        if (ctx->gexec) {
+            YK_CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+        } else {
+            if (int rc = enqueue_step(ctx)) return rc;
+        }
+    }
+    return YK_OK;
+}
+
+int yk_euler_update(yk_ctx* ctx, int c, const double* force, const double* xi, yk_obs* obs)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!force || !xi) {
+        set_error("yk_euler_update: force and xi are required");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    YK_CK(cudaMemcpyAsync(C.drift, force, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream));
+    YK_CK(cudaMemcpyAsync(C.xi, xi, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream));
+    StepArgs s = chain_step_args(ctx, c);
+    YK_CK(launch_force_drift(s, ctx->d_sys, 2, 1, ctx->stream));
+    YK_CK(launch_update(s, ctx->d_state, ctx->stream));
+    if (obs) return yk_observables(ctx, c, obs);
+    return YK_OK;
+}
+
+int yk_observables(yk_ctx* ctx, int c, yk_obs* obs)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    YK_CK(cudaMemcpyAsync(obs, &ctx->d_chains[c].obs, sizeof(yk_obs), cudaMemcpyDeviceToHost, ctx->stream));
+    return status_of_err(ctx);
+}
+
+int yk_time_slices(yk_ctx* ctx, int c, double* slices)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    Chain& C = ctx->ch[c];
+    YK_CK(launch_time_slices(C.phi, C.slices, C.Nt, C.Nx, ctx->stream));
+    YK_CK(cudaMemcpyAsync(slices, C.slices, sizeof(double) * C.Nt, cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_correlator(yk_ctx* ctx, int c, double* corr, yk_solve_stats* stats)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (int rc = ensure_ws(ctx, c, 1)) return rc;
+    Chain& C = ctx->ch[c];
+    Workspace& w = C.ws;
+    // point source in[0] = in[1] = 1 at site 0 (main.cu:441-450)
+    YK_CK(cudaMemsetAsync(w.point, 0, sizeof(double) * 8 * (size_t)C.V, ctx->stream));
+    const double one = 1.0;
+    YK_CK(cudaMemcpyAsync(w.point + 0, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    YK_CK(cudaMemcpyAsync(w.point + 2, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    w.h_sys[0].b = w.point;
+    w.h_sys[0].x = w.work;
+    // CG.solve(in, out, Normal); applyD(out, in, Dagger) (main.cu:456-457)
+    int rc = ws_solve(ctx, c, 1, YK_NORMAL, ctx->tol, ctx->tol_mode, ctx->max_iter, ctx->precision, stats);
+    if (rc && rc != YK_ENOCONV) return rc;
+    YK_CK(launch_dirac(w.work, w.point, C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r, 1, YK_FP64, 2, ctx->stream));
+    YK_CK(launch_time_slices_spinor(w.point, w.corr, C.Nt, C.Nx, 2, ctx->stream));
+    YK_CK(cudaMemcpyAsync(corr, w.corr, sizeof(double) * C.Nt, cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return rc;
+}
+
+int yk_condensate(yk_ctx* ctx, int c, double* cond, yk_solve_stats* stats)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    Chain& C = ctx->ch[c];
+    if (C.a.g == 0.0) {
+        *cond = 0.0;   // main.cu:477-481
+        if (stats) *stats = yk_solve_stats{0, 0, 0.0, 0.0, 1};
+        return YK_OK;
+    }
+    int rc = chain_solve(ctx, c, 3, stats);   // fresh noise: Philox stream kind 3
+    if (rc && rc != YK_ENOCONV) return rc;
+    StepArgs s = chain_step_args(ctx, c);
+    YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
+    std::vector<double> F(C.V);
+    YK_CK(cudaMemcpyAsync(F.data(), C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    double tr = 0.0;
+    for (double f : F) tr += f;
+    *cond = (tr / C.a.g) / (double)C.V;   // main.cu:473-483
+    return rc;
+}
+
+int yk_set_eps_bar(yk_ctx* ctx, int c, double eps_bar)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    ctx->h_chains[c].eps_bar = eps_bar;
+    ctx->ch[c].a.eps_bar = eps_bar;
+    YK_CK(cudaMemcpyAsync(&ctx->d_chains[c].eps_bar, &ctx->h_chains[c].eps_bar, sizeof(double),
+                          cudaMemcpyHostToDevice, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_get_step(yk_ctx* ctx, int c, int64_t* step)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    YK_CK(cudaMemcpyAsync(step, &ctx->d_chains[c].step, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_set_time(yk_ctx* ctx, int c, double t)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    ctx->h_chains[c].time = t;
+    YK_CK(cudaMemcpyAsync(&ctx->d_chains[c].time, &ctx->h_chains[c].time, sizeof(double), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_set_step(yk_ctx* ctx, int c, int64_t step)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    ctx->h_chains[c].step = step;
+    YK_CK(cudaMemcpyAsync(&ctx->d_chains[c].step, &ctx->h_chains[c].step, sizeof(int64_t), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+}  // extern "C"

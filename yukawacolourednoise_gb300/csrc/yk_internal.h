@@ -1,0 +1,146 @@
+// yk_internal.h -- structures shared by the host runtime and the kernels.
+// Device tables are plain structs in device memory; kernels get them through
+// small by-value argument structs.
+#pragma once
+
+#include <stdint.h>
+
+#include "yukawa.h"
+
+#ifdef __CUDACC__
+#define YK_HD __host__ __device__
+#else
+#define YK_HD
+#endif
+
+namespace yk {
+
+constexpr int kBlock = 256;   // threads per block of the site kernels
+constexpr int kTile = 256;    // lattice sites per tile (one per thread)
+constexpr int kMaxFFT = 4096; // longest FFT edge handled in shared memory
+constexpr int kMaxDFT = 256;  // longest non-power-of-two edge (direct DFT)
+
+struct GridBarrier {
+    unsigned count;
+    unsigned gen;
+    unsigned pad[30];
+};
+
+// One linear system (chain, right-hand side) of a batched CG solve.
+struct SysDev {
+    int chain, rhs;
+    int Nt, Nx, V;
+    int tile0, ntiles;   // tiles of this system in the tile table
+    double m0, g, r;     // Dirac parameters of the chain
+    const double* sigma; // the chain's scalar field
+    // FP64 vectors (K real planes per spinor entry)
+    double* b;           // right-hand side (eta)
+    double* x;           // solution
+    double* r64;         // FP64 residual (FP64 solver)
+    double* p64[2];      // search directions, double-buffered
+    double* t64;         // D p (or D x in reliable updates)
+    double* Ap64;        // D^dag D p
+    // FP32 vectors (mixed solver)
+    float* r32;
+    float* p32[2];
+    float* t32;
+    float* Ap32;
+    float* xs32;         // solution increment since the last reliable update
+    // noise generation for b: kind/rhs of the Philox stream, or gen = 0
+    int gen_eta;
+    uint64_t seed;
+    const int64_t* step; // device step counter of the chain
+};
+
+// Per-system CG scalars, written by the finaliser block of each reduction.
+struct CGState {
+    double rr, rr0, rr_prev, stop;
+    double alpha_re, alpha_im;
+    double beta;
+    int active;
+    int iters;
+    int converged;
+    int status;
+    int ru;      // reliable update pending
+    int n_ru;
+    int last;    // iteration cap reached: finish with a reliable update
+    unsigned counter;
+};
+
+struct CGArgs {
+    SysDev* sys;
+    int sys_first, sys_count;   // systems taking part in this solve
+    const int2* tiles;          // (system, first site) of the whole table
+    int tile_begin, tile_end;   // tiles of this solve
+    int eta_kind;               // Philox stream kind of generated right-hand sides
+    CGState* st;
+    double2* partial;    // one per tile
+    GridBarrier* bar;
+    int* err;
+    int* n_active;
+    int* any_ru;
+    int max_iter;
+    int mtype;           // YK_DAGGER: A = D^dag D;  YK_NORMAL: A = D D^dag
+    int tol_mode;
+    double tol;
+    int reliable_every;
+};
+
+// Per-chain device record of the Langevin step.
+struct ChainDev {
+    int Nt, Nx, V;
+    int n_rhs;
+    int sys0;            // first CG system of the chain
+    int tile0, ntiles;   // site tiles of the chain (force / update kernels)
+    double m2, lambda, g, m0, r, cut, eps_bar, fixed_dt;
+    int drift_mode;
+    int filter;          // 1 if the cutoff removes modes (FFT path), 0 if white
+    uint64_t seed;
+    uint32_t chain_id;
+    double* phi;
+    double* drift;
+    double* xi;
+    double* white;
+    double2* spec;       // Nt*Nx complex work buffer of the noise FFT
+    const uint8_t* keep; // Nt*Nx keep-flags of the momentum cutoff
+    const double2* tw_t; // twiddles exp(-2 pi i k / Nt), k < Nt
+    const double2* tw_x; // twiddles exp(-2 pi i k / Nx), k < Nx
+    int64_t step;        // Philox step counter (advanced by the update kernel)
+    double time;         // accumulated Langevin time
+    yk_obs obs;          // last-step observables
+    unsigned counter;    // finaliser counter of the update kernel
+    unsigned counter2;
+    int status;
+};
+
+struct StepArgs {
+    ChainDev* ch;
+    int nch;
+    const int2* tiles;   // (chain, first site)
+    int ntiles;
+    int tile_base;       // index of tiles[0] in the per-tile arrays
+    double* tile_max;    // per-tile max |drift|
+    double2* tile_sum;   // per-tile partial sums
+    double* tile_sum2;
+};
+
+// Block tables of the coloured-noise passes (built once per context).
+struct NoiseTables {
+    const int2* rows;    // (chain, t) for every chain whose cutoff removes modes
+    int nrows;
+    const int2* cols;    // (chain, first column) strips of width noise_strip(Nt)
+    int ncols;
+    const int2* white;   // (chain, first site) tiles of chains with every mode kept
+    int nwhite;
+};
+
+// Columns per block of the column pass: the strip holds <= kMaxFFT complex.
+YK_HD inline int noise_strip(int Nt)
+{
+    int cw = kMaxFFT / Nt;
+    if (cw > 64) cw = 64;
+    if (cw < 1) cw = 1;
+    return cw;
+}
+
+}  // namespace yk

@@ -1,0 +1,43 @@
+// yk_kernels.h -- host-side launchers of the sm_103a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "yk_internal.h"
+
+namespace yk {
+
+// Wilson-Dirac apply on one lattice (K real planes per entry; K = 2 for
+// interleaved complex buffers).  prec YK_FP64 (double) or YK_FP32 (float).
+cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt, int Nx,
+                         double m0, double g, double r, int dagger, int prec, int K,
+                         cudaStream_t stream);
+
+// Batched CG (yk_cg.cu).  Also launches its one-block preparation kernel.
+cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out);
+// Largest co-resident grid of the CG kernel (cached; call before capturing).
+int cg_max_grid(int K, bool mixed);
+// Raises the shared-memory limit of the FFT kernels (call before capturing).
+void noise_init_attributes();
+
+// Coloured noise of every chain in the tables (yk_noise.cu): xi = filtered
+// Philox white noise at each chain's current step, or the filtered `given`
+// white field (tables of a single chain).
+cudaError_t launch_noise_tables(ChainDev* d_chains, const NoiseTables& tb, int max_nx,
+                                int max_cols_elems, const double* given, cudaStream_t stream);
+
+// Force + drift (+ per-tile max|drift| and sum F), then the Euler update and
+// observables (yk_langevin.cu).  mode 0: drift = F + bosonic drift;
+// mode 1: drift = F (the fermion force alone); mode 2: drift (preset to a
+// given force) += bosonic drift.
+cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K,
+                               cudaStream_t stream);
+cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream);
+
+// Point-source / time-slice helpers.
+cudaError_t launch_time_slices_spinor(const double* psi, double* corr, int Nt, int Nx, int K,
+                                      cudaStream_t stream);
+cudaError_t launch_time_slices(const double* phi, double* out, int Nt, int Nx, cudaStream_t stream);
+
+}  // namespace yk

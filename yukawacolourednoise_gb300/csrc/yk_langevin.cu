@@ -1,0 +1,228 @@
+// yk_langevin.cu -- the parts of a Langevin step after the CG solve.
+//
+// force_drift (mode 0: step, 1: force only, 2: injected force + bosonic drift):
+//   chi_j = D x_j is formed on the fly (never stored) and
+//   contracted with eta_j:  F_n = -g/N sum_j Re sum_c conj(chi_{j,n,c}) eta_{j,n,c}
+//   (FermionicDrift.cu:57-100, N = 1 in the reference); the bosonic drift
+//   phi (m^2 + lambda/6 phi^2) - Lap phi (langevin_gpu_v2.cu:9-27, 41-63,
+//   Laplacian columns in the sorted CSR order of Laplace.cu:61-100) is added
+//   in the same pass, and each tile publishes max|drift| and sum F.
+// update: every block reduces the per-tile maxima of its chain (deterministic),
+//   applies the clamp and the adaptive step eps = epsBar*30/max|drift| (or a
+//   fixed dt) and the Euler update phi -= eps drift + sqrt(2 eps) xi
+//   (langevin_gpu_v2.cu:65-118); the last tile of a chain writes the step's
+//   observables, advances Langevin time and the Philox step counter on the
+//   device, so the host never waits for eps (the reference copies eps to the
+//   host every step, main.cu:378-381).
+#include "yk_common.cuh"
+#include "yk_kernels.h"
+
+namespace yk {
+
+__device__ __forceinline__ void cswap(int& a, int& b)
+{
+    const int lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const SysDev* __restrict__ sys,
+                                                            int mode)
+{
+    __shared__ double red[64];
+    const int2 ct = s.tiles[blockIdx.x];
+    ChainDev& C = s.ch[ct.x];
+    const int n = ct.y + threadIdx.x;
+    double F = 0.0, d = 0.0;
+    bool bad = false;
+    if (n < C.V) {
+        const Nbr nb = neighbours(n, C.Nt, C.Nx);
+        if (mode == 2) {
+            F = C.drift[n];   // injected force
+        } else if (C.g != 0.0 && C.n_rhs > 0) {
+            const double scale = (C.drift_mode == 1) ? C.cut * C.cut : 1.0;
+            const double diag = 2.0 * C.r + C.m0 + C.g * C.phi[n];
+            for (int j = 0; j < C.n_rhs; ++j) {
+                const SysDev& S = sys[C.sys0 + j];
+                const Site<double, K> c = load_site<double, K>(S.x, n);
+                const Site<double, K> tu = load_site<double, K>(S.x, nb.tu);
+                const Site<double, K> td = load_site<double, K>(S.x, nb.td);
+                const Site<double, K> xu = load_site<double, K>(S.x, nb.xu);
+                const Site<double, K> xd = load_site<double, K>(S.x, nb.xd);
+                const Site<double, K> chi =
+                    dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, C.r, (double)nb.sp, (double)nb.sm);
+                const Site<double, K> e = load_site<double, K>(S.b, n);
+                double sj = 0.0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    double pq = chi.v[q * K] * e.v[q * K];
+                    if constexpr (K == 2) pq += chi.v[q * K + 1] * e.v[q * K + 1];
+                    sj = (q == 0) ? pq : sj + pq;
+                }
+                F += -(scale * C.g) * sj;
+            }
+            if (C.n_rhs > 1) F /= (double)C.n_rhs;
+        }
+        if (mode != 1) {
+            const double v = C.phi[n];
+            d = F;
+            d += v * (C.m2 + (C.lambda / 6.0) * (v * v));
+            int col[5] = {n, (int)nb.tu, (int)nb.td, (int)nb.xu, (int)nb.xd};
+            // 5-input sorting network (9 comparators)
+            cswap(col[0], col[1]); cswap(col[3], col[4]); cswap(col[2], col[4]);
+            cswap(col[2], col[3]); cswap(col[0], col[3]); cswap(col[0], col[2]);
+            cswap(col[1], col[4]); cswap(col[1], col[3]); cswap(col[1], col[2]);
+            double lap = 0.0;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) lap += (col[q] != n ? 1.0 : -4.0) * C.phi[col[q]];
+            d -= lap;
+            C.drift[n] = d;
+        } else {
+            d = F;
+            C.drift[n] = F;
+        }
+        bad = !isfinite(d);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(&C.status, 0, (int)YK_ENAN);
+    const double m = block_max(fabs(d), red);
+    const double2 sf = block_sum2(F, 0.0, red);
+    if (threadIdx.x == 0) {
+        s.tile_max[s.tile_base + blockIdx.x] = m;
+        s.tile_sum2[s.tile_base + blockIdx.x] = sf.x;
+    }
+}
+
+__global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState* __restrict__ st)
+{
+    __shared__ double red[64];
+    __shared__ double s_eps, s_max;
+    __shared__ int s_last;
+    const int2 ct = s.tiles[blockIdx.x];
+    ChainDev& C = s.ch[ct.x];
+    double m = 0.0;
+    for (int i = threadIdx.x; i < C.ntiles; i += blockDim.x) m = fmax(m, s.tile_max[C.tile0 + i]);
+    m = block_max(m, red);
+    if (threadIdx.x == 0) {
+        if (m > 1e5) m = 1e5;               // langevin_gpu_v2.cu:83-91
+        else if (m < 1e-5) m = 1e-5;
+        s_max = m;
+        s_eps = (C.fixed_dt > 0.0) ? C.fixed_dt : C.eps_bar * 30.0 / m;
+    }
+    __syncthreads();
+    const double eps = s_eps;
+    const double fact = sqrt(2.0 * eps);
+    const int n = ct.y + threadIdx.x;
+    double p1 = 0.0, p2 = 0.0;
+    if (n < C.V) {
+        double v = C.phi[n];
+        v -= eps * C.drift[n] + fact * C.xi[n];
+        C.phi[n] = v;
+        p1 = v;
+        p2 = v * v;
+    }
+    const double2 ps = block_sum2(p1, p2, red);
+    if (threadIdx.x == 0) {
+        s.tile_sum[s.tile_base + blockIdx.x] = ps;
+        __threadfence();
+        const unsigned prev = atomicAdd(&C.counter, 1u);
+        s_last = (prev == (unsigned)C.ntiles - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x < 32) {
+        __threadfence();
+        const int lane = threadIdx.x;
+        double a = 0.0, b = 0.0, f = 0.0;
+        for (int i = lane; i < C.ntiles; i += 32) {
+            const double2 q = __ldcg(s.tile_sum + C.tile0 + i);
+            a += q.x;
+            b += q.y;
+            f += __ldcg(s.tile_sum2 + C.tile0 + i);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        f = warp_sum(f);
+        if (lane == 0) {
+            int iters = 0, status = *(volatile int*)&C.status;
+            if (C.g != 0.0)
+                for (int j = 0; j < C.n_rhs; ++j) {
+                    iters += st[C.sys0 + j].iters;
+                    if (status == 0 && st[C.sys0 + j].status) status = st[C.sys0 + j].status;
+                }
+            C.time += eps;
+            C.obs.t = C.time;
+            C.obs.eps = eps;
+            C.obs.max_drift = s_max;
+            C.obs.sum_phi = a;
+            C.obs.sum_phi2 = b;
+            C.obs.sum_force = f;
+            C.obs.steps += 1;
+            C.obs.cg_iterations = iters;
+            C.obs.status = status;
+            C.step += 1;
+            C.counter = 0;
+            C.status = 0;
+        }
+    }
+}
+
+cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K, cudaStream_t stream)
+{
+    if (K == 1)
+        force_drift_kernel<1><<<s.ntiles, kTile, 0, stream>>>(s, sys, mode);
+    else
+        force_drift_kernel<2><<<s.ntiles, kTile, 0, stream>>>(s, sys, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream)
+{
+    update_kernel<<<s.ntiles, kTile, 0, stream>>>(s, st);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Observables used by the export block of main.cu:385-483.
+// ---------------------------------------------------------------------------
+__global__ void time_slices_kernel(const double* __restrict__ phi, double* out, int Nx)
+{
+    __shared__ double red[64];
+    const int t = blockIdx.x;
+    double a = 0.0;
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) a += phi[(int64_t)t * Nx + x];
+    const double2 r = block_sum2(a, 0.0, red);
+    if (threadIdx.x == 0) out[t] = r.x;
+}
+
+template <int K>
+__global__ void time_slices_spinor_kernel(const double* __restrict__ psi, double* out, int Nx)
+{
+    __shared__ double red[64];
+    const int t = blockIdx.x;
+    double a = 0.0;
+    for (int x = threadIdx.x; x < Nx; x += blockDim.x) {
+        const double* p = psi + ((int64_t)t * Nx + x) * 4 * K;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) a += p[c * K];
+    }
+    const double2 r = block_sum2(a, 0.0, red);
+    if (threadIdx.x == 0) out[t] = r.x;
+}
+
+cudaError_t launch_time_slices(const double* phi, double* out, int Nt, int Nx, cudaStream_t stream)
+{
+    time_slices_kernel<<<Nt, kBlock, 0, stream>>>(phi, out, Nx);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_time_slices_spinor(const double* psi, double* corr, int Nt, int Nx, int K,
+                                      cudaStream_t stream)
+{
+    if (K == 1)
+        time_slices_spinor_kernel<1><<<Nt, kBlock, 0, stream>>>(psi, corr, Nx);
+    else
+        time_slices_spinor_kernel<2><<<Nt, kBlock, 0, stream>>>(psi, corr, Nx);
+    return cudaGetLastError();
+}
+
+}  // namespace yk
