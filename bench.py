@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Langevin steps/sec of the 2-D Yukawa hot path on GB300 (one JSON line).
+
+Workload (the precision configuration of the headline metric): a 256 x 256
+lattice, m^2 = -0.5, lambda = 1, Yukawa g = 0.5, m0 = 0.1, Wilson r = 1,
+coloured-noise cutoff Lambda = pi/2 (cutFraction = 1/(2 sqrt 2)), fixed Euler
+step dt = 0.01, one Gaussian stochastic right-hand side per step, CG on
+D^dag D to relative residual 1e-10 with FP32 iterations and an FP64 reliable
+update every 50 iterations, FP64 field.  Synthetic data: the field starts
+iid Uniform[-1, 1] from seed 1234 and all noise is drawn from Philox.
+
+One step = coloured noise + fermion force (CG) + drift/Euler update +
+per-step observables, replayed as one CUDA graph.  L2 (129 MB) is flushed by a
+256 MiB write between timed steps, outside the timed events.
+
+  --impl ours (default): the CUDA path; `value` = steps/s of all ranks.
+  --impl reference: the CPU oracle (C restatement of the reference's
+      algorithm; the reference itself has no CPU path) on the host cores.
+
+Multi-GPU: chains are independent, so N GPUs run N replicas (weak scaling,
+no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Langevin steps/sec @CG rel-res 1e-10, learned+mixed vs plain FP64 CG; Dirac HBM GB/s"
+NT = NX = 256
+CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (sqrt(2) pi)
+BYTES_CG_ITER_MIXED = 224          # unique bytes per site per FP32 CG iteration
+BYTES_CG_ITER_FP64 = 448
+
+
+def workload(precision: str) -> dict:
+    return {"workload": f"2D {NT}x{NX} Yukawa Langevin step (coloured noise + CG force + Euler), "
+                        f"CG rel-res 1e-10, {precision} CG, 1 RHS, fixed dt 0.01",
+            "lattice": [NT, NX], "n_rhs": 1, "precision": precision, "cg_tol_rel": 1e-10,
+            "reliable_every": 50, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
+            "l2": "flushed between timed steps (256 MiB write)"}
+
+
+def make_params(yk, precision, seed=1234, Nt=NT, Nx=NX):
+    return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=0.1,
+                             wilson_param=1.0, cut_fraction=CUT, Nt=Nt, Nx=Nx, fixed_dt=0.01,
+                             precision=yk.YK_MIXED if precision == "mixed" else yk.YK_FP64,
+                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=50,
+                             n_rhs=1, seed=seed, init=yk.YK_INIT_PHILOX)
+
+
+# ---------------------------------------------------------------- distributed
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic():
+    """DRAM bytes per CG launch from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "cg_kernel_256x256_traffic.json"
+    if f.exists():
+        try:
+            return json.loads(f.read_text())
+        except Exception:
+            return None
+    return None
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, ws, rank, local):
+    import torch
+    import yukawacolourednoise_gb300 as yk
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed_steps(ctx, k):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        with torch.cuda.stream(stream):
+            for i in range(k):
+                starts[i].record(stream)
+                ctx.step(1)
+                ends[i].record(stream)
+                flush.fill_(i & 0xFF)
+        stream.synchronize()
+        return sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / 1e3
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    ctx = yk.Context(make_params(yk, args.precision, seed=1234 + rank))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.step(args.warmup)
+    ctx.synchronize()
+
+    barrier()
+    clocks = Clocks(local)
+    t_sec = timed_steps(ctx, args.steps)
+    barrier()
+    clk = clocks.stop()
+    obs = ctx.observables()
+    if obs.status not in (0,):
+        raise RuntimeError(f"step status {obs.status}")
+    t_all = t_sec
+    if dist is not None:
+        t = torch.tensor([t_sec], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_all = float(t.item())
+    value = args.steps * ws / t_all
+
+    extras = {}
+    if rank == 0 and not args.quick:
+        # kernel timing of the same workload: CUDA events around each kernel class
+        ctx.profile_begin()
+        with torch.cuda.stream(stream):
+            ctx.step(args.profile_steps)
+        pr = ctx.profile_end()
+        per_launch_ms = pr.cg_ms / max(pr.cg_launches, 1)
+        bpi = BYTES_CG_ITER_MIXED if args.precision == "mixed" else BYTES_CG_ITER_FP64
+        alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
+        pk = peaks()
+        achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+        tr = ncu_traffic()
+        traffic = None
+        if tr and tr.get("precision") == args.precision:
+            traffic = tr["dram_bytes_per_iteration"] * pr.cg_iterations / max(pr.cg_launches, 1)
+        extras["roofline"] = {"bound": "hbm", "kernel": f"cg_kernel<1,{'mixed' if args.precision == 'mixed' else 'fp64'}>",
+                              "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                              "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+                              "peak_source": pk["source"],
+                              "bytes_per_site_iteration": bpi,
+                              "cg_iterations_per_step": pr.cg_iterations / max(pr.steps, 1),
+                              "ms_per_launch": round(per_launch_ms, 4)}
+        tot = pr.noise_ms + pr.cg_ms + pr.force_ms + pr.update_ms
+        extras["kernel_share"] = {k: round(v / tot, 4) for k, v in
+                                  (("noise", pr.noise_ms), ("cg", pr.cg_ms), ("force_drift", pr.force_ms),
+                                   ("update", pr.update_ms))}
+        launches_per_step = pr.launches / max(pr.steps, 1)
+
+        # end to end through the C ABI with host buffers (pinned), every step:
+        # H2D of the field, one step, D2H of the field and the observables
+        import numpy as np
+        V = NT * NX
+        host_in = torch.empty(V, dtype=torch.float64).pin_memory()
+        host_out = torch.empty(V, dtype=torch.float64).pin_memory()
+        host_in.copy_(torch.from_numpy(ctx.get_field()))
+        lib = yk.lib()
+        import ctypes as C
+        o = yk.Obs()
+        ke = args.e2e_steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            yk._check(lib.yk_set_field_host(ctx.h, 0, C.c_void_p(host_in.data_ptr())))
+            yk._check(lib.yk_langevin_step(ctx.h, 1))
+            yk._check(lib.yk_get_field_host(ctx.h, 0, C.c_void_p(host_out.data_ptr())))
+            yk._check(lib.yk_observables(ctx.h, 0, C.byref(o)))
+            host_in, host_out = host_out, host_in
+        e2e_sec = time.perf_counter() - t0
+        extras["e2e"] = {"value": round(ke / e2e_sec, 2), "unit": "steps/s", "h2d_bytes_per_step": 8 * V,
+                         "d2h_bytes_per_step": 8 * V + C.sizeof(yk.Obs)}
+
+        # plain FP64 CG form of the same workload (the metric's denominator)
+        if args.precision == "mixed":
+            ctx64 = yk.Context(make_params(yk, "fp64"))
+            ctx64.set_stream(stream.cuda_stream)
+            ctx64.step(args.warmup)
+            ctx64.synchronize()
+            t64 = timed_steps(ctx64, args.fp64_steps)
+            extras["plain_fp64"] = {"value": round(args.fp64_steps / t64, 2), "unit": "steps/s",
+                                    "speedup_mixed_over_fp64": round(value / ws / (args.fp64_steps / t64), 3)}
+            ctx64.close()
+
+        # Dirac apply HBM bandwidth on a lattice larger than L2 (complex buffers)
+        extras["dirac_hbm"] = dirac_hbm(yk, torch, stream)
+        extras["gpu_launches"] = int(round(launches_per_step * args.steps))
+
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return None
+    line = {"metric": METRIC, "value": round(value, 2), "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_all / args.steps * 1e3, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
+            "config": workload(args.precision), "clocks": clk}
+    line.update(extras)
+    if "gpu_launches" not in line:
+        line["gpu_launches"] = 7 * args.steps
+    if not args.no_cpu and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    return line
+
+
+def dirac_hbm(yk, torch, stream, Nt=4096, Nx=4096, reps=20):
+    out = {}
+    pk = peaks()["hbm_gbs"]
+    p = make_params(yk, "fp64", Nt=Nt, Nx=Nx).copy(cut_fraction=1.0, yukawa_coupling=0.0)
+    ctx = yk.Context(p)
+    ctx.set_stream(stream.cuda_stream)
+    V = Nt * Nx
+    for prec, dt, bps in (("fp64", torch.complex128, 136), ("fp32", torch.complex64, 72)):
+        x = torch.randn(V, 4, dtype=dt, device="cuda")
+        y = torch.empty_like(x)
+        code = yk.YK_FP64 if prec == "fp64" else yk.YK_FP32
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                ctx.dirac_apply(x, y, False, code)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                ctx.dirac_apply(x, y, False, code)
+            b.record(stream)
+        stream.synchronize()
+        ms = a.elapsed_time(b) / reps
+        gbs = V * bps / (ms * 1e-3) / 1e9
+        out[prec] = {"lattice": [Nt, Nx], "bytes_per_site": bps, "ms": round(ms, 4), "GB/s": round(gbs, 1),
+                     "frac": round(gbs / pk, 4)}
+        del x, y
+    ctx.close()
+    return out
+
+
+# ---------------------------------------------------------------- CPU arms
+def cpu_steps(seconds_budget: float, max_steps: int):
+    """Times full 256x256 Langevin steps of the CPU oracle (all host threads)."""
+    from oracle import oracle as O
+    a = O.action(m2=-0.5, lam=1.0, g=0.5, m0=0.1, r=1.0, cut_fraction=CUT)
+    phi = O.uniform_field(1234, 0, NT * NX)
+    t0 = time.perf_counter()
+    phi, _ = O.langevin_step(NT, NX, a, phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    first = time.perf_counter() - t0
+    n = max(1, min(max_steps, int(seconds_budget / max(first, 1e-6))))
+    t0 = time.perf_counter()
+    for s in range(n):
+        phi, _ = O.langevin_step(NT, NX, a, phi, 1234, 0, s + 1, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    dt = time.perf_counter() - t0
+    return n, dt, O.threads()
+
+
+def cpu_baseline(seconds: float) -> dict:
+    n, dt, threads = cpu_steps(seconds, 10_000)
+    return {"value": round(n / dt, 4), "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} full {NT}x{NX} Langevin steps (FP64 CG rel-res 1e-10, OpenMP over sites)"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    budget = float(os.environ.get("YK_REF_SECONDS", "120"))
+    per = budget / max(args.steps + args.warmup, 1)
+    # warm-up: one step each (bounded)
+    cpu_steps(per, max(1, min(args.warmup, 3)))
+    n, dt, threads = cpu_steps(max(budget * args.steps / (args.steps + args.warmup), per), args.steps)
+    v = n / dt
+    return {"metric": METRIC, "value": round(v, 4), "unit": "steps/s", "n_gpus": ws, "steps": n,
+            "warmup": args.warmup, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
+            "config": workload("fp64"),
+            "cpu_baseline": {"value": round(v, 4), "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{n} of {args.steps} requested {NT}x{NX} Langevin steps "
+                                       f"(CPU restatement of the reference; the reference has no CPU path)"},
+            "e2e": {"value": round(v, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--profile-steps", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=300)
+    ap.add_argument("--fp64-steps", type=int, default=500)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="timed region only")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    ws, rank, local = dist_env()
+    line = run_reference(args, ws, rank) if args.impl == "reference" else run_ours(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -110,6 +110,7 @@ typedef struct yk_obs {
     double sum_force;          /* sum_n F_n of the step's fermion force          */
     int64_t steps;             /* steps taken by this chain                       */
     int cg_iterations;         /* CG iterations of the last step                  */
+    int64_t cg_iterations_total; /* CG iterations of all steps of this chain       */
     int status;                /* yk_status of the last step                      */
 } yk_obs;
 
@@ -182,6 +183,22 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps);
  * sqrt(2 eps) xi.  force, xi: V doubles (device).  Advances the chain's step
  * counter and Langevin time like yk_langevin_step; obs may be NULL. */
 int yk_euler_update(yk_ctx* ctx, int chain, const double* force, const double* xi, yk_obs* obs);
+
+/* Kernel timing of yk_langevin_step: between begin and end the step runs as
+ * direct launches bracketed by CUDA events on the context's stream (instead
+ * of the captured graph); end sums the device time per kernel class. */
+typedef struct yk_profile {
+    int steps;                   /* Langevin steps profiled                       */
+    int launches;                /* kernels launched by those steps               */
+    int cg_launches;             /* persistent CG launches                        */
+    int cg_grid;                 /* blocks of the last CG launch                  */
+    double noise_ms, cg_ms, force_ms, update_ms;   /* summed device time          */
+    int64_t cg_iterations;       /* CG iterations, summed over systems            */
+    int64_t cg_site_iterations;  /* sum over chains of iterations x volume        */
+    int64_t sites;               /* sum of the chains' volumes                    */
+} yk_profile;
+int yk_profile_begin(yk_ctx* ctx);
+int yk_profile_end(yk_ctx* ctx, yk_profile* out);
 
 /* Host copy of a chain's last-step observables (synchronises the stream). */
 int yk_observables(yk_ctx* ctx, int chain, yk_obs* obs);

@@ -3,12 +3,16 @@
 The reference fixes the lattice at compile time (code/src/params.h:28, patched
 by runs.py:80-85 with sed before each build).  For each golden lattice size
 this recipe copies code/src into a temporary directory OUTSIDE the repository,
-patches the Sizes line the same way, compiles the kernel translation units
-with nvcc for sm_103a (-rdc, --expt-relaxed-constexpr, -DUSE_cuFFT: the flags
-of code/Makefile), adds consts.cu (the __constant__ symbols that main.cu
-defines; main.cu itself needs the absent toml11 header) and device-links them
-into oracle/_ref/ref_<Nt>x<Nx>.fatbin.  The mangled kernel names are read from
-the host objects with `nm` into oracle/_ref/symbols_<Nt>x<Nx>.txt.  Nothing of
+patches the Sizes line the same way, and compiles the kernel sources with
+nvcc for sm_103a (--expt-relaxed-constexpr, -DUSE_cuFFT: the flags of
+code/Makefile) as one translation unit that #includes them, preceded by
+consts.cu (the __constant__ symbols that main.cu defines; main.cu itself needs
+the absent toml11 header), into oracle/_ref/ref_<Nt>x<Nx>.fatbin.  In that
+single unit the sources' `extern __constant__` re-declarations are dropped
+from the copies (consts.cu defines the symbols; a non-relocatable unit cannot
+hold both), which is the only other edit besides the Sizes line.  The mangled
+kernel names are read from the host object of the same unit with `nm` into
+oracle/_ref/symbols_<Nt>x<Nx>.txt.  Nothing of
 the reference is written into the repository; only compiled device code
 lands in oracle/_ref/ (git-ignored).
 
@@ -17,7 +21,6 @@ prebuilt fatbins through oracle/ref/ref_harness.cpp.
 """
 from __future__ import annotations
 
-import concurrent.futures as cf
 import shutil
 import subprocess
 import tempfile
@@ -30,7 +33,7 @@ SIZES = [(8, 4), (6, 10), (16, 16)]
 TUS = ["Dirac.cu", "CGsolver.cu", "FermionicDrift.cu", "reductions.cu", "langevin_gpu_v2.cu", "Lattice.cu"]
 KERNELS = ["applyD_gpu", "solve_kernel", "computeDrift", "Run", "gpuMagnetisation", "gpuTimeSlices",
            "gpuTimeSlices_spinors", "gpuTraces", "ApplyMask"]
-FLAGS = ["-arch=sm_103a", "--expt-relaxed-constexpr", "-rdc=true", "-DUSE_cuFFT", "-O3", "-w"]
+FLAGS = ["-arch=sm_103a", "--expt-relaxed-constexpr", "-DUSE_cuFFT", "-O3", "-w"]
 
 
 def _nvcc():
@@ -61,24 +64,21 @@ def build_size(Nt: int, Nx: int) -> Path:
             "__constant__ thrust::complex<double> im_gpu;\n__constant__ double cutFraction_gpu;\n"
             "__constant__ double sq2Kappa_gpu;\n__constant__ DriftMode driftMode_gpu;\n"
             "__constant__ double WilsonParam_gpu;\n")
-        jobs = [(src / t, Path(td) / (Path(t).stem + ".o"), []) for t in TUS + ["consts.cu"]]
-        jobs.append((src / "colouredNoise.cpp", Path(td) / "colouredNoise.o", ["-x", "cu"]))
-
-        def comp(job):
-            s, o, extra = job
-            r = subprocess.run([_nvcc()] + FLAGS + extra + ["-I", str(src), "-c", str(s), "-o", str(o)],
-                               capture_output=True, text=True)
-            if r.returncode:
-                raise RuntimeError(f"{s.name}: {r.stderr}")
-            return o
-
-        with cf.ThreadPoolExecutor(8) as ex:
-            objs = list(ex.map(comp, jobs))
+        for f in src.iterdir():
+            if f.suffix in (".cu", ".cpp") and f.name != "consts.cu":
+                lines = f.read_text().splitlines(keepends=True)
+                f.chmod(0o644)
+                f.write_text("".join(l for l in lines if not l.lstrip().startswith("extern __constant__")))
+        unity = src / "unity.cu"
+        unity.write_text("".join(f'#include "{t}"\n' for t in ["consts.cu"] + TUS + ["colouredNoise.cpp"]))
         OUT.mkdir(exist_ok=True)
-        r = subprocess.run([_nvcc(), "-arch=sm_103a", "-dlink", "-fatbin"] + [str(o) for o in objs] +
-                           ["-o", str(fat)], capture_output=True, text=True)
-        if r.returncode:
-            raise RuntimeError(r.stderr)
+        obj = Path(td) / "unity.o"
+        for extra in (["-fatbin", "-o", str(fat)], ["-c", "-o", str(obj)]):
+            r = subprocess.run([_nvcc()] + FLAGS + ["-I", str(src), str(unity)] + extra, capture_output=True,
+                               text=True)
+            if r.returncode:
+                raise RuntimeError(r.stderr)
+        objs = [obj]
         names = subprocess.run(["nm", "--defined-only"] + [str(o) for o in objs], capture_output=True,
                                text=True).stdout.split()
         lines = []

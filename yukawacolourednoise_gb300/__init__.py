@@ -101,7 +101,14 @@ class SolveStats(C.Structure):
 class Obs(C.Structure):
     _fields_ = [("t", C.c_double), ("eps", C.c_double), ("max_drift", C.c_double), ("sum_phi", C.c_double),
                 ("sum_phi2", C.c_double), ("sum_force", C.c_double), ("steps", C.c_int64),
-                ("cg_iterations", C.c_int), ("status", C.c_int)]
+                ("cg_iterations", C.c_int), ("cg_iterations_total", C.c_int64), ("status", C.c_int)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("steps", C.c_int), ("launches", C.c_int), ("cg_launches", C.c_int), ("cg_grid", C.c_int),
+                ("noise_ms", C.c_double), ("cg_ms", C.c_double), ("force_ms", C.c_double),
+                ("update_ms", C.c_double), ("cg_iterations", C.c_int64), ("cg_site_iterations", C.c_int64),
+                ("sites", C.c_int64)]
 
 
 _lib = None
@@ -131,6 +138,8 @@ _SIGS = {
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
     "yk_euler_update": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(Obs)]),
     "yk_observables": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Obs)]),
+    "yk_profile_begin": (C.c_int, [C.c_void_p]),
+    "yk_profile_end": (C.c_int, [C.c_void_p, C.POINTER(Profile)]),
     "yk_time_slices": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "yk_correlator": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_condensate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(SolveStats)]),
@@ -269,6 +278,14 @@ class Context:
         o = Obs()
         _check(lib().yk_euler_update(self.h, chain, _ptr(force), _ptr(xi), C.byref(o)))
         return o
+
+    def profile_begin(self):
+        _check(lib().yk_profile_begin(self.h))
+
+    def profile_end(self) -> Profile:
+        pr = Profile()
+        _check(lib().yk_profile_end(self.h, C.byref(pr)))
+        return pr
 
     def observables(self, chain=0) -> Obs:
         o = Obs()

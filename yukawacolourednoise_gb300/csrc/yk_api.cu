@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -116,6 +117,16 @@ struct yk_ctx {
     cudaGraphExec_t gexec = nullptr;
     bool graph_failed = false;
     int cg_grid = 0;
+    // profiling: CUDA events around each kernel class of the step
+    bool profiling = false;
+    struct Rec {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    int prof_steps = 0, prof_launches = 0;
+    std::vector<int64_t> prof_iters0;
 };
 
 namespace {
@@ -207,12 +218,45 @@ StepArgs step_args(yk_ctx* ctx)
     return s;
 }
 
+cudaEvent_t take_event(yk_ctx* ctx)
+{
+    if (!ctx->pool.empty()) {
+        cudaEvent_t e = ctx->pool.back();
+        ctx->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Events around one kernel class when profiling (no-ops otherwise).
+void prof_begin(yk_ctx* ctx, cudaEvent_t* a)
+{
+    if (!ctx->profiling) return;
+    *a = take_event(ctx);
+    cudaEventRecord(*a, ctx->stream);
+}
+
+void prof_end(yk_ctx* ctx, int cls, cudaEvent_t a, int launches)
+{
+    if (!ctx->profiling) return;
+    cudaEvent_t b = take_event(ctx);
+    cudaEventRecord(b, ctx->stream);
+    ctx->recs.push_back({cls, a, b});
+    ctx->prof_launches += launches;
+}
+
 // Enqueues one Langevin step of every chain.
 int enqueue_step(yk_ctx* ctx)
 {
+    cudaEvent_t e = nullptr;
+    prof_begin(ctx, &e);
     NoiseTables nt = {ctx->d_rows, ctx->nrows, ctx->d_cols, ctx->ncols, ctx->d_white, ctx->nwhite};
     YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
+    prof_end(ctx, 0, e, (ctx->nwhite > 0 ? 1 : 0) + (ctx->nrows > 0 ? 3 : 0));
     if (ctx->nsys > 0) {
+        prof_begin(ctx, &e);
         CGArgs a = base_args(ctx);
         a.sys = ctx->d_sys;
         a.sys_first = 0;
@@ -224,10 +268,16 @@ int enqueue_step(yk_ctx* ctx)
         a.st = ctx->d_state;
         a.partial = ctx->d_partial;
         YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
+        prof_end(ctx, 1, e, 2);
     }
     StepArgs s = step_args(ctx);
+    prof_begin(ctx, &e);
     YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream));
+    prof_end(ctx, 2, e, 1);
+    prof_begin(ctx, &e);
     YK_CK(launch_update(s, ctx->d_state, ctx->stream));
+    prof_end(ctx, 3, e, 1);
+    if (ctx->profiling) ctx->prof_steps += 1;
     return YK_OK;
 }
 
@@ -727,6 +777,11 @@ int yk_ctx_destroy(yk_ctx* ctx)
     if (!ctx) return YK_OK;
     cudaStreamSynchronize(ctx->stream);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (auto& r : ctx->recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : ctx->pool) cudaEventDestroy(e);
     for (auto& C : ctx->ch)
         if (C.ws.mem) cudaFree(C.ws.mem);
     if (ctx->mem) cudaFree(ctx->mem);
@@ -905,7 +960,7 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
         }
     }
     for (int i = 0; i < n_steps; ++i) {
-        if (ctx->gexec) {
+        if (ctx->gexec && !ctx->profiling) {
             YK_CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
         } else {
             if (int rc = enqueue_step(ctx)) return rc;
@@ -928,6 +983,57 @@ int yk_euler_update(yk_ctx* ctx, int c, const double* force, const double* xi, y
     YK_CK(launch_force_drift(s, ctx->d_sys, 2, 1, ctx->stream));
     YK_CK(launch_update(s, ctx->d_state, ctx->stream));
     if (obs) return yk_observables(ctx, c, obs);
+    return YK_OK;
+}
+
+int yk_profile_begin(yk_ctx* ctx)
+{
+    if (!ctx) return YK_EINVAL;
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->profiling = true;
+    ctx->recs.clear();
+    ctx->prof_steps = 0;
+    ctx->prof_launches = 0;
+    ctx->prof_iters0.assign(ctx->ch.size(), 0);
+    for (size_t c = 0; c < ctx->ch.size(); ++c) {
+        yk_obs o;
+        if (int rc = yk_observables(ctx, (int)c, &o)) return rc;
+        ctx->prof_iters0[c] = o.cg_iterations_total;
+    }
+    return YK_OK;
+}
+
+int yk_profile_end(yk_ctx* ctx, yk_profile* out)
+{
+    if (!ctx || !out) return YK_EINVAL;
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    std::memset(out, 0, sizeof(*out));
+    for (auto& r : ctx->recs) {
+        float ms = 0.f;
+        YK_CK(cudaEventElapsedTime(&ms, r.a, r.b));
+        if (r.cls == 0) out->noise_ms += ms;
+        if (r.cls == 1) {
+            out->cg_ms += ms;
+            out->cg_launches += 1;
+        }
+        if (r.cls == 2) out->force_ms += ms;
+        if (r.cls == 3) out->update_ms += ms;
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->recs.clear();
+    out->steps = ctx->prof_steps;
+    out->launches = ctx->prof_launches;
+    for (size_t c = 0; c < ctx->ch.size(); ++c) {
+        yk_obs o;
+        if (int rc = yk_observables(ctx, (int)c, &o)) return rc;
+        const int64_t it = o.cg_iterations_total - ctx->prof_iters0[c];
+        out->cg_iterations += it;
+        out->cg_site_iterations += it * (int64_t)ctx->ch[c].V;
+        out->sites += (int64_t)ctx->ch[c].V;
+    }
+    out->cg_grid = ctx->cg_grid;
+    ctx->profiling = false;
     return YK_OK;
 }
 

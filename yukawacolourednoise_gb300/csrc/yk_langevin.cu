@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
             C.obs.sum_force = f;
             C.obs.steps += 1;
             C.obs.cg_iterations = iters;
+            C.obs.cg_iterations_total += iters;
             C.obs.status = status;
             C.step += 1;
             C.counter = 0;
