@@ -39,7 +39,7 @@ METRIC = "Langevin steps/sec @CG rel-res 1e-10, learned+mixed vs plain FP64 CG; 
 NT = NX = 256
 CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (sqrt(2) pi)
 BYTES_CG_ITER_MIXED = 224          # unique bytes per site per FP32 CG iteration
-BYTES_CG_ITER_FP64 = 448
+BYTES_CG_ITER_FP64 = 432
 
 
 def workload(precision: str) -> dict:
@@ -160,8 +160,10 @@ def run_ours(args, ws, rank, local):
     barrier()
     clk = clocks.stop()
     obs = ctx.observables()
-    if obs.status not in (0,):
+    if obs.status not in (0, yk.YK_ENOCONV):
         raise RuntimeError(f"step status {obs.status}")
+    cg_stats = {"iterations_per_step": round(obs.cg_iterations_total / max(obs.steps, 1), 1),
+                "steps_at_iteration_cap": int(obs.noconv_steps), "iteration_cap": 20000}
     t_all = t_sec
     if dist is not None:
         t = torch.tensor([t_sec], device="cuda")
@@ -245,7 +247,7 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": round(t_all / args.steps * 1e3, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
             "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
-            "config": workload(args.precision), "clocks": clk}
+            "config": workload(args.precision), "clocks": clk, "cg": cg_stats}
     line.update(extras)
     if "gpu_launches" not in line:
         line["gpu_launches"] = 7 * args.steps

@@ -111,6 +111,7 @@ typedef struct yk_obs {
     int64_t steps;             /* steps taken by this chain                       */
     int cg_iterations;         /* CG iterations of the last step                  */
     int64_t cg_iterations_total; /* CG iterations of all steps of this chain       */
+    int64_t noconv_steps;      /* steps whose CG hit its iteration cap            */
     int status;                /* yk_status of the last step                      */
 } yk_obs;
 

@@ -227,6 +227,23 @@ static void cg_solve(CUdeviceptr in, CUdeviceptr out, int mtype, CUdeviceptr M, 
                 a8 = M, a9 = T.iup, a10 = T.idn, a12 = B.dot, a13 = B.rmodsq;
     int mt = mtype;
     void* args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10, &mt, &a12, &a13};
+    // One block of one warp.  With the occupancy-sized grid of CGsolver.cu:44-58
+    // the kernel races: thread 0 of block 0 negates *alpha (CGsolver.cu:146)
+    // with no grid sync after the x update that reads *alpha (:143), so other
+    // blocks can apply -alpha to x.  In a single warp every lane reads *alpha
+    // before lane 0 negates it; the kernel's arithmetic is unchanged.
+    CK(cuLaunchCooperativeKernel(fns.at("solve_kernel"), 1, 1, 1, 32, 1, 1, 16, nullptr, args));
+    CK(cuCtxSynchronize());
+}
+
+// The same solve with the reference's own occupancy-sized launch (racy x).
+static void cg_solve_occupancy(CUdeviceptr in, CUdeviceptr out, int mtype, CUdeviceptr M, const Tables& T,
+                               CGBufs& B)
+{
+    CUdeviceptr a0 = in, a1 = out, a2 = B.temp, a3 = B.temp2, a4 = B.r, a5 = B.p, a6 = B.alpha, a7 = B.beta,
+                a8 = M, a9 = T.iup, a10 = T.idn, a12 = B.dot, a13 = B.rmodsq;
+    int mt = mtype;
+    void* args[] = {&a0, &a1, &a2, &a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10, &mt, &a12, &a13};
     coop("solve_kernel", args, 16);   // smem = sizeof(complex<double>) * (threads / 32)
 }
 
@@ -379,6 +396,10 @@ int main(int argc, char** argv)
     cg_solve(psi, out, 0, M, T, B);
     put("cg_x_nor", d2h(out, 8 * V));
     put("cg_rr_nor", d2h(B.rmodsq, 1));
+    // record of the race: the reference's own launch geometry
+    cg_solve_occupancy(psi, out, 1, M, T, B);
+    put("cg_x_dag_occupancy", d2h(out, 8 * V));
+    put("cg_rr_dag_occupancy", d2h(B.rmodsq, 1));
 
     // ---- fermion force with injected real eta, normal and rescaled drift mode
     std::vector<double> eta(8 * V, 0.0);

@@ -101,7 +101,8 @@ class SolveStats(C.Structure):
 class Obs(C.Structure):
     _fields_ = [("t", C.c_double), ("eps", C.c_double), ("max_drift", C.c_double), ("sum_phi", C.c_double),
                 ("sum_phi2", C.c_double), ("sum_force", C.c_double), ("steps", C.c_int64),
-                ("cg_iterations", C.c_int), ("cg_iterations_total", C.c_int64), ("status", C.c_int)]
+                ("cg_iterations", C.c_int), ("cg_iterations_total", C.c_int64), ("noconv_steps", C.c_int64),
+                ("status", C.c_int)]
 
 
 class Profile(C.Structure):

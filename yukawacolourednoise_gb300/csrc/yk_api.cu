@@ -56,7 +56,7 @@ struct Workspace {
     SysDev* d_sys = nullptr;
     int2* d_tiles = nullptr;
     CGState* d_state = nullptr;
-    double2* d_partial = nullptr;
+    Partial* d_partial = nullptr;
     ChainDev* d_chain = nullptr;   // chain copy whose sys0 = 0 refers to d_sys
     int2* d_site_tiles = nullptr;
     std::vector<SysDev> h_sys;
@@ -97,7 +97,7 @@ struct yk_ctx {
     int2* d_sys_tiles = nullptr;
     int n_sys_tiles = 0;
     CGState* d_state = nullptr;
-    double2* d_partial = nullptr;
+    Partial* d_partial = nullptr;
     GridBarrier* d_bar = nullptr;
     int* d_err = nullptr;
     int* d_nactive = nullptr;
@@ -298,7 +298,7 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
     const size_t o_sys = ar.reserve(sizeof(SysDev) * R);
     const size_t o_tiles = ar.reserve(sizeof(int2) * (size_t)R * nt);
     const size_t o_state = ar.reserve(sizeof(CGState) * R);
-    const size_t o_part = ar.reserve(sizeof(double2) * (size_t)R * nt);
+    const size_t o_part = ar.reserve(sizeof(Partial) * (size_t)R * nt);
     const size_t o_chain = ar.reserve(sizeof(ChainDev));
     const size_t o_stile = ar.reserve(sizeof(int2) * nt);
     const size_t o_point = ar.reserve(v64);
@@ -307,7 +307,8 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
     std::vector<size_t> o_vec(R * 12);
     for (int j = 0; j < R; ++j) {
         for (int q = 0; q < 6; ++q) o_vec[j * 12 + q] = ar.reserve(v64);       // x r p0 p1 t Ap
-        for (int q = 6; q < 12; ++q) o_vec[j * 12 + q] = ar.reserve(v32);      // r p0 p1 t Ap xs
+        for (int q = 6; q < 12; ++q)                                             // r p0 p1 t Ap xs
+            o_vec[j * 12 + q] = ar.reserve((q == 6 || q == 9) ? 2 * v32 : v32);   // r and t hold two vectors
     }
     void* mem = nullptr;
     if (cudaMalloc(&mem, ar.used) != cudaSuccess) {
@@ -321,7 +322,7 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
     w.d_sys = ar.at<SysDev>(o_sys);
     w.d_tiles = ar.at<int2>(o_tiles);
     w.d_state = ar.at<CGState>(o_state);
-    w.d_partial = ar.at<double2>(o_part);
+    w.d_partial = ar.at<Partial>(o_part);
     w.d_chain = ar.at<ChainDev>(o_chain);
     w.d_site_tiles = ar.at<int2>(o_stile);
     w.point = ar.at<double>(o_point);
@@ -583,10 +584,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             o.x = ar.reserve(d);
             o.t64 = ar.reserve(d);
             if (mixed) {
-                o.r32 = ar.reserve(f);
+                o.r32 = ar.reserve(2 * f);
                 o.q0 = ar.reserve(f);
                 o.q1 = ar.reserve(f);
-                o.t32 = ar.reserve(f);
+                o.t32 = ar.reserve(2 * f);
                 o.ap32 = ar.reserve(f);
                 o.xs = ar.reserve(f);
             } else {
@@ -601,7 +602,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     const size_t o_sys = ar.reserve(sizeof(SysDev) * (nsys > 0 ? nsys : 1));
     const size_t o_systiles = ar.reserve(sizeof(int2) * (nsys_tiles > 0 ? nsys_tiles : 1));
     const size_t o_state = ar.reserve(sizeof(CGState) * (nsys > 0 ? nsys : 1));
-    const size_t o_partial = ar.reserve(sizeof(double2) * (nsys_tiles > 0 ? nsys_tiles : 1));
+    const size_t o_partial = ar.reserve(sizeof(Partial) * (nsys_tiles > 0 ? nsys_tiles : 1));
     const size_t o_bar = ar.reserve(sizeof(GridBarrier));
     const size_t o_err = ar.reserve(sizeof(int) * 4);
     const size_t o_sitetiles = ar.reserve(sizeof(int2) * nsite_tiles);
@@ -624,7 +625,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     ctx->d_sys = ar.at<SysDev>(o_sys);
     ctx->d_sys_tiles = ar.at<int2>(o_systiles);
     ctx->d_state = ar.at<CGState>(o_state);
-    ctx->d_partial = ar.at<double2>(o_partial);
+    ctx->d_partial = ar.at<Partial>(o_partial);
     ctx->d_bar = ar.at<GridBarrier>(o_bar);
     ctx->d_err = ar.at<int>(o_err);
     ctx->d_nactive = ctx->d_err + 1;

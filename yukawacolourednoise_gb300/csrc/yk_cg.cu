@@ -1,20 +1,26 @@
 // yk_cg.cu -- batched CG on D^dag D (or D D^dag) as one persistent
 // cooperative kernel per solve.
 //
-// Follows the algorithm of code/src/CGsolver.cu:72-170 (x0 = 0, r = p = b,
-// alpha = |r|^2 / <p, A p>, x += alpha p, r -= alpha A p, beta = |r'|^2/|r|^2,
-// p = r + beta p; stop when sqrt(|r|^2) <= tol), restructured for GB300:
-//   * one launch solves every (chain, rhs) system of a context; sites are cut
-//     into tiles and a bounded grid barrier separates the three phases of an
-//     iteration (the reference pays 15 grid syncs per iteration);
-//   * p_{k+1} = r + beta p_k is never a separate pass: the D apply of the next
-//     iteration forms it on the fly (double-buffered p);
-//   * dot products are deterministic: per-tile partials are summed in tile
-//     order by the last tile to finish (no floating-point atomics);
-//   * MIXED: FP32 vectors and stencil, FP64 partial sums, and every
-//     `reliable_every` iterations (or when the FP32 residual claims
-//     convergence) an FP64 reliable update x += xs, r = b - A x.  Convergence
-//     is only declared on the FP64 true residual.
+// FP64 (cg64_kernel): the algorithm of code/src/CGsolver.cu:72-170 --
+//   x0 = 0, r = p = b, alpha = |r|^2 / <p, A p>, x += alpha p,
+//   r -= alpha A p, beta = |r'|^2 / |r|^2, p = r + beta p, stop when
+//   sqrt(|r|^2) <= tol -- in three phases per iteration (the reference pays
+//   15 grid syncs): p is formed on the fly inside the first D apply
+//   (double-buffered), the second D apply carries <p, Ap>, the axpys carry |r|^2.
+//
+// MIXED (cgcg_kernel): Chronopoulos-Gear CG (one fused reduction of (r, r)
+//   and (A r, r) per iteration) on FP32 vectors with FP64 partial sums, in two
+//   phases per iteration: r_{k+1} = r_k - alpha (w_k + beta s_{k-1}) is formed
+//   on the fly at the four neighbours inside D, and D^dag follows.  Every
+//   `reliable_every` iterations, when the FP32 residual claims convergence,
+//   or at the iteration cap, an FP64 reliable update folds the FP32 solution
+//   increment into the FP64 solution and recomputes r = b - A x in FP64;
+//   convergence is only declared on that FP64 residual.
+//
+// Both: one launch solves every (chain, rhs) system; each block owns a
+// contiguous range of 256-site tiles; a bounded sense-reversing grid barrier
+// separates phases; reductions are deterministic (per-tile partials, summed
+// in tile order by every block that needs them, right after the barrier).
 #include <type_traits>
 
 #include "yk_common.cuh"
@@ -24,183 +30,150 @@ namespace yk {
 
 namespace {
 
-enum Phase { PH_INIT = 0, PH_ALPHA = 1, PH_BETA = 2, PH_RU = 3 };
+constexpr int kMaxSysPerBlock = 48;
 
-__device__ __forceinline__ void deactivate(const CGArgs& a, volatile CGState& s, int converged, int status)
-{
-    s.active = 0;
-    s.converged = converged;
-    if (status) s.status = status;
-    atomicSub(a.n_active, 1);
-}
+// Per-block view of one system whose tiles fall in the block's range.
+struct SysLocal {
+    int sys;
+    int owner;       // this block holds the system's first tile: writes CGState
+    int active;
+    int iters;
+    int ru;          // reliable update pending (mixed)
+    int ru_done;     // the last reduction came from a reliable update
+    int last;        // iteration cap reached
+    int status;
+    double rr, rr0, stop, alpha, alpha_im, beta, gamma;
+    double sx, sy, sz;   // reduction results of the current phase
+};
 
-// Runs in one thread: turns the summed partials of system `s` into the
-// scalars the next phase needs.
-template <bool MIXED>
-__device__ void finalize(const CGArgs& a, int sys, int ph, double x, double y)
+// Sense-reversing grid barrier (one counter word; block 0 adds 2^31 - (n-1),
+// the others 1, so bit 31 flips once every block has arrived).  Bounded:
+// after kBarrierCycles it records YK_ETIMEOUT and every caller leaves.
+__device__ __forceinline__ bool gsync(GridBarrier* b, int* err)
 {
-    // volatile: other SMs finalised this system in earlier phases
-    volatile CGState& s = a.st[sys];
-    if (ph == PH_INIT) {
-        s.rr = x;
-        s.rr0 = x;
-        s.rr_prev = x;
-        s.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(x);
-        s.iters = 0;
-        s.n_ru = 0;
-        s.ru = 0;
-        s.last = 0;
-        s.status = 0;
-        s.beta = 0.0;
-        s.active = 1;
-        s.converged = 0;
-        if (!isfinite(x)) deactivate(a, s, 0, YK_ENAN);
-        else if (!(sqrt(x) > s.stop)) deactivate(a, s, 1, 0);
-        else if (a.max_iter <= 0) deactivate(a, s, 0, YK_ENOCONV);
-    } else if (ph == PH_ALPHA) {
-        // alpha = rr / (x + i y), Smith's complex division
-        const double c = x, d = y, num = s.rr;
-        double ar, ai;
-        if (fabs(c) >= fabs(d)) {
-            const double q = d / c, den = c + d * q;
-            ar = num / den;
-            ai = (-num * q) / den;
-        } else {
-            const double q = c / d, den = c * q + d;
-            ar = (num * q) / den;
-            ai = -num / den;
-        }
-        s.alpha_re = ar;
-        s.alpha_im = ai;
-        if (!isfinite(ar) || !isfinite(ai)) deactivate(a, s, 0, YK_ENAN);
-    } else if (ph == PH_BETA) {
-        const double rr = x;
-        s.iters += 1;
-        s.beta = rr / s.rr;
-        s.rr_prev = s.rr;
-        s.rr = rr;
-        if (!isfinite(rr)) {
-            deactivate(a, s, 0, YK_ENAN);
-        } else if (!MIXED) {
-            if (!(sqrt(rr) > s.stop)) deactivate(a, s, 1, 0);
-            else if (s.iters >= a.max_iter) deactivate(a, s, 0, YK_ENOCONV);
-        } else {
-            const bool cand = !(sqrt(rr) > s.stop);
-            const bool due = a.reliable_every > 0 && (s.iters % a.reliable_every) == 0;
-            const bool cap = s.iters >= a.max_iter;
-            if (cand || due || cap) {
-                s.ru = 1;
-                s.last = cap ? 1 : 0;
-                atomicOr(a.any_ru, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned inc = (blockIdx.x == 0) ? (0x80000000u - (gridDim.x - 1)) : 1u;
+        __threadfence();
+        const unsigned old = atomicAdd(&b->count, inc);
+        volatile unsigned* vc = &b->count;
+        const long long t0 = clock64();
+        while (((*vc ^ old) & 0x80000000u) == 0) {
+            if (clock64() - t0 > kBarrierCycles) {
+                atomicCAS(err, 0, YK_ETIMEOUT);
+                break;
             }
+            __nanosleep(20);
         }
-    } else {  // PH_RU: x holds |b - A x|^2 in FP64
-        const double rt = x;
-        s.n_ru += 1;
-        s.ru = 0;
-        if (!isfinite(rt)) {
-            deactivate(a, s, 0, YK_ENAN);
-        } else if (!(sqrt(rt) > s.stop)) {
-            s.rr = rt;
-            deactivate(a, s, 1, 0);
-        } else if (s.last) {
-            s.rr = rt;
-            deactivate(a, s, 0, YK_ENOCONV);
-        } else {
-            s.beta = rt / s.rr_prev;
-            s.rr = rt;
-        }
+        __threadfence();
     }
-    __threadfence();
+    __syncthreads();
+    return *(volatile int*)err == 0;
 }
 
-// Publishes the block's partial of `tile`; the last tile of the system sums
-// all partials of the system in tile order and finalises.
-template <bool MIXED>
-__device__ __forceinline__ void tile_reduce(const CGArgs& a, int tile, int sys, const SysDev& S,
-                                            double2 v, int ph, volatile int* s_last)
+// Builds the block's system table from its tile range [tb, te).
+__device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* nsl, int* tile_slot)
 {
     if (threadIdx.x == 0) {
-        a.partial[tile] = v;
-        __threadfence();
-        const unsigned prev = atomicAdd(&a.st[sys].counter, 1u);
-        *s_last = (prev == (unsigned)S.ntiles - 1) ? 1 : 0;
+        int n = 0, last = -1;
+        for (int t = tb; t < te; ++t) {
+            const int s = a.tiles[t].x;
+            if (s != last) {
+                if (n == kMaxSysPerBlock) {
+                    atomicCAS(a.err, 0, YK_EINVAL);
+                    break;
+                }
+                SysLocal& L = sl[n];
+                L.sys = s;
+                L.owner = (a.sys[s].tile0 >= tb && a.sys[s].tile0 < te) ? 1 : 0;
+                L.active = 1;
+                L.iters = 0;
+                L.ru = 0;
+                L.ru_done = 0;
+                L.last = 0;
+                L.status = 0;
+                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = L.gamma = 0.0;
+                L.sx = L.sy = L.sz = 0.0;
+                ++n;
+                last = s;
+            }
+            tile_slot[t - tb] = n - 1;
+        }
+        *nsl = n;
     }
     __syncthreads();
-    if (*s_last) {
-        if (threadIdx.x < 32) {
-            __threadfence();
-            const int lane = threadIdx.x;
-            double x = 0.0, y = 0.0;
-            for (int i = lane; i < S.ntiles; i += 32) {
-                const double2 p = __ldcg(a.partial + S.tile0 + i);
-                x += p.x;
-                y += p.y;
-            }
-            x = warp_sum(x);
-            y = warp_sum(y);
-            if (lane == 0) {
-                *(volatile unsigned*)&a.st[sys].counter = 0;
-                finalize<MIXED>(a, sys, ph, x, y);
-            }
+}
+
+// Sums the partials of every active system of the block (one warp per
+// system, lane-strided over the system's tiles, fixed order).
+__device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = w; j < nsl; j += nw) {
+        if (!sl[j].active) continue;
+        const SysDev& S = a.sys[sl[j].sys];
+        double x = 0.0, y = 0.0, z = 0.0;
+        for (int i = lane; i < S.ntiles; i += 32) {
+            const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + i);
+            const double2 p0 = __ldcg(q), p1 = __ldcg(q + 1);
+            x += p0.x;
+            y += p0.y;
+            z += p1.x;
+        }
+        x = warp_sum(x);
+        y = warp_sum(y);
+        z = warp_sum(z);
+        if (lane == 0) {
+            sl[j].sx = x;
+            sl[j].sy = y;
+            sl[j].sz = z;
         }
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ int st_active(const CGArgs& a, int sys)
+__device__ void retire(const CGArgs& a, SysLocal& L, int converged, int status)
 {
-    return *(volatile int*)&a.st[sys].active;
+    L.active = 0;
+    if (status) L.status = status;
+    if (L.owner) {
+        volatile CGState& s = a.st[L.sys];
+        s.converged = converged;
+        s.status = L.status;
+        s.iters = L.iters;
+        s.rr = L.rr;
+        s.rr0 = L.rr0;
+        s.active = 0;
+        __threadfence();
+        atomicSub(a.n_active, 1);
+    }
 }
 
-__device__ __forceinline__ double st_load(const double* p) { return *(volatile const double*)p; }
+__device__ void publish(const CGArgs& a, const SysLocal& L, int n_ru)
+{
+    if (L.owner) {
+        volatile CGState& s = a.st[L.sys];
+        s.iters = L.iters;
+        s.rr = L.rr;
+        s.rr0 = L.rr0;
+        s.n_ru = n_ru;
+    }
+}
 
-// p_k at site m: p_0 = b (already stored), p_k = r + beta p_{k-1}.
 template <typename W, int K>
-__device__ __forceinline__ Site<W, K> p_at(const W* r, const W* pold, int64_t m, W beta, bool fresh)
-{
-    Site<W, K> po = load_site_cg<W, K>(pold, m);
-    if (fresh) return po;
-    const Site<W, K> rv = load_site_cg<W, K>(r, m);
-#pragma unroll
-    for (int i = 0; i < 4 * K; ++i) po.v[i] = fma(beta, po.v[i], rv.v[i]);
-    return po;
-}
-
-template <typename W, int K, bool DAG>
-__device__ __forceinline__ Site<W, K> apply_site(const Site<W, K>& c, const Site<W, K>& tu,
-                                                 const Site<W, K>& td, const Site<W, K>& xu,
-                                                 const Site<W, K>& xd, W diag, W r, const Nbr& nb)
-{
-    return dirac_combine<W, K, DAG>(c, tu, td, xu, xd, diag, r, (W)nb.sp, (W)nb.sm);
-}
-
-template <typename W, int K>
-__device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& S, bool dag,
-                                              bool cg_loads)
+__device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& S, bool dag)
 {
     const Nbr nb = neighbours(n, S.Nt, S.Nx);
-    Site<W, K> c, tu, td, xu, xd;
-    if (cg_loads) {
-        c = load_site_cg<W, K>(in, n);
-        tu = load_site_cg<W, K>(in, nb.tu);
-        td = load_site_cg<W, K>(in, nb.td);
-        xu = load_site_cg<W, K>(in, nb.xu);
-        xd = load_site_cg<W, K>(in, nb.xd);
-    } else {
-        c = load_site<W, K>(in, n);
-        tu = load_site<W, K>(in, nb.tu);
-        td = load_site<W, K>(in, nb.td);
-        xu = load_site<W, K>(in, nb.xu);
-        xd = load_site<W, K>(in, nb.xd);
-    }
+    const Site<W, K> c = load_site<W, K>(in, n);
+    const Site<W, K> tu = load_site<W, K>(in, nb.tu);
+    const Site<W, K> td = load_site<W, K>(in, nb.td);
+    const Site<W, K> xu = load_site<W, K>(in, nb.xu);
+    const Site<W, K> xd = load_site<W, K>(in, nb.xd);
     const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
-    const W r = (W)S.r;
-    return dag ? apply_site<W, K, true>(c, tu, td, xu, xd, diag, r, nb)
-               : apply_site<W, K, false>(c, tu, td, xu, xd, diag, r, nb);
+    return dag ? dirac_combine<W, K, true>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm)
+               : dirac_combine<W, K, false>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm);
 }
 
-// Re and Im of sum conj(a) b over one site.
 template <typename W, int K>
 __device__ __forceinline__ double2 site_dot(const Site<W, K>& a, const Site<W, K>& b)
 {
@@ -218,7 +191,6 @@ __device__ __forceinline__ double2 site_dot(const Site<W, K>& a, const Site<W, K
     return make_double2((double)re, (double)im);
 }
 
-// y += (ar + i ai) * v
 template <typename W, int K>
 __device__ __forceinline__ void site_axpy(Site<W, K>& y, W ar, W ai, const Site<W, K>& v)
 {
@@ -252,25 +224,47 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
     return s;
 }
 
+// Block partial sums -> the tile's partial slot (thread 0).
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double* red,
+                                            bool keep_z = false)
+{
+    const double2 s = block_sum2(x, y, red);
+    double zz = 0.0;
+    if (!keep_z) zz = block_sum2(z, 0.0, red).x;
+    if (threadIdx.x == 0) {
+        Partial p;
+        p.x = s.x;
+        p.y = s.y;
+        p.z = keep_z ? a.partial[tile].z : zz;
+        p.w = 0.0;
+        a.partial[tile] = p;
+    }
+}
+
 }  // namespace
 
-template <int K, bool MIXED>
-__global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
+// ---------------------------------------------------------------------------
+// FP64 Hestenes-Stiefel CG (the reference's algorithm)
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
 {
-    using W = typename std::conditional<MIXED, float, double>::type;
     __shared__ double red[64];
-    __shared__ int s_last;
-    const unsigned nb = gridDim.x;
+    __shared__ SysLocal sl[kMaxSysPerBlock];
+    __shared__ int nsl;
+    __shared__ int tslot[kMaxTilesPerBlock];
+    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
+    const int te = min(tb + a.tiles_per_block, a.tile_end);
+    build_table(a, tb, te, sl, &nsl, tslot);
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
 
     // ---------------- init: x = 0, r = p_0 = b, |b|^2
-    for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-        const int2 td = a.tiles[tile];
-        const SysDev& S = a.sys[td.x];
-        const int n = td.y + threadIdx.x;
+    for (int tile = tb; tile < te; ++tile) {
+        const SysDev& S = a.sys[a.tiles[tile].x];
+        const int n = a.tiles[tile].y + threadIdx.x;
         double pr = 0.0;
         if (n < S.V) {
-            Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
+            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
             if (S.gen_eta) store_site<double, K>(S.b, n, bv);
             Site<double, K> z;
 #pragma unroll
@@ -279,179 +273,426 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                 pr = fma(bv.v[i], bv.v[i], pr);
             }
             store_site<double, K>(S.x, n, z);
-            if constexpr (MIXED) {
-                Site<float, K> bf, zf;
-#pragma unroll
-                for (int i = 0; i < 4 * K; ++i) {
-                    bf.v[i] = (float)bv.v[i];
-                    zf.v[i] = 0.f;
-                }
-                store_site<float, K>(S.r32, n, bf);
-                store_site<float, K>(S.p32[0], n, bf);
-                store_site<float, K>(S.xs32, n, zf);
-            } else {
-                store_site<double, K>(S.r64, n, bv);
-                store_site<double, K>(S.p64[0], n, bv);
-            }
+            store_site<double, K>(S.r64, n, bv);
+            store_site<double, K>(S.p64[0], n, bv);
         }
-        const double2 v = block_sum2(pr, 0.0, red);
-        tile_reduce<MIXED>(a, tile, td.x, S, v, PH_INIT, &s_last);
+        put_partial(a, tile, pr, 0.0, 0.0, red);
     }
-    if (!grid_sync(a.bar, nb, a.err)) return;
+    if (!gsync(a.bar, a.err)) return;
 
     for (int k = 0; k <= a.max_iter + 1; ++k) {
-        if (*(volatile int*)a.n_active == 0) break;
         const bool fresh = (k == 0);
         const int cur = k & 1, prv = (k + 1) & 1;
-
-        // ---------------- phase 1: p_k (on the fly) and t = D_first p_k
-        for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-            const int2 td = a.tiles[tile];
-            if (!st_active(a, td.x)) continue;
-            const SysDev& S = a.sys[td.x];
-            const int n = td.y + threadIdx.x;
-            if (n >= S.V) continue;
-            const W beta = (W)st_load(&a.st[td.x].beta);
-            const W* rv;
-            const W* pold;
-            W* pnew;
-            W* tv;
-            if constexpr (MIXED) {
-                rv = S.r32; pold = S.p32[fresh ? 0 : prv]; pnew = S.p32[cur]; tv = S.t32;
-            } else {
-                rv = S.r64; pold = S.p64[fresh ? 0 : prv]; pnew = S.p64[cur]; tv = S.t64;
+        // ---------------- phase 1: rr -> beta / stop; p_k on the fly; t = D_first p_k
+        reduce_systems(a, sl, nsl);
+        if (threadIdx.x == 0) {
+            for (int j = 0; j < nsl; ++j) {
+                SysLocal& L = sl[j];
+                if (!L.active) continue;
+                if (fresh) {
+                    L.rr = L.rr0 = L.sx;
+                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(L.sx);
+                    L.beta = 0.0;
+                    if (!isfinite(L.sx)) retire(a, L, 0, YK_ENAN);
+                    else if (!(sqrt(L.sx) > L.stop)) retire(a, L, 1, 0);
+                    else if (a.max_iter <= 0) retire(a, L, 0, YK_ENOCONV);
+                } else {
+                    const double rr = L.sx;
+                    L.iters += 1;
+                    L.beta = rr / L.rr;
+                    L.rr = rr;
+                    if (!isfinite(rr)) retire(a, L, 0, YK_ENAN);
+                    else if (!(sqrt(rr) > L.stop)) retire(a, L, 1, 0);
+                    else if (L.iters >= a.max_iter) retire(a, L, 0, YK_ENOCONV);
+                }
             }
-            const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-            const Site<W, K> c = p_at<W, K>(rv, pold, n, beta, fresh);
-            const Site<W, K> tu = p_at<W, K>(rv, pold, nbr.tu, beta, fresh);
-            const Site<W, K> tdn = p_at<W, K>(rv, pold, nbr.td, beta, fresh);
-            const Site<W, K> xu = p_at<W, K>(rv, pold, nbr.xu, beta, fresh);
-            const Site<W, K> xd = p_at<W, K>(rv, pold, nbr.xd, beta, fresh);
-            const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
-            const Site<W, K> o = first_dag
-                ? apply_site<W, K, true>(c, tu, tdn, xu, xd, diag, (W)S.r, nbr)
-                : apply_site<W, K, false>(c, tu, tdn, xu, xd, diag, (W)S.r, nbr);
-            store_site<W, K>(tv, n, o);
-            if (!fresh) store_site<W, K>(pnew, n, c);
         }
-        if (!grid_sync(a.bar, nb, a.err)) return;
+        __syncthreads();
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (!L.active) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
+            if (n >= S.V) continue;
+            const double beta = L.beta;
+            const double* pold = S.p64[fresh ? 0 : prv];
+            const Nbr nbr = neighbours(n, S.Nt, S.Nx);
+            auto p_at = [&](int64_t m) {
+                Site<double, K> po = load_site<double, K>(pold, m);
+                if (!fresh) {
+                    const Site<double, K> rv = load_site<double, K>(S.r64, m);
+#pragma unroll
+                    for (int i = 0; i < 4 * K; ++i) po.v[i] = fma(beta, po.v[i], rv.v[i]);
+                }
+                return po;
+            };
+            const Site<double, K> c = p_at(n), tu = p_at(nbr.tu), tdn = p_at(nbr.td), xu = p_at(nbr.xu),
+                                  xd = p_at(nbr.xd);
+            const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+            const Site<double, K> o = first_dag
+                ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
+                : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
+            store_site<double, K>(S.t64, n, o);
+            if (!fresh) store_site<double, K>(S.p64[cur], n, c);
+        }
+        if (!gsync(a.bar, a.err)) return;
+        if (*(volatile int*)a.n_active == 0) break;
 
         // ---------------- phase 2: Ap = D_second t, <p, Ap>
-        for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-            const int2 td = a.tiles[tile];
-            if (!st_active(a, td.x)) continue;
-            const SysDev& S = a.sys[td.x];
-            const int n = td.y + threadIdx.x;
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (!L.active) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
             double2 d = make_double2(0.0, 0.0);
             if (n < S.V) {
-                const W* tv;
-                const W* pk;
-                W* apv;
-                if constexpr (MIXED) { tv = S.t32; pk = S.p32[cur]; apv = S.Ap32; }
-                else { tv = S.t64; pk = S.p64[cur]; apv = S.Ap64; }
-                const Site<W, K> ap = apply_d<W, K>(tv, n, S, !first_dag, true);
-                store_site<W, K>(apv, n, ap);
-                const Site<W, K> pv = load_site_cg<W, K>(pk, n);
-                d = site_dot<W, K>(pv, ap);
+                const Site<double, K> ap = apply_d<double, K>(S.t64, n, S, !first_dag);
+                store_site<double, K>(S.Ap64, n, ap);
+                d = site_dot<double, K>(load_site<double, K>(S.p64[cur], n), ap);
             }
-            const double2 v = block_sum2(d.x, d.y, red);
-            tile_reduce<MIXED>(a, tile, td.x, S, v, PH_ALPHA, &s_last);
+            put_partial(a, tile, d.x, d.y, 0.0, red);
         }
-        if (!grid_sync(a.bar, nb, a.err)) return;
+        if (!gsync(a.bar, a.err)) return;
 
-        // ---------------- phase 3: x += alpha p, r -= alpha Ap, |r|^2
-        for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-            const int2 td = a.tiles[tile];
-            if (!st_active(a, td.x)) continue;
-            const SysDev& S = a.sys[td.x];
-            const int n = td.y + threadIdx.x;
+        // ---------------- phase 3: alpha; x += alpha p, r -= alpha Ap, |r|^2
+        reduce_systems(a, sl, nsl);
+        if (threadIdx.x == 0) {
+            for (int j = 0; j < nsl; ++j) {
+                SysLocal& L = sl[j];
+                if (!L.active) continue;
+                // alpha = rr / (sx + i sy), Smith's complex division (CGsolver.cu:137)
+                const double c = L.sx, d = L.sy, num = L.rr;
+                double ar, ai;
+                if (fabs(c) >= fabs(d)) {
+                    const double q = d / c, den = c + d * q;
+                    ar = num / den;
+                    ai = (-num * q) / den;
+                } else {
+                    const double q = c / d, den = c * q + d;
+                    ar = (num * q) / den;
+                    ai = -num / den;
+                }
+                L.alpha = ar;
+                L.alpha_im = ai;
+                if (!isfinite(ar) || !isfinite(ai)) retire(a, L, 0, YK_ENAN);
+            }
+        }
+        __syncthreads();
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (!L.active) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
             double rr = 0.0;
             if (n < S.V) {
-                const W ar = (W)st_load(&a.st[td.x].alpha_re);
-                const W ai = (W)st_load(&a.st[td.x].alpha_im);
-                const W* pk;
-                const W* apv;
-                W* xv;
-                W* rv;
-                if constexpr (MIXED) { pk = S.p32[cur]; apv = S.Ap32; xv = S.xs32; rv = S.r32; }
-                else { pk = S.p64[cur]; apv = S.Ap64; xv = S.x; rv = S.r64; }
-                const Site<W, K> pv = load_site_cg<W, K>(pk, n);
-                const Site<W, K> ap = load_site_cg<W, K>(apv, n);
-                Site<W, K> xs = load_site_cg<W, K>(xv, n);
-                Site<W, K> rs = load_site_cg<W, K>(rv, n);
-                site_axpy<W, K>(xs, ar, ai, pv);
-                site_axpy<W, K>(rs, -ar, -ai, ap);
-                store_site<W, K>(xv, n, xs);
-                store_site<W, K>(rv, n, rs);
-                W acc = 0;
+                const Site<double, K> pv = load_site<double, K>(S.p64[cur], n);
+                const Site<double, K> ap = load_site<double, K>(S.Ap64, n);
+                Site<double, K> xs = load_site<double, K>(S.x, n);
+                Site<double, K> rs = load_site<double, K>(S.r64, n);
+                site_axpy<double, K>(xs, L.alpha, L.alpha_im, pv);
+                site_axpy<double, K>(rs, -L.alpha, -L.alpha_im, ap);
+                store_site<double, K>(S.x, n, xs);
+                store_site<double, K>(S.r64, n, rs);
 #pragma unroll
-                for (int i = 0; i < 4 * K; ++i) acc = fma(rs.v[i], rs.v[i], acc);
-                rr = (double)acc;
+                for (int i = 0; i < 4 * K; ++i) rr = fma(rs.v[i], rs.v[i], rr);
             }
-            const double2 v = block_sum2(rr, 0.0, red);
-            tile_reduce<MIXED>(a, tile, td.x, S, v, PH_BETA, &s_last);
+            put_partial(a, tile, rr, 0.0, 0.0, red);
         }
-        if (!grid_sync(a.bar, nb, a.err)) return;
+        if (!gsync(a.bar, a.err)) return;
+    }
+    if (threadIdx.x == 0)
+        for (int j = 0; j < nsl; ++j) publish(a, sl[j], 0);
+}
 
-        if constexpr (MIXED) {
-            if (*(volatile int*)a.any_ru) {
-                // RU1: x += xs, xs = 0
-                for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-                    const int2 td = a.tiles[tile];
-                    if (!*(volatile int*)&a.st[td.x].ru) continue;
-                    const SysDev& S = a.sys[td.x];
-                    const int n = td.y + threadIdx.x;
-                    if (n >= S.V) continue;
-                    Site<double, K> xv = load_site_cg<double, K>(S.x, n);
-                    const Site<float, K> xs = load_site_cg<float, K>(S.xs32, n);
-                    Site<float, K> z;
+// ---------------------------------------------------------------------------
+// Mixed FP32/FP64 Chronopoulos-Gear CG with reliable updates.
+// Buffers of a system: r32 (2 V: r double-buffered), p32[0] (p),
+// p32[1] and Ap32 (s = A p, double-buffered), t32 (2 V: t = D r and w = A r),
+// xs32 (FP32 solution increment), FP64 x, b, t64.
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
+{
+    using W = float;
+    __shared__ double red[64];
+    __shared__ SysLocal sl[kMaxSysPerBlock];
+    __shared__ int nsl;
+    __shared__ int tslot[kMaxTilesPerBlock];
+    __shared__ int s_nru;
+    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
+    const int te = min(tb + a.tiles_per_block, a.tile_end);
+    build_table(a, tb, te, sl, &nsl, tslot);
+    if (threadIdx.x == 0) s_nru = 0;
+    const bool first_dag = (a.mtype == YK_NORMAL);
+    auto Rb = [](const SysDev& S, int i) { return S.r32 + (i ? (int64_t)S.V * 4 * K : 0); };
+    auto Sb = [](const SysDev& S, int i) { return i ? S.Ap32 : S.p32[1]; };
+    auto Wb = [](const SysDev& S) { return S.t32 + (int64_t)S.V * 4 * K; };
+
+    // ---------------- I0: b (generated or given), x = 0, xs = 0, p = 0, s_{-1} = 0, r_0 = b, |b|^2
+    for (int tile = tb; tile < te; ++tile) {
+        const SysDev& S = a.sys[a.tiles[tile].x];
+        const int n = a.tiles[tile].y + threadIdx.x;
+        double bb = 0.0;
+        if (n < S.V) {
+            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
+            if (S.gen_eta) store_site<double, K>(S.b, n, bv);
+            Site<double, K> z;
+            Site<W, K> bf, zf;
+#pragma unroll
+            for (int i = 0; i < 4 * K; ++i) {
+                z.v[i] = 0.0;
+                zf.v[i] = 0.f;
+                bf.v[i] = (W)bv.v[i];
+                bb = fma(bv.v[i], bv.v[i], bb);
+            }
+            store_site<double, K>(S.x, n, z);
+            store_site<W, K>(S.xs32, n, zf);
+            store_site<W, K>(S.p32[0], n, zf);
+            store_site<W, K>(Sb(S, 1), n, zf);
+            store_site<W, K>(Rb(S, 0), n, bf);
+        }
+        put_partial(a, tile, 0.0, 0.0, bb, red);
+    }
+    if (!gsync(a.bar, a.err)) return;
+    // ---------------- I1: t = D_first r_0
+    for (int tile = tb; tile < te; ++tile) {
+        const SysDev& S = a.sys[a.tiles[tile].x];
+        const int n = a.tiles[tile].y + threadIdx.x;
+        if (n < S.V) store_site<W, K>(S.t32, n, apply_d<W, K>(Rb(S, 0), n, S, first_dag));
+    }
+    if (!gsync(a.bar, a.err)) return;
+    // ---------------- I2: w_0 = D_second t; (r,r), (w,r); |b|^2 kept in z
+    for (int tile = tb; tile < te; ++tile) {
+        const SysDev& S = a.sys[a.tiles[tile].x];
+        const int n = a.tiles[tile].y + threadIdx.x;
+        double g = 0.0, d = 0.0;
+        if (n < S.V) {
+            const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
+            store_site<W, K>(Wb(S), n, w);
+            const Site<W, K> r = load_site<W, K>(Rb(S, 0), n);
+            g = site_dot<W, K>(r, r).x;
+            d = site_dot<W, K>(w, r).x;
+        }
+        put_partial(a, tile, g, d, 0.0, red, true);
+    }
+    if (!gsync(a.bar, a.err)) return;
+
+    for (int k = 0; k <= a.max_iter + 1; ++k) {
+        const int cur = k & 1, nxt = (k + 1) & 1;
+        // ---------------- phase A: reduce; s_k, p_k, xs += alpha p_k, r_{k+1} (on the fly), t = D r_{k+1}
+        reduce_systems(a, sl, nsl);
+        if (threadIdx.x == 0) {
+            int want_ru = 0;
+            for (int j = 0; j < nsl; ++j) {
+                SysLocal& L = sl[j];
+                if (!L.active) continue;
+                const double gam = L.sx, del = L.sy;
+                if (k == 0) {
+                    L.rr0 = L.sz;
+                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(L.sz);
+                    L.rr = L.sz;
+                    if (!isfinite(L.sz)) { retire(a, L, 0, YK_ENAN); continue; }
+                    if (!(sqrt(L.sz) > L.stop)) { retire(a, L, 1, 0); continue; }
+                    if (a.max_iter <= 0) { retire(a, L, 0, YK_ENOCONV); continue; }
+                    L.beta = 0.0;
+                    L.alpha = gam / del;
+                    L.gamma = gam;
+                } else {
+                    L.iters += 1;
+                    if (L.ru_done) {
+                        // z holds |b - A x|^2 in FP64 from the reliable update
+                        L.ru_done = 0;
+                        L.rr = L.sz;
+                        if (!isfinite(L.sz)) { retire(a, L, 0, YK_ENAN); continue; }
+                        if (!(sqrt(L.sz) > L.stop)) { retire(a, L, 1, 0); continue; }
+                        if (L.last) { retire(a, L, 0, YK_ENOCONV); continue; }
+                    } else {
+                        L.rr = gam;
+                    }
+                    const double beta = gam / L.gamma;
+                    const double den = del - beta * gam / L.alpha;
+                    L.beta = beta;
+                    L.alpha = gam / den;
+                    L.gamma = gam;
+                }
+                if (!isfinite(L.alpha) || !isfinite(L.beta)) { retire(a, L, 0, YK_ENAN); continue; }
+                // reliable update after this iteration?
+                const bool cand = !(sqrt(gam) > L.stop);
+                const bool due = a.reliable_every > 0 && ((L.iters + 1) % a.reliable_every) == 0;
+                const bool cap = (L.iters + 1) >= a.max_iter;
+                if (cand || due || cap) {
+                    L.ru = 1;
+                    L.last = cap ? 1 : 0;
+                    want_ru = 1;
+                }
+            }
+            if (want_ru) atomicMax(a.any_ru, k + 1);
+        }
+        __syncthreads();
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (!L.active) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
+            if (n >= S.V) continue;
+            const W al = (W)L.alpha, be = (W)L.beta;
+            const W* Rc = Rb(S, cur);
+            const W* Sp = Sb(S, nxt);   // s_{k-1}
+            const W* Wk = Wb(S);
+            const Nbr nbr = neighbours(n, S.Nt, S.Nx);
+            // r_{k+1}(m) = r_k(m) - alpha (w_k(m) + beta s_{k-1}(m))
+            auto rnext = [&](int64_t m, Site<W, K>* s_out) {
+                const Site<W, K> rv = load_site<W, K>(Rc, m);
+                const Site<W, K> wv = load_site<W, K>(Wk, m);
+                const Site<W, K> sv = load_site<W, K>(Sp, m);
+                Site<W, K> o;
+#pragma unroll
+                for (int i = 0; i < 4 * K; ++i) {
+                    const W s = fma(be, sv.v[i], wv.v[i]);
+                    if (s_out) s_out->v[i] = s;
+                    o.v[i] = fma(-al, s, rv.v[i]);
+                }
+                return o;
+            };
+            Site<W, K> sk;
+            const Site<W, K> c = rnext(n, &sk);
+            const Site<W, K> tu = rnext(nbr.tu, nullptr), tdn = rnext(nbr.td, nullptr);
+            const Site<W, K> xu = rnext(nbr.xu, nullptr), xd = rnext(nbr.xd, nullptr);
+            // p_k = r_k + beta p_{k-1}; xs += alpha p_k
+            const Site<W, K> rk = load_site<W, K>(Rc, n);
+            Site<W, K> pk = load_site<W, K>(S.p32[0], n);
+            Site<W, K> xs = load_site<W, K>(S.xs32, n);
+#pragma unroll
+            for (int i = 0; i < 4 * K; ++i) {
+                pk.v[i] = fma(be, pk.v[i], rk.v[i]);
+                xs.v[i] = fma(al, pk.v[i], xs.v[i]);
+            }
+            store_site<W, K>(S.p32[0], n, pk);
+            store_site<W, K>(S.xs32, n, xs);
+            store_site<W, K>(Sb(S, cur), n, sk);
+            store_site<W, K>(Rb(S, nxt), n, c);
+            const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
+            const Site<W, K> t = first_dag
+                ? dirac_combine<W, K, true>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm)
+                : dirac_combine<W, K, false>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm);
+            store_site<W, K>(S.t32, n, t);
+        }
+        if (!gsync(a.bar, a.err)) return;
+        if (*(volatile int*)a.n_active == 0) break;
+
+        // ---------------- phase B: w_{k+1} = D_second t; (r,r), (w,r)
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (!L.active) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
+            double g = 0.0, d = 0.0;
+            if (n < S.V) {
+                const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
+                store_site<W, K>(Wb(S), n, w);
+                const Site<W, K> r = load_site<W, K>(Rb(S, nxt), n);
+                g = site_dot<W, K>(r, r).x;
+                d = site_dot<W, K>(w, r).x;
+            }
+            put_partial(a, tile, g, d, 0.0, red);
+        }
+        if (!gsync(a.bar, a.err)) return;
+
+        if (*(volatile int*)a.any_ru == k + 1) {
+            // RU1: t64 = D_first (x + xs)  (FP64, formed on the fly)
+            for (int tile = tb; tile < te; ++tile) {
+                const SysLocal& L = sl[tslot[tile - tb]];
+                if (!L.active || !L.ru) continue;
+                const SysDev& S = a.sys[L.sys];
+                const int n = a.tiles[tile].y + threadIdx.x;
+                if (n >= S.V) continue;
+                const Nbr nbr = neighbours(n, S.Nt, S.Nx);
+                auto xat = [&](int64_t m) {
+                    Site<double, K> xv = load_site<double, K>(S.x, m);
+                    const Site<W, K> xs = load_site<W, K>(S.xs32, m);
+#pragma unroll
+                    for (int i = 0; i < 4 * K; ++i) xv.v[i] += (double)xs.v[i];
+                    return xv;
+                };
+                const Site<double, K> c = xat(n), tu = xat(nbr.tu), tdn = xat(nbr.td), xu = xat(nbr.xu),
+                                      xd = xat(nbr.xd);
+                const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+                const Site<double, K> t = first_dag
+                    ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
+                    : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
+                store_site<double, K>(S.t64, n, t);
+            }
+            if (!gsync(a.bar, a.err)) return;
+            // RU2: x += xs, xs = 0; r = b - D_second t64 (FP64) -> r_{k+1}; |r|^2 in z
+            for (int tile = tb; tile < te; ++tile) {
+                const SysLocal& L = sl[tslot[tile - tb]];
+                if (!L.active || !L.ru) continue;
+                const SysDev& S = a.sys[L.sys];
+                const int n = a.tiles[tile].y + threadIdx.x;
+                double rr = 0.0;
+                if (n < S.V) {
+                    Site<double, K> xv = load_site<double, K>(S.x, n);
+                    const Site<W, K> xs = load_site<W, K>(S.xs32, n);
+                    Site<W, K> zf;
 #pragma unroll
                     for (int i = 0; i < 4 * K; ++i) {
                         xv.v[i] += (double)xs.v[i];
-                        z.v[i] = 0.f;
+                        zf.v[i] = 0.f;
                     }
                     store_site<double, K>(S.x, n, xv);
-                    store_site<float, K>(S.xs32, n, z);
-                }
-                if (!grid_sync(a.bar, nb, a.err)) return;
-                if (blockIdx.x == 0 && threadIdx.x == 0) *a.any_ru = 0;
-                // RU2: t = D_first x  (FP64)
-                for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-                    const int2 td = a.tiles[tile];
-                    if (!*(volatile int*)&a.st[td.x].ru) continue;
-                    const SysDev& S = a.sys[td.x];
-                    const int n = td.y + threadIdx.x;
-                    if (n >= S.V) continue;
-                    const Site<double, K> t = apply_d<double, K>(S.x, n, S, first_dag, true);
-                    store_site<double, K>(S.t64, n, t);
-                }
-                if (!grid_sync(a.bar, nb, a.err)) return;
-                // RU3: r = b - D_second t  (FP64), r32 = r, |r|^2
-                for (int tile = a.tile_begin + blockIdx.x; tile < a.tile_end; tile += nb) {
-                    const int2 td = a.tiles[tile];
-                    if (!*(volatile int*)&a.st[td.x].ru) continue;
-                    const SysDev& S = a.sys[td.x];
-                    const int n = td.y + threadIdx.x;
-                    double rr = 0.0;
-                    if (n < S.V) {
-                        const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag, true);
-                        const Site<double, K> bv = load_site_cg<double, K>(S.b, n);
-                        Site<float, K> rf;
+                    store_site<W, K>(S.xs32, n, zf);
+                    const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
+                    const Site<double, K> bv = load_site<double, K>(S.b, n);
+                    Site<W, K> rf;
 #pragma unroll
-                        for (int i = 0; i < 4 * K; ++i) {
-                            const double rv = bv.v[i] - ax.v[i];
-                            rr = fma(rv, rv, rr);
-                            rf.v[i] = (float)rv;
-                        }
-                        store_site<float, K>(S.r32, n, rf);
+                    for (int i = 0; i < 4 * K; ++i) {
+                        const double rv = bv.v[i] - ax.v[i];
+                        rr = fma(rv, rv, rr);
+                        rf.v[i] = (W)rv;
                     }
-                    const double2 v = block_sum2(rr, 0.0, red);
-                    tile_reduce<MIXED>(a, tile, td.x, S, v, PH_RU, &s_last);
+                    store_site<W, K>(Rb(S, nxt), n, rf);
                 }
-                if (!grid_sync(a.bar, nb, a.err)) return;
+                put_partial(a, tile, 0.0, 0.0, rr, red);
             }
+            if (!gsync(a.bar, a.err)) return;
+            // RU3: t = D_first r
+            for (int tile = tb; tile < te; ++tile) {
+                const SysLocal& L = sl[tslot[tile - tb]];
+                if (!L.active || !L.ru) continue;
+                const SysDev& S = a.sys[L.sys];
+                const int n = a.tiles[tile].y + threadIdx.x;
+                if (n < S.V) store_site<W, K>(S.t32, n, apply_d<W, K>(Rb(S, nxt), n, S, first_dag));
+            }
+            if (!gsync(a.bar, a.err)) return;
+            // RU4: w = D_second t; (r,r), (w,r); z kept
+            for (int tile = tb; tile < te; ++tile) {
+                const SysLocal& L = sl[tslot[tile - tb]];
+                if (!L.active || !L.ru) continue;
+                const SysDev& S = a.sys[L.sys];
+                const int n = a.tiles[tile].y + threadIdx.x;
+                double g = 0.0, d = 0.0;
+                if (n < S.V) {
+                    const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
+                    store_site<W, K>(Wb(S), n, w);
+                    const Site<W, K> r = load_site<W, K>(Rb(S, nxt), n);
+                    g = site_dot<W, K>(r, r).x;
+                    d = site_dot<W, K>(w, r).x;
+                }
+                put_partial(a, tile, g, d, 0.0, red, true);
+            }
+            if (threadIdx.x == 0) {
+                for (int j = 0; j < nsl; ++j)
+                    if (sl[j].active && sl[j].ru) {
+                        sl[j].ru = 0;
+                        sl[j].ru_done = 1;
+                    }
+                s_nru += 1;
+            }
+            if (!gsync(a.bar, a.err)) return;
         }
     }
+    if (threadIdx.x == 0)
+        for (int j = 0; j < nsl; ++j) publish(a, sl[j], s_nru);
 }
 
 // Resets the barrier, counters and activity flags before a solve.
@@ -459,11 +700,13 @@ __global__ void cg_prepare_kernel(CGArgs a)
 {
     for (int i = a.sys_first + threadIdx.x; i < a.sys_first + a.sys_count; i += blockDim.x) {
         a.st[i].counter = 0;
-        a.st[i].active = 0;
+        a.st[i].active = 1;
         a.st[i].iters = 0;
         a.st[i].converged = 0;
         a.st[i].status = 0;
         a.st[i].n_ru = 0;
+        a.st[i].rr = 0.0;
+        a.st[i].rr0 = 0.0;
     }
     if (threadIdx.x == 0) {
         *a.n_active = a.sys_count;
@@ -483,10 +726,19 @@ static int max_coresident(const void* fn, int block)
 }
 
 template <int K, bool MIXED>
+static const void* kernel_of()
+{
+    if constexpr (MIXED)
+        return (const void*)cgcg_kernel<K>;
+    else
+        return (const void*)cg64_kernel<K>;
+}
+
+template <int K, bool MIXED>
 static int max_grid_t()
 {
     static int maxg = -1;
-    if (maxg < 0) maxg = max_coresident((const void*)cg_kernel<K, MIXED>, kBlock);
+    if (maxg < 0) maxg = max_coresident(kernel_of<K, MIXED>(), kBlock);
     return maxg;
 }
 
@@ -496,13 +748,28 @@ int cg_max_grid(int K, bool mixed)
     return mixed ? max_grid_t<2, true>() : max_grid_t<2, false>();
 }
 
-template <int K, bool MIXED>
-static cudaError_t launch_cg_t(const CGArgs& a, cudaStream_t stream, int* grid_out)
+int cg_grid_for(int ntiles, int maxg, int* tiles_per_block)
 {
+    int grid = ntiles < maxg ? ntiles : maxg;
+    if (grid < 1) grid = 1;
+    int tpb = (ntiles + grid - 1) / grid;
+    if (tpb < 1) tpb = 1;
+    grid = (ntiles + tpb - 1) / tpb;
+    if (grid < 1) grid = 1;
+    *tiles_per_block = tpb;
+    return grid;
+}
+
+template <int K, bool MIXED>
+static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out)
+{
+    CGArgs a = a0;
     const int maxg = max_grid_t<K, MIXED>();
     const int nt = a.tile_end - a.tile_begin;
-    int grid = nt < maxg ? nt : maxg;
-    if (grid < 1) grid = 1;
+    int tpb = 1;
+    const int grid = cg_grid_for(nt, maxg, &tpb);
+    if (tpb > kMaxTilesPerBlock || grid > maxg) return cudaErrorInvalidConfiguration;
+    a.tiles_per_block = tpb;
     if (grid_out) *grid_out = grid;
     cg_prepare_kernel<<<1, 256, 0, stream>>>(a);
     cudaLaunchConfig_t cfg = {};
@@ -515,7 +782,10 @@ static cudaError_t launch_cg_t(const CGArgs& a, cudaStream_t stream, int* grid_o
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, cg_kernel<K, MIXED>, a);
+    if constexpr (MIXED)
+        return cudaLaunchKernelEx(&cfg, cgcg_kernel<K>, a);
+    else
+        return cudaLaunchKernelEx(&cfg, cg64_kernel<K>, a);
 }
 
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out)

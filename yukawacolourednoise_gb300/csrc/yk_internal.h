@@ -19,6 +19,7 @@ constexpr int kBlock = 256;   // threads per block of the site kernels
 constexpr int kTile = 256;    // lattice sites per tile (one per thread)
 constexpr int kMaxFFT = 4096; // longest FFT edge handled in shared memory
 constexpr int kMaxDFT = 256;  // longest non-power-of-two edge (direct DFT)
+constexpr int kMaxTilesPerBlock = 512;   // tiles one CG block may own
 
 struct GridBarrier {
     unsigned count;
@@ -41,15 +42,20 @@ struct SysDev {
     double* t64;         // D p (or D x in reliable updates)
     double* Ap64;        // D^dag D p
     // FP32 vectors (mixed solver)
-    float* r32;
-    float* p32[2];
-    float* t32;
-    float* Ap32;
+    float* r32;          // mixed: 2 V sites (r double-buffered)
+    float* p32[2];       // mixed: p, and one of the two s = A p buffers
+    float* t32;          // mixed: 2 V sites (t = D r, w = A r)
+    float* Ap32;         // mixed: the other s = A p buffer
     float* xs32;         // solution increment since the last reliable update
     // noise generation for b: kind/rhs of the Philox stream, or gen = 0
     int gen_eta;
     uint64_t seed;
     const int64_t* step; // device step counter of the chain
+};
+
+// Per-tile reduction slot of the CG kernels.
+struct __align__(16) Partial {
+    double x, y, z, w;
 };
 
 // Per-system CG scalars, written by the finaliser block of each reduction.
@@ -74,7 +80,8 @@ struct CGArgs {
     int tile_begin, tile_end;   // tiles of this solve
     int eta_kind;               // Philox stream kind of generated right-hand sides
     CGState* st;
-    double2* partial;    // one per tile
+    Partial* partial;    // one per tile: (x, y) reduction pair, z FP64 residual
+    int tiles_per_block; // contiguous tile range of each block (set by the launcher)
     GridBarrier* bar;
     int* err;
     int* n_active;

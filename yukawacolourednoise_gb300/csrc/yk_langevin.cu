@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
             C.obs.steps += 1;
             C.obs.cg_iterations = iters;
             C.obs.cg_iterations_total += iters;
+            if (status == YK_ENOCONV) C.obs.noconv_steps += 1;
             C.obs.status = status;
             C.step += 1;
             C.counter = 0;
