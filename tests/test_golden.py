@@ -6,7 +6,7 @@ GPU); test_gpu_golden.py checks the CUDA path against the same vectors.
 Tolerances: operator applications 1e-14 relative (the reference sums in a
 different order and uses FMA contraction); CG solutions at the reference's
 absolute 1e-8 stopping rule 1e-9 relative; noise 1e-13 absolute (cuFFT vs
-radix-2); steps 1e-10 absolute.
+radix-2); steps 1e-10 absolute on the field, 1e-9 relative on eps (it follows max|drift|, whose force carries the CG tolerance).
 """
 import numpy as np
 import pytest
@@ -100,6 +100,6 @@ def test_langevin_steps(gold):
         F, _ = O.force(Nt, Nx, a, phi, cplx(d[f"step_eta{s}"])[None])
         drift = O.bosonic_drift(Nt, Nx, m2, lam, phi, F)
         phi, eps, m = O.euler_update(phi, drift, xi, eps_bar)
-        assert abs(eps - d[f"step_eps{s}"][0]) < 1e-12 * eps
+        assert abs(eps - d[f"step_eps{s}"][0]) < 1e-9 * eps
         assert np.abs(phi - d[f"step_phi{s + 1}"]).max() < 1e-10, s
         phi = d[f"step_phi{s + 1}"]

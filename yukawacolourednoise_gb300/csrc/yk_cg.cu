@@ -42,8 +42,9 @@ struct SysLocal {
     int ru_done;     // the last reduction came from a reliable update
     int last;        // iteration cap reached
     int status;
-    double rr, rr0, stop, alpha, alpha_im, beta, gamma;
-    double sx, sy, sz;   // reduction results of the current phase
+    int iters_ru;    // iteration of the last reliable update (mixed)
+    double rr, rr0, stop, alpha, alpha_im, beta, gamma, gamma_ru;
+    double sx, sy, sz, sw, su;   // reduction results of the current phase
 };
 
 // Sense-reversing grid barrier (one counter word; block 0 adds 2^31 - (n-1),
@@ -92,8 +93,9 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 L.ru_done = 0;
                 L.last = 0;
                 L.status = 0;
-                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = L.gamma = 0.0;
-                L.sx = L.sy = L.sz = 0.0;
+                L.iters_ru = 0;
+                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = L.gamma = L.gamma_ru = 0.0;
+                L.sx = L.sy = L.sz = L.sw = L.su = 0.0;
                 ++n;
                 last = s;
             }
@@ -104,29 +106,49 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
     __syncthreads();
 }
 
-// Sums the partials of every active system of the block (one warp per
-// system, lane-strided over the system's tiles, fixed order).
+// Sums the partials of every active system of the block: one warp per
+// system; lane l adds tiles l, l+32, l+64, ... in order, then a fixed
+// butterfly -- the same bits in every block that reduces the system.  Eight
+// tiles per lane are loaded before they are added, so a 256-tile system
+// costs one L2 round trip.
+template <int NV>
 __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    constexpr int U = 8;
     for (int j = w; j < nsl; j += nw) {
         if (!sl[j].active) continue;
         const SysDev& S = a.sys[sl[j].sys];
-        double x = 0.0, y = 0.0, z = 0.0;
-        for (int i = lane; i < S.ntiles; i += 32) {
-            const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + i);
-            const double2 p0 = __ldcg(q), p1 = __ldcg(q + 1);
-            x += p0.x;
-            y += p0.y;
-            z += p1.x;
+        double acc[2 * NV];
+#pragma unroll
+        for (int q = 0; q < 2 * NV; ++q) acc[q] = 0.0;
+        for (int base = lane; base < S.ntiles; base += 32 * U) {
+            double2 v[U][NV];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int i = base + 32 * u;
+                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + i);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) v[u][c] = (i < S.ntiles) ? __ldcg(q + c) : make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    acc[2 * c] += v[u][c].x;
+                    acc[2 * c + 1] += v[u][c].y;
+                }
         }
-        x = warp_sum(x);
-        y = warp_sum(y);
-        z = warp_sum(z);
+#pragma unroll
+        for (int q = 0; q < 2 * NV; ++q) acc[q] = warp_sum(acc[q]);
         if (lane == 0) {
-            sl[j].sx = x;
-            sl[j].sy = y;
-            sl[j].sz = z;
+            sl[j].sx = acc[0];
+            sl[j].sy = acc[1];
+            if (NV > 1) {
+                sl[j].sz = acc[2 % (2 * NV)];
+                sl[j].sw = acc[3 % (2 * NV)];
+            }
+            if (NV > 2) sl[j].su = acc[4 % (2 * NV)];
         }
     }
     __syncthreads();
@@ -224,19 +246,20 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
     return s;
 }
 
-// Block partial sums -> the tile's partial slot (thread 0).
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double* red,
-                                            bool keep_z = false)
+// Block partial sums -> the tile's partial slot (thread 0), one pass.
+// keep_z: the slot's z (the FP64 residual of a reliable update) is kept.
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double w,
+                                            double u, double* red, bool keep_z = false)
 {
-    const double2 s = block_sum2(x, y, red);
-    double zz = 0.0;
-    if (!keep_z) zz = block_sum2(z, 0.0, red).x;
+    const double4 s = block_sum4(x, y, keep_z ? w : z, keep_z ? u : w, red);
     if (threadIdx.x == 0) {
         Partial p;
         p.x = s.x;
         p.y = s.y;
-        p.z = keep_z ? a.partial[tile].z : zz;
-        p.w = 0.0;
+        p.z = keep_z ? a.partial[tile].z : s.z;
+        p.w = keep_z ? s.z : s.w;
+        p.u = keep_z ? s.w : 0.0;
+        p.v = 0.0;
         a.partial[tile] = p;
     }
 }
@@ -276,7 +299,7 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             store_site<double, K>(S.r64, n, bv);
             store_site<double, K>(S.p64[0], n, bv);
         }
-        put_partial(a, tile, pr, 0.0, 0.0, red);
+        put_partial(a, tile, pr, 0.0, 0.0, 0.0, 0.0, red);
     }
     if (!gsync(a.bar, a.err)) return;
 
@@ -284,7 +307,7 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
         const bool fresh = (k == 0);
         const int cur = k & 1, prv = (k + 1) & 1;
         // ---------------- phase 1: rr -> beta / stop; p_k on the fly; t = D_first p_k
-        reduce_systems(a, sl, nsl);
+        reduce_systems<1>(a, sl, nsl);
         if (threadIdx.x == 0) {
             for (int j = 0; j < nsl; ++j) {
                 SysLocal& L = sl[j];
@@ -350,12 +373,12 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
                 store_site<double, K>(S.Ap64, n, ap);
                 d = site_dot<double, K>(load_site<double, K>(S.p64[cur], n), ap);
             }
-            put_partial(a, tile, d.x, d.y, 0.0, red);
+            put_partial(a, tile, d.x, d.y, 0.0, 0.0, 0.0, red);
         }
         if (!gsync(a.bar, a.err)) return;
 
         // ---------------- phase 3: alpha; x += alpha p, r -= alpha Ap, |r|^2
-        reduce_systems(a, sl, nsl);
+        reduce_systems<1>(a, sl, nsl);
         if (threadIdx.x == 0) {
             for (int j = 0; j < nsl; ++j) {
                 SysLocal& L = sl[j];
@@ -396,7 +419,7 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
 #pragma unroll
                 for (int i = 0; i < 4 * K; ++i) rr = fma(rs.v[i], rs.v[i], rr);
             }
-            put_partial(a, tile, rr, 0.0, 0.0, red);
+            put_partial(a, tile, rr, 0.0, 0.0, 0.0, 0.0, red);
         }
         if (!gsync(a.bar, a.err)) return;
     }
@@ -451,7 +474,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
             store_site<W, K>(Sb(S, 1), n, zf);
             store_site<W, K>(Rb(S, 0), n, bf);
         }
-        put_partial(a, tile, 0.0, 0.0, bb, red);
+        put_partial(a, tile, 0.0, 0.0, bb, 0.0, 0.0, red);
     }
     if (!gsync(a.bar, a.err)) return;
     // ---------------- I1: t = D_first r_0
@@ -473,14 +496,14 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
             g = site_dot<W, K>(r, r).x;
             d = site_dot<W, K>(w, r).x;
         }
-        put_partial(a, tile, g, d, 0.0, red, true);
+        put_partial(a, tile, g, d, 0.0, 0.0, 0.0, red, true);
     }
     if (!gsync(a.bar, a.err)) return;
 
     for (int k = 0; k <= a.max_iter + 1; ++k) {
         const int cur = k & 1, nxt = (k + 1) & 1;
         // ---------------- phase A: reduce; s_k, p_k, xs += alpha p_k, r_{k+1} (on the fly), t = D r_{k+1}
-        reduce_systems(a, sl, nsl);
+        reduce_systems<3>(a, sl, nsl);
         if (threadIdx.x == 0) {
             int want_ru = 0;
             for (int j = 0; j < nsl; ++j) {
@@ -497,28 +520,46 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                     L.beta = 0.0;
                     L.alpha = gam / del;
                     L.gamma = gam;
+                    L.gamma_ru = gam;
+                    L.iters_ru = 0;
                 } else {
                     L.iters += 1;
+                    const double beta = gam / L.gamma;
                     if (L.ru_done) {
-                        // z holds |b - A x|^2 in FP64 from the reliable update
+                        // z holds |b - A x|^2 in FP64 from the reliable update; the
+                        // recurrence restarts from the recomputed r, w with alpha from
+                        // (p, A p) = (r, w) + beta ((r, s) + (p, w)) + beta^2 (p, s)
                         L.ru_done = 0;
                         L.rr = L.sz;
                         if (!isfinite(L.sz)) { retire(a, L, 0, YK_ENAN); continue; }
                         if (!(sqrt(L.sz) > L.stop)) { retire(a, L, 1, 0); continue; }
                         if (L.last) { retire(a, L, 0, YK_ENOCONV); continue; }
+                        const double pap = del + beta * L.sw + beta * beta * L.su;
+                        L.alpha = gam / pap;
+                        L.gamma_ru = gam;
+                        L.iters_ru = L.iters;
                     } else {
                         L.rr = gam;
+                        const double den = del - beta * gam / L.alpha;
+                        L.alpha = gam / den;
                     }
-                    const double beta = gam / L.gamma;
-                    const double den = del - beta * gam / L.alpha;
                     L.beta = beta;
-                    L.alpha = gam / den;
                     L.gamma = gam;
                 }
-                if (!isfinite(L.alpha) || !isfinite(L.beta)) { retire(a, L, 0, YK_ENAN); continue; }
-                // reliable update after this iteration?
-                const bool cand = !(sqrt(gam) > L.stop);
-                const bool due = a.reliable_every > 0 && ((L.iters + 1) % a.reliable_every) == 0;
+                if (!isfinite(gam) || !isfinite(L.beta)) {
+                    retire(a, L, 0, YK_ENAN);
+                    continue;
+                }
+                // a breakdown of the short recurrence (alpha <= 0 from rounding):
+                // no update this iteration and a reliable update, which recomputes
+                // alpha from (p, A p)
+                const bool broken = !isfinite(L.alpha) || !(L.alpha > 0.0);
+                if (broken) L.alpha = 0.0;
+                // reliable update after this iteration: residual down 100x since the
+                // last one, FP32 residual below the target, interval, or the cap
+                const bool cand = broken || !(sqrt(gam) > L.stop);
+                const bool drop = gam < 1e-4 * L.gamma_ru;
+                const bool due = drop || (a.reliable_every > 0 && (L.iters + 1 - L.iters_ru) >= a.reliable_every);
                 const bool cap = (L.iters + 1) >= a.max_iter;
                 if (cand || due || cap) {
                     L.ru = 1;
@@ -594,7 +635,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 g = site_dot<W, K>(r, r).x;
                 d = site_dot<W, K>(w, r).x;
             }
-            put_partial(a, tile, g, d, 0.0, red);
+            put_partial(a, tile, g, d, 0.0, 0.0, 0.0, red);
         }
         if (!gsync(a.bar, a.err)) return;
 
@@ -652,7 +693,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                     }
                     store_site<W, K>(Rb(S, nxt), n, rf);
                 }
-                put_partial(a, tile, 0.0, 0.0, rr, red);
+                put_partial(a, tile, 0.0, 0.0, rr, 0.0, 0.0, red);
             }
             if (!gsync(a.bar, a.err)) return;
             // RU3: t = D_first r
@@ -664,21 +705,25 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 if (n < S.V) store_site<W, K>(S.t32, n, apply_d<W, K>(Rb(S, nxt), n, S, first_dag));
             }
             if (!gsync(a.bar, a.err)) return;
-            // RU4: w = D_second t; (r,r), (w,r); z kept
+            // RU4: w = D_second t; (r,r), (w,r), (r,s_k) + (p_k,w), (p_k,s_k); z kept
             for (int tile = tb; tile < te; ++tile) {
                 const SysLocal& L = sl[tslot[tile - tb]];
                 if (!L.active || !L.ru) continue;
                 const SysDev& S = a.sys[L.sys];
                 const int n = a.tiles[tile].y + threadIdx.x;
-                double g = 0.0, d = 0.0;
+                double g = 0.0, d = 0.0, c1 = 0.0, c2 = 0.0;
                 if (n < S.V) {
                     const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
                     store_site<W, K>(Wb(S), n, w);
                     const Site<W, K> r = load_site<W, K>(Rb(S, nxt), n);
+                    const Site<W, K> sk = load_site<W, K>(Sb(S, cur), n);
+                    const Site<W, K> pk = load_site<W, K>(S.p32[0], n);
                     g = site_dot<W, K>(r, r).x;
                     d = site_dot<W, K>(w, r).x;
+                    c1 = site_dot<W, K>(r, sk).x + site_dot<W, K>(pk, w).x;
+                    c2 = site_dot<W, K>(pk, sk).x;
                 }
-                put_partial(a, tile, g, d, 0.0, red, true);
+                put_partial(a, tile, g, d, 0.0, c1, c2, red, true);
             }
             if (threadIdx.x == 0) {
                 for (int j = 0; j < nsl; ++j)

@@ -55,7 +55,7 @@ struct SysDev {
 
 // Per-tile reduction slot of the CG kernels.
 struct __align__(16) Partial {
-    double x, y, z, w;
+    double x, y, z, w, u, v;
 };
 
 // Per-system CG scalars, written by the finaliser block of each reduction.
