@@ -37,8 +37,8 @@ def _sources():
     return sorted(p for p in CSRC.iterdir() if p.suffix in (".cu", ".cpp") and p.name != "yk_run_main.cpp")
 
 
-def _compile(src: Path, extra: list[str]) -> Path:
-    obj = BUILD / (src.stem + ".o")
+def _compile(src: Path, extra: list[str], build_dir: Path) -> Path:
+    obj = build_dir / (src.stem + ".o")
     deps = [src] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "yukawa.h"]
     if obj.exists() and obj.stat().st_mtime > max(d.stat().st_mtime for d in deps):
         return obj
@@ -55,11 +55,14 @@ def _compile(src: Path, extra: list[str]) -> Path:
 def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     """Compile every translation unit for sm_103a and link the library and CLI."""
     extra = list(extra or [])
-    BUILD.mkdir(exist_ok=True)
+    # objects of a build with extra flags live apart from the default build's
+    build_dir = BUILD if not extra else BUILD.with_name(BUILD.name + "_" + "_".join(
+        f.strip("-").replace("=", "_") for f in extra))
+    build_dir.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
+        objs = list(ex.map(lambda s: _compile(s, extra, build_dir), srcs))
     cmd = [nvcc()] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -21,12 +21,50 @@
 // contiguous range of 256-site tiles; a bounded sense-reversing grid barrier
 // separates phases; reductions are deterministic (per-tile partials, summed
 // in tile order by every block that needs them, right after the barrier).
+#include <cstdio>
 #include <type_traits>
 
 #include "yk_common.cuh"
 #include "yk_kernels.h"
 
 namespace yk {
+
+#ifdef YK_CG_CHECKED
+// Self-checking build: every site access of the CG kernels is checked
+// against the system's volume and for null buffers; the first bad access is
+// printed with its source line and skipped.
+__device__ int g_cg_bad;
+
+template <typename R, int K>
+__device__ Site<R, K> chk_ld(const R* p, int64_t n, int V, int line)
+{
+    if (p == nullptr || n < 0 || n >= V) {
+        if (atomicCAS(&g_cg_bad, 0, line) == 0)
+            printf("cg check: bad load line %d ptr %p n %lld V %d block %d\n", line, p, (long long)n, V, blockIdx.x);
+        Site<R, K> z;
+#pragma unroll
+        for (int i = 0; i < 4 * K; ++i) z.v[i] = R(0);
+        return z;
+    }
+    return load_site<R, K>(p, n);
+}
+
+template <typename R, int K>
+__device__ void chk_st(R* p, int64_t n, const Site<R, K>& v, int V, int line)
+{
+    if (p == nullptr || n < 0 || n >= V) {
+        if (atomicCAS(&g_cg_bad, 0, line) == 0)
+            printf("cg check: bad store line %d ptr %p n %lld V %d block %d\n", line, p, (long long)n, V, blockIdx.x);
+        return;
+    }
+    store_site<R, K>(p, n, v);
+}
+#define YK_LD(R, K, p, n) chk_ld<R, K>((p), (n), S.V, __LINE__)
+#define YK_ST(R, K, p, n, v) chk_st<R, K>((p), (n), (v), S.V, __LINE__)
+#else
+#define YK_LD(R, K, p, n) load_site<R, K>((p), (n))
+#define YK_ST(R, K, p, n, v) store_site<R, K>((p), (n), (v))
+#endif
 
 namespace {
 
@@ -126,10 +164,16 @@ __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
             double2 v[U][NV];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
+                // the load address is clamped into the system's tiles, so a load the
+                // compiler issues ahead of the range test never leaves the array
                 const int i = base + 32 * u;
-                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + i);
+                const int ii = i < S.ntiles ? i : S.ntiles - 1;
+                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
 #pragma unroll
-                for (int c = 0; c < NV; ++c) v[u][c] = (i < S.ntiles) ? __ldcg(q + c) : make_double2(0.0, 0.0);
+                for (int c = 0; c < NV; ++c) {
+                    const double2 t = __ldcg(q + c);
+                    v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
+                }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
@@ -186,11 +230,11 @@ template <typename W, int K>
 __device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& S, bool dag)
 {
     const Nbr nb = neighbours(n, S.Nt, S.Nx);
-    const Site<W, K> c = load_site<W, K>(in, n);
-    const Site<W, K> tu = load_site<W, K>(in, nb.tu);
-    const Site<W, K> td = load_site<W, K>(in, nb.td);
-    const Site<W, K> xu = load_site<W, K>(in, nb.xu);
-    const Site<W, K> xd = load_site<W, K>(in, nb.xd);
+    const Site<W, K> c = YK_LD(W, K, in, n);
+    const Site<W, K> tu = YK_LD(W, K, in, nb.tu);
+    const Site<W, K> td = YK_LD(W, K, in, nb.td);
+    const Site<W, K> xu = YK_LD(W, K, in, nb.xu);
+    const Site<W, K> xd = YK_LD(W, K, in, nb.xd);
     const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
     return dag ? dirac_combine<W, K, true>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm)
                : dirac_combine<W, K, false>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm);
@@ -248,10 +292,8 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
 
 // Block partial sums -> the tile's partial slot (thread 0), one pass.
 // keep_z: the slot's z (the FP64 residual of a reliable update) is kept.
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double w,
-                                            double u, double* red, bool keep_z = false)
+__device__ __forceinline__ void store_partial(const CGArgs& a, int tile, const double4& s, bool keep_z)
 {
-    const double4 s = block_sum4(x, y, keep_z ? w : z, keep_z ? u : w, red);
     if (threadIdx.x == 0) {
         Partial p;
         p.x = s.x;
@@ -260,8 +302,37 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x,
         p.w = keep_z ? s.z : s.w;
         p.u = keep_z ? s.w : 0.0;
         p.v = 0.0;
+#ifdef YK_CG_CHECKED
+        if (tile < 0 || tile >= a.tile_end) {
+            if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d end %d\n", tile, a.tile_end);
+            return;
+        }
+#endif
         a.partial[tile] = p;
     }
+}
+
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double w,
+                                            double u, double* red, bool keep_z = false)
+{
+    store_partial(a, tile, block_sum4(x, y, keep_z ? w : z, keep_z ? u : w, red), keep_z);
+}
+
+// FP32 per-site values: FP32 within each warp, FP64 above (block_sum4f).
+__device__ __forceinline__ void put_partial_f(const CGArgs& a, int tile, float x, float y, float z, float w,
+                                              float u, double* red, bool keep_z = false)
+{
+    store_partial(a, tile, block_sum4f(x, y, keep_z ? w : z, keep_z ? u : w, red), keep_z);
+}
+
+// Real part of sum conj(a) b over one site, in the vectors' own precision.
+template <int K>
+__device__ __forceinline__ float site_dotf(const Site<float, K>& a, const Site<float, K>& b)
+{
+    float re = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4 * K; ++i) re = fmaf(a.v[i], b.v[i], re);
+    return re;
 }
 
 }  // namespace
@@ -287,17 +358,17 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
         const int n = a.tiles[tile].y + threadIdx.x;
         double pr = 0.0;
         if (n < S.V) {
-            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
-            if (S.gen_eta) store_site<double, K>(S.b, n, bv);
+            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+            if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
             Site<double, K> z;
 #pragma unroll
             for (int i = 0; i < 4 * K; ++i) {
                 z.v[i] = 0.0;
                 pr = fma(bv.v[i], bv.v[i], pr);
             }
-            store_site<double, K>(S.x, n, z);
-            store_site<double, K>(S.r64, n, bv);
-            store_site<double, K>(S.p64[0], n, bv);
+            YK_ST(double, K, S.x, n, z);
+            YK_ST(double, K, S.r64, n, bv);
+            YK_ST(double, K, S.p64[0], n, bv);
         }
         put_partial(a, tile, pr, 0.0, 0.0, 0.0, 0.0, red);
     }
@@ -341,9 +412,9 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const double* pold = S.p64[fresh ? 0 : prv];
             const Nbr nbr = neighbours(n, S.Nt, S.Nx);
             auto p_at = [&](int64_t m) {
-                Site<double, K> po = load_site<double, K>(pold, m);
+                Site<double, K> po = YK_LD(double, K, pold, m);
                 if (!fresh) {
-                    const Site<double, K> rv = load_site<double, K>(S.r64, m);
+                    const Site<double, K> rv = YK_LD(double, K, S.r64, m);
 #pragma unroll
                     for (int i = 0; i < 4 * K; ++i) po.v[i] = fma(beta, po.v[i], rv.v[i]);
                 }
@@ -355,8 +426,8 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const Site<double, K> o = first_dag
                 ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
                 : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
-            store_site<double, K>(S.t64, n, o);
-            if (!fresh) store_site<double, K>(S.p64[cur], n, c);
+            YK_ST(double, K, S.t64, n, o);
+            if (!fresh) YK_ST(double, K, S.p64[cur], n, c);
         }
         if (!gsync(a.bar, a.err)) return;
         if (*(volatile int*)a.n_active == 0) break;
@@ -370,8 +441,8 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             double2 d = make_double2(0.0, 0.0);
             if (n < S.V) {
                 const Site<double, K> ap = apply_d<double, K>(S.t64, n, S, !first_dag);
-                store_site<double, K>(S.Ap64, n, ap);
-                d = site_dot<double, K>(load_site<double, K>(S.p64[cur], n), ap);
+                YK_ST(double, K, S.Ap64, n, ap);
+                d = site_dot<double, K>(YK_LD(double, K, S.p64[cur], n), ap);
             }
             put_partial(a, tile, d.x, d.y, 0.0, 0.0, 0.0, red);
         }
@@ -408,14 +479,14 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const int n = a.tiles[tile].y + threadIdx.x;
             double rr = 0.0;
             if (n < S.V) {
-                const Site<double, K> pv = load_site<double, K>(S.p64[cur], n);
-                const Site<double, K> ap = load_site<double, K>(S.Ap64, n);
-                Site<double, K> xs = load_site<double, K>(S.x, n);
-                Site<double, K> rs = load_site<double, K>(S.r64, n);
+                const Site<double, K> pv = YK_LD(double, K, S.p64[cur], n);
+                const Site<double, K> ap = YK_LD(double, K, S.Ap64, n);
+                Site<double, K> xs = YK_LD(double, K, S.x, n);
+                Site<double, K> rs = YK_LD(double, K, S.r64, n);
                 site_axpy<double, K>(xs, L.alpha, L.alpha_im, pv);
                 site_axpy<double, K>(rs, -L.alpha, -L.alpha_im, ap);
-                store_site<double, K>(S.x, n, xs);
-                store_site<double, K>(S.r64, n, rs);
+                YK_ST(double, K, S.x, n, xs);
+                YK_ST(double, K, S.r64, n, rs);
 #pragma unroll
                 for (int i = 0; i < 4 * K; ++i) rr = fma(rs.v[i], rs.v[i], rr);
             }
@@ -457,8 +528,8 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
         const int n = a.tiles[tile].y + threadIdx.x;
         double bb = 0.0;
         if (n < S.V) {
-            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
-            if (S.gen_eta) store_site<double, K>(S.b, n, bv);
+            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+            if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
             Site<double, K> z;
             Site<W, K> bf, zf;
 #pragma unroll
@@ -468,11 +539,11 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 bf.v[i] = (W)bv.v[i];
                 bb = fma(bv.v[i], bv.v[i], bb);
             }
-            store_site<double, K>(S.x, n, z);
-            store_site<W, K>(S.xs32, n, zf);
-            store_site<W, K>(S.p32[0], n, zf);
-            store_site<W, K>(Sb(S, 1), n, zf);
-            store_site<W, K>(Rb(S, 0), n, bf);
+            YK_ST(double, K, S.x, n, z);
+            YK_ST(W, K, S.xs32, n, zf);
+            YK_ST(W, K, S.p32[0], n, zf);
+            YK_ST(W, K, Sb(S, 1), n, zf);
+            YK_ST(W, K, Rb(S, 0), n, bf);
         }
         put_partial(a, tile, 0.0, 0.0, bb, 0.0, 0.0, red);
     }
@@ -481,22 +552,22 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
     for (int tile = tb; tile < te; ++tile) {
         const SysDev& S = a.sys[a.tiles[tile].x];
         const int n = a.tiles[tile].y + threadIdx.x;
-        if (n < S.V) store_site<W, K>(S.t32, n, apply_d<W, K>(Rb(S, 0), n, S, first_dag));
+        if (n < S.V) YK_ST(W, K, S.t32, n, (apply_d<W, K>(Rb(S, 0), n, S, first_dag)));
     }
     if (!gsync(a.bar, a.err)) return;
     // ---------------- I2: w_0 = D_second t; (r,r), (w,r); |b|^2 kept in z
     for (int tile = tb; tile < te; ++tile) {
         const SysDev& S = a.sys[a.tiles[tile].x];
         const int n = a.tiles[tile].y + threadIdx.x;
-        double g = 0.0, d = 0.0;
+        float g = 0.f, d = 0.f;
         if (n < S.V) {
             const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-            store_site<W, K>(Wb(S), n, w);
-            const Site<W, K> r = load_site<W, K>(Rb(S, 0), n);
-            g = site_dot<W, K>(r, r).x;
-            d = site_dot<W, K>(w, r).x;
+            YK_ST(W, K, Wb(S), n, w);
+            const Site<W, K> r = YK_LD(W, K, Rb(S, 0), n);
+            g = site_dotf<K>(r, r);
+            d = site_dotf<K>(w, r);
         }
-        put_partial(a, tile, g, d, 0.0, 0.0, 0.0, red, true);
+        put_partial_f(a, tile, g, d, 0.f, 0.f, 0.f, red, true);
     }
     if (!gsync(a.bar, a.err)) return;
 
@@ -583,9 +654,9 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
             const Nbr nbr = neighbours(n, S.Nt, S.Nx);
             // r_{k+1}(m) = r_k(m) - alpha (w_k(m) + beta s_{k-1}(m))
             auto rnext = [&](int64_t m, Site<W, K>* s_out) {
-                const Site<W, K> rv = load_site<W, K>(Rc, m);
-                const Site<W, K> wv = load_site<W, K>(Wk, m);
-                const Site<W, K> sv = load_site<W, K>(Sp, m);
+                const Site<W, K> rv = YK_LD(W, K, Rc, m);
+                const Site<W, K> wv = YK_LD(W, K, Wk, m);
+                const Site<W, K> sv = YK_LD(W, K, Sp, m);
                 Site<W, K> o;
 #pragma unroll
                 for (int i = 0; i < 4 * K; ++i) {
@@ -600,23 +671,23 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
             const Site<W, K> tu = rnext(nbr.tu, nullptr), tdn = rnext(nbr.td, nullptr);
             const Site<W, K> xu = rnext(nbr.xu, nullptr), xd = rnext(nbr.xd, nullptr);
             // p_k = r_k + beta p_{k-1}; xs += alpha p_k
-            const Site<W, K> rk = load_site<W, K>(Rc, n);
-            Site<W, K> pk = load_site<W, K>(S.p32[0], n);
-            Site<W, K> xs = load_site<W, K>(S.xs32, n);
+            const Site<W, K> rk = YK_LD(W, K, Rc, n);
+            Site<W, K> pk = YK_LD(W, K, S.p32[0], n);
+            Site<W, K> xs = YK_LD(W, K, S.xs32, n);
 #pragma unroll
             for (int i = 0; i < 4 * K; ++i) {
                 pk.v[i] = fma(be, pk.v[i], rk.v[i]);
                 xs.v[i] = fma(al, pk.v[i], xs.v[i]);
             }
-            store_site<W, K>(S.p32[0], n, pk);
-            store_site<W, K>(S.xs32, n, xs);
-            store_site<W, K>(Sb(S, cur), n, sk);
-            store_site<W, K>(Rb(S, nxt), n, c);
+            YK_ST(W, K, S.p32[0], n, pk);
+            YK_ST(W, K, S.xs32, n, xs);
+            YK_ST(W, K, Sb(S, cur), n, sk);
+            YK_ST(W, K, Rb(S, nxt), n, c);
             const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
             const Site<W, K> t = first_dag
                 ? dirac_combine<W, K, true>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm)
                 : dirac_combine<W, K, false>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm);
-            store_site<W, K>(S.t32, n, t);
+            YK_ST(W, K, S.t32, n, t);
         }
         if (!gsync(a.bar, a.err)) return;
         if (*(volatile int*)a.n_active == 0) break;
@@ -627,15 +698,15 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
             if (!L.active) continue;
             const SysDev& S = a.sys[L.sys];
             const int n = a.tiles[tile].y + threadIdx.x;
-            double g = 0.0, d = 0.0;
+            float g = 0.f, d = 0.f;
             if (n < S.V) {
                 const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-                store_site<W, K>(Wb(S), n, w);
-                const Site<W, K> r = load_site<W, K>(Rb(S, nxt), n);
-                g = site_dot<W, K>(r, r).x;
-                d = site_dot<W, K>(w, r).x;
+                YK_ST(W, K, Wb(S), n, w);
+                const Site<W, K> r = YK_LD(W, K, Rb(S, nxt), n);
+                g = site_dotf<K>(r, r);
+                d = site_dotf<K>(w, r);
             }
-            put_partial(a, tile, g, d, 0.0, 0.0, 0.0, red);
+            put_partial_f(a, tile, g, d, 0.f, 0.f, 0.f, red);
         }
         if (!gsync(a.bar, a.err)) return;
 
@@ -649,8 +720,8 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 if (n >= S.V) continue;
                 const Nbr nbr = neighbours(n, S.Nt, S.Nx);
                 auto xat = [&](int64_t m) {
-                    Site<double, K> xv = load_site<double, K>(S.x, m);
-                    const Site<W, K> xs = load_site<W, K>(S.xs32, m);
+                    Site<double, K> xv = YK_LD(double, K, S.x, m);
+                    const Site<W, K> xs = YK_LD(W, K, S.xs32, m);
 #pragma unroll
                     for (int i = 0; i < 4 * K; ++i) xv.v[i] += (double)xs.v[i];
                     return xv;
@@ -661,7 +732,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 const Site<double, K> t = first_dag
                     ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
                     : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
-                store_site<double, K>(S.t64, n, t);
+                YK_ST(double, K, S.t64, n, t);
             }
             if (!gsync(a.bar, a.err)) return;
             // RU2: x += xs, xs = 0; r = b - D_second t64 (FP64) -> r_{k+1}; |r|^2 in z
@@ -672,18 +743,18 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 const int n = a.tiles[tile].y + threadIdx.x;
                 double rr = 0.0;
                 if (n < S.V) {
-                    Site<double, K> xv = load_site<double, K>(S.x, n);
-                    const Site<W, K> xs = load_site<W, K>(S.xs32, n);
+                    Site<double, K> xv = YK_LD(double, K, S.x, n);
+                    const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
                     Site<W, K> zf;
 #pragma unroll
                     for (int i = 0; i < 4 * K; ++i) {
                         xv.v[i] += (double)xs.v[i];
                         zf.v[i] = 0.f;
                     }
-                    store_site<double, K>(S.x, n, xv);
-                    store_site<W, K>(S.xs32, n, zf);
+                    YK_ST(double, K, S.x, n, xv);
+                    YK_ST(W, K, S.xs32, n, zf);
                     const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
-                    const Site<double, K> bv = load_site<double, K>(S.b, n);
+                    const Site<double, K> bv = YK_LD(double, K, S.b, n);
                     Site<W, K> rf;
 #pragma unroll
                     for (int i = 0; i < 4 * K; ++i) {
@@ -691,7 +762,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                         rr = fma(rv, rv, rr);
                         rf.v[i] = (W)rv;
                     }
-                    store_site<W, K>(Rb(S, nxt), n, rf);
+                    YK_ST(W, K, Rb(S, nxt), n, rf);
                 }
                 put_partial(a, tile, 0.0, 0.0, rr, 0.0, 0.0, red);
             }
@@ -702,7 +773,7 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 if (!L.active || !L.ru) continue;
                 const SysDev& S = a.sys[L.sys];
                 const int n = a.tiles[tile].y + threadIdx.x;
-                if (n < S.V) store_site<W, K>(S.t32, n, apply_d<W, K>(Rb(S, nxt), n, S, first_dag));
+                if (n < S.V) YK_ST(W, K, S.t32, n, (apply_d<W, K>(Rb(S, nxt), n, S, first_dag)));
             }
             if (!gsync(a.bar, a.err)) return;
             // RU4: w = D_second t; (r,r), (w,r), (r,s_k) + (p_k,w), (p_k,s_k); z kept
@@ -711,19 +782,19 @@ __global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
                 if (!L.active || !L.ru) continue;
                 const SysDev& S = a.sys[L.sys];
                 const int n = a.tiles[tile].y + threadIdx.x;
-                double g = 0.0, d = 0.0, c1 = 0.0, c2 = 0.0;
+                float g = 0.f, d = 0.f, c1 = 0.f, c2 = 0.f;
                 if (n < S.V) {
                     const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-                    store_site<W, K>(Wb(S), n, w);
-                    const Site<W, K> r = load_site<W, K>(Rb(S, nxt), n);
-                    const Site<W, K> sk = load_site<W, K>(Sb(S, cur), n);
-                    const Site<W, K> pk = load_site<W, K>(S.p32[0], n);
-                    g = site_dot<W, K>(r, r).x;
-                    d = site_dot<W, K>(w, r).x;
-                    c1 = site_dot<W, K>(r, sk).x + site_dot<W, K>(pk, w).x;
-                    c2 = site_dot<W, K>(pk, sk).x;
+                    YK_ST(W, K, Wb(S), n, w);
+                    const Site<W, K> r = YK_LD(W, K, Rb(S, nxt), n);
+                    const Site<W, K> sk = YK_LD(W, K, Sb(S, cur), n);
+                    const Site<W, K> pk = YK_LD(W, K, S.p32[0], n);
+                    g = site_dotf<K>(r, r);
+                    d = site_dotf<K>(w, r);
+                    c1 = site_dotf<K>(r, sk) + site_dotf<K>(pk, w);
+                    c2 = site_dotf<K>(pk, sk);
                 }
-                put_partial(a, tile, g, d, 0.0, c1, c2, red, true);
+                put_partial_f(a, tile, g, d, 0.f, c1, c2, red, true);
             }
             if (threadIdx.x == 0) {
                 for (int j = 0; j < nsl; ++j)
