@@ -620,6 +620,9 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     }
     ar.base = (char*)ctx->mem;
     YK_CK(cudaMemsetAsync(ctx->mem, 0, ar.used, ctx->stream));
+    // the synchronous uploads below run on the legacy stream, which does not
+    // wait for the context's non-blocking stream
+    YK_CK(cudaStreamSynchronize(ctx->stream));
 
     ctx->d_chains = ar.at<ChainDev>(o_chains);
     ctx->d_sys = ar.at<SysDev>(o_sys);

@@ -171,7 +171,7 @@ __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
                 const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
 #pragma unroll
                 for (int c = 0; c < NV; ++c) {
-                    const double2 t = __ldcg(q + c);
+                    const double2 t = ld_volatile2(q + c);
                     v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
                 }
             }

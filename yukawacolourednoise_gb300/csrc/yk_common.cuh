@@ -45,23 +45,17 @@ __device__ __forceinline__ Site<R, K> load_site(const R* base, int64_t n)
     return s;
 }
 
-// L2-only load: for data other blocks of a persistent kernel wrote earlier in
-// the same launch (L1 is not coherent across SMs).
-template <typename R, int K>
-__device__ __forceinline__ Site<R, K> load_site_cg(const R* base, int64_t n)
+// Coherent 16-byte load of data that other blocks of the same launch wrote
+// before the last grid barrier.  A volatile access: the compiler neither
+// caches nor speculates it (the __ldcg/__ldg intrinsics are plain inline asm
+// that it may hoist, merge or issue ahead of a bounds test).
+__device__ __forceinline__ double2 ld_volatile2(const double2* p)
 {
-    Site<R, K> s;
-    const float4* p = reinterpret_cast<const float4*>(base + n * (4 * K));
-    constexpr int NV = (int)(sizeof(R) * 4 * K / 16);
-    constexpr int PER = (int)(16 / sizeof(R));
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        const float4 a = __ldcg(p + i);
-#pragma unroll
-        for (int j = 0; j < PER; ++j) s.v[i * PER + j] = reinterpret_cast<const R*>(&a)[j];
-    }
-    return s;
+    const volatile double* q = reinterpret_cast<const volatile double*>(p);
+    return make_double2(q[0], q[1]);
 }
+
+__device__ __forceinline__ double ld_volatile(const double* p) { return *reinterpret_cast<const volatile double*>(p); }
 
 template <typename R, int K>
 __device__ __forceinline__ void store_site(R* base, int64_t n, const Site<R, K>& s)

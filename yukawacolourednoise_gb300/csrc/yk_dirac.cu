@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kBlock) dirac_kernel(const R* __restrict__ in,
         const Site<R, K> td = load_site<R, K>(in, nb.td);
         const Site<R, K> xu = load_site<R, K>(in, nb.xu);
         const Site<R, K> xd = load_site<R, K>(in, nb.xd);
-        const R diag = (R)(2.0 * r + m0 + g * __ldg(sigma + n));
+        const R diag = (R)(2.0 * r + m0 + g * sigma[n]);
         const Site<R, K> o = dirac_combine<R, K, DAG>(c, tu, td, xu, xd, diag, rr, (R)nb.sp, (R)nb.sm);
         store_site<R, K>(out, n, o);
     }

@@ -134,10 +134,10 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
         const int lane = threadIdx.x;
         double a = 0.0, b = 0.0, f = 0.0;
         for (int i = lane; i < C.ntiles; i += 32) {
-            const double2 q = __ldcg(s.tile_sum + C.tile0 + i);
+            const double2 q = ld_volatile2(s.tile_sum + C.tile0 + i);
             a += q.x;
             b += q.y;
-            f += __ldcg(s.tile_sum2 + C.tile0 + i);
+            f += ld_volatile(s.tile_sum2 + C.tile0 + i);
         }
         a = warp_sum(a);
         b = warp_sum(b);

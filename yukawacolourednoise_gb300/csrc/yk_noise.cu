@@ -46,7 +46,7 @@ __device__ void smem_fft(double2* buf, double2* tmp, int N, int nseq, int sj, in
                 const int c = idx / (N >> 1), bidx = idx - c * (N >> 1);
                 const int grp = bidx / h, k = bidx - grp * h;
                 const int i0 = grp * len + k, i1 = i0 + h;
-                double2 w = __ldg(tw + k * step);
+                double2 w = tw[k * step];
                 if (inverse) w.y = -w.y;
                 double2* pa = buf + i0 * sj + c * sc;
                 double2* pb = buf + i1 * sj + c * sc;
@@ -62,7 +62,7 @@ __device__ void smem_fft(double2* buf, double2* tmp, int N, int nseq, int sj, in
             const int c = idx / N, k = idx - c * N;
             double sr = 0.0, si = 0.0;
             for (int j = 0; j < N; ++j) {
-                double2 w = __ldg(tw + (int)(((long long)j * k) % N));
+                double2 w = tw[(int)(((long long)j * k) % N)];
                 if (inverse) w.y = -w.y;
                 const double2 x = buf[j * sj + c * sc];
                 sr += x.x * w.x - x.y * w.y;
