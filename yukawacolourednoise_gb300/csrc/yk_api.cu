@@ -584,10 +584,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             o.x = ar.reserve(d);
             o.t64 = ar.reserve(d);
             if (mixed) {
-                o.r32 = ar.reserve(2 * f);
+                o.r32 = ar.reserve(f);
                 o.q0 = ar.reserve(f);
                 o.q1 = ar.reserve(f);
-                o.t32 = ar.reserve(2 * f);
+                o.t32 = ar.reserve(f);
                 o.ap32 = ar.reserve(f);
                 o.xs = ar.reserve(f);
             } else {

@@ -1,26 +1,21 @@
 // yk_cg.cu -- batched CG on D^dag D (or D D^dag) as one persistent
-// cooperative kernel per solve.
+// cooperative kernel per solve: the algorithm of code/src/CGsolver.cu:72-170
+// -- x0 = 0, r = p = b, alpha = |r|^2 / <p, A p>, x += alpha p,
+// r -= alpha A p, beta = |r'|^2 / |r|^2, p = r + beta p, stop when
+// sqrt(|r|^2) <= tol -- in three phases per iteration (the reference pays 15
+// grid syncs): p is formed on the fly inside the first D apply
+// (double-buffered), the second D apply carries <p, Ap>, the axpys carry |r|^2.
 //
-// FP64 (cg64_kernel): the algorithm of code/src/CGsolver.cu:72-170 --
-//   x0 = 0, r = p = b, alpha = |r|^2 / <p, A p>, x += alpha p,
-//   r -= alpha A p, beta = |r'|^2 / |r|^2, p = r + beta p, stop when
-//   sqrt(|r|^2) <= tol -- in three phases per iteration (the reference pays
-//   15 grid syncs): p is formed on the fly inside the first D apply
-//   (double-buffered), the second D apply carries <p, Ap>, the axpys carry |r|^2.
+// FP64: every vector and scalar in FP64.  MIXED: FP32 vectors and stencils,
+// FP64 partial sums and scalars, FP64 reliable updates (the solution is kept
+// as an FP64 x plus an FP32 increment; r = b - A x is recomputed in FP64
+// when the FP32 residual claims convergence, every `reliable_every`
+// iterations and at the cap; convergence is only declared on that residual).
 //
-// MIXED (cgcg_kernel): Chronopoulos-Gear CG (one fused reduction of (r, r)
-//   and (A r, r) per iteration) on FP32 vectors with FP64 partial sums, in two
-//   phases per iteration: r_{k+1} = r_k - alpha (w_k + beta s_{k-1}) is formed
-//   on the fly at the four neighbours inside D, and D^dag follows.  Every
-//   `reliable_every` iterations, when the FP32 residual claims convergence,
-//   or at the iteration cap, an FP64 reliable update folds the FP32 solution
-//   increment into the FP64 solution and recomputes r = b - A x in FP64;
-//   convergence is only declared on that FP64 residual.
-//
-// Both: one launch solves every (chain, rhs) system; each block owns a
-// contiguous range of 256-site tiles; a bounded sense-reversing grid barrier
-// separates phases; reductions are deterministic (per-tile partials, summed
-// in tile order by every block that needs them, right after the barrier).
+// One launch solves every (chain, rhs) system; each block owns a contiguous
+// range of 256-site tiles; a bounded sense-reversing grid barrier separates
+// phases; reductions are deterministic (per-tile partials, summed in tile
+// order by every block that needs them, right after the barrier).
 #include <cstdio>
 #include <type_traits>
 
@@ -78,11 +73,10 @@ struct SysLocal {
     int iters;
     int ru;          // reliable update pending (mixed)
     int ru_done;     // the last reduction came from a reliable update
-    int last;        // iteration cap reached
+    int go;          // phase 1 forms p and t for this system in this pass
     int status;
-    int iters_ru;    // iteration of the last reliable update (mixed)
-    double rr, rr0, stop, alpha, alpha_im, beta, gamma, gamma_ru;
-    double sx, sy, sz, sw, su;   // reduction results of the current phase
+    double rr, rr0, stop, alpha, alpha_im, beta;
+    double sx, sy;   // reduction results of the current phase
 };
 
 // Sense-reversing grid barrier (one counter word; block 0 adds 2^31 - (n-1),
@@ -129,11 +123,10 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 L.iters = 0;
                 L.ru = 0;
                 L.ru_done = 0;
-                L.last = 0;
+                L.go = 0;
                 L.status = 0;
-                L.iters_ru = 0;
-                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = L.gamma = L.gamma_ru = 0.0;
-                L.sx = L.sy = L.sz = L.sw = L.su = 0.0;
+                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = 0.0;
+                L.sx = L.sy = 0.0;
                 ++n;
                 last = s;
             }
@@ -144,12 +137,11 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
     __syncthreads();
 }
 
-// Sums the partials of every active system of the block: one warp per
-// system; lane l adds tiles l, l+32, l+64, ... in order, then a fixed
+// Sums the (x, y) partials of every active system of the block: one warp
+// per system; lane l adds tiles l, l+32, l+64, ... in order, then a fixed
 // butterfly -- the same bits in every block that reduces the system.  Eight
 // tiles per lane are loaded before they are added, so a 256-tile system
 // costs one L2 round trip.
-template <int NV>
 __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -157,42 +149,29 @@ __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
     for (int j = w; j < nsl; j += nw) {
         if (!sl[j].active) continue;
         const SysDev& S = a.sys[sl[j].sys];
-        double acc[2 * NV];
-#pragma unroll
-        for (int q = 0; q < 2 * NV; ++q) acc[q] = 0.0;
+        double ax = 0.0, ay = 0.0;
         for (int base = lane; base < S.ntiles; base += 32 * U) {
-            double2 v[U][NV];
+            double2 v[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 // the load address is clamped into the system's tiles, so a load the
                 // compiler issues ahead of the range test never leaves the array
                 const int i = base + 32 * u;
                 const int ii = i < S.ntiles ? i : S.ntiles - 1;
-                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
-#pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    const double2 t = ld_volatile2(q + c);
-                    v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
-                }
+                const double2 t = ld_volatile2(reinterpret_cast<const double2*>(a.partial + S.tile0 + ii));
+                v[u] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
             }
 #pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int c = 0; c < NV; ++c) {
-                    acc[2 * c] += v[u][c].x;
-                    acc[2 * c + 1] += v[u][c].y;
-                }
+            for (int u = 0; u < U; ++u) {
+                ax += v[u].x;
+                ay += v[u].y;
+            }
         }
-#pragma unroll
-        for (int q = 0; q < 2 * NV; ++q) acc[q] = warp_sum(acc[q]);
+        ax = warp_sum(ax);
+        ay = warp_sum(ay);
         if (lane == 0) {
-            sl[j].sx = acc[0];
-            sl[j].sy = acc[1];
-            if (NV > 1) {
-                sl[j].sz = acc[2 % (2 * NV)];
-                sl[j].sw = acc[3 % (2 * NV)];
-            }
-            if (NV > 2) sl[j].su = acc[4 % (2 * NV)];
+            sl[j].sx = ax;
+            sl[j].sy = ay;
         }
     }
     __syncthreads();
@@ -291,58 +270,43 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
 }
 
 // Block partial sums -> the tile's partial slot (thread 0), one pass.
-// keep_z: the slot's z (the FP64 residual of a reliable update) is kept.
-__device__ __forceinline__ void store_partial(const CGArgs& a, int tile, const double4& s, bool keep_z)
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double* red)
 {
+    const double2 s = block_sum2(x, y, red);
     if (threadIdx.x == 0) {
-        Partial p;
-        p.x = s.x;
-        p.y = s.y;
-        p.z = keep_z ? a.partial[tile].z : s.z;
-        p.w = keep_z ? s.z : s.w;
-        p.u = keep_z ? s.w : 0.0;
-        p.v = 0.0;
 #ifdef YK_CG_CHECKED
         if (tile < 0 || tile >= a.tile_end) {
             if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d end %d\n", tile, a.tile_end);
             return;
         }
 #endif
+        Partial p;
+        p.x = s.x;
+        p.y = s.y;
         a.partial[tile] = p;
     }
-}
-
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double z, double w,
-                                            double u, double* red, bool keep_z = false)
-{
-    store_partial(a, tile, block_sum4(x, y, keep_z ? w : z, keep_z ? u : w, red), keep_z);
-}
-
-// FP32 per-site values: FP32 within each warp, FP64 above (block_sum4f).
-__device__ __forceinline__ void put_partial_f(const CGArgs& a, int tile, float x, float y, float z, float w,
-                                              float u, double* red, bool keep_z = false)
-{
-    store_partial(a, tile, block_sum4f(x, y, keep_z ? w : z, keep_z ? u : w, red), keep_z);
-}
-
-// Real part of sum conj(a) b over one site, in the vectors' own precision.
-template <int K>
-__device__ __forceinline__ float site_dotf(const Site<float, K>& a, const Site<float, K>& b)
-{
-    float re = 0.f;
-#pragma unroll
-    for (int i = 0; i < 4 * K; ++i) re = fmaf(a.v[i], b.v[i], re);
-    return re;
 }
 
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// FP64 Hestenes-Stiefel CG (the reference's algorithm)
+// Hestenes-Stiefel CG (the reference's algorithm), three phases per iteration:
+//   1. reduce |r|^2 -> beta / convergence; p = r + beta p formed on the fly at
+//      the five stencil sites; t = D_first p
+//   2. Ap = D_second t; partial <p, Ap>
+//   3. reduce -> alpha (Smith division); x += alpha p, r -= alpha Ap; |r|^2
+// W = double: the plain FP64 solver.  W = float (MIXED): FP32 vectors and
+// stencil, FP64 partial sums and scalars.  When the FP32 residual claims
+// convergence, every `reliable_every` iterations and at the iteration cap,
+// phase 1 is followed by a reliable update -- t64 = D_first (x + xs) and
+// r = b - D_second t64 in FP64, x += xs, xs = 0 -- and phase 1 is run again
+// for the systems concerned on that FP64 residual; convergence is only
+// declared on it.
 // ---------------------------------------------------------------------------
-template <int K>
-__global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
+template <int K, bool MIXED>
+__global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
 {
+    using W = typename std::conditional<MIXED, float, double>::type;
     __shared__ double red[64];
     __shared__ SysLocal sl[kMaxSysPerBlock];
     __shared__ int nsl;
@@ -351,8 +315,23 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     build_table(a, tb, te, sl, &nsl, tslot);
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
+    auto Rv = [](const SysDev& S) -> W* {
+        if constexpr (MIXED) return S.r32; else return S.r64;
+    };
+    auto Pv = [](const SysDev& S, int i) -> W* {
+        if constexpr (MIXED) return S.p32[i]; else return S.p64[i];
+    };
+    auto Tv = [](const SysDev& S) -> W* {
+        if constexpr (MIXED) return S.t32; else return S.t64;
+    };
+    auto Av = [](const SysDev& S) -> W* {
+        if constexpr (MIXED) return S.Ap32; else return S.Ap64;
+    };
+    auto Xv = [](const SysDev& S) -> W* {
+        if constexpr (MIXED) return S.xs32; else return S.x;
+    };
 
-    // ---------------- init: x = 0, r = p_0 = b, |b|^2
+    // ---------------- init: x = 0 (and xs = 0), r = p_0 = b, |b|^2
     for (int tile = tb; tile < te; ++tile) {
         const SysDev& S = a.sys[a.tiles[tile].x];
         const int n = a.tiles[tile].y + threadIdx.x;
@@ -361,76 +340,183 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
             if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
             Site<double, K> z;
+            Site<W, K> bw, zw;
 #pragma unroll
             for (int i = 0; i < 4 * K; ++i) {
                 z.v[i] = 0.0;
+                zw.v[i] = W(0);
+                bw.v[i] = (W)bv.v[i];
                 pr = fma(bv.v[i], bv.v[i], pr);
             }
             YK_ST(double, K, S.x, n, z);
-            YK_ST(double, K, S.r64, n, bv);
-            YK_ST(double, K, S.p64[0], n, bv);
+            if constexpr (MIXED) YK_ST(W, K, S.xs32, n, zw);
+            YK_ST(W, K, Rv(S), n, bw);
+            YK_ST(W, K, Pv(S, 0), n, bw);
         }
-        put_partial(a, tile, pr, 0.0, 0.0, 0.0, 0.0, red);
+        put_partial(a, tile, pr, 0.0, red);
     }
     if (!gsync(a.bar, a.err)) return;
 
-    for (int k = 0; k <= a.max_iter + 1; ++k) {
-        const bool fresh = (k == 0);
-        const int cur = k & 1, prv = (k + 1) & 1;
-        // ---------------- phase 1: rr -> beta / stop; p_k on the fly; t = D_first p_k
-        reduce_systems<1>(a, sl, nsl);
+    int n_ru = 0;
+    bool redo = false;   // phase 1 again after a reliable update, same k
+    int k = 0;
+    while (k <= a.max_iter) {   // every system retires in phase 1 of k = max_iter at the latest
+        const int cur = k & 1, prv = cur ^ 1;   // p_k lives in P[cur]
+        // ---------------- phase 1
+        reduce_systems(a, sl, nsl);
         if (threadIdx.x == 0) {
+            int want_ru = 0;
             for (int j = 0; j < nsl; ++j) {
                 SysLocal& L = sl[j];
-                if (!L.active) continue;
-                if (fresh) {
-                    L.rr = L.rr0 = L.sx;
-                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(L.sx);
+                L.go = 0;
+                if (!L.active || (redo && !L.ru_done)) continue;
+                const double rr = L.sx;
+                if (k == 0) {
+                    L.rr = L.rr0 = rr;
+                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(rr);
                     L.beta = 0.0;
-                    if (!isfinite(L.sx)) retire(a, L, 0, YK_ENAN);
-                    else if (!(sqrt(L.sx) > L.stop)) retire(a, L, 1, 0);
-                    else if (a.max_iter <= 0) retire(a, L, 0, YK_ENOCONV);
-                } else {
-                    const double rr = L.sx;
-                    L.iters += 1;
-                    L.beta = rr / L.rr;
-                    L.rr = rr;
                     if (!isfinite(rr)) retire(a, L, 0, YK_ENAN);
                     else if (!(sqrt(rr) > L.stop)) retire(a, L, 1, 0);
-                    else if (L.iters >= a.max_iter) retire(a, L, 0, YK_ENOCONV);
+                    else if (a.max_iter <= 0) retire(a, L, 0, YK_ENOCONV);
+                    else L.go = 1;
+                    continue;
                 }
+                if (!L.ru_done) L.iters += 1;
+                if (!isfinite(rr)) {
+                    retire(a, L, 0, YK_ENAN);
+                    continue;
+                }
+                if (MIXED && !L.ru_done) {
+                    const bool cand = !(sqrt(rr) > L.stop);
+                    const bool due = a.reliable_every > 0 && (L.iters % a.reliable_every) == 0;
+                    const bool cap = L.iters >= a.max_iter;
+                    if (cand || due || cap) {
+                        L.ru = 1;
+                        want_ru = 1;
+                        continue;
+                    }
+                } else {
+                    L.ru_done = 0;
+                    if (!(sqrt(rr) > L.stop)) {
+                        L.rr = rr;
+                        retire(a, L, 1, 0);
+                        continue;
+                    }
+                    if (L.iters >= a.max_iter) {
+                        L.rr = rr;
+                        retire(a, L, 0, YK_ENOCONV);
+                        continue;
+                    }
+                }
+                L.beta = rr / L.rr;
+                L.rr = rr;
+                L.go = 1;
             }
+            if (want_ru) atomicMax(a.any_ru, k + 1);
         }
         __syncthreads();
         for (int tile = tb; tile < te; ++tile) {
             const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.active) continue;
+            if (!L.go) continue;
             const SysDev& S = a.sys[L.sys];
             const int n = a.tiles[tile].y + threadIdx.x;
             if (n >= S.V) continue;
-            const double beta = L.beta;
-            const double* pold = S.p64[fresh ? 0 : prv];
+            const W beta = (W)L.beta;
+            const W* pold = Pv(S, k == 0 ? 0 : prv);
+            const W* rv = Rv(S);
             const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-            auto p_at = [&](int64_t m) {
-                Site<double, K> po = YK_LD(double, K, pold, m);
-                if (!fresh) {
-                    const Site<double, K> rv = YK_LD(double, K, S.r64, m);
+            Site<W, K> st[5];
+            const int64_t m5[5] = {n, nbr.tu, nbr.td, nbr.xu, nbr.xd};
 #pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) po.v[i] = fma(beta, po.v[i], rv.v[i]);
+            for (int q = 0; q < 5; ++q) {
+                st[q] = YK_LD(W, K, pold, m5[q]);
+                if (k > 0) {
+                    const Site<W, K> r = YK_LD(W, K, rv, m5[q]);
+#pragma unroll
+                    for (int i = 0; i < 4 * K; ++i) st[q].v[i] = fma(beta, st[q].v[i], r.v[i]);
                 }
-                return po;
-            };
-            const Site<double, K> c = p_at(n), tu = p_at(nbr.tu), tdn = p_at(nbr.td), xu = p_at(nbr.xu),
-                                  xd = p_at(nbr.xd);
-            const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-            const Site<double, K> o = first_dag
-                ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
-                : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
-            YK_ST(double, K, S.t64, n, o);
-            if (!fresh) YK_ST(double, K, S.p64[cur], n, c);
+            }
+            const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
+            const Site<W, K> o = first_dag
+                ? dirac_combine<W, K, true>(st[0], st[1], st[2], st[3], st[4], diag, (W)S.r, (W)nbr.sp, (W)nbr.sm)
+                : dirac_combine<W, K, false>(st[0], st[1], st[2], st[3], st[4], diag, (W)S.r, (W)nbr.sp, (W)nbr.sm);
+            YK_ST(W, K, Tv(S), n, o);
+            if (k > 0) YK_ST(W, K, Pv(S, cur), n, st[0]);
         }
         if (!gsync(a.bar, a.err)) return;
         if (*(volatile int*)a.n_active == 0) break;
+
+        if constexpr (MIXED) {
+            if (!redo && *(volatile int*)a.any_ru == k + 1) {
+                // RU1: t64 = D_first (x + xs), formed on the fly in FP64
+                for (int tile = tb; tile < te; ++tile) {
+                    const SysLocal& L = sl[tslot[tile - tb]];
+                    if (!L.active || !L.ru) continue;
+                    const SysDev& S = a.sys[L.sys];
+                    const int n = a.tiles[tile].y + threadIdx.x;
+                    if (n >= S.V) continue;
+                    const Nbr nbr = neighbours(n, S.Nt, S.Nx);
+                    Site<double, K> xt[5];
+                    const int64_t m5[5] = {n, nbr.tu, nbr.td, nbr.xu, nbr.xd};
+#pragma unroll
+                    for (int q = 0; q < 5; ++q) {
+                        xt[q] = YK_LD(double, K, S.x, m5[q]);
+                        const Site<W, K> xs = YK_LD(W, K, S.xs32, m5[q]);
+#pragma unroll
+                        for (int i = 0; i < 4 * K; ++i) xt[q].v[i] += (double)xs.v[i];
+                    }
+                    const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+                    const Site<double, K> t = first_dag
+                        ? dirac_combine<double, K, true>(xt[0], xt[1], xt[2], xt[3], xt[4], diag, S.r, (double)nbr.sp, (double)nbr.sm)
+                        : dirac_combine<double, K, false>(xt[0], xt[1], xt[2], xt[3], xt[4], diag, S.r, (double)nbr.sp, (double)nbr.sm);
+                    YK_ST(double, K, S.t64, n, t);
+                }
+                if (!gsync(a.bar, a.err)) return;
+                // RU2: x += xs, xs = 0; r = b - D_second t64 in FP64; |r|^2
+                for (int tile = tb; tile < te; ++tile) {
+                    const SysLocal& L = sl[tslot[tile - tb]];
+                    if (!L.active || !L.ru) continue;
+                    const SysDev& S = a.sys[L.sys];
+                    const int n = a.tiles[tile].y + threadIdx.x;
+                    double rr = 0.0;
+                    if (n < S.V) {
+                        Site<double, K> xv = YK_LD(double, K, S.x, n);
+                        const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
+                        Site<W, K> zw;
+#pragma unroll
+                        for (int i = 0; i < 4 * K; ++i) {
+                            xv.v[i] += (double)xs.v[i];
+                            zw.v[i] = W(0);
+                        }
+                        YK_ST(double, K, S.x, n, xv);
+                        YK_ST(W, K, S.xs32, n, zw);
+                        const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
+                        const Site<double, K> bv = YK_LD(double, K, S.b, n);
+                        Site<W, K> rw;
+#pragma unroll
+                        for (int i = 0; i < 4 * K; ++i) {
+                            const double r = bv.v[i] - ax.v[i];
+                            rr = fma(r, r, rr);
+                            rw.v[i] = (W)r;
+                        }
+                        YK_ST(W, K, Rv(S), n, rw);
+                    }
+                    put_partial(a, tile, rr, 0.0, red);
+                }
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    for (int j = 0; j < nsl; ++j)
+                        if (sl[j].active && sl[j].ru) {
+                            sl[j].ru = 0;
+                            sl[j].ru_done = 1;
+                        }
+                ++n_ru;
+                redo = true;
+                if (!gsync(a.bar, a.err)) return;
+                continue;
+            }
+        }
+        redo = false;
 
         // ---------------- phase 2: Ap = D_second t, <p, Ap>
         for (int tile = tb; tile < te; ++tile) {
@@ -440,16 +526,16 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const int n = a.tiles[tile].y + threadIdx.x;
             double2 d = make_double2(0.0, 0.0);
             if (n < S.V) {
-                const Site<double, K> ap = apply_d<double, K>(S.t64, n, S, !first_dag);
-                YK_ST(double, K, S.Ap64, n, ap);
-                d = site_dot<double, K>(YK_LD(double, K, S.p64[cur], n), ap);
+                const Site<W, K> ap = apply_d<W, K>(Tv(S), n, S, !first_dag);
+                YK_ST(W, K, Av(S), n, ap);
+                d = site_dot<W, K>(YK_LD(W, K, Pv(S, cur), n), ap);
             }
-            put_partial(a, tile, d.x, d.y, 0.0, 0.0, 0.0, red);
+            put_partial(a, tile, d.x, d.y, red);
         }
         if (!gsync(a.bar, a.err)) return;
 
         // ---------------- phase 3: alpha; x += alpha p, r -= alpha Ap, |r|^2
-        reduce_systems<1>(a, sl, nsl);
+        reduce_systems(a, sl, nsl);
         if (threadIdx.x == 0) {
             for (int j = 0; j < nsl; ++j) {
                 SysLocal& L = sl[j];
@@ -479,343 +565,30 @@ __global__ void __launch_bounds__(kBlock) cg64_kernel(CGArgs a)
             const int n = a.tiles[tile].y + threadIdx.x;
             double rr = 0.0;
             if (n < S.V) {
-                const Site<double, K> pv = YK_LD(double, K, S.p64[cur], n);
-                const Site<double, K> ap = YK_LD(double, K, S.Ap64, n);
-                Site<double, K> xs = YK_LD(double, K, S.x, n);
-                Site<double, K> rs = YK_LD(double, K, S.r64, n);
-                site_axpy<double, K>(xs, L.alpha, L.alpha_im, pv);
-                site_axpy<double, K>(rs, -L.alpha, -L.alpha_im, ap);
-                YK_ST(double, K, S.x, n, xs);
-                YK_ST(double, K, S.r64, n, rs);
+                const Site<W, K> pv = YK_LD(W, K, Pv(S, cur), n);
+                const Site<W, K> ap = YK_LD(W, K, Av(S), n);
+                Site<W, K> xs = YK_LD(W, K, Xv(S), n);
+                Site<W, K> rs = YK_LD(W, K, Rv(S), n);
+                site_axpy<W, K>(xs, (W)L.alpha, (W)L.alpha_im, pv);
+                site_axpy<W, K>(rs, (W)-L.alpha, (W)-L.alpha_im, ap);
+                YK_ST(W, K, Xv(S), n, xs);
+                YK_ST(W, K, Rv(S), n, rs);
 #pragma unroll
-                for (int i = 0; i < 4 * K; ++i) rr = fma(rs.v[i], rs.v[i], rr);
+                for (int i = 0; i < 4 * K; ++i) rr = fma((double)rs.v[i], (double)rs.v[i], rr);
             }
-            put_partial(a, tile, rr, 0.0, 0.0, 0.0, 0.0, red);
+            put_partial(a, tile, rr, 0.0, red);
         }
         if (!gsync(a.bar, a.err)) return;
+        ++k;
     }
     if (threadIdx.x == 0)
-        for (int j = 0; j < nsl; ++j) publish(a, sl[j], 0);
-}
-
-// ---------------------------------------------------------------------------
-// Mixed FP32/FP64 Chronopoulos-Gear CG with reliable updates.
-// Buffers of a system: r32 (2 V: r double-buffered), p32[0] (p),
-// p32[1] and Ap32 (s = A p, double-buffered), t32 (2 V: t = D r and w = A r),
-// xs32 (FP32 solution increment), FP64 x, b, t64.
-// ---------------------------------------------------------------------------
-template <int K>
-__global__ void __launch_bounds__(kBlock) cgcg_kernel(CGArgs a)
-{
-    using W = float;
-    __shared__ double red[64];
-    __shared__ SysLocal sl[kMaxSysPerBlock];
-    __shared__ int nsl;
-    __shared__ int tslot[kMaxTilesPerBlock];
-    __shared__ int s_nru;
-    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
-    const int te = min(tb + a.tiles_per_block, a.tile_end);
-    build_table(a, tb, te, sl, &nsl, tslot);
-    if (threadIdx.x == 0) s_nru = 0;
-    const bool first_dag = (a.mtype == YK_NORMAL);
-    auto Rb = [](const SysDev& S, int i) { return S.r32 + (i ? (int64_t)S.V * 4 * K : 0); };
-    auto Sb = [](const SysDev& S, int i) { return i ? S.Ap32 : S.p32[1]; };
-    auto Wb = [](const SysDev& S) { return S.t32 + (int64_t)S.V * 4 * K; };
-
-    // ---------------- I0: b (generated or given), x = 0, xs = 0, p = 0, s_{-1} = 0, r_0 = b, |b|^2
-    for (int tile = tb; tile < te; ++tile) {
-        const SysDev& S = a.sys[a.tiles[tile].x];
-        const int n = a.tiles[tile].y + threadIdx.x;
-        double bb = 0.0;
-        if (n < S.V) {
-            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
-            if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
-            Site<double, K> z;
-            Site<W, K> bf, zf;
-#pragma unroll
-            for (int i = 0; i < 4 * K; ++i) {
-                z.v[i] = 0.0;
-                zf.v[i] = 0.f;
-                bf.v[i] = (W)bv.v[i];
-                bb = fma(bv.v[i], bv.v[i], bb);
-            }
-            YK_ST(double, K, S.x, n, z);
-            YK_ST(W, K, S.xs32, n, zf);
-            YK_ST(W, K, S.p32[0], n, zf);
-            YK_ST(W, K, Sb(S, 1), n, zf);
-            YK_ST(W, K, Rb(S, 0), n, bf);
-        }
-        put_partial(a, tile, 0.0, 0.0, bb, 0.0, 0.0, red);
-    }
-    if (!gsync(a.bar, a.err)) return;
-    // ---------------- I1: t = D_first r_0
-    for (int tile = tb; tile < te; ++tile) {
-        const SysDev& S = a.sys[a.tiles[tile].x];
-        const int n = a.tiles[tile].y + threadIdx.x;
-        if (n < S.V) YK_ST(W, K, S.t32, n, (apply_d<W, K>(Rb(S, 0), n, S, first_dag)));
-    }
-    if (!gsync(a.bar, a.err)) return;
-    // ---------------- I2: w_0 = D_second t; (r,r), (w,r); |b|^2 kept in z
-    for (int tile = tb; tile < te; ++tile) {
-        const SysDev& S = a.sys[a.tiles[tile].x];
-        const int n = a.tiles[tile].y + threadIdx.x;
-        float g = 0.f, d = 0.f;
-        if (n < S.V) {
-            const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-            YK_ST(W, K, Wb(S), n, w);
-            const Site<W, K> r = YK_LD(W, K, Rb(S, 0), n);
-            g = site_dotf<K>(r, r);
-            d = site_dotf<K>(w, r);
-        }
-        put_partial_f(a, tile, g, d, 0.f, 0.f, 0.f, red, true);
-    }
-    if (!gsync(a.bar, a.err)) return;
-
-    for (int k = 0; k <= a.max_iter + 1; ++k) {
-        const int cur = k & 1, nxt = (k + 1) & 1;
-        // ---------------- phase A: reduce; s_k, p_k, xs += alpha p_k, r_{k+1} (on the fly), t = D r_{k+1}
-        reduce_systems<3>(a, sl, nsl);
-        if (threadIdx.x == 0) {
-            int want_ru = 0;
-            for (int j = 0; j < nsl; ++j) {
-                SysLocal& L = sl[j];
-                if (!L.active) continue;
-                const double gam = L.sx, del = L.sy;
-                if (k == 0) {
-                    L.rr0 = L.sz;
-                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(L.sz);
-                    L.rr = L.sz;
-                    if (!isfinite(L.sz)) { retire(a, L, 0, YK_ENAN); continue; }
-                    if (!(sqrt(L.sz) > L.stop)) { retire(a, L, 1, 0); continue; }
-                    if (a.max_iter <= 0) { retire(a, L, 0, YK_ENOCONV); continue; }
-                    L.beta = 0.0;
-                    L.alpha = gam / del;
-                    L.gamma = gam;
-                    L.gamma_ru = gam;
-                    L.iters_ru = 0;
-                } else {
-                    L.iters += 1;
-                    const double beta = gam / L.gamma;
-                    if (L.ru_done) {
-                        // z holds |b - A x|^2 in FP64 from the reliable update; the
-                        // recurrence restarts from the recomputed r, w with alpha from
-                        // (p, A p) = (r, w) + beta ((r, s) + (p, w)) + beta^2 (p, s)
-                        L.ru_done = 0;
-                        L.rr = L.sz;
-                        if (!isfinite(L.sz)) { retire(a, L, 0, YK_ENAN); continue; }
-                        if (!(sqrt(L.sz) > L.stop)) { retire(a, L, 1, 0); continue; }
-                        if (L.last) { retire(a, L, 0, YK_ENOCONV); continue; }
-                        const double pap = del + beta * L.sw + beta * beta * L.su;
-                        L.alpha = gam / pap;
-                        L.gamma_ru = gam;
-                        L.iters_ru = L.iters;
-                    } else {
-                        L.rr = gam;
-                        const double den = del - beta * gam / L.alpha;
-                        L.alpha = gam / den;
-                    }
-                    L.beta = beta;
-                    L.gamma = gam;
-                }
-                if (!isfinite(gam) || !isfinite(L.beta)) {
-                    retire(a, L, 0, YK_ENAN);
-                    continue;
-                }
-                // a breakdown of the short recurrence (alpha <= 0 from rounding):
-                // no update this iteration and a reliable update, which recomputes
-                // alpha from (p, A p)
-                const bool broken = !isfinite(L.alpha) || !(L.alpha > 0.0);
-                if (broken) L.alpha = 0.0;
-                // reliable update after this iteration: residual down 100x since the
-                // last one, FP32 residual below the target, interval, or the cap
-                const bool cand = broken || !(sqrt(gam) > L.stop);
-                const bool drop = gam < 1e-4 * L.gamma_ru;
-                const bool due = drop || (a.reliable_every > 0 && (L.iters + 1 - L.iters_ru) >= a.reliable_every);
-                const bool cap = (L.iters + 1) >= a.max_iter;
-                if (cand || due || cap) {
-                    L.ru = 1;
-                    L.last = cap ? 1 : 0;
-                    want_ru = 1;
-                }
-            }
-            if (want_ru) atomicMax(a.any_ru, k + 1);
-        }
-        __syncthreads();
-        for (int tile = tb; tile < te; ++tile) {
-            const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.active) continue;
-            const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
-            if (n >= S.V) continue;
-            const W al = (W)L.alpha, be = (W)L.beta;
-            const W* Rc = Rb(S, cur);
-            const W* Sp = Sb(S, nxt);   // s_{k-1}
-            const W* Wk = Wb(S);
-            const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-            // r_{k+1}(m) = r_k(m) - alpha (w_k(m) + beta s_{k-1}(m))
-            auto rnext = [&](int64_t m, Site<W, K>* s_out) {
-                const Site<W, K> rv = YK_LD(W, K, Rc, m);
-                const Site<W, K> wv = YK_LD(W, K, Wk, m);
-                const Site<W, K> sv = YK_LD(W, K, Sp, m);
-                Site<W, K> o;
-#pragma unroll
-                for (int i = 0; i < 4 * K; ++i) {
-                    const W s = fma(be, sv.v[i], wv.v[i]);
-                    if (s_out) s_out->v[i] = s;
-                    o.v[i] = fma(-al, s, rv.v[i]);
-                }
-                return o;
-            };
-            Site<W, K> sk;
-            const Site<W, K> c = rnext(n, &sk);
-            const Site<W, K> tu = rnext(nbr.tu, nullptr), tdn = rnext(nbr.td, nullptr);
-            const Site<W, K> xu = rnext(nbr.xu, nullptr), xd = rnext(nbr.xd, nullptr);
-            // p_k = r_k + beta p_{k-1}; xs += alpha p_k
-            const Site<W, K> rk = YK_LD(W, K, Rc, n);
-            Site<W, K> pk = YK_LD(W, K, S.p32[0], n);
-            Site<W, K> xs = YK_LD(W, K, S.xs32, n);
-#pragma unroll
-            for (int i = 0; i < 4 * K; ++i) {
-                pk.v[i] = fma(be, pk.v[i], rk.v[i]);
-                xs.v[i] = fma(al, pk.v[i], xs.v[i]);
-            }
-            YK_ST(W, K, S.p32[0], n, pk);
-            YK_ST(W, K, S.xs32, n, xs);
-            YK_ST(W, K, Sb(S, cur), n, sk);
-            YK_ST(W, K, Rb(S, nxt), n, c);
-            const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
-            const Site<W, K> t = first_dag
-                ? dirac_combine<W, K, true>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm)
-                : dirac_combine<W, K, false>(c, tu, tdn, xu, xd, diag, (W)S.r, (W)nbr.sp, (W)nbr.sm);
-            YK_ST(W, K, S.t32, n, t);
-        }
-        if (!gsync(a.bar, a.err)) return;
-        if (*(volatile int*)a.n_active == 0) break;
-
-        // ---------------- phase B: w_{k+1} = D_second t; (r,r), (w,r)
-        for (int tile = tb; tile < te; ++tile) {
-            const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.active) continue;
-            const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
-            float g = 0.f, d = 0.f;
-            if (n < S.V) {
-                const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-                YK_ST(W, K, Wb(S), n, w);
-                const Site<W, K> r = YK_LD(W, K, Rb(S, nxt), n);
-                g = site_dotf<K>(r, r);
-                d = site_dotf<K>(w, r);
-            }
-            put_partial_f(a, tile, g, d, 0.f, 0.f, 0.f, red);
-        }
-        if (!gsync(a.bar, a.err)) return;
-
-        if (*(volatile int*)a.any_ru == k + 1) {
-            // RU1: t64 = D_first (x + xs)  (FP64, formed on the fly)
-            for (int tile = tb; tile < te; ++tile) {
-                const SysLocal& L = sl[tslot[tile - tb]];
-                if (!L.active || !L.ru) continue;
-                const SysDev& S = a.sys[L.sys];
-                const int n = a.tiles[tile].y + threadIdx.x;
-                if (n >= S.V) continue;
-                const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-                auto xat = [&](int64_t m) {
-                    Site<double, K> xv = YK_LD(double, K, S.x, m);
-                    const Site<W, K> xs = YK_LD(W, K, S.xs32, m);
-#pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) xv.v[i] += (double)xs.v[i];
-                    return xv;
-                };
-                const Site<double, K> c = xat(n), tu = xat(nbr.tu), tdn = xat(nbr.td), xu = xat(nbr.xu),
-                                      xd = xat(nbr.xd);
-                const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-                const Site<double, K> t = first_dag
-                    ? dirac_combine<double, K, true>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm)
-                    : dirac_combine<double, K, false>(c, tu, tdn, xu, xd, diag, S.r, (double)nbr.sp, (double)nbr.sm);
-                YK_ST(double, K, S.t64, n, t);
-            }
-            if (!gsync(a.bar, a.err)) return;
-            // RU2: x += xs, xs = 0; r = b - D_second t64 (FP64) -> r_{k+1}; |r|^2 in z
-            for (int tile = tb; tile < te; ++tile) {
-                const SysLocal& L = sl[tslot[tile - tb]];
-                if (!L.active || !L.ru) continue;
-                const SysDev& S = a.sys[L.sys];
-                const int n = a.tiles[tile].y + threadIdx.x;
-                double rr = 0.0;
-                if (n < S.V) {
-                    Site<double, K> xv = YK_LD(double, K, S.x, n);
-                    const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
-                    Site<W, K> zf;
-#pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) {
-                        xv.v[i] += (double)xs.v[i];
-                        zf.v[i] = 0.f;
-                    }
-                    YK_ST(double, K, S.x, n, xv);
-                    YK_ST(W, K, S.xs32, n, zf);
-                    const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
-                    const Site<double, K> bv = YK_LD(double, K, S.b, n);
-                    Site<W, K> rf;
-#pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) {
-                        const double rv = bv.v[i] - ax.v[i];
-                        rr = fma(rv, rv, rr);
-                        rf.v[i] = (W)rv;
-                    }
-                    YK_ST(W, K, Rb(S, nxt), n, rf);
-                }
-                put_partial(a, tile, 0.0, 0.0, rr, 0.0, 0.0, red);
-            }
-            if (!gsync(a.bar, a.err)) return;
-            // RU3: t = D_first r
-            for (int tile = tb; tile < te; ++tile) {
-                const SysLocal& L = sl[tslot[tile - tb]];
-                if (!L.active || !L.ru) continue;
-                const SysDev& S = a.sys[L.sys];
-                const int n = a.tiles[tile].y + threadIdx.x;
-                if (n < S.V) YK_ST(W, K, S.t32, n, (apply_d<W, K>(Rb(S, nxt), n, S, first_dag)));
-            }
-            if (!gsync(a.bar, a.err)) return;
-            // RU4: w = D_second t; (r,r), (w,r), (r,s_k) + (p_k,w), (p_k,s_k); z kept
-            for (int tile = tb; tile < te; ++tile) {
-                const SysLocal& L = sl[tslot[tile - tb]];
-                if (!L.active || !L.ru) continue;
-                const SysDev& S = a.sys[L.sys];
-                const int n = a.tiles[tile].y + threadIdx.x;
-                float g = 0.f, d = 0.f, c1 = 0.f, c2 = 0.f;
-                if (n < S.V) {
-                    const Site<W, K> w = apply_d<W, K>(S.t32, n, S, !first_dag);
-                    YK_ST(W, K, Wb(S), n, w);
-                    const Site<W, K> r = YK_LD(W, K, Rb(S, nxt), n);
-                    const Site<W, K> sk = YK_LD(W, K, Sb(S, cur), n);
-                    const Site<W, K> pk = YK_LD(W, K, S.p32[0], n);
-                    g = site_dotf<K>(r, r);
-                    d = site_dotf<K>(w, r);
-                    c1 = site_dotf<K>(r, sk) + site_dotf<K>(pk, w);
-                    c2 = site_dotf<K>(pk, sk);
-                }
-                put_partial_f(a, tile, g, d, 0.f, c1, c2, red, true);
-            }
-            if (threadIdx.x == 0) {
-                for (int j = 0; j < nsl; ++j)
-                    if (sl[j].active && sl[j].ru) {
-                        sl[j].ru = 0;
-                        sl[j].ru_done = 1;
-                    }
-                s_nru += 1;
-            }
-            if (!gsync(a.bar, a.err)) return;
-        }
-    }
-    if (threadIdx.x == 0)
-        for (int j = 0; j < nsl; ++j) publish(a, sl[j], s_nru);
+        for (int j = 0; j < nsl; ++j) publish(a, sl[j], n_ru);
 }
 
 // Resets the barrier, counters and activity flags before a solve.
 __global__ void cg_prepare_kernel(CGArgs a)
 {
     for (int i = a.sys_first + threadIdx.x; i < a.sys_first + a.sys_count; i += blockDim.x) {
-        a.st[i].counter = 0;
         a.st[i].active = 1;
         a.st[i].iters = 0;
         a.st[i].converged = 0;
@@ -842,19 +615,10 @@ static int max_coresident(const void* fn, int block)
 }
 
 template <int K, bool MIXED>
-static const void* kernel_of()
-{
-    if constexpr (MIXED)
-        return (const void*)cgcg_kernel<K>;
-    else
-        return (const void*)cg64_kernel<K>;
-}
-
-template <int K, bool MIXED>
 static int max_grid_t()
 {
     static int maxg = -1;
-    if (maxg < 0) maxg = max_coresident(kernel_of<K, MIXED>(), kBlock);
+    if (maxg < 0) maxg = max_coresident((const void*)cg_kernel<K, MIXED>, kBlock);
     return maxg;
 }
 
@@ -898,10 +662,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if constexpr (MIXED)
-        return cudaLaunchKernelEx(&cfg, cgcg_kernel<K>, a);
-    else
-        return cudaLaunchKernelEx(&cfg, cg64_kernel<K>, a);
+    return cudaLaunchKernelEx(&cfg, cg_kernel<K, MIXED>, a);
 }
 
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out)

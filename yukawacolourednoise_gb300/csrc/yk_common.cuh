@@ -232,72 +232,6 @@ __device__ __forceinline__ double2 block_sum2(double a, double b, double* scratc
     return r;
 }
 
-__device__ __forceinline__ float warp_sumf(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Block sum of four FP32 values: each warp's 32 values are summed in FP32,
-// the warp sums in FP64 (GB300 issues FP64 at a small fraction of FP32, so
-// the per-site butterfly stays in FP32).  Results valid in thread 0.
-__device__ __forceinline__ double4 block_sum4f(float a, float b, float c, float d, double* scratch)
-{
-    a = warp_sumf(a);
-    b = warp_sumf(b);
-    c = warp_sumf(c);
-    d = warp_sumf(d);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) {
-        scratch[4 * w] = (double)a;
-        scratch[4 * w + 1] = (double)b;
-        scratch[4 * w + 2] = (double)c;
-        scratch[4 * w + 3] = (double)d;
-    }
-    __syncthreads();
-    double4 r = make_double4(0.0, 0.0, 0.0, 0.0);
-    if (w == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        double x = lane < nw ? scratch[4 * lane] : 0.0;
-        double y = lane < nw ? scratch[4 * lane + 1] : 0.0;
-        double z = lane < nw ? scratch[4 * lane + 2] : 0.0;
-        double q = lane < nw ? scratch[4 * lane + 3] : 0.0;
-        r = make_double4(warp_sum(x), warp_sum(y), warp_sum(z), warp_sum(q));
-    }
-    return r;
-}
-
-// Block sum of up to four values in one pass; results valid in thread 0.
-// scratch: >= 4*32 doubles.
-__device__ __forceinline__ double4 block_sum4(double a, double b, double c, double d, double* scratch)
-{
-    a = warp_sum(a);
-    b = warp_sum(b);
-    c = warp_sum(c);
-    d = warp_sum(d);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) {
-        scratch[4 * w] = a;
-        scratch[4 * w + 1] = b;
-        scratch[4 * w + 2] = c;
-        scratch[4 * w + 3] = d;
-    }
-    __syncthreads();
-    double4 r = make_double4(0.0, 0.0, 0.0, 0.0);
-    if (w == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        double x = lane < nw ? scratch[4 * lane] : 0.0;
-        double y = lane < nw ? scratch[4 * lane + 1] : 0.0;
-        double z = lane < nw ? scratch[4 * lane + 2] : 0.0;
-        double q = lane < nw ? scratch[4 * lane + 3] : 0.0;
-        r = make_double4(warp_sum(x), warp_sum(y), warp_sum(z), warp_sum(q));
-    }
-    return r;
-}
-
 __device__ __forceinline__ double block_max(double a, double* scratch)
 {
     a = warp_max(a);

@@ -42,10 +42,10 @@ struct SysDev {
     double* t64;         // D p (or D x in reliable updates)
     double* Ap64;        // D^dag D p
     // FP32 vectors (mixed solver)
-    float* r32;          // mixed: 2 V sites (r double-buffered)
-    float* p32[2];       // mixed: p, and one of the two s = A p buffers
-    float* t32;          // mixed: 2 V sites (t = D r, w = A r)
-    float* Ap32;         // mixed: the other s = A p buffer
+    float* r32;          // residual
+    float* p32[2];       // search directions, double-buffered
+    float* t32;          // D p
+    float* Ap32;         // D^dag D p
     float* xs32;         // solution increment since the last reliable update
     // noise generation for b: kind/rhs of the Philox stream, or gen = 0
     int gen_eta;
@@ -55,22 +55,17 @@ struct SysDev {
 
 // Per-tile reduction slot of the CG kernels.
 struct __align__(16) Partial {
-    double x, y, z, w, u, v;
+    double x, y;
 };
 
 // Per-system CG scalars, written by the finaliser block of each reduction.
 struct CGState {
-    double rr, rr0, rr_prev, stop;
-    double alpha_re, alpha_im;
-    double beta;
+    double rr, rr0;
     int active;
     int iters;
     int converged;
     int status;
-    int ru;      // reliable update pending
-    int n_ru;
-    int last;    // iteration cap reached: finish with a reliable update
-    unsigned counter;
+    int n_ru;    // reliable updates (mixed)
 };
 
 struct CGArgs {
@@ -80,7 +75,7 @@ struct CGArgs {
     int tile_begin, tile_end;   // tiles of this solve
     int eta_kind;               // Philox stream kind of generated right-hand sides
     CGState* st;
-    Partial* partial;    // one per tile: (x, y) reduction pair, z FP64 residual
+    Partial* partial;    // one per tile: the (x, y) reduction pair of the phase
     int tiles_per_block; // contiguous tile range of each block (set by the launcher)
     GridBarrier* bar;
     int* err;
