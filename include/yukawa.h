@@ -80,7 +80,9 @@ typedef struct yk_params {
     int cg_tol_mode;           /* YK_TOL_ABS (reference) or YK_TOL_REL            */
     double cg_tol;             /* 1e-8 (reference)                                */
     int cg_max_iter;           /* 1000 (reference)                                */
-    int reliable_every;        /* mixed precision: FP64 residual every N iters    */
+    int reliable_every;        /* mixed: also an FP64 update every N iters (0 off)*/
+    double reliable_delta;     /* mixed: FP64 update when |r| < delta * max |r|   */
+                               /*   since the last one (0.1)                    */
     double fixed_dt;           /* > 0: fixed Euler step instead of adaptive eps   */
     int init;                  /* YK_INIT_DRAND48 (reference), YK_INIT_PHILOX     */
 } yk_params;

@@ -111,7 +111,8 @@ struct yk_ctx {
     int nrows = 0, ncols = 0, nwhite = 0;
     int max_nx = 1, max_cols = 1;
     // solver settings (shared by all chains of a context)
-    int precision = YK_FP64, tol_mode = YK_TOL_ABS, max_iter = 1000, reliable_every = 50;
+    int precision = YK_FP64, tol_mode = YK_TOL_ABS, max_iter = 1000, reliable_every = 0;
+    double reliable_delta = 0.1;
     double tol = 1e-8;
     // step graph
     cudaGraphExec_t gexec = nullptr;
@@ -164,6 +165,10 @@ int check_params(const yk_params& p, int c)
         set_error("chain %d: cg_max_iter out of range", c);
         return YK_EINVAL;
     }
+    if (p.reliable_every < 0 || !(p.reliable_delta > 0.0 && p.reliable_delta < 1.0)) {
+        set_error("chain %d: reliable_every must be >= 0 and reliable_delta in (0, 1)", c);
+        return YK_EINVAL;
+    }
     return YK_OK;
 }
 
@@ -201,6 +206,7 @@ CGArgs base_args(yk_ctx* ctx)
     a.tol_mode = ctx->tol_mode;
     a.tol = ctx->tol;
     a.reliable_every = ctx->reliable_every;
+    a.reliable_delta = ctx->reliable_delta;
     a.mtype = YK_DAGGER;
     return a;
 }
@@ -488,7 +494,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     for (int c = 1; c < n_chains; ++c) {
         const yk_params& p = params[c];
         if (p.precision != p0.precision || p.cg_tol_mode != p0.cg_tol_mode || p.cg_tol != p0.cg_tol ||
-            p.cg_max_iter != p0.cg_max_iter || p.reliable_every != p0.reliable_every) {
+            p.cg_max_iter != p0.cg_max_iter || p.reliable_every != p0.reliable_every ||
+            p.reliable_delta != p0.reliable_delta) {
             set_error("chains of one context must share precision and CG settings");
             return YK_EINVAL;
         }
@@ -502,6 +509,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     ctx->tol = p0.cg_tol;
     ctx->max_iter = p0.cg_max_iter;
     ctx->reliable_every = p0.reliable_every;
+    ctx->reliable_delta = p0.reliable_delta;
     const bool mixed = ctx->precision == YK_MIXED;
     // occupancy queries and kernel attributes before any stream capture
     cg_max_grid(1, mixed);

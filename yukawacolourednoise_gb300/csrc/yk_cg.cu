@@ -76,7 +76,9 @@ struct SysLocal {
     int go;          // phase 1 forms p and t for this system in this pass
     int status;
     double rr, rr0, stop, alpha, alpha_im, beta;
-    double sx, sy;   // reduction results of the current phase
+    double cre, cim;         // p = beta p + c r (c = 1 except after a reliable update)
+    double rmax;             // largest |r| since the last reliable update (mixed)
+    double sx, sy, sz, sw;   // reduction results of the current phase
 };
 
 // Sense-reversing grid barrier (one counter word; block 0 adds 2^31 - (n-1),
@@ -126,7 +128,10 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 L.go = 0;
                 L.status = 0;
                 L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = 0.0;
-                L.sx = L.sy = 0.0;
+                L.cre = 1.0;
+                L.cim = 0.0;
+                L.rmax = 0.0;
+                L.sx = L.sy = L.sz = L.sw = 0.0;
                 ++n;
                 last = s;
             }
@@ -137,11 +142,12 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
     __syncthreads();
 }
 
-// Sums the (x, y) partials of every active system of the block: one warp
-// per system; lane l adds tiles l, l+32, l+64, ... in order, then a fixed
-// butterfly -- the same bits in every block that reduces the system.  Eight
-// tiles per lane are loaded before they are added, so a 256-tile system
-// costs one L2 round trip.
+// Sums the (x, y) partials -- and (z, w) when NV = 2 -- of every active
+// system of the block: one warp per system; lane l adds tiles l, l+32,
+// l+64, ... in order, then a fixed butterfly -- the same bits in every block
+// that reduces the system.  Eight tiles per lane are loaded before they are
+// added, so a 256-tile system costs one L2 round trip.
+template <int NV>
 __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -149,29 +155,41 @@ __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
     for (int j = w; j < nsl; j += nw) {
         if (!sl[j].active) continue;
         const SysDev& S = a.sys[sl[j].sys];
-        double ax = 0.0, ay = 0.0;
+        double acc[2 * NV];
+#pragma unroll
+        for (int c = 0; c < 2 * NV; ++c) acc[c] = 0.0;
         for (int base = lane; base < S.ntiles; base += 32 * U) {
-            double2 v[U];
+            double2 v[U][NV];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 // the load address is clamped into the system's tiles, so a load the
                 // compiler issues ahead of the range test never leaves the array
                 const int i = base + 32 * u;
                 const int ii = i < S.ntiles ? i : S.ntiles - 1;
-                const double2 t = ld_volatile2(reinterpret_cast<const double2*>(a.partial + S.tile0 + ii));
-                v[u] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
+                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    const double2 t = ld_volatile2(q + c);
+                    v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
+                }
             }
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                ax += v[u].x;
-                ay += v[u].y;
-            }
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int c = 0; c < NV; ++c) {
+                    acc[2 * c] += v[u][c].x;
+                    acc[2 * c + 1] += v[u][c].y;
+                }
         }
-        ax = warp_sum(ax);
-        ay = warp_sum(ay);
+#pragma unroll
+        for (int c = 0; c < 2 * NV; ++c) acc[c] = warp_sum(acc[c]);
         if (lane == 0) {
-            sl[j].sx = ax;
-            sl[j].sy = ay;
+            sl[j].sx = acc[0];
+            sl[j].sy = acc[1];
+            if constexpr (NV == 2) {
+                sl[j].sz = acc[2 % (2 * NV)];
+                sl[j].sw = acc[3 % (2 * NV)];
+            }
         }
     }
     __syncthreads();
@@ -269,10 +287,13 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
     return s;
 }
 
-// Block partial sums -> the tile's partial slot (thread 0), one pass.
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double* red)
+// Block partial sums -> the tile's partial slot (thread 0).  z, w: only
+// reliable updates pass them (a second block reduction).
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double* red,
+                                            bool zw = false, double z = 0.0, double w = 0.0)
 {
     const double2 s = block_sum2(x, y, red);
+    const double2 s2 = zw ? block_sum2(z, w, red + 32) : make_double2(0.0, 0.0);
     if (threadIdx.x == 0) {
 #ifdef YK_CG_CHECKED
         if (tile < 0 || tile >= a.tile_end) {
@@ -283,6 +304,8 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x,
         Partial p;
         p.x = s.x;
         p.y = s.y;
+        p.z = s2.x;
+        p.w = s2.y;
         a.partial[tile] = p;
     }
 }
@@ -363,7 +386,10 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
     while (k <= a.max_iter) {   // every system retires in phase 1 of k = max_iter at the latest
         const int cur = k & 1, prv = cur ^ 1;   // p_k lives in P[cur]
         // ---------------- phase 1
-        reduce_systems(a, sl, nsl);
+        if (redo)
+            reduce_systems<2>(a, sl, nsl);
+        else
+            reduce_systems<1>(a, sl, nsl);
         if (threadIdx.x == 0) {
             int want_ru = 0;
             for (int j = 0; j < nsl; ++j) {
@@ -375,6 +401,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                     L.rr = L.rr0 = rr;
                     L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(rr);
                     L.beta = 0.0;
+                    L.rmax = sqrt(rr);
                     if (!isfinite(rr)) retire(a, L, 0, YK_ENAN);
                     else if (!(sqrt(rr) > L.stop)) retire(a, L, 1, 0);
                     else if (a.max_iter <= 0) retire(a, L, 0, YK_ENOCONV);
@@ -386,26 +413,46 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                     retire(a, L, 0, YK_ENAN);
                     continue;
                 }
+                const double rn = sqrt(rr);
                 if (MIXED && !L.ru_done) {
-                    const bool cand = !(sqrt(rr) > L.stop);
+                    // reliable update: the FP32 residual claims convergence, has
+                    // dropped by reliable_delta since the last update, is due, or
+                    // the cap is reached (QUDA-style triggers)
+                    L.rmax = fmax(L.rmax, rn);
+                    const bool cand = !(rn > L.stop);
+                    const bool drop = rn < a.reliable_delta * L.rmax;
                     const bool due = a.reliable_every > 0 && (L.iters % a.reliable_every) == 0;
                     const bool cap = L.iters >= a.max_iter;
-                    if (cand || due || cap) {
+                    if (cand || drop || due || cap) {
                         L.ru = 1;
                         want_ru = 1;
                         continue;
                     }
+                    L.cre = 1.0;
+                    L.cim = 0.0;
                 } else {
-                    L.ru_done = 0;
-                    if (!(sqrt(rr) > L.stop)) {
+                    if (!(rn > L.stop)) {
                         L.rr = rr;
+                        L.ru_done = 0;
                         retire(a, L, 1, 0);
                         continue;
                     }
                     if (L.iters >= a.max_iter) {
                         L.rr = rr;
+                        L.ru_done = 0;
                         retire(a, L, 0, YK_ENOCONV);
                         continue;
+                    }
+                    if (MIXED) {
+                        // after a reliable update p is first made orthogonal to the
+                        // new residual: p <- p - gamma r, gamma = <r, p> / |r|^2, so
+                        // p_new = r + beta (p - gamma r) = beta p + (1 - beta gamma) r
+                        const double beta = rr / L.rr;
+                        const double gre = L.sz / rr, gim = L.sw / rr;
+                        L.cre = 1.0 - beta * gre;
+                        L.cim = -beta * gim;
+                        L.rmax = rn;
+                        L.ru_done = 0;
                     }
                 }
                 L.beta = rr / L.rr;
@@ -421,7 +468,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
             const SysDev& S = a.sys[L.sys];
             const int n = a.tiles[tile].y + threadIdx.x;
             if (n >= S.V) continue;
-            const W beta = (W)L.beta;
+            const W beta = (W)L.beta, cre = (W)L.cre, cim = (W)L.cim;
             const W* pold = Pv(S, k == 0 ? 0 : prv);
             const W* rv = Rv(S);
             const Nbr nbr = neighbours(n, S.Nt, S.Nx);
@@ -431,9 +478,18 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
             for (int q = 0; q < 5; ++q) {
                 st[q] = YK_LD(W, K, pold, m5[q]);
                 if (k > 0) {
+                    // p = beta p + c r  (c = 1 but after a reliable update)
                     const Site<W, K> r = YK_LD(W, K, rv, m5[q]);
 #pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) st[q].v[i] = fma(beta, st[q].v[i], r.v[i]);
+                    for (int e = 0; e < 4; ++e) {
+                        if constexpr (K == 1) {
+                            st[q].v[e] = fma(beta, st[q].v[e], cre * r.v[e]);
+                        } else {
+                            const W re = r.v[2 * e], im = r.v[2 * e + 1];
+                            st[q].v[2 * e] = fma(beta, st[q].v[2 * e], fma(cre, re, -cim * im));
+                            st[q].v[2 * e + 1] = fma(beta, st[q].v[2 * e + 1], fma(cre, im, cim * re));
+                        }
+                    }
                 }
             }
             const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
@@ -479,6 +535,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                     const SysDev& S = a.sys[L.sys];
                     const int n = a.tiles[tile].y + threadIdx.x;
                     double rr = 0.0;
+                    double2 rp = make_double2(0.0, 0.0);
                     if (n < S.V) {
                         Site<double, K> xv = YK_LD(double, K, S.x, n);
                         const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
@@ -492,16 +549,21 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                         YK_ST(W, K, S.xs32, n, zw);
                         const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
                         const Site<double, K> bv = YK_LD(double, K, S.b, n);
+                        const Site<W, K> pw = YK_LD(W, K, Pv(S, prv), n);   // p_{k-1}
                         Site<W, K> rw;
+                        Site<double, K> rd, pd;
 #pragma unroll
                         for (int i = 0; i < 4 * K; ++i) {
                             const double r = bv.v[i] - ax.v[i];
                             rr = fma(r, r, rr);
                             rw.v[i] = (W)r;
+                            rd.v[i] = r;
+                            pd.v[i] = (double)pw.v[i];
                         }
+                        rp = site_dot<double, K>(rd, pd);
                         YK_ST(W, K, Rv(S), n, rw);
                     }
-                    put_partial(a, tile, rr, 0.0, red);
+                    put_partial(a, tile, rr, 0.0, red, true, rp.x, rp.y);
                 }
                 __syncthreads();
                 if (threadIdx.x == 0)
@@ -535,7 +597,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         if (!gsync(a.bar, a.err)) return;
 
         // ---------------- phase 3: alpha; x += alpha p, r -= alpha Ap, |r|^2
-        reduce_systems(a, sl, nsl);
+        reduce_systems<1>(a, sl, nsl);
         if (threadIdx.x == 0) {
             for (int j = 0; j < nsl; ++j) {
                 SysLocal& L = sl[j];

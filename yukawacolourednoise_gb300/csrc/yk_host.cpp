@@ -265,7 +265,8 @@ void yk_params_default(yk_params* p)
     p->cg_tol_mode = YK_TOL_ABS;
     p->cg_tol = 1e-8;
     p->cg_max_iter = 1000;
-    p->reliable_every = 50;
+    p->reliable_every = 0;
+    p->reliable_delta = 0.1;
     p->fixed_dt = 0.0;
     p->init = YK_INIT_DRAND48;
 }
@@ -335,6 +336,7 @@ int yk_params_from_toml(const char* path, yk_params* p)
     get_d(kv, "gpu.cg_tol", &p->cg_tol);
     get_i(kv, "gpu.cg_max_iter", &p->cg_max_iter);
     get_i(kv, "gpu.reliable_every", &p->reliable_every);
+    get_d(kv, "gpu.reliable_delta", &p->reliable_delta);
     get_d(kv, "gpu.fixed_dt", &p->fixed_dt);
     if (kv.count("gpu.init")) {
         const std::string v = s("gpu.init");

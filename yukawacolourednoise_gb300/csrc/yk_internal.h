@@ -55,7 +55,8 @@ struct SysDev {
 
 // Per-tile reduction slot of the CG kernels.
 struct __align__(16) Partial {
-    double x, y;
+    double x, y;   // the reduction pair of every phase
+    double z, w;   // reliable updates: <r, p> of the new FP64 residual
 };
 
 // Per-system CG scalars, written by the finaliser block of each reduction.
@@ -86,6 +87,7 @@ struct CGArgs {
     int tol_mode;
     double tol;
     int reliable_every;
+    double reliable_delta;
 };
 
 // Per-chain device record of the Langevin step.
