@@ -163,6 +163,21 @@ int yk_dirac_apply(yk_ctx* ctx, int chain, const void* in, void* out, int dagger
 int yk_cg_solve(yk_ctx* ctx, int chain, const void* b, void* x, int mtype, double tol,
                 int tol_mode, int max_iter, int precision, yk_solve_stats* stats);
 
+/* No reference counterpart: the FP64 solve of yk_cg_solve for callers that
+ * cannot allocate device memory (cudaMalloc / cudaFree can synchronise the
+ * whole device and stall other streams, and hosts that embed the solver with
+ * a fixed device-memory budget must not grow it).  No context: sigma (V
+ * doubles), b and x (4V FP64 complex) are the caller's device buffers and
+ * m0, g, r the Dirac parameters of yk_action; the work runs on `stream`
+ * (a cudaStream_t, NULL = legacy stream) and the call returns after it.
+ * The scratch is one fixed device array sized for V = Nt*Nx <= 16384 sites;
+ * larger lattices return YK_EINVAL.  Calls that overlap in time share that
+ * array and race.  Make the first call on a device before any stream capture
+ * (it looks the array's address up once per device). */
+int yk_cg_solve_static(const double* sigma, int Nt, int Nx, double m0, double g, double r,
+                       const void* b, void* x, int mtype, double tol, int tol_mode, int max_iter,
+                       void* stream, yk_solve_stats* stats);
+
 /* FermionicDrift::getForce (code/src/FermionicDrift.cuh:15, FermionicDrift.cu:57-100):
  * F_n = -g Re sum_c conj(chi_{n,c}) eta_{n,c}, chi = D (D^dag D)^-1 eta, averaged
  * over the chain's n_rhs right-hand sides; eta (n_rhs * 4V FP64 complex, device)

@@ -135,6 +135,9 @@ _SIGS = {
     "yk_dirac_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "yk_cg_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                               C.c_int, C.c_int, C.POINTER(SolveStats)]),
+    "yk_cg_solve_static": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
+                                     C.POINTER(SolveStats)]),
     "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
