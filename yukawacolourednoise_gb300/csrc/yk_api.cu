@@ -57,6 +57,7 @@ struct Workspace {
     int2* d_tiles = nullptr;
     CGState* d_state = nullptr;
     Partial* d_partial = nullptr;
+    CGCoef* d_coef = nullptr;
     ChainDev* d_chain = nullptr;   // chain copy whose sys0 = 0 refers to d_sys
     int2* d_site_tiles = nullptr;
     std::vector<SysDev> h_sys;
@@ -98,6 +99,8 @@ struct yk_ctx {
     int n_sys_tiles = 0;
     CGState* d_state = nullptr;
     Partial* d_partial = nullptr;
+    CGCoef* d_coef = nullptr;
+    unsigned* d_flags = nullptr;   // neighbour flags of the CG launches (shared: one stream)
     GridBarrier* d_bar = nullptr;
     int* d_err = nullptr;
     int* d_nactive = nullptr;
@@ -199,6 +202,7 @@ CGArgs base_args(yk_ctx* ctx)
 {
     CGArgs a = {};
     a.bar = ctx->d_bar;
+    a.flags = ctx->d_flags;
     a.err = ctx->d_err;
     a.n_active = ctx->d_nactive;
     a.any_ru = ctx->d_anyru;
@@ -273,6 +277,7 @@ int enqueue_step(yk_ctx* ctx)
         a.eta_kind = 2;
         a.st = ctx->d_state;
         a.partial = ctx->d_partial;
+        a.coef = ctx->d_coef;
         YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
         prof_end(ctx, 1, e, 2);
     }
@@ -305,16 +310,18 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
     const size_t o_tiles = ar.reserve(sizeof(int2) * (size_t)R * nt);
     const size_t o_state = ar.reserve(sizeof(CGState) * R);
     const size_t o_part = ar.reserve(sizeof(Partial) * (size_t)R * nt);
+    const size_t o_coef = ar.reserve(sizeof(CGCoef) * R);
     const size_t o_chain = ar.reserve(sizeof(ChainDev));
     const size_t o_stile = ar.reserve(sizeof(int2) * nt);
     const size_t o_point = ar.reserve(v64);
     const size_t o_work = ar.reserve(v64);
     const size_t o_corr = ar.reserve(sizeof(double) * C.Nt);
-    std::vector<size_t> o_vec(R * 12);
+    constexpr int NVEC = 15;   // FP64: x r0 r1 p0 p1 t Ap; FP32: r0 r1 p0 p1 t Ap xs; diag
+    std::vector<size_t> o_vec(R * NVEC);
     for (int j = 0; j < R; ++j) {
-        for (int q = 0; q < 6; ++q) o_vec[j * 12 + q] = ar.reserve(v64);       // x r p0 p1 t Ap
-        for (int q = 6; q < 12; ++q)                                             // r p0 p1 t Ap xs
-            o_vec[j * 12 + q] = ar.reserve((q == 6 || q == 9) ? 2 * v32 : v32);   // r and t hold two vectors
+        for (int q = 0; q < 7; ++q) o_vec[j * NVEC + q] = ar.reserve(v64);
+        for (int q = 7; q < 14; ++q) o_vec[j * NVEC + q] = ar.reserve(v32);
+        o_vec[j * NVEC + 14] = ar.reserve(sizeof(float) * (size_t)V);
     }
     void* mem = nullptr;
     if (cudaMalloc(&mem, ar.used) != cudaSuccess) {
@@ -329,6 +336,7 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
     w.d_tiles = ar.at<int2>(o_tiles);
     w.d_state = ar.at<CGState>(o_state);
     w.d_partial = ar.at<Partial>(o_part);
+    w.d_coef = ar.at<CGCoef>(o_coef);
     w.d_chain = ar.at<ChainDev>(o_chain);
     w.d_site_tiles = ar.at<int2>(o_stile);
     w.point = ar.at<double>(o_point);
@@ -350,18 +358,22 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
         S.g = C.a.g;
         S.r = C.a.r;
         S.sigma = C.phi;
-        S.x = ar.at<double>(o_vec[j * 12 + 0]);
-        S.r64 = ar.at<double>(o_vec[j * 12 + 1]);
-        S.p64[0] = ar.at<double>(o_vec[j * 12 + 2]);
-        S.p64[1] = ar.at<double>(o_vec[j * 12 + 3]);
-        S.t64 = ar.at<double>(o_vec[j * 12 + 4]);
-        S.Ap64 = ar.at<double>(o_vec[j * 12 + 5]);
-        S.r32 = ar.at<float>(o_vec[j * 12 + 6]);
-        S.p32[0] = ar.at<float>(o_vec[j * 12 + 7]);
-        S.p32[1] = ar.at<float>(o_vec[j * 12 + 8]);
-        S.t32 = ar.at<float>(o_vec[j * 12 + 9]);
-        S.Ap32 = ar.at<float>(o_vec[j * 12 + 10]);
-        S.xs32 = ar.at<float>(o_vec[j * 12 + 11]);
+        const size_t* o = &o_vec[(size_t)j * NVEC];
+        S.x = ar.at<double>(o[0]);
+        S.r64[0] = ar.at<double>(o[1]);
+        S.r64[1] = ar.at<double>(o[2]);
+        S.p64[0] = ar.at<double>(o[3]);
+        S.p64[1] = ar.at<double>(o[4]);
+        S.t64 = ar.at<double>(o[5]);
+        S.Ap64 = ar.at<double>(o[6]);
+        S.r32[0] = ar.at<float>(o[7]);
+        S.r32[1] = ar.at<float>(o[8]);
+        S.p32[0] = ar.at<float>(o[9]);
+        S.p32[1] = ar.at<float>(o[10]);
+        S.t32 = ar.at<float>(o[11]);
+        S.Ap32 = ar.at<float>(o[12]);
+        S.xs32 = ar.at<float>(o[13]);
+        S.diag32 = ar.at<float>(o[14]);
         S.gen_eta = 0;
         for (int t = 0; t < nt; ++t) tiles[(size_t)j * nt + t] = make_int2(j, t * kTile);
     }
@@ -394,6 +406,7 @@ int ws_solve(yk_ctx* ctx, int c, int count, int mtype, double tol, int tol_mode,
     a.eta_kind = 0;
     a.st = w.d_state;
     a.partial = w.d_partial;
+    a.coef = w.d_coef;
     a.mtype = mtype;
     a.tol = tol;
     a.tol_mode = tol_mode;
@@ -441,6 +454,7 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
     a.eta_kind = kind;
     a.st = ctx->d_state;
     a.partial = ctx->d_partial;
+    a.coef = ctx->d_coef;
     YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, nullptr));
     std::vector<CGState> st(C.n_rhs_step);
     YK_CK(cudaMemcpyAsync(st.data(), ctx->d_state + C.sys0, sizeof(CGState) * C.n_rhs_step,
@@ -568,7 +582,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     };
     std::vector<COff> co(n_chains);
     struct SOff {
-        size_t b, x, r64, p0, p1, t64, ap64, r32, q0, q1, t32, ap32, xs;
+        size_t b, x, r0, r1, p0, p1, t64, ap64, s0, s1, q0, q1, t32, ap32, xs, diag;
     };
     std::vector<SOff> so(nsys);
     for (int c = 0; c < n_chains; ++c) {
@@ -592,14 +606,17 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             o.x = ar.reserve(d);
             o.t64 = ar.reserve(d);
             if (mixed) {
-                o.r32 = ar.reserve(f);
+                o.s0 = ar.reserve(f);
+                o.s1 = ar.reserve(f);
                 o.q0 = ar.reserve(f);
                 o.q1 = ar.reserve(f);
                 o.t32 = ar.reserve(f);
                 o.ap32 = ar.reserve(f);
                 o.xs = ar.reserve(f);
+                o.diag = ar.reserve(sizeof(float) * V);
             } else {
-                o.r64 = ar.reserve(d);
+                o.r0 = ar.reserve(d);
+                o.r1 = ar.reserve(d);
                 o.p0 = ar.reserve(d);
                 o.p1 = ar.reserve(d);
                 o.ap64 = ar.reserve(d);
@@ -611,6 +628,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     const size_t o_systiles = ar.reserve(sizeof(int2) * (nsys_tiles > 0 ? nsys_tiles : 1));
     const size_t o_state = ar.reserve(sizeof(CGState) * (nsys > 0 ? nsys : 1));
     const size_t o_partial = ar.reserve(sizeof(Partial) * (nsys_tiles > 0 ? nsys_tiles : 1));
+    const size_t o_coef = ar.reserve(sizeof(CGCoef) * (nsys > 0 ? nsys : 1));
+    const size_t o_flags = ar.reserve(sizeof(unsigned) * kFlagStride * (size_t)kMaxGrid);
     const size_t o_bar = ar.reserve(sizeof(GridBarrier));
     const size_t o_err = ar.reserve(sizeof(int) * 4);
     const size_t o_sitetiles = ar.reserve(sizeof(int2) * nsite_tiles);
@@ -637,6 +656,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     ctx->d_sys_tiles = ar.at<int2>(o_systiles);
     ctx->d_state = ar.at<CGState>(o_state);
     ctx->d_partial = ar.at<Partial>(o_partial);
+    ctx->d_coef = ar.at<CGCoef>(o_coef);
+    ctx->d_flags = ar.at<unsigned>(o_flags);
     ctx->d_bar = ar.at<GridBarrier>(o_bar);
     ctx->d_err = ar.at<int>(o_err);
     ctx->d_nactive = ctx->d_err + 1;
@@ -686,14 +707,17 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             S.x = ar.at<double>(q.x);
             S.t64 = ar.at<double>(q.t64);
             if (mixed) {
-                S.r32 = ar.at<float>(q.r32);
+                S.r32[0] = ar.at<float>(q.s0);
+                S.r32[1] = ar.at<float>(q.s1);
                 S.p32[0] = ar.at<float>(q.q0);
                 S.p32[1] = ar.at<float>(q.q1);
                 S.t32 = ar.at<float>(q.t32);
                 S.Ap32 = ar.at<float>(q.ap32);
                 S.xs32 = ar.at<float>(q.xs);
+                S.diag32 = ar.at<float>(q.diag);
             } else {
-                S.r64 = ar.at<double>(q.r64);
+                S.r64[0] = ar.at<double>(q.r0);
+                S.r64[1] = ar.at<double>(q.r1);
                 S.p64[0] = ar.at<double>(q.p0);
                 S.p64[1] = ar.at<double>(q.p1);
                 S.Ap64 = ar.at<double>(q.ap64);

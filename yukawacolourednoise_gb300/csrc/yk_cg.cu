@@ -1,21 +1,37 @@
 // yk_cg.cu -- batched CG on D^dag D (or D D^dag) as one persistent
 // cooperative kernel per solve: the algorithm of code/src/CGsolver.cu:72-170
-// -- x0 = 0, r = p = b, alpha = |r|^2 / <p, A p>, x += alpha p,
-// r -= alpha A p, beta = |r'|^2 / |r|^2, p = r + beta p, stop when
-// sqrt(|r|^2) <= tol -- in three phases per iteration (the reference pays 15
-// grid syncs): p is formed on the fly inside the first D apply
-// (double-buffered), the second D apply carries <p, Ap>, the axpys carry |r|^2.
+// (x0 = 0, r = p = b, alpha = |r|^2 / <p, A p>, x += alpha p, r -= alpha A p,
+// beta = |r'|^2 / |r|^2, p = r + beta p, stop when sqrt(|r|^2) <= tol or after
+// IterMax iterations) with one neighbour synchronisation and one grid-wide
+// reduction per iteration (the reference pays 15 grid syncs):
 //
-// FP64: every vector and scalar in FP64.  MIXED: FP32 vectors and stencils,
-// FP64 partial sums and scalars, FP64 reliable updates (the solution is kept
-// as an FP64 x plus an FP32 increment; r = b - A x is recomputed in FP64
-// when the FP32 residual claims convergence, every `reliable_every`
-// iterations and at the cap; convergence is only declared on that residual).
+//   A(k): r_k = r_{k-1} - alpha A p_{k-1} and p_k = r_k + beta p_{k-1} are
+//         formed on the fly at each site and its four neighbours, t = D_first
+//         p_k is stored, x += alpha p_{k-1}                -> neighbour sync
+//   B(k): A p_k = D_second t; per-tile partials of |r_k|^2, |A p_k|^2,
+//         <p_k, A p_k> and <r_k, A p_k>                     -> grid reduction
 //
-// One launch solves every (chain, rhs) system; each block owns a contiguous
-// range of 256-site tiles; a bounded sense-reversing grid barrier separates
-// phases; reductions are deterministic (per-tile partials, summed in tile
-// order by every block that needs them, right after the barrier).
+// The block that arrives last at the grid barrier sums the partials of every
+// system in a fixed order and runs the scalar recurrence: the stopping rule on
+// the directly summed |r_k|^2, alpha_k = |r_k|^2 / <p_k, A p_k>, |r_{k+1}|^2 =
+// |r_k - alpha_k A p_k|^2 expanded in the sums, beta_k = |r_{k+1}|^2 / |r_k|^2.
+// It publishes the coefficients together with the barrier; the other blocks
+// wait only for that.  r and p are double-buffered (A(k+1) of one block may
+// overlap the neighbour reads of A(k) of another); t and A p are not (a grid
+// reduction or a neighbour sync separates their writes from the last reads).
+//
+// FP64: every vector and scalar in FP64.  MIXED: FP32 vectors, stencils and
+// per-warp sums, FP64 partial sums and scalars; the solution is an FP64 x plus
+// an FP32 increment.  When |r| reaches the target, drops below reliable_delta
+// times its maximum since the last update, every reliable_every iterations and
+// at the cap, a reliable update folds the increment into x, recomputes
+// r = b - A x in FP64, re-orthogonalises p against it (p <- p - <r, p> r /
+// |r|^2) and convergence is only declared on that FP64 residual.
+//
+// One launch solves every (chain, rhs) system; blocks own contiguous ranges of
+// 256-site tiles and wait only for the blocks that hold their stencil
+// neighbours.  Every wait is bounded (about 2 s): a block that gives up sets
+// YK_ETIMEOUT and every block leaves.
 #include <cstdio>
 #include <type_traits>
 
@@ -25,9 +41,9 @@
 namespace yk {
 
 #ifdef YK_CG_CHECKED
-// Self-checking build: every site access of the CG kernels is checked
-// against the system's volume and for null buffers; the first bad access is
-// printed with its source line and skipped.
+// Self-checking build: every site access of the CG kernel is checked against
+// the system's volume and for null buffers; the first bad access is printed
+// with its source line and skipped.
 __device__ int g_cg_bad;
 
 template <typename R, int K>
@@ -64,53 +80,80 @@ __device__ void chk_st(R* p, int64_t n, const Site<R, K>& v, int V, int line)
 namespace {
 
 constexpr int kMaxSysPerBlock = 48;
+constexpr int kMaxDeps = 64;
+constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
-// Per-block view of one system whose tiles fall in the block's range.
-struct SysLocal {
-    int sys;
-    int owner;       // this block holds the system's first tile: writes CGState
-    int active;
-    int iters;
-    int ru;          // reliable update pending (mixed)
-    int ru_done;     // the last reduction came from a reliable update
-    int go;          // phase 1 forms p and t for this system in this pass
-    int status;
-    double rr, rr0, stop, alpha, alpha_im, beta;
-    double cre, cim;         // p = beta p + c r (c = 1 except after a reliable update)
-    double rmax;             // largest |r| since the last reliable update (mixed)
-    double sx, sy, sz, sw;   // reduction results of the current phase
+// What a system does in the next pass (published with each grid reduction).
+enum CGMode {
+    kIdle = 0,   // retired
+    kStep = 1,   // ordinary iteration
+    kRu = 2,     // reliable update (mixed): fold x, then r = b - A x in FP64
+    kRedo = 3,   // after a reliable update: p = c r + beta p from the FP64 residual
+    kWait = 4,   // another system's reliable update runs; this one already stepped
 };
 
-// Sense-reversing grid barrier (one counter word; block 0 adds 2^31 - (n-1),
-// the others 1, so bit 31 flips once every block has arrived).  Bounded:
-// after kBarrierCycles it records YK_ETIMEOUT and every caller leaves.
-__device__ __forceinline__ bool gsync(GridBarrier* b, int* err)
+// Per-block copy of the coefficients of one system whose tiles it owns.
+struct SysLocal {
+    int sys;
+    int mode;
+    double alpha_re, alpha_im, beta, c_re, c_im;
+};
+
+// Blocks holding stencil neighbours of this block's sites.
+struct Deps {
+    int n;
+    int all;   // more than kMaxDeps: wait for every block
+    int b[kMaxDeps];
+};
+
+// True when the wait should end: timed out (recorded) or another block failed.
+__device__ __forceinline__ bool wait_over(long long t0, int* err)
+{
+    if (clock64() - t0 > kWaitCycles) {
+        atomicCAS(err, 0, YK_ETIMEOUT);
+        return true;
+    }
+    return *(volatile int*)err != 0;
+}
+
+__device__ __forceinline__ void wait_flag(const unsigned* f, unsigned epoch, int* err)
+{
+    const volatile unsigned* q = f;
+    const long long t0 = clock64();
+    while ((int)(*q - epoch) < 0)
+        if (wait_over(t0, err)) return;
+}
+
+// Neighbour synchronisation: publish this block's epoch, wait until every
+// block in `d` has published it too.  Release: bar.sync + thread 0's fence;
+// acquire: each waiting thread's fence + bar.sync.
+__device__ bool nsync(const CGArgs& a, unsigned epoch, const Deps& d)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned inc = (blockIdx.x == 0) ? (0x80000000u - (gridDim.x - 1)) : 1u;
         __threadfence();
-        const unsigned old = atomicAdd(&b->count, inc);
-        volatile unsigned* vc = &b->count;
-        const long long t0 = clock64();
-        while (((*vc ^ old) & 0x80000000u) == 0) {
-            if (clock64() - t0 > kBarrierCycles) {
-                atomicCAS(err, 0, YK_ETIMEOUT);
-                break;
-            }
-            __nanosleep(20);
-        }
+        *(volatile unsigned*)(a.flags + (size_t)blockIdx.x * kFlagStride) = epoch;
+    }
+    if (d.all) {
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            if (b != (int)blockIdx.x) wait_flag(a.flags + (size_t)b * kFlagStride, epoch, a.err);
+        __threadfence();
+    } else if ((int)threadIdx.x < d.n) {
+        wait_flag(a.flags + (size_t)d.b[threadIdx.x] * kFlagStride, epoch, a.err);
         __threadfence();
     }
     __syncthreads();
-    return *(volatile int*)err == 0;
+    return *(volatile int*)a.err == 0;
 }
 
-// Builds the block's system table from its tile range [tb, te).
-__device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* nsl, int* tile_slot)
+// The block's system table and neighbour blocks, from its tile range [tb, te).
+// A tile's stencil reaches at most Nx sites away (wrapping within its system),
+// i.e. fewer than Nx / 256 + 2 tiles; only tiles that close to an end of the
+// block's range or of their system can reach another block.
+__device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* nsl, int* tslot, Deps* dp)
 {
     if (threadIdx.x == 0) {
-        int n = 0, last = -1;
+        int n = 0, last = -1, nd = 0, all = 0;
         for (int t = tb; t < te; ++t) {
             const int s = a.tiles[t].x;
             if (s != last) {
@@ -120,55 +163,178 @@ __device__ void build_table(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 }
                 SysLocal& L = sl[n];
                 L.sys = s;
-                L.owner = (a.sys[s].tile0 >= tb && a.sys[s].tile0 < te) ? 1 : 0;
-                L.active = 1;
-                L.iters = 0;
-                L.ru = 0;
-                L.ru_done = 0;
-                L.go = 0;
-                L.status = 0;
-                L.rr = L.rr0 = L.stop = L.alpha = L.alpha_im = L.beta = 0.0;
-                L.cre = 1.0;
-                L.cim = 0.0;
-                L.rmax = 0.0;
-                L.sx = L.sy = L.sz = L.sw = 0.0;
+                L.mode = kStep;
+                L.alpha_re = L.alpha_im = L.beta = L.c_im = 0.0;
+                L.c_re = 1.0;
                 ++n;
                 last = s;
             }
-            tile_slot[t - tb] = n - 1;
+            tslot[t - tb] = n - 1;
+            const SysDev& S = a.sys[s];
+            const int h = S.Nx / kTile + 2;
+            const int rel = t - S.tile0;
+            if (t - tb >= h && te - 1 - t >= h && rel >= h && S.ntiles - 1 - rel >= h) continue;
+            for (int d = -h; d <= h && !all; ++d) {
+                if (d == 0) continue;
+                int q = (rel + d) % S.ntiles;
+                if (q < 0) q += S.ntiles;
+                const int blk = (S.tile0 + q - a.tile_begin) / a.tiles_per_block;
+                if (blk == (int)blockIdx.x) continue;
+                bool seen = false;
+                for (int i = 0; i < nd && !seen; ++i) seen = (dp->b[i] == blk);
+                if (seen) continue;
+                if (nd == kMaxDeps)
+                    all = 1;
+                else
+                    dp->b[nd++] = blk;
+            }
         }
         *nsl = n;
+        dp->n = nd;
+        dp->all = all;
     }
     __syncthreads();
 }
 
-// Sums the (x, y) partials -- and (z, w) when NV = 2 -- of every active
-// system of the block: one warp per system; lane l adds tiles l, l+32,
-// l+64, ... in order, then a fixed butterfly -- the same bits in every block
-// that reduces the system.  Eight tiles per lane are loaded before they are
-// added, so a 256-tile system costs one L2 round trip.
-template <int NV>
-__device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
+// Coefficients of the block's systems after a grid reduction.
+__device__ void load_coefs(const CGArgs& a, SysLocal* sl, int nsl, int* s_nact, int* s_anyru)
+{
+    for (int j = threadIdx.x; j < nsl; j += blockDim.x) {
+        const volatile CGCoef& c = a.coef[sl[j].sys];
+        sl[j].mode = c.mode;
+        sl[j].alpha_re = c.alpha_re;
+        sl[j].alpha_im = c.alpha_im;
+        sl[j].beta = c.beta;
+        sl[j].c_re = c.c_re;
+        sl[j].c_im = c.c_im;
+    }
+    if (threadIdx.x == 0) {
+        *s_nact = *(volatile int*)a.n_active;
+        *s_anyru = *(volatile int*)a.any_ru;
+    }
+    __syncthreads();
+}
+
+// Scalar recurrence of one system after its partials were summed (one thread).
+// s: |r|^2, |Ap|^2, <p,Ap> re/im, <r,Ap> re/im; after a reliable update
+// |r|^2 and <r, p_{k-1}> re/im in s[0], s[2], s[3].
+template <bool MIXED>
+__device__ void scalar_step(const CGArgs& a, int j, int k, bool ru_round, const double* s, int* s_active,
+                            int* s_ru)
+{
+    volatile CGState& st = a.st[j];
+    volatile CGCoef& cf = a.coef[j];
+    auto retire = [&](int conv, int status) {
+        st.active = 0;
+        st.converged = conv;
+        st.status = status;
+        cf.mode = kIdle;
+    };
+    const double rr = s[0];
+    st.rr = rr;
+    st.iters = k;
+    if (ru_round) {
+        st.n_ru = st.n_ru + 1;
+        if (!isfinite(rr)) return retire(0, YK_ENAN);
+        if (!(sqrt(rr) > st.stop)) return retire(1, 0);
+        if (k >= a.max_iter) return retire(0, YK_ENOCONV);
+        // p_k = r + beta (p_{k-1} - gamma r), gamma = <r, p_{k-1}> / |r|^2
+        const double beta = rr / st.rr_prev;
+        cf.beta = beta;
+        cf.c_re = 1.0 - beta * (s[2] / rr);
+        cf.c_im = -beta * (s[3] / rr);
+        cf.mode = kRedo;
+        st.rmax = sqrt(rr);
+        atomicAdd(s_active, 1);
+        return;
+    }
+    if (k == 0) {
+        st.rr0 = rr;
+        st.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(rr);
+        st.rmax = sqrt(rr);
+    }
+    if (!isfinite(rr)) return retire(0, YK_ENAN);
+    // mixed: x is exact only at k = 0 and after a reliable update
+    if ((!MIXED || k == 0) && !(sqrt(rr) > st.stop)) return retire(1, 0);
+    if (k >= a.max_iter) return retire(0, YK_ENOCONV);
+    // alpha = rr / <p, Ap>, Smith's complex division (CGsolver.cu:137)
+    const double c = s[2], d = s[3];
+    double ar, ai;
+    if (fabs(c) >= fabs(d)) {
+        const double q = d / c, den = c + d * q;
+        ar = rr / den;
+        ai = (-rr * q) / den;
+    } else {
+        const double q = c / d, den = c * q + d;
+        ar = (rr * q) / den;
+        ai = -rr / den;
+    }
+    if (!isfinite(ar) || !isfinite(ai)) return retire(0, YK_ENAN);
+    // |r - alpha q|^2 = |r|^2 - 2 Re(alpha <r, q>) + |alpha|^2 |q|^2
+    double est = rr - 2.0 * (ar * s[4] - ai * s[5]) + (ar * ar + ai * ai) * s[1];
+    if (!(est > 0.0)) est = 0.0;
+    st.rr_prev = rr;
+    cf.alpha_re = ar;
+    cf.alpha_im = ai;
+    cf.beta = est / rr;
+    cf.c_re = 1.0;
+    cf.c_im = 0.0;
+    int mode = kStep;
+    if constexpr (MIXED) {
+        const double rn = sqrt(rr), en = sqrt(est);
+        const double rmax = fmax(st.rmax, rn);
+        st.rmax = rmax;
+        const bool cand = !(rn > st.stop) || !(en > st.stop);
+        const bool drop = en < a.reliable_delta * rmax;
+        const bool due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
+        const bool cap = k + 1 >= a.max_iter;
+        if (cand || drop || due || cap) {
+            mode = kRu;
+            atomicOr(s_ru, 1);
+        }
+    }
+    cf.mode = mode;
+    atomicAdd(s_active, 1);
+}
+
+// The last block at a grid barrier: sums the partials of every system that
+// took part in the pass (one warp per system; lane l adds tiles l, l+32, ...
+// in order, then a fixed butterfly) and runs the scalar recurrence.
+template <bool MIXED>
+__device__ void finish_reduction(const CGArgs& a, int k, bool ru_round, int* s_active, int* s_ru)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) {
+        *s_active = 0;
+        *s_ru = 0;
+    }
+    __syncthreads();
     constexpr int U = 8;
-    for (int j = w; j < nsl; j += nw) {
-        if (!sl[j].active) continue;
-        const SysDev& S = a.sys[sl[j].sys];
-        double acc[2 * NV];
+    for (int j = a.sys_first + w; j < a.sys_first + a.sys_count; j += nw) {
+        const int mode = *(volatile int*)&a.coef[j].mode;
+        if (mode == kIdle) continue;
+        if (ru_round && mode != kRu) {
+            if (lane == 0) {
+                *(volatile int*)&a.coef[j].mode = kWait;
+                atomicAdd(s_active, 1);
+            }
+            continue;
+        }
+        const SysDev& S = a.sys[j];
+        double acc[6];
 #pragma unroll
-        for (int c = 0; c < 2 * NV; ++c) acc[c] = 0.0;
+        for (int q = 0; q < 6; ++q) acc[q] = 0.0;
         for (int base = lane; base < S.ntiles; base += 32 * U) {
-            double2 v[U][NV];
+            double2 v[U][3];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                // the load address is clamped into the system's tiles, so a load the
-                // compiler issues ahead of the range test never leaves the array
+                // the address is clamped into the system's tiles, so a load issued
+                // ahead of the range test never leaves the array
                 const int i = base + 32 * u;
                 const int ii = i < S.ntiles ? i : S.ntiles - 1;
                 const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
 #pragma unroll
-                for (int c = 0; c < NV; ++c) {
+                for (int c = 0; c < 3; ++c) {
                     const double2 t = ld_volatile2(q + c);
                     v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
                 }
@@ -176,54 +342,68 @@ __device__ void reduce_systems(const CGArgs& a, SysLocal* sl, int nsl)
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
-                for (int c = 0; c < NV; ++c) {
+                for (int c = 0; c < 3; ++c) {
                     acc[2 * c] += v[u][c].x;
                     acc[2 * c + 1] += v[u][c].y;
                 }
         }
 #pragma unroll
-        for (int c = 0; c < 2 * NV; ++c) acc[c] = warp_sum(acc[c]);
-        if (lane == 0) {
-            sl[j].sx = acc[0];
-            sl[j].sy = acc[1];
-            if constexpr (NV == 2) {
-                sl[j].sz = acc[2 % (2 * NV)];
-                sl[j].sw = acc[3 % (2 * NV)];
-            }
-        }
+        for (int q = 0; q < 6; ++q) acc[q] = warp_sum(acc[q]);
+        if (lane == 0) scalar_step<MIXED>(a, j, k, ru_round, acc, s_active, s_ru);
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+        *(volatile int*)a.n_active = *s_active;
+        *(volatile int*)a.any_ru = *s_ru;
+    }
 }
 
-__device__ void retire(const CGArgs& a, SysLocal& L, int converged, int status)
+// Grid barrier that also completes the reduction of the pass: the last block
+// to arrive sums the partials and publishes the coefficients, then advances
+// the generation the others wait on.
+template <bool MIXED>
+__device__ bool grid_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, int* s_flag, int* s_active,
+                            int* s_ru)
 {
-    L.active = 0;
-    if (status) L.status = status;
-    if (L.owner) {
-        volatile CGState& s = a.st[L.sys];
-        s.converged = converged;
-        s.status = L.status;
-        s.iters = L.iters;
-        s.rr = L.rr;
-        s.rr0 = L.rr0;
-        s.active = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
         __threadfence();
-        atomicSub(a.n_active, 1);
+        const unsigned old = atomicAdd(&a.bar->arrive, 1u);
+        const int last = (old == gridDim.x - 1) ? 1 : 0;
+        if (last) __threadfence();
+        *s_flag = last;
     }
+    __syncthreads();
+    if (*s_flag) {
+        finish_reduction<MIXED>(a, k, ru_round, s_active, s_ru);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            *(volatile unsigned*)&a.bar->arrive = 0u;
+            __threadfence();
+            *(volatile unsigned*)&a.bar->gen = gen + 1u;
+        }
+    } else if (threadIdx.x == 0) {
+        const volatile unsigned* g = &a.bar->gen;
+        const long long t0 = clock64();
+        while (*g == gen)
+            if (wait_over(t0, a.err)) break;
+        __threadfence();
+    }
+    __syncthreads();
+    ++gen;
+    return *(volatile int*)a.err == 0;
 }
 
-__device__ void publish(const CGArgs& a, const SysLocal& L, int n_ru)
+template <typename W, bool MIXED>
+__device__ __forceinline__ W diag_of(const SysDev& S, int n)
 {
-    if (L.owner) {
-        volatile CGState& s = a.st[L.sys];
-        s.iters = L.iters;
-        s.rr = L.rr;
-        s.rr0 = L.rr0;
-        s.n_ru = n_ru;
-    }
+    if constexpr (MIXED)
+        return S.diag32[n];
+    else
+        return 2.0 * S.r + S.m0 + S.g * S.sigma[n];
 }
 
-template <typename W, int K>
+template <typename W, int K, bool MIXED>
 __device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& S, bool dag)
 {
     const Nbr nb = neighbours(n, S.Nt, S.Nx);
@@ -232,15 +412,17 @@ __device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& 
     const Site<W, K> td = YK_LD(W, K, in, nb.td);
     const Site<W, K> xu = YK_LD(W, K, in, nb.xu);
     const Site<W, K> xd = YK_LD(W, K, in, nb.xd);
-    const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
+    const W diag = diag_of<W, MIXED>(S, n);
     return dag ? dirac_combine<W, K, true>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm)
                : dirac_combine<W, K, false>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm);
 }
 
+// sum conj(a) b over one site, in the vectors' precision
 template <typename W, int K>
-__device__ __forceinline__ double2 site_dot(const Site<W, K>& a, const Site<W, K>& b)
+__device__ __forceinline__ void site_dot(const Site<W, K>& a, const Site<W, K>& b, W& re, W& im)
 {
-    W re = 0, im = 0;
+    re = W(0);
+    im = W(0);
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         if constexpr (K == 1) {
@@ -251,9 +433,18 @@ __device__ __forceinline__ double2 site_dot(const Site<W, K>& a, const Site<W, K
             im = fma(ar, bi, fma(-ai, br, im));
         }
     }
-    return make_double2((double)re, (double)im);
 }
 
+template <typename W, int K>
+__device__ __forceinline__ W site_norm2(const Site<W, K>& a)
+{
+    W s = W(0);
+#pragma unroll
+    for (int i = 0; i < 4 * K; ++i) s = fma(a.v[i], a.v[i], s);
+    return s;
+}
+
+// y += (ar + i ai) v
 template <typename W, int K>
 __device__ __forceinline__ void site_axpy(Site<W, K>& y, W ar, W ai, const Site<W, K>& v)
 {
@@ -267,6 +458,24 @@ __device__ __forceinline__ void site_axpy(Site<W, K>& y, W ar, W ai, const Site<
             y.v[2 * e + 1] = fma(ar, vi, fma(ai, vr, y.v[2 * e + 1]));
         }
     }
+}
+
+// c r + beta p  (c complex)
+template <typename W, int K>
+__device__ __forceinline__ Site<W, K> p_next(const Site<W, K>& r, const Site<W, K>& p, W beta, W cre, W cim)
+{
+    Site<W, K> o;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        if constexpr (K == 1) {
+            o.v[e] = fma(beta, p.v[e], cre * r.v[e]);
+        } else {
+            const W re = r.v[2 * e], im = r.v[2 * e + 1];
+            o.v[2 * e] = fma(beta, p.v[2 * e], fma(cre, re, -cim * im));
+            o.v[2 * e + 1] = fma(beta, p.v[2 * e + 1], fma(cre, im, cim * re));
+        }
+    }
+    return o;
 }
 
 template <int K>
@@ -287,59 +496,68 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
     return s;
 }
 
-// Block partial sums -> the tile's partial slot (thread 0).  z, w: only
-// reliable updates pass them (a second block reduction).
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, double x, double y, double* red,
-                                            bool zw = false, double z = 0.0, double w = 0.0)
+// Block sums of a tile's six values -> its partial slot.  Per-site values and
+// warp sums in T (FP32 for the mixed solver), FP64 across the warps.  Values
+// listed in `skip` are known to be zero and are not reduced.
+template <typename T, int SKIP_MASK>
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, T (&v)[6], double* red)
 {
-    const double2 s = block_sum2(x, y, red);
-    const double2 s2 = zw ? block_sum2(z, w, red + 32) : make_double2(0.0, 0.0);
-    if (threadIdx.x == 0) {
-#ifdef YK_CG_CHECKED
-        if (tile < 0 || tile >= a.tile_end) {
-            if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d end %d\n", tile, a.tile_end);
-            return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        if (!((SKIP_MASK >> i) & 1))
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) red[w * 6 + i] = (double)v[i];
+    __syncthreads();
+    if (w == 0) {
+        double t[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            t[i] = lane < nw ? red[lane * 6 + i] : 0.0;
+            if (!((SKIP_MASK >> i) & 1)) t[i] = warp_sum(t[i]);
         }
+        if (lane == 0) {
+#ifdef YK_CG_CHECKED
+            if (tile < a.tile_begin || tile >= a.tile_end) {
+                if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
+                return;
+            }
 #endif
-        Partial p;
-        p.x = s.x;
-        p.y = s.y;
-        p.z = s2.x;
-        p.w = s2.y;
-        a.partial[tile] = p;
+            Partial p;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) p.v[i] = t[i];
+            a.partial[tile] = p;
+        }
     }
 }
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// Hestenes-Stiefel CG (the reference's algorithm), three phases per iteration:
-//   1. reduce |r|^2 -> beta / convergence; p = r + beta p formed on the fly at
-//      the five stencil sites; t = D_first p
-//   2. Ap = D_second t; partial <p, Ap>
-//   3. reduce -> alpha (Smith division); x += alpha p, r -= alpha Ap; |r|^2
-// W = double: the plain FP64 solver.  W = float (MIXED): FP32 vectors and
-// stencil, FP64 partial sums and scalars.  When the FP32 residual claims
-// convergence, every `reliable_every` iterations and at the iteration cap,
-// phase 1 is followed by a reliable update -- t64 = D_first (x + xs) and
-// r = b - D_second t64 in FP64, x += xs, xs = 0 -- and phase 1 is run again
-// for the systems concerned on that FP64 residual; convergence is only
-// declared on it.
-// ---------------------------------------------------------------------------
 template <int K, bool MIXED>
 __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
 {
     using W = typename std::conditional<MIXED, float, double>::type;
+    // the imaginary parts (slots 3 and 5) vanish on the real K = 1 path
+    constexpr int kSkipIm = (K == 1) ? ((1 << 3) | (1 << 5)) : 0;
     __shared__ double red[64];
     __shared__ SysLocal sl[kMaxSysPerBlock];
     __shared__ int nsl;
     __shared__ int tslot[kMaxTilesPerBlock];
+    __shared__ Deps deps;
+    __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
-    build_table(a, tb, te, sl, &nsl, tslot);
+    setup_block(a, tb, te, sl, &nsl, tslot, &deps);
+    if (*(volatile int*)a.err) return;   // the other blocks' waits see the flag and end
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
-    auto Rv = [](const SysDev& S) -> W* {
-        if constexpr (MIXED) return S.r32; else return S.r64;
+    unsigned epoch = 0, gen = 0;
+
+    auto Rv = [](const SysDev& S, int i) -> W* {
+        if constexpr (MIXED) return S.r32[i]; else return S.r64[i];
     };
     auto Pv = [](const SysDev& S, int i) -> W* {
         if constexpr (MIXED) return S.p32[i]; else return S.p64[i];
@@ -354,315 +572,230 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         if constexpr (MIXED) return S.xs32; else return S.x;
     };
 
-    // ---------------- init: x = 0 (and xs = 0), r = p_0 = b, |b|^2
+    // B(k): Ap = D_second t and the partials of every system that stepped
+    auto pass_b = [&](int cur) {
+        for (int tile = tb; tile < te; ++tile) {
+            const SysLocal& L = sl[tslot[tile - tb]];
+            if (L.mode == kIdle || L.mode == kRu) continue;
+            const SysDev& S = a.sys[L.sys];
+            const int n = a.tiles[tile].y + threadIdx.x;
+            W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
+            if (n < S.V) {
+                const Site<W, K> ap = apply_d<W, K, MIXED>(Tv(S), n, S, !first_dag);
+                YK_ST(W, K, Av(S), n, ap);
+                const Site<W, K> r = YK_LD(W, K, Rv(S, cur), n);
+                const Site<W, K> p = YK_LD(W, K, Pv(S, cur), n);
+                v[0] = site_norm2<W, K>(r);
+                v[1] = site_norm2<W, K>(ap);
+                site_dot<W, K>(p, ap, v[2], v[3]);
+                site_dot<W, K>(r, ap, v[4], v[5]);
+            }
+            put_partial<W, kSkipIm>(a, tile, v, red);
+        }
+    };
+
+    // ---------------- round 0: b, x = 0, r_0 = p_0 = b; t = D_first p_0; B(0)
     for (int tile = tb; tile < te; ++tile) {
         const SysDev& S = a.sys[a.tiles[tile].x];
         const int n = a.tiles[tile].y + threadIdx.x;
-        double pr = 0.0;
-        if (n < S.V) {
-            const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
-            if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
-            Site<double, K> z;
-            Site<W, K> bw, zw;
+        if (n >= S.V) continue;
+        const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+        if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
+        Site<double, K> z;
+        Site<W, K> bw, zw;
 #pragma unroll
-            for (int i = 0; i < 4 * K; ++i) {
-                z.v[i] = 0.0;
-                zw.v[i] = W(0);
-                bw.v[i] = (W)bv.v[i];
-                pr = fma(bv.v[i], bv.v[i], pr);
-            }
-            YK_ST(double, K, S.x, n, z);
-            if constexpr (MIXED) YK_ST(W, K, S.xs32, n, zw);
-            YK_ST(W, K, Rv(S), n, bw);
-            YK_ST(W, K, Pv(S, 0), n, bw);
+        for (int i = 0; i < 4 * K; ++i) {
+            z.v[i] = 0.0;
+            zw.v[i] = W(0);
+            bw.v[i] = (W)bv.v[i];
         }
-        put_partial(a, tile, pr, 0.0, red);
+        YK_ST(double, K, S.x, n, z);
+        if constexpr (MIXED) {
+            YK_ST(W, K, S.xs32, n, zw);
+            S.diag32[n] = (float)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
+        }
+        YK_ST(W, K, Rv(S, 0), n, bw);
+        YK_ST(W, K, Pv(S, 0), n, bw);
     }
-    if (!gsync(a.bar, a.err)) return;
+    if (!nsync(a, ++epoch, deps)) return;
+    for (int tile = tb; tile < te; ++tile) {
+        const SysDev& S = a.sys[a.tiles[tile].x];
+        const int n = a.tiles[tile].y + threadIdx.x;
+        if (n >= S.V) continue;
+        YK_ST(W, K, Tv(S), n, (apply_d<W, K, MIXED>(Pv(S, 0), n, S, first_dag)));
+    }
+    if (!nsync(a, ++epoch, deps)) return;
+    pass_b(0);
+    if (!grid_reduce<MIXED>(a, gen, 0, false, &s_flag, &s_active, &s_ru)) return;
 
-    int n_ru = 0;
-    bool redo = false;   // phase 1 again after a reliable update, same k
-    int k = 0;
-    while (k <= a.max_iter) {   // every system retires in phase 1 of k = max_iter at the latest
-        const int cur = k & 1, prv = cur ^ 1;   // p_k lives in P[cur]
-        // ---------------- phase 1
-        if (redo)
-            reduce_systems<2>(a, sl, nsl);
-        else
-            reduce_systems<1>(a, sl, nsl);
-        if (threadIdx.x == 0) {
-            int want_ru = 0;
-            for (int j = 0; j < nsl; ++j) {
-                SysLocal& L = sl[j];
-                L.go = 0;
-                if (!L.active || (redo && !L.ru_done)) continue;
-                const double rr = L.sx;
-                if (k == 0) {
-                    L.rr = L.rr0 = rr;
-                    L.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(rr);
-                    L.beta = 0.0;
-                    L.rmax = sqrt(rr);
-                    if (!isfinite(rr)) retire(a, L, 0, YK_ENAN);
-                    else if (!(sqrt(rr) > L.stop)) retire(a, L, 1, 0);
-                    else if (a.max_iter <= 0) retire(a, L, 0, YK_ENOCONV);
-                    else L.go = 1;
-                    continue;
-                }
-                if (!L.ru_done) L.iters += 1;
-                if (!isfinite(rr)) {
-                    retire(a, L, 0, YK_ENAN);
-                    continue;
-                }
-                const double rn = sqrt(rr);
-                if (MIXED && !L.ru_done) {
-                    // reliable update: the FP32 residual claims convergence, has
-                    // dropped by reliable_delta since the last update, is due, or
-                    // the cap is reached (QUDA-style triggers)
-                    L.rmax = fmax(L.rmax, rn);
-                    const bool cand = !(rn > L.stop);
-                    const bool drop = rn < a.reliable_delta * L.rmax;
-                    const bool due = a.reliable_every > 0 && (L.iters % a.reliable_every) == 0;
-                    const bool cap = L.iters >= a.max_iter;
-                    if (cand || drop || due || cap) {
-                        L.ru = 1;
-                        want_ru = 1;
-                        continue;
-                    }
-                    L.cre = 1.0;
-                    L.cim = 0.0;
-                } else {
-                    if (!(rn > L.stop)) {
-                        L.rr = rr;
-                        L.ru_done = 0;
-                        retire(a, L, 1, 0);
-                        continue;
-                    }
-                    if (L.iters >= a.max_iter) {
-                        L.rr = rr;
-                        L.ru_done = 0;
-                        retire(a, L, 0, YK_ENOCONV);
-                        continue;
-                    }
-                    if (MIXED) {
-                        // after a reliable update p is first made orthogonal to the
-                        // new residual: p <- p - gamma r, gamma = <r, p> / |r|^2, so
-                        // p_new = r + beta (p - gamma r) = beta p + (1 - beta gamma) r
-                        const double beta = rr / L.rr;
-                        const double gre = L.sz / rr, gim = L.sw / rr;
-                        L.cre = 1.0 - beta * gre;
-                        L.cim = -beta * gim;
-                        L.rmax = rn;
-                        L.ru_done = 0;
-                    }
-                }
-                L.beta = rr / L.rr;
-                L.rr = rr;
-                L.go = 1;
-            }
-            if (want_ru) atomicMax(a.any_ru, k + 1);
-        }
-        __syncthreads();
+    int k = 1;
+    while (k <= a.max_iter) {   // every system retires at k = max_iter at the latest
+        load_coefs(a, sl, nsl, &s_nact, &s_anyru);
+        if (s_nact == 0) break;
+        const bool any_ru = MIXED && s_anyru;
+        const int cur = k & 1, prv = cur ^ 1;
+        // ---------------- A(k)
         for (int tile = tb; tile < te; ++tile) {
             const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.go) continue;
+            const int mode = L.mode;
+            if (mode != kStep && mode != kRu && mode != kRedo) continue;
             const SysDev& S = a.sys[L.sys];
             const int n = a.tiles[tile].y + threadIdx.x;
             if (n >= S.V) continue;
-            const W beta = (W)L.beta, cre = (W)L.cre, cim = (W)L.cim;
-            const W* pold = Pv(S, k == 0 ? 0 : prv);
-            const W* rv = Rv(S);
-            const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-            Site<W, K> st[5];
-            const int64_t m5[5] = {n, nbr.tu, nbr.td, nbr.xu, nbr.xd};
+            if constexpr (MIXED) {
+                if (mode == kRu) {
+                    // fold x_k = x + xs + alpha p_{k-1} into the FP64 x; xs = 0
+                    Site<double, K> xv = YK_LD(double, K, S.x, n);
+                    const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
+                    const Site<W, K> pv = YK_LD(W, K, Pv(S, prv), n);
+                    Site<double, K> pd;
+                    Site<W, K> zw;
 #pragma unroll
-            for (int q = 0; q < 5; ++q) {
-                st[q] = YK_LD(W, K, pold, m5[q]);
-                if (k > 0) {
-                    // p = beta p + c r  (c = 1 but after a reliable update)
-                    const Site<W, K> r = YK_LD(W, K, rv, m5[q]);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        if constexpr (K == 1) {
-                            st[q].v[e] = fma(beta, st[q].v[e], cre * r.v[e]);
-                        } else {
-                            const W re = r.v[2 * e], im = r.v[2 * e + 1];
-                            st[q].v[2 * e] = fma(beta, st[q].v[2 * e], fma(cre, re, -cim * im));
-                            st[q].v[2 * e + 1] = fma(beta, st[q].v[2 * e + 1], fma(cre, im, cim * re));
-                        }
+                    for (int i = 0; i < 4 * K; ++i) {
+                        xv.v[i] += (double)xs.v[i];
+                        pd.v[i] = (double)pv.v[i];
+                        zw.v[i] = W(0);
                     }
+                    site_axpy<double, K>(xv, L.alpha_re, L.alpha_im, pd);
+                    YK_ST(double, K, S.x, n, xv);
+                    YK_ST(W, K, S.xs32, n, zw);
+                    continue;
                 }
             }
-            const W diag = (W)(2.0 * S.r + S.m0 + S.g * S.sigma[n]);
-            const Site<W, K> o = first_dag
-                ? dirac_combine<W, K, true>(st[0], st[1], st[2], st[3], st[4], diag, (W)S.r, (W)nbr.sp, (W)nbr.sm)
-                : dirac_combine<W, K, false>(st[0], st[1], st[2], st[3], st[4], diag, (W)S.r, (W)nbr.sp, (W)nbr.sm);
-            YK_ST(W, K, Tv(S), n, o);
-            if (k > 0) YK_ST(W, K, Pv(S, cur), n, st[0]);
+            const Nbr nb = neighbours(n, S.Nt, S.Nx);
+            const int64_t m5[5] = {n, nb.tu, nb.td, nb.xu, nb.xd};
+            const W beta = (W)L.beta;
+            Site<W, K> pn[5];
+            if (mode == kStep) {
+                const W ar = (W)L.alpha_re, ai = (W)L.alpha_im;
+                Site<W, K> r_own, p_old;
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    Site<W, K> r = YK_LD(W, K, Rv(S, prv), m5[q]);
+                    const Site<W, K> ap = YK_LD(W, K, Av(S), m5[q]);
+                    const Site<W, K> po = YK_LD(W, K, Pv(S, prv), m5[q]);
+                    site_axpy<W, K>(r, -ar, -ai, ap);
+#pragma unroll
+                    for (int i = 0; i < 4 * K; ++i) pn[q].v[i] = fma(beta, po.v[i], r.v[i]);
+                    if (q == 0) {
+                        r_own = r;
+                        p_old = po;
+                    }
+                }
+                Site<W, K> xv = YK_LD(W, K, Xv(S), n);
+                site_axpy<W, K>(xv, ar, ai, p_old);
+                YK_ST(W, K, Xv(S), n, xv);
+                YK_ST(W, K, Rv(S, cur), n, r_own);
+            } else {
+                // kRedo: r_k is the FP64 residual (rounded) in R[cur]
+                const W cre = (W)L.c_re, cim = (W)L.c_im;
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    const Site<W, K> r = YK_LD(W, K, Rv(S, cur), m5[q]);
+                    const Site<W, K> po = YK_LD(W, K, Pv(S, prv), m5[q]);
+                    pn[q] = p_next<W, K>(r, po, beta, cre, cim);
+                }
+            }
+            const W diag = diag_of<W, MIXED>(S, n);
+            const Site<W, K> t = first_dag
+                ? dirac_combine<W, K, true>(pn[0], pn[1], pn[2], pn[3], pn[4], diag, (W)S.r, (W)nb.sp, (W)nb.sm)
+                : dirac_combine<W, K, false>(pn[0], pn[1], pn[2], pn[3], pn[4], diag, (W)S.r, (W)nb.sp, (W)nb.sm);
+            YK_ST(W, K, Tv(S), n, t);
+            YK_ST(W, K, Pv(S, cur), n, pn[0]);
         }
-        if (!gsync(a.bar, a.err)) return;
-        if (*(volatile int*)a.n_active == 0) break;
+        if (!nsync(a, ++epoch, deps)) return;
 
         if constexpr (MIXED) {
-            if (!redo && *(volatile int*)a.any_ru == k + 1) {
-                // RU1: t64 = D_first (x + xs), formed on the fly in FP64
+            if (any_ru) {
+                // RU1: t64 = D_first x (FP64)
                 for (int tile = tb; tile < te; ++tile) {
                     const SysLocal& L = sl[tslot[tile - tb]];
-                    if (!L.active || !L.ru) continue;
+                    if (L.mode != kRu) continue;
                     const SysDev& S = a.sys[L.sys];
                     const int n = a.tiles[tile].y + threadIdx.x;
                     if (n >= S.V) continue;
-                    const Nbr nbr = neighbours(n, S.Nt, S.Nx);
-                    Site<double, K> xt[5];
-                    const int64_t m5[5] = {n, nbr.tu, nbr.td, nbr.xu, nbr.xd};
-#pragma unroll
-                    for (int q = 0; q < 5; ++q) {
-                        xt[q] = YK_LD(double, K, S.x, m5[q]);
-                        const Site<W, K> xs = YK_LD(W, K, S.xs32, m5[q]);
-#pragma unroll
-                        for (int i = 0; i < 4 * K; ++i) xt[q].v[i] += (double)xs.v[i];
-                    }
+                    const Nbr nb = neighbours(n, S.Nt, S.Nx);
+                    const Site<double, K> c = YK_LD(double, K, S.x, n);
+                    const Site<double, K> tu = YK_LD(double, K, S.x, nb.tu);
+                    const Site<double, K> td = YK_LD(double, K, S.x, nb.td);
+                    const Site<double, K> xu = YK_LD(double, K, S.x, nb.xu);
+                    const Site<double, K> xd = YK_LD(double, K, S.x, nb.xd);
                     const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
                     const Site<double, K> t = first_dag
-                        ? dirac_combine<double, K, true>(xt[0], xt[1], xt[2], xt[3], xt[4], diag, S.r, (double)nbr.sp, (double)nbr.sm)
-                        : dirac_combine<double, K, false>(xt[0], xt[1], xt[2], xt[3], xt[4], diag, S.r, (double)nbr.sp, (double)nbr.sm);
+                        ? dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
+                        : dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
                     YK_ST(double, K, S.t64, n, t);
                 }
-                if (!gsync(a.bar, a.err)) return;
-                // RU2: x += xs, xs = 0; r = b - D_second t64 in FP64; |r|^2
+                if (!nsync(a, ++epoch, deps)) return;
+                // RU2: r = b - D_second t64 in FP64 -> R[cur]; |r|^2, <r, p_{k-1}>
                 for (int tile = tb; tile < te; ++tile) {
                     const SysLocal& L = sl[tslot[tile - tb]];
-                    if (!L.active || !L.ru) continue;
+                    if (L.mode != kRu) continue;
                     const SysDev& S = a.sys[L.sys];
                     const int n = a.tiles[tile].y + threadIdx.x;
-                    double rr = 0.0;
-                    double2 rp = make_double2(0.0, 0.0);
+                    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
                     if (n < S.V) {
-                        Site<double, K> xv = YK_LD(double, K, S.x, n);
-                        const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
-                        Site<W, K> zw;
-#pragma unroll
-                        for (int i = 0; i < 4 * K; ++i) {
-                            xv.v[i] += (double)xs.v[i];
-                            zw.v[i] = W(0);
-                        }
-                        YK_ST(double, K, S.x, n, xv);
-                        YK_ST(W, K, S.xs32, n, zw);
-                        const Site<double, K> ax = apply_d<double, K>(S.t64, n, S, !first_dag);
+                        const Nbr nb = neighbours(n, S.Nt, S.Nx);
+                        const Site<double, K> c = YK_LD(double, K, S.t64, n);
+                        const Site<double, K> tu = YK_LD(double, K, S.t64, nb.tu);
+                        const Site<double, K> td = YK_LD(double, K, S.t64, nb.td);
+                        const Site<double, K> xu = YK_LD(double, K, S.t64, nb.xu);
+                        const Site<double, K> xd = YK_LD(double, K, S.t64, nb.xd);
+                        const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+                        const Site<double, K> ax = first_dag
+                            ? dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
+                            : dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
                         const Site<double, K> bv = YK_LD(double, K, S.b, n);
-                        const Site<W, K> pw = YK_LD(W, K, Pv(S, prv), n);   // p_{k-1}
-                        Site<W, K> rw;
+                        const Site<W, K> pw = YK_LD(W, K, Pv(S, prv), n);
                         Site<double, K> rd, pd;
+                        Site<W, K> rw;
 #pragma unroll
                         for (int i = 0; i < 4 * K; ++i) {
-                            const double r = bv.v[i] - ax.v[i];
-                            rr = fma(r, r, rr);
-                            rw.v[i] = (W)r;
-                            rd.v[i] = r;
+                            rd.v[i] = bv.v[i] - ax.v[i];
+                            rw.v[i] = (W)rd.v[i];
                             pd.v[i] = (double)pw.v[i];
                         }
-                        rp = site_dot<double, K>(rd, pd);
-                        YK_ST(W, K, Rv(S), n, rw);
+                        YK_ST(W, K, Rv(S, cur), n, rw);
+                        v[0] = site_norm2<double, K>(rd);
+                        site_dot<double, K>(rd, pd, v[2], v[3]);
                     }
-                    put_partial(a, tile, rr, 0.0, red, true, rp.x, rp.y);
+                    // slots 1, 4, 5 unused here
+                    put_partial<double, (1 << 1) | (1 << 4) | (1 << 5) | kSkipIm>(a, tile, v, red);
                 }
-                __syncthreads();
-                if (threadIdx.x == 0)
-                    for (int j = 0; j < nsl; ++j)
-                        if (sl[j].active && sl[j].ru) {
-                            sl[j].ru = 0;
-                            sl[j].ru_done = 1;
-                        }
-                ++n_ru;
-                redo = true;
-                if (!gsync(a.bar, a.err)) return;
-                continue;
+                if (!grid_reduce<MIXED>(a, gen, k, true, &s_flag, &s_active, &s_ru)) return;
+                continue;   // same k: the systems that updated redo A(k)
             }
         }
-        redo = false;
 
-        // ---------------- phase 2: Ap = D_second t, <p, Ap>
-        for (int tile = tb; tile < te; ++tile) {
-            const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.active) continue;
-            const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
-            double2 d = make_double2(0.0, 0.0);
-            if (n < S.V) {
-                const Site<W, K> ap = apply_d<W, K>(Tv(S), n, S, !first_dag);
-                YK_ST(W, K, Av(S), n, ap);
-                d = site_dot<W, K>(YK_LD(W, K, Pv(S, cur), n), ap);
-            }
-            put_partial(a, tile, d.x, d.y, red);
-        }
-        if (!gsync(a.bar, a.err)) return;
-
-        // ---------------- phase 3: alpha; x += alpha p, r -= alpha Ap, |r|^2
-        reduce_systems<1>(a, sl, nsl);
-        if (threadIdx.x == 0) {
-            for (int j = 0; j < nsl; ++j) {
-                SysLocal& L = sl[j];
-                if (!L.active) continue;
-                // alpha = rr / (sx + i sy), Smith's complex division (CGsolver.cu:137)
-                const double c = L.sx, d = L.sy, num = L.rr;
-                double ar, ai;
-                if (fabs(c) >= fabs(d)) {
-                    const double q = d / c, den = c + d * q;
-                    ar = num / den;
-                    ai = (-num * q) / den;
-                } else {
-                    const double q = c / d, den = c * q + d;
-                    ar = (num * q) / den;
-                    ai = -num / den;
-                }
-                L.alpha = ar;
-                L.alpha_im = ai;
-                if (!isfinite(ar) || !isfinite(ai)) retire(a, L, 0, YK_ENAN);
-            }
-        }
-        __syncthreads();
-        for (int tile = tb; tile < te; ++tile) {
-            const SysLocal& L = sl[tslot[tile - tb]];
-            if (!L.active) continue;
-            const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
-            double rr = 0.0;
-            if (n < S.V) {
-                const Site<W, K> pv = YK_LD(W, K, Pv(S, cur), n);
-                const Site<W, K> ap = YK_LD(W, K, Av(S), n);
-                Site<W, K> xs = YK_LD(W, K, Xv(S), n);
-                Site<W, K> rs = YK_LD(W, K, Rv(S), n);
-                site_axpy<W, K>(xs, (W)L.alpha, (W)L.alpha_im, pv);
-                site_axpy<W, K>(rs, (W)-L.alpha, (W)-L.alpha_im, ap);
-                YK_ST(W, K, Xv(S), n, xs);
-                YK_ST(W, K, Rv(S), n, rs);
-#pragma unroll
-                for (int i = 0; i < 4 * K; ++i) rr = fma((double)rs.v[i], (double)rs.v[i], rr);
-            }
-            put_partial(a, tile, rr, 0.0, red);
-        }
-        if (!gsync(a.bar, a.err)) return;
+        // ---------------- B(k)
+        pass_b(cur);
+        if (!grid_reduce<MIXED>(a, gen, k, false, &s_flag, &s_active, &s_ru)) return;
         ++k;
     }
-    if (threadIdx.x == 0)
-        for (int j = 0; j < nsl; ++j) publish(a, sl[j], n_ru);
 }
 
-// Resets the barrier, counters and activity flags before a solve.
+// Resets the barrier, flags, counters and per-system state before a solve.
 __global__ void cg_prepare_kernel(CGArgs a)
 {
     for (int i = a.sys_first + threadIdx.x; i < a.sys_first + a.sys_count; i += blockDim.x) {
-        a.st[i].active = 1;
-        a.st[i].iters = 0;
-        a.st[i].converged = 0;
-        a.st[i].status = 0;
-        a.st[i].n_ru = 0;
-        a.st[i].rr = 0.0;
-        a.st[i].rr0 = 0.0;
+        CGState& s = a.st[i];
+        s.rr = s.rr0 = s.rr_prev = s.stop = s.rmax = 0.0;
+        s.active = 1;
+        s.iters = 0;
+        s.converged = 0;
+        s.status = 0;
+        s.n_ru = 0;
+        CGCoef& c = a.coef[i];
+        c.alpha_re = c.alpha_im = c.beta = c.c_im = 0.0;
+        c.c_re = 1.0;
+        c.mode = kStep;
     }
+    for (int b = threadIdx.x; b < a.grid; b += blockDim.x) a.flags[(size_t)b * kFlagStride] = 0u;
     if (threadIdx.x == 0) {
         *a.n_active = a.sys_count;
         *a.any_ru = 0;
-        a.bar->count = 0;
+        a.bar->arrive = 0u;
+        a.bar->gen = 0u;
         *a.err = 0;
     }
 }
@@ -673,7 +806,8 @@ static int max_coresident(const void* fn, int block)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, 0);
-    return per * nsm;
+    const int g = per * nsm;
+    return g < kMaxGrid ? g : kMaxGrid;
 }
 
 template <int K, bool MIXED>
@@ -710,8 +844,9 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     const int nt = a.tile_end - a.tile_begin;
     int tpb = 1;
     const int grid = cg_grid_for(nt, maxg, &tpb);
-    if (tpb > kMaxTilesPerBlock || grid > maxg) return cudaErrorInvalidConfiguration;
+    if (tpb > kMaxTilesPerBlock || grid > maxg || grid > kMaxGrid) return cudaErrorInvalidConfiguration;
     a.tiles_per_block = tpb;
+    a.grid = grid;
     if (grid_out) *grid_out = grid;
     cg_prepare_kernel<<<1, 256, 0, stream>>>(a);
     cudaLaunchConfig_t cfg = {};

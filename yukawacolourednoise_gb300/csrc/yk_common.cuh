@@ -1,6 +1,6 @@
 // yk_common.cuh -- device-side building blocks shared by the sm_103a kernels:
-// spinor site vectors, the Wilson-Dirac site stencil, Philox4x32-10 normals,
-// deterministic block reductions and a bounded grid barrier.
+// spinor site vectors, the Wilson-Dirac site stencil, Philox4x32-10 normals
+// and deterministic block reductions.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -246,41 +246,6 @@ __device__ __forceinline__ double block_max(double a, double* scratch)
         r = warp_max(r);
     }
     return r;
-}
-
-// ---------------------------------------------------------------------------
-// Grid barrier for cooperative (co-resident) launches.  Every wait is bounded:
-// after ~kBarrierCycles it records YK_ETIMEOUT in *err and returns, and every
-// caller leaves the kernel once *err is set.
-// ---------------------------------------------------------------------------
-constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at 2 GHz
-
-__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned nblocks, int* err)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = &b->gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&b->count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&b->count, 0u);
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*vgen == g) {
-                if (clock64() - t0 > kBarrierCycles) {
-                    atomicCAS(err, 0, YK_ETIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int*)err == 0;
 }
 
 }  // namespace yk

@@ -20,11 +20,16 @@ constexpr int kTile = 256;    // lattice sites per tile (one per thread)
 constexpr int kMaxFFT = 4096; // longest FFT edge handled in shared memory
 constexpr int kMaxDFT = 256;  // longest non-power-of-two edge (direct DFT)
 constexpr int kMaxTilesPerBlock = 512;   // tiles one CG block may own
+constexpr int kMaxGrid = 2048;           // blocks of a CG launch (neighbour flags allocated)
+constexpr int kFlagStride = 32;          // one 128-byte line per neighbour flag
 
+// Grid barrier of the CG kernel: arrivals are counted on one line; the last
+// block to arrive finishes the reduction and advances `gen` on another.
 struct GridBarrier {
-    unsigned count;
+    unsigned arrive;
+    unsigned pad0[31];
     unsigned gen;
-    unsigned pad[30];
+    unsigned pad1[31];
 };
 
 // One linear system (chain, right-hand side) of a batched CG solve.
@@ -37,36 +42,51 @@ struct SysDev {
     // FP64 vectors (K real planes per spinor entry)
     double* b;           // right-hand side (eta)
     double* x;           // solution
-    double* r64;         // FP64 residual (FP64 solver)
+    double* r64[2];      // residual, double-buffered (FP64 solver)
     double* p64[2];      // search directions, double-buffered
     double* t64;         // D p (or D x in reliable updates)
     double* Ap64;        // D^dag D p
     // FP32 vectors (mixed solver)
-    float* r32;          // residual
+    float* r32[2];       // residual, double-buffered
     float* p32[2];       // search directions, double-buffered
     float* t32;          // D p
     float* Ap32;         // D^dag D p
     float* xs32;         // solution increment since the last reliable update
+    float* diag32;       // 2r + m0 + g sigma per site (one float)
     // noise generation for b: kind/rhs of the Philox stream, or gen = 0
     int gen_eta;
     uint64_t seed;
     const int64_t* step; // device step counter of the chain
 };
 
-// Per-tile reduction slot of the CG kernels.
+// Per-tile reduction slot of the CG kernel: |r|^2, |Ap|^2, <p, Ap>, <r, Ap>
+// (re, im); after a reliable update |r|^2 and <r, p> of the FP64 residual.
 struct __align__(16) Partial {
-    double x, y;   // the reduction pair of every phase
-    double z, w;   // reliable updates: <r, p> of the new FP64 residual
+    double v[6];
 };
 
-// Per-system CG scalars, written by the finaliser block of each reduction.
+// Per-system CG scalars.  Written only by the block that completes a grid
+// reduction (one at a time), read by the host after the solve.
 struct CGState {
-    double rr, rr0;
+    double rr, rr0;      // last |r|^2, |b|^2
+    double rr_prev;      // |r|^2 of the previous iteration (mixed: beta after a reliable update)
+    double stop;         // stopping threshold on |r|
+    double rmax;         // largest |r| since the last reliable update (mixed)
     int active;
     int iters;
     int converged;
     int status;
-    int n_ru;    // reliable updates (mixed)
+    int n_ru;            // reliable updates (mixed)
+    int pad;
+};
+
+// Per-system coefficients of the next pass, published with each grid reduction.
+struct CGCoef {
+    double alpha_re, alpha_im;   // x += alpha p, r -= alpha A p
+    double beta;                 // p = c r + beta p
+    double c_re, c_im;
+    int mode;                    // CGMode
+    int pad;
 };
 
 struct CGArgs {
@@ -76,8 +96,11 @@ struct CGArgs {
     int tile_begin, tile_end;   // tiles of this solve
     int eta_kind;               // Philox stream kind of generated right-hand sides
     CGState* st;
-    Partial* partial;    // one per tile: the (x, y) reduction pair of the phase
+    Partial* partial;    // one per tile
+    CGCoef* coef;        // one per system
+    unsigned* flags;     // kMaxGrid neighbour flags, kFlagStride apart
     int tiles_per_block; // contiguous tile range of each block (set by the launcher)
+    int grid;            // blocks of the launch (set by the launcher)
     GridBarrier* bar;
     int* err;
     int* n_active;

@@ -1,8 +1,9 @@
 // yk_noalloc.cu -- yk_cg_solve_static: the FP64 CG solve of yk_cg_solve
 // (CGsolver::solve, code/src/CGsolver.cu:42-59) without a context and without
-// any device allocation.  Its scratch -- the CG vectors r, p (two), D p and
-// A p, the per-tile partial sums, the tile table, the system record, the
-// solver state, the grid barrier and the error flags -- lives in one
+// any device allocation.  Its scratch -- the CG vectors r and p (two each),
+// D p and A p, the per-tile partial sums, the tile table, the system record,
+// the solver state and coefficients, the grid barrier, the neighbour flags
+// and the error flags -- lives in one
 // file-scope device array of fixed size, so lattices up to
 // kStaticMaxSites sites are accepted and larger ones are refused.
 //
@@ -30,8 +31,9 @@ constexpr size_t up(size_t n) { return (n + kAlign - 1) / kAlign * kAlign; }
 
 // byte offsets of the pieces inside the array
 constexpr size_t kVecBytes = sizeof(double) * 8 * kStaticMaxSites;   // one FP64 complex spinor field
-constexpr size_t oR = 0;
-constexpr size_t oP0 = oR + kVecBytes;
+constexpr size_t oR0 = 0;
+constexpr size_t oR1 = oR0 + kVecBytes;
+constexpr size_t oP0 = oR1 + kVecBytes;
 constexpr size_t oP1 = oP0 + kVecBytes;
 constexpr size_t oT = oP1 + kVecBytes;
 constexpr size_t oAp = oT + kVecBytes;
@@ -39,9 +41,11 @@ constexpr size_t oPartial = oAp + kVecBytes;
 constexpr size_t oTiles = oPartial + up(sizeof(Partial) * kStaticMaxTiles);
 constexpr size_t oSys = oTiles + up(sizeof(int2) * kStaticMaxTiles);
 constexpr size_t oState = oSys + up(sizeof(SysDev));
-constexpr size_t oBar = oState + up(sizeof(CGState));
-constexpr size_t oFlags = oBar + up(sizeof(GridBarrier));
-constexpr size_t kStaticScratchBytes = oFlags + up(sizeof(int) * 4);   // about 5.3 MB
+constexpr size_t oCoef = oState + up(sizeof(CGState));
+constexpr size_t oBar = oCoef + up(sizeof(CGCoef));
+constexpr size_t oNbr = oBar + up(sizeof(GridBarrier));
+constexpr size_t oFlags = oNbr + up(sizeof(unsigned) * kFlagStride * kMaxGrid);
+constexpr size_t kStaticScratchBytes = oFlags + up(sizeof(int) * 4);   // about 6.6 MB
 
 static __device__ __align__(256) unsigned char g_cg_scratch[kStaticScratchBytes];
 
@@ -72,7 +76,8 @@ __global__ void static_setup_kernel(unsigned char* base, const double* sigma, co
         S.sigma = sigma;
         S.b = const_cast<double*>(b);
         S.x = x;
-        S.r64 = reinterpret_cast<double*>(base + oR);
+        S.r64[0] = reinterpret_cast<double*>(base + oR0);
+        S.r64[1] = reinterpret_cast<double*>(base + oR1);
         S.p64[0] = reinterpret_cast<double*>(base + oP0);
         S.p64[1] = reinterpret_cast<double*>(base + oP1);
         S.t64 = reinterpret_cast<double*>(base + oT);
@@ -146,6 +151,8 @@ extern "C" int yk_cg_solve_static(const double* sigma, int Nt, int Nx, double m0
     a.eta_kind = 0;
     a.st = reinterpret_cast<CGState*>(base + oState);
     a.partial = reinterpret_cast<Partial*>(base + oPartial);
+    a.coef = reinterpret_cast<CGCoef*>(base + oCoef);
+    a.flags = reinterpret_cast<unsigned*>(base + oNbr);
     a.bar = reinterpret_cast<GridBarrier*>(base + oBar);
     a.err = reinterpret_cast<int*>(base + oFlags);
     a.n_active = a.err + 1;
