@@ -5,8 +5,12 @@ GPU); test_gpu_golden.py checks the CUDA path against the same vectors.
 
 Tolerances: operator applications 1e-14 relative (the reference sums in a
 different order and uses FMA contraction); CG solutions at the reference's
-absolute 1e-8 stopping rule 1e-9 relative; noise 1e-13 absolute (cuFFT vs
-radix-2); steps 1e-10 absolute on the field, 1e-9 relative on eps (it follows max|drift|, whose force carries the CG tolerance).
+absolute 1e-8 stopping rule 1e-9 relative; fermion forces from those solves
+3e-9 absolute (two FP64 CGs that take the same number of iterations still
+differ by rounding amplified through the iteration: the oracle and the
+reference differ by up to 6.5e-10 in F on the 8x4 lattice); noise 1e-13
+absolute (cuFFT vs radix-2); steps 1e-10 absolute on the field, 1e-9 relative
+on eps (it follows max|drift|, whose force carries the CG tolerance).
 """
 import numpy as np
 import pytest
@@ -61,9 +65,9 @@ def test_force(gold):
     d, Nt, Nx, (m2, lam, g, m0, eps_bar) = gold
     eta = cplx(d["force_eta"])[None]
     F, _ = O.force(Nt, Nx, O.action(m2=m2, lam=lam, g=g, m0=m0), d["sigma"], eta)
-    assert np.abs(F - d["force_F"]).max() < 1e-9
+    assert np.abs(F - d["force_F"]).max() < 3e-9
     Fr, _ = O.force(Nt, Nx, O.action(m2=m2, lam=lam, g=g, m0=m0, cut_fraction=0.5, drift_mode=1), d["sigma"], eta)
-    assert np.abs(Fr - d["force_F_resc"]).max() < 1e-9
+    assert np.abs(Fr - d["force_F_resc"]).max() < 3e-9
 
 
 def test_mask_and_noise(gold):

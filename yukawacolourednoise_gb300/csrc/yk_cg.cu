@@ -33,6 +33,7 @@
 // neighbours.  Every wait is bounded (about 2 s): a block that gives up sets
 // YK_ETIMEOUT and every block leaves.
 #include <cstdio>
+#include <cstdlib>
 #include <type_traits>
 
 #include "yk_common.cuh"
@@ -77,6 +78,34 @@ __device__ void chk_st(R* p, int64_t n, const Site<R, K>& v, int V, int line)
 #define YK_ST(R, K, p, n, v) store_site<R, K>((p), (n), (v))
 #endif
 
+#ifdef YK_CG_TIMING
+// Timing build: block 0 accumulates the clock cycles of each part of an
+// iteration and prints the per-iteration averages when the solve ends.
+// g_cg_t: arrival cycles / count, finisher cycles / count, release cycles,
+// waiter spin cycles / count, arrival spread (ns, first to last arrival).
+__device__ unsigned long long g_cg_t[10];
+__device__ unsigned long long g_cg_f[8];   // finisher: start->sums ready, ->scalar done, ->end
+__device__ unsigned long long g_cg_first;
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+#define YK_TMARK(i)                                              \
+    do {                                                         \
+        if (blockIdx.x == 0 && threadIdx.x == 0) {               \
+            const long long t_ = clock64();                      \
+            tacc[i] += t_ - tlast;                               \
+            tlast = t_;                                          \
+        }                                                        \
+    } while (0)
+#else
+#define YK_TMARK(i) \
+    do {            \
+    } while (0)
+#endif
+
 namespace {
 
 constexpr int kMaxSysPerBlock = 48;
@@ -92,12 +121,54 @@ enum CGMode {
     kWait = 4,   // another system's reliable update runs; this one already stepped
 };
 
-// Per-block copy of the coefficients of one system whose tiles it owns.
+// Per-block copy of the coefficients of one system whose tiles it owns (FP64,
+// and FP32 copies for the mixed solver: a conversion from FP64 costs an FP64
+// instruction per thread otherwise).
 struct SysLocal {
     int sys;
     int mode;
     double alpha_re, alpha_im, beta, c_re, c_im;
+    float f_alpha_re, f_alpha_im, f_beta, f_c_re, f_c_im;
 };
+
+template <typename W>
+__device__ __forceinline__ W pick(double d, float f)
+{
+    if constexpr (sizeof(W) == sizeof(float))
+        return f;
+    else
+        return d;
+}
+
+// ---------------------------------------------------------------------------
+// Float-float sums (hi + lo, about 48 significant bits) for the mixed solver:
+// GB300 issues FP64 at 1/64 of the FP32 rate, so its reductions run on the
+// FP32 pipes.  Knuth's two-sum; no multiplications, so no FMA contraction.
+// ---------------------------------------------------------------------------
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const float s = a.hi + b.hi;
+    const float bp = s - a.hi;
+    float e = (a.hi - (s - bp)) + (b.hi - bp);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return FF{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ FF ff_of(double x)
+{
+    const float hi = (float)x;
+    return FF{hi, (float)(x - (double)hi)};
+}
+
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
+{
+    return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+}
 
 // Blocks holding stencil neighbours of this block's sites.
 struct Deps {
@@ -166,6 +237,8 @@ __device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 L.mode = kStep;
                 L.alpha_re = L.alpha_im = L.beta = L.c_im = 0.0;
                 L.c_re = 1.0;
+                L.f_alpha_re = L.f_alpha_im = L.f_beta = L.f_c_im = 0.f;
+                L.f_c_re = 1.f;
                 ++n;
                 last = s;
             }
@@ -196,202 +269,471 @@ __device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
     __syncthreads();
 }
 
-// Coefficients of the block's systems after a grid reduction.
-__device__ void load_coefs(const CGArgs& a, SysLocal* sl, int nsl, int* s_nact, int* s_anyru)
+// 16-byte load of data another block wrote before the last synchronisation:
+// relaxed at gpu scope (served by L2), independent loads stay in flight
+// together, and the asm's memory clobber keeps the compiler from moving it
+// across the synchronisation.
+__device__ __forceinline__ double2 ld_sync2(const void* p)
 {
-    for (int j = threadIdx.x; j < nsl; j += blockDim.x) {
-        const volatile CGCoef& c = a.coef[sl[j].sys];
-        sl[j].mode = c.mode;
-        sl[j].alpha_re = c.alpha_re;
-        sl[j].alpha_im = c.alpha_im;
-        sl[j].beta = c.beta;
-        sl[j].c_re = c.c_re;
-        sl[j].c_im = c.c_im;
-    }
-    if (threadIdx.x == 0) {
-        *s_nact = *(volatile int*)a.n_active;
-        *s_anyru = *(volatile int*)a.any_ru;
-    }
-    __syncthreads();
+    double2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+    return v;
 }
 
-// Scalar recurrence of one system after its partials were summed (one thread).
-// s: |r|^2, |Ap|^2, <p,Ap> re/im, <r,Ap> re/im; after a reliable update
-// |r|^2 and <r, p_{k-1}> re/im in s[0], s[2], s[3].
-template <bool MIXED>
-__device__ void scalar_step(const CGArgs& a, int j, int k, bool ru_round, const double* s, int* s_active,
-                            int* s_ru)
+__device__ __forceinline__ float4 ld_sync4f(const void* p)
 {
-    volatile CGState& st = a.st[j];
-    volatile CGCoef& cf = a.coef[j];
+    float4 v;
+    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Published coefficients.  The block that finishes a grid reduction writes
+// every system's next-pass coefficients as 64-bit words, 32 bits of payload
+// and the barrier generation in the high half (an aligned 64-bit access is
+// single-copy atomic), and the grid word the same way; a waiting block polls
+// the words of its systems and the grid word until each carries the new
+// generation -- the data is the flag.  The writer fences once before its
+// stores (release; it has no stores of its own outstanding then) and each
+// poller fences after its last poll (acquire), which also orders the vector
+// data of the pass for the next one.
+// ---------------------------------------------------------------------------
+struct CoefVals {
+    double alpha_re, alpha_im, beta, c_re, c_im;
+    int mode;
+};
+
+__device__ __forceinline__ unsigned long long stamp(unsigned payload, unsigned gen)
+{
+    return ((unsigned long long)gen << 32) | payload;
+}
+
+__device__ __forceinline__ void st_pair(unsigned long long* p, unsigned long long a, unsigned long long b)
+{
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
+
+__device__ __forceinline__ ulonglong2 ld_pair(const unsigned long long* p)
+{
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_word(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// words: alpha_re, alpha_im, beta, c_re, c_im as (low, high) halves, then mode
+__device__ __forceinline__ void publish_coef(CGCoef* c, const CoefVals& v, unsigned gen)
+{
+    const double d[5] = {v.alpha_re, v.alpha_im, v.beta, v.c_re, v.c_im};
+    unsigned long long w[12];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const unsigned long long u = (unsigned long long)__double_as_longlong(d[i]);
+        w[2 * i] = stamp((unsigned)u, gen);
+        w[2 * i + 1] = stamp((unsigned)(u >> 32), gen);
+    }
+    w[10] = stamp((unsigned)v.mode, gen);
+    w[11] = stamp(0u, gen);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) st_pair(c->w + 2 * i, w[2 * i], w[2 * i + 1]);
+}
+
+// Polls one system's words until all carry `gen`; false if the wait ended.
+__device__ bool poll_coef(const CGCoef* c, unsigned gen, CoefVals& v, int* err)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        ulonglong2 q[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) q[i] = ld_pair(c->w + 2 * i);
+        bool ok = true;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ok = ok && (unsigned)(q[i].x >> 32) == gen && (unsigned)(q[i].y >> 32) == gen;
+        if (ok) {
+            double d[5];
+            const unsigned long long h[12] = {q[0].x, q[0].y, q[1].x, q[1].y, q[2].x, q[2].y,
+                                              q[3].x, q[3].y, q[4].x, q[4].y, q[5].x, q[5].y};
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                d[i] = __longlong_as_double((long long)(((h[2 * i + 1] & 0xffffffffull) << 32) |
+                                                        (h[2 * i] & 0xffffffffull)));
+            v.alpha_re = d[0];
+            v.alpha_im = d[1];
+            v.beta = d[2];
+            v.c_re = d[3];
+            v.c_im = d[4];
+            v.mode = (int)(unsigned)(h[10] & 0xffffffffull);
+            return true;
+        }
+        if (wait_over(t0, err)) return false;
+    }
+}
+
+// After a grid reduction: every block polls the words of its systems and the
+// grid word (bounded waits), then copies the coefficients into its table.
+__device__ bool poll_coefs(const CGArgs& a, SysLocal* sl, int nsl, unsigned gen, int* s_nact, int* s_anyru)
+{
+    for (int j = threadIdx.x; j < nsl; j += blockDim.x) {
+        CoefVals v;
+        if (poll_coef(a.coef + sl[j].sys, gen, v, a.err)) {
+            sl[j].mode = v.mode;
+            sl[j].alpha_re = v.alpha_re;
+            sl[j].alpha_im = v.alpha_im;
+            sl[j].beta = v.beta;
+            sl[j].c_re = v.c_re;
+            sl[j].c_im = v.c_im;
+            sl[j].f_alpha_re = (float)v.alpha_re;
+            sl[j].f_alpha_im = (float)v.alpha_im;
+            sl[j].f_beta = (float)v.beta;
+            sl[j].f_c_re = (float)v.c_re;
+            sl[j].f_c_im = (float)v.c_im;
+        }
+        __threadfence();
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        const long long t0 = clock64();
+        unsigned long long g;
+        while ((unsigned)((g = ld_word(&a.bar->gword)) >> 32) != gen)
+            if (wait_over(t0, a.err)) break;
+        *s_nact = (int)(g & 0x7fffffffull);
+        *s_anyru = (int)((g >> 31) & 1ull);
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)a.err == 0;
+}
+
+// Scalar recurrence of one system after its partials were summed (one thread):
+// updates the system's state `st` (a copy) and returns the coefficients of
+// the next pass.  s: |r|^2, |Ap|^2, <p,Ap> re/im, <r,Ap> re/im; after a
+// reliable update |r|^2 and <r, p_{k-1}> re/im in s[0], s[2], s[3].  FP64
+// division and square root each cost ~650 cycles of latency on GB300: the
+// comparisons are made on squares, the mixed solver divides in FP32.
+template <bool MIXED>
+__device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const double* s, CGState& st, int* s_active,
+                                int* s_ru)
+{
+    CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
     auto retire = [&](int conv, int status) {
         st.active = 0;
         st.converged = conv;
         st.status = status;
-        cf.mode = kIdle;
+        return cv;
     };
     const double rr = s[0];
     st.rr = rr;
     st.iters = k;
     if (ru_round) {
-        st.n_ru = st.n_ru + 1;
+        st.n_ru += 1;
         if (!isfinite(rr)) return retire(0, YK_ENAN);
-        if (!(sqrt(rr) > st.stop)) return retire(1, 0);
+        if (!(rr > st.stop2)) return retire(1, 0);
         if (k >= a.max_iter) return retire(0, YK_ENOCONV);
         // p_k = r + beta (p_{k-1} - gamma r), gamma = <r, p_{k-1}> / |r|^2
-        const double beta = rr / st.rr_prev;
-        cf.beta = beta;
-        cf.c_re = 1.0 - beta * (s[2] / rr);
-        cf.c_im = -beta * (s[3] / rr);
-        cf.mode = kRedo;
-        st.rmax = sqrt(rr);
+        const double beta = rr / st.rr_prev, inv_rr = 1.0 / rr;
+        cv.beta = beta;
+        cv.c_re = 1.0 - beta * (s[2] * inv_rr);
+        cv.c_im = -beta * (s[3] * inv_rr);
+        cv.mode = kRedo;
+        st.rmax2 = rr;
         atomicAdd(s_active, 1);
-        return;
+        return cv;
     }
     if (k == 0) {
+        st.stop2 = (a.tol_mode == YK_TOL_ABS) ? a.tol * a.tol : a.tol * a.tol * rr;
+        st.rmax2 = rr;
         st.rr0 = rr;
-        st.stop = (a.tol_mode == YK_TOL_ABS) ? a.tol : a.tol * sqrt(rr);
-        st.rmax = sqrt(rr);
     }
     if (!isfinite(rr)) return retire(0, YK_ENAN);
     // mixed: x is exact only at k = 0 and after a reliable update
-    if ((!MIXED || k == 0) && !(sqrt(rr) > st.stop)) return retire(1, 0);
+    if ((!MIXED || k == 0) && !(rr > st.stop2)) return retire(1, 0);
     if (k >= a.max_iter) return retire(0, YK_ENOCONV);
-    // alpha = rr / <p, Ap>, Smith's complex division (CGsolver.cu:137)
+    // alpha = rr / <p, Ap> = rr conj(<p, Ap>) / |<p, Ap>|^2  (CGsolver.cu:137)
     const double c = s[2], d = s[3];
     double ar, ai;
-    if (fabs(c) >= fabs(d)) {
-        const double q = d / c, den = c + d * q;
-        ar = rr / den;
-        ai = (-rr * q) / den;
+    if constexpr (MIXED) {
+        const float cf_ = (float)c, df_ = (float)d, rf = (float)rr;
+        const float inv = 1.f / fmaf(cf_, cf_, df_ * df_);
+        ar = (double)(rf * cf_ * inv);
+        ai = (double)(-rf * df_ * inv);
     } else {
-        const double q = c / d, den = c * q + d;
-        ar = (rr * q) / den;
-        ai = -rr / den;
+        const double inv_pap = 1.0 / fma(c, c, d * d);
+        ar = rr * c * inv_pap;
+        ai = -rr * d * inv_pap;
     }
     if (!isfinite(ar) || !isfinite(ai)) return retire(0, YK_ENAN);
     // |r - alpha q|^2 = |r|^2 - 2 Re(alpha <r, q>) + |alpha|^2 |q|^2
     double est = rr - 2.0 * (ar * s[4] - ai * s[5]) + (ar * ar + ai * ai) * s[1];
     if (!(est > 0.0)) est = 0.0;
     st.rr_prev = rr;
-    cf.alpha_re = ar;
-    cf.alpha_im = ai;
-    cf.beta = est / rr;
-    cf.c_re = 1.0;
-    cf.c_im = 0.0;
-    int mode = kStep;
+    cv.alpha_re = ar;
+    cv.alpha_im = ai;
+    if constexpr (MIXED)
+        cv.beta = (double)((float)est / (float)rr);
+    else
+        cv.beta = est / rr;
+    cv.mode = kStep;
     if constexpr (MIXED) {
-        const double rn = sqrt(rr), en = sqrt(est);
-        const double rmax = fmax(st.rmax, rn);
-        st.rmax = rmax;
-        const bool cand = !(rn > st.stop) || !(en > st.stop);
-        const bool drop = en < a.reliable_delta * rmax;
+        st.rmax2 = fmax(st.rmax2, rr);
+        const bool cand = !(rr > st.stop2) || !(est > st.stop2);
+        const bool drop = est < a.reliable_delta * a.reliable_delta * st.rmax2;
         const bool due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
         const bool cap = k + 1 >= a.max_iter;
         if (cand || drop || due || cap) {
-            mode = kRu;
+            cv.mode = kRu;
             atomicOr(s_ru, 1);
         }
     }
-    cf.mode = mode;
     atomicAdd(s_active, 1);
+    return cv;
+}
+
+__device__ __forceinline__ void load_state(const CGState* p, CGState& st)
+{
+    const volatile CGState& v = *p;
+    st.rr = v.rr;
+    st.rr0 = v.rr0;
+    st.rr_prev = v.rr_prev;
+    st.stop2 = v.stop2;
+    st.rmax2 = v.rmax2;
+    st.active = v.active;
+    st.iters = v.iters;
+    st.converged = v.converged;
+    st.status = v.status;
+    st.n_ru = v.n_ru;
+    st.mode = v.mode;
+}
+
+__device__ __forceinline__ void store_state(CGState* p, const CGState& st)
+{
+    volatile CGState& v = *p;
+    v.rr = st.rr;
+    v.rr0 = st.rr0;
+    v.rr_prev = st.rr_prev;
+    v.stop2 = st.stop2;
+    v.rmax2 = st.rmax2;
+    v.active = st.active;
+    v.iters = st.iters;
+    v.converged = st.converged;
+    v.status = st.status;
+    v.n_ru = st.n_ru;
+    v.mode = st.mode;
 }
 
 // The last block at a grid barrier: sums the partials of every system that
-// took part in the pass (one warp per system; lane l adds tiles l, l+32, ...
-// in order, then a fixed butterfly) and runs the scalar recurrence.
+// took part in the pass, runs the scalar recurrence and publishes the
+// coefficients, the same bits whichever block finishes.  Mixed solver:
+// float-float sums on the FP32 pipes, the block's warps in groups of
+// G = 8 / (systems) warps (at least one), a group's threads adding tiles t,
+// t + 32 G, ... in order, a fixed butterfly in each warp and the warps' sums
+// in warp order.  FP64 solver: one warp per system (its 1/64-rate
+// instructions are the cost), lanes adding tiles l, l + 32, ... in order,
+// then a fixed butterfly.  The partial sums and the system's state are loaded
+// in one batch; a single-system solve takes its tile range from the
+// arguments.  The system state lives in CGState (read and written only here;
+// the host reads it after the solve).
 template <bool MIXED>
-__device__ void finish_reduction(const CGArgs& a, int k, bool ru_round, int* s_active, int* s_ru)
+__device__ void finish_reduction(const CGArgs& a, int k, bool ru_round, int* s_active, int* s_ru, double* red,
+                                 unsigned gen)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int G = MIXED ? nw : 1;
+    while (G > 1 && G * a.sys_count > nw) G >>= 1;
+    const int ngroups = nw / G, gid = w / G, wg = w % G, T = 32 * G, tg = wg * 32 + lane;
+    float2* red2 = reinterpret_cast<float2*>(red);
     if (threadIdx.x == 0) {
         *s_active = 0;
         *s_ru = 0;
     }
     __syncthreads();
-    constexpr int U = 8;
-    for (int j = a.sys_first + w; j < a.sys_first + a.sys_count; j += nw) {
-        const int mode = *(volatile int*)&a.coef[j].mode;
-        if (mode == kIdle) continue;
-        if (ru_round && mode != kRu) {
-            if (lane == 0) {
-                *(volatile int*)&a.coef[j].mode = kWait;
+    const int rounds = (a.sys_count + ngroups - 1) / ngroups;
+#ifdef YK_CG_TIMING
+    const long long f0 = clock64();
+    long long f1 = 0, f2 = 0, f_ld = 0;
+#endif
+    for (int rnd = 0; rnd < rounds; ++rnd) {
+        const int j = a.sys_first + rnd * ngroups + gid;
+        const bool have = j < a.sys_first + a.sys_count;
+        CGState st;
+        int tile0 = 0, ntiles = 0;
+        if (have) {
+            if (tg == 0) load_state(a.st + j, st);
+            if (a.sys_count == 1) {
+                tile0 = a.tile_begin;
+                ntiles = a.tile_end - a.tile_begin;
+            } else {
+                tile0 = a.sys[j].tile0;
+                ntiles = a.sys[j].ntiles;
+            }
+        }
+        double s[6];
+        if constexpr (MIXED) {
+            FF acc[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] = FF{0.f, 0.f};
+#pragma unroll 2
+            for (int i = tg; i < ntiles; i += T) {
+                const Partial* pp = a.partial + tile0 + i;
+                const float4 q0 = ld_sync4f(&pp->f[0]), q1 = ld_sync4f(&pp->f[2]), q2 = ld_sync4f(&pp->f[4]);
+                acc[0] = ff_add(acc[0], FF{q0.x, q0.y});
+                acc[1] = ff_add(acc[1], FF{q0.z, q0.w});
+                acc[2] = ff_add(acc[2], FF{q1.x, q1.y});
+                acc[3] = ff_add(acc[3], FF{q1.z, q1.w});
+                acc[4] = ff_add(acc[4], FF{q2.x, q2.y});
+                acc[5] = ff_add(acc[5], FF{q2.z, q2.w});
+            }
+#ifdef YK_CG_TIMING
+            if (threadIdx.x == 0) f_ld = clock64();
+#endif
+            // level-outer: the six independent chains interleave
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] = ff_add(acc[c], ff_shfl_xor(acc[c], o));
+            if (lane == 0)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) red2[w * 6 + c] = make_float2(acc[c].hi, acc[c].lo);
+            __syncthreads();
+            if (have && tg == 0) {
+                FF t[6];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) t[c] = FF{red2[w * 6 + c].x, red2[w * 6 + c].y};
+                for (int u = 1; u < G; ++u)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) t[c] = ff_add(t[c], FF{red2[(w + u) * 6 + c].x, red2[(w + u) * 6 + c].y});
+#pragma unroll
+                for (int c = 0; c < 6; ++c) s[c] = (double)t[c].hi + (double)t[c].lo;
+            }
+        } else {
+            constexpr int U = 8;
+            double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int base = tg; base < ntiles; base += T * U) {
+                double2 v[U][3];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    // the address is clamped into the system's tiles, so a load
+                    // issued ahead of the range test never leaves the array
+                    const int i = base + T * u;
+                    const int ii = i < ntiles ? i : ntiles - 1;
+                    const Partial* pp = a.partial + tile0 + ii;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const double2 t = ld_sync2(&pp->d[2 * c]);
+                        v[u][c] = (i < ntiles) ? t : make_double2(0.0, 0.0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        acc[2 * c] += v[u][c].x;
+                        acc[2 * c + 1] += v[u][c].y;
+                    }
+            }
+#ifdef YK_CG_TIMING
+            if (threadIdx.x == 0) f_ld = clock64();
+#endif
+            // G = 1: the warp is the group; level-outer butterfly
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[c] = acc[c];
+            __syncthreads();
+        }
+#ifdef YK_CG_TIMING
+        if (threadIdx.x == 0) f1 = clock64();
+#endif
+        const bool writer = have && tg == 0;
+        CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
+        if (writer && st.mode != kIdle) {
+            if (ru_round && st.mode != kRu) {
+                cv.mode = kWait;
                 atomicAdd(s_active, 1);
+            } else {
+                cv = scalar_step<MIXED>(a, k, ru_round, s, st, s_active, s_ru);
             }
-            continue;
         }
-        const SysDev& S = a.sys[j];
-        double acc[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) acc[q] = 0.0;
-        for (int base = lane; base < S.ntiles; base += 32 * U) {
-            double2 v[U][3];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                // the address is clamped into the system's tiles, so a load issued
-                // ahead of the range test never leaves the array
-                const int i = base + 32 * u;
-                const int ii = i < S.ntiles ? i : S.ntiles - 1;
-                const double2* q = reinterpret_cast<const double2*>(a.partial + S.tile0 + ii);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const double2 t = ld_volatile2(q + c);
-                    v[u][c] = (i < S.ntiles) ? t : make_double2(0.0, 0.0);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    acc[2 * c] += v[u][c].x;
-                    acc[2 * c + 1] += v[u][c].y;
-                }
+#ifdef YK_CG_TIMING
+        if (threadIdx.x == 0) f2 = clock64();
+#endif
+        __syncthreads();   // the counts of the round are complete
+        const bool last_round = rnd == rounds - 1;
+        if (writer || (last_round && threadIdx.x == 0)) __threadfence();
+        if (writer) publish_coef(a.coef + j, cv, gen);
+        if (last_round && threadIdx.x == 0)
+            st_word(&a.bar->gword, stamp((unsigned)*s_active | ((unsigned)(*s_ru != 0) << 31), gen));
+        if (writer) {
+            st.mode = cv.mode;
+            store_state(a.st + j, st);
         }
-#pragma unroll
-        for (int q = 0; q < 6; ++q) acc[q] = warp_sum(acc[q]);
-        if (lane == 0) scalar_step<MIXED>(a, j, k, ru_round, acc, s_active, s_ru);
+        __syncthreads();
     }
-    __syncthreads();
+#ifdef YK_CG_TIMING
     if (threadIdx.x == 0) {
-        *(volatile int*)a.n_active = *s_active;
-        *(volatile int*)a.any_ru = *s_ru;
+        const long long f3 = clock64();
+        atomicAdd(&g_cg_f[0], (unsigned long long)(f1 - f0));
+        atomicAdd(&g_cg_f[4], (unsigned long long)(f_ld - f0));
+        atomicAdd(&g_cg_f[1], (unsigned long long)(f2 - f1));
+        atomicAdd(&g_cg_f[2], (unsigned long long)(f3 - f2));
+        atomicAdd(&g_cg_f[3], 1ull);
     }
+#endif
 }
 
 // Grid barrier that also completes the reduction of the pass: the last block
-// to arrive sums the partials and publishes the coefficients, then advances
-// the generation the others wait on.
+// to arrive (the arrival counter runs on across the solve) sums the partials
+// and publishes the coefficients of generation gen + 1; the caller then
+// polls them (poll_coefs).
 template <bool MIXED>
-__device__ bool grid_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, int* s_flag, int* s_active,
-                            int* s_ru)
+__device__ void grid_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, int* s_flag, int* s_active,
+                            int* s_ru, double* red)
 {
     __syncthreads();
+#ifdef YK_CG_TIMING
+    const long long c0 = clock64();
+#endif
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned old = atomicAdd(&a.bar->arrive, 1u);
-        const int last = (old == gridDim.x - 1) ? 1 : 0;
+        const int last = (old + 1u == gridDim.x * (gen + 1u)) ? 1 : 0;
+#ifdef YK_CG_TIMING
+        if (old == gridDim.x * gen) g_cg_first = gtimer();
+        if (last) atomicAdd(&g_cg_t[8], gtimer() - *(volatile unsigned long long*)&g_cg_first);
+        atomicAdd(&g_cg_t[0], (unsigned long long)(clock64() - c0));
+        atomicAdd(&g_cg_t[1], 1ull);
+#endif
         if (last) __threadfence();
         *s_flag = last;
     }
     __syncthreads();
     if (*s_flag) {
-        finish_reduction<MIXED>(a, k, ru_round, s_active, s_ru);
-        __syncthreads();
+#ifdef YK_CG_TIMING
+        const long long c1 = clock64();
+#endif
+        finish_reduction<MIXED>(a, k, ru_round, s_active, s_ru, red, gen + 1u);
+#ifdef YK_CG_TIMING
         if (threadIdx.x == 0) {
-            *(volatile unsigned*)&a.bar->arrive = 0u;
-            __threadfence();
-            *(volatile unsigned*)&a.bar->gen = gen + 1u;
+            atomicAdd(&g_cg_t[2], (unsigned long long)(clock64() - c1));
+            atomicAdd(&g_cg_t[3], 1ull);
         }
-    } else if (threadIdx.x == 0) {
-        const volatile unsigned* g = &a.bar->gen;
-        const long long t0 = clock64();
-        while (*g == gen)
-            if (wait_over(t0, a.err)) break;
-        __threadfence();
+#endif
     }
-    __syncthreads();
     ++gen;
-    return *(volatile int*)a.err == 0;
 }
 
 template <typename W, bool MIXED>
@@ -504,34 +846,68 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, T (&v)[6]
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int i = 0; i < 6; ++i)
-        if (!((SKIP_MASK >> i) & 1))
+    for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+        for (int i = 0; i < 6; ++i)
+            if (!((SKIP_MASK >> i) & 1)) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
     __syncthreads();
     if (lane == 0)
 #pragma unroll
         for (int i = 0; i < 6; ++i) red[w * 6 + i] = (double)v[i];
     __syncthreads();
-    if (w == 0) {
-        double t[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            t[i] = lane < nw ? red[lane * 6 + i] : 0.0;
-            if (!((SKIP_MASK >> i) & 1)) t[i] = warp_sum(t[i]);
-        }
-        if (lane == 0) {
+    // one thread per value adds the warps' sums in warp order (few FP64
+    // instructions: GB300 issues them at 1/64 of the FP32 rate)
+    if (threadIdx.x < 6) {
+        const int i = threadIdx.x;
+        double t = red[i];
+        for (int u = 1; u < nw; ++u) t += red[u * 6 + i];
 #ifdef YK_CG_CHECKED
-            if (tile < a.tile_begin || tile >= a.tile_end) {
-                if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
-                return;
-            }
-#endif
-            Partial p;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) p.v[i] = t[i];
-            a.partial[tile] = p;
+        if (tile < a.tile_begin || tile >= a.tile_end) {
+            if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
+            return;
         }
+#endif
+        a.partial[tile].d[i] = t;
+    }
+}
+
+// Block sums of a tile's six values -> its partial slot as float-float pairs
+// (mixed solver).  WARP_FF: the per-site values carry a low part (FP64
+// residuals of a reliable update) and the warp butterfly runs in float-float;
+// otherwise the warp sums are plain FP32 (the per-site values are FP32
+// products).  The warps' sums are added in warp order by one thread per value.
+template <int SKIP_MASK, bool WARP_FF>
+__device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, FF (&v)[6], double* red)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float2* red2 = reinterpret_cast<float2*>(red);
+    // level-outer: the independent chains interleave
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            if (!((SKIP_MASK >> i) & 1)) {
+                if constexpr (WARP_FF)
+                    v[i] = ff_add(v[i], ff_shfl_xor(v[i], o));
+                else
+                    v[i].hi += __shfl_xor_sync(0xffffffffu, v[i].hi, o);
+            }
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) red2[w * 6 + i] = make_float2(v[i].hi, v[i].lo);
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int i = threadIdx.x;
+        FF t{red2[i].x, red2[i].y};
+        for (int u = 1; u < nw; ++u) t = ff_add(t, FF{red2[u * 6 + i].x, red2[u * 6 + i].y});
+#ifdef YK_CG_CHECKED
+        if (tile < a.tile_begin || tile >= a.tile_end) {
+            if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
+            return;
+        }
+#endif
+        a.partial[tile].f[i] = make_float2(t.hi, t.lo);
     }
 }
 
@@ -555,6 +931,10 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
     if (*(volatile int*)a.err) return;   // the other blocks' waits see the flag and end
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
     unsigned epoch = 0, gen = 0;
+#ifdef YK_CG_TIMING
+    long long tacc[5] = {0, 0, 0, 0, 0}, tlast = clock64();
+    int tit = 0;
+#endif
 
     auto Rv = [](const SysDev& S, int i) -> W* {
         if constexpr (MIXED) return S.r32[i]; else return S.r64[i];
@@ -590,7 +970,14 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                 site_dot<W, K>(p, ap, v[2], v[3]);
                 site_dot<W, K>(r, ap, v[4], v[5]);
             }
-            put_partial<W, kSkipIm>(a, tile, v, red);
+            if constexpr (MIXED) {
+                FF f[6];
+#pragma unroll
+                for (int i = 0; i < 6; ++i) f[i] = FF{v[i], 0.f};
+                put_partial_ff<kSkipIm, false>(a, tile, f, red);
+            } else {
+                put_partial<W, kSkipIm>(a, tile, v, red);
+            }
         }
     };
 
@@ -626,11 +1013,12 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
     }
     if (!nsync(a, ++epoch, deps)) return;
     pass_b(0);
-    if (!grid_reduce<MIXED>(a, gen, 0, false, &s_flag, &s_active, &s_ru)) return;
+    grid_reduce<MIXED>(a, gen, 0, false, &s_flag, &s_active, &s_ru, red);
 
     int k = 1;
     while (k <= a.max_iter) {   // every system retires at k = max_iter at the latest
-        load_coefs(a, sl, nsl, &s_nact, &s_anyru);
+        if (!poll_coefs(a, sl, nsl, gen, &s_nact, &s_anyru)) return;
+        YK_TMARK(0);   // grid reduction + coefficient load
         if (s_nact == 0) break;
         const bool any_ru = MIXED && s_anyru;
         const int cur = k & 1, prv = cur ^ 1;
@@ -664,10 +1052,10 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
             }
             const Nbr nb = neighbours(n, S.Nt, S.Nx);
             const int64_t m5[5] = {n, nb.tu, nb.td, nb.xu, nb.xd};
-            const W beta = (W)L.beta;
+            const W beta = pick<W>(L.beta, L.f_beta);
             Site<W, K> pn[5];
             if (mode == kStep) {
-                const W ar = (W)L.alpha_re, ai = (W)L.alpha_im;
+                const W ar = pick<W>(L.alpha_re, L.f_alpha_re), ai = pick<W>(L.alpha_im, L.f_alpha_im);
                 Site<W, K> r_own, p_old;
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
@@ -688,7 +1076,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                 YK_ST(W, K, Rv(S, cur), n, r_own);
             } else {
                 // kRedo: r_k is the FP64 residual (rounded) in R[cur]
-                const W cre = (W)L.c_re, cim = (W)L.c_im;
+                const W cre = pick<W>(L.c_re, L.f_c_re), cim = pick<W>(L.c_im, L.f_c_im);
 #pragma unroll
                 for (int q = 0; q < 5; ++q) {
                     const Site<W, K> r = YK_LD(W, K, Rv(S, cur), m5[q]);
@@ -703,7 +1091,9 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
             YK_ST(W, K, Tv(S), n, t);
             YK_ST(W, K, Pv(S, cur), n, pn[0]);
         }
+        YK_TMARK(1);   // pass A
         if (!nsync(a, ++epoch, deps)) return;
+        YK_TMARK(2);   // neighbour sync
 
         if constexpr (MIXED) {
             if (any_ru) {
@@ -760,18 +1150,40 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                         site_dot<double, K>(rd, pd, v[2], v[3]);
                     }
                     // slots 1, 4, 5 unused here
-                    put_partial<double, (1 << 1) | (1 << 4) | (1 << 5) | kSkipIm>(a, tile, v, red);
+                    FF f[6];
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+                    put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, f, red);
                 }
-                if (!grid_reduce<MIXED>(a, gen, k, true, &s_flag, &s_active, &s_ru)) return;
+                grid_reduce<MIXED>(a, gen, k, true, &s_flag, &s_active, &s_ru, red);
                 continue;   // same k: the systems that updated redo A(k)
             }
         }
 
         // ---------------- B(k)
         pass_b(cur);
-        if (!grid_reduce<MIXED>(a, gen, k, false, &s_flag, &s_active, &s_ru)) return;
+        YK_TMARK(3);   // pass B
+        grid_reduce<MIXED>(a, gen, k, false, &s_flag, &s_active, &s_ru, red);
         ++k;
+#ifdef YK_CG_TIMING
+        ++tit;
+#endif
     }
+#ifdef YK_CG_TIMING
+    if (blockIdx.x == 0 && threadIdx.x == 0 && tit > 0)
+    {
+        printf("cg timing (block 0, cycles per iteration over %d): reduce+coef %lld  A %lld  nsync %lld  B %lld\n", tit,
+               tacc[0] / tit, tacc[1] / tit, tacc[2] / tit, tacc[3] / tit);
+        volatile unsigned long long* t = g_cg_t;
+        printf("cg timing (all blocks, cycles per event): arrive %llu  finish %llu  arrival spread %llu ns\n",
+               t[0] / (t[1] ? t[1] : 1), t[2] / (t[3] ? t[3] : 1), t[8] / (t[3] ? t[3] : 1));
+        volatile unsigned long long* f = g_cg_f;
+        printf("cg timing (finisher, cycles per event): sums %llu (loads %llu)  scalar %llu  tail %llu\n",
+               f[0] / (f[3] ? f[3] : 1), f[4] / (f[3] ? f[3] : 1), f[1] / (f[3] ? f[3] : 1), f[2] / (f[3] ? f[3] : 1));
+        for (int i = 0; i < 10; ++i) t[i] = 0;
+        for (int i = 0; i < 8; ++i) f[i] = 0;
+    }
+#endif
 }
 
 // Resets the barrier, flags, counters and per-system state before a solve.
@@ -779,23 +1191,22 @@ __global__ void cg_prepare_kernel(CGArgs a)
 {
     for (int i = a.sys_first + threadIdx.x; i < a.sys_first + a.sys_count; i += blockDim.x) {
         CGState& s = a.st[i];
-        s.rr = s.rr0 = s.rr_prev = s.stop = s.rmax = 0.0;
+        s.rr = s.rr0 = s.rr_prev = s.stop2 = s.rmax2 = 0.0;
         s.active = 1;
         s.iters = 0;
         s.converged = 0;
         s.status = 0;
         s.n_ru = 0;
-        CGCoef& c = a.coef[i];
-        c.alpha_re = c.alpha_im = c.beta = c.c_im = 0.0;
-        c.c_re = 1.0;
-        c.mode = kStep;
+        s.mode = kStep;
+        // generation 0: the coefficients of round 0 (never polled)
+        for (int q = 0; q < 12; ++q) a.coef[i].w[q] = 0ull;
     }
     for (int b = threadIdx.x; b < a.grid; b += blockDim.x) a.flags[(size_t)b * kFlagStride] = 0u;
     if (threadIdx.x == 0) {
         *a.n_active = a.sys_count;
         *a.any_ru = 0;
         a.bar->arrive = 0u;
-        a.bar->gen = 0u;
+        a.bar->gword = 0ull;
         *a.err = 0;
     }
 }
@@ -810,11 +1221,20 @@ static int max_coresident(const void* fn, int block)
     return g < kMaxGrid ? g : kMaxGrid;
 }
 
+// Largest grid of the CG kernel: the co-resident maximum, capped by the
+// environment variable YK_CG_MAX_GRID when it is set (a tuning knob: fewer
+// blocks own more tiles each).
 template <int K, bool MIXED>
 static int max_grid_t()
 {
     static int maxg = -1;
-    if (maxg < 0) maxg = max_coresident((const void*)cg_kernel<K, MIXED>, kBlock);
+    if (maxg < 0) {
+        maxg = max_coresident((const void*)cg_kernel<K, MIXED>, kBlock);
+        if (const char* e = getenv("YK_CG_MAX_GRID")) {
+            const int cap = atoi(e);
+            if (cap > 0 && cap < maxg) maxg = cap;
+        }
+    }
     return maxg;
 }
 

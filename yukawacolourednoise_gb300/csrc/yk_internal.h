@@ -23,13 +23,15 @@ constexpr int kMaxTilesPerBlock = 512;   // tiles one CG block may own
 constexpr int kMaxGrid = 2048;           // blocks of a CG launch (neighbour flags allocated)
 constexpr int kFlagStride = 32;          // one 128-byte line per neighbour flag
 
-// Grid barrier of the CG kernel: arrivals are counted on one line; the last
-// block to arrive finishes the reduction and advances `gen` on another.
+// Grid barrier of the CG kernel: arrivals are counted (monotonically within a
+// solve) on one line; the last block to arrive finishes the reduction and
+// publishes the grid word (active systems, reliable-update flag) stamped with
+// the barrier's generation on another.
 struct GridBarrier {
     unsigned arrive;
     unsigned pad0[31];
-    unsigned gen;
-    unsigned pad1[31];
+    unsigned long long gword;
+    unsigned long long pad1[15];
 };
 
 // One linear system (chain, right-hand side) of a batched CG solve.
@@ -59,10 +61,12 @@ struct SysDev {
     const int64_t* step; // device step counter of the chain
 };
 
-// Per-tile reduction slot of the CG kernel: |r|^2, |Ap|^2, <p, Ap>, <r, Ap>
-// (re, im); after a reliable update |r|^2 and <r, p> of the FP64 residual.
-struct __align__(16) Partial {
-    double v[6];
+// Per-tile reduction slot of the CG kernel: |r|^2, |Ap|^2, <p, Ap> (re, im),
+// <r, Ap> (re, im); after a reliable update |r|^2 and <r, p> of the FP64
+// residual.  FP64 solver: FP64 sums; mixed solver: float-float (hi, lo) sums.
+union __align__(16) Partial {
+    double d[6];
+    float2 f[6];
 };
 
 // Per-system CG scalars.  Written only by the block that completes a grid
@@ -70,23 +74,22 @@ struct __align__(16) Partial {
 struct CGState {
     double rr, rr0;      // last |r|^2, |b|^2
     double rr_prev;      // |r|^2 of the previous iteration (mixed: beta after a reliable update)
-    double stop;         // stopping threshold on |r|
-    double rmax;         // largest |r| since the last reliable update (mixed)
+    double stop2;        // stopping threshold on |r|^2 (tol^2, or tol^2 |b|^2)
+    double rmax2;        // largest |r|^2 since the last reliable update (mixed)
     int active;
     int iters;
     int converged;
     int status;
     int n_ru;            // reliable updates (mixed)
-    int pad;
+    int mode;            // the system's mode in the pass that follows
 };
 
-// Per-system coefficients of the next pass, published with each grid reduction.
-struct CGCoef {
-    double alpha_re, alpha_im;   // x += alpha p, r -= alpha A p
-    double beta;                 // p = c r + beta p
-    double c_re, c_im;
-    int mode;                    // CGMode
-    int pad;
+// Per-system coefficients of the next pass (alpha: x += alpha p, r -= alpha A p;
+// beta, c: p = c r + beta p; the mode), published with each grid reduction as
+// twelve 64-bit words, each carrying 32 bits of payload and the barrier
+// generation in its high half.
+struct __align__(16) CGCoef {
+    unsigned long long w[12];
 };
 
 struct CGArgs {
