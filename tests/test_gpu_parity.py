@@ -225,7 +225,11 @@ def test_langevin_steps_match_oracle(ylib, cuda, Nt, Nx, s, fixed_dt):
         assert ctx.get_step() == 4 and obs.steps == 4
 
 
-def test_langevin_mixed_precision_step(ylib, cuda):
+@pytest.mark.parametrize("cluster", ["1", "0"], ids=["cluster_cg", "grid_cg"])
+def test_langevin_mixed_precision_step(ylib, cuda, monkeypatch, cluster):
+    # the cluster-resident CG (default for lattices that fit a 16-CTA cluster)
+    # and the grid-wide CG kernel
+    monkeypatch.setenv("YK_CG_CLUSTER", cluster)
     yk = ylib
     Nt, Nx = 32, 32
     p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
@@ -254,6 +258,29 @@ def test_batched_chains_equal_single_chains(ylib, cuda):
             phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=2, tol=1e-12, tol_mode=1)
         assert np.abs(batched[c] - phi).max() < 1e-9, c
         assert obs_b[c].steps == 3
+
+
+@pytest.mark.parametrize("cluster", ["1", "0"], ids=["cluster_cg", "grid_cg"])
+def test_batched_mixed_chains(ylib, cuda, monkeypatch, cluster):
+    # batched chains of different shapes (rows not divisible by 16, CTAs of a
+    # cluster without rows, two right-hand sides) through the mixed solver
+    monkeypatch.setenv("YK_CG_CLUSTER", cluster)
+    yk = ylib
+    specs = [(40, 24, 0.1, 0.5, S_HALF_PI, 2), (8, 8, 0.25, 0.3, 0.2, 1), (16, 64, 0.05, 0.8, 1.0, 1)]
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, cut_fraction=s, n_rhs=nr, precision=yk.YK_MIXED,
+                 cg_tol=1e-10, fixed_dt=0.01)
+          for nt, nx, m0, g, s, nr in specs]
+    with yk.Context(ps) as ctx:
+        ctx.step(2)
+        got = [ctx.get_field(c) for c in range(len(ps))]
+        obs = [ctx.observables(c) for c in range(len(ps))]
+    for c, p in enumerate(ps):
+        phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+        for step in range(2):
+            phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10, tol_mode=1,
+                                     fixed_dt=0.01)
+        assert np.abs(got[c] - phi).max() < 1e-8, c
+        assert obs[c].steps == 2 and obs[c].status == 0
 
 
 def test_deterministic(ylib, cuda):

@@ -8,6 +8,7 @@
 // buffers with a device synchronisation after every launch.
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -121,6 +122,11 @@ struct yk_ctx {
     cudaGraphExec_t gexec = nullptr;
     bool graph_failed = false;
     int cg_grid = 0;
+    // mixed precision with every step system fitting one 16-CTA cluster: the
+    // cluster-resident CG (YK_CG_CLUSTER=0 in the environment selects the
+    // grid-wide kernel instead)
+    bool cg_cluster = false;
+    int cluster_sites = 0;   // largest per-CTA share of the step systems
     // profiling: CUDA events around each kernel class of the step
     bool profiling = false;
     struct Rec {
@@ -278,7 +284,13 @@ int enqueue_step(yk_ctx* ctx)
         a.st = ctx->d_state;
         a.partial = ctx->d_partial;
         a.coef = ctx->d_coef;
-        YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
+        if (ctx->cg_cluster) {
+            YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles, ctx->n_sys_tiles, 2, ctx->stream));
+            YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
+            ctx->cg_grid = 16 * ctx->nsys;
+        } else {
+            YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
+        }
         prof_end(ctx, 1, e, 2);
     }
     StepArgs s = step_args(ctx);
@@ -455,7 +467,12 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
     a.st = ctx->d_state;
     a.partial = ctx->d_partial;
     a.coef = ctx->d_coef;
-    YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, nullptr));
+    if (ctx->cg_cluster) {
+        YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles + C.cg_tile0, C.cg_tile1 - C.cg_tile0, kind, ctx->stream));
+        YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
+    } else {
+        YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, nullptr));
+    }
     std::vector<CGState> st(C.n_rhs_step);
     YK_CK(cudaMemcpyAsync(st.data(), ctx->d_state + C.sys0, sizeof(CGState) * C.n_rhs_step,
                           cudaMemcpyDeviceToHost, ctx->stream));
@@ -530,6 +547,20 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     cg_max_grid(2, false);
     cg_max_grid(2, true);
     noise_init_attributes();
+    {
+        const char* env = getenv("YK_CG_CLUSTER");
+        bool want = mixed && !(env && env[0] == '0');
+        int sites = 0;
+        for (int c = 0; c < n_chains && want; ++c) {
+            const yk_params& q = params[c];
+            if (!cg_cluster_fits(q.Nt, q.Nx))
+                want = false;
+            else
+                sites = std::max(sites, ((q.Nt + 15) / 16) * q.Nx);
+        }
+        ctx->cg_cluster = want && cg_cluster_init();
+        ctx->cluster_sites = sites;
+    }
 
     ctx->ch.resize(n_chains);
     int nsys = 0, nsys_tiles = 0, nsite_tiles = 0, nrows = 0, ncols = 0, nwhite = 0;

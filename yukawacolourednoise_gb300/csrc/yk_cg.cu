@@ -820,24 +820,6 @@ __device__ __forceinline__ Site<W, K> p_next(const Site<W, K>& r, const Site<W, 
     return o;
 }
 
-template <int K>
-__device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int kind)
-{
-    // real Gaussian entries, imaginary parts zero (FermionicDrift.cu:102-110)
-    const RngStream rs = rng_stream(S.seed, (uint32_t)S.chain, (uint64_t)(*S.step), (uint32_t)kind,
-                                    (uint32_t)S.rhs);
-    const double2 a = normal_pair(rs, (uint32_t)(2 * n));
-    const double2 b = normal_pair(rs, (uint32_t)(2 * n + 1));
-    Site<double, K> s;
-    const double e[4] = {a.x, a.y, b.x, b.y};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        s.v[i * K] = e[i];
-        if constexpr (K == 2) s.v[i * K + 1] = 0.0;
-    }
-    return s;
-}
-
 // Block sums of a tile's six values -> its partial slot.  Per-site values and
 // warp sums in T (FP32 for the mixed solver), FP64 across the warps.  Values
 // listed in `skip` are known to be zero and are not reduced.

@@ -191,6 +191,26 @@ __device__ __forceinline__ double2 normal_pair(const RngStream& s, uint32_t e)
     return make_double2(R * cs, R * sn);
 }
 
+// Fermion noise eta of one CG system at site n: real Gaussian entries from the
+// Philox stream (seed, chain; step, kind, rhs), imaginary parts zero
+// (FermionicDrift.cu:102-110).
+template <int K>
+__device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int kind)
+{
+    const RngStream rs = rng_stream(S.seed, (uint32_t)S.chain, (uint64_t)(*S.step), (uint32_t)kind,
+                                    (uint32_t)S.rhs);
+    const double2 a = normal_pair(rs, (uint32_t)(2 * n));
+    const double2 b = normal_pair(rs, (uint32_t)(2 * n + 1));
+    Site<double, K> s;
+    const double e[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        s.v[i * K] = e[i];
+        if constexpr (K == 2) s.v[i * K + 1] = 0.0;
+    }
+    return s;
+}
+
 // ---------------------------------------------------------------------------
 // Reductions (fixed order => deterministic for a given block size).
 // ---------------------------------------------------------------------------

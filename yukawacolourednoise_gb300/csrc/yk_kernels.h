@@ -18,6 +18,17 @@ cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt,
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out);
 // Largest co-resident grid of the CG kernel (cached; call before capturing).
 int cg_max_grid(int K, bool mixed);
+
+// Cluster-resident mixed CG (yk_cg_cluster.cu): one 16-CTA cluster per system
+// of real (K = 1) vectors whose rows fit the cluster (cg_cluster_fits);
+// max_sites = the largest per-CTA share (ceil(Nt / 16) * Nx) of the systems.
+// cg_cluster_init opts in to the cluster size and shared memory and checks
+// residency (call before capturing).  launch_eta draws b = eta for the
+// systems of the given tiles (the cluster kernel reads b).
+bool cg_cluster_fits(int Nt, int Nx);
+bool cg_cluster_init();
+cudaError_t launch_cg_cluster(const CGArgs& a, int max_sites, cudaStream_t stream);
+cudaError_t launch_eta(const SysDev* sys, const int2* tiles, int ntiles, int kind, cudaStream_t stream);
 // Raises the shared-memory limit of the FFT kernels (call before capturing).
 void noise_init_attributes();
 
