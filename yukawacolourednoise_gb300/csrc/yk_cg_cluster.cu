@@ -33,6 +33,24 @@
 
 namespace cg = cooperative_groups;
 
+#ifdef YK_CG_TIMING
+#include <cstdio>
+// Timing build: CTA 0 of the first cluster accumulates the clock cycles of
+// each part of an iteration and prints the averages when the solve ends.
+#define YK_CMARK(i)                                                       \
+    do {                                                                  \
+        if (blockIdx.x == 0 && threadIdx.x == 0) {                        \
+            const long long t_ = clock64();                               \
+            tacc[i] += t_ - tlast;                                        \
+            tlast = t_;                                                   \
+        }                                                                 \
+    } while (0)
+#else
+#define YK_CMARK(i) \
+    do {            \
+    } while (0)
+#endif
+
 namespace yk {
 
 namespace {
@@ -106,27 +124,45 @@ struct CGeo {
     unsigned rank;
 };
 
-// Element x of global row `row` of a CTA-distributed buffer (local or remote).
-__device__ __forceinline__ const float4* row_elem(const float4* buf, int row, int x, const CGeo& g,
-                                                  cg::cluster_group& cl)
+// The rows just above and below this CTA's rows, in the CTAs that own them
+// (row 0 follows row Nt - 1): element 0 of each, as generic pointers into
+// distributed shared memory, for one CTA-distributed buffer.
+struct Halo {
+    const float4* up;
+    const float4* dn;
+};
+
+__device__ __forceinline__ Halo halo_of(const float4* buf, const CGeo& g, cg::cluster_group& cl)
 {
-    const unsigned q = (unsigned)(row / g.R);
-    const float4* base = (q == g.rank) ? buf : cl.map_shared_rank(buf, q);
-    return base + (row - (int)q * g.R) * g.Nx + x;
+    Halo h = {nullptr, nullptr};
+    if (g.rows == 0) return h;
+    const unsigned q_up = (g.row0 + g.rows == g.Nt) ? 0u : g.rank + 1;   // its local row 0
+    const unsigned q_dn = (g.row0 == 0) ? (unsigned)((g.Nt - 1) / g.R) : g.rank - 1;
+    const int dn_row = (g.row0 == 0) ? (g.Nt - 1) - (int)q_dn * g.R : g.R - 1;
+    h.up = cl.map_shared_rank(buf, q_up);
+    h.dn = cl.map_shared_rank(buf, q_dn) + dn_row * g.Nx;
+    return h;
 }
 
-// FP32 stencil of a CTA-distributed buffer at local site l.
+// FP32 stencil of a CTA-distributed buffer at local site l = (local row lr,
+// column x); rows outside the CTA come from the halo pointers.
 template <bool DAG>
-__device__ __forceinline__ float4 stencil32(const float4* buf, int l, const CGeo& g, cg::cluster_group& cl, float diag,
-                                            float r)
+__device__ __forceinline__ float4 stencil32(const float4* buf, const Halo& h, int l, int lr, int x, const CGeo& g,
+                                            float diag, float r)
 {
-    const int lr = l / g.Nx, x = l - lr * g.Nx, t = g.row0 + lr;
-    const int tu = (t + 1 == g.Nt) ? 0 : t + 1, td = (t == 0) ? g.Nt - 1 : t - 1;
+    const int t = g.row0 + lr;
     const float4 c = buf[l];
-    const float4 xu = buf[l - x + (x + 1 == g.Nx ? 0 : x + 1)];
-    const float4 xd = buf[l - x + (x == 0 ? g.Nx - 1 : x - 1)];
-    const float4 vu = (lr + 1 < g.rows) ? buf[l + g.Nx] : *row_elem(buf, tu, x, g, cl);
-    const float4 vd = (lr > 0) ? buf[l - g.Nx] : *row_elem(buf, td, x, g, cl);
+    const float4 xu = buf[l + (x + 1 == g.Nx ? 1 - g.Nx : 1)];
+    const float4 xd = buf[l + (x == 0 ? g.Nx - 1 : -1)];
+    float4 vu, vd;
+    if (lr + 1 < g.rows)
+        vu = buf[l + g.Nx];
+    else
+        vu = h.up[x];
+    if (lr > 0)
+        vd = buf[l - g.Nx];
+    else
+        vd = h.dn[x];
     const float sp = (t + 1 == g.Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
     return f4(dirac_combine<float, 1, DAG>(s4(c), s4(vu), s4(vd), s4(xu), s4(xd), diag, r, sp, sm));
 }
@@ -344,7 +380,10 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
     const int n0 = g.row0 * g.Nx;   // first global site of the CTA
 
     // per-thread state: r and the FP32 solution increment of its sites
+    // l = threadIdx.x + j * kCThreads (row l >> lgx, column l & (Nx - 1))
     float4 r[kCSpt], xs[kCSpt];
+    const int lgx = __ffs(g.Nx) - 1;   // Nx is a power of two (cg_cluster_fits)
+    const Halo hp = halo_of(sh.p, g, cl), ht = halo_of(sh.t, g, cl);
 
     // ---------------- round 0: r = p = b, x = 0
     if (threadIdx.x == 0) {
@@ -370,25 +409,34 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
         }
     }
     int k = 0;
+#ifdef YK_CG_TIMING
+    long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tlast = clock64();
+    int nit = 0;
+#endif
     for (;;) {
         // ---------------- t = D_first p
+        YK_CMARK(0);   // A pass / reliable update
         cl.sync();
-#pragma unroll
+        YK_CMARK(1);   // barrier
+#pragma unroll 2
         for (int j = 0; j < kCSpt; ++j) {
             const int l = threadIdx.x + j * kCThreads;
             if (l < g.L)
-                sh.t[l] = first_dag ? stencil32<true>(sh.p, l, g, cl, sh.diag[l], rW)
-                                    : stencil32<false>(sh.p, l, g, cl, sh.diag[l], rW);
+                sh.t[l] = first_dag ? stencil32<true>(sh.p, hp, l, l >> lgx, l & (g.Nx - 1), g, sh.diag[l], rW)
+                                    : stencil32<false>(sh.p, hp, l, l >> lgx, l & (g.Nx - 1), g, sh.diag[l], rW);
         }
+        YK_CMARK(2);   // T pass
         cl.sync();
+        YK_CMARK(1);
         // ---------------- A p = D_second t; |r|^2, |Ap|^2, <p,Ap>, <r,Ap>
         float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
 #pragma unroll
         for (int j = 0; j < kCSpt; ++j) {
             const int l = threadIdx.x + j * kCThreads;
             if (l < g.L) {
-                const float4 ap = first_dag ? stencil32<false>(sh.t, l, g, cl, sh.diag[l], rW)
-                                            : stencil32<true>(sh.t, l, g, cl, sh.diag[l], rW);
+                const float4 ap = first_dag
+                    ? stencil32<false>(sh.t, ht, l, l >> lgx, l & (g.Nx - 1), g, sh.diag[l], rW)
+                    : stencil32<true>(sh.t, ht, l, l >> lgx, l & (g.Nx - 1), g, sh.diag[l], rW);
                 sh.ap[l] = ap;
                 const float4 p = sh.p[l], rr = r[j];
                 v0 = fmaf(rr.x, rr.x, fmaf(rr.y, rr.y, fmaf(rr.z, rr.z, fmaf(rr.w, rr.w, v0))));
@@ -397,9 +445,16 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
                 v3 = fmaf(rr.x, ap.x, fmaf(rr.y, ap.y, fmaf(rr.z, ap.z, fmaf(rr.w, ap.w, v3))));
             }
         }
+        YK_CMARK(3);   // B pass
         cta_partials(v0, v1, v2, v3, sh);
+        YK_CMARK(4);   // CTA partials
         cl.sync();
+        YK_CMARK(1);
         cluster_step(a, sh, cl, st, k, false);
+        YK_CMARK(5);   // cluster sums + scalars
+#ifdef YK_CG_TIMING
+        ++nit;
+#endif
         if (st.done) break;
         ++k;
         if (st.mode == kCRu) {
@@ -466,6 +521,7 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
                                           fmaf(be, p.z, c * r[j].z), fmaf(be, p.w, c * r[j].w));
                 }
             }
+            YK_CMARK(6);   // reliable update
         } else {
             // ---------------- r -= alpha Ap, xs += alpha p, p = r + beta p
             const float al = st.alpha, be = st.beta;
@@ -490,6 +546,13 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
             }
         }
     }
+#ifdef YK_CG_TIMING
+    if (blockIdx.x == 0 && threadIdx.x == 0 && nit > 0)
+        printf("cluster cg timing (cycles per iteration over %d): A %lld  barriers %lld  T %lld  B %lld  "
+               "partials %lld  step %lld | reliable updates %d, %lld cycles each\n", nit, tacc[0] / nit,
+               tacc[1] / nit, tacc[2] / nit, tacc[3] / nit, tacc[4] / nit, tacc[5] / nit, st.n_ru,
+               st.n_ru ? tacc[6] / st.n_ru : 0ll);
+#endif
     // x is complete: convergence is declared only after a reliable update
     // folded the increment (or at k = 0, where x = 0 is exact)
     if (g.rank == 0 && threadIdx.x == 0) {
@@ -533,7 +596,7 @@ static size_t cluster_smem(int max_sites)
 bool cg_cluster_fits(int Nt, int Nx)
 {
     const int R = (Nt + kCC - 1) / kCC;
-    return (int64_t)R * Nx <= kCMaxSites;
+    return Nx >= 1 && (Nx & (Nx - 1)) == 0 && (int64_t)R * Nx <= kCMaxSites;
 }
 
 // Opt in to 16-CTA clusters and the shared memory of the largest case, and
