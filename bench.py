@@ -6,7 +6,7 @@ lattice, m^2 = -0.5, lambda = 1, Yukawa g = 0.5, m0 = 0.1, Wilson r = 1,
 coloured-noise cutoff Lambda = pi/2 (cutFraction = 1/(2 sqrt 2)), fixed Euler
 step dt = 0.01, one Gaussian stochastic right-hand side per step, CG on
 D^dag D to relative residual 1e-10 with FP32 iterations and FP64 reliable
-updates (each time the FP32 residual drops tenfold), FP64 field.  Synthetic data: the field starts
+updates (each time the FP32 residual drops a hundredfold), FP64 field.  Synthetic data: the field starts
 iid Uniform[-1, 1] from seed 1234 and all noise is drawn from Philox.
 
 One step = coloured noise + fermion force (CG) + drift/Euler update +
@@ -46,7 +46,7 @@ def workload(precision: str) -> dict:
     return {"workload": f"2D {NT}x{NX} Yukawa Langevin step (coloured noise + CG force + Euler), "
                         f"CG rel-res 1e-10, {precision} CG, 1 RHS, fixed dt 0.01",
             "lattice": [NT, NX], "n_rhs": 1, "precision": precision, "cg_tol_rel": 1e-10,
-            "reliable_delta": 0.1, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
+            "reliable_delta": 0.01, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
             "l2": "flushed between timed steps (256 MiB write)"}
 
 
@@ -54,7 +54,7 @@ def make_params(yk, precision, seed=1234, Nt=NT, Nx=NX):
     return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=0.1,
                              wilson_param=1.0, cut_fraction=CUT, Nt=Nt, Nx=Nx, fixed_dt=0.01,
                              precision=yk.YK_MIXED if precision == "mixed" else yk.YK_FP64,
-                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=0, reliable_delta=0.1,
+                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=0, reliable_delta=0.01,
                              n_rhs=1, seed=seed, init=yk.YK_INIT_PHILOX)
 
 

@@ -227,7 +227,7 @@ def test_langevin_steps_match_oracle(ylib, cuda, Nt, Nx, s, fixed_dt):
 
 @pytest.mark.parametrize("cluster", ["1", "0"], ids=["cluster_cg", "grid_cg"])
 def test_langevin_mixed_precision_step(ylib, cuda, monkeypatch, cluster):
-    # the cluster-resident CG (default for lattices that fit a 16-CTA cluster)
+    # the cluster-resident CG (lattices that fit a 16-CTA cluster, opt-in)
     # and the grid-wide CG kernel
     monkeypatch.setenv("YK_CG_CLUSTER", cluster)
     yk = ylib

@@ -116,15 +116,15 @@ struct yk_ctx {
     int max_nx = 1, max_cols = 1;
     // solver settings (shared by all chains of a context)
     int precision = YK_FP64, tol_mode = YK_TOL_ABS, max_iter = 1000, reliable_every = 0;
-    double reliable_delta = 0.1;
+    double reliable_delta = 0.01;
     double tol = 1e-8;
     // step graph
     cudaGraphExec_t gexec = nullptr;
     bool graph_failed = false;
     int cg_grid = 0;
-    // mixed precision with every step system fitting one 16-CTA cluster: the
-    // cluster-resident CG (YK_CG_CLUSTER=0 in the environment selects the
-    // grid-wide kernel instead)
+    // mixed precision with every step system fitting one 16-CTA cluster and
+    // YK_CG_CLUSTER=1 in the environment: the cluster-resident CG instead of
+    // the grid-wide kernel
     bool cg_cluster = false;
     int cluster_sites = 0;   // largest per-CTA share of the step systems
     // profiling: CUDA events around each kernel class of the step
@@ -548,8 +548,9 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     cg_max_grid(2, true);
     noise_init_attributes();
     {
+        // opt-in while its FP64 reliable updates run on 16 SMs only
         const char* env = getenv("YK_CG_CLUSTER");
-        bool want = mixed && !(env && env[0] == '0');
+        bool want = mixed && env && env[0] == '1';
         int sites = 0;
         for (int c = 0; c < n_chains && want; ++c) {
             const yk_params& q = params[c];

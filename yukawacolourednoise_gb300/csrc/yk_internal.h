@@ -164,10 +164,13 @@ struct NoiseTables {
     int nwhite;
 };
 
-// Columns per block of the column pass: the strip holds <= kMaxFFT complex.
+// Columns per block of the column pass: enough that the block's threads all
+// hold a butterfly (2 kBlock / Nt), so the FP64 transforms -- issued at 1/64
+// of the FP32 rate on GB300 -- spread over as many SMs as there are column
+// pairs (a 256 x 256 lattice: 128 blocks).
 YK_HD inline int noise_strip(int Nt)
 {
-    int cw = kMaxFFT / Nt;
+    int cw = 2 * kBlock / Nt;
     if (cw > 64) cw = 64;
     if (cw < 1) cw = 1;
     return cw;
