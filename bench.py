@@ -38,8 +38,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Langevin steps/sec @CG rel-res 1e-10, learned+mixed vs plain FP64 CG; Dirac HBM GB/s"
 NT = NX = 256
 CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (sqrt(2) pi)
-BYTES_CG_ITER_MIXED = 224          # unique bytes per site per FP32 CG iteration
-BYTES_CG_ITER_FP64 = 432
+BYTES_CG_ITER_MIXED = 200          # unique bytes per site per FP32 CG iteration (passes A and B)
+BYTES_CG_ITER_FP64 = 400
 
 
 def workload(precision: str) -> dict:
