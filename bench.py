@@ -118,6 +118,21 @@ def ncu_traffic():
     return None
 
 
+def max_over_ranks(t_sec: float, dist, device) -> float:
+    """The job's time: the slowest rank's timed region (all ranks call this)."""
+    if dist is None:
+        return t_sec
+    import torch
+    t = torch.tensor([t_sec], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(steps: int, ws: int, t_all: float) -> float:
+    """Whole-job steps/s: every rank runs an independent replica of `steps` steps."""
+    return steps * ws / t_all
+
+
 # ---------------------------------------------------------------- our arm
 def run_ours(args, ws, rank, local):
     import torch
@@ -164,12 +179,8 @@ def run_ours(args, ws, rank, local):
         raise RuntimeError(f"step status {obs.status}")
     cg_stats = {"iterations_per_step": round(obs.cg_iterations_total / max(obs.steps, 1), 1),
                 "steps_at_iteration_cap": int(obs.noconv_steps), "iteration_cap": 20000}
-    t_all = t_sec
-    if dist is not None:
-        t = torch.tensor([t_sec], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_all = float(t.item())
-    value = args.steps * ws / t_all
+    t_all = max_over_ranks(t_sec, dist, "cuda")
+    value = job_value(args.steps, ws, t_all)
 
     extras = {}
     if rank == 0 and not args.quick:
@@ -322,9 +333,9 @@ def run_reference(args, ws, rank):
             "warmup": args.warmup, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
             "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
-            "config": workload("fp64"),
+            "config": workload(args.precision),
             "cpu_baseline": {"value": round(v, 4), "unit": "steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{n} of {args.steps} requested {NT}x{NX} Langevin steps "
+                             "sample": f"{n} of {args.steps} requested {NT}x{NX} Langevin steps in FP64 "
                                        f"(CPU restatement of the reference; the reference has no CPU path)"},
             "e2e": {"value": round(v, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
