@@ -546,7 +546,7 @@ __device__ __forceinline__ void store_state(CGState* p, const CGState& st)
 // arguments.  The system state lives in CGState (read and written only here;
 // the host reads it after the solve).
 template <bool MIXED>
-__device__ void finish_reduction(const CGArgs& a, int k, bool ru_round, int* s_active, int* s_ru, double* red,
+__device__ __noinline__ void finish_reduction(const CGArgs& a, int k, bool ru_round, int* s_active, int* s_ru, double* red,
                                  unsigned gen)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -736,6 +736,141 @@ __device__ void grid_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round
     ++gen;
 }
 
+// Sum of one system's tile partials, the same bits in every block that calls
+// it: mixed solver, every thread adds tiles t, t + blockDim, ... in
+// float-float, then a fixed butterfly in each warp and the warps' sums in warp
+// order; FP64 solver, warp 0 alone (its 1/64-rate instructions are the cost),
+// lanes adding tiles l, l + 32, ... in order, then a fixed butterfly.  The sums
+// are valid in thread 0.
+template <bool MIXED>
+__device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red, double* s)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if constexpr (MIXED) {
+        float2* red2 = reinterpret_cast<float2*>(red);
+        FF acc[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] = FF{0.f, 0.f};
+#pragma unroll 2
+        for (int i = threadIdx.x; i < ntiles; i += blockDim.x) {
+            const Partial* pp = a.partial + tile0 + i;
+            const float4 q0 = ld_sync4f(&pp->f[0]), q1 = ld_sync4f(&pp->f[2]), q2 = ld_sync4f(&pp->f[4]);
+            acc[0] = ff_add(acc[0], FF{q0.x, q0.y});
+            acc[1] = ff_add(acc[1], FF{q0.z, q0.w});
+            acc[2] = ff_add(acc[2], FF{q1.x, q1.y});
+            acc[3] = ff_add(acc[3], FF{q1.z, q1.w});
+            acc[4] = ff_add(acc[4], FF{q2.x, q2.y});
+            acc[5] = ff_add(acc[5], FF{q2.z, q2.w});
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] = ff_add(acc[c], ff_shfl_xor(acc[c], o));
+        if (lane == 0)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) red2[w * 6 + c] = make_float2(acc[c].hi, acc[c].lo);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            FF t[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) t[c] = FF{red2[c].x, red2[c].y};
+            for (int u = 1; u < nw; ++u)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) t[c] = ff_add(t[c], FF{red2[u * 6 + c].x, red2[u * 6 + c].y});
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[c] = (double)t[c].hi + (double)t[c].lo;
+        }
+    } else {
+        if (w == 0) {
+            constexpr int U = 8;
+            double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int base = lane; base < ntiles; base += 32 * U) {
+                double2 v[U][3];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    // the address is clamped into the system's tiles, so a load
+                    // issued ahead of the range test never leaves the array
+                    const int i = base + 32 * u;
+                    const int ii = i < ntiles ? i : ntiles - 1;
+                    const Partial* pp = a.partial + tile0 + ii;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const double2 t = ld_sync2(&pp->d[2 * c]);
+                        v[u][c] = (i < ntiles) ? t : make_double2(0.0, 0.0);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        acc[2 * c] += v[u][c].x;
+                        acc[2 * c + 1] += v[u][c].y;
+                    }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[c] = acc[c];
+        }
+    }
+    __syncthreads();
+}
+
+// Single-system solves: the grid barrier is an arrival counter only; every
+// block then sums the system's tile partials itself (sum_partials: the same
+// loads in the same order, so the same bits in every block) and runs the
+// scalar recurrence on its own copy of the system state.  No block finishes
+// for the others and nothing is published: the chain of the other path
+// (finisher's loads, release, the others' polls of the published words) is
+// replaced by one round of loads in every block.  Block 0 keeps the
+// host-visible CGState up to date.
+template <bool MIXED>
+__device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red, CGState& lst,
+                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&a.bar->arrive, 1u);
+        const unsigned target = gridDim.x * (gen + 1u);
+        const volatile unsigned* c = &a.bar->arrive;
+        const long long t0 = clock64();
+        while ((int)(*c - target) < 0)
+            if (wait_over(t0, a.err)) break;
+        __threadfence();
+        s_cnt[0] = 0;
+        s_cnt[1] = 0;
+    }
+    __syncthreads();
+    ++gen;
+    if (*(volatile int*)a.err) return false;
+    double s[6];
+    sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
+    if (threadIdx.x == 0) {
+        CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
+        if (lst.mode != kIdle) cv = scalar_step<MIXED>(a, k, ru_round, s, lst, s_cnt, s_cnt + 1);
+        lst.mode = cv.mode;
+        L.mode = cv.mode;
+        L.alpha_re = cv.alpha_re;
+        L.alpha_im = cv.alpha_im;
+        L.beta = cv.beta;
+        L.c_re = cv.c_re;
+        L.c_im = cv.c_im;
+        L.f_alpha_re = (float)cv.alpha_re;
+        L.f_alpha_im = (float)cv.alpha_im;
+        L.f_beta = (float)cv.beta;
+        L.f_c_re = (float)cv.c_re;
+        L.f_c_im = (float)cv.c_im;
+        *s_nact = s_cnt[0];
+        *s_anyru = s_cnt[1] != 0;
+        if (blockIdx.x == 0) store_state(a.st + a.sys_first, lst);
+    }
+    __syncthreads();
+    return true;
+}
+
 template <typename W, bool MIXED>
 __device__ __forceinline__ W diag_of(const SysDev& S, int n)
 {
@@ -907,6 +1042,9 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
     __shared__ int tslot[kMaxTilesPerBlock];
     __shared__ Deps deps;
     __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
+    __shared__ int s_cnt[2];
+    __shared__ CGState lst;   // single-system solves: this block's copy of the state
+    const bool solo = (a.sys_count == 1);
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
@@ -995,11 +1133,23 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
     }
     if (!nsync(a, ++epoch, deps)) return;
     pass_b(0);
-    grid_reduce<MIXED>(a, gen, 0, false, &s_flag, &s_active, &s_ru, red);
+    if (solo && threadIdx.x == 0) {
+        lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
+        lst.active = 1;
+        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
+        lst.mode = kStep;
+    }
+    // the reduction that ends a pass: see solo_reduce and grid_reduce
+    auto reduce = [&](int kk, bool ru) -> bool {
+        if (solo) return solo_reduce<MIXED>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt);
+        grid_reduce<MIXED>(a, gen, kk, ru, &s_flag, &s_active, &s_ru, red);
+        return true;
+    };
+    if (!reduce(0, false)) return;
 
     int k = 1;
     while (k <= a.max_iter) {   // every system retires at k = max_iter at the latest
-        if (!poll_coefs(a, sl, nsl, gen, &s_nact, &s_anyru)) return;
+        if (!solo && !poll_coefs(a, sl, nsl, gen, &s_nact, &s_anyru)) return;
         YK_TMARK(0);   // grid reduction + coefficient load
         if (s_nact == 0) break;
         const bool any_ru = MIXED && s_anyru;
@@ -1137,7 +1287,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                     for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
                     put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, f, red);
                 }
-                grid_reduce<MIXED>(a, gen, k, true, &s_flag, &s_active, &s_ru, red);
+                if (!reduce(k, true)) return;
                 continue;   // same k: the systems that updated redo A(k)
             }
         }
@@ -1145,7 +1295,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         // ---------------- B(k)
         pass_b(cur);
         YK_TMARK(3);   // pass B
-        grid_reduce<MIXED>(a, gen, k, false, &s_flag, &s_active, &s_ru, red);
+        if (!reduce(k, false)) return;
         ++k;
 #ifdef YK_CG_TIMING
         ++tit;
