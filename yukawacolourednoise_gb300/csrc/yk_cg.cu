@@ -955,13 +955,17 @@ __device__ __forceinline__ Site<W, K> p_next(const Site<W, K>& r, const Site<W, 
     return o;
 }
 
-// Block sums of a tile's six values -> its partial slot.  Per-site values and
-// warp sums in T (FP32 for the mixed solver), FP64 across the warps.  Values
-// listed in `skip` are known to be zero and are not reduced.
+// Sums of a tile's six values -> its partial slot.  A block processes
+// blockDim / 256 tiles at once, one per 256-thread half; each half reduces its
+// own tile (its 8 warps in warp order) and writes the slot if `write`.  Per-site
+// values and warp sums in T, FP64 across the warps.  Values listed in
+// SKIP_MASK are known to be zero and are not reduced.  Every thread of the
+// block calls this (it synchronises the block).
 template <typename T, int SKIP_MASK>
-__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, T (&v)[6], double* red)
+__device__ __forceinline__ void put_partial(const CGArgs& a, int tile, bool write, T (&v)[6], double* red)
 {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int hw = kTile / 32;   // warps per tile
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -974,10 +978,11 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, T (&v)[6]
     __syncthreads();
     // one thread per value adds the warps' sums in warp order (few FP64
     // instructions: GB300 issues them at 1/64 of the FP32 rate)
-    if (threadIdx.x < 6) {
-        const int i = threadIdx.x;
-        double t = red[i];
-        for (int u = 1; u < nw; ++u) t += red[u * 6 + i];
+    const int ts = threadIdx.x % kTile, w0 = (threadIdx.x / kTile) * hw;
+    if (write && ts < 6) {
+        const int i = ts;
+        double t = red[w0 * 6 + i];
+        for (int u = 1; u < hw; ++u) t += red[(w0 + u) * 6 + i];
 #ifdef YK_CG_CHECKED
         if (tile < a.tile_begin || tile >= a.tile_end) {
             if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
@@ -988,15 +993,17 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, T (&v)[6]
     }
 }
 
-// Block sums of a tile's six values -> its partial slot as float-float pairs
-// (mixed solver).  WARP_FF: the per-site values carry a low part (FP64
-// residuals of a reliable update) and the warp butterfly runs in float-float;
-// otherwise the warp sums are plain FP32 (the per-site values are FP32
-// products).  The warps' sums are added in warp order by one thread per value.
+// Sums of a tile's six values -> its partial slot as float-float pairs (mixed
+// solver), one tile per 256-thread half as in put_partial.  WARP_FF: the
+// per-site values carry a low part (FP64 residuals of a reliable update) and
+// the warp butterfly runs in float-float; otherwise the warp sums are plain
+// FP32 (the per-site values are FP32 products).  The warps' sums are added in
+// warp order by one thread per value.
 template <int SKIP_MASK, bool WARP_FF>
-__device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, FF (&v)[6], double* red)
+__device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool write, FF (&v)[6], double* red)
 {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int hw = kTile / 32;   // warps per tile
     float2* red2 = reinterpret_cast<float2*>(red);
     // level-outer: the independent chains interleave
 #pragma unroll
@@ -1014,10 +1021,11 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, FF (&v
 #pragma unroll
         for (int i = 0; i < 6; ++i) red2[w * 6 + i] = make_float2(v[i].hi, v[i].lo);
     __syncthreads();
-    if (threadIdx.x < 6) {
-        const int i = threadIdx.x;
-        FF t{red2[i].x, red2[i].y};
-        for (int u = 1; u < nw; ++u) t = ff_add(t, FF{red2[u * 6 + i].x, red2[u * 6 + i].y});
+    const int ts = threadIdx.x % kTile, w0 = (threadIdx.x / kTile) * hw;
+    if (write && ts < 6) {
+        const int i = ts;
+        FF t{red2[w0 * 6 + i].x, red2[w0 * 6 + i].y};
+        for (int u = 1; u < hw; ++u) t = ff_add(t, FF{red2[(w0 + u) * 6 + i].x, red2[(w0 + u) * 6 + i].y});
 #ifdef YK_CG_CHECKED
         if (tile < a.tile_begin || tile >= a.tile_end) {
             if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
@@ -1030,13 +1038,24 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, FF (&v
 
 }  // namespace
 
+// Threads per block of the CG kernel: two 256-site tiles at once for the real
+// path (one block per SM, so every SM holds the same work and the blocks reach
+// the barriers together), one tile for the complex path (its registers).
+template <int K>
+constexpr int cg_threads()
+{
+    return K == 1 ? 2 * kTile : kTile;
+}
+
 template <int K, bool MIXED>
-__global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
+__global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
 {
     using W = typename std::conditional<MIXED, float, double>::type;
     // the imaginary parts (slots 3 and 5) vanish on the real K = 1 path
     constexpr int kSkipIm = (K == 1) ? ((1 << 3) | (1 << 5)) : 0;
-    __shared__ double red[64];
+    constexpr int TP = cg_threads<K>() / kTile;   // tiles processed at once
+    const int hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;   // tile slot, thread in tile
+    __shared__ double red[128];
     __shared__ SysLocal sl[kMaxSysPerBlock];
     __shared__ int nsl;
     __shared__ int tslot[kMaxTilesPerBlock];
@@ -1074,13 +1093,15 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
 
     // B(k): Ap = D_second t and the partials of every system that stepped
     auto pass_b = [&](int cur) {
-        for (int tile = tb; tile < te; ++tile) {
-            const SysLocal& L = sl[tslot[tile - tb]];
-            if (L.mode == kIdle || L.mode == kRu) continue;
+        for (int base = tb; base < te; base += TP) {   // the same trip count in every thread
+            const int tile = base + hf;
+            bool on = tile < te;
+            const SysLocal& L = sl[tslot[(on ? tile : tb) - tb]];
+            on = on && L.mode != kIdle && L.mode != kRu;
             const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
+            const int n = on ? a.tiles[tile].y + ts : 0;
             W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
-            if (n < S.V) {
+            if (on && n < S.V) {
                 const Site<W, K> ap = apply_d<W, K, MIXED>(Tv(S), n, S, !first_dag);
                 YK_ST(W, K, Av(S), n, ap);
                 const Site<W, K> r = YK_LD(W, K, Rv(S, cur), n);
@@ -1094,17 +1115,17 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                 FF f[6];
 #pragma unroll
                 for (int i = 0; i < 6; ++i) f[i] = FF{v[i], 0.f};
-                put_partial_ff<kSkipIm, false>(a, tile, f, red);
+                put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
             } else {
-                put_partial<W, kSkipIm>(a, tile, v, red);
+                put_partial<W, kSkipIm>(a, tile, on, v, red);
             }
         }
     };
 
     // ---------------- round 0: b, x = 0, r_0 = p_0 = b; t = D_first p_0; B(0)
-    for (int tile = tb; tile < te; ++tile) {
+    for (int tile = tb + hf; tile < te; tile += TP) {
         const SysDev& S = a.sys[a.tiles[tile].x];
-        const int n = a.tiles[tile].y + threadIdx.x;
+        const int n = a.tiles[tile].y + ts;
         if (n >= S.V) continue;
         const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
         if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
@@ -1125,9 +1146,9 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         YK_ST(W, K, Pv(S, 0), n, bw);
     }
     if (!nsync(a, ++epoch, deps)) return;
-    for (int tile = tb; tile < te; ++tile) {
+    for (int tile = tb + hf; tile < te; tile += TP) {
         const SysDev& S = a.sys[a.tiles[tile].x];
-        const int n = a.tiles[tile].y + threadIdx.x;
+        const int n = a.tiles[tile].y + ts;
         if (n >= S.V) continue;
         YK_ST(W, K, Tv(S), n, (apply_d<W, K, MIXED>(Pv(S, 0), n, S, first_dag)));
     }
@@ -1155,12 +1176,12 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         const bool any_ru = MIXED && s_anyru;
         const int cur = k & 1, prv = cur ^ 1;
         // ---------------- A(k)
-        for (int tile = tb; tile < te; ++tile) {
+        for (int tile = tb + hf; tile < te; tile += TP) {
             const SysLocal& L = sl[tslot[tile - tb]];
             const int mode = L.mode;
             if (mode != kStep && mode != kRu && mode != kRedo) continue;
             const SysDev& S = a.sys[L.sys];
-            const int n = a.tiles[tile].y + threadIdx.x;
+            const int n = a.tiles[tile].y + ts;
             if (n >= S.V) continue;
             if constexpr (MIXED) {
                 if (mode == kRu) {
@@ -1230,11 +1251,11 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
         if constexpr (MIXED) {
             if (any_ru) {
                 // RU1: t64 = D_first x (FP64)
-                for (int tile = tb; tile < te; ++tile) {
+                for (int tile = tb + hf; tile < te; tile += TP) {
                     const SysLocal& L = sl[tslot[tile - tb]];
                     if (L.mode != kRu) continue;
                     const SysDev& S = a.sys[L.sys];
-                    const int n = a.tiles[tile].y + threadIdx.x;
+                    const int n = a.tiles[tile].y + ts;
                     if (n >= S.V) continue;
                     const Nbr nb = neighbours(n, S.Nt, S.Nx);
                     const Site<double, K> c = YK_LD(double, K, S.x, n);
@@ -1250,13 +1271,15 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                 }
                 if (!nsync(a, ++epoch, deps)) return;
                 // RU2: r = b - D_second t64 in FP64 -> R[cur]; |r|^2, <r, p_{k-1}>
-                for (int tile = tb; tile < te; ++tile) {
-                    const SysLocal& L = sl[tslot[tile - tb]];
-                    if (L.mode != kRu) continue;
+                for (int base = tb; base < te; base += TP) {   // the same trip count in every thread
+                    const int tile = base + hf;
+                    bool on = tile < te;
+                    const SysLocal& L = sl[tslot[(on ? tile : tb) - tb]];
+                    on = on && L.mode == kRu;
                     const SysDev& S = a.sys[L.sys];
-                    const int n = a.tiles[tile].y + threadIdx.x;
+                    const int n = on ? a.tiles[tile].y + ts : 0;
                     double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-                    if (n < S.V) {
+                    if (on && n < S.V) {
                         const Nbr nb = neighbours(n, S.Nt, S.Nx);
                         const Site<double, K> c = YK_LD(double, K, S.t64, n);
                         const Site<double, K> tu = YK_LD(double, K, S.t64, nb.tu);
@@ -1285,7 +1308,7 @@ __global__ void __launch_bounds__(kBlock) cg_kernel(CGArgs a)
                     FF f[6];
 #pragma unroll
                     for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
-                    put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, f, red);
+                    put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, on, f, red);
                 }
                 if (!reduce(k, true)) return;
                 continue;   // same k: the systems that updated redo A(k)
@@ -1361,7 +1384,7 @@ static int max_grid_t()
 {
     static int maxg = -1;
     if (maxg < 0) {
-        maxg = max_coresident((const void*)cg_kernel<K, MIXED>, kBlock);
+        maxg = max_coresident((const void*)cg_kernel<K, MIXED>, cg_threads<K>());
         if (const char* e = getenv("YK_CG_MAX_GRID")) {
             const int cap = atoi(e);
             if (cap > 0 && cap < maxg) maxg = cap;
@@ -1403,7 +1426,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     cg_prepare_kernel<<<1, 256, 0, stream>>>(a);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kBlock);
+    cfg.blockDim = dim3(cg_threads<K>());
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
