@@ -170,6 +170,40 @@ __device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
     return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-point sums (mixed single-system solves, real path).  Each tile adds
+// round(x * 2^e) of its four values (|r|^2, |Ap|^2, <p,Ap>, <r,Ap>) with a
+// 64-bit integer atomic: integer addition is exact and associative, so the
+// total is the same whatever order the blocks arrive in, and every block reads
+// one word per value instead of every tile's partial.  e comes from the
+// previous iteration's totals (identical in every block) with 2^12 of headroom
+// for growth and 2^-48 resolution relative to the previous total; a total
+// that comes out too large for the headroom is detected by every block alike
+// and that iteration falls back to the float-float tile partials, which are
+// always written too.
+// ---------------------------------------------------------------------------
+constexpr int kFixBits = 48;                 // resolution: 2^-48 of the previous total
+constexpr long long kFixLimit = 1ll << 61;   // a total at or above this is not trusted
+
+__device__ __forceinline__ long long to_fixed(FF t, int e)
+{
+    return __double2ll_rn(scalbn((double)t.hi + (double)t.lo, e));
+}
+
+// scale exponent for a total of magnitude m (> 0): m * 2^e ~ 2^kFixBits
+__device__ __forceinline__ int fix_scale(double m)
+{
+    int ex;
+    frexp(m, &ex);
+    return kFixBits - ex;
+}
+
+// tile slot of value c (|r|^2, |Ap|^2, <p,Ap> re, <r,Ap> re) on the real path
+__device__ __forceinline__ int fix_value_of_slot(int i)
+{
+    return i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 2 : i == 4 ? 3 : -1;
+}
+
 // Blocks holding stencil neighbours of this block's sites.
 struct Deps {
     int n;
@@ -826,12 +860,23 @@ __device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red
 // (finisher's loads, release, the others' polls of the published words) is
 // replaced by one round of loads in every block.  Block 0 keeps the
 // host-visible CGState up to date.
-template <bool MIXED>
+template <int K, bool MIXED>
 __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red, CGState& lst,
-                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt)
+                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast)
 {
+    constexpr bool kFix = MIXED && K == 1;   // fixed-point sums available
     __syncthreads();
+#ifdef YK_CG_TIMING
+    const long long q0 = clock64();
+#endif
     if (threadIdx.x == 0) {
+        if (kFix && blockIdx.x == 0) {
+            // the buffer of the barrier after this one: nobody reads it any more
+            // (its last readers arrived here already) and nobody adds to it
+            // before this block has arrived
+            long long (*z)[16] = a.bar->fsum[(gen + 2u) % 3u];
+            for (int c = 0; c < 4; ++c) z[c][0] = 0;
+        }
         __threadfence();
         atomicAdd(&a.bar->arrive, 1u);
         const unsigned target = gridDim.x * (gen + 1u);
@@ -847,7 +892,38 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
     ++gen;
     if (*(volatile int*)a.err) return false;
     double s[6];
-    sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
+#ifdef YK_CG_TIMING
+    const long long q1 = clock64();
+#endif
+    // fixed-point totals of this barrier, if the tiles added them
+    bool fast = false;
+    if constexpr (kFix) {
+        if (!ru_round && *s_fast) {
+            if (threadIdx.x == 0) {
+                const long long(*f)[16] = a.bar->fsum[gen % 3u];
+                long long S[4];
+                for (int c = 0; c < 4; ++c) S[c] = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[c][0]));
+                bool ok = true;
+                for (int c = 0; c < 4; ++c) ok = ok && S[c] < kFixLimit && S[c] > -kFixLimit;
+                if (ok) {
+                    s[0] = scalbn((double)S[0], -esc[0]);
+                    s[1] = scalbn((double)S[1], -esc[1]);
+                    s[2] = scalbn((double)S[2], -esc[2]);
+                    s[4] = scalbn((double)S[3], -esc[3]);
+                    s[3] = s[5] = 0.0;
+                }
+                s_cnt[0] = ok ? 1 : 0;
+            }
+            __syncthreads();
+            fast = s_cnt[0] != 0;
+            __syncthreads();
+            if (threadIdx.x == 0) s_cnt[0] = 0;
+        }
+    }
+    if (!fast) sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
+#ifdef YK_CG_TIMING
+    const long long q2 = clock64();
+#endif
     if (threadIdx.x == 0) {
         CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
         if (lst.mode != kIdle) cv = scalar_step<MIXED>(a, k, ru_round, s, lst, s_cnt, s_cnt + 1);
@@ -866,6 +942,30 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
         *s_nact = s_cnt[0];
         *s_anyru = s_cnt[1] != 0;
         if (blockIdx.x == 0) store_state(a.st + a.sys_first, lst);
+        if constexpr (kFix) {
+            // scales of the next iteration's sums, from these totals
+            if (ru_round) {
+                if (s[0] > 0.0 && isfinite(s[0])) esc[0] = fix_scale(s[0]);
+            } else {
+                const bool ok = s[0] > 0.0 && s[1] > 0.0 && s[2] > 0.0 && isfinite(s[0]) && isfinite(s[1]) &&
+                                isfinite(s[2]);
+                if (ok) {
+                    esc[0] = fix_scale(s[0]);
+                    esc[1] = fix_scale(s[1]);
+                    esc[2] = fix_scale(s[2]);
+                    esc[3] = fix_scale(sqrt(s[0] * s[1]));   // |<r, Ap>| <= |r| |Ap|
+                }
+                *s_fast = ok ? 1 : 0;
+            }
+        }
+#ifdef YK_CG_TIMING
+        if (blockIdx.x == 0) {
+            atomicAdd(&g_cg_f[0], (unsigned long long)(q1 - q0));
+            atomicAdd(&g_cg_f[4], (unsigned long long)(q2 - q1));
+            atomicAdd(&g_cg_f[1], (unsigned long long)(clock64() - q2));
+            atomicAdd(&g_cg_f[3], 1ull);
+        }
+#endif
     }
     __syncthreads();
     return true;
@@ -1000,7 +1100,8 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, bool writ
 // FP32 (the per-site values are FP32 products).  The warps' sums are added in
 // warp order by one thread per value.
 template <int SKIP_MASK, bool WARP_FF>
-__device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool write, FF (&v)[6], double* red)
+__device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool write, FF (&v)[6], double* red,
+                                               long long (*fsum)[16] = nullptr, const int* esc = nullptr)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int hw = kTile / 32;   // warps per tile
@@ -1033,6 +1134,10 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool w
         }
 #endif
         a.partial[tile].f[i] = make_float2(t.hi, t.lo);
+        if (fsum) {
+            const int c = fix_value_of_slot(i);
+            if (c >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(&fsum[c][0]), (unsigned long long)to_fixed(t, esc[c]));
+        }
     }
 }
 
@@ -1062,12 +1167,21 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     __shared__ Deps deps;
     __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
     __shared__ int s_cnt[2];
+    __shared__ int s_esc[4], s_fast;   // fixed-point scales and whether they hold
     __shared__ CGState lst;   // single-system solves: this block's copy of the state
     const bool solo = (a.sys_count == 1);
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
     if (*(volatile int*)a.err) return;   // the other blocks' waits see the flag and end
+    if (solo && threadIdx.x == 0) {
+        s_fast = 0;
+        lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
+        lst.active = 1;
+        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
+        lst.mode = kStep;
+    }
+    __syncthreads();
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
     unsigned epoch = 0, gen = 0;
 #ifdef YK_CG_TIMING
@@ -1115,7 +1229,10 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
                 FF f[6];
 #pragma unroll
                 for (int i = 0; i < 6; ++i) f[i] = FF{v[i], 0.f};
-                put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
+                if (K == 1 && solo && s_fast)
+                    put_partial_ff<kSkipIm, false>(a, tile, on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
+                else
+                    put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
             } else {
                 put_partial<W, kSkipIm>(a, tile, on, v, red);
             }
@@ -1154,15 +1271,9 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     }
     if (!nsync(a, ++epoch, deps)) return;
     pass_b(0);
-    if (solo && threadIdx.x == 0) {
-        lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
-        lst.active = 1;
-        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
-        lst.mode = kStep;
-    }
     // the reduction that ends a pass: see solo_reduce and grid_reduce
     auto reduce = [&](int kk, bool ru) -> bool {
-        if (solo) return solo_reduce<MIXED>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt);
+        if (solo) return solo_reduce<K, MIXED>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast);
         grid_reduce<MIXED>(a, gen, kk, ru, &s_flag, &s_active, &s_ru, red);
         return true;
     };
@@ -1362,6 +1473,8 @@ __global__ void cg_prepare_kernel(CGArgs a)
         *a.any_ru = 0;
         a.bar->arrive = 0u;
         a.bar->gword = 0ull;
+        for (int b = 0; b < 3; ++b)
+            for (int c = 0; c < 4; ++c) a.bar->fsum[b][c][0] = 0;
         *a.err = 0;
     }
 }

@@ -32,6 +32,9 @@ struct GridBarrier {
     unsigned pad0[31];
     unsigned long long gword;
     unsigned long long pad1[15];
+    // mixed-precision single-system solves: fixed-point sums of the four
+    // reduced values, three rotating buffers, each value on its own 128-byte line
+    long long fsum[3][4][16];
 };
 
 // One linear system (chain, right-hand side) of a batched CG solve.
