@@ -185,10 +185,27 @@ __device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
 constexpr int kFixBits = 48;                 // resolution: 2^-48 of the previous total
 constexpr long long kFixLimit = 1ll << 61;   // a total at or above this is not trusted
 
-__device__ __forceinline__ long long to_fixed(FF t, int e)
+// round(x * 2^e) from the bits of x: integer operations only (no FP64).
+// Magnitudes beyond the window saturate to kFixLimit, which the readers
+// reject; values below 2^-e round to zero.
+__device__ __forceinline__ long long f2fix(float x, int e)
 {
-    return __double2ll_rn(scalbn((double)t.hi + (double)t.lo, e));
+    const unsigned u = __float_as_uint(x);
+    const int ex = (int)((u >> 23) & 0xffu);
+    if (ex == 0) return 0;   // zero (subnormals are below every window used)
+    const long long m = (long long)((u & 0x7fffffu) | 0x800000u);
+    const int sh = ex - 150 + e;   // x = m * 2^(ex - 150)
+    long long v;
+    if (sh >= 0)
+        v = sh > 38 ? kFixLimit : (m << sh);
+    else if (sh > -40)
+        v = (m + (1ll << (-sh - 1))) >> (-sh);
+    else
+        v = 0;
+    return (u >> 31) ? -v : v;
 }
+
+__device__ __forceinline__ long long to_fixed(FF t, int e) { return f2fix(t.hi, e) + f2fix(t.lo, e); }
 
 // scale exponent for a total of magnitude m (> 0): m * 2^e ~ 2^kFixBits
 __device__ __forceinline__ int fix_scale(double m)
@@ -196,6 +213,13 @@ __device__ __forceinline__ int fix_scale(double m)
     int ex;
     frexp(m, &ex);
     return kFixBits - ex;
+}
+
+// the same from a fixed-point total S (> 0) at scale e: integer operations only
+__device__ __forceinline__ int fix_rescale(long long S, int e)
+{
+    const int bits = 64 - __clzll(S);   // S < 2^bits, so the total < 2^(bits - e)
+    return kFixBits - (bits - e);
 }
 
 // tile slot of value c (|r|^2, |Ap|^2, <p,Ap> re, <r,Ap> re) on the real path
@@ -897,6 +921,7 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
 #endif
     // fixed-point totals of this barrier, if the tiles added them
     bool fast = false;
+    int s_scales = 0;   // thread 0: 2 = next scales set from the integer totals
     if constexpr (kFix) {
         if (!ru_round && *s_fast) {
             if (threadIdx.x == 0) {
@@ -911,13 +936,28 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
                     s[2] = scalbn((double)S[2], -esc[2]);
                     s[4] = scalbn((double)S[3], -esc[3]);
                     s[3] = s[5] = 0.0;
+                    // next scales straight from the integer totals
+                    if (S[0] > 0 && S[1] > 0 && S[2] > 0) {
+                        const int e0 = fix_rescale(S[0], esc[0]), e1 = fix_rescale(S[1], esc[1]);
+                        esc[2] = fix_rescale(S[2], esc[2]);
+                        esc[3] = (e0 + e1) / 2 - 1;   // |<r, Ap>| <= |r| |Ap|
+                        esc[0] = e0;
+                        esc[1] = e1;
+                        s_cnt[1] = 2;   // scales already set
+                    } else {
+                        s_cnt[1] = 3;   // no usable scales: the next sums go through the tile partials
+                    }
                 }
                 s_cnt[0] = ok ? 1 : 0;
             }
             __syncthreads();
             fast = s_cnt[0] != 0;
             __syncthreads();
-            if (threadIdx.x == 0) s_cnt[0] = 0;
+            if (threadIdx.x == 0) {
+                s_cnt[0] = 0;
+                s_scales = s_cnt[1];
+                s_cnt[1] = 0;
+            }
         }
     }
     if (!fast) sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
@@ -944,7 +984,9 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
         if (blockIdx.x == 0) store_state(a.st + a.sys_first, lst);
         if constexpr (kFix) {
             // scales of the next iteration's sums, from these totals
-            if (ru_round) {
+            if (fast) {
+                *s_fast = s_scales == 2 ? 1 : 0;
+            } else if (ru_round) {
                 if (s[0] > 0.0 && isfinite(s[0])) esc[0] = fix_scale(s[0]);
             } else {
                 const bool ok = s[0] > 0.0 && s[1] > 0.0 && s[2] > 0.0 && isfinite(s[0]) && isfinite(s[1]) &&
