@@ -6,7 +6,8 @@ lattice, m^2 = -0.5, lambda = 1, Yukawa g = 0.5, m0 = 0.1, Wilson r = 1,
 coloured-noise cutoff Lambda = pi/2 (cutFraction = 1/(2 sqrt 2)), fixed Euler
 step dt = 0.01, one Gaussian stochastic right-hand side per step, CG on
 D^dag D to relative residual 1e-10 with FP32 iterations and FP64 reliable
-updates (each time the FP32 residual drops a hundredfold), FP64 field.  Synthetic data: the field starts
+updates (every 50 iterations, and each time the FP32 residual drops a
+hundredfold), FP64 field.  Synthetic data: the field starts
 iid Uniform[-1, 1] from seed 1234 and all noise is drawn from Philox.
 
 One step = coloured noise + fermion force (CG) + drift/Euler update +
@@ -46,7 +47,7 @@ def workload(precision: str) -> dict:
     return {"workload": f"2D {NT}x{NX} Yukawa Langevin step (coloured noise + CG force + Euler), "
                         f"CG rel-res 1e-10, {precision} CG, 1 RHS, fixed dt 0.01",
             "lattice": [NT, NX], "n_rhs": 1, "precision": precision, "cg_tol_rel": 1e-10,
-            "reliable_delta": 0.01, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
+            "reliable_every": 50, "reliable_delta": 0.01, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
             "l2": "flushed between timed steps (256 MiB write)"}
 
 
@@ -54,7 +55,7 @@ def make_params(yk, precision, seed=1234, Nt=NT, Nx=NX):
     return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=0.1,
                              wilson_param=1.0, cut_fraction=CUT, Nt=Nt, Nx=Nx, fixed_dt=0.01,
                              precision=yk.YK_MIXED if precision == "mixed" else yk.YK_FP64,
-                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=0, reliable_delta=0.01,
+                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=50, reliable_delta=0.01,
                              n_rhs=1, seed=seed, init=yk.YK_INIT_PHILOX)
 
 
@@ -248,6 +249,8 @@ def run_ours(args, ws, rank, local):
 
         # Dirac apply HBM bandwidth on a lattice larger than L2 (complex buffers)
         extras["dirac_hbm"] = dirac_hbm(yk, torch, stream)
+        # the batching configuration (many chains of uneven sizes in one graph)
+        extras["batching"] = batched(yk, torch, stream)
         extras["gpu_launches"] = int(round(launches_per_step * args.steps))
 
     ctx.close()
@@ -266,6 +269,40 @@ def run_ours(args, ws, rank, local):
     if not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     return line
+
+
+def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
+    """The batching configuration: 64 chains of seeded sizes {32, 64, 128, 256}^2,
+    m0 ~ U[0.05, 0.3], g ~ U[0.3, 0.8], 4 stochastic right-hand sides per chain,
+    mixed CG at rel-res 1e-10, every chain stepped by one graph replay."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    Ls = rng.choice([32, 64, 128, 256], size=n_chains)
+    m0s = rng.uniform(0.05, 0.3, size=n_chains)
+    gs = rng.uniform(0.3, 0.8, size=n_chains)
+    ps = [yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=float(g), fermion_mass=float(m0),
+                            wilson_param=1.0, cut_fraction=CUT, Nt=int(L), Nx=int(L), fixed_dt=0.01,
+                            precision=yk.YK_MIXED, cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000,
+                            reliable_every=50, reliable_delta=0.01, n_rhs=4, seed=seed, init=yk.YK_INIT_PHILOX)
+          for L, m0, g in zip(Ls, m0s, gs)]
+    ctx = yk.Context(ps)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.step(warmup)
+    ctx.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        ctx.step(steps)
+        b.record(stream)
+    stream.synchronize()
+    sec = a.elapsed_time(b) / 1e3
+    obs = [ctx.observables(c) for c in range(n_chains)]
+    ctx.close()
+    sites = int(sum(int(L) * int(L) for L in Ls))
+    return {"config": f"{n_chains} chains, L in {{32,64,128,256}} (seed {seed}), 4 RHS, mixed CG rel-res 1e-10",
+            "value": round(steps * n_chains / sec, 2), "unit": "chain-steps/s",
+            "site_steps_per_s": round(steps * sites / sec, 1), "steps": steps,
+            "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
 
 
 def dirac_hbm(yk, torch, stream, Nt=4096, Nx=4096, reps=20):
