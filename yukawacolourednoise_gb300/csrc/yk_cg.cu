@@ -32,6 +32,7 @@
 // 256-site tiles and wait only for the blocks that hold their stencil
 // neighbours.  Every wait is bounded (about 2 s): a block that gives up sets
 // YK_ETIMEOUT and every block leaves.
+#include <cfloat>
 #include <cstdio>
 #include <cstdlib>
 #include <type_traits>
@@ -221,6 +222,45 @@ __device__ __forceinline__ int fix_rescale(long long S, int e)
     const int bits = 64 - __clzll(S);   // S < 2^bits, so the total < 2^(bits - e)
     return kFixBits - (bits - e);
 }
+
+// 2^k as a float, k in [-126, 127]
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
+// S * 2^-e as a float-float pair, from the integer's bits: the top 24 bits
+// give hi exactly, the bits below give lo (truncated to about 24 bits).  No
+// FP64 and no 64-bit conversions.  False when the value lies outside
+// [2^-80, 2^100), where the caller takes the FP64 route instead.
+__device__ __forceinline__ bool fix_to_ff(long long S, int e, FF& out)
+{
+    if (S == 0) {
+        out = FF{0.f, 0.f};
+        return true;
+    }
+    const unsigned long long u = S < 0 ? 0ull - (unsigned long long)S : (unsigned long long)S;
+    const int b = 63 - __clzll((long long)u);   // u in [2^b, 2^(b+1)); |S| < 2^61
+    if (b - e < -80 || b - e >= 100) return false;
+    const int sh = b > 23 ? b - 23 : 0;              // bits below the top 24
+    const unsigned top = (unsigned)(u >> sh);         // < 2^24
+    const unsigned long long rest = u - ((unsigned long long)top << sh);   // < 2^sh, sh <= 37
+    const float scale = pow2f(sh - e);                // sh - e in [-103, 100]
+    const float hi = (float)top * scale;
+    const float lo_m = fmaf((float)(unsigned)(rest >> 20), 1048576.f, (float)(unsigned)(rest & 0xfffffu));
+    const float lo = lo_m * pow2f(-sh) * scale;
+    out = S < 0 ? FF{-hi, -lo} : FF{hi, lo};
+    return true;
+}
+
+// float-float times float (Dekker's product through the FMA, then a fast two-sum)
+__device__ __forceinline__ FF ff_mul(FF a, float b)
+{
+    const float p = a.hi * b;
+    float err = fmaf(a.hi, b, -p);
+    err = fmaf(a.lo, b, err);
+    const float s = p + err;
+    return FF{s, err - (s - p)};
+}
+
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
 
 // tile slot of value c (|r|^2, |Ap|^2, <p,Ap> re, <r,Ap> re) on the real path
 __device__ __forceinline__ int fix_value_of_slot(int i)
@@ -559,6 +599,72 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
     return cv;
 }
 
+// FP32 copies of the state fields the mixed single-system fast step reads and
+// writes (rmax2, rr_prev) or compares against (stop2, delta^2).  `valid` says
+// the copies are the current values; the FP64 fields of CGState are brought
+// up to date from them whenever the FP64 step takes over.
+struct FastShadow {
+    float rr_prev, rmax2, stop2, d2;
+    int valid;
+};
+
+// One step of the mixed single-system recurrence from the four fixed-point
+// totals (|r|^2, |Ap|^2, <p, Ap>, <r, Ap> at scales esc), on the FP32 pipes:
+// the scalar work runs in one thread per block on the critical path, where
+// every FP64 instruction would cost tens of cycles.  alpha and beta are FP32
+// as in scalar_step<true>; |r_{k+1}|^2 = |r|^2 - alpha (2 <r, Ap> - alpha |Ap|^2)
+// is formed in float-float because its terms cancel.  Returns false without
+// changing anything when the ordinary case does not hold (first iteration,
+// iteration cap, values out of the float-float window, a non-positive
+// curvature or a non-finite alpha); the caller then takes the FP64 step.
+__device__ bool fast_step(const CGArgs& a, int k, const long long (&S)[4], const int* esc, CGState& st,
+                          FastShadow& fs, SysLocal& L)
+{
+    if (k == 0 || k >= a.max_iter) return false;
+    FF rr, apap, pap, rap;
+    if (!fix_to_ff(S[0], esc[0], rr) || !fix_to_ff(S[1], esc[1], apap) || !fix_to_ff(S[2], esc[2], pap) ||
+        !fix_to_ff(S[3], esc[3], rap))
+        return false;
+    const float rrf = rr.hi + rr.lo, papf = pap.hi + pap.lo;
+    if (!(rrf > 0.f) || !(papf > 0.f)) return false;
+    const float alpha = rrf / papf;   // CGsolver.cu:137
+    if (!isfinite(alpha)) return false;
+    if (!fs.valid) {
+        fs.rmax2 = (float)st.rmax2;
+        fs.stop2 = fmaxf((float)st.stop2, FLT_MIN);
+        fs.d2 = (float)(a.reliable_delta * a.reliable_delta);
+        fs.valid = 1;
+    }
+    const FF w = ff_mul(ff_add(FF{2.f * rap.hi, 2.f * rap.lo}, ff_neg(ff_mul(apap, alpha))), alpha);
+    const FF e = ff_add(rr, ff_neg(w));
+    float est = e.hi + e.lo;
+    if (!(est > 0.f)) est = 0.f;
+    fs.rmax2 = fmaxf(fs.rmax2, rrf);
+    fs.rr_prev = rrf;
+    st.iters = k;
+    const bool cand = !(rrf > fs.stop2) || !(est > fs.stop2);
+    const bool drop = est < fs.d2 * fs.rmax2;
+    const bool due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
+    const bool cap = k + 1 >= a.max_iter;
+    int mode = kStep;
+    if (cand || drop || due || cap) {
+        // the reliable update that follows runs the FP64 step: hand it the state
+        mode = kRu;
+        st.rr = (double)rrf;
+        st.rr_prev = st.rr;
+        st.rmax2 = (double)fs.rmax2;
+        fs.valid = 0;
+        L.alpha_re = (double)alpha;   // the FP64 fold of x uses the FP64 copy
+        L.alpha_im = 0.0;
+    }
+    st.mode = mode;
+    L.mode = mode;
+    L.f_alpha_re = alpha;
+    L.f_alpha_im = 0.f;
+    L.f_beta = est / rrf;
+    return true;
+}
+
 __device__ __forceinline__ void load_state(const CGState* p, CGState& st)
 {
     const volatile CGState& v = *p;
@@ -886,7 +992,7 @@ __device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red
 // host-visible CGState up to date.
 template <int K, bool MIXED>
 __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red, CGState& lst,
-                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast)
+                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast, FastShadow& fs)
 {
     constexpr bool kFix = MIXED && K == 1;   // fixed-point sums available
     __syncthreads();
@@ -920,7 +1026,7 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
     const long long q1 = clock64();
 #endif
     // fixed-point totals of this barrier, if the tiles added them
-    bool fast = false;
+    bool fast = false, stepped = false;
     int s_scales = 0;   // thread 0: 2 = next scales set from the integer totals
     if constexpr (kFix) {
         if (!ru_round && *s_fast) {
@@ -930,12 +1036,17 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
                 for (int c = 0; c < 4; ++c) S[c] = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[c][0]));
                 bool ok = true;
                 for (int c = 0; c < 4; ++c) ok = ok && S[c] < kFixLimit && S[c] > -kFixLimit;
+                bool done = false;
                 if (ok) {
-                    s[0] = scalbn((double)S[0], -esc[0]);
-                    s[1] = scalbn((double)S[1], -esc[1]);
-                    s[2] = scalbn((double)S[2], -esc[2]);
-                    s[4] = scalbn((double)S[3], -esc[3]);
-                    s[3] = s[5] = 0.0;
+                    // the ordinary step on the FP32 pipes; the FP64 one otherwise
+                    done = lst.mode != kIdle && fast_step(a, k, S, esc, lst, fs, L);
+                    if (!done) {
+                        s[0] = scalbn((double)S[0], -esc[0]);
+                        s[1] = scalbn((double)S[1], -esc[1]);
+                        s[2] = scalbn((double)S[2], -esc[2]);
+                        s[4] = scalbn((double)S[3], -esc[3]);
+                        s[3] = s[5] = 0.0;
+                    }
                     // next scales straight from the integer totals
                     if (S[0] > 0 && S[1] > 0 && S[2] > 0) {
                         const int e0 = fix_rescale(S[0], esc[0]), e1 = fix_rescale(S[1], esc[1]);
@@ -948,10 +1059,11 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
                         s_cnt[1] = 3;   // no usable scales: the next sums go through the tile partials
                     }
                 }
-                s_cnt[0] = ok ? 1 : 0;
+                s_cnt[0] = ok ? (done ? 2 : 1) : 0;
             }
             __syncthreads();
             fast = s_cnt[0] != 0;
+            stepped = s_cnt[0] == 2;
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_cnt[0] = 0;
@@ -964,7 +1076,18 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
 #ifdef YK_CG_TIMING
     const long long q2 = clock64();
 #endif
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && stepped) {
+        *s_nact = 1;
+        *s_anyru = lst.mode == kRu;
+        if (blockIdx.x == 0) store_state(a.st + a.sys_first, lst);
+        *s_fast = s_scales == 2 ? 1 : 0;
+    } else if (threadIdx.x == 0) {
+        if (fs.valid) {
+            // the FP64 step continues from the fast steps' FP32 state
+            lst.rr_prev = (double)fs.rr_prev;
+            lst.rmax2 = (double)fs.rmax2;
+            fs.valid = 0;
+        }
         CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
         if (lst.mode != kIdle) cv = scalar_step<MIXED>(a, k, ru_round, s, lst, s_cnt, s_cnt + 1);
         lst.mode = cv.mode;
@@ -1000,15 +1123,15 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
                 *s_fast = ok ? 1 : 0;
             }
         }
-#ifdef YK_CG_TIMING
-        if (blockIdx.x == 0) {
-            atomicAdd(&g_cg_f[0], (unsigned long long)(q1 - q0));
-            atomicAdd(&g_cg_f[4], (unsigned long long)(q2 - q1));
-            atomicAdd(&g_cg_f[1], (unsigned long long)(clock64() - q2));
-            atomicAdd(&g_cg_f[3], 1ull);
-        }
-#endif
     }
+#ifdef YK_CG_TIMING
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        atomicAdd(&g_cg_f[0], (unsigned long long)(q1 - q0));
+        atomicAdd(&g_cg_f[4], (unsigned long long)(q2 - q1));
+        atomicAdd(&g_cg_f[1], (unsigned long long)(clock64() - q2));
+        atomicAdd(&g_cg_f[3], 1ull);
+    }
+#endif
     __syncthreads();
     return true;
 }
@@ -1211,6 +1334,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     __shared__ int s_cnt[2];
     __shared__ int s_esc[4], s_fast;   // fixed-point scales and whether they hold
     __shared__ CGState lst;   // single-system solves: this block's copy of the state
+    __shared__ FastShadow fsh;   // and its FP32 copies for the fast step
     const bool solo = (a.sys_count == 1);
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
@@ -1222,6 +1346,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
         lst.active = 1;
         lst.iters = lst.converged = lst.status = lst.n_ru = 0;
         lst.mode = kStep;
+        fsh.valid = 0;
     }
     __syncthreads();
     const bool first_dag = (a.mtype == YK_NORMAL);   // Normal: A = D D^dag, apply D^dag first
@@ -1315,7 +1440,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     pass_b(0);
     // the reduction that ends a pass: see solo_reduce and grid_reduce
     auto reduce = [&](int kk, bool ru) -> bool {
-        if (solo) return solo_reduce<K, MIXED>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast);
+        if (solo) return solo_reduce<K, MIXED>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh);
         grid_reduce<MIXED>(a, gen, kk, ru, &s_flag, &s_active, &s_ru, red);
         return true;
     };
