@@ -39,7 +39,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Langevin steps/sec @CG rel-res 1e-10, learned+mixed vs plain FP64 CG; Dirac HBM GB/s"
 NT = NX = 256
 CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (sqrt(2) pi)
-BYTES_CG_ITER_MIXED = 200          # unique bytes per site per FP32 CG iteration (passes A and B)
+BYTES_CG_ITER_MIXED = 200          # unique bytes per site per FP32 CG iteration of cg_kernel (passes A and B)
+BYTES_CG_ITER_HALO = 128           # the same for cg_halo_kernel: D p stays in shared memory, diag is cached
 BYTES_CG_ITER_FP64 = 400
 
 
@@ -191,15 +192,17 @@ def run_ours(args, ws, rank, local):
             ctx.step(args.profile_steps)
         pr = ctx.profile_end()
         per_launch_ms = pr.cg_ms / max(pr.cg_launches, 1)
-        bpi = BYTES_CG_ITER_MIXED if args.precision == "mixed" else BYTES_CG_ITER_FP64
+        halo = pr.cg_kernel == 1
+        bpi = (BYTES_CG_ITER_HALO if halo else BYTES_CG_ITER_MIXED) if args.precision == "mixed" else BYTES_CG_ITER_FP64
+        kname = "cg_halo_kernel" if halo else f"cg_kernel<1,{'mixed' if args.precision == 'mixed' else 'fp64'}>"
         alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
         pk = peaks()
         achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
         tr = ncu_traffic()
         traffic = None
-        if tr and tr.get("precision") == args.precision:
+        if tr and tr.get("precision") == args.precision and tr.get("kernel", "cg_kernel<1,mixed>") == kname:
             traffic = tr["dram_bytes_per_iteration"] * pr.cg_iterations / max(pr.cg_launches, 1)
-        extras["roofline"] = {"bound": "hbm", "kernel": f"cg_kernel<1,{'mixed' if args.precision == 'mixed' else 'fp64'}>",
+        extras["roofline"] = {"bound": "hbm", "kernel": kname,
                               "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                               "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
                               "peak_source": pk["source"],

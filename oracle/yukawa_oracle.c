@@ -122,14 +122,32 @@ void yko_dirac(int Nt, int Nx, const yko_action* a, const double* sigma,
 /* ------------------------------------------------------------------------- */
 static void cdot(int64_t n, const double* a, const double* b, double* re, double* im)
 {
-    /* sum conj(a_i) b_i over n complex */
-    double sr = 0.0, si = 0.0;
-#pragma omp parallel for reduction(+ : sr, si) schedule(static)
-    for (int64_t i = 0; i < n; ++i) {
-        const double ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
-        sr += ar * br + ai * bi;
-        si += ar * bi - ai * br;
+    /* sum conj(a_i) b_i over n complex: chunks of kDotChunk entries summed in
+       order (in parallel over chunks), then the chunk sums in order, so the
+       result depends neither on the thread count nor on the threads' timing
+       (an OpenMP reduction clause combines the threads' sums in any order) */
+    enum { kDotChunk = 4096, kDotStack = 64 };
+    const int64_t nc = (n + kDotChunk - 1) / kDotChunk;
+    double stack_part[2 * kDotStack];
+    double* part = nc <= kDotStack ? stack_part : (double*)malloc(sizeof(double) * 2 * (size_t)nc);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nc; ++c) {
+        const int64_t e = (c + 1) * kDotChunk < n ? (c + 1) * kDotChunk : n;
+        double sr = 0.0, si = 0.0;
+        for (int64_t i = c * kDotChunk; i < e; ++i) {
+            const double ar = a[2 * i], ai = a[2 * i + 1], br = b[2 * i], bi = b[2 * i + 1];
+            sr += ar * br + ai * bi;
+            si += ar * bi - ai * br;
+        }
+        part[2 * c] = sr;
+        part[2 * c + 1] = si;
     }
+    double sr = 0.0, si = 0.0;
+    for (int64_t c = 0; c < nc; ++c) {
+        sr += part[2 * c];
+        si += part[2 * c + 1];
+    }
+    if (part != stack_part) free(part);
     *re = sr;
     *im = si;
 }

@@ -242,6 +242,46 @@ def test_langevin_mixed_precision_step(ylib, cuda, monkeypatch, cluster):
         assert ctx.observables().status == 0
 
 
+def _mixed_run(yk, monkeypatch, halo, Nt, Nx, steps):
+    monkeypatch.setenv("YK_CG_HALO", halo)
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    with yk.Context(p) as ctx:
+        ctx.profile_begin()
+        ctx.step(steps)
+        pr = ctx.profile_end()
+        return ctx.get_field(), pr.cg_kernel, pr.cg_iterations, ctx.observables().status
+
+
+@pytest.mark.parametrize("Nt,Nx", [(32, 32), (128, 64), (256, 256), (1024, 64), (40, 24)])
+def test_halo_cg_matches_grid_cg(ylib, cuda, monkeypatch, Nt, Nx):
+    # the halo CG kernel (single-system mixed solves whose halo slices fit)
+    # against cg_kernel on the same trajectory: the same per-site arithmetic,
+    # tile partials and fixed-point sums, so the same iterates
+    yk = ylib
+    f_halo, k_halo, it_halo, st_halo = _mixed_run(yk, monkeypatch, "1", Nt, Nx, 3)
+    f_grid, k_grid, it_grid, st_grid = _mixed_run(yk, monkeypatch, "0", Nt, Nx, 3)
+    assert (k_halo, k_grid) == (1, 0)
+    assert st_halo == 0 and st_grid == 0
+    assert it_halo == it_grid
+    assert np.array_equal(f_halo, f_grid)
+
+
+def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
+    # one Langevin step through the halo kernel against the FP64 oracle
+    monkeypatch.setenv("YK_CG_HALO", "1")
+    yk = ylib
+    Nt, Nx = 48, 32
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        ctx.profile_begin()
+        ctx.step(1)
+        assert ctx.profile_end().cg_kernel == 1
+        want, _ = O.langevin_step(Nt, Nx, act(p), phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+        assert np.abs(ctx.get_field() - want).max() < 1e-8
+        assert ctx.observables().status == 0
+
+
 def test_batched_chains_equal_single_chains(ylib, cuda):
     yk = ylib
     specs = [(16, 16, 0.1, 0.5, S_HALF_PI), (32, 8, 0.25, 0.3, 0.2), (8, 8, 0.05, 0.8, 1.0)]

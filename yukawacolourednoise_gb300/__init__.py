@@ -108,6 +108,7 @@ class Obs(C.Structure):
 
 class Profile(C.Structure):
     _fields_ = [("steps", C.c_int), ("launches", C.c_int), ("cg_launches", C.c_int), ("cg_grid", C.c_int),
+                ("cg_kernel", C.c_int),
                 ("noise_ms", C.c_double), ("cg_ms", C.c_double), ("force_ms", C.c_double),
                 ("update_ms", C.c_double), ("cg_iterations", C.c_int64), ("cg_site_iterations", C.c_int64),
                 ("sites", C.c_int64)]

@@ -122,11 +122,15 @@ struct yk_ctx {
     cudaGraphExec_t gexec = nullptr;
     bool graph_failed = false;
     int cg_grid = 0;
+    int cg_kernel = 0;   // kernel of the last step CG launch (yk_profile.cg_kernel)
     // mixed precision with every step system fitting one 16-CTA cluster and
     // YK_CG_CLUSTER=1 in the environment: the cluster-resident CG instead of
     // the grid-wide kernel
     bool cg_cluster = false;
     int cluster_sites = 0;   // largest per-CTA share of the step systems
+    // single-system mixed solves may take the halo CG kernel (YK_CG_HALO=0 in
+    // the environment at context creation: never)
+    bool cg_halo = true;
     // profiling: CUDA events around each kernel class of the step
     bool profiling = false;
     struct Rec {
@@ -284,12 +288,19 @@ int enqueue_step(yk_ctx* ctx)
         a.st = ctx->d_state;
         a.partial = ctx->d_partial;
         a.coef = ctx->d_coef;
+        if (ctx->nsys == 1 && ctx->cg_halo)
+            for (const Chain& C : ctx->ch)
+                if (C.n_rhs_step > 0) {
+                    a.solo_nt = C.Nt;
+                    a.solo_nx = C.Nx;
+                }
         if (ctx->cg_cluster) {
             YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles, ctx->n_sys_tiles, 2, ctx->stream));
             YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
             ctx->cg_grid = 16 * ctx->nsys;
+            ctx->cg_kernel = 2;
         } else {
-            YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid));
+            YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid, &ctx->cg_kernel));
         }
         prof_end(ctx, 1, e, 2);
     }
@@ -467,6 +478,10 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
     a.st = ctx->d_state;
     a.partial = ctx->d_partial;
     a.coef = ctx->d_coef;
+    if (C.n_rhs_step == 1 && ctx->cg_halo) {
+        a.solo_nt = C.Nt;
+        a.solo_nx = C.Nx;
+    }
     if (ctx->cg_cluster) {
         YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles + C.cg_tile0, C.cg_tile1 - C.cg_tile0, kind, ctx->stream));
         YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
@@ -546,6 +561,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     cg_max_grid(1, mixed);
     cg_max_grid(2, false);
     cg_max_grid(2, true);
+    if (mixed) cg_halo_init();
     noise_init_attributes();
     {
         // opt-in while its FP64 reliable updates run on 16 SMs only
@@ -561,6 +577,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         }
         ctx->cg_cluster = want && cg_cluster_init();
         ctx->cluster_sites = sites;
+        const char* he = getenv("YK_CG_HALO");
+        ctx->cg_halo = !(he && he[0] == '0');
     }
 
     ctx->ch.resize(n_chains);
@@ -1015,7 +1033,11 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
         cudaGraph_t g = nullptr;
         bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
         if (ok) {
+            // the graph holds no profiling events (profiled steps run uncaptured)
+            const bool profiling = ctx->profiling;
+            ctx->profiling = false;
             const int rc = enqueue_step(ctx);
+            ctx->profiling = profiling;
             const bool end_ok = cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess;
             ok = (rc == YK_OK) && end_ok && g;
             if (ok) ok = cudaGraphInstantiate(&ctx->gexec, g, 0) == cudaSuccess;
@@ -1101,6 +1123,7 @@ int yk_profile_end(yk_ctx* ctx, yk_profile* out)
         out->sites += (int64_t)ctx->ch[c].V;
     }
     out->cg_grid = ctx->cg_grid;
+    out->cg_kernel = ctx->cg_kernel;
     ctx->profiling = false;
     return YK_OK;
 }

@@ -285,17 +285,21 @@ __device__ __forceinline__ bool wait_over(long long t0, int* err)
     return *(volatile int*)err != 0;
 }
 
-__device__ __forceinline__ void wait_flag(const unsigned* f, unsigned epoch, int* err)
+// True when the wait gave up (timed out, or another block failed).
+__device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned epoch, int* err)
 {
     const volatile unsigned* q = f;
     const long long t0 = clock64();
     while ((int)(*q - epoch) < 0)
-        if (wait_over(t0, err)) return;
+        if (wait_over(t0, err)) return true;
+    return false;
 }
 
 // Neighbour synchronisation: publish this block's epoch, wait until every
 // block in `d` has published it too.  Release: bar.sync + thread 0's fence;
-// acquire: each waiting thread's fence + bar.sync.
+// acquire: each waiting thread's fence + bar.sync.  False when a wait gave
+// up (the final barrier ORs the waiters' outcomes: no global read of the
+// error flag on the way out).
 __device__ bool nsync(const CGArgs& a, unsigned epoch, const Deps& d)
 {
     __syncthreads();
@@ -303,16 +307,16 @@ __device__ bool nsync(const CGArgs& a, unsigned epoch, const Deps& d)
         __threadfence();
         *(volatile unsigned*)(a.flags + (size_t)blockIdx.x * kFlagStride) = epoch;
     }
+    int bad = 0;
     if (d.all) {
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            if (b != (int)blockIdx.x) wait_flag(a.flags + (size_t)b * kFlagStride, epoch, a.err);
+        for (int b = threadIdx.x; b < (int)gridDim.x && !bad; b += blockDim.x)
+            if (b != (int)blockIdx.x) bad = wait_flag(a.flags + (size_t)b * kFlagStride, epoch, a.err);
         __threadfence();
     } else if ((int)threadIdx.x < d.n) {
-        wait_flag(a.flags + (size_t)d.b[threadIdx.x] * kFlagStride, epoch, a.err);
+        bad = wait_flag(a.flags + (size_t)d.b[threadIdx.x] * kFlagStride, epoch, a.err);
         __threadfence();
     }
-    __syncthreads();
-    return *(volatile int*)a.err == 0;
+    return __syncthreads_or(bad) == 0;
 }
 
 // The block's system table and neighbour blocks, from its tile range [tb, te).
@@ -485,9 +489,12 @@ __device__ bool poll_coef(const CGCoef* c, unsigned gen, CoefVals& v, int* err)
 // grid word (bounded waits), then copies the coefficients into its table.
 __device__ bool poll_coefs(const CGArgs& a, SysLocal* sl, int nsl, unsigned gen, int* s_nact, int* s_anyru)
 {
+    int bad = 0;
     for (int j = threadIdx.x; j < nsl; j += blockDim.x) {
         CoefVals v;
-        if (poll_coef(a.coef + sl[j].sys, gen, v, a.err)) {
+        if (!poll_coef(a.coef + sl[j].sys, gen, v, a.err)) {
+            bad = 1;
+        } else {
             sl[j].mode = v.mode;
             sl[j].alpha_re = v.alpha_re;
             sl[j].alpha_im = v.alpha_im;
@@ -506,13 +513,15 @@ __device__ bool poll_coefs(const CGArgs& a, SysLocal* sl, int nsl, unsigned gen,
         const long long t0 = clock64();
         unsigned long long g;
         while ((unsigned)((g = ld_word(&a.bar->gword)) >> 32) != gen)
-            if (wait_over(t0, a.err)) break;
+            if (wait_over(t0, a.err)) {
+                bad = 1;
+                break;
+            }
         *s_nact = (int)(g & 0x7fffffffull);
         *s_anyru = (int)((g >> 31) & 1ull);
         __threadfence();
     }
-    __syncthreads();
-    return *(volatile int*)a.err == 0;
+    return __syncthreads_or(bad) == 0;
 }
 
 // Scalar recurrence of one system after its partials were summed (one thread):
@@ -995,6 +1004,7 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
                             SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast, FastShadow& fs)
 {
     constexpr bool kFix = MIXED && K == 1;   // fixed-point sums available
+    int bad = 0;   // thread 0: its wait gave up
     __syncthreads();
 #ifdef YK_CG_TIMING
     const long long q0 = clock64();
@@ -1013,14 +1023,16 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
         const volatile unsigned* c = &a.bar->arrive;
         const long long t0 = clock64();
         while ((int)(*c - target) < 0)
-            if (wait_over(t0, a.err)) break;
+            if (wait_over(t0, a.err)) {
+                bad = 1;
+                break;
+            }
         __threadfence();
         s_cnt[0] = 0;
         s_cnt[1] = 0;
     }
-    __syncthreads();
     ++gen;
-    if (*(volatile int*)a.err) return false;
+    if (__syncthreads_or(bad)) return false;
     double s[6];
 #ifdef YK_CG_TIMING
     const long long q1 = clock64();
@@ -1306,6 +1318,102 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool w
     }
 }
 
+// Reliable update (mixed solver), first part, at one site of a system in
+// mode kRu: fold x_k = x + xs + alpha p_{k-1} into the FP64 x; xs = 0.
+template <int K>
+__device__ __forceinline__ void ru_fold(const SysDev& S, int n, const SysLocal& L, int prv)
+{
+    Site<double, K> xv = YK_LD(double, K, S.x, n);
+    const Site<float, K> xs = YK_LD(float, K, S.xs32, n);
+    const Site<float, K> pv = YK_LD(float, K, S.p32[prv], n);
+    Site<double, K> pd;
+    Site<float, K> zw;
+#pragma unroll
+    for (int i = 0; i < 4 * K; ++i) {
+        xv.v[i] += (double)xs.v[i];
+        pd.v[i] = (double)pv.v[i];
+        zw.v[i] = 0.f;
+    }
+    site_axpy<double, K>(xv, L.alpha_re, L.alpha_im, pd);
+    YK_ST(double, K, S.x, n, xv);
+    YK_ST(float, K, S.xs32, n, zw);
+}
+
+// Reliable update (mixed solver), second part, after the fold and a
+// neighbour sync: t64 = D_first x in FP64, a neighbour sync, then
+// r = b - D_second t64 in FP64, rounded into R[cur], with the partials |r|^2
+// and <r, p_{k-1}> of every tile in mode kRu.  The block's tiles go
+// blockDim / 256 at a time as in the passes of the kernels calling this.
+// False when a neighbour wait gave up.
+template <int K>
+__device__ bool ru_residual(const CGArgs& a, const SysLocal* sl, const int* tslot, int tb, int te, bool first_dag,
+                            int cur, int prv, unsigned& epoch, const Deps& deps, double* red)
+{
+    constexpr int kSkipIm = (K == 1) ? ((1 << 3) | (1 << 5)) : 0;
+    const int TP = blockDim.x / kTile, hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;
+    // RU1: t64 = D_first x (FP64)
+    for (int tile = tb + hf; tile < te; tile += TP) {
+        const SysLocal& L = sl[tslot[tile - tb]];
+        if (L.mode != kRu) continue;
+        const SysDev& S = a.sys[L.sys];
+        const int n = a.tiles[tile].y + ts;
+        if (n >= S.V) continue;
+        const Nbr nb = neighbours(n, S.Nt, S.Nx);
+        const Site<double, K> c = YK_LD(double, K, S.x, n);
+        const Site<double, K> tu = YK_LD(double, K, S.x, nb.tu);
+        const Site<double, K> td = YK_LD(double, K, S.x, nb.td);
+        const Site<double, K> xu = YK_LD(double, K, S.x, nb.xu);
+        const Site<double, K> xd = YK_LD(double, K, S.x, nb.xd);
+        const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+        const Site<double, K> t = first_dag
+            ? dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
+            : dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
+        YK_ST(double, K, S.t64, n, t);
+    }
+    if (!nsync(a, ++epoch, deps)) return false;
+    // RU2: r = b - D_second t64 in FP64 -> R[cur]; |r|^2, <r, p_{k-1}>
+    for (int base = tb; base < te; base += TP) {   // the same trip count in every thread
+        const int tile = base + hf;
+        bool on = tile < te;
+        const SysLocal& L = sl[tslot[(on ? tile : tb) - tb]];
+        on = on && L.mode == kRu;
+        const SysDev& S = a.sys[L.sys];
+        const int n = on ? a.tiles[tile].y + ts : 0;
+        double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (on && n < S.V) {
+            const Nbr nb = neighbours(n, S.Nt, S.Nx);
+            const Site<double, K> c = YK_LD(double, K, S.t64, n);
+            const Site<double, K> tu = YK_LD(double, K, S.t64, nb.tu);
+            const Site<double, K> td = YK_LD(double, K, S.t64, nb.td);
+            const Site<double, K> xu = YK_LD(double, K, S.t64, nb.xu);
+            const Site<double, K> xd = YK_LD(double, K, S.t64, nb.xd);
+            const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+            const Site<double, K> ax = first_dag
+                ? dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
+                : dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
+            const Site<double, K> bv = YK_LD(double, K, S.b, n);
+            const Site<float, K> pw = YK_LD(float, K, S.p32[prv], n);
+            Site<double, K> rd, pd;
+            Site<float, K> rw;
+#pragma unroll
+            for (int i = 0; i < 4 * K; ++i) {
+                rd.v[i] = bv.v[i] - ax.v[i];
+                rw.v[i] = (float)rd.v[i];
+                pd.v[i] = (double)pw.v[i];
+            }
+            YK_ST(float, K, S.r32[cur], n, rw);
+            v[0] = site_norm2<double, K>(rd);
+            site_dot<double, K>(rd, pd, v[2], v[3]);
+        }
+        // slots 1, 4, 5 unused here
+        FF f[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+        put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, on, f, red);
+    }
+    return true;
+}
+
 }  // namespace
 
 // Threads per block of the CG kernel: two 256-site tiles at once for the real
@@ -1463,21 +1571,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
             if (n >= S.V) continue;
             if constexpr (MIXED) {
                 if (mode == kRu) {
-                    // fold x_k = x + xs + alpha p_{k-1} into the FP64 x; xs = 0
-                    Site<double, K> xv = YK_LD(double, K, S.x, n);
-                    const Site<W, K> xs = YK_LD(W, K, S.xs32, n);
-                    const Site<W, K> pv = YK_LD(W, K, Pv(S, prv), n);
-                    Site<double, K> pd;
-                    Site<W, K> zw;
-#pragma unroll
-                    for (int i = 0; i < 4 * K; ++i) {
-                        xv.v[i] += (double)xs.v[i];
-                        pd.v[i] = (double)pv.v[i];
-                        zw.v[i] = W(0);
-                    }
-                    site_axpy<double, K>(xv, L.alpha_re, L.alpha_im, pd);
-                    YK_ST(double, K, S.x, n, xv);
-                    YK_ST(W, K, S.xs32, n, zw);
+                    ru_fold<K>(S, n, L, prv);
                     continue;
                 }
             }
@@ -1528,66 +1622,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
 
         if constexpr (MIXED) {
             if (any_ru) {
-                // RU1: t64 = D_first x (FP64)
-                for (int tile = tb + hf; tile < te; tile += TP) {
-                    const SysLocal& L = sl[tslot[tile - tb]];
-                    if (L.mode != kRu) continue;
-                    const SysDev& S = a.sys[L.sys];
-                    const int n = a.tiles[tile].y + ts;
-                    if (n >= S.V) continue;
-                    const Nbr nb = neighbours(n, S.Nt, S.Nx);
-                    const Site<double, K> c = YK_LD(double, K, S.x, n);
-                    const Site<double, K> tu = YK_LD(double, K, S.x, nb.tu);
-                    const Site<double, K> td = YK_LD(double, K, S.x, nb.td);
-                    const Site<double, K> xu = YK_LD(double, K, S.x, nb.xu);
-                    const Site<double, K> xd = YK_LD(double, K, S.x, nb.xd);
-                    const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-                    const Site<double, K> t = first_dag
-                        ? dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
-                        : dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
-                    YK_ST(double, K, S.t64, n, t);
-                }
-                if (!nsync(a, ++epoch, deps)) return;
-                // RU2: r = b - D_second t64 in FP64 -> R[cur]; |r|^2, <r, p_{k-1}>
-                for (int base = tb; base < te; base += TP) {   // the same trip count in every thread
-                    const int tile = base + hf;
-                    bool on = tile < te;
-                    const SysLocal& L = sl[tslot[(on ? tile : tb) - tb]];
-                    on = on && L.mode == kRu;
-                    const SysDev& S = a.sys[L.sys];
-                    const int n = on ? a.tiles[tile].y + ts : 0;
-                    double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-                    if (on && n < S.V) {
-                        const Nbr nb = neighbours(n, S.Nt, S.Nx);
-                        const Site<double, K> c = YK_LD(double, K, S.t64, n);
-                        const Site<double, K> tu = YK_LD(double, K, S.t64, nb.tu);
-                        const Site<double, K> td = YK_LD(double, K, S.t64, nb.td);
-                        const Site<double, K> xu = YK_LD(double, K, S.t64, nb.xu);
-                        const Site<double, K> xd = YK_LD(double, K, S.t64, nb.xd);
-                        const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-                        const Site<double, K> ax = first_dag
-                            ? dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
-                            : dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
-                        const Site<double, K> bv = YK_LD(double, K, S.b, n);
-                        const Site<W, K> pw = YK_LD(W, K, Pv(S, prv), n);
-                        Site<double, K> rd, pd;
-                        Site<W, K> rw;
-#pragma unroll
-                        for (int i = 0; i < 4 * K; ++i) {
-                            rd.v[i] = bv.v[i] - ax.v[i];
-                            rw.v[i] = (W)rd.v[i];
-                            pd.v[i] = (double)pw.v[i];
-                        }
-                        YK_ST(W, K, Rv(S, cur), n, rw);
-                        v[0] = site_norm2<double, K>(rd);
-                        site_dot<double, K>(rd, pd, v[2], v[3]);
-                    }
-                    // slots 1, 4, 5 unused here
-                    FF f[6];
-#pragma unroll
-                    for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
-                    put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, on, f, red);
-                }
+                if (!ru_residual<K>(a, sl, tslot, tb, te, first_dag, cur, prv, epoch, deps, red)) return;
                 if (!reduce(k, true)) return;
                 continue;   // same k: the systems that updated redo A(k)
             }
@@ -1617,6 +1652,299 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
         for (int i = 0; i < 8; ++i) f[i] = 0;
     }
 #endif
+}
+
+// ---------------------------------------------------------------------------
+// Halo variant of the mixed single-system CG on the real path (K = 1).
+//
+// Each block owns the contiguous site range [n0, n1) of its tiles.  Every
+// iteration it forms p_k itself on that range widened by two time slices on
+// each side (2 Nx sites), from r, A p and p of the previous iteration, which
+// the grid barrier of that iteration has completed; applies D_first on the
+// range widened by one slice; and applies D_second on its own sites -- both
+// stencils in shared memory.  An iteration is then one round of loads, two
+// shared-memory stencils and the reducing grid barrier: no neighbour
+// synchronisation and no round trip of D p through L2.  The price is the
+// redundant work on the four halo slices, so the launcher takes this kernel
+// only while 4 Nx <= 2 (n1 - n0) (and the widened range fits the lattice and
+// shared memory).
+//
+// Per site the arithmetic is that of cg_kernel<1, true> (the same formation
+// of r and p, the same stencil calls, the same tile partials and fixed-point
+// sums), so the two kernels produce the same iterates.  A p is double-buffered
+// here (S.Ap32 for even k, S.t32 for odd k), because a block may store A p_k
+// while a neighbour still reads A p_{k-1} on its halo.  Round 0 and the
+// reliable updates run as in cg_kernel, with neighbour synchronisation.
+// ---------------------------------------------------------------------------
+constexpr int kHaloThreads = 2 * kTile;
+constexpr int kHaloChunk = 3;   // P-range sites per thread loaded together
+
+__device__ __forceinline__ int wrap_site(int m, int V) { return m < 0 ? m + V : (m >= V ? m - V : m); }
+
+__device__ __forceinline__ Site<float, 1> ld_sm(const float4* s, int j)
+{
+    const float4 a = s[j];
+    Site<float, 1> o;
+    o.v[0] = a.x;
+    o.v[1] = a.y;
+    o.v[2] = a.z;
+    o.v[3] = a.w;
+    return o;
+}
+
+__device__ __forceinline__ void st_sm(float4* s, int j, const Site<float, 1>& v)
+{
+    s[j] = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+
+// D (DAG = false) or D^dag (DAG = true) at site m from a shared-memory copy
+// `in` of a contiguous site range holding m at index j and both of m's time
+// slices; diag at m given.
+template <bool DAG>
+__device__ __forceinline__ Site<float, 1> apply_d_sm(const float4* in, int j, int m, int Nt, int Nx, float diag, float r)
+{
+    const Nbr nb = neighbours(m, Nt, Nx);
+    const Site<float, 1> c = ld_sm(in, j);
+    const Site<float, 1> tu = ld_sm(in, j + Nx);
+    const Site<float, 1> td = ld_sm(in, j - Nx);
+    const Site<float, 1> xu = ld_sm(in, j + (int)(nb.xu - m));
+    const Site<float, 1> xd = ld_sm(in, j + (int)(nb.xd - m));
+    return dirac_combine<float, 1, DAG>(c, tu, td, xu, xd, diag, r, nb.sp, nb.sm);
+}
+
+enum { kHaloInit = 0 };   // A1 of round 0: p_0 = b as stored
+
+__global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
+{
+    constexpr int K = 1;
+    constexpr int kSkipIm = (1 << 3) | (1 << 5);
+    using W = float;
+    extern __shared__ float4 hsm[];
+    const int hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;
+    __shared__ double red[128];
+    __shared__ SysLocal sl[kMaxSysPerBlock];
+    __shared__ int nsl;
+    __shared__ int tslot[kMaxTilesPerBlock];
+    __shared__ Deps deps;
+    __shared__ int s_nact, s_anyru;
+    __shared__ int s_cnt[2];
+    __shared__ int s_esc[4], s_fast;
+    __shared__ CGState lst;
+    __shared__ FastShadow fsh;
+    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
+    const int te = min(tb + a.tiles_per_block, a.tile_end);
+    setup_block(a, tb, te, sl, &nsl, tslot, &deps);
+    if (*(volatile int*)a.err) return;
+    if (threadIdx.x == 0) {
+        s_fast = 0;
+        lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
+        lst.active = 1;
+        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
+        lst.mode = kStep;
+        fsh.valid = 0;
+    }
+    const SysDev& S = a.sys[a.sys_first];
+    const int Nt = S.Nt, Nx = S.Nx, V = S.V;
+    const int n0 = a.tiles[tb].y;
+    const int n1 = min(a.tiles[te - 1].y + kTile, V);
+    const int own = n1 - n0;
+    const int nP = own + 4 * Nx, nT = own + 2 * Nx;
+    float4* p_s = hsm;                                   // p_k on [n0 - 2 Nx, n1 + 2 Nx)
+    float4* t_s = p_s + nP;                              // D_first p_k on [n0 - Nx, n1 + Nx)
+    float4* r_s = t_s + nT;                              // r_k on [n0, n1)
+    float* d_s = reinterpret_cast<float*>(r_s + own);    // diag on [n0 - Nx, n1 + Nx)
+    const bool first_dag = (a.mtype == YK_NORMAL);       // Normal: A = D D^dag, apply D^dag first
+    const float rw = (float)S.r;
+    for (int j = threadIdx.x; j < nT; j += kHaloThreads) {
+        const int m = wrap_site(n0 - Nx + j, V);
+        d_s[j] = (float)(2.0 * S.r + S.m0 + S.g * S.sigma[m]);
+    }
+    unsigned epoch = 0, gen = 0;
+#ifdef YK_CG_TIMING
+    long long tacc[5] = {0, 0, 0, 0, 0}, tlast = clock64();
+    int tit = 0;
+#endif
+
+    // A1: p_k (and r_k, x_k on the own sites) on the widened range
+    auto pass_a1 = [&](int mode, int cur, int prv) {
+        const SysLocal& L = sl[0];
+        const W ar = L.f_alpha_re, beta = L.f_beta, cre = L.f_c_re, cim = L.f_c_im;
+        const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
+        const float* Al = prv == 0 ? S.Ap32 : S.t32;
+        const float* Pl = (mode == kHaloInit) ? S.p32[0] : S.p32[prv];
+        for (int base = 0; base < nP; base += kHaloThreads * kHaloChunk) {
+            Site<W, K> rv[kHaloChunk], av[kHaloChunk], pv[kHaloChunk], xv[kHaloChunk];
+            int mm[kHaloChunk], oo[kHaloChunk];
+#pragma unroll
+            for (int g = 0; g < kHaloChunk; ++g) {
+                const int j = base + g * kHaloThreads + threadIdx.x;
+                mm[g] = -1;
+                oo[g] = -1;
+                if (j >= nP) continue;
+                const int m = wrap_site(n0 - 2 * Nx + j, V);
+                const int o = j - 2 * Nx;
+                mm[g] = m;
+                oo[g] = (o >= 0 && o < own) ? o : -1;
+                pv[g] = YK_LD(W, K, Pl, m);
+                if (mode == kStep) {
+                    rv[g] = YK_LD(W, K, Rl, m);
+                    av[g] = YK_LD(W, K, Al, m);
+                    if (oo[g] >= 0) xv[g] = YK_LD(W, K, S.xs32, m);
+                } else if (mode == kRedo) {
+                    rv[g] = YK_LD(W, K, Rl, m);
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < kHaloChunk; ++g) {
+                if (mm[g] < 0) continue;
+                const int j = base + g * kHaloThreads + threadIdx.x, m = mm[g], o = oo[g];
+                Site<W, K> p;
+                if (mode == kStep) {
+                    Site<W, K> r = rv[g];
+                    site_axpy<W, K>(r, -ar, W(0), av[g]);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) p.v[i] = fma(beta, pv[g].v[i], r.v[i]);
+                    if (o >= 0) {
+                        Site<W, K> x = xv[g];
+                        site_axpy<W, K>(x, ar, W(0), pv[g]);
+                        YK_ST(W, K, S.xs32, m, x);
+                        YK_ST(W, K, S.r32[cur], m, r);
+                        YK_ST(W, K, S.p32[cur], m, p);
+                        st_sm(r_s, o, r);
+                    }
+                } else if (mode == kRedo) {
+                    p = p_next<W, K>(rv[g], pv[g], beta, cre, cim);
+                    if (o >= 0) {
+                        YK_ST(W, K, S.p32[cur], m, p);
+                        st_sm(r_s, o, rv[g]);
+                    }
+                } else {
+                    p = pv[g];
+                    if (o >= 0) st_sm(r_s, o, p);   // r_0 = p_0 = b
+                }
+                st_sm(p_s, j, p);
+            }
+        }
+    };
+
+    // A2: t = D_first p_k on [n0 - Nx, n1 + Nx)
+    auto pass_a2 = [&]() {
+        for (int j = threadIdx.x; j < nT; j += kHaloThreads) {
+            const int m = wrap_site(n0 - Nx + j, V);
+            const Site<W, K> t = first_dag ? apply_d_sm<true>(p_s, j + Nx, m, Nt, Nx, d_s[j], rw)
+                                           : apply_d_sm<false>(p_s, j + Nx, m, Nt, Nx, d_s[j], rw);
+            st_sm(t_s, j, t);
+        }
+    };
+
+    // B(k): A p_k = D_second t on the own sites -> Ap[cur]; the tile partials
+    auto pass_b = [&](int cur) {
+        float* Ac = cur == 0 ? S.Ap32 : S.t32;
+        for (int base = tb; base < te; base += 2) {   // the same trip count in every thread
+            const int tile = base + hf;
+            const int n = tile < te ? a.tiles[tile].y + ts : V;
+            const bool on = n < V;
+            W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
+            if (on) {
+                const int o = n - n0, jt = o + Nx;
+                const Site<W, K> ap = first_dag ? apply_d_sm<false>(t_s, jt, n, Nt, Nx, d_s[jt], rw)
+                                                : apply_d_sm<true>(t_s, jt, n, Nt, Nx, d_s[jt], rw);
+                YK_ST(W, K, Ac, n, ap);
+                const Site<W, K> r = ld_sm(r_s, o);
+                const Site<W, K> p = ld_sm(p_s, o + 2 * Nx);
+                v[0] = site_norm2<W, K>(r);
+                v[1] = site_norm2<W, K>(ap);
+                site_dot<W, K>(p, ap, v[2], v[3]);
+                site_dot<W, K>(r, ap, v[4], v[5]);
+            }
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = FF{v[i], 0.f};
+            if (s_fast)
+                put_partial_ff<kSkipIm, false>(a, tile, on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
+            else
+                put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
+        }
+    };
+
+    auto reduce = [&](int kk, bool ru) -> bool {
+        return solo_reduce<K, true>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh);
+    };
+
+    // ---------------- round 0: b, x = 0, r_0 = p_0 = b; t = D_first p_0; B(0)
+    for (int tile = tb + hf; tile < te; tile += 2) {
+        const int n = a.tiles[tile].y + ts;
+        if (n >= V) continue;
+        const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+        if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
+        Site<double, K> z;
+        Site<W, K> bw, zw;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            z.v[i] = 0.0;
+            zw.v[i] = W(0);
+            bw.v[i] = (W)bv.v[i];
+        }
+        YK_ST(double, K, S.x, n, z);
+        YK_ST(W, K, S.xs32, n, zw);
+        YK_ST(W, K, S.r32[0], n, bw);
+        YK_ST(W, K, S.p32[0], n, bw);
+    }
+    if (!nsync(a, ++epoch, deps)) return;
+    pass_a1(kHaloInit, 0, 0);
+    __syncthreads();
+    pass_a2();
+    __syncthreads();
+    pass_b(0);
+    if (!reduce(0, false)) return;
+
+    int k = 1;
+    while (k <= a.max_iter) {   // the system retires at k = max_iter at the latest
+        YK_TMARK(0);   // grid reduction
+        if (s_nact == 0) break;
+        const int cur = k & 1, prv = cur ^ 1;
+        const int mode = sl[0].mode;
+        if (mode == kRu) {
+            for (int tile = tb + hf; tile < te; tile += 2) {
+                const int n = a.tiles[tile].y + ts;
+                if (n < V) ru_fold<K>(S, n, sl[0], prv);
+            }
+            if (!nsync(a, ++epoch, deps)) return;
+            if (!ru_residual<K>(a, sl, tslot, tb, te, first_dag, cur, prv, epoch, deps, red)) return;
+            if (!reduce(k, true)) return;
+            continue;   // same k: redo A(k) from the FP64 residual
+        }
+        pass_a1(mode, cur, prv);
+        __syncthreads();
+        YK_TMARK(1);
+        pass_a2();
+        __syncthreads();
+        YK_TMARK(2);
+        pass_b(cur);
+        YK_TMARK(3);
+        if (!reduce(k, false)) return;
+        ++k;
+#ifdef YK_CG_TIMING
+        ++tit;
+#endif
+    }
+#ifdef YK_CG_TIMING
+    if (blockIdx.x == 0 && threadIdx.x == 0 && tit > 0) {
+        printf("cg timing (block 0, cycles per iteration over %d): reduce+coef %lld  A1 %lld  A2 %lld  B %lld\n", tit,
+               tacc[0] / tit, tacc[1] / tit, tacc[2] / tit, tacc[3] / tit);
+        volatile unsigned long long* f = g_cg_f;
+        printf("cg timing (finisher, cycles per event): sums %llu (loads %llu)  scalar %llu  tail %llu\n",
+               f[0] / (f[3] ? f[3] : 1), f[4] / (f[3] ? f[3] : 1), f[1] / (f[3] ? f[3] : 1), f[2] / (f[3] ? f[3] : 1));
+        for (int i = 0; i < 8; ++i) f[i] = 0;
+    }
+#endif
+}
+
+// Shared memory of cg_halo_kernel for own sites per block and Nx.
+static size_t halo_smem_bytes(int own, int Nx)
+{
+    const size_t nP = (size_t)own + 4 * (size_t)Nx, nT = (size_t)own + 2 * (size_t)Nx;
+    return (nP + nT + (size_t)own) * sizeof(float4) + nT * sizeof(float);
 }
 
 // Resets the barrier, flags, counters and per-system state before a solve.
@@ -1691,8 +2019,40 @@ int cg_grid_for(int ntiles, int maxg, int* tiles_per_block)
     return grid;
 }
 
+constexpr size_t kHaloMaxSmem = 200 * 1024;
+
+// Whether cg_halo_kernel takes a single-system solve on an Nt x Nx lattice
+// whose blocks own tpb tiles each: at most 8 tiles per block, halo work at
+// most twice the own work (4 Nx <= 2 * own), the widened range within the
+// lattice, and its shared memory within kHaloMaxSmem.  Callers that do not
+// give the lattice (Nt = Nx = 0) get cg_kernel.
+static bool halo_takes(int Nt, int Nx, int tpb, size_t* smem)
+{
+    if (Nt < 1 || Nx < 1 || tpb < 1 || tpb > 8) return false;
+    const long long own = (long long)tpb * kTile, V = (long long)Nt * Nx;
+    if (4LL * Nx > 2 * own || own + 4LL * Nx > V) return false;
+    *smem = halo_smem_bytes((int)own, Nx);
+    return *smem <= kHaloMaxSmem;
+}
+
+static int halo_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        cudaFuncSetAttribute((const void*)cg_halo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHaloMaxSmem);
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_halo_kernel, kHaloThreads, kHaloMaxSmem);
+        maxg = per * nsm;
+    }
+    return maxg;
+}
+
+void cg_halo_init() { halo_max_grid(); }
+
 template <int K, bool MIXED>
-static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out)
+static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out, int* kernel_out)
 {
     CGArgs a = a0;
     const int maxg = max_grid_t<K, MIXED>();
@@ -1703,24 +2063,41 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     a.tiles_per_block = tpb;
     a.grid = grid;
     if (grid_out) *grid_out = grid;
+    const void* fn = (const void*)cg_kernel<K, MIXED>;
+    unsigned threads = cg_threads<K>();
+    size_t smem = 0;
+    if constexpr (K == 1 && MIXED) {
+        // the same tile partition as cg_kernel<1, true>, so the same partials
+        size_t hs = 0;
+        if (a.sys_count == 1 && halo_takes(a.solo_nt, a.solo_nx, tpb, &hs) && grid <= halo_max_grid()) {
+            fn = (const void*)cg_halo_kernel;
+            threads = kHaloThreads;
+            smem = hs;
+        }
+    }
+    if (kernel_out) *kernel_out = (fn == (const void*)cg_halo_kernel) ? 1 : 0;
     cg_prepare_kernel<<<1, 256, 0, stream>>>(a);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(cg_threads<K>());
-    cfg.dynamicSmemBytes = 0;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, cg_kernel<K, MIXED>, a);
+    void* args[] = {&a};
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out)
+cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out, int* kernel_out)
 {
-    if (K == 1) return mixed ? launch_cg_t<1, true>(a, stream, grid_out) : launch_cg_t<1, false>(a, stream, grid_out);
-    return mixed ? launch_cg_t<2, true>(a, stream, grid_out) : launch_cg_t<2, false>(a, stream, grid_out);
+    if (K == 1)
+        return mixed ? launch_cg_t<1, true>(a, stream, grid_out, kernel_out)
+                     : launch_cg_t<1, false>(a, stream, grid_out, kernel_out);
+    return mixed ? launch_cg_t<2, true>(a, stream, grid_out, kernel_out)
+                 : launch_cg_t<2, false>(a, stream, grid_out, kernel_out);
 }
 
 }  // namespace yk

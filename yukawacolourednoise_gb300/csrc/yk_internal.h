@@ -117,6 +117,7 @@ struct CGArgs {
     double tol;
     int reliable_every;
     double reliable_delta;
+    int solo_nt, solo_nx;   // lattice of a single-system solve (0: not given; the halo kernel needs it)
 };
 
 // Per-chain device record of the Langevin step.

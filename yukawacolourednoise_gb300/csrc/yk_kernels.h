@@ -15,9 +15,12 @@ cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt,
                          cudaStream_t stream);
 
 // Batched CG (yk_cg.cu).  Also launches its one-block preparation kernel.
-cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out);
+// grid_out: blocks launched; kernel_out: 0 cg_kernel, 1 cg_halo_kernel (either may be null)
+cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out, int* kernel_out = nullptr);
 // Largest co-resident grid of the CG kernel (cached; call before capturing).
 int cg_max_grid(int K, bool mixed);
+// Kernel attributes and occupancy of the halo CG kernel (call before any stream capture).
+void cg_halo_init();
 
 // Cluster-resident mixed CG (yk_cg_cluster.cu): one 16-CTA cluster per system
 // of real (K = 1) vectors whose rows fit the cluster (cg_cluster_fits);
