@@ -87,6 +87,15 @@ __device__ void chk_st(R* p, int64_t n, const Site<R, K>& v, int V, int line)
 __device__ unsigned long long g_cg_t[10];
 __device__ unsigned long long g_cg_f[8];   // finisher: start->sums ready, ->scalar done, ->end
 __device__ unsigned long long g_cg_first;
+__device__ unsigned long long g_cg_q[16];   // single-system reduction, block 0: cycles between marks
+#define YK_QMARK(i)                                               \
+    do {                                                          \
+        if (blockIdx.x == 0 && threadIdx.x == 0) {                \
+            const long long t_ = clock64();                       \
+            atomicAdd(&g_cg_q[i], (unsigned long long)(t_ - ql)); \
+            ql = t_;                                              \
+        }                                                         \
+    } while (0)
 __device__ __forceinline__ unsigned long long gtimer()
 {
     unsigned long long t;
@@ -103,6 +112,9 @@ __device__ __forceinline__ unsigned long long gtimer()
     } while (0)
 #else
 #define YK_TMARK(i) \
+    do {            \
+    } while (0)
+#define YK_QMARK(i) \
     do {            \
     } while (0)
 #endif
@@ -185,6 +197,15 @@ __device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
 // ---------------------------------------------------------------------------
 constexpr int kFixBits = 48;                 // resolution: 2^-48 of the previous total
 constexpr long long kFixLimit = 1ll << 61;   // a total at or above this is not trusted
+constexpr int kFixOverflowWord = 8;          // fsum[b][0][8]: set when a tile's value was too large
+
+// Largest tile value added to a total of ntiles tiles: ntiles values below
+// it cannot overflow 63 bits, whatever their signs.  A larger one is not
+// added; the tile flags the total instead.
+__device__ __forceinline__ long long fix_tile_limit(int ntiles)
+{
+    return 1ll << (62 - (32 - __clz(ntiles)));
+}
 
 // round(x * 2^e) from the bits of x: integer operations only (no FP64).
 // Magnitudes beyond the window saturate to kFixLimit, which the readers
@@ -379,6 +400,21 @@ __device__ __forceinline__ double2 ld_sync2(const void* p)
 {
     double2 v;
     asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
+    return v;
+}
+
+// Arrival at the single-system barrier (release: this thread's writes, and the
+// block's writes ordered before it by bar.sync, are visible to a block that
+// acquires the final count) and the acquiring poll of the count.
+__device__ __forceinline__ void arrive_release(unsigned* p)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(p) : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -617,26 +653,28 @@ struct FastShadow {
     int valid;
 };
 
-// One step of the mixed single-system recurrence from the four fixed-point
-// totals (|r|^2, |Ap|^2, <p, Ap>, <r, Ap> at scales esc), on the FP32 pipes:
-// the scalar work runs in one thread per block on the critical path, where
-// every FP64 instruction would cost tens of cycles.  alpha and beta are FP32
-// as in scalar_step<true>; |r_{k+1}|^2 = |r|^2 - alpha (2 <r, Ap> - alpha |Ap|^2)
-// is formed in float-float because its terms cancel.  Returns false without
-// changing anything when the ordinary case does not hold (first iteration,
-// iteration cap, values out of the float-float window, a non-positive
+// One step of the mixed single-system recurrence from the four totals
+// (|r|^2, |Ap|^2, <p, Ap>, <r, Ap>, converted from fixed point to float-float
+// by the lanes of warp 0), on the FP32 pipes: the scalar work runs in one
+// thread per block on the critical path, where every FP64 instruction would
+// cost tens of cycles.  alpha and beta are FP32 as in scalar_step<true>;
+// |r_{k+1}|^2 = |r|^2 - alpha (2 <r, Ap> - alpha |Ap|^2) is formed in
+// float-float because its terms cancel.  `due`: the periodic reliable update
+// falls on k + 1.  Returns false without changing anything when the ordinary
+// case does not hold (first iteration, iteration cap, a non-positive
 // curvature or a non-finite alpha); the caller then takes the FP64 step.
-__device__ bool fast_step(const CGArgs& a, int k, const long long (&S)[4], const int* esc, CGState& st,
+__device__ bool fast_step(const CGArgs& a, int k, FF rr, FF apap, FF pap, FF rap, bool due, CGState& st,
                           FastShadow& fs, SysLocal& L)
 {
+#ifdef YK_CG_TIMING
+    long long ql = clock64();
+#endif
     if (k == 0 || k >= a.max_iter) return false;
-    FF rr, apap, pap, rap;
-    if (!fix_to_ff(S[0], esc[0], rr) || !fix_to_ff(S[1], esc[1], apap) || !fix_to_ff(S[2], esc[2], pap) ||
-        !fix_to_ff(S[3], esc[3], rap))
-        return false;
     const float rrf = rr.hi + rr.lo, papf = pap.hi + pap.lo;
     if (!(rrf > 0.f) || !(papf > 0.f)) return false;
-    const float alpha = rrf / papf;   // CGsolver.cu:137
+    // CGsolver.cu:137.  Approximate division (reciprocal and product, within
+    // 2 ulp): every block computes the same bits, which is what matters
+    const float alpha = __fdividef(rrf, papf);
     if (!isfinite(alpha)) return false;
     if (!fs.valid) {
         fs.rmax2 = (float)st.rmax2;
@@ -648,12 +686,12 @@ __device__ bool fast_step(const CGArgs& a, int k, const long long (&S)[4], const
     const FF e = ff_add(rr, ff_neg(w));
     float est = e.hi + e.lo;
     if (!(est > 0.f)) est = 0.f;
-    fs.rmax2 = fmaxf(fs.rmax2, rrf);
+    const float rmax2 = fmaxf(fs.rmax2, rrf);
+    fs.rmax2 = rmax2;
     fs.rr_prev = rrf;
     st.iters = k;
     const bool cand = !(rrf > fs.stop2) || !(est > fs.stop2);
-    const bool drop = est < fs.d2 * fs.rmax2;
-    const bool due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
+    const bool drop = est < fs.d2 * rmax2;
     const bool cap = k + 1 >= a.max_iter;
     int mode = kStep;
     if (cand || drop || due || cap) {
@@ -661,7 +699,7 @@ __device__ bool fast_step(const CGArgs& a, int k, const long long (&S)[4], const
         mode = kRu;
         st.rr = (double)rrf;
         st.rr_prev = st.rr;
-        st.rmax2 = (double)fs.rmax2;
+        st.rmax2 = (double)rmax2;
         fs.valid = 0;
         L.alpha_re = (double)alpha;   // the FP64 fold of x uses the FP64 copy
         L.alpha_im = 0.0;
@@ -670,7 +708,8 @@ __device__ bool fast_step(const CGArgs& a, int k, const long long (&S)[4], const
     L.mode = mode;
     L.f_alpha_re = alpha;
     L.f_alpha_im = 0.f;
-    L.f_beta = est / rrf;
+    L.f_beta = __fdividef(est, rrf);
+    YK_QMARK(12);
     return true;
 }
 
@@ -1000,15 +1039,20 @@ __device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red
 // replaced by one round of loads in every block.  Block 0 keeps the
 // host-visible CGState up to date.
 template <int K, bool MIXED>
-__device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red, CGState& lst,
-                            SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast, FastShadow& fs)
+__device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red,
+                                                 CGState& lst, SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt,
+                                                 int* esc, int* s_fast, FastShadow& fs)
 {
     constexpr bool kFix = MIXED && K == 1;   // fixed-point sums available
     int bad = 0;   // thread 0: its wait gave up
+#ifdef YK_CG_TIMING
+    long long ql = clock64();
+#endif
     __syncthreads();
 #ifdef YK_CG_TIMING
     const long long q0 = clock64();
 #endif
+    YK_QMARK(0);
     if (threadIdx.x == 0) {
         if (kFix && blockIdx.x == 0) {
             // the buffer of the barrier after this one: nobody reads it any more
@@ -1016,23 +1060,24 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
             // before this block has arrived
             long long (*z)[16] = a.bar->fsum[(gen + 2u) % 3u];
             for (int c = 0; c < 4; ++c) z[c][0] = 0;
+            z[0][kFixOverflowWord] = 0;
         }
-        __threadfence();
-        atomicAdd(&a.bar->arrive, 1u);
+        arrive_release(&a.bar->arrive);
+        YK_QMARK(1);
         const unsigned target = gridDim.x * (gen + 1u);
-        const volatile unsigned* c = &a.bar->arrive;
         const long long t0 = clock64();
-        while ((int)(*c - target) < 0)
+        while ((int)(ld_acquire(&a.bar->arrive) - target) < 0)
             if (wait_over(t0, a.err)) {
                 bad = 1;
                 break;
             }
-        __threadfence();
+        YK_QMARK(2);
         s_cnt[0] = 0;
         s_cnt[1] = 0;
     }
     ++gen;
     if (__syncthreads_or(bad)) return false;
+    YK_QMARK(3);
     double s[6];
 #ifdef YK_CG_TIMING
     const long long q1 = clock64();
@@ -1040,48 +1085,75 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
     // fixed-point totals of this barrier, if the tiles added them
     bool fast = false, stepped = false;
     int s_scales = 0;   // thread 0: 2 = next scales set from the integer totals
+    __shared__ int s_dec;   // thread 0's verdict on the fixed-point totals (0 none, 1 sums, 2 stepped)
     if constexpr (kFix) {
         if (!ru_round && *s_fast) {
-            if (threadIdx.x == 0) {
+            if (threadIdx.x < 32) {
+                // lanes 0-3: one total each (load, range check, conversion,
+                // next scale); lane 4: the overflow flag; lane 5: the
+                // periodic trigger; lane 0 then steps
+                const unsigned full = 0xffffffffu;
+                const int lane = threadIdx.x;
                 const long long(*f)[16] = a.bar->fsum[gen % 3u];
-                long long S[4];
-                for (int c = 0; c < 4; ++c) S[c] = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[c][0]));
-                bool ok = true;
-                for (int c = 0; c < 4; ++c) ok = ok && S[c] < kFixLimit && S[c] > -kFixLimit;
-                bool done = false;
-                if (ok) {
-                    // the ordinary step on the FP32 pipes; the FP64 one otherwise
-                    done = lst.mode != kIdle && fast_step(a, k, S, esc, lst, fs, L);
-                    if (!done) {
-                        s[0] = scalbn((double)S[0], -esc[0]);
-                        s[1] = scalbn((double)S[1], -esc[1]);
-                        s[2] = scalbn((double)S[2], -esc[2]);
-                        s[4] = scalbn((double)S[3], -esc[3]);
-                        s[3] = s[5] = 0.0;
-                    }
-                    // next scales straight from the integer totals
-                    if (S[0] > 0 && S[1] > 0 && S[2] > 0) {
-                        const int e0 = fix_rescale(S[0], esc[0]), e1 = fix_rescale(S[1], esc[1]);
-                        esc[2] = fix_rescale(S[2], esc[2]);
-                        esc[3] = (e0 + e1) / 2 - 1;   // |<r, Ap>| <= |r| |Ap|
-                        esc[0] = e0;
-                        esc[1] = e1;
-                        s_cnt[1] = 2;   // scales already set
-                    } else {
-                        s_cnt[1] = 3;   // no usable scales: the next sums go through the tile partials
-                    }
+                long long Sv = 0;
+                bool okl = true, conv = true;
+                FF fv = {0.f, 0.f};
+                int er = 0, due = 0;
+                if (lane < 4) {
+                    Sv = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[lane][0]));
+                    okl = Sv < kFixLimit && Sv > -kFixLimit;
+                    conv = okl && fix_to_ff(Sv, esc[lane], fv);
+                    if (lane < 3 && Sv > 0) er = fix_rescale(Sv, esc[lane]);
+                } else if (lane == 4) {
+                    okl = ld_word(reinterpret_cast<const unsigned long long*>(&f[0][kFixOverflowWord])) == 0ull;
+                } else if (lane == 5) {
+                    due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
                 }
-                s_cnt[0] = ok ? (done ? 2 : 1) : 0;
+                const bool ok = __all_sync(full, okl);
+                const bool convall = __all_sync(full, conv);
+                const bool pos = __all_sync(full, lane >= 3 || Sv > 0);
+                FF v[4];
+                long long S[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    v[c] = FF{__shfl_sync(full, fv.hi, c), __shfl_sync(full, fv.lo, c)};
+                    S[c] = __shfl_sync(full, Sv, c);
+                }
+                const int e0 = __shfl_sync(full, er, 0), e1 = __shfl_sync(full, er, 1), e2 = __shfl_sync(full, er, 2);
+                due = __shfl_sync(full, due, 5);
+                YK_QMARK(4);
+                __syncwarp();   // every lane has read esc
+                if (lane == 0) {
+                    bool done = false;
+                    if (ok) {
+                        // the ordinary step on the FP32 pipes; the FP64 one otherwise
+                        done = convall && lst.mode != kIdle && fast_step(a, k, v[0], v[1], v[2], v[3], due != 0, lst, fs, L);
+                        if (!done) {
+                            s[0] = scalbn((double)S[0], -esc[0]);
+                            s[1] = scalbn((double)S[1], -esc[1]);
+                            s[2] = scalbn((double)S[2], -esc[2]);
+                            s[4] = scalbn((double)S[3], -esc[3]);
+                            s[3] = s[5] = 0.0;
+                        }
+                        // next scales straight from the integer totals
+                        if (pos) {
+                            esc[0] = e0;
+                            esc[1] = e1;
+                            esc[2] = e2;
+                            esc[3] = (e0 + e1) / 2 - 1;   // |<r, Ap>| <= |r| |Ap|
+                            s_scales = 2;   // scales already set
+                        } else {
+                            s_scales = 3;   // no usable scales: the next sums go through the tile partials
+                        }
+                    }
+                    s_dec = ok ? (done ? 2 : 1) : 0;
+                    YK_QMARK(5);
+                }
             }
+            // s_dec is written again only after the barriers of the passes that follow
             __syncthreads();
-            fast = s_cnt[0] != 0;
-            stepped = s_cnt[0] == 2;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                s_cnt[0] = 0;
-                s_scales = s_cnt[1];
-                s_cnt[1] = 0;
-            }
+            fast = s_dec != 0;
+            stepped = s_dec == 2;
         }
     }
     if (!fast) sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
@@ -1089,9 +1161,10 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
     const long long q2 = clock64();
 #endif
     if (threadIdx.x == 0 && stepped) {
+        // (the host-visible state is stored by the FP64 steps: every solve
+        // ends in one)
         *s_nact = 1;
         *s_anyru = lst.mode == kRu;
-        if (blockIdx.x == 0) store_state(a.st + a.sys_first, lst);
         *s_fast = s_scales == 2 ? 1 : 0;
     } else if (threadIdx.x == 0) {
         if (fs.valid) {
@@ -1136,6 +1209,7 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
             }
         }
     }
+    YK_QMARK(6);
 #ifdef YK_CG_TIMING
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         atomicAdd(&g_cg_f[0], (unsigned long long)(q1 - q0));
@@ -1145,7 +1219,19 @@ __device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, 
     }
 #endif
     __syncthreads();
+    YK_QMARK(7);
     return true;
+}
+
+// Out of line for cg_kernel, whose registers do not leave room for it inline;
+// cg_halo_kernel inlines the body (a call costs a save and restore of
+// registers through local memory, which the barrier's acquire leaves cold).
+template <int K, bool MIXED>
+__device__ __noinline__ bool solo_reduce(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red, CGState& lst,
+                                         SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt, int* esc, int* s_fast,
+                                         FastShadow& fs)
+{
+    return solo_reduce_body<K, MIXED>(a, gen, k, ru_round, red, lst, L, s_nact, s_anyru, s_cnt, esc, s_fast, fs);
 }
 
 template <typename W, bool MIXED>
@@ -1313,7 +1399,13 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool w
         a.partial[tile].f[i] = make_float2(t.hi, t.lo);
         if (fsum) {
             const int c = fix_value_of_slot(i);
-            if (c >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(&fsum[c][0]), (unsigned long long)to_fixed(t, esc[c]));
+            if (c >= 0) {
+                const long long v = to_fixed(t, esc[c]), lim = fix_tile_limit(a.tile_end - a.tile_begin);
+                if (v < lim && v > -lim)
+                    atomicAdd(reinterpret_cast<unsigned long long*>(&fsum[c][0]), (unsigned long long)v);
+                else
+                    atomicOr(reinterpret_cast<unsigned long long*>(&fsum[0][kFixOverflowWord]), 1ull);
+            }
         }
     }
 }
@@ -1731,6 +1823,13 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     __shared__ int s_esc[4], s_fast;
     __shared__ CGState lst;
     __shared__ FastShadow fsh;
+    // the system record in shared memory: the grid barrier's fence leaves L1
+    // cold, and the vector addresses would otherwise cost a round trip to L2
+    // before every pass
+    __shared__ SysDev S;
+    // and the arguments, for the reduction (a function of its own, which
+    // would otherwise read them through memory too)
+    __shared__ CGArgs sa;
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
@@ -1742,8 +1841,10 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         lst.iters = lst.converged = lst.status = lst.n_ru = 0;
         lst.mode = kStep;
         fsh.valid = 0;
+        S = a.sys[a.sys_first];
+        sa = a;
     }
-    const SysDev& S = a.sys[a.sys_first];
+    __syncthreads();
     const int Nt = S.Nt, Nx = S.Nx, V = S.V;
     const int n0 = a.tiles[tb].y;
     const int n1 = min(a.tiles[te - 1].y + kTile, V);
@@ -1842,7 +1943,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         float* Ac = cur == 0 ? S.Ap32 : S.t32;
         for (int base = tb; base < te; base += 2) {   // the same trip count in every thread
             const int tile = base + hf;
-            const int n = tile < te ? a.tiles[tile].y + ts : V;
+            const int n = tile < te ? n0 + (tile - tb) * kTile + ts : V;   // the tiles are contiguous
             const bool on = n < V;
             W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
             if (on) {
@@ -1868,7 +1969,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     };
 
     auto reduce = [&](int kk, bool ru) -> bool {
-        return solo_reduce<K, true>(a, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh);
+        return solo_reduce_body<K, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh);
     };
 
     // ---------------- round 0: b, x = 0, r_0 = p_0 = b; t = D_first p_0; B(0)
@@ -1935,7 +2036,15 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         volatile unsigned long long* f = g_cg_f;
         printf("cg timing (finisher, cycles per event): sums %llu (loads %llu)  scalar %llu  tail %llu\n",
                f[0] / (f[3] ? f[3] : 1), f[4] / (f[3] ? f[3] : 1), f[1] / (f[3] ? f[3] : 1), f[2] / (f[3] ? f[3] : 1));
+        volatile unsigned long long* q = g_cg_q;
+        const unsigned long long nq = f[3] ? f[3] : 1;
+        printf("cg timing (reduction marks): entry-sync %llu  fence+arrive %llu  wait %llu  fence+sync %llu  "
+               "loads %llu  step %llu  bcast %llu  end-sync %llu\n",
+               q[0] / nq, q[1] / nq, q[2] / nq, q[3] / nq, q[4] / nq, q[5] / nq, q[6] / nq, q[7] / nq);
+        printf("cg timing (fast step marks): convert %llu  alpha %llu  estimate %llu  triggers %llu  state %llu\n",
+               q[8] / nq, q[9] / nq, q[10] / nq, q[11] / nq, q[12] / nq);
         for (int i = 0; i < 8; ++i) f[i] = 0;
+        for (int i = 0; i < 16; ++i) q[i] = 0;
     }
 #endif
 }
@@ -1968,8 +2077,10 @@ __global__ void cg_prepare_kernel(CGArgs a)
         *a.any_ru = 0;
         a.bar->arrive = 0u;
         a.bar->gword = 0ull;
-        for (int b = 0; b < 3; ++b)
+        for (int b = 0; b < 3; ++b) {
             for (int c = 0; c < 4; ++c) a.bar->fsum[b][c][0] = 0;
+            a.bar->fsum[b][0][kFixOverflowWord] = 0;
+        }
         *a.err = 0;
     }
 }
