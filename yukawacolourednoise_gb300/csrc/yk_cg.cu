@@ -1038,10 +1038,17 @@ __device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red
 // (finisher's loads, release, the others' polls of the published words) is
 // replaced by one round of loads in every block.  Block 0 keeps the
 // host-visible CGState up to date.
-template <int K, bool MIXED>
+// after_barrier() runs in every thread once the barrier has been passed
+// (the other blocks' writes of the pass are visible), before the scalar
+// work: the halo kernel issues the next pass's loads there.
+struct NoHook {
+    __device__ void operator()() const {}
+};
+
+template <int K, bool MIXED, typename Hook = NoHook>
 __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red,
                                                  CGState& lst, SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt,
-                                                 int* esc, int* s_fast, FastShadow& fs)
+                                                 int* esc, int* s_fast, FastShadow& fs, Hook after_barrier = Hook())
 {
     constexpr bool kFix = MIXED && K == 1;   // fixed-point sums available
     int bad = 0;   // thread 0: its wait gave up
@@ -1077,6 +1084,19 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
     }
     ++gen;
     if (__syncthreads_or(bad)) return false;
+    // the fixed-point totals of this barrier, if the tiles added them: lanes
+    // 0-3 load one each, lane 4 the overflow flag -- ahead of the hook's loads
+    const bool fix_now = kFix && !ru_round && *s_fast;
+    long long Sv = 0;
+    unsigned long long over_v = 0ull;
+    if (fix_now && threadIdx.x < 5) {
+        const long long(*f)[16] = a.bar->fsum[gen % 3u];
+        if (threadIdx.x < 4)
+            Sv = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[threadIdx.x][0]));
+        else
+            over_v = ld_word(reinterpret_cast<const unsigned long long*>(&f[0][kFixOverflowWord]));
+    }
+    after_barrier();
     YK_QMARK(3);
     double s[6];
 #ifdef YK_CG_TIMING
@@ -1087,25 +1107,22 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
     int s_scales = 0;   // thread 0: 2 = next scales set from the integer totals
     __shared__ int s_dec;   // thread 0's verdict on the fixed-point totals (0 none, 1 sums, 2 stepped)
     if constexpr (kFix) {
-        if (!ru_round && *s_fast) {
+        if (fix_now) {
             if (threadIdx.x < 32) {
                 // lanes 0-3: one total each (load, range check, conversion,
                 // next scale); lane 4: the overflow flag; lane 5: the
                 // periodic trigger; lane 0 then steps
                 const unsigned full = 0xffffffffu;
                 const int lane = threadIdx.x;
-                const long long(*f)[16] = a.bar->fsum[gen % 3u];
-                long long Sv = 0;
                 bool okl = true, conv = true;
                 FF fv = {0.f, 0.f};
                 int er = 0, due = 0;
                 if (lane < 4) {
-                    Sv = (long long)ld_word(reinterpret_cast<const unsigned long long*>(&f[lane][0]));
                     okl = Sv < kFixLimit && Sv > -kFixLimit;
                     conv = okl && fix_to_ff(Sv, esc[lane], fv);
                     if (lane < 3 && Sv > 0) er = fix_rescale(Sv, esc[lane]);
                 } else if (lane == 4) {
-                    okl = ld_word(reinterpret_cast<const unsigned long long*>(&f[0][kFixOverflowWord])) == 0ull;
+                    okl = over_v == 0ull;
                 } else if (lane == 5) {
                     due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
                 }
@@ -1754,12 +1771,20 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
 // each side (2 Nx sites), from r, A p and p of the previous iteration, which
 // the grid barrier of that iteration has completed; applies D_first on the
 // range widened by one slice; and applies D_second on its own sites -- both
-// stencils in shared memory.  An iteration is then one round of loads, two
-// shared-memory stencils and the reducing grid barrier: no neighbour
-// synchronisation and no round trip of D p through L2.  The price is the
-// redundant work on the four halo slices, so the launcher takes this kernel
-// only while 4 Nx <= 2 (n1 - n0) (and the widened range fits the lattice and
-// shared memory).
+// stencils in shared memory.  An iteration is then one round of bulk copies
+// into shared memory, two shared-memory stencils and the reducing grid
+// barrier: no neighbour synchronisation and no round trip of D p through L2.
+// The price is the redundant work on the four halo slices, so the launcher
+// takes this kernel only while 4 Nx <= 2 (n1 - n0) (and the widened range fits
+// the lattice and shared memory).
+//
+// The widened range of r, A p and p (and x on the own sites) is staged into
+// shared memory with asynchronous copies (cp.async, each thread the sites it
+// forms in A1), issued as soon as the barrier of the previous iteration has
+// been passed -- before that iteration's scalar step, on the guess that the
+// next iteration is an ordinary step -- so the copies travel while warp 0
+// loads the sums and steps the recurrence, and hold no registers meanwhile.
+// A1 then forms p (and r) in place in the staging buffers.
 //
 // Per site the arithmetic is that of cg_kernel<1, true> (the same formation
 // of r and p, the same stencil calls, the same tile partials and fixed-point
@@ -1769,7 +1794,6 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
 // reliable updates run as in cg_kernel, with neighbour synchronisation.
 // ---------------------------------------------------------------------------
 constexpr int kHaloThreads = 2 * kTile;
-constexpr int kHaloChunk = 3;   // P-range sites per thread loaded together
 
 __device__ __forceinline__ int wrap_site(int m, int V) { return m < 0 ? m + V : (m >= V ? m - V : m); }
 
@@ -1789,19 +1813,38 @@ __device__ __forceinline__ void st_sm(float4* s, int j, const Site<float, 1>& v)
     s[j] = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
 }
 
+// Shared-memory address and the per-thread asynchronous copy (cp.async, 16
+// bytes, L2 only: the barrier's acquire is what makes other blocks' writes
+// visible, and no line of them may come from this SM's L1).
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // D (DAG = false) or D^dag (DAG = true) at site m from a shared-memory copy
 // `in` of a contiguous site range holding m at index j and both of m's time
-// slices; diag at m given.
+// slices; diag at m given.  sh = log2 Nx when Nx is a power of two, else -1.
 template <bool DAG>
-__device__ __forceinline__ Site<float, 1> apply_d_sm(const float4* in, int j, int m, int Nt, int Nx, float diag, float r)
+__device__ __forceinline__ Site<float, 1> apply_d_sm(const float4* in, int j, int m, int Nt, int Nx, int sh, float diag,
+                                                     float r)
 {
-    const Nbr nb = neighbours(m, Nt, Nx);
+    const int t = sh >= 0 ? (m >> sh) : m / Nx;
+    const int x = m - t * Nx;
+    const int ju = j + ((x + 1 == Nx) ? 1 - Nx : 1);   // the hops of neighbours(), as offsets
+    const int jd = j + ((x == 0) ? Nx - 1 : -1);
+    const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
     const Site<float, 1> c = ld_sm(in, j);
     const Site<float, 1> tu = ld_sm(in, j + Nx);
     const Site<float, 1> td = ld_sm(in, j - Nx);
-    const Site<float, 1> xu = ld_sm(in, j + (int)(nb.xu - m));
-    const Site<float, 1> xd = ld_sm(in, j + (int)(nb.xd - m));
-    return dirac_combine<float, 1, DAG>(c, tu, td, xu, xd, diag, r, nb.sp, nb.sm);
+    const Site<float, 1> xu = ld_sm(in, ju);
+    const Site<float, 1> xd = ld_sm(in, jd);
+    return dirac_combine<float, 1, DAG>(c, tu, td, xu, xd, diag, r, sp, sm);
 }
 
 enum { kHaloInit = 0 };   // A1 of round 0: p_0 = b as stored
@@ -1823,12 +1866,11 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     __shared__ int s_esc[4], s_fast;
     __shared__ CGState lst;
     __shared__ FastShadow fsh;
-    // the system record in shared memory: the grid barrier's fence leaves L1
+    // the system record in shared memory: the grid barrier's acquire leaves L1
     // cold, and the vector addresses would otherwise cost a round trip to L2
     // before every pass
     __shared__ SysDev S;
-    // and the arguments, for the reduction (a function of its own, which
-    // would otherwise read them through memory too)
+    // and the arguments, for the reduction
     __shared__ CGArgs sa;
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
@@ -1846,14 +1888,18 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     }
     __syncthreads();
     const int Nt = S.Nt, Nx = S.Nx, V = S.V;
+    const int sh = (Nx & (Nx - 1)) == 0 ? __ffs(Nx) - 1 : -1;
     const int n0 = a.tiles[tb].y;
     const int n1 = min(a.tiles[te - 1].y + kTile, V);
     const int own = n1 - n0;
     const int nP = own + 4 * Nx, nT = own + 2 * Nx;
-    float4* p_s = hsm;                                   // p_k on [n0 - 2 Nx, n1 + 2 Nx)
-    float4* t_s = p_s + nP;                              // D_first p_k on [n0 - Nx, n1 + Nx)
-    float4* r_s = t_s + nT;                              // r_k on [n0, n1)
-    float* d_s = reinterpret_cast<float*>(r_s + own);    // diag on [n0 - Nx, n1 + Nx)
+    const int pfirst = wrap_site(n0 - 2 * Nx, V);        // first site of the widened range
+    float4* P_st = hsm;                                  // p on [n0 - 2 Nx, n1 + 2 Nx): staged p_{k-1}, then p_k
+    float4* R_st = P_st + nP;                            // r there: staged r_{k-1}, then r_k on the own sites
+    float4* A_st = R_st + nP;                            // A p_{k-1} there
+    float4* X_st = A_st + nP;                            // x increment on [n0, n1)
+    float4* t_s = X_st + own;                            // D_first p_k on [n0 - Nx, n1 + Nx)
+    float* d_s = reinterpret_cast<float*>(t_s + nT);     // diag on [n0 - Nx, n1 + Nx)
     const bool first_dag = (a.mtype == YK_NORMAL);       // Normal: A = D D^dag, apply D^dag first
     const float rw = (float)S.r;
     for (int j = threadIdx.x; j < nT; j += kHaloThreads) {
@@ -1861,70 +1907,67 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         d_s[j] = (float)(2.0 * S.r + S.m0 + S.g * S.sigma[m]);
     }
     unsigned epoch = 0, gen = 0;
+    int staged_k = -1;   // the iteration whose ordinary-step staging is in flight
 #ifdef YK_CG_TIMING
     long long tacc[5] = {0, 0, 0, 0, 0}, tlast = clock64();
     int tit = 0;
 #endif
 
-    // A1: p_k (and r_k, x_k on the own sites) on the widened range
+    // Stages the inputs of A1 for `mode`, each thread the sites it forms in
+    // A1: kStep: r, A p, p of iteration prv and x; kRedo: r of cur and p of
+    // prv; round 0: r and p as stored.
+    auto stage = [&](int mode, int cur, int prv) {
+        const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
+        const float* Pl = S.p32[prv];
+        const float* Al = prv == 0 ? S.Ap32 : S.t32;
+        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
+            const int m = wrap_site(pfirst + j, V);
+            const int o = j - 2 * Nx;
+            cp_async16(P_st + j, Pl + 4 * (size_t)m);
+            cp_async16(R_st + j, Rl + 4 * (size_t)m);
+            if (mode == kStep) {
+                cp_async16(A_st + j, Al + 4 * (size_t)m);
+                if (o >= 0 && o < own) cp_async16(X_st + o, S.xs32 + 4 * (size_t)m);
+            }
+        }
+        cp_async_commit();
+    };
+    // this thread's staging copies have landed (A1 reads only its own sites)
+    auto stage_wait = [&]() -> bool {
+        cp_async_wait_all();
+        return true;
+    };
+
+    // A1: p_k (and r_k, x_k on the own sites) on the widened range, in place
     auto pass_a1 = [&](int mode, int cur, int prv) {
         const SysLocal& L = sl[0];
         const W ar = L.f_alpha_re, beta = L.f_beta, cre = L.f_c_re, cim = L.f_c_im;
-        const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
-        const float* Al = prv == 0 ? S.Ap32 : S.t32;
-        const float* Pl = (mode == kHaloInit) ? S.p32[0] : S.p32[prv];
-        for (int base = 0; base < nP; base += kHaloThreads * kHaloChunk) {
-            Site<W, K> rv[kHaloChunk], av[kHaloChunk], pv[kHaloChunk], xv[kHaloChunk];
-            int mm[kHaloChunk], oo[kHaloChunk];
+        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
+            const int o = j - 2 * Nx;
+            const bool is_own = o >= 0 && o < own;
+            const int m = n0 + o;   // an own site when is_own
+            const Site<W, K> po = ld_sm(P_st, j);
+            Site<W, K> p;
+            if (mode == kStep) {
+                Site<W, K> r = ld_sm(R_st, j);
+                site_axpy<W, K>(r, -ar, W(0), ld_sm(A_st, j));
 #pragma unroll
-            for (int g = 0; g < kHaloChunk; ++g) {
-                const int j = base + g * kHaloThreads + threadIdx.x;
-                mm[g] = -1;
-                oo[g] = -1;
-                if (j >= nP) continue;
-                const int m = wrap_site(n0 - 2 * Nx + j, V);
-                const int o = j - 2 * Nx;
-                mm[g] = m;
-                oo[g] = (o >= 0 && o < own) ? o : -1;
-                pv[g] = YK_LD(W, K, Pl, m);
-                if (mode == kStep) {
-                    rv[g] = YK_LD(W, K, Rl, m);
-                    av[g] = YK_LD(W, K, Al, m);
-                    if (oo[g] >= 0) xv[g] = YK_LD(W, K, S.xs32, m);
-                } else if (mode == kRedo) {
-                    rv[g] = YK_LD(W, K, Rl, m);
+                for (int i = 0; i < 4; ++i) p.v[i] = fma(beta, po.v[i], r.v[i]);
+                if (is_own) {
+                    Site<W, K> x = ld_sm(X_st, o);
+                    site_axpy<W, K>(x, ar, W(0), po);
+                    YK_ST(W, K, S.xs32, m, x);
+                    YK_ST(W, K, S.r32[cur], m, r);
+                    YK_ST(W, K, S.p32[cur], m, p);
+                    st_sm(R_st, j, r);
                 }
+            } else if (mode == kRedo) {
+                p = p_next<W, K>(ld_sm(R_st, j), po, beta, cre, cim);
+                if (is_own) YK_ST(W, K, S.p32[cur], m, p);
+            } else {
+                p = po;   // round 0: r_0 = p_0 = b, both staged
             }
-#pragma unroll
-            for (int g = 0; g < kHaloChunk; ++g) {
-                if (mm[g] < 0) continue;
-                const int j = base + g * kHaloThreads + threadIdx.x, m = mm[g], o = oo[g];
-                Site<W, K> p;
-                if (mode == kStep) {
-                    Site<W, K> r = rv[g];
-                    site_axpy<W, K>(r, -ar, W(0), av[g]);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) p.v[i] = fma(beta, pv[g].v[i], r.v[i]);
-                    if (o >= 0) {
-                        Site<W, K> x = xv[g];
-                        site_axpy<W, K>(x, ar, W(0), pv[g]);
-                        YK_ST(W, K, S.xs32, m, x);
-                        YK_ST(W, K, S.r32[cur], m, r);
-                        YK_ST(W, K, S.p32[cur], m, p);
-                        st_sm(r_s, o, r);
-                    }
-                } else if (mode == kRedo) {
-                    p = p_next<W, K>(rv[g], pv[g], beta, cre, cim);
-                    if (o >= 0) {
-                        YK_ST(W, K, S.p32[cur], m, p);
-                        st_sm(r_s, o, rv[g]);
-                    }
-                } else {
-                    p = pv[g];
-                    if (o >= 0) st_sm(r_s, o, p);   // r_0 = p_0 = b
-                }
-                st_sm(p_s, j, p);
-            }
+            st_sm(P_st, j, p);
         }
     };
 
@@ -1932,8 +1975,8 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     auto pass_a2 = [&]() {
         for (int j = threadIdx.x; j < nT; j += kHaloThreads) {
             const int m = wrap_site(n0 - Nx + j, V);
-            const Site<W, K> t = first_dag ? apply_d_sm<true>(p_s, j + Nx, m, Nt, Nx, d_s[j], rw)
-                                           : apply_d_sm<false>(p_s, j + Nx, m, Nt, Nx, d_s[j], rw);
+            const Site<W, K> t = first_dag ? apply_d_sm<true>(P_st, j + Nx, m, Nt, Nx, sh, d_s[j], rw)
+                                           : apply_d_sm<false>(P_st, j + Nx, m, Nt, Nx, sh, d_s[j], rw);
             st_sm(t_s, j, t);
         }
     };
@@ -1948,11 +1991,11 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
             W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
             if (on) {
                 const int o = n - n0, jt = o + Nx;
-                const Site<W, K> ap = first_dag ? apply_d_sm<false>(t_s, jt, n, Nt, Nx, d_s[jt], rw)
-                                                : apply_d_sm<true>(t_s, jt, n, Nt, Nx, d_s[jt], rw);
+                const Site<W, K> ap = first_dag ? apply_d_sm<false>(t_s, jt, n, Nt, Nx, sh, d_s[jt], rw)
+                                                : apply_d_sm<true>(t_s, jt, n, Nt, Nx, sh, d_s[jt], rw);
                 YK_ST(W, K, Ac, n, ap);
-                const Site<W, K> r = ld_sm(r_s, o);
-                const Site<W, K> p = ld_sm(p_s, o + 2 * Nx);
+                const Site<W, K> r = ld_sm(R_st, o + 2 * Nx);
+                const Site<W, K> p = ld_sm(P_st, o + 2 * Nx);
                 v[0] = site_norm2<W, K>(r);
                 v[1] = site_norm2<W, K>(ap);
                 site_dot<W, K>(p, ap, v[2], v[3]);
@@ -1969,7 +2012,16 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     };
 
     auto reduce = [&](int kk, bool ru) -> bool {
-        return solo_reduce_body<K, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh);
+        // once the barrier of an ordinary iteration is passed, stage the next
+        // one on the guess that it is an ordinary step too
+        auto prefetch = [&]() {
+            if (ru) return;
+            const int k1 = kk + 1;
+            stage(kStep, k1 & 1, (k1 & 1) ^ 1);
+            staged_k = k1;
+        };
+        return solo_reduce_body<K, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh,
+                                         prefetch);
     };
 
     // ---------------- round 0: b, x = 0, r_0 = p_0 = b; t = D_first p_0; B(0)
@@ -1992,6 +2044,8 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         YK_ST(W, K, S.p32[0], n, bw);
     }
     if (!nsync(a, ++epoch, deps)) return;
+    stage(kHaloInit, 0, 0);
+    if (!stage_wait()) return;
     pass_a1(kHaloInit, 0, 0);
     __syncthreads();
     pass_a2();
@@ -2002,9 +2056,14 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     int k = 1;
     while (k <= a.max_iter) {   // the system retires at k = max_iter at the latest
         YK_TMARK(0);   // grid reduction
+        const int mode = sl[0].mode;
+        if (s_nact == 0 || mode == kRu) {
+            // the guessed staging is not used: let it land before going on
+            if (staged_k == k && !stage_wait()) return;
+            staged_k = -1;
+        }
         if (s_nact == 0) break;
         const int cur = k & 1, prv = cur ^ 1;
-        const int mode = sl[0].mode;
         if (mode == kRu) {
             for (int tile = tb + hf; tile < te; tile += 2) {
                 const int n = a.tiles[tile].y + ts;
@@ -2015,6 +2074,12 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
             if (!reduce(k, true)) return;
             continue;   // same k: redo A(k) from the FP64 residual
         }
+        if (!(mode == kStep && staged_k == k)) {
+            if (staged_k == k && !stage_wait()) return;   // a guess for another mode
+            stage(mode, cur, prv);
+        }
+        staged_k = -1;
+        if (!stage_wait()) return;
         pass_a1(mode, cur, prv);
         __syncthreads();
         YK_TMARK(1);
@@ -2049,11 +2114,12 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
 #endif
 }
 
-// Shared memory of cg_halo_kernel for own sites per block and Nx.
+// Shared memory of cg_halo_kernel for own sites per block and Nx: the staged
+// widened range (p, r, A p), the own x increment, D_first p and diag.
 static size_t halo_smem_bytes(int own, int Nx)
 {
     const size_t nP = (size_t)own + 4 * (size_t)Nx, nT = (size_t)own + 2 * (size_t)Nx;
-    return (nP + nT + (size_t)own) * sizeof(float4) + nT * sizeof(float);
+    return (3 * nP + (size_t)own + nT) * sizeof(float4) + nT * sizeof(float);
 }
 
 // Resets the barrier, flags, counters and per-system state before a solve.
@@ -2130,7 +2196,7 @@ int cg_grid_for(int ntiles, int maxg, int* tiles_per_block)
     return grid;
 }
 
-constexpr size_t kHaloMaxSmem = 200 * 1024;
+constexpr size_t kHaloMaxSmem = 216 * 1024;
 
 // Whether cg_halo_kernel takes a single-system solve on an Nt x Nx lattice
 // whose blocks own tpb tiles each: at most 8 tiles per block, halo work at
