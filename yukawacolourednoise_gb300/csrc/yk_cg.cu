@@ -1897,7 +1897,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     float4* P_st = hsm;                                  // p on [n0 - 2 Nx, n1 + 2 Nx): staged p_{k-1}, then p_k
     float4* R_st = P_st + nP;                            // r there: staged r_{k-1}, then r_k on the own sites
     float4* A_st = R_st + nP;                            // A p_{k-1} there
-    float4* X_st = A_st + nP;                            // x increment on [n0, n1)
+    float4* X_st = A_st + nP;                            // x increment on [n0, n1), kept here all solve
     float4* t_s = X_st + own;                            // D_first p_k on [n0 - Nx, n1 + Nx)
     float* d_s = reinterpret_cast<float*>(t_s + nT);     // diag on [n0 - Nx, n1 + Nx)
     const bool first_dag = (a.mtype == YK_NORMAL);       // Normal: A = D D^dag, apply D^dag first
@@ -1914,21 +1914,17 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
 #endif
 
     // Stages the inputs of A1 for `mode`, each thread the sites it forms in
-    // A1: kStep: r, A p, p of iteration prv and x; kRedo: r of cur and p of
-    // prv; round 0: r and p as stored.
+    // A1: kStep: r, A p, p of iteration prv; kRedo: r of cur and p of prv;
+    // round 0: r and p as stored.
     auto stage = [&](int mode, int cur, int prv) {
         const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
         const float* Pl = S.p32[prv];
         const float* Al = prv == 0 ? S.Ap32 : S.t32;
         for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
             const int m = wrap_site(pfirst + j, V);
-            const int o = j - 2 * Nx;
             cp_async16(P_st + j, Pl + 4 * (size_t)m);
             cp_async16(R_st + j, Rl + 4 * (size_t)m);
-            if (mode == kStep) {
-                cp_async16(A_st + j, Al + 4 * (size_t)m);
-                if (o >= 0 && o < own) cp_async16(X_st + o, S.xs32 + 4 * (size_t)m);
-            }
+            if (mode == kStep) cp_async16(A_st + j, Al + 4 * (size_t)m);
         }
         cp_async_commit();
     };
@@ -1956,7 +1952,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
                 if (is_own) {
                     Site<W, K> x = ld_sm(X_st, o);
                     site_axpy<W, K>(x, ar, W(0), po);
-                    YK_ST(W, K, S.xs32, m, x);
+                    st_sm(X_st, o, x);
                     YK_ST(W, K, S.r32[cur], m, r);
                     YK_ST(W, K, S.p32[cur], m, p);
                     st_sm(R_st, j, r);
@@ -2039,7 +2035,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
             bw.v[i] = (W)bv.v[i];
         }
         YK_ST(double, K, S.x, n, z);
-        YK_ST(W, K, S.xs32, n, zw);
+        st_sm(X_st, n - n0, zw);
         YK_ST(W, K, S.r32[0], n, bw);
         YK_ST(W, K, S.p32[0], n, bw);
     }
@@ -2065,9 +2061,25 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         if (s_nact == 0) break;
         const int cur = k & 1, prv = cur ^ 1;
         if (mode == kRu) {
-            for (int tile = tb + hf; tile < te; tile += 2) {
-                const int n = a.tiles[tile].y + ts;
-                if (n < V) ru_fold<K>(S, n, sl[0], prv);
+            // fold x_k = x + xs + alpha p_{k-1} into the FP64 x; xs = 0 (as ru_fold,
+            // with the increment from shared memory)
+            const SysLocal& L = sl[0];
+            for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+                const int n = n0 + o;
+                Site<double, K> xv = YK_LD(double, K, S.x, n);
+                const Site<W, K> xs = ld_sm(X_st, o);
+                const Site<W, K> pv = YK_LD(W, K, S.p32[prv], n);
+                Site<double, K> pd;
+                Site<W, K> zw;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    xv.v[i] += (double)xs.v[i];
+                    pd.v[i] = (double)pv.v[i];
+                    zw.v[i] = W(0);
+                }
+                site_axpy<double, K>(xv, L.alpha_re, L.alpha_im, pd);
+                YK_ST(double, K, S.x, n, xv);
+                st_sm(X_st, o, zw);
             }
             if (!nsync(a, ++epoch, deps)) return;
             if (!ru_residual<K>(a, sl, tslot, tb, te, first_dag, cur, prv, epoch, deps, red)) return;
