@@ -111,7 +111,7 @@ def peaks() -> dict:
 
 def ncu_traffic():
     """DRAM bytes per CG launch from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "cg_kernel_256x256_traffic.json"
+    f = ROOT / "profiles" / "cg_halo_kernel_256x256_traffic.json"
     if f.exists():
         try:
             return json.loads(f.read_text())
