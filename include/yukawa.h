@@ -82,7 +82,7 @@ typedef struct yk_params {
     int cg_max_iter;           /* 1000 (reference)                                */
     int reliable_every;        /* mixed: also an FP64 update every N iters (0 off)*/
     double reliable_delta;     /* mixed: FP64 update when |r| < delta * max |r|   */
-                               /*   since the last one (0.01)                   */
+                               /*   since the last one (0.001)                  */
     double fixed_dt;           /* > 0: fixed Euler step instead of adaptive eps   */
     int init;                  /* YK_INIT_DRAND48 (reference), YK_INIT_PHILOX     */
 } yk_params;

@@ -116,7 +116,7 @@ struct yk_ctx {
     int max_nx = 1, max_cols = 1;
     // solver settings (shared by all chains of a context)
     int precision = YK_FP64, tol_mode = YK_TOL_ABS, max_iter = 1000, reliable_every = 0;
-    double reliable_delta = 0.01;
+    double reliable_delta = 0.001;
     double tol = 1e-8;
     // step graph
     cudaGraphExec_t gexec = nullptr;

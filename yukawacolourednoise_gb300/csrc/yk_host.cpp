@@ -266,7 +266,7 @@ void yk_params_default(yk_params* p)
     p->cg_tol = 1e-8;
     p->cg_max_iter = 1000;
     p->reliable_every = 0;
-    p->reliable_delta = 0.01;
+    p->reliable_delta = 0.001;
     p->fixed_dt = 0.0;
     p->init = YK_INIT_DRAND48;
 }
