@@ -89,6 +89,11 @@ struct yk_ctx {
     int dev = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // the step's noise runs on `aux` beside the CG when the CG leaves SMs free
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    int n_sm = 0;
+    bool noise_overlap = true;   // YK_NOISE_OVERLAP=0 at context creation: never
     std::vector<Chain> ch;
     void* mem = nullptr;
     // step tables
@@ -146,6 +151,21 @@ struct yk_ctx {
 namespace {
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// First columns of the column-pass strips (width cw) that hold a column
+// keeping some mode; a column kx keeps some mode exactly when it keeps (0, kx).
+std::vector<int> kept_strips(int Nt, int Nx, double cut_fraction, int cw)
+{
+    std::vector<uint8_t> keep;
+    momentum_keep(Nt, Nx, cut_fraction, keep);
+    std::vector<int> out;
+    for (int x0 = 0; x0 < Nx; x0 += cw) {
+        bool any = false;
+        for (int x = x0; x < x0 + cw && x < Nx; ++x) any = any || keep[x];
+        if (any) out.push_back(x0);
+    }
+    return out;
+}
 
 int check_params(const yk_params& p, int c)
 {
@@ -267,14 +287,33 @@ void prof_end(yk_ctx* ctx, int cls, cudaEvent_t a, int launches)
     ctx->prof_launches += launches;
 }
 
-// Enqueues one Langevin step of every chain.
+// Enqueues one Langevin step of every chain.  The coloured noise does not
+// depend on the step's CG: when the persistent CG (one block per SM) leaves
+// SMs free, the noise passes run on the auxiliary stream beside it, on at
+// most that many blocks, and the update waits for them.  Profiled steps run
+// the kernel classes one after the other.
 int enqueue_step(yk_ctx* ctx)
 {
     cudaEvent_t e = nullptr;
-    prof_begin(ctx, &e);
     NoiseTables nt = {ctx->d_rows, ctx->nrows, ctx->d_cols, ctx->ncols, ctx->d_white, ctx->nwhite};
-    YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
-    prof_end(ctx, 0, e, (ctx->nwhite > 0 ? 1 : 0) + (ctx->nrows > 0 ? 3 : 0));
+    int free_sm = 0;
+    if (ctx->noise_overlap && !ctx->profiling && !ctx->cg_cluster && ctx->nsys > 0 && ctx->nrows > 0) {
+        CGArgs g = base_args(ctx);
+        g.tile_begin = 0;
+        g.tile_end = ctx->n_sys_tiles;
+        free_sm = ctx->n_sm - cg_predict_grid(g, ctx->precision == YK_MIXED);
+    }
+    const bool overlap = free_sm >= 8;
+    if (overlap) {
+        YK_CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
+        YK_CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
+        YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->aux, free_sm));
+        YK_CK(cudaEventRecord(ctx->join_ev, ctx->aux));
+    } else {
+        prof_begin(ctx, &e);
+        YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
+        prof_end(ctx, 0, e, (ctx->nwhite > 0 ? 1 : 0) + (ctx->nrows > 0 ? 3 : 0));
+    }
     if (ctx->nsys > 0) {
         prof_begin(ctx, &e);
         CGArgs a = base_args(ctx);
@@ -306,8 +345,9 @@ int enqueue_step(yk_ctx* ctx)
     }
     StepArgs s = step_args(ctx);
     prof_begin(ctx, &e);
-    YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream));
+    YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream, ctx->d_state));
     prof_end(ctx, 2, e, 1);
+    if (overlap) YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));   // xi of this step
     prof_begin(ctx, &e);
     YK_CK(launch_update(s, ctx->d_state, ctx->stream));
     prof_end(ctx, 3, e, 1);
@@ -550,6 +590,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     YK_CK(cudaGetDevice(&ctx->dev));
     YK_CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
+    YK_CK(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    YK_CK(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+    YK_CK(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
+    YK_CK(cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, ctx->dev));
     ctx->precision = p0.precision;
     ctx->tol_mode = p0.cg_tol_mode;
     ctx->tol = p0.cg_tol;
@@ -579,6 +623,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         ctx->cluster_sites = sites;
         const char* he = getenv("YK_CG_HALO");
         ctx->cg_halo = !(he && he[0] == '0');
+        const char* ne = getenv("YK_NOISE_OVERLAP");
+        ctx->noise_overlap = !(ne && ne[0] == '0');
     }
 
     ctx->ch.resize(n_chains);
@@ -603,11 +649,11 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         nsite_tiles += nt;
         if (C.filter) {
             C.row0 = nrows;
-            C.nrows = C.Nt;
-            nrows += C.Nt;
+            C.nrows = (C.Nt + 1) / 2;   // row pairs
+            nrows += C.nrows;
             const int cw = noise_strip(C.Nt);
             C.col0 = ncols;
-            C.ncols = (C.Nx + cw - 1) / cw;
+            C.ncols = (int)kept_strips(C.Nt, C.Nx, C.p.cut_fraction, cw).size();
             ncols += C.ncols;
             if (C.Nx > ctx->max_nx) ctx->max_nx = C.Nx;
             const int ce = C.Nt * (cw < C.Nx ? cw : C.Nx);
@@ -693,6 +739,9 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         cudaGetLastError();
         set_error("context allocation of %zu bytes failed", ar.used);
         cudaStreamDestroy(ctx->stream);
+        cudaStreamDestroy(ctx->aux);
+        cudaEventDestroy(ctx->fork_ev);
+        cudaEventDestroy(ctx->join_ev);
         return YK_ENOMEM;
     }
     ar.base = (char*)ctx->mem;
@@ -778,9 +827,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             for (int t = 0; t < nt; ++t) sys_tiles.push_back(make_int2(C.sys0 + j, t * kTile));
         }
         if (C.filter) {
-            for (int t = 0; t < C.Nt; ++t) rows.push_back(make_int2(c, t));
-            const int cw = noise_strip(C.Nt);
-            for (int x0 = 0; x0 < C.Nx; x0 += cw) cols.push_back(make_int2(c, x0));
+            for (int t = 0; t < C.Nt; t += 2) rows.push_back(make_int2(c, t));
+            for (int x0 : kept_strips(C.Nt, C.Nx, C.p.cut_fraction, noise_strip(C.Nt))) cols.push_back(make_int2(c, x0));
             std::vector<uint8_t> keep;
             momentum_keep(C.Nt, C.Nx, C.p.cut_fraction, keep);
             std::vector<double> twt, twx;
@@ -871,6 +919,12 @@ int yk_ctx_destroy(yk_ctx* ctx)
     for (auto& C : ctx->ch)
         if (C.ws.mem) cudaFree(C.ws.mem);
     if (ctx->mem) cudaFree(ctx->mem);
+    if (ctx->aux) {
+        cudaStreamSynchronize(ctx->aux);
+        cudaStreamDestroy(ctx->aux);
+    }
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return YK_OK;

@@ -575,6 +575,8 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         st.active = 0;
         st.converged = conv;
         st.status = status;
+        // a reliable-update round has just formed t64 = D_first x of this x
+        st.chi_ready = ru_round ? 1 : 0;
         return cv;
     };
     const double rr = s[0];
@@ -727,6 +729,7 @@ __device__ __forceinline__ void load_state(const CGState* p, CGState& st)
     st.status = v.status;
     st.n_ru = v.n_ru;
     st.mode = v.mode;
+    st.chi_ready = v.chi_ready;
 }
 
 __device__ __forceinline__ void store_state(CGState* p, const CGState& st)
@@ -743,6 +746,7 @@ __device__ __forceinline__ void store_state(CGState* p, const CGState& st)
     v.status = st.status;
     v.n_ru = st.n_ru;
     v.mode = st.mode;
+    v.chi_ready = st.chi_ready;
 }
 
 // The last block at a grid barrier: sums the partials of every system that
@@ -1561,7 +1565,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
         s_fast = 0;
         lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
         lst.active = 1;
-        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
+        lst.iters = lst.converged = lst.status = lst.n_ru = lst.chi_ready = 0;
         lst.mode = kStep;
         fsh.valid = 0;
     }
@@ -1880,7 +1884,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         s_fast = 0;
         lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
         lst.active = 1;
-        lst.iters = lst.converged = lst.status = lst.n_ru = 0;
+        lst.iters = lst.converged = lst.status = lst.n_ru = lst.chi_ready = 0;
         lst.mode = kStep;
         fsh.valid = 0;
         S = a.sys[a.sys_first];
@@ -2145,6 +2149,7 @@ __global__ void cg_prepare_kernel(CGArgs a)
         s.converged = 0;
         s.status = 0;
         s.n_ru = 0;
+        s.chi_ready = 0;
         s.mode = kStep;
         // generation 0: the coefficients of round 0 (never polled)
         for (int q = 0; q < 12; ++q) a.coef[i].w[q] = 0ull;
@@ -2239,6 +2244,12 @@ static int halo_max_grid()
 }
 
 void cg_halo_init() { halo_max_grid(); }
+
+int cg_predict_grid(const CGArgs& a, bool mixed)
+{
+    int tpb = 1;
+    return cg_grid_for(a.tile_end - a.tile_begin, mixed ? max_grid_t<1, true>() : max_grid_t<1, false>(), &tpb);
+}
 
 template <int K, bool MIXED>
 static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out, int* kernel_out)

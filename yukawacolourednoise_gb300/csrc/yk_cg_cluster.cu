@@ -568,6 +568,7 @@ __global__ void __launch_bounds__(kCThreads, 1) cg_cluster_kernel(CGArgs a)
         o.status = st.status;
         o.n_ru = st.n_ru;
         o.mode = 0;
+        o.chi_ready = 0;   // its reliable updates keep D x in shared memory
     }
     cl.sync();   // no CTA leaves while others may still read its shared memory
 }

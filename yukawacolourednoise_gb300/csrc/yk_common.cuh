@@ -228,6 +228,23 @@ __device__ __forceinline__ double warp_max(double v)
     return v;
 }
 
+// Block sum; result valid in thread 0.  scratch: >= 32 doubles.
+__device__ __forceinline__ double block_sum(double a, double* scratch)
+{
+    a = warp_sum(a);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[w] = a;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        r = lane < nw ? scratch[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
 // Block sum of two values; result valid in thread 0.  scratch: >= 2*32 doubles.
 __device__ __forceinline__ double2 block_sum2(double a, double b, double* scratch)
 {

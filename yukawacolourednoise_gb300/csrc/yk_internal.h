@@ -85,6 +85,7 @@ struct CGState {
     int status;
     int n_ru;            // reliable updates (mixed)
     int mode;            // the system's mode in the pass that follows
+    int chi_ready;       // the solve ended in a reliable update: t64 holds D_first x of the final x
 };
 
 // Per-system coefficients of the next pass (alpha: x += alpha p, r -= alpha A p;
@@ -144,6 +145,7 @@ struct ChainDev {
     yk_obs obs;          // last-step observables
     unsigned counter;    // finaliser counter of the update kernel
     unsigned counter2;
+    unsigned long long dmax_bits;   // max |drift| of the step as IEEE bits (atomic max; reset by the update)
     int status;
 };
 
@@ -160,7 +162,7 @@ struct StepArgs {
 
 // Block tables of the coloured-noise passes (built once per context).
 struct NoiseTables {
-    const int2* rows;    // (chain, t) for every chain whose cutoff removes modes
+    const int2* rows;    // (chain, t), t even: the row pairs of every chain whose cutoff removes modes
     int nrows;
     const int2* cols;    // (chain, first column) strips of width noise_strip(Nt)
     int ncols;
@@ -168,13 +170,14 @@ struct NoiseTables {
     int nwhite;
 };
 
-// Columns per block of the column pass: enough that the block's threads all
-// hold a butterfly (2 kBlock / Nt), so the FP64 transforms -- issued at 1/64
-// of the FP32 rate on GB300 -- spread over as many SMs as there are column
-// pairs (a 256 x 256 lattice: 128 blocks).
+// Columns per block of the column pass: kBlock / Nt, so that at Nt = 256 each
+// block transforms one column.  The FP64 transforms (issued at 1/64 of the
+// FP32 rate on GB300) are bound by the FP64 pipe of each SM, so the column
+// pass wants as many blocks as there are kept columns rather than busy
+// threads (half the block holds a butterfly at Nt = 256).
 YK_HD inline int noise_strip(int Nt)
 {
-    int cw = 2 * kBlock / Nt;
+    int cw = kBlock / Nt;
     if (cw > 64) cw = 64;
     if (cw < 1) cw = 1;
     return cw;

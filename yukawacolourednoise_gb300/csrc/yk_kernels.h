@@ -37,16 +37,24 @@ void noise_init_attributes();
 
 // Coloured noise of every chain in the tables (yk_noise.cu): xi = filtered
 // Philox white noise at each chain's current step, or the filtered `given`
-// white field (tables of a single chain).
+// white field (tables of a single chain).  max_blocks > 0 caps the grids of
+// the FFT passes (each block loops over its share of rows / column strips),
+// so the passes can run beside a CG that holds the other SMs.
 cudaError_t launch_noise_tables(ChainDev* d_chains, const NoiseTables& tb, int max_nx,
-                                int max_cols_elems, const double* given, cudaStream_t stream);
+                                int max_cols_elems, const double* given, cudaStream_t stream,
+                                int max_blocks = 0);
+// Blocks (one per SM) of the CG launch_cg would start for `a` (the step's
+// persistent CG on the real path).
+int cg_predict_grid(const CGArgs& a, bool mixed);
 
 // Force + drift (+ per-tile max|drift| and sum F), then the Euler update and
 // observables (yk_langevin.cu).  mode 0: drift = F + bosonic drift;
 // mode 1: drift = F (the fermion force alone); mode 2: drift (preset to a
 // given force) += bosonic drift.
-cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K,
-                               cudaStream_t stream);
+// st: the solves' states when x was just solved (chi = D x is then reused
+// from a solve that ended in a reliable update), else null
+cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K, cudaStream_t stream,
+                               const CGState* st = nullptr);
 cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream);
 
 // Point-source / time-slice helpers.

@@ -1,13 +1,18 @@
 // yk_langevin.cu -- the parts of a Langevin step after the CG solve.
 //
 // force_drift (mode 0: step, 1: force only, 2: injected force + bosonic drift):
-//   chi_j = D x_j is formed on the fly (never stored) and
-//   contracted with eta_j:  F_n = -g/N sum_j Re sum_c conj(chi_{j,n,c}) eta_{j,n,c}
-//   (FermionicDrift.cu:57-100, N = 1 in the reference); the bosonic drift
+//   chi_j = D x_j is contracted with eta_j:
+//   F_n = -g/N sum_j Re sum_c conj(chi_{j,n,c}) eta_{j,n,c}
+//   (FermionicDrift.cu:57-100, N = 1 in the reference).  chi_j is read from the
+//   CG's t64 when the solve ended in a reliable update (the mixed solver's
+//   last round forms exactly D x of the final x there, in FP64), otherwise
+//   formed on the fly (never stored).  The bosonic drift
 //   phi (m^2 + lambda/6 phi^2) - Lap phi (langevin_gpu_v2.cu:9-27, 41-63,
 //   Laplacian columns in the sorted CSR order of Laplace.cu:61-100) is added
-//   in the same pass, and each tile publishes max|drift| and sum F.
-// update: every block reduces the per-tile maxima of its chain (deterministic),
+//   in the same pass; max|drift| goes into the chain's word by an integer
+//   atomic max on the IEEE bits (exact and order-free: non-negative doubles
+//   order like their bit patterns), and each tile publishes sum F.
+// update: every block reads the chain's max|drift|,
 //   applies the clamp and the adaptive step eps = epsBar*30/max|drift| (or a
 //   fixed dt) and the Euler update phi -= eps drift + sqrt(2 eps) xi
 //   (langevin_gpu_v2.cu:65-118); the last tile of a chain writes the step's
@@ -26,9 +31,24 @@ __device__ __forceinline__ void cswap(int& a, int& b)
     b = hi;
 }
 
+// Block max of non-negative IEEE bit patterns into *word (one atomic per block).
+__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* word)
+{
+    __shared__ unsigned long long s_max;
+    if (threadIdx.x == 0) s_max = 0ull;
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned mh = __reduce_max_sync(full, hi);
+    const unsigned ml = __reduce_max_sync(full, hi == mh ? lo : 0u);
+    if ((threadIdx.x & 31) == 0) atomicMax(&s_max, ((unsigned long long)mh << 32) | ml);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_max) atomicMax(word, s_max);
+}
+
 template <int K>
 __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const SysDev* __restrict__ sys,
-                                                            int mode)
+                                                            const CGState* __restrict__ st, int mode)
 {
     __shared__ double red[64];
     const int2 ct = s.tiles[blockIdx.x];
@@ -45,13 +65,17 @@ __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const Sy
             const double diag = 2.0 * C.r + C.m0 + C.g * C.phi[n];
             for (int j = 0; j < C.n_rhs; ++j) {
                 const SysDev& S = sys[C.sys0 + j];
-                const Site<double, K> c = load_site<double, K>(S.x, n);
-                const Site<double, K> tu = load_site<double, K>(S.x, nb.tu);
-                const Site<double, K> td = load_site<double, K>(S.x, nb.td);
-                const Site<double, K> xu = load_site<double, K>(S.x, nb.xu);
-                const Site<double, K> xd = load_site<double, K>(S.x, nb.xd);
-                const Site<double, K> chi =
-                    dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, C.r, (double)nb.sp, (double)nb.sm);
+                Site<double, K> chi;
+                if (st && st[C.sys0 + j].chi_ready) {
+                    chi = load_site<double, K>(S.t64, n);
+                } else {
+                    const Site<double, K> c = load_site<double, K>(S.x, n);
+                    const Site<double, K> tu = load_site<double, K>(S.x, nb.tu);
+                    const Site<double, K> td = load_site<double, K>(S.x, nb.td);
+                    const Site<double, K> xu = load_site<double, K>(S.x, nb.xu);
+                    const Site<double, K> xd = load_site<double, K>(S.x, nb.xd);
+                    chi = dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, C.r, (double)nb.sp, (double)nb.sm);
+                }
                 const Site<double, K> e = load_site<double, K>(S.b, n);
                 double sj = 0.0;
 #pragma unroll
@@ -85,33 +109,32 @@ __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const Sy
         bad = !isfinite(d);
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicCAS(&C.status, 0, (int)YK_ENAN);
-    const double m = block_max(fabs(d), red);
-    const double2 sf = block_sum2(F, 0.0, red);
-    if (threadIdx.x == 0) {
-        s.tile_max[s.tile_base + blockIdx.x] = m;
-        s.tile_sum2[s.tile_base + blockIdx.x] = sf.x;
-    }
+    // max|drift| (a NaN does not count, as fmax ignores it) for the update;
+    // mode 1 is not followed by one and leaves the word alone
+    if (mode != 1) block_max_bits(isnan(d) ? 0ull : (unsigned long long)__double_as_longlong(fabs(d)), &C.dmax_bits);
+    const double sf = block_sum(F, red);
+    if (threadIdx.x == 0) s.tile_sum2[s.tile_base + blockIdx.x] = sf;
 }
 
 __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState* __restrict__ st)
 {
     __shared__ double red[64];
-    __shared__ double s_eps, s_max;
+    __shared__ double s_eps, s_fact, s_max;
     __shared__ int s_last;
     const int2 ct = s.tiles[blockIdx.x];
     ChainDev& C = s.ch[ct.x];
-    double m = 0.0;
-    for (int i = threadIdx.x; i < C.ntiles; i += blockDim.x) m = fmax(m, s.tile_max[C.tile0 + i]);
-    m = block_max(m, red);
     if (threadIdx.x == 0) {
+        double m = __longlong_as_double((long long)*(volatile unsigned long long*)&C.dmax_bits);
         if (m > 1e5) m = 1e5;               // langevin_gpu_v2.cu:83-91
         else if (m < 1e-5) m = 1e-5;
         s_max = m;
-        s_eps = (C.fixed_dt > 0.0) ? C.fixed_dt : C.eps_bar * 30.0 / m;
+        const double e = (C.fixed_dt > 0.0) ? C.fixed_dt : C.eps_bar * 30.0 / m;
+        s_eps = e;
+        s_fact = sqrt(2.0 * e);   // once per block: an FP64 square root is a long sequence on GB300
     }
     __syncthreads();
     const double eps = s_eps;
-    const double fact = sqrt(2.0 * eps);
+    const double fact = s_fact;
     const int n = ct.y + threadIdx.x;
     double p1 = 0.0, p2 = 0.0;
     if (n < C.V) {
@@ -129,20 +152,22 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
         s_last = (prev == (unsigned)C.ntiles - 1) ? 1 : 0;
     }
     __syncthreads();
-    if (s_last && threadIdx.x < 32) {
+    if (s_last) {
+        // the last tile of the chain: every thread loads its tiles' sums at
+        // once (one round trip), then a fixed-order block reduction
         __threadfence();
-        const int lane = threadIdx.x;
         double a = 0.0, b = 0.0, f = 0.0;
-        for (int i = lane; i < C.ntiles; i += 32) {
+        for (int i = threadIdx.x; i < C.ntiles; i += blockDim.x) {
             const double2 q = ld_volatile2(s.tile_sum + C.tile0 + i);
             a += q.x;
             b += q.y;
             f += ld_volatile(s.tile_sum2 + C.tile0 + i);
         }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        f = warp_sum(f);
-        if (lane == 0) {
+        const double2 ab = block_sum2(a, b, red);
+        f = block_sum(f, red);
+        a = ab.x;
+        b = ab.y;
+        if (threadIdx.x == 0) {
             int iters = 0, status = *(volatile int*)&C.status;
             if (C.g != 0.0)
                 for (int j = 0; j < C.n_rhs; ++j) {
@@ -164,16 +189,18 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
             C.step += 1;
             C.counter = 0;
             C.status = 0;
+            C.dmax_bits = 0ull;   // every block read it before counting in
         }
     }
 }
 
-cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K, cudaStream_t stream)
+cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K, cudaStream_t stream,
+                               const CGState* st)
 {
     if (K == 1)
-        force_drift_kernel<1><<<s.ntiles, kTile, 0, stream>>>(s, sys, mode);
+        force_drift_kernel<1><<<s.ntiles, kTile, 0, stream>>>(s, sys, st, mode);
     else
-        force_drift_kernel<2><<<s.ntiles, kTile, 0, stream>>>(s, sys, mode);
+        force_drift_kernel<2><<<s.ntiles, kTile, 0, stream>>>(s, sys, st, mode);
     return cudaGetLastError();
 }
 
