@@ -91,7 +91,7 @@ struct yk_ctx {
     bool own_stream = false;
     // the step's noise runs on `aux` beside the CG when the CG leaves SMs free
     cudaStream_t aux = nullptr;
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join2_ev = nullptr;
     int n_sm = 0;
     bool noise_overlap = true;   // YK_NOISE_OVERLAP=0 at context creation: never
     std::vector<Chain> ch;
@@ -309,6 +309,9 @@ int enqueue_step(yk_ctx* ctx)
         YK_CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
         YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->aux, free_sm));
         YK_CK(cudaEventRecord(ctx->join_ev, ctx->aux));
+        // the next step's sources, which its CG would otherwise generate first
+        YK_CK(launch_eta_ahead(ctx->d_sys, ctx->d_sys_tiles, ctx->n_sys_tiles, free_sm, ctx->aux));
+        YK_CK(cudaEventRecord(ctx->join2_ev, ctx->aux));
     } else {
         prof_begin(ctx, &e);
         YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
@@ -351,6 +354,7 @@ int enqueue_step(yk_ctx* ctx)
     prof_begin(ctx, &e);
     YK_CK(launch_update(s, ctx->d_state, ctx->stream));
     prof_end(ctx, 3, e, 1);
+    if (overlap) YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join2_ev, 0));   // the next step's eta
     if (ctx->profiling) ctx->prof_steps += 1;
     return YK_OK;
 }
@@ -593,6 +597,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     YK_CK(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
     YK_CK(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
     YK_CK(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
+    YK_CK(cudaEventCreateWithFlags(&ctx->join2_ev, cudaEventDisableTiming));
     YK_CK(cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, ctx->dev));
     ctx->precision = p0.precision;
     ctx->tol_mode = p0.cg_tol_mode;
@@ -678,7 +683,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     };
     std::vector<COff> co(n_chains);
     struct SOff {
-        size_t b, x, r0, r1, p0, p1, t64, ap64, s0, s1, q0, q1, t32, ap32, xs, diag;
+        size_t b, x, r0, r1, p0, p1, t64, ap64, s0, s1, q0, q1, t32, ap32, xs, diag, eta0, eta1, tag;
     };
     std::vector<SOff> so(nsys);
     for (int c = 0; c < n_chains; ++c) {
@@ -701,6 +706,9 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             o.b = ar.reserve(d);
             o.x = ar.reserve(d);
             o.t64 = ar.reserve(d);
+            o.eta0 = ar.reserve(d);
+            o.eta1 = ar.reserve(d);
+            o.tag = ar.reserve(2 * sizeof(int64_t));
             if (mixed) {
                 o.s0 = ar.reserve(f);
                 o.s1 = ar.reserve(f);
@@ -742,6 +750,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         cudaStreamDestroy(ctx->aux);
         cudaEventDestroy(ctx->fork_ev);
         cudaEventDestroy(ctx->join_ev);
+        cudaEventDestroy(ctx->join2_ev);
         return YK_ENOMEM;
     }
     ar.base = (char*)ctx->mem;
@@ -824,6 +833,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             S.gen_eta = 1;
             S.seed = (uint64_t)C.p.seed;
             S.step = &ctx->d_chains[c].step;
+            S.eta_ahead[0] = ar.at<double>(q.eta0);
+            S.eta_ahead[1] = ar.at<double>(q.eta1);
+            S.eta_tag = ar.at<int64_t>(q.tag);
+            YK_CK(cudaMemsetAsync(S.eta_tag, 0xff, 2 * sizeof(int64_t), ctx->stream));   // -1: holds no step
             for (int t = 0; t < nt; ++t) sys_tiles.push_back(make_int2(C.sys0 + j, t * kTile));
         }
         if (C.filter) {
@@ -925,6 +938,7 @@ int yk_ctx_destroy(yk_ctx* ctx)
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+    if (ctx->join2_ev) cudaEventDestroy(ctx->join2_ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return YK_OK;

@@ -1632,7 +1632,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
         const SysDev& S = a.sys[a.tiles[tile].x];
         const int n = a.tiles[tile].y + ts;
         if (n >= S.V) continue;
-        const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+        const Site<double, K> bv = S.gen_eta ? eta_of_step<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
         if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
         Site<double, K> z;
         Site<W, K> bw, zw;
@@ -2028,7 +2028,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     for (int tile = tb + hf; tile < te; tile += 2) {
         const int n = a.tiles[tile].y + ts;
         if (n >= V) continue;
-        const Site<double, K> bv = S.gen_eta ? eta_site<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
+        const Site<double, K> bv = S.gen_eta ? eta_of_step<K>(S, n, a.eta_kind) : YK_LD(double, K, S.b, n);
         if (S.gen_eta) YK_ST(double, K, S.b, n, bv);
         Site<double, K> z;
         Site<W, K> bw, zw;

@@ -195,10 +195,9 @@ __device__ __forceinline__ double2 normal_pair(const RngStream& s, uint32_t e)
 // Philox stream (seed, chain; step, kind, rhs), imaginary parts zero
 // (FermionicDrift.cu:102-110).
 template <int K>
-__device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int kind)
+__device__ __forceinline__ Site<double, K> eta_site_at(const SysDev& S, int n, int kind, int64_t step)
 {
-    const RngStream rs = rng_stream(S.seed, (uint32_t)S.chain, (uint64_t)(*S.step), (uint32_t)kind,
-                                    (uint32_t)S.rhs);
+    const RngStream rs = rng_stream(S.seed, (uint32_t)S.chain, (uint64_t)step, (uint32_t)kind, (uint32_t)S.rhs);
     const double2 a = normal_pair(rs, (uint32_t)(2 * n));
     const double2 b = normal_pair(rs, (uint32_t)(2 * n + 1));
     Site<double, K> s;
@@ -209,6 +208,23 @@ __device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int 
         if constexpr (K == 2) s.v[i * K + 1] = 0.0;
     }
     return s;
+}
+
+template <int K>
+__device__ __forceinline__ Site<double, K> eta_site(const SysDev& S, int n, int kind)
+{
+    return eta_site_at<K>(S, n, kind, *S.step);
+}
+
+// eta of the step at site n (kind 2: the Langevin step's sources): from the
+// buffer generated one step ahead when it holds this step, else generated
+// here.  Both give the same bits (the same Philox stream and arithmetic).
+template <int K>
+__device__ __forceinline__ Site<double, K> eta_of_step(const SysDev& S, int n, int kind)
+{
+    const int64_t st = *S.step;
+    if (kind == 2 && S.eta_tag && S.eta_tag[st & 1] == st) return load_site<double, K>(S.eta_ahead[st & 1], n);
+    return eta_site_at<K>(S, n, kind, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -62,6 +62,10 @@ struct SysDev {
     int gen_eta;
     uint64_t seed;
     const int64_t* step; // device step counter of the chain
+    // eta of the step's systems (kind 2) generated one step ahead, by step
+    // parity, with the step each buffer holds (null: never generated ahead)
+    double* eta_ahead[2];
+    int64_t* eta_tag;
 };
 
 // Per-tile reduction slot of the CG kernel: |r|^2, |Ap|^2, <p, Ap> (re, im),

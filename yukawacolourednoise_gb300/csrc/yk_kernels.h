@@ -43,6 +43,8 @@ void noise_init_attributes();
 cudaError_t launch_noise_tables(ChainDev* d_chains, const NoiseTables& tb, int max_nx,
                                 int max_cols_elems, const double* given, cudaStream_t stream,
                                 int max_blocks = 0);
+// eta of the next step into the systems' ahead buffers (yk_langevin.cu).
+cudaError_t launch_eta_ahead(const SysDev* sys, const int2* tiles, int ntiles, int max_blocks, cudaStream_t stream);
 // Blocks (one per SM) of the CG launch_cg would start for `a` (the step's
 // persistent CG on the real path).
 int cg_predict_grid(const CGArgs& a, bool mixed);

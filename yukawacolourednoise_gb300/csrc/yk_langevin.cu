@@ -204,6 +204,32 @@ cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, i
     return cudaGetLastError();
 }
 
+// eta (kind 2) of the step after each chain's current one at every site of
+// the tiles' systems, into the buffer of that step's parity, tagged with the
+// step.  Grid-stride over the tiles, so it can run on a few SMs beside the CG.
+__global__ void __launch_bounds__(kTile) eta_ahead_kernel(const SysDev* __restrict__ sys,
+                                                          const int2* __restrict__ tiles, int ntiles)
+{
+    for (int item = blockIdx.x; item < ntiles; item += gridDim.x) {
+        const int2 tl = tiles[item];
+        const SysDev& S = sys[tl.x];
+        const int64_t step = *S.step + 1;
+        const int par = (int)(step & 1);
+        const int n = tl.y + threadIdx.x;
+        if (n < S.V) store_site<double, 1>(S.eta_ahead[par], n, eta_site_at<1>(S, n, 2, step));
+        // read only after this kernel has finished (the next step's CG)
+        if (tl.y == 0 && threadIdx.x == 0) S.eta_tag[par] = step;
+    }
+}
+
+cudaError_t launch_eta_ahead(const SysDev* sys, const int2* tiles, int ntiles, int max_blocks, cudaStream_t stream)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    const int grid = (max_blocks > 0 && ntiles > max_blocks) ? max_blocks : ntiles;
+    eta_ahead_kernel<<<grid, kTile, 0, stream>>>(sys, tiles, ntiles);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream)
 {
     update_kernel<<<s.ntiles, kTile, 0, stream>>>(s, st);
