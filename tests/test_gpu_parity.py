@@ -252,7 +252,7 @@ def _mixed_run(yk, monkeypatch, halo, Nt, Nx, steps):
         return ctx.get_field(), pr.cg_kernel, pr.cg_iterations, ctx.observables().status
 
 
-@pytest.mark.parametrize("Nt,Nx", [(32, 32), (128, 64), (256, 256), (1024, 64), (40, 24)])
+@pytest.mark.parametrize("Nt,Nx", [(32, 32), (128, 64), (256, 256), (1024, 64), (40, 24), (41, 25)])
 def test_halo_cg_matches_grid_cg(ylib, cuda, monkeypatch, Nt, Nx):
     # the halo CG kernel (single-system mixed solves whose halo slices fit)
     # against cg_kernel on the same trajectory: the same per-site arithmetic,

@@ -1986,7 +1986,8 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
         float* Ac = cur == 0 ? S.Ap32 : S.t32;
         for (int base = tb; base < te; base += 2) {   // the same trip count in every thread
             const int tile = base + hf;
-            const int n = tile < te ? n0 + (tile - tb) * kTile + ts : V;   // the tiles are contiguous
+            const bool tile_on = tile < te;   // the tile writes its partial (every value thread)
+            const int n = tile_on ? n0 + (tile - tb) * kTile + ts : V;   // the tiles are contiguous
             const bool on = n < V;
             W v[6] = {W(0), W(0), W(0), W(0), W(0), W(0)};
             if (on) {
@@ -2005,9 +2006,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
 #pragma unroll
             for (int i = 0; i < 6; ++i) f[i] = FF{v[i], 0.f};
             if (s_fast)
-                put_partial_ff<kSkipIm, false>(a, tile, on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
+                put_partial_ff<kSkipIm, false>(a, tile, tile_on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
             else
-                put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
+                put_partial_ff<kSkipIm, false>(a, tile, tile_on, f, red);
         }
     };
 
