@@ -178,6 +178,15 @@ int yk_cg_solve_static(const double* sigma, int Nt, int Nx, double m0, double g,
                        const void* b, void* x, int mtype, double tol, int tol_mode, int max_iter,
                        void* stream, yk_solve_stats* stats);
 
+/* No reference counterpart (failure detection): runs on `stream` (NULL =
+ * legacy stream) a two-block kernel in which block 0 waits, through the
+ * persistent CG's neighbour synchronisation, on a flag that block 1 never
+ * sets.  The wait gives up after its bound (about 2 s), records YK_ETIMEOUT
+ * and the kernel returns; *status receives the recorded device status.
+ * Returns YK_ETIMEOUT when the wait ran out as designed (the device stays
+ * usable), YK_OK if it did not, YK_ECUDA on a CUDA error. */
+int yk_check_wait_timeout(void* stream, int* status);
+
 /* FermionicDrift::getForce (code/src/FermionicDrift.cuh:15, FermionicDrift.cu:57-100):
  * F_n = -g Re sum_c conj(chi_{n,c}) eta_{n,c}, chi = D (D^dag D)^-1 eta, averaged
  * over the chain's n_rhs right-hand sides; eta (n_rhs * 4V FP64 complex, device)

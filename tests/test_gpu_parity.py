@@ -368,3 +368,21 @@ def test_checkpoint_roundtrip(ylib, cuda, tmp_path):
         assert ctx2.get_step() == 2
         ctx2.step(2)
         assert np.array_equal(ctx2.get_field(), f4)
+
+
+def test_bounded_wait_runs_out(ylib, cuda):
+    # a device wait on a flag that nothing sets gives up after its bound,
+    # records YK_ETIMEOUT for the host and leaves the device usable
+    import ctypes as C
+    import time
+    yk = ylib
+    st = C.c_int(-1)
+    t0 = time.perf_counter()
+    rc = yk.lib().yk_check_wait_timeout(None, C.byref(st))
+    dt = time.perf_counter() - t0
+    assert rc == yk.YK_ETIMEOUT and st.value == yk.YK_ETIMEOUT
+    assert 0.5 < dt < 30.0, dt
+    p = params(yk, 16, 16)
+    with yk.Context(p) as ctx:
+        ctx.step(1)
+        assert ctx.observables().status == 0

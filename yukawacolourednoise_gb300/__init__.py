@@ -139,6 +139,7 @@ _SIGS = {
     "yk_cg_solve_static": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_void_p,
                                      C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                      C.POINTER(SolveStats)]),
+    "yk_check_wait_timeout": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),

@@ -954,6 +954,21 @@ int yk_ctx_set_stream(yk_ctx* ctx, void* stream)
     return YK_OK;
 }
 
+int yk_check_wait_timeout(void* stream, int* status)
+{
+    int st = 0;
+    if (wait_timeout_probe(static_cast<cudaStream_t>(stream), &st) != 0) {
+        set_error("yk_check_wait_timeout: %s", cudaGetErrorString(cudaGetLastError()));
+        return YK_ECUDA;
+    }
+    if (status) *status = st;
+    if (st == YK_ETIMEOUT) {
+        set_error("the probe's bounded wait gave up (as designed)");
+        return YK_ETIMEOUT;
+    }
+    return YK_OK;
+}
+
 int yk_ctx_synchronize(yk_ctx* ctx)
 {
     if (!ctx) return YK_EINVAL;

@@ -2139,6 +2139,48 @@ static size_t halo_smem_bytes(int own, int Nx)
     return (3 * nP + (size_t)own + nT) * sizeof(float4) + nT * sizeof(float);
 }
 
+// Failure detection without a fault: block 0 waits through nsync on block
+// 1's neighbour flag, which block 1 never sets (it returns at once); the
+// bounded wait gives up, records YK_ETIMEOUT in *err and the kernel returns.
+__device__ unsigned g_probe_flags[2 * kFlagStride];
+__device__ int g_probe_err;
+
+__global__ void wait_timeout_probe_kernel(CGArgs a)
+{
+    if (blockIdx.x == 1) return;
+    __shared__ Deps d;
+    if (threadIdx.x == 0) {
+        d.n = 1;
+        d.all = 0;
+        d.b[0] = 1;
+    }
+    __syncthreads();
+    nsync(a, 1u, d);
+}
+
+int wait_timeout_probe(cudaStream_t stream, int* status)
+{
+    void* flags = nullptr;
+    void* err = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&flags, g_probe_flags);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&err, g_probe_err);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, sizeof(g_probe_flags), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), stream);
+    CGArgs a = {};
+    a.flags = static_cast<unsigned*>(flags);
+    a.err = static_cast<int*>(err);
+    if (e == cudaSuccess) {
+        wait_timeout_probe_kernel<<<2, 32, 0, stream>>>(a);
+        e = cudaGetLastError();
+    }
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return -1;
+    *status = h;
+    return 0;
+}
+
 // Resets the barrier, flags, counters and per-system state before a solve.
 __global__ void cg_prepare_kernel(CGArgs a)
 {

@@ -21,6 +21,9 @@ cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, i
 int cg_max_grid(int K, bool mixed);
 // Kernel attributes and occupancy of the halo CG kernel (call before any stream capture).
 void cg_halo_init();
+// Runs the wait-timeout probe kernel on `stream`; *status = the device status
+// it recorded.  Returns 0, or -1 on a CUDA error.
+int wait_timeout_probe(cudaStream_t stream, int* status);
 
 // Cluster-resident mixed CG (yk_cg_cluster.cu): one 16-CTA cluster per system
 // of real (K = 1) vectors whose rows fit the cluster (cg_cluster_fits);
