@@ -178,6 +178,60 @@ int yk_cg_solve_static(const double* sigma, int Nt, int Nx, double m0, double g,
                        const void* b, void* x, int mtype, double tol, int tol_mode, int max_iter,
                        void* stream, yk_solve_stats* stats);
 
+/* Learned preconditioner (no reference counterpart; the reference solves with
+ * plain CG, code/src/CGsolver.cu:72-170).  Per chain, a linear convolutional
+ * network z = M(r) = skip r + N(r) on the chain's lattice, for the real
+ * (one-plane) fields of the Langevin step; N: input channels (r, sigma r),
+ * `layers` 3x3 convolutions with the fermions' antiperiodic time wrap, 8
+ * hidden channels, 4 outputs, weights [layer][tap 9][in][out] FP32.  The skip
+ * term keeps every direction of the residual in M(r), so a flexible Krylov
+ * method never stalls on directions N nearly annihilates.  Trained on the GPU from (residual,
+ * error) pairs that the chain's own CG solves generate, and used in a
+ * flexible GCR inside FP64 iterative refinement; a learned solve returns
+ * YK_OK only when its FP64 true residual meets the tolerance. */
+typedef struct yk_net_train_cfg {
+    int n_sources;             /* Philox right-hand sides (streams 100 + i)     */
+    int n_levels;              /* CG iterates per source: after base_iter * 2^k */
+    int base_iter;             /*   iterations, k < n_levels                    */
+    int steps;                 /* Adam steps                                    */
+    int batch;                 /* pairs per step                                */
+    double lr;                 /* Adam learning rate                            */
+    uint64_t seed;             /* batch order                                   */
+} yk_net_train_cfg;
+
+typedef struct yk_net_train_stats {
+    int pairs;                 /* training pairs generated                      */
+    double loss0, loss1;       /* mean (Mr-e)^T A (Mr-e) / e^T A e, before/after */
+    double ms;                 /* wall time of pair generation and training     */
+} yk_net_train_stats;
+
+/* Creates (or replaces) chain's network with `layers` (2..8) layers, the
+ * skip weight `skip` (< 0: 1 / (4r + |m0| + 2)^2, a Richardson step of D^dag D)
+ * and deterministic initial weights from `seed`, N starting small next to the
+ * skip term. */
+int yk_net_setup(yk_ctx* ctx, int chain, int layers, uint64_t seed, double skip);
+/* Number of weights of chain's network (0 without one). */
+int yk_net_size(yk_ctx* ctx, int chain);
+/* Copies the weights to (set = 0) or from (set = 1) host memory. */
+int yk_net_weights(yk_ctx* ctx, int chain, float* host, int set);
+/* z = M(r) for device r, z (4V floats each, site-major), sigma the chain's field. */
+int yk_net_apply(yk_ctx* ctx, int chain, const float* r, float* z);
+/* Weight gradient (host, yk_net_size floats) and value of the training loss
+ * (M r - e)^T A (M r - e) = |D (M r - e)|^2 for device r, e (4V floats
+ * each): the energy norm of the error left by the correction M r. */
+int yk_net_grad(yk_ctx* ctx, int chain, const float* r, const float* e, float* grad, double* loss);
+/* Generates training pairs with the chain's CG (the context's solver and
+ * tolerance) and trains the chain's network with Adam. */
+int yk_net_train(yk_ctx* ctx, int chain, const yk_net_train_cfg* cfg, yk_net_train_stats* stats);
+/* Solves (D^dag D) x = b for real fields (b, x: 4V doubles, device) by
+ * flexible GCR with the chain's network (use_net = 1) or the identity
+ * (use_net = 0) as preconditioner, inside FP64 iterative refinement; stops
+ * at the tolerance rule of yk_cg_solve or after max_iter FGCR iterations.
+ * stats->iterations counts preconditioner applications, reliable_updates the
+ * FP64 refinement rounds. */
+int yk_fgcr_solve(yk_ctx* ctx, int chain, const double* b, double* x, double tol, int tol_mode, int max_iter,
+                  int use_net, yk_solve_stats* stats);
+
 /* No reference counterpart (failure detection): runs on `stream` (NULL =
  * legacy stream) a two-block kernel in which block 0 waits, through the
  * persistent CG's neighbour synchronisation, on a flag that block 1 never

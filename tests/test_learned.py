@@ -1,0 +1,134 @@
+"""The learned preconditioner: its oracle (CPU), the CUDA network against the
+oracle, training, and what the trained network gains in a flexible Krylov
+solve (GPU).
+
+Tolerances: the oracle's gradients against central finite differences 1e-6
+relative; the FP32 network against the FP64 oracle 2e-6 (forward) and 2e-5
+(weight gradients) relative to the largest entry; every solve to the FP64
+relative residual 1e-10.
+"""
+import numpy as np
+import pytest
+
+from oracle import learned as N
+from oracle import oracle as O
+
+
+def _action(m0=0.1):
+    return O.action(m2=-0.5, lam=1.0, g=0.5, m0=m0, r=1.0, cut_fraction=0.35355339059327373, eps_bar=0.01,
+                    drift_mode=0)
+
+
+def _fd_worst(fn, Ws, args):
+    L, g = fn(Ws, *args)
+    worst = 0.0
+    for l in range(len(Ws)):
+        for idx in [(0, 0, 0), (4, 3, 2), (8, 7, Ws[l].shape[2] - 1), (2, 5, 1)]:
+            W2 = [w.copy() for w in Ws]
+            h = 1e-6
+            W2[l][idx] += h
+            Lp, _ = fn(W2, *args)
+            W2[l][idx] -= 2 * h
+            Lm, _ = fn(W2, *args)
+            fd = (Lp - Lm) / (2 * h)
+            worst = max(worst, abs(fd - g[l][idx]) / max(1e-9, abs(fd)))
+    return worst
+
+
+def test_oracle_preconditioner_is_symmetric_positive():
+    Nt, Nx = 6, 5
+    rng = np.random.default_rng(0)
+    Ws = N.init_weights(8, 3, 3)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    a, b = rng.normal(size=(2, 4, Nt * Nx))
+    Ma = N.apply_M(Ws, a, sig, Nt, Nx, 0.03)[0]
+    Mb = N.apply_M(Ws, b, sig, Nt, Nx, 0.03)[0]
+    assert abs(np.sum(b * Ma) - np.sum(a * Mb)) < 1e-12 * abs(np.sum(b * Ma))
+    assert np.sum(a * Ma) > 0.03 * np.sum(a * a)
+
+
+@pytest.mark.parametrize("kind", ["plain", "energy"])
+def test_oracle_gradients_match_finite_differences(kind):
+    Nt, Nx = 6, 5
+    rng = np.random.default_rng(1)
+    Ws = N.init_weights(8, 3, 3)
+    r, e = rng.normal(size=(2, 4, Nt * Nx))
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    if kind == "plain":
+        worst = _fd_worst(N.plain_loss_and_grad, Ws, (r, e, sig, Nt, Nx, 0.03))
+    else:
+        worst = _fd_worst(N.energy_loss_and_grad, Ws, (r, e, sig, Nt, Nx, _action(), 0.03))
+    assert worst < 1e-6, worst
+
+
+def _params(yk, Nt, Nx, m0, precision):
+    return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=m0, wilson_param=1.0,
+                             cut_fraction=0.35355339059327373, Nt=Nt, Nx=Nx, cg_tol=1e-10,
+                             cg_tol_mode=yk.YK_TOL_REL, seed=1234, init=yk.YK_INIT_PHILOX, precision=precision,
+                             fixed_dt=0.01)
+
+
+@pytest.mark.gpu
+def test_network_forward_and_gradient_match_oracle(ylib, cuda):
+    yk, torch = ylib, cuda
+    Nt, Nx = 16, 12
+    V = Nt * Nx
+    rng = np.random.default_rng(0)
+    with yk.Context(_params(yk, Nt, Nx, 0.1, yk.YK_FP64)) as ctx:
+        sig = rng.uniform(-1, 1, V)
+        ctx.set_field(sig)
+        ctx.net_setup(4, 1, skip=0.05)
+        Ws = N.init_weights(8, 4, 3)
+        ctx.net_set_weights(np.concatenate([w.ravel() for w in Ws]))
+        assert np.array_equal(ctx.net_get_weights(), np.concatenate([w.ravel() for w in Ws]).astype(np.float32))
+        W32 = [w.astype(np.float32).astype(np.float64) for w in Ws]
+        r = rng.normal(size=(V, 4)).astype(np.float32)
+        e = rng.normal(size=(V, 4)).astype(np.float32)
+        rd, ed = torch.from_numpy(r).cuda(), torch.from_numpy(e).cuda()
+        zd = torch.empty_like(rd)
+        ctx.net_apply(rd, zd)
+        want = N.apply_M(W32, r.T.astype(np.float64), sig, Nt, Nx, np.float32(0.05))[0]
+        assert np.abs(zd.cpu().numpy().T - want).max() < 2e-6 * np.abs(want).max()
+        g, loss = ctx.net_grad(rd, ed)
+        lo, go = N.energy_loss_and_grad(W32, r.T.astype(np.float64), e.T.astype(np.float64), sig, Nt, Nx,
+                                        _action(0.1), np.float32(0.05))
+        go = np.concatenate([x.ravel() for x in go])
+        assert abs(loss - lo) < 1e-5 * lo
+        assert np.abs(g - go).max() < 2e-5 * np.abs(go).max()
+
+
+@pytest.mark.gpu
+def test_trained_network_cuts_iterations(ylib, cuda):
+    # near the critical mass (m0 = 0.02): the trained network against the
+    # method without it (the same flexible solver with z = r) and against the
+    # context's mixed CG; every solve must meet the FP64 tolerance
+    yk, torch = ylib, cuda
+    Nt, Nx = 32, 32
+    V = Nt * Nx
+    p = _params(yk, Nt, Nx, 0.02, yk.YK_MIXED)
+    with yk.Context(p) as ctx:
+        ctx.step(20)
+        ctx.net_setup(4, 7)
+        st = ctx.net_train(n_sources=4, n_levels=5, base_iter=4, steps=400, batch=4, lr=2e-3, seed=3)
+        assert st.pairs == 20
+        assert st.loss1 < 0.8 * st.loss0
+        rng = np.random.default_rng(5)
+        b = rng.normal(size=(V, 4))
+        bd = torch.from_numpy(b).cuda()
+        its = {}
+        sig = ctx.get_field()
+        a = O.action(m2=p.mass, lam=p.g, g=p.yukawa_coupling, m0=p.fermion_mass, r=p.wilson_param,
+                     cut_fraction=p.cut_fraction, eps_bar=p.average_epsilon, drift_mode=p.drift_mode)
+        for use in (False, True):
+            x = torch.zeros_like(bd)
+            s = ctx.fgcr_solve(bd, x, tol=1e-10, max_iter=20000, use_net=use)
+            assert s.converged == 1 and s.rr <= 1e-20 * s.rr0
+            xs = x.cpu().numpy().astype(np.complex128)
+            Ax = O.dirac(Nt, Nx, a, sig, O.dirac(Nt, Nx, a, sig, xs, False), True)
+            assert np.linalg.norm(Ax - b) < 1e-9 * np.linalg.norm(b)
+            its[use] = s.iterations
+        xc = torch.zeros(V, 4, dtype=torch.complex128, device="cuda")
+        cg = ctx.cg_solve(torch.complex(bd, torch.zeros_like(bd)).contiguous(), xc, tol=1e-10,
+                          tol_mode=yk.YK_TOL_REL, max_iter=20000, precision=yk.YK_MIXED)
+        assert its[True] * 5 < its[False], its
+        assert its[True] < cg.iterations, (its, cg.iterations)

@@ -99,6 +99,15 @@ class SolveStats(C.Structure):
                 ("rr0", C.c_double), ("converged", C.c_int)]
 
 
+class NetTrainCfg(C.Structure):
+    _fields_ = [("n_sources", C.c_int), ("n_levels", C.c_int), ("base_iter", C.c_int), ("steps", C.c_int),
+                ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_uint64)]
+
+
+class NetTrainStats(C.Structure):
+    _fields_ = [("pairs", C.c_int), ("loss0", C.c_double), ("loss1", C.c_double), ("ms", C.c_double)]
+
+
 class Obs(C.Structure):
     _fields_ = [("t", C.c_double), ("eps", C.c_double), ("max_drift", C.c_double), ("sum_phi", C.c_double),
                 ("sum_phi2", C.c_double), ("sum_force", C.c_double), ("steps", C.c_int64),
@@ -140,6 +149,14 @@ _SIGS = {
                                      C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                      C.POINTER(SolveStats)]),
     "yk_check_wait_timeout": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "yk_net_setup": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_double]),
+    "yk_net_size": (C.c_int, [C.c_void_p, C.c_int]),
+    "yk_net_weights": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
+    "yk_net_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "yk_net_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "yk_net_train": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(NetTrainCfg), C.POINTER(NetTrainStats)]),
+    "yk_fgcr_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
+                                C.POINTER(SolveStats)]),
     "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
@@ -268,6 +285,50 @@ class Context:
         ok = (YK_OK, YK_ENOCONV) if allow_noconv else (YK_OK,)
         _check(lib().yk_cg_solve(self.h, chain, _ptr(b), _ptr(x), int(mtype), tol, tol_mode, max_iter, precision,
                                  C.byref(st)), ok)
+        return st
+
+    # ---- learned preconditioner ----
+    def net_setup(self, layers=4, seed=1, skip=-1.0, chain=0):
+        _check(lib().yk_net_setup(self.h, chain, layers, seed, skip))
+
+    def net_size(self, chain=0) -> int:
+        return lib().yk_net_size(self.h, chain)
+
+    def net_get_weights(self, chain=0):
+        import numpy as np
+        w = np.empty(self.net_size(chain), dtype=np.float32)
+        _check(lib().yk_net_weights(self.h, chain, w.ctypes.data, 0))
+        return w
+
+    def net_set_weights(self, w, chain=0):
+        import numpy as np
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.net_size(chain)
+        _check(lib().yk_net_weights(self.h, chain, w.ctypes.data, 1))
+
+    def net_apply(self, r, z, chain=0):
+        _check(lib().yk_net_apply(self.h, chain, _ptr(r), _ptr(z)))
+
+    def net_grad(self, r, e, chain=0):
+        import numpy as np
+        g = np.empty(self.net_size(chain), dtype=np.float32)
+        loss = C.c_double()
+        _check(lib().yk_net_grad(self.h, chain, _ptr(r), _ptr(e), g.ctypes.data, C.byref(loss)))
+        return g, loss.value
+
+    def net_train(self, n_sources=4, n_levels=4, base_iter=4, steps=200, batch=4, lr=1e-3, seed=1,
+                  chain=0) -> NetTrainStats:
+        cfg = NetTrainCfg(n_sources, n_levels, base_iter, steps, batch, lr, seed)
+        st = NetTrainStats()
+        _check(lib().yk_net_train(self.h, chain, C.byref(cfg), C.byref(st)))
+        return st
+
+    def fgcr_solve(self, b, x, tol=1e-10, tol_mode=YK_TOL_REL, max_iter=2000, use_net=True, chain=0,
+                   allow_noconv=False) -> SolveStats:
+        st = SolveStats()
+        ok = (YK_OK, YK_ENOCONV) if allow_noconv else (YK_OK,)
+        _check(lib().yk_fgcr_solve(self.h, chain, _ptr(b), _ptr(x), tol, tol_mode, max_iter, int(bool(use_net)),
+                                   C.byref(st)), ok)
         return st
 
     def fermion_force(self, F, eta=None, chain=0) -> SolveStats:

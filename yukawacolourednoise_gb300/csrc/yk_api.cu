@@ -6,6 +6,8 @@
 // Langevin step.  The reference's equivalents are process-global
 // __constant__ parameters (code/src/main.cu:268-278) and per-object managed
 // buffers with a device synchronisation after every launch.
+#include <chrono>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -81,6 +83,7 @@ struct Chain {
     uint8_t* keep;
     double2 *tw_t, *tw_x;
     Workspace ws;
+    LearnedNet* net = nullptr;   // the learned preconditioner (yk_net_setup)
 };
 
 }  // namespace
@@ -929,8 +932,10 @@ int yk_ctx_destroy(yk_ctx* ctx)
         cudaEventDestroy(r.b);
     }
     for (auto e : ctx->pool) cudaEventDestroy(e);
-    for (auto& C : ctx->ch)
+    for (auto& C : ctx->ch) {
         if (C.ws.mem) cudaFree(C.ws.mem);
+        net_destroy(C.net);
+    }
     if (ctx->mem) cudaFree(ctx->mem);
     if (ctx->aux) {
         cudaStreamSynchronize(ctx->aux);
@@ -1309,6 +1314,187 @@ int yk_set_step(yk_ctx* ctx, int c, int64_t step)
     YK_CK(cudaMemcpyAsync(&ctx->d_chains[c].step, &ctx->h_chains[c].step, sizeof(int64_t), cudaMemcpyHostToDevice,
                           ctx->stream));
     YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+
+// ---- learned preconditioner ----
+
+static int net_ok(yk_ctx* ctx, int c)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!ctx->ch[c].net) {
+        set_error("chain %d has no network (yk_net_setup)", c);
+        return YK_EINVAL;
+    }
+    return YK_OK;
+}
+
+int yk_net_setup(yk_ctx* ctx, int c, int layers, uint64_t seed, double skip)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (layers < 2 || layers > 8) {
+        set_error("yk_net_setup: layers = %d outside [2, 8]", layers);
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    net_destroy(C.net);
+    C.net = nullptr;
+    cudaError_t e = cudaSuccess;
+    C.net = net_create(C.Nt, C.Nx, layers, &e);
+    if (!C.net) {
+        set_error("yk_net_setup: %s", cudaGetErrorString(e));
+        return YK_ECUDA;
+    }
+    // small normal weights, 1 / sqrt(fan-in) (splitmix64 + Box-Muller)
+    std::vector<float> w((size_t)net_size(C.net));
+    uint64_t st = seed;
+    auto u01 = [&st]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    if (skip < 0.0) {
+        const double d = 4.0 * C.a.r + std::fabs(C.a.m0) + 2.0;
+        skip = 1.0 / (d * d);
+    }
+    net_set_skip(C.net, (float)skip);
+    // the last layer starts at 0.1 skip: N(r) ~ 0.1 skip r beside the skip term
+    const double scale = 1.0 / std::sqrt(9.0 * 8.0);
+    const size_t last = w.size() - 9 * 8 * 4;
+    for (size_t i = 0; i < w.size(); ++i) {
+        const double a = u01(), b = u01();
+        const double f = i >= last && skip != 0.0 ? 0.1 * skip : 1.0;
+        w[i] = (float)(f * scale * std::sqrt(-2.0 * std::log(a)) * std::cos(6.283185307179586 * b));
+    }
+    YK_CK(net_weights(C.net, w.data(), true));
+    return YK_OK;
+}
+
+int yk_net_size(yk_ctx* ctx, int c)
+{
+    if (chain_ok(ctx, c) || !ctx->ch[c].net) return 0;
+    return net_size(ctx->ch[c].net);
+}
+
+int yk_net_weights(yk_ctx* ctx, int c, float* host, int set)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!host) {
+        set_error("yk_net_weights: host buffer is null");
+        return YK_EINVAL;
+    }
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    YK_CK(net_weights(ctx->ch[c].net, host, set != 0));
+    return YK_OK;
+}
+
+int yk_net_apply(yk_ctx* ctx, int c, const float* r, float* z)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!r || !z) {
+        set_error("yk_net_apply: null buffer");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    YK_CK(net_forward(C.net, r, C.phi, z, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_net_grad(yk_ctx* ctx, int c, const float* r, const float* e, float* grad, double* loss)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!r || !e || !grad) {
+        set_error("yk_net_grad: null buffer");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    double l = 0.0;
+    const NetOp op = {C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r};
+    YK_CK(net_zero_grad(C.net, ctx->stream));
+    YK_CK(net_accumulate_grad(C.net, r, e, op, ctx->stream, &l));
+    YK_CK(net_grad_to_host(C.net, grad, ctx->stream));
+    if (loss) *loss = l;
+    return YK_OK;
+}
+
+int yk_net_train(yk_ctx* ctx, int c, const yk_net_train_cfg* cfg, yk_net_train_stats* stats)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    Chain& C = ctx->ch[c];
+    if (!cfg || cfg->n_sources < 1 || cfg->n_levels < 1 || cfg->base_iter < 1 || cfg->steps < 0 ||
+        cfg->batch < 1 || !(cfg->lr > 0.0)) {
+        set_error("yk_net_train: bad configuration");
+        return YK_EINVAL;
+    }
+    if (C.n_rhs_step == 0) {
+        set_error("yk_net_train: chain %d has no fermion systems (g = 0)", c);
+        return YK_EINVAL;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    SysDev S;
+    YK_CK(cudaMemcpy(&S, ctx->d_sys + C.sys0, sizeof(SysDev), cudaMemcpyDeviceToHost));
+    const size_t V4 = 4 * (size_t)C.V;
+    double* xstar = nullptr;
+    YK_CK(cudaMalloc(&xstar, sizeof(double) * V4));
+    const int cap = cfg->n_sources * cfg->n_levels;
+    const int keep_iter = ctx->max_iter;
+    int rc = YK_OK;
+    for (int src = 0; src < cfg->n_sources && rc == YK_OK; ++src) {
+        const int kind = 100 + src;
+        ctx->max_iter = keep_iter;
+        rc = chain_solve(ctx, c, kind, nullptr);
+        if (rc == YK_ENOCONV) rc = YK_OK;
+        if (rc) break;
+        if (cudaMemcpyAsync(xstar, S.x, sizeof(double) * V4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
+            rc = YK_ECUDA;
+            break;
+        }
+        for (int lv = 0; lv < cfg->n_levels && rc == YK_OK; ++lv) {
+            ctx->max_iter = cfg->base_iter << lv;
+            rc = chain_solve(ctx, c, kind, nullptr);
+            if (rc == YK_ENOCONV) rc = YK_OK;
+            if (rc) break;
+            const cudaError_t e = net_add_pair(C.net, cap, C.phi, C.a.m0, C.a.g, C.a.r, S.b, xstar, S.x, ctx->stream);
+            if (e != cudaSuccess && e != cudaErrorInvalidValue) rc = YK_ECUDA;   // a vanished error adds no pair
+        }
+    }
+    ctx->max_iter = keep_iter;
+    cudaFree(xstar);
+    if (rc) return rc;
+    yk_net_train_stats out = {};
+    out.pairs = net_pairs(C.net);
+    const NetOp op = {C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r};
+    YK_CK(net_mean_loss(C.net, op, ctx->stream, &out.loss0));
+    YK_CK(net_train(C.net, op, cfg->steps, cfg->batch, (float)cfg->lr, cfg->seed, ctx->stream));
+    YK_CK(net_mean_loss(C.net, op, ctx->stream, &out.loss1));
+    out.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = out;
+    return YK_OK;
+}
+
+int yk_fgcr_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, int tol_mode, int max_iter, int use_net,
+                  yk_solve_stats* stats)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!b || !x || b == x || max_iter < 0 || !(tol >= 0.0) || (tol_mode != YK_TOL_ABS && tol_mode != YK_TOL_REL)) {
+        set_error("yk_fgcr_solve: bad arguments");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    FgcrResult r = {};
+    YK_CK(fgcr_solve(C.net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, b, x, tol, tol_mode, max_iter, 16, 1e-4,
+                     ctx->stream, &r));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (stats) *stats = yk_solve_stats{r.iterations, r.outer, r.rr, r.rr0, r.converged};
+    if (!r.converged) {
+        set_error("yk_fgcr_solve: %d iterations, |r|^2 = %g > the tolerance", r.iterations, r.rr);
+        return YK_ENOCONV;
+    }
     return YK_OK;
 }
 

@@ -67,4 +67,41 @@ cudaError_t launch_time_slices_spinor(const double* psi, double* corr, int Nt, i
                                       cudaStream_t stream);
 cudaError_t launch_time_slices(const double* phi, double* out, int Nt, int Nx, cudaStream_t stream);
 
+// Learned preconditioner (yk_learned.cu): a linear convolutional network on
+// one Nt x Nx lattice (real plane), its training and the flexible GCR that
+// uses it.
+struct LearnedNet;
+// the operator A = D^dag D of a chain (real plane): its field and action
+struct NetOp {
+    const double* sigma;
+    int Nt, Nx;
+    double m0, g, r;
+};
+struct FgcrResult {
+    int iterations;   // FGCR iterations (preconditioner applications)
+    int outer;        // FP64 refinement rounds
+    double rr, rr0;   // final FP64 |r|^2 and |b|^2
+    int converged;
+};
+LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err);
+void net_destroy(LearnedNet* n);
+int net_size(const LearnedNet* n);
+void net_set_skip(LearnedNet* n, float skip);   // M(r) = skip r + N(r)
+cudaError_t net_weights(LearnedNet* n, float* host, bool set);
+cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);
+cudaError_t net_zero_grad(LearnedNet* n, cudaStream_t s);
+// loss of a pair: (M r - e)^T A (M r - e); accumulates its weight gradient
+cudaError_t net_accumulate_grad(LearnedNet* n, const float* r, const float* e, const NetOp& op, cudaStream_t s,
+                                double* loss);
+cudaError_t net_grad_to_host(LearnedNet* n, float* host, cudaStream_t s);
+cudaError_t net_adam_step(LearnedNet* n, float lr, int batch, cudaStream_t s);
+cudaError_t net_add_pair(LearnedNet* n, int cap, const double* sigma, double m0, double g, double r, const double* b,
+                         const double* xstar, const double* xk, cudaStream_t s);
+int net_pairs(const LearnedNet* n);
+cudaError_t net_mean_loss(LearnedNet* n, const NetOp& op, cudaStream_t s, double* out);
+cudaError_t net_train(LearnedNet* n, const NetOp& op, int steps, int batch, float lr, uint64_t seed, cudaStream_t s);
+cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                       const double* b, double* x, double tol, int tol_mode, int max_iter, int restart,
+                       double inner_tol, cudaStream_t s, FgcrResult* res);
+
 }  // namespace yk

@@ -1,0 +1,887 @@
+// yk_learned.cu -- the learned preconditioner: a small convolutional network
+// z = M(r) on the lattice, its training on the GPU (own forward and backward
+// kernels, Adam), and a flexible GCR solver that uses it inside FP64
+// iterative refinement.  No reference counterpart: the reference solves with
+// plain CG (code/src/CGsolver.cu:72-170); a learned solve is accepted only
+// when its FP64 true residual meets the same tolerance.
+//
+// Network (one real plane; D has real coefficients, so a complex field is
+// two independent real planes): M(r) = skip r + N^T N r, symmetric positive
+// definite by construction (so A M has a positive real spectrum and a
+// Krylov method cannot stall on it), with N:
+//   features X0 = F r = (r, sigma r): 8 channels, adapted to sigma;
+//   layers Y[o, n] = sum_k sum_i W[k][i][o] s_k(n) X[i, nb_k(n)] over the 3x3
+//   taps k = (dt + 1) * 3 + (dx + 1), s_k(n) = -1 when t + dt wraps
+//   (antiperiodic time, as the fermion fields); no activation;
+//   channels 8 -> 8 -> ... -> 8 -> 4;
+// and N^T the same layers transposed in reverse order, then F^T (a, b) =
+// a + sigma b.  Each weight serves twice (in N and in N^T).
+// Activations are channel-major float arrays [C][V]; the residual and the
+// output are site-major (4 floats per site, the layout of the CG vectors).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "yk_common.cuh"
+#include "yk_kernels.h"
+
+namespace yk {
+
+namespace {
+
+constexpr int kNetThreads = 256;
+constexpr int kNetC = 8;          // feature and hidden channels
+constexpr int kNetOut = 4;        // output channels (spinor components)
+constexpr int kWTile = 64;        // sites per shared-memory tile of the weight gradient
+
+struct TapSite {
+    int m;      // neighbour site
+    float s;    // boundary sign
+};
+
+// the site at tap k of n = t * Nx + x, with its antiperiodic sign
+__device__ __forceinline__ TapSite tap_site(int t, int x, int k, int Nt, int Nx)
+{
+    const int dt = k / 3 - 1, dx = k % 3 - 1;
+    int tt = t + dt;
+    float s = 1.f;
+    if (tt < 0) {
+        tt += Nt;
+        s = -1.f;
+    } else if (tt >= Nt) {
+        tt -= Nt;
+        s = -1.f;
+    }
+    int xx = x + dx;
+    if (xx < 0) xx += Nx;
+    else if (xx >= Nx) xx -= Nx;
+    return TapSite{tt * Nx + xx, s};
+}
+
+__global__ void __launch_bounds__(kNetThreads) net_features_kernel(const float* __restrict__ r,
+                                                                   const double* __restrict__ sigma,
+                                                                   float* __restrict__ X, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const float4 v = reinterpret_cast<const float4*>(r)[n];
+        const float sg = (float)sigma[n];
+        X[0 * V + n] = v.x;
+        X[1 * V + n] = v.y;
+        X[2 * V + n] = v.z;
+        X[3 * V + n] = v.w;
+        X[4 * V + n] = sg * v.x;
+        X[5 * V + n] = sg * v.y;
+        X[6 * V + n] = sg * v.z;
+        X[7 * V + n] = sg * v.w;
+    }
+}
+
+// X (8 channels) = F g = (g, sigma g) for a channel-major 4-channel g
+__global__ void __launch_bounds__(kNetThreads) net_feat_cm_kernel(const float* __restrict__ g,
+                                                                  const double* __restrict__ sigma,
+                                                                  float* __restrict__ X, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const float sg = (float)sigma[n];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float v = g[c * V + n];
+            X[c * V + n] = v;
+            X[(4 + c) * V + n] = sg * v;
+        }
+    }
+}
+
+// z (site-major) = F^T a + skip r = a[0..3] + sigma a[4..7] + skip r
+__global__ void __launch_bounds__(kNetThreads) net_featT_kernel(const float* __restrict__ a,
+                                                                const double* __restrict__ sigma,
+                                                                const float* __restrict__ r, float skip,
+                                                                float* __restrict__ z, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const float sg = (float)sigma[n];
+        const float4 rv = reinterpret_cast<const float4*>(r)[n];
+        float4 o;
+        o.x = fmaf(sg, a[4 * V + n], a[0 * V + n]) + skip * rv.x;
+        o.y = fmaf(sg, a[5 * V + n], a[1 * V + n]) + skip * rv.y;
+        o.z = fmaf(sg, a[6 * V + n], a[2 * V + n]) + skip * rv.z;
+        o.w = fmaf(sg, a[7 * V + n], a[3 * V + n]) + skip * rv.w;
+        reinterpret_cast<float4*>(z)[n] = o;
+    }
+}
+
+// Y[COUT][V] = conv(X[8][V]); the last layer (COUT = 4) may write site-major.
+template <int COUT, bool SITE_OUT>
+__global__ void __launch_bounds__(kNetThreads) net_conv_fwd_kernel(const float* __restrict__ X, float* __restrict__ Y,
+                                                                   const float* __restrict__ Wl, int Nt, int Nx)
+{
+    __shared__ float w[9 * kNetC * COUT];
+    for (int i = threadIdx.x; i < 9 * kNetC * COUT; i += blockDim.x) w[i] = Wl[i];
+    __syncthreads();
+    const int V = Nt * Nx;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const int t = n / Nx, x = n - t * Nx;
+        float acc[COUT];
+#pragma unroll
+        for (int o = 0; o < COUT; ++o) acc[o] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const TapSite q = tap_site(t, x, k, Nt, Nx);
+#pragma unroll
+            for (int i = 0; i < kNetC; ++i) {
+                const float xv = q.s * X[i * V + q.m];
+#pragma unroll
+                for (int o = 0; o < COUT; ++o) acc[o] = fmaf(w[(k * kNetC + i) * COUT + o], xv, acc[o]);
+            }
+        }
+        if constexpr (SITE_OUT) {
+            reinterpret_cast<float4*>(Y)[n] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        } else {
+#pragma unroll
+            for (int o = 0; o < COUT; ++o) Y[o * V + n] = acc[o];
+        }
+    }
+}
+
+// gX[8][V] = conv^T(gY[COUT][V]): the transpose of a tap is the opposite tap
+// with the same sign (a wrap from n to m by +d is a wrap from m to n by -d).
+template <int COUT>
+__global__ void __launch_bounds__(kNetThreads) net_conv_bwd_in_kernel(const float* __restrict__ gY,
+                                                                      float* __restrict__ gX,
+                                                                      const float* __restrict__ Wl, int Nt, int Nx)
+{
+    __shared__ float w[9 * kNetC * COUT];
+    for (int i = threadIdx.x; i < 9 * kNetC * COUT; i += blockDim.x) w[i] = Wl[i];
+    __syncthreads();
+    const int V = Nt * Nx;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < V; m += gridDim.x * blockDim.x) {
+        const int t = m / Nx, x = m - t * Nx;
+        float acc[kNetC];
+#pragma unroll
+        for (int i = 0; i < kNetC; ++i) acc[i] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const TapSite q = tap_site(t, x, 8 - k, Nt, Nx);   // the opposite tap
+            float g[COUT];
+#pragma unroll
+            for (int o = 0; o < COUT; ++o) g[o] = q.s * gY[o * V + q.m];
+#pragma unroll
+            for (int i = 0; i < kNetC; ++i)
+#pragma unroll
+                for (int o = 0; o < COUT; ++o) acc[i] = fmaf(w[(k * kNetC + i) * COUT + o], g[o], acc[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < kNetC; ++i) gX[i * V + m] = acc[i];
+    }
+}
+
+// Per-block partial weight gradients of one layer:
+// gW[k][i][o] = sum_n s_k(n) X[i, nb_k(n)] gY[o, n], a [72 x V] x [V x COUT]
+// product staged through shared memory tiles of kWTile sites.  gY may be
+// site-major (the output layer's gradient).
+template <int COUT, bool SITE_GY>
+__global__ void __launch_bounds__(kNetThreads) net_conv_bwd_w_kernel(const float* __restrict__ X,
+                                                                     const float* __restrict__ gY,
+                                                                     float* __restrict__ part, int Nt, int Nx)
+{
+    constexpr int NW = 9 * kNetC * COUT;
+    constexpr int PER = (NW + kNetThreads - 1) / kNetThreads;
+    __shared__ float nb[kWTile][9 * kNetC + 1];
+    __shared__ float gy[kWTile][COUT];
+    const int V = Nt * Nx;
+    float acc[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) acc[j] = 0.f;
+    for (int base = blockIdx.x * kWTile; base < V; base += gridDim.x * kWTile) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kWTile * 9; idx += blockDim.x) {
+            const int ts = idx / 9, k = idx - ts * 9, n = base + ts;
+            if (n < V) {
+                const int t = n / Nx, x = n - t * Nx;
+                const TapSite q = tap_site(t, x, k, Nt, Nx);
+#pragma unroll
+                for (int i = 0; i < kNetC; ++i) nb[ts][k * kNetC + i] = q.s * X[i * V + q.m];
+            } else {
+#pragma unroll
+                for (int i = 0; i < kNetC; ++i) nb[ts][k * kNetC + i] = 0.f;
+            }
+        }
+        for (int idx = threadIdx.x; idx < kWTile * COUT; idx += blockDim.x) {
+            const int ts = idx / COUT, o = idx - ts * COUT, n = base + ts;
+            gy[ts][o] = n < V ? (SITE_GY ? gY[(size_t)n * COUT + o] : gY[o * V + n]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int wi = threadIdx.x + j * kNetThreads;
+            if (wi < NW) {
+                const int kk = wi / COUT, o = wi - kk * COUT;
+                float a = acc[j];
+                for (int ts = 0; ts < kWTile; ++ts) a = fmaf(nb[ts][kk], gy[ts][o], a);
+                acc[j] = a;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int wi = threadIdx.x + j * kNetThreads;
+        if (wi < NW) part[(size_t)blockIdx.x * NW + wi] = acc[j];
+    }
+}
+
+// g[i] += sum over blocks of part[b][i], in block order (deterministic)
+__global__ void net_reduce_w_kernel(const float* __restrict__ part, int nblocks, int nw, float* __restrict__ g)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * nw + i];
+        g[i] += s;
+    }
+}
+
+// d = z - e (site-major)
+__global__ void net_diff_kernel(const float* __restrict__ z, const float* __restrict__ e, float* __restrict__ d, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = z[i] - e[i];
+}
+
+// gZ (channel-major [4][V]) = 2 u (site-major)
+__global__ void net_gz_kernel(const float* __restrict__ u, float* __restrict__ gz, int V)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * V; i += gridDim.x * blockDim.x)
+        gz[(i & 3) * V + (i >> 2)] = 2.f * u[i];
+}
+
+__global__ void net_adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                                float* __restrict__ v, int nw, float lr, float c1, float c2, float gscale)
+{
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) {
+        const float gi = g[i] * gscale;
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+// ---- vectors of the flexible solver (4V floats or doubles, site-major) ----
+
+// per-block partial sums of a . b (products in FP32, sums in FP64)
+__global__ void __launch_bounds__(kNetThreads) fvec_dot_kernel(const float* __restrict__ a, const float* __restrict__ b,
+                                                               double* __restrict__ part, int n)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        s = fma((double)a[i], (double)b[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kNetThreads) dvec_dot_kernel(const double* __restrict__ a,
+                                                               const double* __restrict__ b,
+                                                               double* __restrict__ part, int n)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s = fma(a[i], b[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// y += a x
+__global__ void fvec_axpy_kernel(float* __restrict__ y, const float* __restrict__ x, float a, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = fmaf(a, x[i], y[i]);
+}
+
+// r = b - t (FP64) and its float copy
+__global__ void dvec_residual_kernel(const double* __restrict__ b, const double* __restrict__ t, double* __restrict__ r,
+                                     float* __restrict__ rf, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double v = b[i] - t[i];
+        r[i] = v;
+        rf[i] = (float)v;
+    }
+}
+
+// out = (float) a
+__global__ void dvec_to_f_kernel(const double* __restrict__ a, float* __restrict__ out, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)a[i];
+}
+
+// x += d (FP64 from FP32)
+__global__ void dvec_add_f_kernel(double* __restrict__ x, const float* __restrict__ d, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)d[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct LearnedNet {
+    int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
+    std::vector<int> woff;            // each layer's first weight
+    float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    float* act = nullptr;             // layers x [8][V]: the input of each layer of N
+    float* dec = nullptr;             // (layers + 1) x [8][V]: dec[L] = N r, dec[l] = L_l^T dec[l + 1]
+    float* gbuf[2] = {nullptr, nullptr};   // [8][V] input gradients (ping-pong)
+    float* gz = nullptr;              // [4][V] output gradient
+    float* z = nullptr;               // 4V site-major output
+    float* part = nullptr;            // nblk x 576 weight-gradient partials
+    double* dpart = nullptr;          // grid doubles of dot partials
+    double* hpart = nullptr;          // pinned host copy of dpart
+    size_t hpart_cap = 0;             // doubles in dpart and hpart
+    int adam_t = 0;
+    float skip = 0.f;                 // M(r) = skip r + N(r)
+    // training pairs: npairs x (r, e), 4V floats each, scaled to |e| = 1
+    float* pairs = nullptr;
+    int npairs = 0, pair_cap = 0;
+    // FP64 and FP32 scratch of the pair builder and of the solver
+    double *d0 = nullptr, *d1 = nullptr, *d2 = nullptr;
+    float *f0 = nullptr, *f1 = nullptr, *f2 = nullptr, *f3 = nullptr;
+    float* Zs = nullptr;              // restart x 4V: preconditioned directions
+    float* Ws = nullptr;              // restart x 4V: their images under A
+    int restart = 0;
+};
+
+namespace {
+
+int cout_of(const LearnedNet* n, int l) { return l == n->layers - 1 ? kNetOut : kNetC; }
+
+cudaError_t alloc_f(float** p, size_t n) { return cudaMalloc(p, sizeof(float) * (n ? n : 1)); }
+cudaError_t alloc_d(double** p, size_t n) { return cudaMalloc(p, sizeof(double) * (n ? n : 1)); }
+
+// sum of the dot partials of the last dot launch (in block order)
+cudaError_t host_sum(LearnedNet* n, cudaStream_t s, double* out)
+{
+    cudaError_t e = cudaMemcpyAsync(n->hpart, n->dpart, sizeof(double) * n->grid, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    double t = 0.0;
+    for (int i = 0; i < n->grid; ++i) t += n->hpart[i];
+    *out = t;
+    return e;
+}
+
+}  // namespace
+
+namespace {
+
+using DiracArgs = NetOp;
+
+// out = D^dag D in (K = 1), FP64 or FP32 (tmp: scratch of the same type)
+cudaError_t apply_A(const DiracArgs& d, const void* in, void* tmp, void* out, int prec, cudaStream_t s)
+{
+    cudaError_t e = launch_dirac(in, tmp, d.sigma, d.Nt, d.Nx, d.m0, d.g, d.r, 0, prec, 1, s);
+    if (e == cudaSuccess) e = launch_dirac(tmp, out, d.sigma, d.Nt, d.Nx, d.m0, d.g, d.r, 1, prec, 1, s);
+    return e;
+}
+
+cudaError_t ensure_scratch(LearnedNet* n, int restart)
+{
+    const size_t V4 = 4 * (size_t)n->V;
+    cudaError_t e = cudaSuccess;
+    if (!n->d0) e = alloc_d(&n->d0, V4);
+    if (e == cudaSuccess && !n->d1) e = alloc_d(&n->d1, V4);
+    if (e == cudaSuccess && !n->d2) e = alloc_d(&n->d2, V4);
+    if (e == cudaSuccess && !n->f0) e = alloc_f(&n->f0, V4);
+    if (e == cudaSuccess && !n->f1) e = alloc_f(&n->f1, V4);
+    if (e == cudaSuccess && !n->f2) e = alloc_f(&n->f2, V4);
+    if (e == cudaSuccess && !n->f3) e = alloc_f(&n->f3, V4);
+    if (e == cudaSuccess && restart > n->restart) {
+        if (n->Zs) cudaFree(n->Zs);
+        if (n->Ws) cudaFree(n->Ws);
+        n->Zs = n->Ws = nullptr;
+        e = alloc_f(&n->Zs, (size_t)restart * V4);
+        if (e == cudaSuccess) e = alloc_f(&n->Ws, (size_t)restart * V4);
+        n->restart = e == cudaSuccess ? restart : 0;
+    }
+    return e;
+}
+
+cudaError_t dot_f(LearnedNet* n, const float* a, const float* b, cudaStream_t s, double* out)
+{
+    fvec_dot_kernel<<<n->grid, kNetThreads, 0, s>>>(a, b, n->dpart, 4 * n->V);
+    return host_sum(n, s, out);
+}
+
+cudaError_t dot_d(LearnedNet* n, const double* a, const double* b, cudaStream_t s, double* out)
+{
+    dvec_dot_kernel<<<n->grid, kNetThreads, 0, s>>>(a, b, n->dpart, 4 * n->V);
+    return host_sum(n, s, out);
+}
+
+}  // namespace
+
+void net_destroy(LearnedNet* n)
+{
+    if (!n) return;
+    float* fs[] = {n->w, n->g, n->m, n->v, n->act, n->dec, n->gbuf[0], n->gbuf[1], n->gz, n->z, n->part, n->pairs,
+                   n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws};
+    for (float* p : fs)
+        if (p) cudaFree(p);
+    double* ds[] = {n->dpart, n->d0, n->d1, n->d2};
+    for (double* p : ds)
+        if (p) cudaFree(p);
+    if (n->hpart) cudaFreeHost(n->hpart);
+    delete n;
+}
+
+int net_size(const LearnedNet* n) { return n->nw; }
+
+void net_set_skip(LearnedNet* n, float skip) { n->skip = skip; }
+
+LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
+{
+    LearnedNet* n = new LearnedNet();
+    n->Nt = Nt;
+    n->Nx = Nx;
+    n->V = Nt * Nx;
+    n->layers = layers;
+    for (int l = 0; l < layers; ++l) {
+        n->woff.push_back(n->nw);
+        n->nw += 9 * kNetC * cout_of(n, l);
+    }
+    const size_t V = (size_t)n->V;
+    n->grid = (int)std::min<size_t>((V + kNetThreads - 1) / kNetThreads, 1024);
+    n->nblk = (int)std::min<size_t>((V + kWTile - 1) / kWTile, 512);
+    cudaError_t e = alloc_f(&n->w, n->nw);
+    if (e == cudaSuccess) e = alloc_f(&n->g, n->nw);
+    if (e == cudaSuccess) e = alloc_f(&n->m, n->nw);
+    if (e == cudaSuccess) e = alloc_f(&n->v, n->nw);
+    if (e == cudaSuccess) e = alloc_f(&n->act, (size_t)layers * kNetC * V);
+    if (e == cudaSuccess) e = alloc_f(&n->dec, (size_t)(layers + 1) * kNetC * V);
+    if (e == cudaSuccess) e = alloc_f(&n->gbuf[0], kNetC * V);
+    if (e == cudaSuccess) e = alloc_f(&n->gbuf[1], kNetC * V);
+    if (e == cudaSuccess) e = alloc_f(&n->gz, kNetOut * V);
+    if (e == cudaSuccess) e = alloc_f(&n->z, 4 * V);
+    if (e == cudaSuccess) e = alloc_f(&n->part, (size_t)n->nblk * 9 * kNetC * kNetC);
+    if (e == cudaSuccess) e = alloc_d(&n->dpart, n->grid);
+    if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * n->grid);
+    if (e == cudaSuccess) n->hpart_cap = (size_t)n->grid;
+    if (e == cudaSuccess) e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
+    if (e == cudaSuccess) e = cudaMemset(n->v, 0, sizeof(float) * n->nw);
+    if (e == cudaSuccess) e = cudaMemset(n->g, 0, sizeof(float) * n->nw);
+    if (e != cudaSuccess) {
+        net_destroy(n);
+        n = nullptr;
+    }
+    *err = e;
+    return n;
+}
+
+cudaError_t net_weights(LearnedNet* n, float* host, bool set)
+{
+    if (set) {
+        n->adam_t = 0;
+        cudaError_t e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
+        if (e == cudaSuccess) e = cudaMemset(n->v, 0, sizeof(float) * n->nw);
+        if (e == cudaSuccess) e = cudaMemcpy(n->w, host, sizeof(float) * n->nw, cudaMemcpyHostToDevice);
+        return e;
+    }
+    return cudaMemcpy(host, n->w, sizeof(float) * n->nw, cudaMemcpyDeviceToHost);
+}
+
+// z = M(r): r, z 4V floats site-major; sigma the chain's field
+namespace {
+
+// conv of layer l (8 -> cout_l channels)
+void conv_fwd(LearnedNet* n, int l, const float* X, float* Y, cudaStream_t s)
+{
+    if (cout_of(n, l) == kNetOut)
+        net_conv_fwd_kernel<kNetOut, false><<<n->grid, kNetThreads, 0, s>>>(X, Y, n->w + n->woff[l], n->Nt, n->Nx);
+    else
+        net_conv_fwd_kernel<kNetC, false><<<n->grid, kNetThreads, 0, s>>>(X, Y, n->w + n->woff[l], n->Nt, n->Nx);
+}
+
+// transposed conv of layer l (cout_l -> 8 channels)
+void conv_T(LearnedNet* n, int l, const float* Y, float* X, cudaStream_t s)
+{
+    if (cout_of(n, l) == kNetOut)
+        net_conv_bwd_in_kernel<kNetOut><<<n->grid, kNetThreads, 0, s>>>(Y, X, n->w + n->woff[l], n->Nt, n->Nx);
+    else
+        net_conv_bwd_in_kernel<kNetC><<<n->grid, kNetThreads, 0, s>>>(Y, X, n->w + n->woff[l], n->Nt, n->Nx);
+}
+
+// g[layer l] += sum_n s_k(n) X[i, nb_k(n)] Y[o, n]  (X 8 channels, Y cout_l)
+void conv_wgrad(LearnedNet* n, int l, const float* X, const float* Y, cudaStream_t s)
+{
+    const int co = cout_of(n, l);
+    if (co == kNetOut)
+        net_conv_bwd_w_kernel<kNetOut, false><<<n->nblk, kNetThreads, 0, s>>>(X, Y, n->part, n->Nt, n->Nx);
+    else
+        net_conv_bwd_w_kernel<kNetC, false><<<n->nblk, kNetThreads, 0, s>>>(X, Y, n->part, n->Nt, n->Nx);
+    const int nwl = 9 * kNetC * co;
+    net_reduce_w_kernel<<<(nwl + 255) / 256, 256, 0, s>>>(n->part, n->nblk, nwl, n->g + n->woff[l]);
+}
+
+float* act_of(LearnedNet* n, int l) { return n->act + (size_t)l * kNetC * n->V; }
+float* dec_of(LearnedNet* n, int l) { return n->dec + (size_t)l * kNetC * n->V; }
+
+}  // namespace
+
+// z = M(r) = skip r + N^T N r (r, z site-major)
+cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s)
+{
+    const int V = n->V, L = n->layers;
+    net_features_kernel<<<n->grid, kNetThreads, 0, s>>>(r, sigma, n->act, V);
+    for (int l = 0; l < L - 1; ++l) conv_fwd(n, l, act_of(n, l), act_of(n, l + 1), s);
+    conv_fwd(n, L - 1, act_of(n, L - 1), dec_of(n, L), s);
+    for (int l = L - 1; l >= 0; --l) conv_T(n, l, dec_of(n, l + 1), dec_of(n, l), s);
+    net_featT_kernel<<<n->grid, kNetThreads, 0, s>>>(n->dec, sigma, r, n->skip, z, V);
+    return cudaGetLastError();
+}
+
+// The loss of a pair (r, e): the energy norm of the error left by the
+// correction M(r), L = (M r - e)^T A (M r - e) = |D (M r - e)|^2 (A = D^dag D;
+// the pairs are scaled to e^T A e = 1).  The plain norm |M r - e|^2 would be
+// dominated by the smooth, low modes of e and train a network whose output
+// never corrects the high modes that dominate the residual.  Leaves
+// d = M r - e in f0, D d in f1 and the loss partials in dpart.
+cudaError_t net_loss_terms(LearnedNet* n, const float* r, const float* e, const DiracArgs& op, cudaStream_t s)
+{
+    cudaError_t err = ensure_scratch(n, 0);
+    if (err == cudaSuccess) err = net_forward(n, r, op.sigma, n->z, s);
+    if (err != cudaSuccess) return err;
+    const int V4 = 4 * n->V;
+    net_diff_kernel<<<n->grid, kNetThreads, 0, s>>>(n->z, e, n->f0, V4);
+    err = launch_dirac(n->f0, n->f1, op.sigma, op.Nt, op.Nx, op.m0, op.g, op.r, 0, YK_FP32, 1, s);
+    if (err == cudaSuccess) fvec_dot_kernel<<<n->grid, kNetThreads, 0, s>>>(n->f1, n->f1, n->dpart, V4);
+    return err == cudaSuccess ? cudaGetLastError() : err;
+}
+
+// accumulates into n->g the weight gradient of the pair's loss; *loss (if
+// given) receives its value
+cudaError_t net_accumulate_grad(LearnedNet* n, const float* r, const float* e, const DiracArgs& op, cudaStream_t s,
+                                double* loss)
+{
+    const int V = n->V, L = n->layers;
+    cudaError_t err = net_loss_terms(n, r, e, op, s);
+    if (err != cudaSuccess) return err;
+    // dL/dz = 2 A d = 2 D^dag (D d)
+    err = launch_dirac(n->f1, n->f2, op.sigma, op.Nt, op.Nx, op.m0, op.g, op.r, 1, YK_FP32, 1, s);
+    if (err != cudaSuccess) return err;
+    net_gz_kernel<<<n->grid, kNetThreads, 0, s>>>(n->f2, n->gz, V);
+    // through F^T and the transposed layers (dec[l] = L_l^T dec[l + 1]):
+    // the weight gradient of a transposed conv has the conv's form with the
+    // roles of input and output swapped, and the gradient flows on by the conv
+    net_feat_cm_kernel<<<n->grid, kNetThreads, 0, s>>>(n->gz, op.sigma, n->gbuf[0], V);
+    int cur = 0;
+    for (int l = 0; l < L; ++l) {
+        conv_wgrad(n, l, n->gbuf[cur], dec_of(n, l + 1), s);
+        if (l < L - 1) {
+            conv_fwd(n, l, n->gbuf[cur], n->gbuf[cur ^ 1], s);
+            cur ^= 1;
+        } else {
+            conv_fwd(n, l, n->gbuf[cur], n->gz, s);   // the gradient of N r
+        }
+    }
+    // through N
+    const float* gy = n->gz;
+    for (int l = L - 1; l >= 0; --l) {
+        conv_wgrad(n, l, act_of(n, l), gy, s);
+        if (l > 0) {
+            float* gx = n->gbuf[l & 1];
+            conv_T(n, l, gy, gx, s);
+            gy = gx;
+        }
+    }
+    err = cudaGetLastError();
+    if (err == cudaSuccess && loss) {
+        // the loss partials were written by net_loss_terms into dpart
+        err = host_sum(n, s, loss);
+    }
+    return err;
+}
+
+cudaError_t net_zero_grad(LearnedNet* n, cudaStream_t s) { return cudaMemsetAsync(n->g, 0, sizeof(float) * n->nw, s); }
+
+cudaError_t net_grad_to_host(LearnedNet* n, float* host, cudaStream_t s)
+{
+    cudaError_t e = cudaMemcpyAsync(host, n->g, sizeof(float) * n->nw, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
+// one Adam step on the accumulated gradient of `batch` pairs
+cudaError_t net_adam_step(LearnedNet* n, float lr, int batch, cudaStream_t s)
+{
+    n->adam_t += 1;
+    const float c1 = 1.f / (1.f - powf(0.9f, (float)n->adam_t)), c2 = 1.f / (1.f - powf(0.999f, (float)n->adam_t));
+    net_adam_kernel<<<(n->nw + 255) / 256, 256, 0, s>>>(n->w, n->g, n->m, n->v, n->nw, lr, c1, c2, 1.f / batch);
+    return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void dvec_sub_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) c[i] = a[i] - b[i];
+}
+
+// one training pair, scaled: r = (b - A xk) * sc, e = (x* - xk) * sc (= e_in * sc)
+__global__ void pair_make_kernel(const double* __restrict__ b, const double* __restrict__ Axk,
+                                 const double* __restrict__ e, double sc, float* __restrict__ pr,
+                                 float* __restrict__ pe, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        pr[i] = (float)((b[i] - Axk[i]) * sc);
+        pe[i] = (float)(e[i] * sc);
+    }
+}
+
+}  // namespace
+
+// Adds the training pair (b - A xk, x* - xk), scaled to e^T A e = 1, to the
+// network's pair store (capacity cap pairs).  Returns cudaErrorInvalidValue
+// when the error vanishes (x* = xk).
+cudaError_t net_add_pair(LearnedNet* n, int cap, const double* sigma, double m0, double g, double r, const double* b,
+                         const double* xstar, const double* xk, cudaStream_t s)
+{
+    const size_t V4 = 4 * (size_t)n->V;
+    cudaError_t e = ensure_scratch(n, 0);
+    if (e != cudaSuccess) return e;
+    if (!n->pairs || cap != n->pair_cap) {
+        if (n->pairs) cudaFree(n->pairs);
+        n->pairs = nullptr;
+        n->npairs = 0;
+        e = alloc_f(&n->pairs, (size_t)cap * 2 * V4);
+        if (e != cudaSuccess) return e;
+        n->pair_cap = cap;
+    }
+    if (n->npairs >= n->pair_cap) return cudaSuccess;   // full: ignore
+    const DiracArgs d = {sigma, n->Nt, n->Nx, m0, g, r};
+    e = apply_A(d, xk, n->d0, n->d1, YK_FP64, s);
+    if (e != cudaSuccess) return e;
+    dvec_sub_kernel<<<n->grid, kNetThreads, 0, s>>>(xstar, xk, n->d2, (int)V4);
+    dvec_sub_kernel<<<n->grid, kNetThreads, 0, s>>>(b, n->d1, n->d0, (int)V4);
+    // e^T A e through A e = b - A xk (x* solves to the tolerance)
+    double ee = 0.0;
+    e = dot_d(n, n->d2, n->d0, s, &ee);
+    if (e != cudaSuccess) return e;
+    if (!(ee > 0.0)) return cudaErrorInvalidValue;
+    float* pr = n->pairs + (size_t)n->npairs * 2 * V4;
+    pair_make_kernel<<<n->grid, kNetThreads, 0, s>>>(b, n->d1, n->d2, 1.0 / std::sqrt(ee), pr, pr + V4, (int)V4);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) n->npairs += 1;
+    return e;
+}
+
+int net_pairs(const LearnedNet* n) { return n->npairs; }
+
+// mean of |M(r) - e|^2 over the stored pairs
+cudaError_t net_mean_loss(LearnedNet* n, const DiracArgs& op, cudaStream_t s, double* out)
+{
+    const size_t V4 = 4 * (size_t)n->V;
+    double sum = 0.0;
+    for (int p = 0; p < n->npairs; ++p) {
+        const float* pr = n->pairs + (size_t)p * 2 * V4;
+        cudaError_t e = net_loss_terms(n, pr, pr + V4, op, s);
+        if (e != cudaSuccess) return e;
+        double l = 0.0;
+        e = host_sum(n, s, &l);
+        if (e != cudaSuccess) return e;
+        sum += l;
+    }
+    *out = n->npairs ? sum / n->npairs : 0.0;
+    return cudaSuccess;
+}
+
+// `steps` Adam steps on mini-batches of `batch` stored pairs drawn by a
+// xorshift generator from `seed`
+cudaError_t net_train(LearnedNet* n, const DiracArgs& op, int steps, int batch, float lr, uint64_t seed,
+                      cudaStream_t s)
+{
+    if (n->npairs == 0) return cudaErrorInvalidValue;
+    const size_t V4 = 4 * (size_t)n->V;
+    uint64_t st = seed ? seed : 0x9E3779B97F4A7C15ull;
+    for (int it = 0; it < steps; ++it) {
+        cudaError_t e = net_zero_grad(n, s);
+        for (int b = 0; b < batch && e == cudaSuccess; ++b) {
+            st ^= st << 13;
+            st ^= st >> 7;
+            st ^= st << 17;
+            const float* pr = n->pairs + (size_t)(st % (uint64_t)n->npairs) * 2 * V4;
+            e = net_accumulate_grad(n, pr, pr + V4, op, s, nullptr);
+        }
+        if (e == cudaSuccess) e = net_adam_step(n, lr, batch, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaStreamSynchronize(s);
+}
+
+namespace {
+
+// part[i * gridDim.x + block] = partial of <Ws[i], w>, i < cnt (Ws contiguous, n floats each)
+__global__ void __launch_bounds__(kNetThreads) fvec_multidot_kernel(const float* __restrict__ Ws, int cnt,
+                                                                    const float* __restrict__ w,
+                                                                    double* __restrict__ part, int n)
+{
+    __shared__ double red[32];
+    for (int i = 0; i < cnt; ++i) {
+        const float* a = Ws + (size_t)i * n;
+        double s = 0.0;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+            s = fma((double)a[j], (double)w[j], s);
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) part[(size_t)i * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+    }
+}
+
+// part[0][block] = partial <w, w>, part[1][block] = partial <w, r>
+__global__ void __launch_bounds__(kNetThreads) fvec_dot2_kernel(const float* __restrict__ w, const float* __restrict__ r,
+                                                                double* __restrict__ part, int n)
+{
+    __shared__ double red[64];
+    double s0 = 0.0, s1 = 0.0;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const double wj = (double)w[j];
+        s0 = fma(wj, wj, s0);
+        s1 = fma(wj, (double)r[j], s1);
+    }
+    const double2 t = block_sum2(s0, s1, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = t.x;
+        part[gridDim.x + blockIdx.x] = t.y;
+    }
+}
+
+// y -= sum_i c[i] Xs[i] (c in constant-size argument arrays)
+constexpr int kMaxRestart = 32;
+struct Coefs {
+    float c[kMaxRestart];
+};
+
+__global__ void fvec_multi_axpy_kernel(float* __restrict__ y, const float* __restrict__ Xs, int cnt, Coefs c, int n)
+{
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        float v = y[j];
+        for (int i = 0; i < cnt; ++i) v = fmaf(-c.c[i], Xs[(size_t)i * n + j], v);
+        y[j] = v;
+    }
+}
+
+cudaError_t ensure_parts(LearnedNet* n, int segs)
+{
+    const size_t need = (size_t)segs * n->grid;
+    if (n->hpart_cap >= need) return cudaSuccess;
+    if (n->dpart) cudaFree(n->dpart);
+    if (n->hpart) cudaFreeHost(n->hpart);
+    n->dpart = nullptr;
+    n->hpart = nullptr;
+    cudaError_t e = alloc_d(&n->dpart, need);
+    if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * need);
+    n->hpart_cap = e == cudaSuccess ? need : 0;
+    return e;
+}
+
+// sums of `segs` consecutive partial segments (block order)
+cudaError_t host_sums(LearnedNet* n, int segs, cudaStream_t s, double* out)
+{
+    cudaError_t e =
+        cudaMemcpyAsync(n->hpart, n->dpart, sizeof(double) * segs * n->grid, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (int k = 0; k < segs; ++k) {
+        double t = 0.0;
+        for (int i = 0; i < n->grid; ++i) t += n->hpart[(size_t)k * n->grid + i];
+        out[k] = t;
+    }
+    return e;
+}
+
+}  // namespace
+
+// Restarted flexible GCR (FP32) with z = M(r) (the network) or z = r as the
+// preconditioner, inside FP64 iterative refinement: x = 0; repeat
+// r = b - A x (FP64); solve A d = r to relative `inner_tol` by FGCR (at most
+// `restart` directions); x += d; until |r|^2 <= stop2 or max_iter FGCR
+// iterations.  A = D^dag D (K = 1); b, x: 4V doubles (device).  Classical
+// Gram-Schmidt of A z against the stored directions, all its dots in one
+// launch: two host synchronisations per iteration.
+cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                       const double* b, double* x, double tol, int tol_mode, int max_iter, int restart,
+                       double inner_tol, cudaStream_t s, FgcrResult* res)
+{
+    if (restart < 1) restart = 1;
+    if (restart > kMaxRestart) restart = kMaxRestart;
+    const int V4 = 4 * n->V;
+    const DiracArgs d = {sigma, n->Nt, n->Nx, m0, g, r};
+    cudaError_t e = ensure_scratch(n, restart);
+    if (e == cudaSuccess) e = ensure_parts(n, restart + 2);
+    if (e != cudaSuccess) return e;
+    double* Ax = n->d1;
+    double* r64 = n->d2;
+    float* rf = n->f0;
+    float* dd = n->f1;
+    float* rin = n->f2;
+    float* tmp = n->f3;
+    e = cudaMemsetAsync(x, 0, sizeof(double) * V4, s);
+    double bb = 0.0;
+    if (e == cudaSuccess) e = dot_d(n, b, b, s, &bb);
+    if (e != cudaSuccess) return e;
+    const double stop2 = tol_mode == YK_TOL_REL ? tol * tol * bb : tol * tol;
+    double rr = bb, ww[kMaxRestart], sums[kMaxRestart + 2];
+    int iters = 0, outer = 0;
+    e = cudaMemcpyAsync(r64, b, sizeof(double) * V4, cudaMemcpyDeviceToDevice, s);   // r = b (x = 0)
+    while (e == cudaSuccess && rr > stop2 && iters < max_iter) {
+        ++outer;
+        // the FP32 copy of the residual, the correction and the inner residual
+        dvec_to_f_kernel<<<n->grid, kNetThreads, 0, s>>>(r64, rf, V4);
+        e = cudaMemsetAsync(dd, 0, sizeof(float) * V4, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(rin, rf, sizeof(float) * V4, cudaMemcpyDeviceToDevice, s);
+        double rin2 = 0.0;
+        if (e == cudaSuccess) e = dot_f(n, rin, rin, s, &rin2);
+        const double rin2_0 = rin2;
+        for (int j = 0; j < restart && e == cudaSuccess && iters < max_iter; ++j) {
+            float* Zj = n->Zs + (size_t)j * V4;
+            float* Wj = n->Ws + (size_t)j * V4;
+            if (use_net)
+                e = net_forward(n, rin, sigma, Zj, s);
+            else
+                e = cudaMemcpyAsync(Zj, rin, sizeof(float) * V4, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = apply_A(d, Zj, tmp, Wj, YK_FP32, s);
+            if (e == cudaSuccess && j > 0) {
+                fvec_multidot_kernel<<<n->grid, kNetThreads, 0, s>>>(n->Ws, j, Wj, n->dpart, V4);
+                e = host_sums(n, j, s, sums);
+                Coefs c = {};
+                for (int i = 0; i < j; ++i) c.c[i] = (float)(sums[i] / ww[i]);
+                fvec_multi_axpy_kernel<<<n->grid, kNetThreads, 0, s>>>(Wj, n->Ws, j, c, V4);
+                fvec_multi_axpy_kernel<<<n->grid, kNetThreads, 0, s>>>(Zj, n->Zs, j, c, V4);
+            }
+            if (e != cudaSuccess) break;
+            fvec_dot2_kernel<<<n->grid, kNetThreads, 0, s>>>(Wj, rin, n->dpart, V4);
+            e = host_sums(n, 2, s, sums);
+            if (e != cudaSuccess) break;
+            ww[j] = sums[0];
+            if (!(ww[j] > 0.0)) break;
+            const double alpha = sums[1] / ww[j];
+            fvec_axpy_kernel<<<n->grid, kNetThreads, 0, s>>>(dd, Zj, (float)alpha, V4);
+            fvec_axpy_kernel<<<n->grid, kNetThreads, 0, s>>>(rin, Wj, (float)-alpha, V4);
+            rin2 -= sums[1] * sums[1] / ww[j];
+            ++iters;
+            if (rin2 <= inner_tol * inner_tol * rin2_0) break;
+        }
+        if (e != cudaSuccess) break;
+        // x += d; r = b - A x in FP64
+        dvec_add_f_kernel<<<n->grid, kNetThreads, 0, s>>>(x, dd, V4);
+        e = apply_A(d, x, n->d0, Ax, YK_FP64, s);
+        if (e == cudaSuccess) dvec_residual_kernel<<<n->grid, kNetThreads, 0, s>>>(b, Ax, r64, rf, V4);
+        if (e == cudaSuccess) e = dot_d(n, r64, r64, s, &rr);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    res->iterations = iters;
+    res->outer = outer;
+    res->rr = rr;
+    res->rr0 = bb;
+    res->converged = rr <= stop2 ? 1 : 0;
+    return e;
+}
+
+}  // namespace yk
