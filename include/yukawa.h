@@ -216,6 +216,10 @@ int yk_net_size(yk_ctx* ctx, int chain);
 int yk_net_weights(yk_ctx* ctx, int chain, float* host, int set);
 /* z = M(r) for device r, z (4V floats each, site-major), sigma the chain's field. */
 int yk_net_apply(yk_ctx* ctx, int chain, const float* r, float* z);
+/* As yk_net_apply, through the TF32 tensor-core convolutions (FP32
+ * accumulation) that yk_fgcr_solve, yk_pcg_solve and
+ * yk_langevin_step_learned apply. */
+int yk_net_apply_tc(yk_ctx* ctx, int chain, const float* r, float* z);
 /* Weight gradient (host, yk_net_size floats) and value of the training loss
  * (M r - e)^T A (M r - e) = |D (M r - e)|^2 for device r, e (4V floats
  * each): the energy norm of the error left by the correction M r. */
@@ -231,6 +235,12 @@ int yk_net_train(yk_ctx* ctx, int chain, const yk_net_train_cfg* cfg, yk_net_tra
  * FP64 refinement rounds. */
 int yk_fgcr_solve(yk_ctx* ctx, int chain, const double* b, double* x, double tol, int tol_mode, int max_iter,
                   int use_net, yk_solve_stats* stats);
+/* As yk_fgcr_solve, by preconditioned CG (the network's M = s I + N^T N is
+ * symmetric positive definite, so plain PCG applies): FP32 vectors with the
+ * iteration's scalars kept on the device (the host reads |r|^2 every 8
+ * iterations), inside FP64 iterative refinement. */
+int yk_pcg_solve(yk_ctx* ctx, int chain, const double* b, double* x, double tol, int tol_mode, int max_iter,
+                 int use_net, yk_solve_stats* stats);
 
 /* No reference counterpart (failure detection): runs on `stream` (NULL =
  * legacy stream) a two-block kernel in which block 0 waits, through the
@@ -257,6 +267,16 @@ int yk_coloured_noise(yk_ctx* ctx, int chain, const double* white, double* xi);
  * Run kernel langevin_gpu_v2.cu:65-118), fully on the device; the step
  * graph is captured once and replayed. */
 int yk_langevin_step(yk_ctx* ctx, int n_steps);
+
+/* As yk_langevin_step, with every fermion solve of the step done by
+ * yk_pcg_solve (flexible preconditioned CG inside FP64 refinement, to the
+ * context's tolerance) with the chain's network (use_net = 1; every chain
+ * with fermions needs one, see yk_net_setup) or the identity (use_net = 0).
+ * The same sources, force, update and observables as yk_langevin_step; the
+ * solves are driven from the host (not a captured graph).  stats (may be
+ * NULL) sums the solver statistics over the steps' solves.  No reference
+ * counterpart: the reference solves with plain CG (CGsolver.cu:72-170). */
+int yk_langevin_step_learned(yk_ctx* ctx, int n_steps, int use_net, yk_solve_stats* stats);
 
 /* The Run kernel (code/src/langevin_gpu_v2.cu:65-118, launched at main.cu:377)
  * on injected inputs: drift = force + phi (m^2 + lambda/6 phi^2) - Lap phi,

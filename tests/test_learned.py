@@ -4,8 +4,9 @@ solve (GPU).
 
 Tolerances: the oracle's gradients against central finite differences 1e-6
 relative; the FP32 network against the FP64 oracle 2e-6 (forward) and 2e-5
-(weight gradients) relative to the largest entry; every solve to the FP64
-relative residual 1e-10.
+(weight gradients) relative to the largest entry, its TF32 tensor-core form
+(the one the solvers apply) 5e-3; every solve to the FP64 relative residual
+1e-10.
 """
 import numpy as np
 import pytest
@@ -89,6 +90,10 @@ def test_network_forward_and_gradient_match_oracle(ylib, cuda):
         ctx.net_apply(rd, zd)
         want = N.apply_M(W32, r.T.astype(np.float64), sig, Nt, Nx, np.float32(0.05))[0]
         assert np.abs(zd.cpu().numpy().T - want).max() < 2e-6 * np.abs(want).max()
+        # the solvers' form: TF32 tensor-core convolutions (11-bit significands)
+        ctx.net_apply(rd, zd, tensor_cores=True)
+        err = np.abs(zd.cpu().numpy().T - want).max() / np.abs(want).max()
+        assert err < 5e-3, err
         g, loss = ctx.net_grad(rd, ed)
         lo, go = N.energy_loss_and_grad(W32, r.T.astype(np.float64), e.T.astype(np.float64), sig, Nt, Nx,
                                         _action(0.1), np.float32(0.05))
@@ -119,16 +124,46 @@ def test_trained_network_cuts_iterations(ylib, cuda):
         sig = ctx.get_field()
         a = O.action(m2=p.mass, lam=p.g, g=p.yukawa_coupling, m0=p.fermion_mass, r=p.wilson_param,
                      cut_fraction=p.cut_fraction, eps_bar=p.average_epsilon, drift_mode=p.drift_mode)
-        for use in (False, True):
-            x = torch.zeros_like(bd)
-            s = ctx.fgcr_solve(bd, x, tol=1e-10, max_iter=20000, use_net=use)
-            assert s.converged == 1 and s.rr <= 1e-20 * s.rr0
-            xs = x.cpu().numpy().astype(np.complex128)
-            Ax = O.dirac(Nt, Nx, a, sig, O.dirac(Nt, Nx, a, sig, xs, False), True)
-            assert np.linalg.norm(Ax - b) < 1e-9 * np.linalg.norm(b)
-            its[use] = s.iterations
+        for solver in ("fgcr", "pcg"):
+            for use in (False, True):
+                x = torch.zeros_like(bd)
+                s = getattr(ctx, solver + "_solve")(bd, x, tol=1e-10, max_iter=20000, use_net=use)
+                assert s.converged == 1 and s.rr <= 1e-20 * s.rr0
+                xs = x.cpu().numpy().astype(np.complex128)
+                Ax = O.dirac(Nt, Nx, a, sig, O.dirac(Nt, Nx, a, sig, xs, False), True)
+                assert np.linalg.norm(Ax - b) < 1e-9 * np.linalg.norm(b)
+                its[solver, use] = s.iterations
         xc = torch.zeros(V, 4, dtype=torch.complex128, device="cuda")
         cg = ctx.cg_solve(torch.complex(bd, torch.zeros_like(bd)).contiguous(), xc, tol=1e-10,
                           tol_mode=yk.YK_TOL_REL, max_iter=20000, precision=yk.YK_MIXED)
-        assert its[True] * 5 < its[False], its
-        assert its[True] < cg.iterations, (its, cg.iterations)
+        assert its["fgcr", True] * 5 < its["fgcr", False], its
+        assert its["fgcr", True] < cg.iterations, (its, cg.iterations)
+        assert its["pcg", True] * 3 < its["pcg", False], its
+        assert its["pcg", True] < cg.iterations, (its, cg.iterations)
+
+
+@pytest.mark.gpu
+def test_learned_step_matches_cg_step(ylib, cuda):
+    # the same Langevin steps with every fermion solve by the learned PCG
+    # (network and identity) and by the step graph's FP64 CG: the fields agree
+    # to the solves' tolerance (rel-res 1e-10 gives a force error ~1e-10)
+    yk, torch = ylib, cuda
+    Nt, Nx = 32, 32
+    fields = {}
+    for mode in ("cg", "identity", "net"):
+        with yk.Context(_params(yk, Nt, Nx, 0.05, yk.YK_FP64)) as ctx:
+            if mode == "net":
+                ctx.net_setup(4, 7)
+                ctx.net_train(n_sources=2, n_levels=4, base_iter=4, steps=100, batch=4, lr=2e-3, seed=3)
+            if mode == "cg":
+                ctx.step(3)
+            else:
+                st = ctx.step_learned(3, use_net=(mode == "net"))
+                assert st.converged == 1 and st.rr <= 1e-20 * st.rr0 * 3
+            o = ctx.observables()
+            assert o.steps == 3 and o.status == 0 and o.cg_iterations > 0
+            fields[mode] = ctx.get_field()
+    ref = fields["cg"]
+    for mode in ("identity", "net"):
+        err = np.abs(fields[mode] - ref).max() / np.abs(ref).max()
+        assert err < 1e-8, (mode, err)

@@ -153,10 +153,14 @@ _SIGS = {
     "yk_net_size": (C.c_int, [C.c_void_p, C.c_int]),
     "yk_net_weights": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "yk_net_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "yk_net_apply_tc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_net_grad": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "yk_net_train": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(NetTrainCfg), C.POINTER(NetTrainStats)]),
     "yk_fgcr_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(SolveStats)]),
+    "yk_langevin_step_learned": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(SolveStats)]),
+    "yk_pcg_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
+                               C.POINTER(SolveStats)]),
     "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
@@ -306,8 +310,9 @@ class Context:
         assert w.size == self.net_size(chain)
         _check(lib().yk_net_weights(self.h, chain, w.ctypes.data, 1))
 
-    def net_apply(self, r, z, chain=0):
-        _check(lib().yk_net_apply(self.h, chain, _ptr(r), _ptr(z)))
+    def net_apply(self, r, z, chain=0, tensor_cores=False):
+        fn = lib().yk_net_apply_tc if tensor_cores else lib().yk_net_apply
+        _check(fn(self.h, chain, _ptr(r), _ptr(z)))
 
     def net_grad(self, r, e, chain=0):
         import numpy as np
@@ -331,6 +336,14 @@ class Context:
                                    C.byref(st)), ok)
         return st
 
+    def pcg_solve(self, b, x, tol=1e-10, tol_mode=YK_TOL_REL, max_iter=2000, use_net=True, chain=0,
+                  allow_noconv=False) -> SolveStats:
+        st = SolveStats()
+        ok = (YK_OK, YK_ENOCONV) if allow_noconv else (YK_OK,)
+        _check(lib().yk_pcg_solve(self.h, chain, _ptr(b), _ptr(x), tol, tol_mode, max_iter, int(bool(use_net)),
+                                  C.byref(st)), ok)
+        return st
+
     def fermion_force(self, F, eta=None, chain=0) -> SolveStats:
         st = SolveStats()
         _check(lib().yk_fermion_force(self.h, chain, _ptr(eta), _ptr(F), C.byref(st)))
@@ -341,6 +354,11 @@ class Context:
 
     def step(self, n=1):
         _check(lib().yk_langevin_step(self.h, n))
+
+    def step_learned(self, n=1, use_net=True) -> SolveStats:
+        st = SolveStats()
+        _check(lib().yk_langevin_step_learned(self.h, n, int(bool(use_net)), C.byref(st)))
+        return st
 
     def euler_update(self, force, xi, chain=0) -> Obs:
         o = Obs()

@@ -84,6 +84,7 @@ struct Chain {
     double2 *tw_t, *tw_x;
     Workspace ws;
     LearnedNet* net = nullptr;   // the learned preconditioner (yk_net_setup)
+    LearnedNet* pcg_ws = nullptr;   // solver buffers of identity-preconditioned solves without a network
 };
 
 }  // namespace
@@ -935,6 +936,7 @@ int yk_ctx_destroy(yk_ctx* ctx)
     for (auto& C : ctx->ch) {
         if (C.ws.mem) cudaFree(C.ws.mem);
         net_destroy(C.net);
+        net_destroy(C.pcg_ws);
     }
     if (ctx->mem) cudaFree(ctx->mem);
     if (ctx->aux) {
@@ -1405,6 +1407,19 @@ int yk_net_apply(yk_ctx* ctx, int c, const float* r, float* z)
     return YK_OK;
 }
 
+int yk_net_apply_tc(yk_ctx* ctx, int c, const float* r, float* z)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!r || !z) {
+        set_error("yk_net_apply_tc: null buffer");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    YK_CK(net_forward_fast(C.net, r, C.phi, z, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
 int yk_net_grad(yk_ctx* ctx, int c, const float* r, const float* e, float* grad, double* loss)
 {
     if (int rc = net_ok(ctx, c)) return rc;
@@ -1493,6 +1508,92 @@ int yk_fgcr_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, in
     if (stats) *stats = yk_solve_stats{r.iterations, r.outer, r.rr, r.rr0, r.converged};
     if (!r.converged) {
         set_error("yk_fgcr_solve: %d iterations, |r|^2 = %g > the tolerance", r.iterations, r.rr);
+        return YK_ENOCONV;
+    }
+    return YK_OK;
+}
+
+int yk_langevin_step_learned(yk_ctx* ctx, int n_steps, int use_net, yk_solve_stats* stats)
+{
+    if (!ctx || n_steps < 0) {
+        set_error("yk_langevin_step_learned: bad arguments");
+        return YK_EINVAL;
+    }
+    for (size_t c = 0; c < ctx->ch.size(); ++c)
+        if (use_net && ctx->ch[c].n_rhs_step > 0 && !ctx->ch[c].net) {
+            set_error("yk_langevin_step_learned: chain %zu has no network (yk_net_setup)", c);
+            return YK_EINVAL;
+        }
+    std::vector<SysDev> sys(ctx->nsys);
+    std::vector<CGState> st(ctx->nsys);
+    if (ctx->nsys > 0)
+        YK_CK(cudaMemcpy(sys.data(), ctx->d_sys, sizeof(SysDev) * ctx->nsys, cudaMemcpyDeviceToHost));
+    yk_solve_stats tot = {0, 0, 0.0, 0.0, 1};
+    NoiseTables nt = {ctx->d_rows, ctx->nrows, ctx->d_cols, ctx->ncols, ctx->d_white, ctx->nwhite};
+    for (int i = 0; i < n_steps; ++i) {
+        YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
+        for (Chain& C : ctx->ch) {
+            if (C.n_rhs_step == 0) continue;
+            // the step's sources (Philox stream 2 at the chain's step), as the CG would draw them
+            YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles + C.cg_tile0, C.cg_tile1 - C.cg_tile0, 2, ctx->stream));
+            for (int j = 0; j < C.n_rhs_step; ++j) {
+                LearnedNet* net = C.net ? C.net : C.pcg_ws;
+                if (!net) {   // identity preconditioner: an unused network provides the solver's buffers
+                    cudaError_t e = cudaSuccess;
+                    net = C.pcg_ws = net_create(C.Nt, C.Nx, 2, &e);
+                    if (!net) {
+                        set_error("yk_langevin_step_learned: %s", cudaGetErrorString(e));
+                        return YK_ECUDA;
+                    }
+                }
+                const SysDev& S = sys[C.sys0 + j];
+                FgcrResult r = {};
+                YK_CK(pcg_solve(net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, S.b, S.x, ctx->tol, ctx->tol_mode,
+                                ctx->max_iter, 1e-4, ctx->stream, &r));
+                CGState& q = st[C.sys0 + j];
+                std::memset(&q, 0, sizeof(q));
+                q.rr = r.rr;
+                q.rr0 = r.rr0;
+                q.iters = r.iterations;
+                q.converged = r.converged;
+                q.status = r.converged ? 0 : YK_ENOCONV;
+                q.n_ru = r.outer;
+                tot.iterations += r.iterations;
+                tot.reliable_updates += r.outer;
+                tot.rr += r.rr;
+                tot.rr0 += r.rr0;
+                if (!r.converged) tot.converged = 0;
+            }
+        }
+        if (ctx->nsys > 0)
+            YK_CK(cudaMemcpyAsync(ctx->d_state, st.data(), sizeof(CGState) * ctx->nsys, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+        StepArgs s = step_args(ctx);
+        YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream, nullptr));
+        YK_CK(launch_update(s, ctx->d_state, ctx->stream));
+        // st is reused by the next step: its copy must have left the host
+        YK_CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (stats) *stats = tot;
+    return YK_OK;
+}
+
+int yk_pcg_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, int tol_mode, int max_iter, int use_net,
+                 yk_solve_stats* stats)
+{
+    if (int rc = net_ok(ctx, c)) return rc;
+    if (!b || !x || b == x || max_iter < 0 || !(tol >= 0.0) || (tol_mode != YK_TOL_ABS && tol_mode != YK_TOL_REL)) {
+        set_error("yk_pcg_solve: bad arguments");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    FgcrResult r = {};
+    YK_CK(pcg_solve(C.net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, b, x, tol, tol_mode, max_iter, 1e-4,
+                    ctx->stream, &r));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (stats) *stats = yk_solve_stats{r.iterations, r.outer, r.rr, r.rr0, r.converged};
+    if (!r.converged) {
+        set_error("yk_pcg_solve: %d iterations, |r|^2 = %g > the tolerance", r.iterations, r.rr);
         return YK_ENOCONV;
     }
     return YK_OK;

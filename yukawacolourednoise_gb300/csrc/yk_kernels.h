@@ -89,6 +89,8 @@ int net_size(const LearnedNet* n);
 void net_set_skip(LearnedNet* n, float skip);   // M(r) = skip r + N(r)
 cudaError_t net_weights(LearnedNet* n, float* host, bool set);
 cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);
+// the same with TF32 tensor-core convolutions (the form the solvers apply)
+cudaError_t net_forward_fast(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);
 cudaError_t net_zero_grad(LearnedNet* n, cudaStream_t s);
 // loss of a pair: (M r - e)^T A (M r - e); accumulates its weight gradient
 cudaError_t net_accumulate_grad(LearnedNet* n, const float* r, const float* e, const NetOp& op, cudaStream_t s,
@@ -103,5 +105,9 @@ cudaError_t net_train(LearnedNet* n, const NetOp& op, int steps, int batch, floa
 cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
                        const double* b, double* x, double tol, int tol_mode, int max_iter, int restart,
                        double inner_tol, cudaStream_t s, FgcrResult* res);
+// preconditioned CG (M SPD) with device-side scalars, inside FP64 refinement
+cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                      const double* b, double* x, double tol, int tol_mode, int max_iter, double inner_tol,
+                      cudaStream_t s, FgcrResult* res);
 
 }  // namespace yk

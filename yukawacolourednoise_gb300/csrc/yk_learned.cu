@@ -18,6 +18,7 @@
 // a + sigma b.  Each weight serves twice (in N and in N^T).
 // Activations are channel-major float arrays [C][V]; the residual and the
 // output are site-major (4 floats per site, the layout of the CG vectors).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -320,13 +321,196 @@ __global__ void dvec_add_f_kernel(double* __restrict__ x, const float* __restric
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)d[i];
 }
 
+// ---- tensor-core convolutions of the solvers' preconditioner ----
+//
+// One 3x3 tap of an 8 -> 8 layer is a [16 sites x 8 in] x [8 in x 8 out]
+// product, exactly one mma.sync m16n8k8 with TF32 inputs and FP32
+// accumulation; a layer is 9 of them per 16 sites.  A warp takes 16
+// consecutive sites; lane (g = lane / 4, c = lane % 4) gathers channels c and
+// c + 4 of the tap's neighbours of sites g and g + 8 (the A fragment) and holds
+// the weights W[k][c][g], W[k][c + 4][g] of every tap (the B fragments) in
+// registers.  The 4-channel layers (the last of N, the first of N^T) pad
+// the product with zero weights.  TF32 keeps 10 mantissa bits: M(r) is then a
+// slightly perturbed operator, which the flexible CG's Polak-Ribiere beta
+// absorbs.  Training and yk_net_apply use the exact FP32 kernels above.
+
+// staged rows a warp loads in the tensor-core convolutions: 8 channels x
+// (R + 2) rows over 8 warps, R <= 8
+constexpr int kStageRows = 10;
+constexpr int kTcMaxR = 8, kTcMaxW = 64;
+// the staged tile s[c][row][col]: staged column j (j = 0: the left halo) at
+// col j + 3, so the interior starts on a 16-byte boundary; row stride kTcSW,
+// channel stride kTcCS = 8 (mod 32) words
+constexpr int kTcSW = kTcMaxW + 8;
+constexpr int kTcCS = ((kTcMaxR + 2) * kTcSW + 23) / 32 * 32 + 8;
+static_assert(kTcCS % 32 == 8 && kTcCS % 4 == 0 && kTcCS >= (kTcMaxR + 2) * kTcSW, "tile channel stride");
+static_assert(kTcSW % 4 == 0 && kTcSW >= kTcMaxW + 5, "tile row stride");
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t to_tf32(float v)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// TRANS = false: Y[COUT][V] = conv(X[8][V]) (the layer of N);
+// TRANS = true: Y[8][V] = conv^T(X[COUT][V]) (its transpose in N^T: the
+// opposite tap, the same sign, W[k] transposed).
+// One block per tile of R x W sites: the tile's input with a one-site halo
+// ((R + 2) x (W + 2) sites, the antiperiodic sign applied to wrapped time
+// rows) is staged in shared memory with coalesced loads, and the A fragments
+// are gathered from there: s[c][row][col], channel stride CS = 8 (mod 32)
+// words, so the 8 sites x 4 channels of a gather fall in 32 distinct banks.
+template <int COUT, bool TRANS>
+__global__ void __launch_bounds__(kNetThreads) net_conv_tc_kernel(const float* __restrict__ X, float* __restrict__ Y,
+                                                                  const float* __restrict__ Wl, int Nt, int Nx,
+                                                                  int R, int W)
+{
+    constexpr int CIN = TRANS ? COUT : kNetC;    // channels gathered
+    constexpr int CO = TRANS ? kNetC : COUT;     // channels written
+    extern __shared__ float sm[];
+    const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
+    const int V = Nt * Nx;
+    const int tiles_x = (Nx + W - 1) / W;
+    const int t0 = (blockIdx.x / tiles_x) * R, x0 = (blockIdx.x % tiles_x) * W;
+    const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
+    constexpr int SW = kTcSW, CS = kTcCS;
+    // stage the tile and its halo with asynchronous copies: warp w takes the
+    // staged rows w, w + 8, ... (channel-major); 16-byte copies of the
+    // interior when rows are 16-byte aligned, else 4-byte copies
+    {
+        const int warp = threadIdx.x >> 5, nrow = CIN * (Rt + 2);
+        const bool vec = (Nx & 3) == 0 && (Wt & 3) == 0;
+        for (int row = warp; row < nrow; row += kNetThreads / 32) {
+            const int ch = row / (Rt + 2), lr = row - ch * (Rt + 2);
+            int t = t0 - 1 + lr;
+            if (t < 0) t += Nt;
+            else if (t >= Nt) t -= Nt;
+            const float* src = X + (size_t)ch * V + (size_t)t * Nx;
+            float* dst = sm + ch * CS + lr * SW + 3;   // staged column 0
+            if (vec) {
+                if (lane < (Wt >> 2)) cp_async16(dst + 1 + 4 * lane, src + x0 + 4 * lane);
+                else if (lane == 30) cp_async4(dst, src + (x0 == 0 ? Nx - 1 : x0 - 1));
+                else if (lane == 31) cp_async4(dst + Wt + 1, src + (x0 + Wt == Nx ? 0 : x0 + Wt));
+            } else {
+                for (int lc = lane; lc < Wt + 2; lc += 32) {
+                    int x = x0 - 1 + lc;
+                    if (x < 0) x += Nx;
+                    else if (x >= Nx) x -= Nx;
+                    cp_async4(dst + lc, src + x);
+                }
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        // the antiperiodic sign of halo rows that wrapped in time
+        const bool top = t0 == 0, bottom = t0 + Rt == Nt;
+        if (top || bottom) {
+            for (int idx = threadIdx.x; idx < CIN * 2 * (Wt + 2); idx += blockDim.x) {
+                const int ch = idx / (2 * (Wt + 2)), rem = idx - ch * 2 * (Wt + 2);
+                const int which = rem / (Wt + 2), lc = rem - which * (Wt + 2);
+                if (which == 0 ? top : bottom) {
+                    float* q = sm + ch * CS + (which == 0 ? 0 : Rt + 1) * SW + 3 + lc;
+                    *q = -*q;
+                }
+            }
+        }
+    }
+    // B fragments: B[kk][j] for the K index kk = c, c + 4 and output j = g
+    uint32_t b0[9], b1[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        float w0 = 0.f, w1 = 0.f;
+        if (!TRANS) {   // B[i][o] = W[k][i][o]
+            if (g < COUT) {
+                w0 = Wl[(k * kNetC + c) * COUT + g];
+                w1 = Wl[(k * kNetC + c + 4) * COUT + g];
+            }
+        } else {        // B[o][i] = W[k][i][o]
+            if (c < COUT) w0 = Wl[(k * kNetC + g) * COUT + c];
+            if (c + 4 < COUT) w1 = Wl[(k * kNetC + g) * COUT + c + 4];
+        }
+        b0[k] = to_tf32(w0);
+        b1[k] = to_tf32(w1);
+    }
+    __syncthreads();
+    const int S = Rt * Wt;
+    for (int base = (threadIdx.x >> 5) * 16; base < S; base += (blockDim.x >> 5) * 16) {
+        const int i0 = base + g, i1 = base + g + 8;
+        const bool in0 = i0 < S, in1 = i1 < S;
+        const int r0 = in0 ? i0 / Wt : 0, c0 = in0 ? i0 - r0 * Wt : 0;
+        const int r1 = in1 ? i1 / Wt : 0, c1 = in1 ? i1 - r1 * Wt : 0;
+        // the sites' centres in the staged tile, channels c and c + 4
+        const float* p0 = sm + c * CS + (r0 + 1) * SW + c0 + 4;
+        const float* p1 = sm + c * CS + (r1 + 1) * SW + c1 + 4;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int kt = TRANS ? 8 - k : k;
+            const int off = (kt / 3 - 1) * SW + (kt % 3 - 1);
+            // FP32 bits as TF32 operands (the low mantissa bits are ignored:
+            // rounding toward zero)
+            uint32_t a[4];
+            a[0] = c < CIN ? __float_as_uint(p0[off]) : 0u;
+            a[1] = c < CIN ? __float_as_uint(p1[off]) : 0u;
+            a[2] = c + 4 < CIN ? __float_as_uint(p0[4 * CS + off]) : 0u;
+            a[3] = c + 4 < CIN ? __float_as_uint(p1[4 * CS + off]) : 0u;
+            mma_tf32(acc, a, b0[k], b1[k]);
+        }
+        // D fragment: rows g, g + 8 (sites), columns 2c, 2c + 1 (output channels)
+        const int n0 = (t0 + r0) * Nx + x0 + c0, n1 = (t0 + r1) * Nx + x0 + c1;
+        const int o0 = 2 * c, o1 = 2 * c + 1;
+        if (o0 < CO) {
+            if (in0) Y[o0 * V + n0] = acc[0];
+            if (in1) Y[o0 * V + n1] = acc[2];
+        }
+        if (o1 < CO) {
+            if (in0) Y[o1 * V + n0] = acc[1];
+            if (in1) Y[o1 * V + n1] = acc[3];
+        }
+    }
+}
+
+// shared memory of a tile (CIN = 8)
+inline size_t conv_tc_smem(int, int) { return sizeof(float) * kNetC * kTcCS; }
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+struct PcgGraph;
+void pcg_graph_destroy(PcgGraph* g);
+
 struct LearnedNet {
     int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
+    int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
+    unsigned* dcnt = nullptr;         // arrival counters of the preconditioned CG's reductions
+    float* sig32 = nullptr;           // FP32 copy of the field of the current solve
     std::vector<int> woff;            // each layer's first weight
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     float* act = nullptr;             // layers x [8][V]: the input of each layer of N
@@ -349,6 +533,9 @@ struct LearnedNet {
     float* Zs = nullptr;              // restart x 4V: preconditioned directions
     float* Ws = nullptr;              // restart x 4V: their images under A
     int restart = 0;
+    double* dsc = nullptr;            // device scalars of the preconditioned CG
+    PcgGraph* pcg = nullptr;          // its captured chunk of iterations
+    bool pcg_no_graph = false;        // capture failed once (e.g. the legacy stream)
 };
 
 namespace {
@@ -423,13 +610,15 @@ void net_destroy(LearnedNet* n)
 {
     if (!n) return;
     float* fs[] = {n->w, n->g, n->m, n->v, n->act, n->dec, n->gbuf[0], n->gbuf[1], n->gz, n->z, n->part, n->pairs,
-                   n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws};
+                   n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws, n->sig32};
     for (float* p : fs)
         if (p) cudaFree(p);
-    double* ds[] = {n->dpart, n->d0, n->d1, n->d2};
+    double* ds[] = {n->dpart, n->d0, n->d1, n->d2, n->dsc};
     for (double* p : ds)
         if (p) cudaFree(p);
     if (n->hpart) cudaFreeHost(n->hpart);
+    pcg_graph_destroy(n->pcg);
+    if (n->dcnt) cudaFree(n->dcnt);
     delete n;
 }
 
@@ -449,8 +638,16 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
         n->nw += 9 * kNetC * cout_of(n, l);
     }
     const size_t V = (size_t)n->V;
-    n->grid = (int)std::min<size_t>((V + kNetThreads - 1) / kNetThreads, 1024);
+    n->grid = (int)std::min<size_t>((V + kNetThreads - 1) / kNetThreads, 4096);
     n->nblk = (int)std::min<size_t>((V + kWTile - 1) / kWTile, 512);
+    // convolution tiles: 64 columns (or the whole row), rows halved from 8
+    // while there are fewer than two tiles per SM
+    int dev = 0, n_sm = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    n->tc_W = std::min(Nx, kTcMaxW);
+    n->tc_R = kTcMaxR;
+    while (n->tc_R > 2 && (int64_t)((Nt + n->tc_R - 1) / n->tc_R) * ((Nx + n->tc_W - 1) / n->tc_W) < 2 * n_sm)
+        n->tc_R /= 2;
     cudaError_t e = alloc_f(&n->w, n->nw);
     if (e == cudaSuccess) e = alloc_f(&n->g, n->nw);
     if (e == cudaSuccess) e = alloc_f(&n->m, n->nw);
@@ -463,6 +660,9 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e == cudaSuccess) e = alloc_f(&n->z, 4 * V);
     if (e == cudaSuccess) e = alloc_f(&n->part, (size_t)n->nblk * 9 * kNetC * kNetC);
     if (e == cudaSuccess) e = alloc_d(&n->dpart, n->grid);
+    if (e == cudaSuccess) e = cudaMalloc(&n->dcnt, sizeof(unsigned) * 4);
+    if (e == cudaSuccess) e = alloc_f(&n->sig32, V);
+    if (e == cudaSuccess) e = cudaMemset(n->dcnt, 0, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * n->grid);
     if (e == cudaSuccess) n->hpart_cap = (size_t)n->grid;
     if (e == cudaSuccess) e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
@@ -524,6 +724,32 @@ void conv_wgrad(LearnedNet* n, int l, const float* X, const float* Y, cudaStream
 float* act_of(LearnedNet* n, int l) { return n->act + (size_t)l * kNetC * n->V; }
 float* dec_of(LearnedNet* n, int l) { return n->dec + (size_t)l * kNetC * n->V; }
 
+// N then N^T on the features in act[0], leaving F^T's input in dec[0]
+// (tensor-core convolutions, one block per tile)
+void net_convs_fast(LearnedNet* n, cudaStream_t s)
+{
+    const int L = n->layers, Nt = n->Nt, Nx = n->Nx, R = n->tc_R, W = n->tc_W;
+    const int grid = ((Nt + R - 1) / R) * ((Nx + W - 1) / W);
+    const size_t sm = conv_tc_smem(R, W);
+    for (int l = 0; l < L; ++l) {
+        float* out = l < L - 1 ? act_of(n, l + 1) : dec_of(n, L);
+        const float* w = n->w + n->woff[l];
+        if (cout_of(n, l) == kNetOut)
+            net_conv_tc_kernel<kNetOut, false><<<grid, kNetThreads, sm, s>>>(act_of(n, l), out, w, Nt, Nx, R, W);
+        else
+            net_conv_tc_kernel<kNetC, false><<<grid, kNetThreads, sm, s>>>(act_of(n, l), out, w, Nt, Nx, R, W);
+    }
+    for (int l = L - 1; l >= 0; --l) {
+        const float* w = n->w + n->woff[l];
+        if (cout_of(n, l) == kNetOut)
+            net_conv_tc_kernel<kNetOut, true><<<grid, kNetThreads, sm, s>>>(dec_of(n, l + 1), dec_of(n, l), w, Nt, Nx,
+                                                                             R, W);
+        else
+            net_conv_tc_kernel<kNetC, true><<<grid, kNetThreads, sm, s>>>(dec_of(n, l + 1), dec_of(n, l), w, Nt, Nx,
+                                                                           R, W);
+    }
+}
+
 }  // namespace
 
 // z = M(r) = skip r + N^T N r (r, z site-major)
@@ -534,6 +760,16 @@ cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, floa
     for (int l = 0; l < L - 1; ++l) conv_fwd(n, l, act_of(n, l), act_of(n, l + 1), s);
     conv_fwd(n, L - 1, act_of(n, L - 1), dec_of(n, L), s);
     for (int l = L - 1; l >= 0; --l) conv_T(n, l, dec_of(n, l + 1), dec_of(n, l), s);
+    net_featT_kernel<<<n->grid, kNetThreads, 0, s>>>(n->dec, sigma, r, n->skip, z, V);
+    return cudaGetLastError();
+}
+
+// z = M(r) with the tensor-core convolutions (the solvers' preconditioner)
+cudaError_t net_forward_fast(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s)
+{
+    const int V = n->V;
+    net_features_kernel<<<n->grid, kNetThreads, 0, s>>>(r, sigma, n->act, V);
+    net_convs_fast(n, s);
     net_featT_kernel<<<n->grid, kNetThreads, 0, s>>>(n->dec, sigma, r, n->skip, z, V);
     return cudaGetLastError();
 }
@@ -843,7 +1079,7 @@ cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double 
             float* Zj = n->Zs + (size_t)j * V4;
             float* Wj = n->Ws + (size_t)j * V4;
             if (use_net)
-                e = net_forward(n, rin, sigma, Zj, s);
+                e = net_forward_fast(n, rin, sigma, Zj, s);
             else
                 e = cudaMemcpyAsync(Zj, rin, sizeof(float) * V4, cudaMemcpyDeviceToDevice, s);
             if (e == cudaSuccess) e = apply_A(d, Zj, tmp, Wj, YK_FP32, s);
@@ -881,6 +1117,373 @@ cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double 
     res->rr = rr;
     res->rr0 = bb;
     res->converged = rr <= stop2 ? 1 : 0;
+    return e;
+}
+
+}  // namespace yk
+// ---------------------------------------------------------------------------
+// Flexible preconditioned CG with the network or the identity: FP32 vectors,
+// FP64 scalars kept on the device, inside FP64 iterative refinement.  The
+// host reads |r|^2 every kPcgChunk iterations; a chunk of iterations is one
+// captured CUDA graph (launched again for every chunk and every solve while
+// the operator, the field and the network's skip are unchanged).
+//
+// beta is the Polak-Ribiere form, beta = <z', r' - r> / <z, r> =
+// -alpha <z', q> / <z, r> (r' - r = -alpha q): equal to the classical
+// <z', r'> / <z, r> for a fixed symmetric positive definite M, and the form
+// that stays robust when M(r) carries rounding (flexible CG).
+// ---------------------------------------------------------------------------
+namespace yk {
+
+namespace {
+
+constexpr int kPcgChunk = 8;
+// device scalars
+enum { kRZ = 0, kPQ = 1, kRR = 2, kAlpha = 3, kBeta = 4, kZQ = 5 };
+
+// Arrival of a block at the end of a reduction kernel (thread 0 has written
+// the block's partials): true in the block that arrives last, which then sees
+// every block's partials and resets the counter for the next launch.
+__device__ __forceinline__ bool last_arrival(unsigned* counter)
+{
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+        if (last) *counter = 0u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// sum of nb <= 16 * blockDim.x partials (fixed order: the result does not
+// depend on timing; the loads are issued together)
+__device__ __forceinline__ double sum_partials(const double* part, int nb, double* red)
+{
+    double w[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int i = threadIdx.x + j * blockDim.x;
+        w[j] = i < nb ? __ldcg(part + i) : 0.0;
+    }
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v += w[j];
+    return block_sum(v, red);
+}
+
+// Block sums of NV FP32 values: FP32 within a warp (32 terms), FP64 across
+// warps (GB300's FP64 pipe is narrow: per-site FP64 work would bound these
+// kernels); the results are valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum_f(float (&v)[NV], double (&out)[NV], double* red)
+{
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) red[j * 32 + w] = (double)v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        double r = 0.0;
+        if (w == 0) {
+            r = lane < nw ? red[j * 32 + lane] : 0.0;
+            r = warp_sum(r);
+        }
+        out[j] = r;
+    }
+}
+
+// <p, q> (FP32 products of a site, FP64 across sites); the last block sets
+// sc[kPQ] and alpha = <r, z> / <p, q>
+__global__ void __launch_bounds__(kNetThreads) pcg_pq_kernel(const float* __restrict__ p, const float* __restrict__ q,
+                                                             double* __restrict__ part, unsigned* counter,
+                                                             double* __restrict__ sc, int V)
+{
+    __shared__ double red[32];
+    float acc[1] = {0.f};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const float4 pv = reinterpret_cast<const float4*>(p)[n], qv = reinterpret_cast<const float4*>(q)[n];
+        acc[0] += fmaf(pv.x, qv.x, fmaf(pv.y, qv.y, fmaf(pv.z, qv.z, pv.w * qv.w)));
+    }
+    double tot[1];
+    block_sum_f<1>(acc, tot, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
+    if (!last_arrival(counter)) return;
+    const double pq = sum_partials(part, gridDim.x, red);
+    if (threadIdx.x == 0) {
+        sc[kPQ] = pq;
+        sc[kAlpha] = pq != 0.0 ? sc[kRZ] / pq : 0.0;
+    }
+}
+
+// x += alpha p, r -= alpha q; with X != null also the network's features of
+// the new r (X[8][V] = (r, sigma r))
+__global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
+                                                             const float* __restrict__ p, const float* __restrict__ q,
+                                                             const double* __restrict__ sc,
+                                                             const float* __restrict__ sigma, float* __restrict__ X,
+                                                             int V)
+{
+    const float a = (float)sc[kAlpha];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        float4 xv = reinterpret_cast<float4*>(x)[n], rv = reinterpret_cast<float4*>(r)[n];
+        const float4 pv = reinterpret_cast<const float4*>(p)[n], qv = reinterpret_cast<const float4*>(q)[n];
+        xv.x = fmaf(a, pv.x, xv.x);
+        xv.y = fmaf(a, pv.y, xv.y);
+        xv.z = fmaf(a, pv.z, xv.z);
+        xv.w = fmaf(a, pv.w, xv.w);
+        rv.x = fmaf(-a, qv.x, rv.x);
+        rv.y = fmaf(-a, qv.y, rv.y);
+        rv.z = fmaf(-a, qv.z, rv.z);
+        rv.w = fmaf(-a, qv.w, rv.w);
+        reinterpret_cast<float4*>(x)[n] = xv;
+        reinterpret_cast<float4*>(r)[n] = rv;
+        if (X) {
+            const float sg = sigma[n];
+            X[0 * V + n] = rv.x;
+            X[1 * V + n] = rv.y;
+            X[2 * V + n] = rv.z;
+            X[3 * V + n] = rv.w;
+            X[4 * V + n] = sg * rv.x;
+            X[5 * V + n] = sg * rv.y;
+            X[6 * V + n] = sg * rv.z;
+            X[7 * V + n] = sg * rv.w;
+        }
+    }
+}
+
+// z = F^T a + skip r (a != null: the network's last transposed layer) or
+// z = r (a == null), with <r, z>, <r, r> and <z, q> (q may be null; FP32
+// products of a site, FP64 across sites).  The last block sets rz, rr and
+// beta = -alpha <z, q> / <r, z>_old (first: the round's first z, beta = 0).
+__global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const float* __restrict__ a,
+                                                            const float* __restrict__ sigma,
+                                                            const float* __restrict__ r, float skip,
+                                                            float* __restrict__ z, const float* __restrict__ q,
+                                                            double* __restrict__ part, unsigned* counter,
+                                                            double* __restrict__ sc, int first, int V)
+{
+    __shared__ double red[96];
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const float4 rv = reinterpret_cast<const float4*>(r)[n];
+        float4 o = rv;
+        if (a) {
+            const float sg = sigma[n];
+            o.x = fmaf(sg, a[4 * V + n], a[0 * V + n]) + skip * rv.x;
+            o.y = fmaf(sg, a[5 * V + n], a[1 * V + n]) + skip * rv.y;
+            o.z = fmaf(sg, a[6 * V + n], a[2 * V + n]) + skip * rv.z;
+            o.w = fmaf(sg, a[7 * V + n], a[3 * V + n]) + skip * rv.w;
+        }
+        reinterpret_cast<float4*>(z)[n] = o;
+        acc[0] += fmaf(rv.x, o.x, fmaf(rv.y, o.y, fmaf(rv.z, o.z, rv.w * o.w)));
+        acc[1] += fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, rv.w * rv.w)));
+        if (q) {
+            const float4 qv = reinterpret_cast<const float4*>(q)[n];
+            acc[2] += fmaf(o.x, qv.x, fmaf(o.y, qv.y, fmaf(o.z, qv.z, o.w * qv.w)));
+        }
+    }
+    double tot[3];
+    block_sum_f<3>(acc, tot, red);
+    const int nb = gridDim.x;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = tot[0];
+        part[nb + blockIdx.x] = tot[1];
+        part[2 * nb + blockIdx.x] = tot[2];
+    }
+    if (!last_arrival(counter)) return;
+    const double rz = sum_partials(part, nb, red);
+    const double rr = sum_partials(part + nb, nb, red);
+    const double zq = sum_partials(part + 2 * nb, nb, red);
+    if (threadIdx.x == 0) {
+        if (!first) {
+            const double rz_old = sc[kRZ];
+            sc[kZQ] = zq;
+            sc[kBeta] = rz_old != 0.0 ? -sc[kAlpha] * zq / rz_old : 0.0;
+        } else {
+            sc[kBeta] = 0.0;
+        }
+        sc[kRZ] = rz;
+        sc[kRR] = rr;
+    }
+}
+
+// FP32 copy of the field (the preconditioner's features)
+__global__ void f_of_d_kernel(const double* __restrict__ a, float* __restrict__ out, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)a[i];
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kNetThreads) pcg_p_kernel(float* __restrict__ p, const float* __restrict__ z,
+                                                            const double* __restrict__ sc, int V)
+{
+    const float b = (float)sc[kBeta];
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        float4 pv = reinterpret_cast<float4*>(p)[n];
+        const float4 zv = reinterpret_cast<const float4*>(z)[n];
+        pv.x = fmaf(b, pv.x, zv.x);
+        pv.y = fmaf(b, pv.y, zv.y);
+        pv.z = fmaf(b, pv.z, zv.z);
+        pv.w = fmaf(b, pv.w, zv.w);
+        reinterpret_cast<float4*>(p)[n] = pv;
+    }
+}
+
+struct PcgBufs {
+    float *r, *x, *z, *p, *q, *tmp;
+    double* sc;
+};
+
+// z = M r, its partials and the scalars; X: the features (already written
+// by pcg_xr_kernel, or written here on the first round)
+void pcg_precond(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs& b, bool first, cudaStream_t s)
+{
+    const int V = n->V, nb = n->grid;
+    if (use_net) {
+        if (first) net_features_kernel<<<nb, kNetThreads, 0, s>>>(b.r, d.sigma, n->act, V);   // FP64 field
+        net_convs_fast(n, s);
+    }
+    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(use_net ? n->dec : nullptr, n->sig32, b.r, n->skip, b.z,
+                                            first ? nullptr : b.q, n->dpart, n->dcnt + 1, b.sc, first ? 1 : 0, V);
+    pcg_p_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.z, b.sc, V);
+}
+
+// `count` iterations (q = A p, alpha, x and r, z = M r, beta, p)
+cudaError_t pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs& b, int count,
+                           cudaStream_t s)
+{
+    const int V = n->V, nb = n->grid;
+    for (int it = 0; it < count; ++it) {
+        cudaError_t e = apply_A(d, b.p, b.tmp, b.q, YK_FP32, s);
+        if (e != cudaSuccess) return e;
+        pcg_pq_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.q, n->dpart, n->dcnt, b.sc, V);
+        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, b.p, b.q, b.sc, n->sig32, use_net ? n->act : nullptr, V);
+        pcg_precond(n, use_net, d, b, false, s);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// the captured chunk of a learned net (see pcg_solve)
+struct PcgGraph {
+    cudaGraphExec_t exec = nullptr;
+    PcgBufs buf = {};
+    const double* dpart = nullptr;
+    bool use_net = false;
+    const double* sigma = nullptr;
+    double m0 = 0, g = 0, r = 0;
+    float skip = 0;
+};
+
+void pcg_graph_destroy(PcgGraph* g)
+{
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    delete g;
+}
+
+cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                      const double* b, double* x, double tol, int tol_mode, int max_iter, double inner_tol,
+                      cudaStream_t s, FgcrResult* res)
+{
+    const int V4 = 4 * n->V;
+    const DiracArgs d = {sigma, n->Nt, n->Nx, m0, g, r};
+    cudaError_t e = ensure_scratch(n, 2);   // Zs, Ws: two 4V float vectors each
+    if (e == cudaSuccess) e = ensure_parts(n, 4);
+    if (e != cudaSuccess) return e;
+    if (!n->dsc) {
+        e = cudaMalloc(&n->dsc, sizeof(double) * 8);
+        if (e != cudaSuccess) return e;
+    }
+    double* Ax = n->d1;
+    double* r64 = n->d2;
+    const PcgBufs B = {n->f0, n->f1, n->f2, n->Zs, n->Ws, n->f3, n->dsc};
+    f_of_d_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->sig32, n->V);
+    const int nb = n->grid;
+    // the chunk graph, captured again when the operator or the network changed
+    PcgGraph*& G = n->pcg;
+    if (G && (G->use_net != use_net || G->sigma != sigma || G->m0 != m0 || G->g != g || G->r != r ||
+              G->skip != n->skip || G->dpart != n->dpart || std::memcmp(&G->buf, &B, sizeof(B)) != 0)) {
+        pcg_graph_destroy(G);
+        G = nullptr;
+    }
+    if (!G && !n->pcg_no_graph) {
+        G = new PcgGraph();
+        G->buf = B;
+        G->dpart = n->dpart;
+        G->use_net = use_net;
+        G->sigma = sigma;
+        G->m0 = m0;
+        G->g = g;
+        G->r = r;
+        G->skip = n->skip;
+        cudaGraph_t graph = nullptr;
+        bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            const cudaError_t ce = pcg_iterations(n, use_net, d, B, kPcgChunk, s);
+            ok = cudaStreamEndCapture(s, &graph) == cudaSuccess && ce == cudaSuccess && graph;
+        }
+        if (ok) ok = cudaGraphInstantiate(&G->exec, graph, 0) == cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+        if (!ok) {   // e.g. the legacy stream, which cannot be captured: run uncaptured
+            cudaGetLastError();
+            pcg_graph_destroy(G);
+            G = nullptr;
+            n->pcg_no_graph = true;
+        }
+    }
+    e = cudaMemsetAsync(x, 0, sizeof(double) * V4, s);
+    double bb = 0.0;
+    if (e == cudaSuccess) e = dot_d(n, b, b, s, &bb);
+    if (e != cudaSuccess) return e;
+    const double stop2 = tol_mode == YK_TOL_REL ? tol * tol * bb : tol * tol;
+    double rr64 = bb;
+    int iters = 0, outer = 0;
+    e = cudaMemcpyAsync(r64, b, sizeof(double) * V4, cudaMemcpyDeviceToDevice, s);
+    while (e == cudaSuccess && rr64 > stop2 && iters < max_iter) {
+        ++outer;
+        dvec_to_f_kernel<<<nb, kNetThreads, 0, s>>>(r64, B.r, V4);
+        e = cudaMemsetAsync(B.x, 0, sizeof(float) * V4, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.p, 0, sizeof(float) * V4, s);
+        if (e != cudaSuccess) break;
+        pcg_precond(n, use_net, d, B, true, s);   // z = M r, p = z
+        double h[8];
+        e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        const double rr0 = h[kRR];
+        double rrc = rr0;
+        while (e == cudaSuccess && iters < max_iter && rrc > inner_tol * inner_tol * rr0) {
+            const int cnt = std::min(kPcgChunk, max_iter - iters);
+            if (G && cnt == kPcgChunk) e = cudaGraphLaunch(G->exec, s);
+            else e = pcg_iterations(n, use_net, d, B, cnt, s);
+            iters += cnt;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            rrc = h[kRR];
+            if (!(rrc == rrc)) break;   // NaN: the FP64 check below decides
+        }
+        if (e != cudaSuccess) break;
+        dvec_add_f_kernel<<<nb, kNetThreads, 0, s>>>(x, B.x, V4);
+        e = apply_A(d, x, n->d0, Ax, YK_FP64, s);
+        if (e == cudaSuccess) dvec_residual_kernel<<<nb, kNetThreads, 0, s>>>(b, Ax, r64, B.r, V4);
+        if (e == cudaSuccess) e = dot_d(n, r64, r64, s, &rr64);
+        if (!(rr64 == rr64)) break;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    res->iterations = iters;
+    res->outer = outer;
+    res->rr = rr64;
+    res->rr0 = bb;
+    res->converged = rr64 <= stop2 ? 1 : 0;
     return e;
 }
 
