@@ -216,7 +216,7 @@ int yk_net_size(yk_ctx* ctx, int chain);
 int yk_net_weights(yk_ctx* ctx, int chain, float* host, int set);
 /* z = M(r) for device r, z (4V floats each, site-major), sigma the chain's field. */
 int yk_net_apply(yk_ctx* ctx, int chain, const float* r, float* z);
-/* As yk_net_apply, through the TF32 tensor-core convolutions (FP32
+/* As yk_net_apply, through the BF16 tensor-core convolutions (FP32
  * accumulation) that yk_fgcr_solve, yk_pcg_solve and
  * yk_langevin_step_learned apply. */
 int yk_net_apply_tc(yk_ctx* ctx, int chain, const float* r, float* z);

@@ -4,8 +4,8 @@ solve (GPU).
 
 Tolerances: the oracle's gradients against central finite differences 1e-6
 relative; the FP32 network against the FP64 oracle 2e-6 (forward) and 2e-5
-(weight gradients) relative to the largest entry, its TF32 tensor-core form
-(the one the solvers apply) 5e-3; every solve to the FP64 relative residual
+(weight gradients) relative to the largest entry, its BF16 tensor-core form
+(the one the solvers apply) 2e-2; every solve to the FP64 relative residual
 1e-10.
 """
 import numpy as np
@@ -90,10 +90,11 @@ def test_network_forward_and_gradient_match_oracle(ylib, cuda):
         ctx.net_apply(rd, zd)
         want = N.apply_M(W32, r.T.astype(np.float64), sig, Nt, Nx, np.float32(0.05))[0]
         assert np.abs(zd.cpu().numpy().T - want).max() < 2e-6 * np.abs(want).max()
-        # the solvers' form: TF32 tensor-core convolutions (11-bit significands)
+        # the solvers' form: BF16 activations (8-bit significands) through
+        # tensor-core convolutions with FP32 accumulation
         ctx.net_apply(rd, zd, tensor_cores=True)
         err = np.abs(zd.cpu().numpy().T - want).max() / np.abs(want).max()
-        assert err < 5e-3, err
+        assert err < 2e-2, err
         g, loss = ctx.net_grad(rd, ed)
         lo, go = N.energy_loss_and_grad(W32, r.T.astype(np.float64), e.T.astype(np.float64), sig, Nt, Nx,
                                         _action(0.1), np.float32(0.05))

@@ -89,7 +89,7 @@ int net_size(const LearnedNet* n);
 void net_set_skip(LearnedNet* n, float skip);   // M(r) = skip r + N(r)
 cudaError_t net_weights(LearnedNet* n, float* host, bool set);
 cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);
-// the same with TF32 tensor-core convolutions (the form the solvers apply)
+// the same with BF16 activations and tensor-core convolutions (the form the solvers apply)
 cudaError_t net_forward_fast(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);
 cudaError_t net_zero_grad(LearnedNet* n, cudaStream_t s);
 // loss of a pair: (M r - e)^T A (M r - e); accumulates its weight gradient

@@ -23,6 +23,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "yk_common.cuh"
 #include "yk_kernels.h"
 
@@ -323,36 +325,25 @@ __global__ void dvec_add_f_kernel(double* __restrict__ x, const float* __restric
 
 // ---- tensor-core convolutions of the solvers' preconditioner ----
 //
-// One 3x3 tap of an 8 -> 8 layer is a [16 sites x 8 in] x [8 in x 8 out]
-// product, exactly one mma.sync m16n8k8 with TF32 inputs and FP32
-// accumulation; a layer is 9 of them per 16 sites.  A warp takes 16
-// consecutive sites; lane (g = lane / 4, c = lane % 4) gathers channels c and
-// c + 4 of the tap's neighbours of sites g and g + 8 (the A fragment) and holds
-// the weights W[k][c][g], W[k][c + 4][g] of every tap (the B fragments) in
-// registers.  The 4-channel layers (the last of N, the first of N^T) pad
-// the product with zero weights.  TF32 keeps 10 mantissa bits: M(r) is then a
-// slightly perturbed operator, which the flexible CG's Polak-Ribiere beta
-// absorbs.  Training and yk_net_apply use the exact FP32 kernels above.
+// The solvers apply M through BF16 activations, site-major: the 8 channels
+// of a site are 16 bytes (uint4).  Two 3x3 taps of an 8 -> 8 layer are one
+// [16 sites x 16] x [16 x 8 out] product, one mma.sync m16n8k16 with BF16
+// inputs and FP32 accumulation (K = tap A's 8 channels, then tap B's), so a
+// layer is 5 of them per 16 sites (the fifth pairs tap 8 with zeros).  A
+// block stages its R x W tile with a one-site halo in shared memory by 16-byte
+// asynchronous copies; lane (g = lane / 4, c = lane % 4) then gathers the
+// 32-bit word c (channels 2c, 2c + 1) of the tap neighbours of sites g and
+// g + 8 (the A fragment: 8 sites x 4 words = 32 distinct banks) and holds the
+// weights as B fragments in registers.  The 4-channel activations (the output
+// of N, the input of N^T) keep 8 channels, 4 of them zero.  BF16 keeps 8
+// mantissa bits: M(r) is then a slightly perturbed operator, which the
+// flexible CG's Polak-Ribiere beta absorbs.  Training and yk_net_apply use the
+// exact FP32 kernels above.
 
-// staged rows a warp loads in the tensor-core convolutions: 8 channels x
-// (R + 2) rows over 8 warps, R <= 8
-constexpr int kStageRows = 10;
 constexpr int kTcMaxR = 8, kTcMaxW = 64;
-// the staged tile s[c][row][col]: staged column j (j = 0: the left halo) at
-// col j + 3, so the interior starts on a 16-byte boundary; row stride kTcSW,
-// channel stride kTcCS = 8 (mod 32) words
-constexpr int kTcSW = kTcMaxW + 8;
-constexpr int kTcCS = ((kTcMaxR + 2) * kTcSW + 23) / 32 * 32 + 8;
-static_assert(kTcCS % 32 == 8 && kTcCS % 4 == 0 && kTcCS >= (kTcMaxR + 2) * kTcSW, "tile channel stride");
-static_assert(kTcSW % 4 == 0 && kTcSW >= kTcMaxW + 5, "tile row stride");
+constexpr int kTcSW = kTcMaxW + 2;   // staged sites per tile row
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-
-__device__ __forceinline__ void cp_async16(float* dst, const float* src)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
 {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
                  "l"(src)
@@ -361,142 +352,158 @@ __device__ __forceinline__ void cp_async16(float* dst, const float* src)
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-__device__ __forceinline__ uint32_t to_tf32(float v)
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
 {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
-    return r;
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+__device__ __forceinline__ float2 unpack_bf2(uint32_t w)
+{
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
 {
     asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
         "{%0,%1,%2,%3};"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// TRANS = false: Y[COUT][V] = conv(X[8][V]) (the layer of N);
-// TRANS = true: Y[8][V] = conv^T(X[COUT][V]) (its transpose in N^T: the
-// opposite tap, the same sign, W[k] transposed).
-// One block per tile of R x W sites: the tile's input with a one-site halo
-// ((R + 2) x (W + 2) sites, the antiperiodic sign applied to wrapped time
-// rows) is staged in shared memory with coalesced loads, and the A fragments
-// are gathered from there: s[c][row][col], channel stride CS = 8 (mod 32)
-// words, so the 8 sites x 4 channels of a gather fall in 32 distinct banks.
+// FP32 copy of the field (the preconditioner's features)
+__global__ void f_of_d_kernel(const double* __restrict__ a, float* __restrict__ out, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)a[i];
+}
+
+// the 8 BF16 channels (r, sigma r) of a site
+__device__ __forceinline__ uint4 features_bf(float4 v, float sg)
+{
+    return make_uint4(pack_bf2(v.x, v.y), pack_bf2(v.z, v.w), pack_bf2(sg * v.x, sg * v.y), pack_bf2(sg * v.z, sg * v.w));
+}
+
+// X = F r (BF16, site-major)
+__global__ void __launch_bounds__(kNetThreads) net_feat_bf_kernel(const float* __restrict__ r,
+                                                                  const float* __restrict__ sigma,
+                                                                  uint4* __restrict__ X, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x)
+        X[n] = features_bf(reinterpret_cast<const float4*>(r)[n], sigma[n]);
+}
+
+// F^T a + skip r for the BF16 site-major a
+__device__ __forceinline__ float4 featT_bf(uint4 a, float sg, float4 rv, float skip)
+{
+    const float2 a01 = unpack_bf2(a.x), a23 = unpack_bf2(a.y), a45 = unpack_bf2(a.z), a67 = unpack_bf2(a.w);
+    return make_float4(fmaf(sg, a45.x, a01.x) + skip * rv.x, fmaf(sg, a45.y, a01.y) + skip * rv.y,
+                       fmaf(sg, a67.x, a23.x) + skip * rv.z, fmaf(sg, a67.y, a23.y) + skip * rv.w);
+}
+
+__global__ void __launch_bounds__(kNetThreads) net_featT_bf_kernel(const uint4* __restrict__ a,
+                                                                   const float* __restrict__ sigma,
+                                                                   const float* __restrict__ r, float skip,
+                                                                   float* __restrict__ z, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x)
+        reinterpret_cast<float4*>(z)[n] = featT_bf(a[n], sigma[n], reinterpret_cast<const float4*>(r)[n], skip);
+}
+
+// TRANS = false: Y = conv(X) (a layer of N, 8 -> COUT channels);
+// TRANS = true: Y = conv^T(X) (its transpose in N^T, COUT -> 8: the opposite
+// tap, the same sign, W[k] transposed).  X, Y: BF16 site-major, 8 channels.
 template <int COUT, bool TRANS>
-__global__ void __launch_bounds__(kNetThreads) net_conv_tc_kernel(const float* __restrict__ X, float* __restrict__ Y,
+__global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* __restrict__ X, uint4* __restrict__ Y,
                                                                   const float* __restrict__ Wl, int Nt, int Nx,
                                                                   int R, int W)
 {
-    constexpr int CIN = TRANS ? COUT : kNetC;    // channels gathered
-    constexpr int CO = TRANS ? kNetC : COUT;     // channels written
-    extern __shared__ float sm[];
+    __shared__ __align__(16) uint4 sm[(kTcMaxR + 2) * kTcSW];
+    constexpr int SW = kTcSW;
     const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
-    const int V = Nt * Nx;
     const int tiles_x = (Nx + W - 1) / W;
     const int t0 = (blockIdx.x / tiles_x) * R, x0 = (blockIdx.x % tiles_x) * W;
     const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
-    constexpr int SW = kTcSW, CS = kTcCS;
-    // stage the tile and its halo with asynchronous copies: warp w takes the
-    // staged rows w, w + 8, ... (channel-major); 16-byte copies of the
-    // interior when rows are 16-byte aligned, else 4-byte copies
-    {
-        const int warp = threadIdx.x >> 5, nrow = CIN * (Rt + 2);
-        const bool vec = (Nx & 3) == 0 && (Wt & 3) == 0;
-        for (int row = warp; row < nrow; row += kNetThreads / 32) {
-            const int ch = row / (Rt + 2), lr = row - ch * (Rt + 2);
-            int t = t0 - 1 + lr;
-            if (t < 0) t += Nt;
-            else if (t >= Nt) t -= Nt;
-            const float* src = X + (size_t)ch * V + (size_t)t * Nx;
-            float* dst = sm + ch * CS + lr * SW + 3;   // staged column 0
-            if (vec) {
-                if (lane < (Wt >> 2)) cp_async16(dst + 1 + 4 * lane, src + x0 + 4 * lane);
-                else if (lane == 30) cp_async4(dst, src + (x0 == 0 ? Nx - 1 : x0 - 1));
-                else if (lane == 31) cp_async4(dst + Wt + 1, src + (x0 + Wt == Nx ? 0 : x0 + Wt));
-            } else {
-                for (int lc = lane; lc < Wt + 2; lc += 32) {
-                    int x = x0 - 1 + lc;
-                    if (x < 0) x += Nx;
-                    else if (x >= Nx) x -= Nx;
-                    cp_async4(dst + lc, src + x);
-                }
-            }
-        }
-        cp_async_wait_all();
-        __syncthreads();
-        // the antiperiodic sign of halo rows that wrapped in time
-        const bool top = t0 == 0, bottom = t0 + Rt == Nt;
-        if (top || bottom) {
-            for (int idx = threadIdx.x; idx < CIN * 2 * (Wt + 2); idx += blockDim.x) {
-                const int ch = idx / (2 * (Wt + 2)), rem = idx - ch * 2 * (Wt + 2);
-                const int which = rem / (Wt + 2), lc = rem - which * (Wt + 2);
-                if (which == 0 ? top : bottom) {
-                    float* q = sm + ch * CS + (which == 0 ? 0 : Rt + 1) * SW + 3 + lc;
-                    *q = -*q;
-                }
-            }
+    // stage the tile and its halo: warp w takes the staged rows w, w + 8
+    for (int lr = threadIdx.x >> 5; lr < Rt + 2; lr += kNetThreads / 32) {
+        int t = t0 - 1 + lr;
+        if (t < 0) t += Nt;
+        else if (t >= Nt) t -= Nt;
+        const uint4* src = X + (size_t)t * Nx;
+        for (int lc = lane; lc < Wt + 2; lc += 32) {
+            int x = x0 - 1 + lc;
+            if (x < 0) x += Nx;
+            else if (x >= Nx) x -= Nx;
+            cp_async16(&sm[lr * SW + lc], src + x);
         }
     }
-    // B fragments: B[kk][j] for the K index kk = c, c + 4 and output j = g
-    uint32_t b0[9], b1[9];
+    // B fragments of the tap pairs (2p, 2p + 1): K = the pair's 16 inputs, N = 8 outputs
+    uint32_t b0[5], b1[5];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        float w0 = 0.f, w1 = 0.f;
-        if (!TRANS) {   // B[i][o] = W[k][i][o]
-            if (g < COUT) {
-                w0 = Wl[(k * kNetC + c) * COUT + g];
-                w1 = Wl[(k * kNetC + c + 4) * COUT + g];
+    for (int p = 0; p < 5; ++p) {
+        float w[4] = {0.f, 0.f, 0.f, 0.f};   // B[2c][g], B[2c + 1][g], B[2c + 8][g], B[2c + 9][g]
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * p + h;
+            if (k > 8) continue;
+            if (!TRANS) {   // B[i][o] = W[k][i][o]
+                if (g < COUT) {
+                    w[2 * h] = Wl[(k * kNetC + 2 * c) * COUT + g];
+                    w[2 * h + 1] = Wl[(k * kNetC + 2 * c + 1) * COUT + g];
+                }
+            } else {        // B[o][i] = W[k][i][o]
+                if (2 * c + 1 < COUT) {
+                    w[2 * h] = Wl[(k * kNetC + g) * COUT + 2 * c];
+                    w[2 * h + 1] = Wl[(k * kNetC + g) * COUT + 2 * c + 1];
+                }
             }
-        } else {        // B[o][i] = W[k][i][o]
-            if (c < COUT) w0 = Wl[(k * kNetC + g) * COUT + c];
-            if (c + 4 < COUT) w1 = Wl[(k * kNetC + g) * COUT + c + 4];
         }
-        b0[k] = to_tf32(w0);
-        b1[k] = to_tf32(w1);
+        b0[p] = pack_bf2(w[0], w[1]);
+        b1[p] = pack_bf2(w[2], w[3]);
     }
+    cp_async_wait_all();
     __syncthreads();
+    // the antiperiodic sign of halo rows that wrapped in time (BF16 sign bits)
+    const bool top = t0 == 0, bottom = t0 + Rt == Nt;
+    if (top || bottom) {
+        uint32_t* w32 = reinterpret_cast<uint32_t*>(sm);
+        for (int idx = threadIdx.x; idx < 2 * (Wt + 2) * 4; idx += blockDim.x) {
+            const int which = idx / ((Wt + 2) * 4), rem = idx - which * (Wt + 2) * 4;
+            if (which == 0 ? top : bottom) w32[((which == 0 ? 0 : Rt + 1) * SW) * 4 + rem] ^= 0x80008000u;
+        }
+        __syncthreads();
+    }
+    const uint32_t* smw = reinterpret_cast<const uint32_t*>(sm);
+    uint32_t* Yw = reinterpret_cast<uint32_t*>(Y);
     const int S = Rt * Wt;
     for (int base = (threadIdx.x >> 5) * 16; base < S; base += (blockDim.x >> 5) * 16) {
         const int i0 = base + g, i1 = base + g + 8;
         const bool in0 = i0 < S, in1 = i1 < S;
         const int r0 = in0 ? i0 / Wt : 0, c0 = in0 ? i0 - r0 * Wt : 0;
         const int r1 = in1 ? i1 / Wt : 0, c1 = in1 ? i1 - r1 * Wt : 0;
-        // the sites' centres in the staged tile, channels c and c + 4
-        const float* p0 = sm + c * CS + (r0 + 1) * SW + c0 + 4;
-        const float* p1 = sm + c * CS + (r1 + 1) * SW + c1 + 4;
+        // word c of the sites' centres in the staged tile
+        const uint32_t* q0 = smw + ((r0 + 1) * SW + c0 + 1) * 4 + c;
+        const uint32_t* q1 = smw + ((r1 + 1) * SW + c1 + 1) * 4 + c;
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const int kt = TRANS ? 8 - k : k;
-            const int off = (kt / 3 - 1) * SW + (kt % 3 - 1);
-            // FP32 bits as TF32 operands (the low mantissa bits are ignored:
-            // rounding toward zero)
+        for (int p = 0; p < 5; ++p) {
+            const int kA = TRANS ? 8 - 2 * p : 2 * p;   // gathered taps
+            const int kB = TRANS ? 7 - 2 * p : 2 * p + 1;
+            const int offA = ((kA / 3 - 1) * SW + (kA % 3 - 1)) * 4;
+            const int offB = ((kB / 3 - 1) * SW + (kB % 3 - 1)) * 4;
             uint32_t a[4];
-            a[0] = c < CIN ? __float_as_uint(p0[off]) : 0u;
-            a[1] = c < CIN ? __float_as_uint(p1[off]) : 0u;
-            a[2] = c + 4 < CIN ? __float_as_uint(p0[4 * CS + off]) : 0u;
-            a[3] = c + 4 < CIN ? __float_as_uint(p1[4 * CS + off]) : 0u;
-            mma_tf32(acc, a, b0[k], b1[k]);
+            a[0] = q0[offA];
+            a[1] = q1[offA];
+            a[2] = p < 4 ? q0[offB] : 0u;
+            a[3] = p < 4 ? q1[offB] : 0u;
+            mma_bf16(acc, a, b0[p], b1[p]);
         }
         // D fragment: rows g, g + 8 (sites), columns 2c, 2c + 1 (output channels)
         const int n0 = (t0 + r0) * Nx + x0 + c0, n1 = (t0 + r1) * Nx + x0 + c1;
-        const int o0 = 2 * c, o1 = 2 * c + 1;
-        if (o0 < CO) {
-            if (in0) Y[o0 * V + n0] = acc[0];
-            if (in1) Y[o0 * V + n1] = acc[2];
-        }
-        if (o1 < CO) {
-            if (in0) Y[o1 * V + n0] = acc[1];
-            if (in1) Y[o1 * V + n1] = acc[3];
-        }
+        if (in0) Yw[(size_t)n0 * 4 + c] = pack_bf2(acc[0], acc[1]);
+        if (in1) Yw[(size_t)n1 * 4 + c] = pack_bf2(acc[2], acc[3]);
     }
 }
-
-// shared memory of a tile (CIN = 8)
-inline size_t conv_tc_smem(int, int) { return sizeof(float) * kNetC * kTcCS; }
 
 }  // namespace
 
@@ -511,6 +518,7 @@ struct LearnedNet {
     int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
     unsigned* dcnt = nullptr;         // arrival counters of the preconditioned CG's reductions
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
+    uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
     std::vector<int> woff;            // each layer's first weight
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     float* act = nullptr;             // layers x [8][V]: the input of each layer of N
@@ -619,6 +627,8 @@ void net_destroy(LearnedNet* n)
     if (n->hpart) cudaFreeHost(n->hpart);
     pcg_graph_destroy(n->pcg);
     if (n->dcnt) cudaFree(n->dcnt);
+    for (uint4* h : n->h16)
+        if (h) cudaFree(h);
     delete n;
 }
 
@@ -662,6 +672,8 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e == cudaSuccess) e = alloc_d(&n->dpart, n->grid);
     if (e == cudaSuccess) e = cudaMalloc(&n->dcnt, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = alloc_f(&n->sig32, V);
+    if (e == cudaSuccess) e = cudaMalloc(&n->h16[0], sizeof(uint4) * V);
+    if (e == cudaSuccess) e = cudaMalloc(&n->h16[1], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMemset(n->dcnt, 0, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * n->grid);
     if (e == cudaSuccess) n->hpart_cap = (size_t)n->grid;
@@ -724,30 +736,28 @@ void conv_wgrad(LearnedNet* n, int l, const float* X, const float* Y, cudaStream
 float* act_of(LearnedNet* n, int l) { return n->act + (size_t)l * kNetC * n->V; }
 float* dec_of(LearnedNet* n, int l) { return n->dec + (size_t)l * kNetC * n->V; }
 
-// N then N^T on the features in act[0], leaving F^T's input in dec[0]
-// (tensor-core convolutions, one block per tile)
-void net_convs_fast(LearnedNet* n, cudaStream_t s)
+// N then N^T on the BF16 features in h16[0] (tensor-core convolutions,
+// one block per tile); returns the buffer that holds F^T's input
+uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
 {
     const int L = n->layers, Nt = n->Nt, Nx = n->Nx, R = n->tc_R, W = n->tc_W;
     const int grid = ((Nt + R - 1) / R) * ((Nx + W - 1) / W);
-    const size_t sm = conv_tc_smem(R, W);
-    for (int l = 0; l < L; ++l) {
-        float* out = l < L - 1 ? act_of(n, l + 1) : dec_of(n, L);
+    int cur = 0;
+    for (int l = 0; l < L; ++l, cur ^= 1) {
         const float* w = n->w + n->woff[l];
         if (cout_of(n, l) == kNetOut)
-            net_conv_tc_kernel<kNetOut, false><<<grid, kNetThreads, sm, s>>>(act_of(n, l), out, w, Nt, Nx, R, W);
+            net_conv_bf_kernel<kNetOut, false><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
         else
-            net_conv_tc_kernel<kNetC, false><<<grid, kNetThreads, sm, s>>>(act_of(n, l), out, w, Nt, Nx, R, W);
+            net_conv_bf_kernel<kNetC, false><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
     }
-    for (int l = L - 1; l >= 0; --l) {
+    for (int l = L - 1; l >= 0; --l, cur ^= 1) {
         const float* w = n->w + n->woff[l];
         if (cout_of(n, l) == kNetOut)
-            net_conv_tc_kernel<kNetOut, true><<<grid, kNetThreads, sm, s>>>(dec_of(n, l + 1), dec_of(n, l), w, Nt, Nx,
-                                                                             R, W);
+            net_conv_bf_kernel<kNetOut, true><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
         else
-            net_conv_tc_kernel<kNetC, true><<<grid, kNetThreads, sm, s>>>(dec_of(n, l + 1), dec_of(n, l), w, Nt, Nx,
-                                                                           R, W);
+            net_conv_bf_kernel<kNetC, true><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
     }
+    return n->h16[cur];
 }
 
 }  // namespace
@@ -768,9 +778,10 @@ cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, floa
 cudaError_t net_forward_fast(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s)
 {
     const int V = n->V;
-    net_features_kernel<<<n->grid, kNetThreads, 0, s>>>(r, sigma, n->act, V);
-    net_convs_fast(n, s);
-    net_featT_kernel<<<n->grid, kNetThreads, 0, s>>>(n->dec, sigma, r, n->skip, z, V);
+    f_of_d_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->sig32, V);
+    net_feat_bf_kernel<<<n->grid, kNetThreads, 0, s>>>(r, n->sig32, n->h16[0], V);
+    const uint4* a = net_convs_fast(n, s);
+    net_featT_bf_kernel<<<n->grid, kNetThreads, 0, s>>>(a, n->sig32, r, n->skip, z, V);
     return cudaGetLastError();
 }
 
@@ -1223,12 +1234,12 @@ __global__ void __launch_bounds__(kNetThreads) pcg_pq_kernel(const float* __rest
     }
 }
 
-// x += alpha p, r -= alpha q; with X != null also the network's features of
-// the new r (X[8][V] = (r, sigma r))
+// x += alpha p, r -= alpha q; with X != null also the network's BF16
+// features (r, sigma r) of the new r
 __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
                                                              const float* __restrict__ p, const float* __restrict__ q,
                                                              const double* __restrict__ sc,
-                                                             const float* __restrict__ sigma, float* __restrict__ X,
+                                                             const float* __restrict__ sigma, uint4* __restrict__ X,
                                                              int V)
 {
     const float a = (float)sc[kAlpha];
@@ -1245,17 +1256,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
         rv.w = fmaf(-a, qv.w, rv.w);
         reinterpret_cast<float4*>(x)[n] = xv;
         reinterpret_cast<float4*>(r)[n] = rv;
-        if (X) {
-            const float sg = sigma[n];
-            X[0 * V + n] = rv.x;
-            X[1 * V + n] = rv.y;
-            X[2 * V + n] = rv.z;
-            X[3 * V + n] = rv.w;
-            X[4 * V + n] = sg * rv.x;
-            X[5 * V + n] = sg * rv.y;
-            X[6 * V + n] = sg * rv.z;
-            X[7 * V + n] = sg * rv.w;
-        }
+        if (X) X[n] = features_bf(rv, sigma[n]);
     }
 }
 
@@ -1263,7 +1264,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
 // z = r (a == null), with <r, z>, <r, r> and <z, q> (q may be null; FP32
 // products of a site, FP64 across sites).  The last block sets rz, rr and
 // beta = -alpha <z, q> / <r, z>_old (first: the round's first z, beta = 0).
-__global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const float* __restrict__ a,
+__global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restrict__ a,
                                                             const float* __restrict__ sigma,
                                                             const float* __restrict__ r, float skip,
                                                             float* __restrict__ z, const float* __restrict__ q,
@@ -1274,14 +1275,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const float* __restr
     float acc[3] = {0.f, 0.f, 0.f};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         const float4 rv = reinterpret_cast<const float4*>(r)[n];
-        float4 o = rv;
-        if (a) {
-            const float sg = sigma[n];
-            o.x = fmaf(sg, a[4 * V + n], a[0 * V + n]) + skip * rv.x;
-            o.y = fmaf(sg, a[5 * V + n], a[1 * V + n]) + skip * rv.y;
-            o.z = fmaf(sg, a[6 * V + n], a[2 * V + n]) + skip * rv.z;
-            o.w = fmaf(sg, a[7 * V + n], a[3 * V + n]) + skip * rv.w;
-        }
+        const float4 o = a ? featT_bf(a[n], sigma[n], rv, skip) : rv;
         reinterpret_cast<float4*>(z)[n] = o;
         acc[0] += fmaf(rv.x, o.x, fmaf(rv.y, o.y, fmaf(rv.z, o.z, rv.w * o.w)));
         acc[1] += fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, rv.w * rv.w)));
@@ -1315,12 +1309,6 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const float* __restr
     }
 }
 
-// FP32 copy of the field (the preconditioner's features)
-__global__ void f_of_d_kernel(const double* __restrict__ a, float* __restrict__ out, int n)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = (float)a[i];
-}
-
 // p = z + beta p
 __global__ void __launch_bounds__(kNetThreads) pcg_p_kernel(float* __restrict__ p, const float* __restrict__ z,
                                                             const double* __restrict__ sc, int V)
@@ -1347,11 +1335,12 @@ struct PcgBufs {
 void pcg_precond(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs& b, bool first, cudaStream_t s)
 {
     const int V = n->V, nb = n->grid;
+    const uint4* a = nullptr;
     if (use_net) {
-        if (first) net_features_kernel<<<nb, kNetThreads, 0, s>>>(b.r, d.sigma, n->act, V);   // FP64 field
-        net_convs_fast(n, s);
+        if (first) net_feat_bf_kernel<<<nb, kNetThreads, 0, s>>>(b.r, n->sig32, n->h16[0], V);
+        a = net_convs_fast(n, s);
     }
-    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(use_net ? n->dec : nullptr, n->sig32, b.r, n->skip, b.z,
+    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(a, n->sig32, b.r, n->skip, b.z,
                                             first ? nullptr : b.q, n->dpart, n->dcnt + 1, b.sc, first ? 1 : 0, V);
     pcg_p_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.z, b.sc, V);
 }
@@ -1365,7 +1354,7 @@ cudaError_t pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, cons
         cudaError_t e = apply_A(d, b.p, b.tmp, b.q, YK_FP32, s);
         if (e != cudaSuccess) return e;
         pcg_pq_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.q, n->dpart, n->dcnt, b.sc, V);
-        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, b.p, b.q, b.sc, n->sig32, use_net ? n->act : nullptr, V);
+        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, b.p, b.q, b.sc, n->sig32, use_net ? n->h16[0] : nullptr, V);
         pcg_precond(n, use_net, d, b, false, s);
     }
     return cudaGetLastError();
