@@ -254,6 +254,9 @@ def run_ours(args, ws, rank, local):
         extras["dirac_hbm"] = dirac_hbm(yk, torch, stream)
         # the batching configuration (many chains of uneven sizes in one graph)
         extras["batching"] = batched(yk, torch, stream)
+        # the learned-preconditioner configuration (512^2 near the chiral regime)
+        if not args.no_learned:
+            extras["learned"] = learned(yk, torch, stream)
         extras["gpu_launches"] = int(round(launches_per_step * args.steps))
 
     ctx.close()
@@ -306,6 +309,77 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
             "value": round(steps * n_chains / sec, 2), "unit": "chain-steps/s",
             "site_steps_per_s": round(steps * sites / sec, 1), "steps": steps,
             "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
+
+
+def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_counts=(4, 2)):
+    """The learned-preconditioner configuration: a 512^2 lattice near the
+    chiral regime (m0 = 0.02, g = 0.5, m^2 = -0.5, lambda = 1), one RHS, every
+    solve to FP64 rel-res 1e-10.  From one burnt-in field, the same `steps`
+    Langevin steps by (a) the plain FP64 CG step graph, (b) the mixed CG step
+    graph and (c) yk_langevin_step_learned: flexible preconditioned CG with the
+    trained network (8 hidden channels; 4 layers as specified, and 2), trained
+    on the GPU on (residual, error) pairs from the chain's own CG at that
+    field.  Wall clock around all the steps of an arm (the learned step is
+    host-driven), no L2 flush (the working set, ~40 MB, lives in L2 in every
+    arm)."""
+    def params(prec):
+        return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=m0,
+                                 wilson_param=1.0, cut_fraction=CUT, Nt=L, Nx=L, fixed_dt=0.01, precision=prec,
+                                 cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=50000, reliable_every=50,
+                                 reliable_delta=0.001, n_rhs=1, seed=1234, init=yk.YK_INIT_PHILOX)
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    out = {"config": f"{L}x{L}, m0 {m0}, g 0.5, m2 -0.5, lambda 1, 1 RHS, rel-res 1e-10 (FP64 true residual), "
+                     f"{steps} steps from a field burnt in for {burn_in} mixed steps", "steps": steps}
+    ctx = yk.Context(params(yk.YK_MIXED))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.step(burn_in)
+    phi0, step0 = ctx.get_field(), ctx.get_step()
+    arms = {}
+    for name, prec in (("plain_fp64", yk.YK_FP64), ("mixed_cg", yk.YK_MIXED)):
+        c = yk.Context(params(prec))
+        c.set_stream(stream.cuda_stream)
+        c.set_field(phi0)
+        c.set_step(step0)
+        c.step(1)   # capture the step graph
+        c.set_field(phi0)
+        c.set_step(step0)
+        before = c.observables().cg_iterations_total
+        sec, _ = wall(lambda: c.step(steps))
+        o = c.observables()
+        arms[name] = {"value": round(steps / sec, 2), "unit": "steps/s",
+                      "cg_iterations_per_step": round((o.cg_iterations_total - before) / steps, 1),
+                      "status": int(o.status)}
+        c.close()
+    for nl in layer_counts:
+        ctx.set_field(phi0)
+        ctx.set_step(step0)
+        ctx.net_setup(nl, 7)
+        st = ctx.net_train(n_sources=4, n_levels=5, base_iter=4, steps=400, batch=4, lr=2e-3, seed=3)
+        ctx.set_field(phi0)
+        ctx.set_step(step0)
+        ctx.step_learned(1)   # capture the solver's chunk graph
+        ctx.set_field(phi0)
+        ctx.set_step(step0)
+        sec, s = wall(lambda: ctx.step_learned(steps))
+        arms[f"learned_{nl}layers"] = {
+            "value": round(steps / sec, 2), "unit": "steps/s",
+            "solver_iterations_per_step": round(s.iterations / steps, 1),
+            "refinement_rounds_per_step": round(s.reliable_updates / steps, 2),
+            "all_converged": bool(s.converged),
+            "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4), "loss_after": round(st.loss1, 4),
+                         "ms": round(st.ms, 1)},
+            "speedup_over_plain_fp64": round((steps / sec) / arms["plain_fp64"]["value"], 3),
+            "speedup_over_mixed_cg": round((steps / sec) / arms["mixed_cg"]["value"], 3)}
+    ctx.close()
+    out.update(arms)
+    return out
 
 
 def dirac_hbm(yk, torch, stream, Nt=4096, Nx=4096, reps=20):
@@ -392,6 +466,7 @@ def main(argv=None):
     ap.add_argument("--fp64-steps", type=int, default=None, help="default: --steps")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner configuration")
     ap.add_argument("--quick", action="store_true", help="timed region only")
     args = ap.parse_args(argv)
     if args.warmup < 3:
