@@ -303,12 +303,15 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
     stream.synchronize()
     sec = a.elapsed_time(b) / 1e3
     obs = [ctx.observables(c) for c in range(n_chains)]
+    t = ctx.tune_report()
     ctx.close()
     sites = int(sum(int(L) * int(L) for L in Ls))
     return {"config": f"{n_chains} chains, L in {{32,64,128,256}} (seed {seed}), 4 RHS, mixed CG rel-res 1e-10",
             "value": round(steps * n_chains / sec, 2), "unit": "chain-steps/s",
             "site_steps_per_s": round(steps * sites / sec, 1), "steps": steps,
-            "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
+            "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs),
+            "autotune": {"cg_grid": t.cg_grid, "cg_grid_max": t.cg_grid_max, "candidates": t.cg_candidates,
+                         "ms_chosen": round(t.cg_ms_chosen, 3), "ms_at_max": round(t.cg_ms_max, 3)}}
 
 
 def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_counts=(4, 2)):
@@ -373,6 +376,8 @@ def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_count
             "solver_iterations_per_step": round(s.iterations / steps, 1),
             "refinement_rounds_per_step": round(s.reliable_updates / steps, 2),
             "all_converged": bool(s.converged),
+            "conv_tile": list(ctx.tune_report().conv_rows_cols) if hasattr(ctx.tune_report(), "conv_rows_cols") else
+            [ctx.tune_report().conv_rows, ctx.tune_report().conv_cols],
             "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4), "loss_after": round(st.loss1, 4),
                          "ms": round(st.ms, 1)},
             "speedup_over_plain_fp64": round((steps / sec) / arms["plain_fp64"]["value"], 3),

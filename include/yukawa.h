@@ -268,6 +268,28 @@ int yk_coloured_noise(yk_ctx* ctx, int chain, const double* white, double* xi);
  * graph is captured once and replayed. */
 int yk_langevin_step(yk_ctx* ctx, int n_steps);
 
+/* The autotuner (no reference counterpart: the reference's launch shapes are
+ * fixed, main.cu:258-266).  Batched contexts (several CG systems per step):
+ * the grid of the step's persistent CG, i.e. how many 256-site tiles each
+ * block owns, chosen by timing the step's CG at candidate grids (the
+ * co-resident maximum, 3/4 and 1/2 of it, one block per SM, half of that).
+ * The learned solver's convolution tile (rows x columns) is chosen by timing
+ * candidates on the network's first solve.  Results never depend on either
+ * choice.  yk_langevin_step tunes automatically before it captures the step
+ * graph (environment YK_AUTOTUNE=0 at context creation: not automatically);
+ * yk_autotune tunes now (dropping a captured graph) and reports. */
+typedef struct yk_tune_result {
+    int cg_grid;               /* chosen grid of the batched step CG (0: not tuned)   */
+    int cg_grid_max;           /* the co-resident maximum                            */
+    int cg_candidates;         /* candidates timed                                   */
+    float cg_ms_chosen;        /* two timed 48-iteration solves at the chosen grid   */
+    float cg_ms_max;           /* the same at the co-resident maximum                */
+    int conv_rows, conv_cols;  /* chain 0 network's convolution tile (0: none yet)   */
+} yk_tune_result;
+int yk_autotune(yk_ctx* ctx, yk_tune_result* out);
+/* The last tuning's choices (all zero before any). */
+int yk_tune_report(yk_ctx* ctx, yk_tune_result* out);
+
 /* As yk_langevin_step, with every fermion solve of the step done by
  * yk_pcg_solve (flexible preconditioned CG inside FP64 refinement, to the
  * context's tolerance) with the chain's network (use_net = 1; every chain

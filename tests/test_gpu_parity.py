@@ -323,6 +323,58 @@ def test_batched_mixed_chains(ylib, cuda, monkeypatch, cluster):
         assert obs[c].steps == 2 and obs[c].status == 0
 
 
+@pytest.mark.parametrize("balance", ["0", "1"], ids=["uniform_ranges", "balanced_ranges"])
+def test_batched_block_ranges_keep_results(ylib, cuda, monkeypatch, balance):
+    # batched chains with block ranges balanced by the previous step's
+    # iterations: the same fields as the uniform ranges (every tile's partial
+    # is summed in a fixed order), checked against the FP64 oracle
+    monkeypatch.setenv("YK_CG_BALANCE", balance)
+    yk = ylib
+    specs = [(40, 24, 0.1, 0.5, S_HALF_PI, 2), (8, 8, 0.25, 0.3, 0.2, 1), (64, 64, 0.05, 0.8, 1.0, 1)]
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, cut_fraction=s, n_rhs=nr, precision=yk.YK_MIXED,
+                 cg_tol=1e-10, fixed_dt=0.01)
+          for nt, nx, m0, g, s, nr in specs]
+    with yk.Context(ps) as ctx:
+        ctx.step(3)
+        got = [ctx.get_field(c) for c in range(len(ps))]
+        assert all(ctx.observables(c).status == 0 for c in range(len(ps)))
+    for c, p in enumerate(ps):
+        phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+        for step in range(3):
+            phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10, tol_mode=1,
+                                     fixed_dt=0.01)
+        assert np.abs(got[c] - phi).max() < 1e-8, c
+
+
+def test_autotune_keeps_results(ylib, cuda, monkeypatch):
+    # batched chains: the tuned CG grid (automatic before the first capture,
+    # and again by an explicit call between steps) gives the same fields, bit
+    # for bit, as the untuned co-resident grid
+    yk = ylib
+    specs = [(40, 24, 0.1, 0.5, S_HALF_PI, 2), (8, 8, 0.25, 0.3, 0.2, 1), (64, 64, 0.05, 0.8, 1.0, 1)]
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, cut_fraction=s, n_rhs=nr, precision=yk.YK_MIXED,
+                 cg_tol=1e-10, fixed_dt=0.01)
+          for nt, nx, m0, g, s, nr in specs]
+    monkeypatch.setenv("YK_AUTOTUNE", "0")
+    with yk.Context(ps) as ctx:
+        ctx.step(4)
+        assert ctx.tune_report().cg_grid == 0
+        want = [ctx.get_field(c) for c in range(len(ps))]
+    monkeypatch.delenv("YK_AUTOTUNE")
+    with yk.Context(ps) as ctx:
+        ctx.step(2)
+        t = ctx.tune_report()
+        assert t.cg_candidates >= 2 and 8 <= t.cg_grid <= t.cg_grid_max
+        assert t.cg_ms_chosen <= t.cg_ms_max
+        t2 = ctx.autotune()
+        assert t2.cg_candidates >= 2
+        ctx.step(2)
+        got = [ctx.get_field(c) for c in range(len(ps))]
+        assert all(ctx.observables(c).status == 0 for c in range(len(ps)))
+    for c in range(len(ps)):
+        assert np.array_equal(got[c], want[c]), c
+
+
 def test_deterministic(ylib, cuda):
     yk = ylib
     p = params(yk, 32, 32)

@@ -161,6 +161,9 @@ def test_learned_step_matches_cg_step(ylib, cuda):
             else:
                 st = ctx.step_learned(3, use_net=(mode == "net"))
                 assert st.converged == 1 and st.rr <= 1e-20 * st.rr0 * 3
+                t = ctx.tune_report()   # the network's convolution tile, chosen on its first solve
+                if mode == "net":
+                    assert t.conv_rows in (2, 4, 8) and 1 <= t.conv_cols <= 64
             o = ctx.observables()
             assert o.steps == 3 and o.status == 0 and o.cg_iterations > 0
             fields[mode] = ctx.get_field()

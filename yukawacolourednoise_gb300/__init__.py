@@ -99,6 +99,12 @@ class SolveStats(C.Structure):
                 ("rr0", C.c_double), ("converged", C.c_int)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("cg_grid", C.c_int), ("cg_grid_max", C.c_int), ("cg_candidates", C.c_int),
+                ("cg_ms_chosen", C.c_float), ("cg_ms_max", C.c_float), ("conv_rows", C.c_int),
+                ("conv_cols", C.c_int)]
+
+
 class NetTrainCfg(C.Structure):
     _fields_ = [("n_sources", C.c_int), ("n_levels", C.c_int), ("base_iter", C.c_int), ("steps", C.c_int),
                 ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_uint64)]
@@ -158,6 +164,8 @@ _SIGS = {
     "yk_net_train": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(NetTrainCfg), C.POINTER(NetTrainStats)]),
     "yk_fgcr_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(SolveStats)]),
+    "yk_autotune": (C.c_int, [C.c_void_p, C.POINTER(TuneResult)]),
+    "yk_tune_report": (C.c_int, [C.c_void_p, C.POINTER(TuneResult)]),
     "yk_langevin_step_learned": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(SolveStats)]),
     "yk_pcg_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int,
                                C.POINTER(SolveStats)]),
@@ -354,6 +362,16 @@ class Context:
 
     def step(self, n=1):
         _check(lib().yk_langevin_step(self.h, n))
+
+    def autotune(self) -> TuneResult:
+        t = TuneResult()
+        _check(lib().yk_autotune(self.h, C.byref(t)))
+        return t
+
+    def tune_report(self) -> TuneResult:
+        t = TuneResult()
+        _check(lib().yk_tune_report(self.h, C.byref(t)))
+        return t
 
     def step_learned(self, n=1, use_net=True) -> SolveStats:
         st = SolveStats()

@@ -115,6 +115,7 @@ struct yk_ctx {
     int* d_err = nullptr;
     int* d_nactive = nullptr;
     int* d_anyru = nullptr;
+    int* d_balance = nullptr;      // work-balanced block ranges of the batched step CG (CGArgs::balance)
     int2* d_site_tiles = nullptr;
     int n_site_tiles = 0;
     double* d_tile_max = nullptr;
@@ -140,6 +141,16 @@ struct yk_ctx {
     // single-system mixed solves may take the halo CG kernel (YK_CG_HALO=0 in
     // the environment at context creation: never)
     bool cg_halo = true;
+    // the autotuner: grid cap of the step's batched CG (0: the co-resident
+    // maximum), chosen by timing candidates before the step graph is captured
+    // (YK_AUTOTUNE=0 at context creation: never automatically)
+    int cg_grid_cap = 0;
+    bool autotune = true, tuned = false;
+    // batched step CG: block ranges balanced by the previous step's
+    // iterations (YK_CG_BALANCE=1 at context creation; default uniform
+    // ranges, which measured faster on the 64-chain configuration)
+    bool cg_balance = false;
+    yk_tune_result tune = {};
     // profiling: CUDA events around each kernel class of the step
     bool profiling = false;
     struct Rec {
@@ -246,6 +257,7 @@ CGArgs base_args(yk_ctx* ctx)
     a.reliable_every = ctx->reliable_every;
     a.reliable_delta = ctx->reliable_delta;
     a.mtype = YK_DAGGER;
+    a.grid_cap = ctx->cg_grid_cap;
     return a;
 }
 
@@ -345,10 +357,15 @@ int enqueue_step(yk_ctx* ctx)
             YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
             ctx->cg_grid = 16 * ctx->nsys;
             ctx->cg_kernel = 2;
+            prof_end(ctx, 1, e, 2);
         } else {
+            // batched: block ranges balanced by the previous step's iterations
+            const bool bal = ctx->nsys > 1 && ctx->cg_balance;
+            if (bal) a.balance = ctx->d_balance;
             YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid, &ctx->cg_kernel));
+            if (bal) YK_CK(launch_cg_balance(a, ctx->cg_grid, ctx->d_balance, ctx->stream));
+            prof_end(ctx, 1, e, bal ? 3 : 2);
         }
-        prof_end(ctx, 1, e, 2);
     }
     StepArgs s = step_args(ctx);
     prof_begin(ctx, &e);
@@ -560,6 +577,87 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
     return YK_OK;
 }
 
+// The autotuner.  Batched steps (several CG systems in one launch): the grid
+// of the persistent CG, i.e. how many tiles each block owns, by timing the
+// step's CG (sources of Philox kind 100, which no step draws; 48 iterations;
+// two launches after one warm-up) at each candidate: the co-resident maximum,
+// 3/4 and 1/2 of it, one block per SM and half of that.  Fewer blocks own
+// more tiles each and synchronise fewer arrivals; more blocks hide latency.
+// The iterates do not depend on the grid (tile partials are summed in a fixed
+// order), so tuning never changes results.  The learned solver's convolution
+// tile is tuned by the network itself on its first solve (net_tile reports it).
+int run_autotune(yk_ctx* ctx)
+{
+    yk_tune_result& T = ctx->tune;
+    T = yk_tune_result{};
+    const bool mixed = ctx->precision == YK_MIXED;
+    if (ctx->nsys > 1 && !ctx->cg_cluster) {
+        const int maxg = cg_max_grid(1, mixed);
+        std::vector<int> cand = {maxg, maxg * 3 / 4, maxg / 2, ctx->n_sm, ctx->n_sm / 2};
+        std::sort(cand.begin(), cand.end(), std::greater<int>());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        YK_CK(cudaEventCreate(&e0));
+        YK_CK(cudaEventCreate(&e1));
+        CGArgs a = base_args(ctx);
+        a.sys = ctx->d_sys;
+        a.sys_first = 0;
+        a.sys_count = ctx->nsys;
+        a.tiles = ctx->d_sys_tiles;
+        a.tile_begin = 0;
+        a.tile_end = ctx->n_sys_tiles;
+        a.eta_kind = 100;
+        a.st = ctx->d_state;
+        a.partial = ctx->d_partial;
+        a.coef = ctx->d_coef;
+        a.max_iter = std::min(ctx->max_iter, 48);
+        int best = 0;
+        float best_ms = 0.f;
+        for (int c : cand) {
+            if (c < 8 || c > maxg) continue;
+            if ((ctx->n_sys_tiles + c - 1) / c > kMaxTilesPerBlock) continue;
+            a.grid_cap = c;
+            cudaError_t e = launch_cg(a, 1, mixed, ctx->stream, nullptr);
+            if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+            for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) e = launch_cg(a, 1, mixed, ctx->stream, nullptr);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                set_error("autotune: %s", cudaGetErrorString(e));
+                return YK_ECUDA;
+            }
+            if (int rc = status_of_err(ctx)) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return rc;
+            }
+            ++T.cg_candidates;
+            if (c == maxg) T.cg_ms_max = ms;
+            if (!best || ms < best_ms) {
+                best = c;
+                best_ms = ms;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->cg_grid_cap = best == maxg ? 0 : best;
+        T.cg_grid = best;
+        T.cg_grid_max = maxg;
+        T.cg_ms_chosen = best_ms;
+    }
+    for (const Chain& C : ctx->ch)
+        if (C.net) {
+            net_tile(C.net, &T.conv_rows, &T.conv_cols);
+            break;
+        }
+    ctx->tuned = true;
+    return YK_OK;
+}
+
 StepArgs chain_step_args(yk_ctx* ctx, int c)
 {
     StepArgs s = step_args(ctx);
@@ -634,6 +732,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         ctx->cg_halo = !(he && he[0] == '0');
         const char* ne = getenv("YK_NOISE_OVERLAP");
         ctx->noise_overlap = !(ne && ne[0] == '0');
+        const char* ae = getenv("YK_AUTOTUNE");
+        ctx->autotune = !(ae && ae[0] == '0');
+        const char* be = getenv("YK_CG_BALANCE");
+        ctx->cg_balance = be && be[0] == '1';
     }
 
     ctx->ch.resize(n_chains);
@@ -740,6 +842,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     const size_t o_flags = ar.reserve(sizeof(unsigned) * kFlagStride * (size_t)kMaxGrid);
     const size_t o_bar = ar.reserve(sizeof(GridBarrier));
     const size_t o_err = ar.reserve(sizeof(int) * 4);
+    const size_t o_balance = ar.reserve(sizeof(int) * (kMaxGrid + 2));
     const size_t o_sitetiles = ar.reserve(sizeof(int2) * nsite_tiles);
     const size_t o_tmax = ar.reserve(sizeof(double) * nsite_tiles);
     const size_t o_tsum = ar.reserve(sizeof(double2) * nsite_tiles);
@@ -774,6 +877,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     ctx->d_err = ar.at<int>(o_err);
     ctx->d_nactive = ctx->d_err + 1;
     ctx->d_anyru = ctx->d_err + 2;
+    ctx->d_balance = ar.at<int>(o_balance);
     ctx->d_site_tiles = ar.at<int2>(o_sitetiles);
     ctx->d_tile_max = ar.at<double>(o_tmax);
     ctx->d_tile_sum = ar.at<double2>(o_tsum);
@@ -1119,6 +1223,8 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
         set_error("yk_langevin_step: bad arguments");
         return YK_EINVAL;
     }
+    if (!ctx->gexec && ctx->autotune && !ctx->tuned && n_steps > 0)
+        if (int rc = run_autotune(ctx)) return rc;
     if (!ctx->gexec && !ctx->graph_failed && ctx->stream) {
         cudaGraph_t g = nullptr;
         bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -1510,6 +1616,37 @@ int yk_fgcr_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, in
         set_error("yk_fgcr_solve: %d iterations, |r|^2 = %g > the tolerance", r.iterations, r.rr);
         return YK_ENOCONV;
     }
+    return YK_OK;
+}
+
+int yk_autotune(yk_ctx* ctx, yk_tune_result* out)
+{
+    if (!ctx) {
+        set_error("yk_autotune: null context");
+        return YK_EINVAL;
+    }
+    if (ctx->gexec) {   // captured with the previous choice
+        YK_CK(cudaStreamSynchronize(ctx->stream));
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+    }
+    if (int rc = run_autotune(ctx)) return rc;
+    if (out) *out = ctx->tune;
+    return YK_OK;
+}
+
+int yk_tune_report(yk_ctx* ctx, yk_tune_result* out)
+{
+    if (!ctx || !out) {
+        set_error("yk_tune_report: bad arguments");
+        return YK_EINVAL;
+    }
+    *out = ctx->tune;
+    for (const Chain& C : ctx->ch)
+        if (C.net) {
+            net_tile(C.net, &out->conv_rows, &out->conv_cols);
+            break;
+        }
     return YK_OK;
 }
 

@@ -122,6 +122,7 @@ __device__ __forceinline__ unsigned long long gtimer()
 namespace {
 
 constexpr int kMaxSysPerBlock = 48;
+constexpr int kFinListMax = 1024;   // batched solves whose finisher compacts the active systems
 constexpr int kMaxDeps = 64;
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
@@ -340,6 +341,39 @@ __device__ bool nsync(const CGArgs& a, unsigned epoch, const Deps& d)
     return __syncthreads_or(bad) == 0;
 }
 
+// Whether the launch uses work-balanced block ranges.
+__device__ __forceinline__ bool balanced(const CGArgs& a)
+{
+    return a.balance != nullptr && a.balance[0] == (int)gridDim.x;
+}
+
+// The block that owns table tile `pos`: uniform ranges, or the last block
+// whose balanced range starts at or before pos (empty ranges share starts).
+__device__ __forceinline__ int owner_of(const CGArgs& a, int pos)
+{
+    if (!balanced(a)) return (pos - a.tile_begin) / a.tiles_per_block;
+    const int* st = a.balance + 1;
+    int lo = 0, hi = (int)gridDim.x - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (st[mid] <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The block's tile range [tb, te).
+__device__ __forceinline__ void block_range(const CGArgs& a, int* tb, int* te)
+{
+    if (balanced(a)) {
+        *tb = a.balance[1 + blockIdx.x];
+        *te = a.balance[2 + blockIdx.x];
+    } else {
+        *tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
+        *te = min(*tb + a.tiles_per_block, a.tile_end);
+    }
+}
+
 // The block's system table and neighbour blocks, from its tile range [tb, te).
 // A tile's stencil reaches at most Nx sites away (wrapping within its system),
 // i.e. fewer than Nx / 256 + 2 tiles; only tiles that close to an end of the
@@ -374,7 +408,7 @@ __device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 if (d == 0) continue;
                 int q = (rel + d) % S.ntiles;
                 if (q < 0) q += S.ntiles;
-                const int blk = (S.tile0 + q - a.tile_begin) / a.tiles_per_block;
+                const int blk = owner_of(a, S.tile0 + q);
                 if (blk == (int)blockIdx.x) continue;
                 bool seen = false;
                 for (int i = 0; i < nd && !seen; ++i) seen = (dp->b[i] == blk);
@@ -766,23 +800,52 @@ __device__ __noinline__ void finish_reduction(const CGArgs& a, int k, bool ru_ro
                                  unsigned gen)
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int G = MIXED ? nw : 1;
-    while (G > 1 && G * a.sys_count > nw) G >>= 1;
-    const int ngroups = nw / G, gid = w / G, wg = w % G, T = 32 * G, tg = wg * 32 + lane;
-    float2* red2 = reinterpret_cast<float2*>(red);
+    // Batched solves: the systems still iterating, compacted (their order in
+    // the list does not matter: each system's sum has a fixed order); a
+    // retired system only republishes its idle coefficients, which the
+    // blocks that own its tiles poll.
+    __shared__ int s_list[kFinListMax];
+    __shared__ int s_nlist;
+    const bool listed = a.sys_count > 1 && a.sys_count <= kFinListMax;
     if (threadIdx.x == 0) {
         *s_active = 0;
         *s_ru = 0;
+        s_nlist = 0;
     }
     __syncthreads();
-    const int rounds = (a.sys_count + ngroups - 1) / ngroups;
+    if (listed) {
+        const CoefVals idle = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
+        bool any_idle = false;
+        for (int q = threadIdx.x; q < a.sys_count; q += blockDim.x) {
+            const int j = a.sys_first + q;
+            if (*(volatile const int*)&a.st[j].mode != kIdle) {
+                s_list[atomicAdd(&s_nlist, 1)] = j;
+            } else {
+                if (!any_idle) __threadfence();
+                any_idle = true;
+                publish_coef(a.coef + j, idle, gen);
+            }
+        }
+        __syncthreads();
+    }
+    const int nsys = listed ? s_nlist : a.sys_count;
+    int G = MIXED ? nw : 1;
+    while (G > 1 && G * nsys > nw) G >>= 1;
+    const int ngroups = nw / G, gid = w / G, wg = w % G, T = 32 * G, tg = wg * 32 + lane;
+    float2* red2 = reinterpret_cast<float2*>(red);
+    const int rounds = (nsys + ngroups - 1) / ngroups;
 #ifdef YK_CG_TIMING
     const long long f0 = clock64();
     long long f1 = 0, f2 = 0, f_ld = 0;
 #endif
+    if (rounds == 0 && threadIdx.x == 0) {   // every system retired
+        __threadfence();
+        st_word(&a.bar->gword, stamp((unsigned)*s_active | ((unsigned)(*s_ru != 0) << 31), gen));
+    }
     for (int rnd = 0; rnd < rounds; ++rnd) {
-        const int j = a.sys_first + rnd * ngroups + gid;
-        const bool have = j < a.sys_first + a.sys_count;
+        const int q = rnd * ngroups + gid;
+        const bool have = q < nsys;
+        const int j = listed ? (have ? s_list[q] : a.sys_first) : a.sys_first + q;
         CGState st;
         int tile0 = 0, ntiles = 0;
         if (have) {
@@ -800,7 +863,7 @@ __device__ __noinline__ void finish_reduction(const CGArgs& a, int k, bool ru_ro
             FF acc[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) acc[c] = FF{0.f, 0.f};
-#pragma unroll 2
+#pragma unroll 4
             for (int i = tg; i < ntiles; i += T) {
                 const Partial* pp = a.partial + tile0 + i;
                 const float4 q0 = ld_sync4f(&pp->f[0]), q1 = ld_sync4f(&pp->f[2]), q2 = ld_sync4f(&pp->f[4]);
@@ -1557,8 +1620,8 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     __shared__ CGState lst;   // single-system solves: this block's copy of the state
     __shared__ FastShadow fsh;   // and its FP32 copies for the fast step
     const bool solo = (a.sys_count == 1);
-    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
-    const int te = min(tb + a.tiles_per_block, a.tile_end);
+    int tb, te;
+    block_range(a, &tb, &te);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
     if (*(volatile int*)a.err) return;   // the other blocks' waits see the flag and end
     if (solo && threadIdx.x == 0) {
@@ -2288,17 +2351,20 @@ static int halo_max_grid()
 
 void cg_halo_init() { halo_max_grid(); }
 
+static int capped(int maxg, int cap) { return cap > 0 && cap < maxg ? cap : maxg; }
+
 int cg_predict_grid(const CGArgs& a, bool mixed)
 {
     int tpb = 1;
-    return cg_grid_for(a.tile_end - a.tile_begin, mixed ? max_grid_t<1, true>() : max_grid_t<1, false>(), &tpb);
+    return cg_grid_for(a.tile_end - a.tile_begin,
+                       capped(mixed ? max_grid_t<1, true>() : max_grid_t<1, false>(), a.grid_cap), &tpb);
 }
 
 template <int K, bool MIXED>
 static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out, int* kernel_out)
 {
     CGArgs a = a0;
-    const int maxg = max_grid_t<K, MIXED>();
+    const int maxg = capped(max_grid_t<K, MIXED>(), a.grid_cap);
     const int nt = a.tile_end - a.tile_begin;
     int tpb = 1;
     const int grid = cg_grid_for(nt, maxg, &tpb);
@@ -2332,6 +2398,78 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     cfg.numAttrs = 1;
     void* args[] = {&a};
     return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+// Work-balanced block ranges for the next solve of the same systems: every
+// tile of system s weighs (iterations of s in the solve just finished + 16),
+// and blocks take contiguous table ranges of about equal weight, at most
+// kMaxTilesPerBlock tiles and kMaxSysPerBlock systems each (greedy over the
+// systems' tile runs, one thread).  A partition that cannot meet the caps is
+// not published ([0] = 0: the next launch uses the uniform ranges).  The
+// iterates of every system do not depend on the ranges (tile partials are
+// summed in a fixed order), only the time does: without balancing, the blocks
+// that own the slowest systems' tiles run the last iterations alone.
+__global__ void cg_balance_kernel(CGArgs a, int grid, int* out)
+{
+    if (threadIdx.x != 0) return;
+    constexpr int kOverhead = 16;
+    double W = 0.0;
+    for (int s = a.sys_first; s < a.sys_first + a.sys_count; ++s)
+        W += (double)a.sys[s].ntiles * (double)(a.st[s].iters + kOverhead);
+    const double target = W / grid;
+    int b = 0, ntb = 0, nsb = 0, last_sys = -1;
+    double acc = 0.0;
+    bool ok = true;
+    out[1] = a.tile_begin;
+    int t = a.tile_begin;
+    while (t < a.tile_end && ok) {
+        const int s = a.tiles[t].x;
+        const SysDev& S = a.sys[s];
+        const int run_end = min(a.tile_end, S.tile0 + S.ntiles);   // the system's tiles are contiguous
+        const double w = (double)(a.st[s].iters + kOverhead);
+        int rem = run_end - t;
+        while (rem > 0) {
+            if (b < grid - 1 && (ntb == kMaxTilesPerBlock || (nsb == kMaxSysPerBlock && s != last_sys))) {
+                out[1 + ++b] = t;
+                acc = 0.0;
+                ntb = nsb = 0;
+                last_sys = -1;
+            }
+            int take = min(rem, kMaxTilesPerBlock - ntb);
+            if (b < grid - 1) {
+                const double need = ceil((target - acc) / w);
+                take = min(take, need < 1.0 ? 1 : (int)min(need, 1e9));
+            }
+            if (take < 1) {   // the last block is full
+                ok = false;
+                break;
+            }
+            if (s != last_sys) {
+                ++nsb;
+                last_sys = s;
+            }
+            acc += take * w;
+            ntb += take;
+            t += take;
+            rem -= take;
+            if (b < grid - 1 && acc >= target) {
+                out[1 + ++b] = t;
+                acc = 0.0;
+                ntb = nsb = 0;
+                last_sys = -1;
+            }
+        }
+        if (nsb > kMaxSysPerBlock || ntb > kMaxTilesPerBlock) ok = false;
+    }
+    for (int q = b + 1; q <= grid; ++q) out[1 + q] = a.tile_end;   // trailing empty ranges, and the end
+    out[0] = ok ? grid : 0;
+}
+
+cudaError_t launch_cg_balance(const CGArgs& a, int grid, int* out, cudaStream_t stream)
+{
+    if (grid < 1 || grid > kMaxGrid || a.sys_count < 2) return cudaSuccess;
+    cg_balance_kernel<<<1, 32, 0, stream>>>(a, grid, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out, int* kernel_out)

@@ -123,6 +123,11 @@ struct CGArgs {
     int reliable_every;
     double reliable_delta;
     int solo_nt, solo_nx;   // lattice of a single-system solve (0: not given; the halo kernel needs it)
+    int grid_cap;           // largest grid the launcher may use (0: the co-resident maximum)
+    // work-balanced block ranges (batched step solves): [0] = the grid they
+    // were computed for, [1 + b] = first tile of block b, [1 + grid] = end;
+    // used when [0] equals the launch's grid, else the uniform ranges
+    const int* balance;
 };
 
 // Per-chain device record of the Langevin step.

@@ -17,6 +17,10 @@ cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt,
 // Batched CG (yk_cg.cu).  Also launches its one-block preparation kernel.
 // grid_out: blocks launched; kernel_out: 0 cg_kernel, 1 cg_halo_kernel (either may be null)
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out, int* kernel_out = nullptr);
+// Work-balanced block ranges (CGArgs::balance) for the next solve of the
+// systems of `a`, from their iteration counts in the solve just finished;
+// grid: the grid of that solve's launch.  No-op for a single system.
+cudaError_t launch_cg_balance(const CGArgs& a, int grid, int* out, cudaStream_t stream);
 // Largest co-resident grid of the CG kernel (cached; call before capturing).
 int cg_max_grid(int K, bool mixed);
 // Kernel attributes and occupancy of the halo CG kernel (call before any stream capture).
@@ -86,6 +90,8 @@ struct FgcrResult {
 LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err);
 void net_destroy(LearnedNet* n);
 int net_size(const LearnedNet* n);
+// the convolution tile of the solvers' M (0 x 0 before the first solve tuned it)
+void net_tile(const LearnedNet* n, int* rows, int* cols);
 void net_set_skip(LearnedNet* n, float skip);   // M(r) = skip r + N(r)
 cudaError_t net_weights(LearnedNet* n, float* host, bool set);
 cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);

@@ -516,6 +516,7 @@ void pcg_graph_destroy(PcgGraph* g);
 struct LearnedNet {
     int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
     int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
+    bool tc_tuned = false;            // tile chosen by timing (first solve)
     unsigned* dcnt = nullptr;         // arrival counters of the preconditioned CG's reductions
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
     uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
@@ -633,6 +634,12 @@ void net_destroy(LearnedNet* n)
 }
 
 int net_size(const LearnedNet* n) { return n->nw; }
+
+void net_tile(const LearnedNet* n, int* rows, int* cols)
+{
+    *rows = n->tc_tuned ? n->tc_R : 0;
+    *cols = n->tc_tuned ? n->tc_W : 0;
+}
 
 void net_set_skip(LearnedNet* n, float skip) { n->skip = skip; }
 
@@ -772,6 +779,46 @@ cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, floa
     for (int l = L - 1; l >= 0; --l) conv_T(n, l, dec_of(n, l + 1), dec_of(n, l), s);
     net_featT_kernel<<<n->grid, kNetThreads, 0, s>>>(n->dec, sigma, r, n->skip, z, V);
     return cudaGetLastError();
+}
+
+// The convolution tile, chosen by timing the network's layers (one warm-up,
+// three timed passes on zeroed activations) at each candidate of 16, 32 or 64
+// columns (at most Nx) and 2, 4 or 8 rows; the default (8 x 64, rows halved
+// while there are fewer than two tiles per SM) is a candidate.
+cudaError_t net_tune_tile(LearnedNet* n, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(n->h16[0], 0, sizeof(uint4) * n->V, s);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    int bestR = n->tc_R, bestW = n->tc_W;
+    float best = -1.f;
+    for (int W : {64, 32, 16}) {
+        if (W > n->Nx && W != 64) continue;
+        for (int R : {8, 4, 2}) {
+            if (e != cudaSuccess) break;
+            n->tc_R = R;
+            n->tc_W = std::min(W, n->Nx);
+            net_convs_fast(n, s);
+            e = cudaEventRecord(e0, s);
+            for (int rep = 0; rep < 3; ++rep) net_convs_fast(n, s);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && (best < 0.f || ms < best)) {
+                best = ms;
+                bestR = n->tc_R;
+                bestW = n->tc_W;
+            }
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    n->tc_R = bestR;
+    n->tc_W = bestW;
+    n->tc_tuned = e == cudaSuccess;
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 // z = M(r) with the tensor-core convolutions (the solvers' preconditioner)
@@ -1398,6 +1445,14 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
     const PcgBufs B = {n->f0, n->f1, n->f2, n->Zs, n->Ws, n->f3, n->dsc};
     f_of_d_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->sig32, n->V);
     const int nb = n->grid;
+    if (use_net && !n->tc_tuned) {
+        e = net_tune_tile(n, s);
+        if (e != cudaSuccess) return e;
+        if (n->pcg) {   // captured with the previous tile
+            pcg_graph_destroy(n->pcg);
+            n->pcg = nullptr;
+        }
+    }
     // the chunk graph, captured again when the operator or the network changed
     PcgGraph*& G = n->pcg;
     if (G && (G->use_net != use_net || G->sigma != sigma || G->m0 != m0 || G->g != g || G->r != r ||
