@@ -371,13 +371,13 @@ def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_count
         ctx.set_field(phi0)
         ctx.set_step(step0)
         sec, s = wall(lambda: ctx.step_learned(steps))
+        tile = ctx.tune_report()
         arms[f"learned_{nl}layers"] = {
             "value": round(steps / sec, 2), "unit": "steps/s",
             "solver_iterations_per_step": round(s.iterations / steps, 1),
             "refinement_rounds_per_step": round(s.reliable_updates / steps, 2),
             "all_converged": bool(s.converged),
-            "conv_tile": list(ctx.tune_report().conv_rows_cols) if hasattr(ctx.tune_report(), "conv_rows_cols") else
-            [ctx.tune_report().conv_rows, ctx.tune_report().conv_cols],
+            "conv_tile_rows_cols": [tile.conv_rows, tile.conv_cols],
             "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4), "loss_after": round(st.loss1, 4),
                          "ms": round(st.ms, 1)},
             "speedup_over_plain_fp64": round((steps / sec) / arms["plain_fp64"]["value"], 3),
