@@ -256,7 +256,7 @@ def run_ours(args, ws, rank, local):
         extras["batching"] = batched(yk, torch, stream)
         # the learned-preconditioner configuration (512^2 near the chiral regime)
         if not args.no_learned:
-            extras["learned"] = learned(yk, torch, stream)
+            extras["learned"] = learned(yk, torch, stream, steps=args.learned_steps)
         extras["gpu_launches"] = int(round(launches_per_step * args.steps))
 
     ctx.close()
@@ -473,9 +473,18 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner configuration")
     ap.add_argument("--quick", action="store_true", help="timed region only")
+    ap.add_argument("--learned-only", action="store_true",
+                    help="only the learned-preconditioner configuration (one JSON object; profiling runs)")
+    ap.add_argument("--learned-steps", type=int, default=20)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.learned_only:
+        import torch
+        import yukawacolourednoise_gb300 as yk
+        stream = torch.cuda.Stream()
+        print(json.dumps({"learned": learned(yk, torch, stream, steps=args.learned_steps)}), flush=True)
+        return 0
     ws, rank, local = dist_env()
     line = run_reference(args, ws, rank) if args.impl == "reference" else run_ours(args, ws, rank, local)
     if line is not None:

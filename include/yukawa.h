@@ -287,6 +287,8 @@ typedef struct yk_tune_result {
     int conv_rows, conv_cols;  /* chain 0 network's convolution tile (0: none yet)   */
 } yk_tune_result;
 int yk_autotune(yk_ctx* ctx, yk_tune_result* out);
+/* (Environment YK_NET_TILE=RxW, e.g. 8x64, fixes the convolution tile
+ * instead of timing candidates: for profiling and reproducible timing.) */
 /* The last tuning's choices (all zero before any). */
 int yk_tune_report(yk_ctx* ctx, yk_tune_result* out);
 

@@ -20,6 +20,8 @@
 // output are site-major (4 floats per site, the layout of the CG vectors).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -519,6 +521,7 @@ struct LearnedNet {
     bool tc_tuned = false;            // tile chosen by timing (first solve)
     unsigned* dcnt = nullptr;         // arrival counters of the preconditioned CG's reductions
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
+    float* diag32 = nullptr;          // FP32 diagonal 2 r + m0 + g sigma of the current solve
     uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
     std::vector<int> woff;            // each layer's first weight
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
@@ -619,7 +622,7 @@ void net_destroy(LearnedNet* n)
 {
     if (!n) return;
     float* fs[] = {n->w, n->g, n->m, n->v, n->act, n->dec, n->gbuf[0], n->gbuf[1], n->gz, n->z, n->part, n->pairs,
-                   n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws, n->sig32};
+                   n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws, n->sig32, n->diag32};
     for (float* p : fs)
         if (p) cudaFree(p);
     double* ds[] = {n->dpart, n->d0, n->d1, n->d2, n->dsc};
@@ -679,6 +682,7 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e == cudaSuccess) e = alloc_d(&n->dpart, n->grid);
     if (e == cudaSuccess) e = cudaMalloc(&n->dcnt, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = alloc_f(&n->sig32, V);
+    if (e == cudaSuccess) e = alloc_f(&n->diag32, V);
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[0], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[1], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMemset(n->dcnt, 0, sizeof(unsigned) * 4);
@@ -787,6 +791,16 @@ cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, floa
 // while there are fewer than two tiles per SM) is a candidate.
 cudaError_t net_tune_tile(LearnedNet* n, cudaStream_t s)
 {
+    // YK_NET_TILE=RxW in the environment fixes the tile (R in 1..8, W in 1..64)
+    if (const char* env = getenv("YK_NET_TILE")) {
+        int R = 0, W = 0;
+        if (sscanf(env, "%dx%d", &R, &W) == 2 && R >= 1 && R <= kTcMaxR && W >= 1 && W <= kTcMaxW) {
+            n->tc_R = R;
+            n->tc_W = std::min(W, n->Nx);
+            n->tc_tuned = true;
+            return cudaSuccess;
+        }
+    }
     cudaError_t e = cudaMemsetAsync(n->h16[0], 0, sizeof(uint4) * n->V, s);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
@@ -1258,29 +1272,6 @@ __device__ __forceinline__ void block_sum_f(float (&v)[NV], double (&out)[NV], d
     }
 }
 
-// <p, q> (FP32 products of a site, FP64 across sites); the last block sets
-// sc[kPQ] and alpha = <r, z> / <p, q>
-__global__ void __launch_bounds__(kNetThreads) pcg_pq_kernel(const float* __restrict__ p, const float* __restrict__ q,
-                                                             double* __restrict__ part, unsigned* counter,
-                                                             double* __restrict__ sc, int V)
-{
-    __shared__ double red[32];
-    float acc[1] = {0.f};
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
-        const float4 pv = reinterpret_cast<const float4*>(p)[n], qv = reinterpret_cast<const float4*>(q)[n];
-        acc[0] += fmaf(pv.x, qv.x, fmaf(pv.y, qv.y, fmaf(pv.z, qv.z, pv.w * qv.w)));
-    }
-    double tot[1];
-    block_sum_f<1>(acc, tot, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
-    if (!last_arrival(counter)) return;
-    const double pq = sum_partials(part, gridDim.x, red);
-    if (threadIdx.x == 0) {
-        sc[kPQ] = pq;
-        sc[kAlpha] = pq != 0.0 ? sc[kRZ] / pq : 0.0;
-    }
-}
-
 // x += alpha p, r -= alpha q; with X != null also the network's BF16
 // features (r, sigma r) of the new r
 __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
@@ -1356,24 +1347,74 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
     }
 }
 
-// p = z + beta p
-__global__ void __launch_bounds__(kNetThreads) pcg_p_kernel(float* __restrict__ p, const float* __restrict__ z,
-                                                            const double* __restrict__ sc, int V)
+// diag32[n] = 2 r + m0 + g sigma[n] in FP32 (the stencils below run on the
+// FP32 pipes only)
+__global__ void diag_f_kernel(const double* __restrict__ sigma, float* __restrict__ out, double m0, double g,
+                              double r, int V)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x)
+        out[n] = (float)(2.0 * r + m0 + g * sigma[n]);
+}
+
+// p' = z + beta p (written at the own site), and t = D p' with the
+// neighbours' p' formed on the fly from z and p (p' goes to the other
+// buffer: a neighbour may still read p)
+__global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __restrict__ z,
+                                                             const float* __restrict__ p, float* __restrict__ p_new,
+                                                             float* __restrict__ t, const float* __restrict__ diag,
+                                                             const double* __restrict__ sc, int Nt, int Nx, float rw)
 {
     const float b = (float)sc[kBeta];
+    const int V = Nt * Nx;
+    auto pn = [&](int m) {
+        const Site<float, 1> zz = load_site<float, 1>(z, m), pp = load_site<float, 1>(p, m);
+        Site<float, 1> o;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o.v[q] = fmaf(b, pp.v[q], zz.v[q]);
+        return o;
+    };
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
-        float4 pv = reinterpret_cast<float4*>(p)[n];
-        const float4 zv = reinterpret_cast<const float4*>(z)[n];
-        pv.x = fmaf(b, pv.x, zv.x);
-        pv.y = fmaf(b, pv.y, zv.y);
-        pv.z = fmaf(b, pv.z, zv.z);
-        pv.w = fmaf(b, pv.w, zv.w);
-        reinterpret_cast<float4*>(p)[n] = pv;
+        const Nbr nb = neighbours(n, Nt, Nx);
+        const Site<float, 1> c = pn(n), tu = pn(nb.tu), td = pn(nb.td), xu = pn(nb.xu), xd = pn(nb.xd);
+        store_site<float, 1>(p_new, n, c);
+        store_site<float, 1>(t, n, dirac_combine<float, 1, false>(c, tu, td, xu, xd, diag[n], rw, (float)nb.sp,
+                                                                  (float)nb.sm));
+    }
+}
+
+// q = D^dag t and <p, q> (FP32 per site, FP64 across warps); the last block
+// sets pq and alpha = <r, z> / <p, q>
+__global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __restrict__ t,
+                                                             const float* __restrict__ p, float* __restrict__ q,
+                                                             const float* __restrict__ diag,
+                                                             double* __restrict__ part, unsigned* counter,
+                                                             double* __restrict__ sc, int Nt, int Nx, float rw)
+{
+    __shared__ double red[32];
+    const int V = Nt * Nx;
+    float acc[1] = {0.f};
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
+        const Nbr nb = neighbours(n, Nt, Nx);
+        const Site<float, 1> o = dirac_combine<float, 1, true>(
+            load_site<float, 1>(t, n), load_site<float, 1>(t, nb.tu), load_site<float, 1>(t, nb.td),
+            load_site<float, 1>(t, nb.xu), load_site<float, 1>(t, nb.xd), diag[n], rw, (float)nb.sp, (float)nb.sm);
+        store_site<float, 1>(q, n, o);
+        const Site<float, 1> pv = load_site<float, 1>(p, n);
+        acc[0] += fmaf(pv.v[0], o.v[0], fmaf(pv.v[1], o.v[1], fmaf(pv.v[2], o.v[2], pv.v[3] * o.v[3])));
+    }
+    double tot[1];
+    block_sum_f<1>(acc, tot, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
+    if (!last_arrival(counter)) return;
+    const double pq = sum_partials(part, gridDim.x, red);
+    if (threadIdx.x == 0) {
+        sc[kPQ] = pq;
+        sc[kAlpha] = pq != 0.0 ? sc[kRZ] / pq : 0.0;
     }
 }
 
 struct PcgBufs {
-    float *r, *x, *z, *p, *q, *tmp;
+    float *r, *x, *z, *p[2], *q, *tmp;
     double* sc;
 };
 
@@ -1389,22 +1430,25 @@ void pcg_precond(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs&
     }
     pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(a, n->sig32, b.r, n->skip, b.z,
                                             first ? nullptr : b.q, n->dpart, n->dcnt + 1, b.sc, first ? 1 : 0, V);
-    pcg_p_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.z, b.sc, V);
 }
 
-// `count` iterations (q = A p, alpha, x and r, z = M r, beta, p)
-cudaError_t pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs& b, int count,
-                           cudaStream_t s)
+// `count` iterations from the direction buffer `parity`: p' = z + beta p and
+// t = D p', q = D^dag t with alpha, x and r (and the features of r),
+// z = M r with beta.  Returns the parity after them.
+int pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs& b, int count, int parity,
+                   cudaStream_t s)
 {
     const int V = n->V, nb = n->grid;
-    for (int it = 0; it < count; ++it) {
-        cudaError_t e = apply_A(d, b.p, b.tmp, b.q, YK_FP32, s);
-        if (e != cudaSuccess) return e;
-        pcg_pq_kernel<<<nb, kNetThreads, 0, s>>>(b.p, b.q, n->dpart, n->dcnt, b.sc, V);
-        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, b.p, b.q, b.sc, n->sig32, use_net ? n->h16[0] : nullptr, V);
+    const float rw = (float)d.r;
+    for (int it = 0; it < count; ++it, parity ^= 1) {
+        float* p = b.p[parity];
+        float* pn = b.p[parity ^ 1];
+        pcg_dp_kernel<<<nb, kNetThreads, 0, s>>>(b.z, p, pn, b.tmp, n->diag32, b.sc, d.Nt, d.Nx, rw);
+        pcg_dq_kernel<<<nb, kNetThreads, 0, s>>>(b.tmp, pn, b.q, n->diag32, n->dpart, n->dcnt, b.sc, d.Nt, d.Nx, rw);
+        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, pn, b.q, b.sc, n->sig32, use_net ? n->h16[0] : nullptr, V);
         pcg_precond(n, use_net, d, b, false, s);
     }
-    return cudaGetLastError();
+    return parity;
 }
 
 }  // namespace
@@ -1442,8 +1486,9 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
     }
     double* Ax = n->d1;
     double* r64 = n->d2;
-    const PcgBufs B = {n->f0, n->f1, n->f2, n->Zs, n->Ws, n->f3, n->dsc};
+    const PcgBufs B = {n->f0, n->f1, n->f2, {n->Zs, n->Zs + (size_t)V4}, n->Ws, n->f3, n->dsc};
     f_of_d_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->sig32, n->V);
+    diag_f_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->diag32, m0, g, r, n->V);
     const int nb = n->grid;
     if (use_net && !n->tc_tuned) {
         e = net_tune_tile(n, s);
@@ -1473,7 +1518,8 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
         cudaGraph_t graph = nullptr;
         bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
         if (ok) {
-            const cudaError_t ce = pcg_iterations(n, use_net, d, B, kPcgChunk, s);
+            pcg_iterations(n, use_net, d, B, kPcgChunk, 0, s);   // an even count: parity 0 -> 0
+            const cudaError_t ce = cudaGetLastError();
             ok = cudaStreamEndCapture(s, &graph) == cudaSuccess && ce == cudaSuccess && graph;
         }
         if (ok) ok = cudaGraphInstantiate(&G->exec, graph, 0) == cudaSuccess;
@@ -1497,9 +1543,10 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
         ++outer;
         dvec_to_f_kernel<<<nb, kNetThreads, 0, s>>>(r64, B.r, V4);
         e = cudaMemsetAsync(B.x, 0, sizeof(float) * V4, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(B.p, 0, sizeof(float) * V4, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.p[0], 0, sizeof(float) * V4, s);   // beta = 0: p' = z
         if (e != cudaSuccess) break;
-        pcg_precond(n, use_net, d, B, true, s);   // z = M r, p = z
+        pcg_precond(n, use_net, d, B, true, s);   // z = M r, beta = 0
+        int parity = 0;
         double h[8];
         e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -1507,8 +1554,12 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
         double rrc = rr0;
         while (e == cudaSuccess && iters < max_iter && rrc > inner_tol * inner_tol * rr0) {
             const int cnt = std::min(kPcgChunk, max_iter - iters);
-            if (G && cnt == kPcgChunk) e = cudaGraphLaunch(G->exec, s);
-            else e = pcg_iterations(n, use_net, d, B, cnt, s);
+            if (G && cnt == kPcgChunk && parity == 0) {
+                e = cudaGraphLaunch(G->exec, s);
+            } else {
+                parity = pcg_iterations(n, use_net, d, B, cnt, parity, s);
+                e = cudaGetLastError();
+            }
             iters += cnt;
             if (e == cudaSuccess) e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
