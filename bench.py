@@ -277,6 +277,47 @@ def run_ours(args, ws, rank, local):
     return line
 
 
+def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8):
+    """The full form at scale: 8 chains of 1024^2 (m0 = 0.01, g = 0.6,
+    Lambda = pi/4, i.e. cutFraction 0.17678), 8 stochastic right-hand sides
+    per step, mixed CG to rel-res 1e-10, all chains in one step graph, against
+    the plain FP64 CG form of the same step.  `steps` timed steps after
+    `warmup` (a step takes seconds: thousands of CG iterations over 64
+    systems of 2^20 sites)."""
+    def params(prec, c):
+        return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.6, fermion_mass=0.01,
+                                 wilson_param=1.0, cut_fraction=0.17677669529663687, Nt=L, Nx=L, fixed_dt=0.01,
+                                 precision=prec, cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=50000,
+                                 reliable_every=50, reliable_delta=0.001, n_rhs=n_rhs, seed=1234 + c,
+                                 init=yk.YK_INIT_PHILOX)
+
+    out = {"config": f"{n_chains} chains of {L}x{L}, m0 0.01, g 0.6, cutFraction 0.17678, {n_rhs} RHS, "
+                     f"rel-res 1e-10, {steps} timed step(s) after {warmup}", "steps": steps}
+    for name, prec in (("mixed_cg", yk.YK_MIXED), ("plain_fp64", yk.YK_FP64)):
+        ctx = yk.Context([params(prec, c) for c in range(n_chains)])
+        ctx.set_stream(stream.cuda_stream)
+        ctx.step(warmup)
+        ctx.synchronize()
+        before = sum(ctx.observables(c).cg_iterations_total for c in range(n_chains))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            ctx.step(steps)
+            b.record(stream)
+        stream.synchronize()
+        sec = a.elapsed_time(b) / 1e3
+        obs = [ctx.observables(c) for c in range(n_chains)]
+        its = sum(o.cg_iterations_total for o in obs) - before
+        out[name] = {"value": round(steps / sec, 4), "unit": "steps/s (all chains)",
+                     "chain_steps_per_s": round(steps * n_chains / sec, 3),
+                     "site_steps_per_s": round(steps * n_chains * L * L / sec, 1),
+                     "cg_iterations_per_system_step": round(its / (steps * n_chains * n_rhs), 1),
+                     "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
+        ctx.close()
+    out["speedup_mixed_over_fp64"] = round(out["mixed_cg"]["value"] / out["plain_fp64"]["value"], 3)
+    return out
+
+
 def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
     """The batching configuration: 64 chains of seeded sizes {32, 64, 128, 256}^2,
     m0 ~ U[0.05, 0.3], g ~ U[0.3, 0.8], 4 stochastic right-hand sides per chain,
@@ -476,9 +517,17 @@ def main(argv=None):
     ap.add_argument("--learned-only", action="store_true",
                     help="only the learned-preconditioner configuration (one JSON object; profiling runs)")
     ap.add_argument("--learned-steps", type=int, default=20)
+    ap.add_argument("--full-scale", action="store_true",
+                    help="only the full form at scale (8 chains of 1024^2, 8 RHS; one JSON object; minutes)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.full_scale:
+        import torch
+        import yukawacolourednoise_gb300 as yk
+        stream = torch.cuda.Stream()
+        print(json.dumps({"full_scale": full_scale(yk, torch, stream)}), flush=True)
+        return 0
     if args.learned_only:
         import torch
         import yukawacolourednoise_gb300 as yk

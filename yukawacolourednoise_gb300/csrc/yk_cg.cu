@@ -378,7 +378,7 @@ __device__ __forceinline__ void block_range(const CGArgs& a, int* tb, int* te)
 // A tile's stencil reaches at most Nx sites away (wrapping within its system),
 // i.e. fewer than Nx / 256 + 2 tiles; only tiles that close to an end of the
 // block's range or of their system can reach another block.
-__device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* nsl, int* tslot, Deps* dp)
+__device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* nsl, unsigned char* tslot, Deps* dp)
 {
     if (threadIdx.x == 0) {
         int n = 0, last = -1, nd = 0, all = 0;
@@ -399,7 +399,7 @@ __device__ void setup_block(const CGArgs& a, int tb, int te, SysLocal* sl, int* 
                 ++n;
                 last = s;
             }
-            tslot[t - tb] = n - 1;
+            tslot[t - tb] = (unsigned char)(n - 1);
             const SysDev& S = a.sys[s];
             const int h = S.Nx / kTile + 2;
             const int rel = t - S.tile0;
@@ -1522,7 +1522,7 @@ __device__ __forceinline__ void ru_fold(const SysDev& S, int n, const SysLocal& 
 // blockDim / 256 at a time as in the passes of the kernels calling this.
 // False when a neighbour wait gave up.
 template <int K>
-__device__ bool ru_residual(const CGArgs& a, const SysLocal* sl, const int* tslot, int tb, int te, bool first_dag,
+__device__ bool ru_residual(const CGArgs& a, const SysLocal* sl, const unsigned char* tslot, int tb, int te, bool first_dag,
                             int cur, int prv, unsigned& epoch, const Deps& deps, double* red)
 {
     constexpr int kSkipIm = (K == 1) ? ((1 << 3) | (1 << 5)) : 0;
@@ -1612,7 +1612,7 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
     __shared__ double red[128];
     __shared__ SysLocal sl[kMaxSysPerBlock];
     __shared__ int nsl;
-    __shared__ int tslot[kMaxTilesPerBlock];
+    __shared__ unsigned char tslot[kMaxTilesPerBlock];   // local system slot of each tile (< kMaxSysPerBlock)
     __shared__ Deps deps;
     __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
     __shared__ int s_cnt[2];
@@ -1926,7 +1926,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_halo_kernel(CGArgs a)
     __shared__ double red[128];
     __shared__ SysLocal sl[kMaxSysPerBlock];
     __shared__ int nsl;
-    __shared__ int tslot[kMaxTilesPerBlock];
+    __shared__ unsigned char tslot[kMaxTilesPerBlock];   // local system slot of each tile (< kMaxSysPerBlock)
     __shared__ Deps deps;
     __shared__ int s_nact, s_anyru;
     __shared__ int s_cnt[2];

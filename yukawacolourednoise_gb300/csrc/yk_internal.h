@@ -19,7 +19,7 @@ constexpr int kBlock = 256;   // threads per block of the site kernels
 constexpr int kTile = 256;    // lattice sites per tile (one per thread)
 constexpr int kMaxFFT = 4096; // longest FFT edge handled in shared memory
 constexpr int kMaxDFT = 256;  // longest non-power-of-two edge (direct DFT)
-constexpr int kMaxTilesPerBlock = 512;   // tiles one CG block may own
+constexpr int kMaxTilesPerBlock = 4096;  // tiles one CG block may own
 constexpr int kMaxGrid = 2048;           // blocks of a CG launch (neighbour flags allocated)
 constexpr int kFlagStride = 32;          // one 128-byte line per neighbour flag
 
