@@ -314,7 +314,33 @@ def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8
                      "cg_iterations_per_system_step": round(its / (steps * n_chains * n_rhs), 1),
                      "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
         ctx.close()
+    # learned: chain 0's 2-layer network trained at its field, its weights
+    # copied to every chain (same couplings; the features adapt to each field)
+    ctx = yk.Context([params(yk.YK_MIXED, c) for c in range(n_chains)])
+    ctx.set_stream(stream.cuda_stream)
+    for c in range(n_chains):
+        ctx.net_setup(2, 7, chain=c)
+    st = ctx.net_train(n_sources=4, n_levels=5, base_iter=4, steps=400, batch=4, lr=2e-3, seed=3)
+    w = ctx.net_get_weights()
+    for c in range(1, n_chains):
+        ctx.net_set_weights(w, chain=c)
+    ctx.step_learned(warmup)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = ctx.step_learned(steps)
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    out["learned_2layers"] = {"value": round(steps / sec, 4), "unit": "steps/s (all chains)",
+                              "chain_steps_per_s": round(steps * n_chains / sec, 3),
+                              "solver_iterations_per_system_step": round(s.iterations / (steps * n_chains * n_rhs), 1),
+                              "all_converged": bool(s.converged),
+                              "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4),
+                                           "loss_after": round(st.loss1, 4), "ms": round(st.ms, 1)}}
+    ctx.close()
     out["speedup_mixed_over_fp64"] = round(out["mixed_cg"]["value"] / out["plain_fp64"]["value"], 3)
+    out["speedup_learned_over_fp64"] = round(out["learned_2layers"]["value"] / out["plain_fp64"]["value"], 3)
+    out["speedup_learned_over_mixed"] = round(out["learned_2layers"]["value"] / out["mixed_cg"]["value"], 3)
     return out
 
 
