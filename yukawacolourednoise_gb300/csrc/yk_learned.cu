@@ -519,7 +519,6 @@ struct LearnedNet {
     int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
     int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
     bool tc_tuned = false;            // tile chosen by timing (first solve)
-    unsigned* dcnt = nullptr;         // arrival counters of the preconditioned CG's reductions
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
     float* diag32 = nullptr;          // FP32 diagonal 2 r + m0 + g sigma of the current solve
     uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
@@ -545,7 +544,6 @@ struct LearnedNet {
     float* Zs = nullptr;              // restart x 4V: preconditioned directions
     float* Ws = nullptr;              // restart x 4V: their images under A
     int restart = 0;
-    double* dsc = nullptr;            // device scalars of the preconditioned CG
     PcgGraph* pcg = nullptr;          // its captured chunk of iterations
     bool pcg_no_graph = false;        // capture failed once (e.g. the legacy stream)
 };
@@ -625,12 +623,11 @@ void net_destroy(LearnedNet* n)
                    n->f0, n->f1, n->f2, n->f3, n->Zs, n->Ws, n->sig32, n->diag32};
     for (float* p : fs)
         if (p) cudaFree(p);
-    double* ds[] = {n->dpart, n->d0, n->d1, n->d2, n->dsc};
+    double* ds[] = {n->dpart, n->d0, n->d1, n->d2};
     for (double* p : ds)
         if (p) cudaFree(p);
     if (n->hpart) cudaFreeHost(n->hpart);
     pcg_graph_destroy(n->pcg);
-    if (n->dcnt) cudaFree(n->dcnt);
     for (uint4* h : n->h16)
         if (h) cudaFree(h);
     delete n;
@@ -680,12 +677,10 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e == cudaSuccess) e = alloc_f(&n->z, 4 * V);
     if (e == cudaSuccess) e = alloc_f(&n->part, (size_t)n->nblk * 9 * kNetC * kNetC);
     if (e == cudaSuccess) e = alloc_d(&n->dpart, n->grid);
-    if (e == cudaSuccess) e = cudaMalloc(&n->dcnt, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = alloc_f(&n->sig32, V);
     if (e == cudaSuccess) e = alloc_f(&n->diag32, V);
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[0], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[1], sizeof(uint4) * V);
-    if (e == cudaSuccess) e = cudaMemset(n->dcnt, 0, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * n->grid);
     if (e == cudaSuccess) n->hpart_cap = (size_t)n->grid;
     if (e == cudaSuccess) e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
@@ -1210,40 +1205,6 @@ namespace yk {
 namespace {
 
 constexpr int kPcgChunk = 8;
-// device scalars
-enum { kRZ = 0, kPQ = 1, kRR = 2, kAlpha = 3, kBeta = 4, kZQ = 5 };
-
-// Arrival of a block at the end of a reduction kernel (thread 0 has written
-// the block's partials): true in the block that arrives last, which then sees
-// every block's partials and resets the counter for the next launch.
-__device__ __forceinline__ bool last_arrival(unsigned* counter)
-{
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(counter, 1u) == gridDim.x - 1;
-        if (last) *counter = 0u;
-    }
-    __syncthreads();
-    if (last) __threadfence();
-    return last;
-}
-
-// sum of nb <= 16 * blockDim.x partials (fixed order: the result does not
-// depend on timing; the loads are issued together)
-__device__ __forceinline__ double sum_partials(const double* part, int nb, double* red)
-{
-    double w[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const int i = threadIdx.x + j * blockDim.x;
-        w[j] = i < nb ? __ldcg(part + i) : 0.0;
-    }
-    double v = 0.0;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) v += w[j];
-    return block_sum(v, red);
-}
 
 // Block sums of NV FP32 values: FP32 within a warp (32 terms), FP64 across
 // warps (GB300's FP64 pipe is narrow: per-site FP64 work would bound these
@@ -1272,15 +1233,61 @@ __device__ __forceinline__ void block_sum_f(float (&v)[NV], double (&out)[NV], d
     }
 }
 
+// The totals of two arrays of nb per-block FP32 partials, in every thread
+// of the block: FP32 sums in a fixed order (so every block computes the same
+// scalar bits; the FP64 pipe is kept out of the iteration), the loads of a
+// chunk of 8 per thread issued together.
+__device__ __forceinline__ float2 block_totals(const float* a, const float* b, int nb)
+{
+    __shared__ float2 wsum[32];
+    __shared__ float2 tot;
+    float sa = 0.f, sb = 0.f;
+    for (int base = 0; base < nb; base += 8 * blockDim.x) {
+        float wa[8], wb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int i = base + threadIdx.x + j * blockDim.x;
+            wa[j] = i < nb ? __ldcg(a + i) : 0.f;
+            wb[j] = i < nb ? __ldcg(b + i) : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            sa += wa[j];
+            sb += wb[j];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sa += __shfl_xor_sync(0xffffffffu, sa, o);
+        sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) wsum[w] = make_float2(sa, sb);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float2 t = make_float2(0.f, 0.f);
+        for (int i = 0; i < nw; ++i) {
+            t.x += wsum[i].x;
+            t.y += wsum[i].y;
+        }
+        tot = t;
+    }
+    __syncthreads();
+    return tot;
+}
+
 // x += alpha p, r -= alpha q; with X != null also the network's BF16
 // features (r, sigma r) of the new r
+// alpha = <r, z> / <p, q> from the z kernel's and the q kernel's partials
 __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
                                                              const float* __restrict__ p, const float* __restrict__ q,
-                                                             const double* __restrict__ sc,
+                                                             const float* __restrict__ part_rz,
+                                                             const float* __restrict__ part_pq, int nb,
                                                              const float* __restrict__ sigma, uint4* __restrict__ X,
                                                              int V)
 {
-    const float a = (float)sc[kAlpha];
+    const float2 t = block_totals(part_rz, part_pq, nb);
+    const float a = t.y != 0.f ? t.x / t.y : 0.f;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         float4 xv = reinterpret_cast<float4*>(x)[n], rv = reinterpret_cast<float4*>(r)[n];
         const float4 pv = reinterpret_cast<const float4*>(p)[n], qv = reinterpret_cast<const float4*>(q)[n];
@@ -1299,15 +1306,14 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
 }
 
 // z = F^T a + skip r (a != null: the network's last transposed layer) or
-// z = r (a == null), with <r, z>, <r, r> and <z, q> (q may be null; FP32
-// products of a site, FP64 across sites).  The last block sets rz, rr and
-// beta = -alpha <z, q> / <r, z>_old (first: the round's first z, beta = 0).
+// z = r (a == null), with the per-block partials of <r, z>, <r, r> and
+// <z, q> (q null: 0) in part[0..nb), part[nb..2nb), part[2nb..3nb) (FP32
+// products of a site, FP64 across warps, stored in FP32).
 __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restrict__ a,
                                                             const float* __restrict__ sigma,
                                                             const float* __restrict__ r, float skip,
                                                             float* __restrict__ z, const float* __restrict__ q,
-                                                            double* __restrict__ part, unsigned* counter,
-                                                            double* __restrict__ sc, int first, int V)
+                                                            float* __restrict__ part, int V)
 {
     __shared__ double red[96];
     float acc[3] = {0.f, 0.f, 0.f};
@@ -1326,24 +1332,9 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
     block_sum_f<3>(acc, tot, red);
     const int nb = gridDim.x;
     if (threadIdx.x == 0) {
-        part[blockIdx.x] = tot[0];
-        part[nb + blockIdx.x] = tot[1];
-        part[2 * nb + blockIdx.x] = tot[2];
-    }
-    if (!last_arrival(counter)) return;
-    const double rz = sum_partials(part, nb, red);
-    const double rr = sum_partials(part + nb, nb, red);
-    const double zq = sum_partials(part + 2 * nb, nb, red);
-    if (threadIdx.x == 0) {
-        if (!first) {
-            const double rz_old = sc[kRZ];
-            sc[kZQ] = zq;
-            sc[kBeta] = rz_old != 0.0 ? -sc[kAlpha] * zq / rz_old : 0.0;
-        } else {
-            sc[kBeta] = 0.0;
-        }
-        sc[kRZ] = rz;
-        sc[kRR] = rr;
+        part[blockIdx.x] = (float)tot[0];
+        part[nb + blockIdx.x] = (float)tot[1];
+        part[2 * nb + blockIdx.x] = (float)tot[2];
     }
 }
 
@@ -1359,12 +1350,18 @@ __global__ void diag_f_kernel(const double* __restrict__ sigma, float* __restric
 // p' = z + beta p (written at the own site), and t = D p' with the
 // neighbours' p' formed on the fly from z and p (p' goes to the other
 // buffer: a neighbour may still read p)
+// beta = -<z', q> / <p, q> (the Polak-Ribiere beta, -alpha <z', q> / <r, z>
+// with alpha = <r, z> / <p, q>) from the partials; 0 when <p, q> = 0 (the
+// round's first direction: the q partials are zeroed)
 __global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __restrict__ z,
                                                              const float* __restrict__ p, float* __restrict__ p_new,
                                                              float* __restrict__ t, const float* __restrict__ diag,
-                                                             const double* __restrict__ sc, int Nt, int Nx, float rw)
+                                                             const float* __restrict__ part_zq,
+                                                             const float* __restrict__ part_pq, int nb, int Nt,
+                                                             int Nx, float rw)
 {
-    const float b = (float)sc[kBeta];
+    const float2 tt = block_totals(part_zq, part_pq, nb);
+    const float b = tt.y != 0.f ? -tt.x / tt.y : 0.f;
     const int V = Nt * Nx;
     auto pn = [&](int m) {
         const Site<float, 1> zz = load_site<float, 1>(z, m), pp = load_site<float, 1>(p, m);
@@ -1382,13 +1379,12 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __rest
     }
 }
 
-// q = D^dag t and <p, q> (FP32 per site, FP64 across warps); the last block
-// sets pq and alpha = <r, z> / <p, q>
+// q = D^dag t and the per-block partials of <p, q> (FP32 per site, FP64
+// across warps)
 __global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __restrict__ t,
                                                              const float* __restrict__ p, float* __restrict__ q,
                                                              const float* __restrict__ diag,
-                                                             double* __restrict__ part, unsigned* counter,
-                                                             double* __restrict__ sc, int Nt, int Nx, float rw)
+                                                             float* __restrict__ part, int Nt, int Nx, float rw)
 {
     __shared__ double red[32];
     const int V = Nt * Nx;
@@ -1404,18 +1400,13 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __rest
     }
     double tot[1];
     block_sum_f<1>(acc, tot, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
-    if (!last_arrival(counter)) return;
-    const double pq = sum_partials(part, gridDim.x, red);
-    if (threadIdx.x == 0) {
-        sc[kPQ] = pq;
-        sc[kAlpha] = pq != 0.0 ? sc[kRZ] / pq : 0.0;
-    }
+    if (threadIdx.x == 0) part[blockIdx.x] = (float)tot[0];
 }
 
 struct PcgBufs {
     float *r, *x, *z, *p[2], *q, *tmp;
-    double* sc;
+    float* part_z;    // 3 x grid FP32 partials of the z kernel: <r, z>, <r, r>, <z, q>
+    float* part_pq;   // grid FP32 partials of <p, q>
 };
 
 // z = M r, its partials and the scalars; X: the features (already written
@@ -1428,8 +1419,7 @@ void pcg_precond(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs&
         if (first) net_feat_bf_kernel<<<nb, kNetThreads, 0, s>>>(b.r, n->sig32, n->h16[0], V);
         a = net_convs_fast(n, s);
     }
-    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(a, n->sig32, b.r, n->skip, b.z,
-                                            first ? nullptr : b.q, n->dpart, n->dcnt + 1, b.sc, first ? 1 : 0, V);
+    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(a, n->sig32, b.r, n->skip, b.z, first ? nullptr : b.q, b.part_z, V);
 }
 
 // `count` iterations from the direction buffer `parity`: p' = z + beta p and
@@ -1443,9 +1433,11 @@ int pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBuf
     for (int it = 0; it < count; ++it, parity ^= 1) {
         float* p = b.p[parity];
         float* pn = b.p[parity ^ 1];
-        pcg_dp_kernel<<<nb, kNetThreads, 0, s>>>(b.z, p, pn, b.tmp, n->diag32, b.sc, d.Nt, d.Nx, rw);
-        pcg_dq_kernel<<<nb, kNetThreads, 0, s>>>(b.tmp, pn, b.q, n->diag32, n->dpart, n->dcnt, b.sc, d.Nt, d.Nx, rw);
-        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, pn, b.q, b.sc, n->sig32, use_net ? n->h16[0] : nullptr, V);
+        pcg_dp_kernel<<<nb, kNetThreads, 0, s>>>(b.z, p, pn, b.tmp, n->diag32, b.part_z + 2 * nb, b.part_pq, nb,
+                                                 d.Nt, d.Nx, rw);
+        pcg_dq_kernel<<<nb, kNetThreads, 0, s>>>(b.tmp, pn, b.q, n->diag32, b.part_pq, d.Nt, d.Nx, rw);
+        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, pn, b.q, b.part_z, b.part_pq, nb, n->sig32,
+                                                 use_net ? n->h16[0] : nullptr, V);
         pcg_precond(n, use_net, d, b, false, s);
     }
     return parity;
@@ -1480,13 +1472,21 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
     cudaError_t e = ensure_scratch(n, 2);   // Zs, Ws: two 4V float vectors each
     if (e == cudaSuccess) e = ensure_parts(n, 4);
     if (e != cudaSuccess) return e;
-    if (!n->dsc) {
-        e = cudaMalloc(&n->dsc, sizeof(double) * 8);
-        if (e != cudaSuccess) return e;
-    }
     double* Ax = n->d1;
     double* r64 = n->d2;
-    const PcgBufs B = {n->f0, n->f1, n->f2, {n->Zs, n->Zs + (size_t)V4}, n->Ws, n->f3, n->dsc};
+    float* fpart = reinterpret_cast<float*>(n->dpart);   // 4 x grid floats in the partials' space
+    const PcgBufs B = {n->f0, n->f1, n->f2, {n->Zs, n->Zs + (size_t)V4}, n->Ws, n->f3, fpart,
+                       fpart + 3 * (size_t)n->grid};
+    // |r|^2 of the inner solve from the z kernel's partials (host sum)
+    auto inner_rr = [&](double* out) -> cudaError_t {
+        float* hf = reinterpret_cast<float*>(n->hpart);
+        cudaError_t ce = cudaMemcpyAsync(hf, B.part_z + n->grid, sizeof(float) * n->grid, cudaMemcpyDeviceToHost, s);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        double t = 0.0;
+        for (int i = 0; i < n->grid; ++i) t += hf[i];
+        *out = t;
+        return ce;
+    };
     f_of_d_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->sig32, n->V);
     diag_f_kernel<<<n->grid, kNetThreads, 0, s>>>(sigma, n->diag32, m0, g, r, n->V);
     const int nb = n->grid;
@@ -1543,14 +1543,14 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
         ++outer;
         dvec_to_f_kernel<<<nb, kNetThreads, 0, s>>>(r64, B.r, V4);
         e = cudaMemsetAsync(B.x, 0, sizeof(float) * V4, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(B.p[0], 0, sizeof(float) * V4, s);   // beta = 0: p' = z
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.p[0], 0, sizeof(float) * V4, s);
+        // zero <p, q> partials: the first direction takes beta = 0, p' = z
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.part_pq, 0, sizeof(float) * nb, s);
         if (e != cudaSuccess) break;
-        pcg_precond(n, use_net, d, B, true, s);   // z = M r, beta = 0
+        pcg_precond(n, use_net, d, B, true, s);   // z = M r
         int parity = 0;
-        double h[8];
-        e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        const double rr0 = h[kRR];
+        double rr0 = 0.0;
+        e = inner_rr(&rr0);
         double rrc = rr0;
         while (e == cudaSuccess && iters < max_iter && rrc > inner_tol * inner_tol * rr0) {
             const int cnt = std::min(kPcgChunk, max_iter - iters);
@@ -1561,9 +1561,7 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
                 e = cudaGetLastError();
             }
             iters += cnt;
-            if (e == cudaSuccess) e = cudaMemcpyAsync(h, B.sc, sizeof(double) * 8, cudaMemcpyDeviceToHost, s);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-            rrc = h[kRR];
+            if (e == cudaSuccess) e = inner_rr(&rrc);
             if (!(rrc == rrc)) break;   // NaN: the FP64 check below decides
         }
         if (e != cudaSuccess) break;
