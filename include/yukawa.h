@@ -285,10 +285,12 @@ typedef struct yk_tune_result {
     float cg_ms_chosen;        /* two timed 48-iteration solves at the chosen grid   */
     float cg_ms_max;           /* the same at the co-resident maximum                */
     int conv_rows, conv_cols;  /* chain 0 network's convolution tile (0: none yet)   */
+    int conv_layers_per_launch; /* its layers per launch (1 .. 2 x layers)           */
 } yk_tune_result;
 int yk_autotune(yk_ctx* ctx, yk_tune_result* out);
-/* (Environment YK_NET_TILE=RxW, e.g. 8x64, fixes the convolution tile
- * instead of timing candidates: for profiling and reproducible timing.) */
+/* (Environment YK_NET_TILE=RxW or RxWxG, e.g. 8x64x4, fixes the convolution
+ * tile and the layers per launch instead of timing candidates: for profiling
+ * and reproducible timing.) */
 /* The last tuning's choices (all zero before any). */
 int yk_tune_report(yk_ctx* ctx, yk_tune_result* out);
 

@@ -70,7 +70,13 @@ def _params(yk, Nt, Nx, m0, precision):
 
 
 @pytest.mark.gpu
-def test_network_forward_and_gradient_match_oracle(ylib, cuda):
+@pytest.mark.parametrize("tile", ["8x64x1", "4x16x4", "2x8x8"], ids=["per_layer", "halves_fused", "all_fused"])
+def test_network_forward_and_gradient_match_oracle(ylib, cuda, monkeypatch, tile):
+    # the solvers' form at three launch shapes: one launch per layer, N and
+    # N^T fused, all eight layers fused (a halo of 8 rows around 2-row tiles
+    # of the 16 x 12 lattice, so staged rows wrap in time, with 8 + 4 column
+    # tiles)
+    monkeypatch.setenv("YK_NET_TILE", tile)
     yk, torch = ylib, cuda
     Nt, Nx = 16, 12
     V = Nt * Nx

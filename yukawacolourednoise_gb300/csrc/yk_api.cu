@@ -651,7 +651,7 @@ int run_autotune(yk_ctx* ctx)
     }
     for (const Chain& C : ctx->ch)
         if (C.net) {
-            net_tile(C.net, &T.conv_rows, &T.conv_cols);
+            net_tile(C.net, &T.conv_rows, &T.conv_cols, &T.conv_layers_per_launch);
             break;
         }
     ctx->tuned = true;
@@ -1644,7 +1644,7 @@ int yk_tune_report(yk_ctx* ctx, yk_tune_result* out)
     *out = ctx->tune;
     for (const Chain& C : ctx->ch)
         if (C.net) {
-            net_tile(C.net, &out->conv_rows, &out->conv_cols);
+            net_tile(C.net, &out->conv_rows, &out->conv_cols, &out->conv_layers_per_launch);
             break;
         }
     return YK_OK;

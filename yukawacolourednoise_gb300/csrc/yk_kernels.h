@@ -90,8 +90,9 @@ struct FgcrResult {
 LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err);
 void net_destroy(LearnedNet* n);
 int net_size(const LearnedNet* n);
-// the convolution tile of the solvers' M (0 x 0 before the first solve tuned it)
-void net_tile(const LearnedNet* n, int* rows, int* cols);
+// the convolution tile of the solvers' M and its layers per launch (zeros
+// before the first solve tuned them)
+void net_tile(const LearnedNet* n, int* rows, int* cols, int* per_launch);
 void net_set_skip(LearnedNet* n, float skip);   // M(r) = skip r + N(r)
 cudaError_t net_weights(LearnedNet* n, float* host, bool set);
 cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, float* z, cudaStream_t s);

@@ -507,6 +507,139 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
     }
 }
 
+// Several layers in one launch.  A block stages its R x W tile with a halo
+// of H sites (H = the layers it runs) and computes layer j on the tile
+// widened by H - 1 - j sites, in shared memory, so that only the last layer
+// writes to global memory.  Time is treated as the antiperiodically extended
+// field: a staged row at virtual time t_v takes the sign (-1)^floor(t_v / Nt)
+// and every tap after that is a plain shift (a convolution commutes with the
+// extension), so rows that wrap more than once are right too.  Each layer's
+// taps, weights and channel counts follow net_conv_bf_kernel.
+constexpr int kFuseMax = 8;   // layers of one fused launch
+constexpr size_t kFusedMaxSmem = 160 * 1024;   // its shared memory (two regions of the widened tile)
+struct FusedLayers {
+    const float* w[kFuseMax];   // weights of each layer
+    int cout[kFuseMax];         // its output channels (8 or 4) in the forward direction
+    int trans[kFuseMax];        // 1: the transposed layer
+    int n;                      // layers in this launch (= the halo H)
+};
+
+__host__ __device__ inline int fused_region(int R, int W, int H) { return (R + 2 * H) * (W + 2 * H); }
+
+__global__ void __launch_bounds__(kNetThreads) net_conv_fused_kernel(const uint4* __restrict__ X,
+                                                                     uint4* __restrict__ Y, FusedLayers L, int Nt,
+                                                                     int Nx, int R, int W)
+{
+    extern __shared__ __align__(16) uint4 fsm[];
+    const int H = L.n;
+    const int cap = fused_region(R, W, H);
+    uint4* bufA = fsm;
+    uint4* bufB = fsm + cap;
+    const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
+    const int tiles_x = (Nx + W - 1) / W;
+    const int t0 = (blockIdx.x / tiles_x) * R, x0 = (blockIdx.x % tiles_x) * W;
+    const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
+    // stage the tile with its halo of H sites (virtual rows carry the
+    // antiperiodic sign; columns wrap periodically)
+    {
+        const int SR = Rt + 2 * H, SC = Wt + 2 * H;
+        for (int lr = threadIdx.x >> 5; lr < SR; lr += kNetThreads / 32) {
+            const int tv = t0 - H + lr;
+            const int k = tv >= 0 ? tv / Nt : -((-tv + Nt - 1) / Nt);   // floor(tv / Nt)
+            const int t = tv - k * Nt;
+            const uint4* src = X + (size_t)t * Nx;
+            for (int lc = lane; lc < SC; lc += 32) {
+                int x = (x0 - H + lc) % Nx;
+                if (x < 0) x += Nx;
+                cp_async16(&bufA[lr * SC + lc], src + x);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        uint32_t* w32 = reinterpret_cast<uint32_t*>(bufA);
+        for (int idx = threadIdx.x; idx < SR * SC * 4; idx += blockDim.x) {
+            const int tv = t0 - H + idx / (SC * 4);
+            const int k = tv >= 0 ? tv / Nt : -((-tv + Nt - 1) / Nt);
+            if (k & 1) w32[idx] ^= 0x80008000u;
+        }
+        __syncthreads();
+    }
+    uint4* in = bufA;
+    uint4* out = bufB;
+    for (int j = 0; j < H; ++j) {
+        const int hin = H - j, hout = H - 1 - j;   // halo of this layer's input and output regions
+        const int SWi = Wt + 2 * hin;              // input row stride (sites)
+        const int RO = Rt + 2 * hout, WO = Wt + 2 * hout;
+        const bool tr = L.trans[j] != 0;
+        const int co = L.cout[j];
+        const float* Wl = L.w[j];
+        uint32_t b0[5], b1[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            float w[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = 2 * p + h;
+                if (k > 8) continue;
+                if (!tr) {
+                    if (g < co) {
+                        w[2 * h] = Wl[(k * kNetC + 2 * c) * co + g];
+                        w[2 * h + 1] = Wl[(k * kNetC + 2 * c + 1) * co + g];
+                    }
+                } else if (2 * c + 1 < co) {
+                    w[2 * h] = Wl[(k * kNetC + g) * co + 2 * c];
+                    w[2 * h + 1] = Wl[(k * kNetC + g) * co + 2 * c + 1];
+                }
+            }
+            b0[p] = pack_bf2(w[0], w[1]);
+            b1[p] = pack_bf2(w[2], w[3]);
+        }
+        // tap word offsets in the input region, in the order of the products
+        int offA[5], offB[5];
+#pragma unroll
+        for (int p = 0; p < 5; ++p) {
+            const int kA = tr ? 8 - 2 * p : 2 * p, kB = tr ? 7 - 2 * p : 2 * p + 1;
+            offA[p] = ((kA / 3 - 1) * SWi + (kA % 3 - 1)) * 4;
+            offB[p] = p < 4 ? ((kB / 3 - 1) * SWi + (kB % 3 - 1)) * 4 : 0;
+        }
+        const uint32_t* inw = reinterpret_cast<const uint32_t*>(in);
+        const bool last = j == H - 1;
+        uint32_t* ow = last ? reinterpret_cast<uint32_t*>(Y) : reinterpret_cast<uint32_t*>(out);
+        const int S = RO * WO;
+        for (int base = (threadIdx.x >> 5) * 16; base < S; base += (blockDim.x >> 5) * 16) {
+            const int i0 = base + g, i1 = base + g + 8;
+            const bool in0 = i0 < S, in1 = i1 < S;
+            const int r0 = in0 ? i0 / WO : 0, c0 = in0 ? i0 - r0 * WO : 0;
+            const int r1 = in1 ? i1 / WO : 0, c1 = in1 ? i1 - r1 * WO : 0;
+            const uint32_t* q0 = inw + ((r0 + 1) * SWi + c0 + 1) * 4 + c;
+            const uint32_t* q1 = inw + ((r1 + 1) * SWi + c1 + 1) * 4 + c;
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int p = 0; p < 5; ++p) {
+                uint32_t a[4];
+                a[0] = q0[offA[p]];
+                a[1] = q1[offA[p]];
+                a[2] = p < 4 ? q0[offB[p]] : 0u;
+                a[3] = p < 4 ? q1[offB[p]] : 0u;
+                mma_bf16(acc, a, b0[p], b1[p]);
+            }
+            if (last) {
+                const int n0 = (t0 + r0) * Nx + x0 + c0, n1 = (t0 + r1) * Nx + x0 + c1;
+                if (in0) ow[(size_t)n0 * 4 + c] = pack_bf2(acc[0], acc[1]);
+                if (in1) ow[(size_t)n1 * 4 + c] = pack_bf2(acc[2], acc[3]);
+            } else {
+                if (in0) ow[(r0 * WO + c0) * 4 + c] = pack_bf2(acc[0], acc[1]);
+                if (in1) ow[(r1 * WO + c1) * 4 + c] = pack_bf2(acc[2], acc[3]);
+            }
+        }
+        __syncthreads();
+        uint4* tmp = in;
+        in = out;
+        out = tmp;
+    }
+}
+
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -518,7 +651,8 @@ void pcg_graph_destroy(PcgGraph* g);
 struct LearnedNet {
     int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
     int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
-    bool tc_tuned = false;            // tile chosen by timing (first solve)
+    int tc_G = 1;                     // layers per launch (1: one launch per layer)
+    bool tc_tuned = false;            // tile chosen by timing (first solve) or by YK_NET_TILE
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
     float* diag32 = nullptr;          // FP32 diagonal 2 r + m0 + g sigma of the current solve
     uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
@@ -635,11 +769,14 @@ void net_destroy(LearnedNet* n)
 
 int net_size(const LearnedNet* n) { return n->nw; }
 
-void net_tile(const LearnedNet* n, int* rows, int* cols)
+void net_tile(const LearnedNet* n, int* rows, int* cols, int* per_launch)
 {
     *rows = n->tc_tuned ? n->tc_R : 0;
     *cols = n->tc_tuned ? n->tc_W : 0;
+    *per_launch = n->tc_tuned ? n->tc_G : 0;
 }
+
+bool net_tile_from_env(LearnedNet* n);
 
 void net_set_skip(LearnedNet* n, float skip) { n->skip = skip; }
 
@@ -663,6 +800,8 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     n->tc_W = std::min(Nx, kTcMaxW);
     n->tc_R = kTcMaxR;
+    cudaFuncSetAttribute((const void*)net_conv_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kFusedMaxSmem);
     while (n->tc_R > 2 && (int64_t)((Nt + n->tc_R - 1) / n->tc_R) * ((Nx + n->tc_W - 1) / n->tc_W) < 2 * n_sm)
         n->tc_R /= 2;
     cudaError_t e = alloc_f(&n->w, n->nw);
@@ -689,6 +828,8 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e != cudaSuccess) {
         net_destroy(n);
         n = nullptr;
+    } else {
+        net_tile_from_env(n);
     }
     *err = e;
     return n;
@@ -744,10 +885,33 @@ float* dec_of(LearnedNet* n, int l) { return n->dec + (size_t)l * kNetC * n->V; 
 
 // N then N^T on the BF16 features in h16[0] (tensor-core convolutions,
 // one block per tile); returns the buffer that holds F^T's input
+size_t fused_smem(int R, int W, int G) { return 2 * sizeof(uint4) * (size_t)fused_region(R, W, G); }
+
 uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
 {
     const int L = n->layers, Nt = n->Nt, Nx = n->Nx, R = n->tc_R, W = n->tc_W;
     const int grid = ((Nt + R - 1) / R) * ((Nx + W - 1) / W);
+    if (n->tc_G > 1) {   // the 2L layers in launches of tc_G
+        FusedLayers seq;
+        int cur = 0;
+        auto flush = [&]() {
+            if (!seq.n) return;
+            net_conv_fused_kernel<<<grid, kNetThreads, fused_smem(R, W, seq.n), s>>>(n->h16[cur], n->h16[cur ^ 1],
+                                                                                      seq, Nt, Nx, R, W);
+            cur ^= 1;
+            seq.n = 0;
+        };
+        seq.n = 0;
+        for (int q = 0; q < 2 * L; ++q) {
+            const int l = q < L ? q : 2 * L - 1 - q;
+            seq.w[seq.n] = n->w + n->woff[l];
+            seq.cout[seq.n] = cout_of(n, l);
+            seq.trans[seq.n] = q >= L ? 1 : 0;
+            if (++seq.n == n->tc_G) flush();
+        }
+        flush();
+        return n->h16[cur];
+    }
     int cur = 0;
     for (int l = 0; l < L; ++l, cur ^= 1) {
         const float* w = n->w + n->woff[l];
@@ -784,41 +948,63 @@ cudaError_t net_forward(LearnedNet* n, const float* r, const double* sigma, floa
 // three timed passes on zeroed activations) at each candidate of 16, 32 or 64
 // columns (at most Nx) and 2, 4 or 8 rows; the default (8 x 64, rows halved
 // while there are fewer than two tiles per SM) is a candidate.
+// YK_NET_TILE=RxW or RxWxG in the environment fixes the tile (R in 1..8,
+// W in 1..64) and the layers per launch (G in 1..8): true if it did
+bool net_tile_from_env(LearnedNet* n)
+{
+    const char* env = getenv("YK_NET_TILE");
+    if (!env) return false;
+    int R = 0, W = 0, G = 1;
+    const int k = sscanf(env, "%dx%dx%d", &R, &W, &G);
+    if (k < 2 || R < 1 || R > kTcMaxR || W < 1 || W > kTcMaxW || G < 1 || G > kFuseMax) return false;
+    if (G > 1 && fused_smem(R, std::min(W, n->Nx), G) > kFusedMaxSmem) return false;
+    n->tc_R = R;
+    n->tc_W = std::min(W, n->Nx);
+    n->tc_G = G;
+    n->tc_tuned = true;
+    return true;
+}
+
+// The convolution tile and the layers per launch, chosen by timing the
+// network's layers (one warm-up, three timed passes on zeroed activations)
+// at each candidate: 16, 32 or 64 columns (at most Nx), 2, 4 or 8 rows, and
+// one launch per layer, per half of the network (N, N^T) or for all 2L
+// layers (when its shared memory fits).
 cudaError_t net_tune_tile(LearnedNet* n, cudaStream_t s)
 {
-    // YK_NET_TILE=RxW in the environment fixes the tile (R in 1..8, W in 1..64)
-    if (const char* env = getenv("YK_NET_TILE")) {
-        int R = 0, W = 0;
-        if (sscanf(env, "%dx%d", &R, &W) == 2 && R >= 1 && R <= kTcMaxR && W >= 1 && W <= kTcMaxW) {
-            n->tc_R = R;
-            n->tc_W = std::min(W, n->Nx);
-            n->tc_tuned = true;
-            return cudaSuccess;
-        }
-    }
+    if (net_tile_from_env(n)) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(n->h16[0], 0, sizeof(uint4) * n->V, s);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    int bestR = n->tc_R, bestW = n->tc_W;
+    int bestR = n->tc_R, bestW = n->tc_W, bestG = 1;
     float best = -1.f;
-    for (int W : {64, 32, 16}) {
-        if (W > n->Nx && W != 64) continue;
-        for (int R : {8, 4, 2}) {
-            if (e != cudaSuccess) break;
-            n->tc_R = R;
-            n->tc_W = std::min(W, n->Nx);
-            net_convs_fast(n, s);
-            e = cudaEventRecord(e0, s);
-            for (int rep = 0; rep < 3; ++rep) net_convs_fast(n, s);
-            if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            if (e == cudaSuccess && (best < 0.f || ms < best)) {
-                best = ms;
-                bestR = n->tc_R;
-                bestW = n->tc_W;
+    const int Gs[3] = {1, n->layers, 2 * n->layers};
+    for (int gi = 0; gi < 3; ++gi) {
+        const int G = Gs[gi];
+        if (G > kFuseMax || (gi > 0 && Gs[gi] == Gs[gi - 1])) continue;
+        for (int W : {64, 32, 16}) {
+            if (W > n->Nx && W != 64) continue;
+            for (int R : {8, 4, 2}) {
+                if (e != cudaSuccess) break;
+                const int Wc = std::min(W, n->Nx);
+                if (G > 1 && fused_smem(R, Wc, G) > kFusedMaxSmem) continue;
+                n->tc_R = R;
+                n->tc_W = Wc;
+                n->tc_G = G;
+                net_convs_fast(n, s);
+                e = cudaEventRecord(e0, s);
+                for (int rep = 0; rep < 3; ++rep) net_convs_fast(n, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e == cudaSuccess && (best < 0.f || ms < best)) {
+                    best = ms;
+                    bestR = n->tc_R;
+                    bestW = n->tc_W;
+                    bestG = n->tc_G;
+                }
             }
         }
     }
@@ -826,6 +1012,7 @@ cudaError_t net_tune_tile(LearnedNet* n, cudaStream_t s)
     if (e1) cudaEventDestroy(e1);
     n->tc_R = bestR;
     n->tc_W = bestW;
+    n->tc_G = bestG;
     n->tc_tuned = e == cudaSuccess;
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
