@@ -892,7 +892,7 @@ uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
     const int L = n->layers, Nt = n->Nt, Nx = n->Nx, R = n->tc_R, W = n->tc_W;
     const int grid = ((Nt + R - 1) / R) * ((Nx + W - 1) / W);
     if (n->tc_G > 1) {   // the 2L layers in launches of tc_G
-        FusedLayers seq;
+        FusedLayers seq = {};
         int cur = 0;
         auto flush = [&]() {
             if (!seq.n) return;
@@ -901,7 +901,6 @@ uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
             cur ^= 1;
             seq.n = 0;
         };
-        seq.n = 0;
         for (int q = 0; q < 2 * L; ++q) {
             const int l = q < L ? q : 2 * L - 1 - q;
             seq.w[seq.n] = n->w + n->woff[l];
