@@ -121,6 +121,37 @@ def energy_loss_and_grad(Ws, r, e, sigma, Nt, Nx, act, skip=0.0):
     return float(np.sum(Dd * Dd)), grad_M(Ws, acts, decs, gz, sigma, Nt, Nx)
 
 
+def flexible_pcg(apply_A, apply_M, b, tol, max_iter, polak_ribiere=True):
+    """Preconditioned CG on A x = b (x0 = 0) with the preconditioner M, the
+    recurrence of csrc/yk_learned.cu (pcg_dp_kernel, pcg_dq_kernel,
+    pcg_xr_kernel, pcg_z_kernel) in FP64: alpha = <r, z> / <p, q>; beta =
+    -<z', q> / <p, q> (Polak-Ribiere, polak_ribiere=True) or <r', z'> / <r, z>
+    (classical).  Returns x, iterations, the |r|^2 history."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = apply_M(r)
+    p = np.zeros_like(b)
+    beta = 0.0
+    rz = float(np.sum(r * z))
+    hist = [float(np.sum(r * r))]
+    stop2 = tol * tol * hist[0]
+    it = 0
+    while hist[-1] > stop2 and it < max_iter:
+        p = z + beta * p
+        q = apply_A(p)
+        pq = float(np.sum(p * q))
+        alpha = rz / pq
+        x = x + alpha * p
+        r = r - alpha * q
+        z = apply_M(r)
+        rz_new = float(np.sum(r * z))
+        beta = -float(np.sum(z * q)) / pq if polak_ribiere else rz_new / rz
+        rz = rz_new
+        hist.append(float(np.sum(r * r)))
+        it += 1
+    return x, it, hist
+
+
 def init_weights(hidden, layers, seed):
     """Deterministic small initial weights (the tests pass them to the GPU)."""
     rng = np.random.default_rng(seed)

@@ -62,6 +62,32 @@ def test_oracle_gradients_match_finite_differences(kind):
     assert worst < 1e-6, worst
 
 
+def test_oracle_flexible_pcg_recurrence():
+    # the solver's recurrence with the (untrained) network as M on an 8 x 6
+    # lattice near the chiral regime: the Polak-Ribiere beta -<z', q>/<p, q>
+    # takes the same steps as the classical <r', z'>/<r, z> for a fixed SPD M
+    # and converges to 1e-10; with zero weights (M = skip I) it is plain CG
+    Nt, Nx = 8, 6
+    rng = np.random.default_rng(3)
+    a = _action(0.02)
+    sig = rng.uniform(-1, 1, Nt * Nx)
+    Ws = N.init_weights(8, 2, 5)
+    skip = 1.0 / (4 + 0.02 + 2) ** 2
+    A = lambda v: N.dirac_real(Nt, Nx, a, sig, N.dirac_real(Nt, Nx, a, sig, v, False), True)
+    M = lambda v: N.apply_M(Ws, v, sig, Nt, Nx, skip)[0]
+    b = rng.normal(size=(4, Nt * Nx))
+    x_pr, it_pr, h_pr = N.flexible_pcg(A, M, b, 1e-10, 2000)
+    x_cl, it_cl, h_cl = N.flexible_pcg(A, M, b, 1e-10, 2000, polak_ribiere=False)
+    assert np.linalg.norm(A(x_pr) - b) < 1e-9 * np.linalg.norm(b)
+    n = min(len(h_pr), len(h_cl), 20)
+    assert np.allclose(h_pr[:n], h_cl[:n], rtol=1e-6, atol=0)
+    assert abs(it_pr - it_cl) <= 2
+    _, it_id, h_id = N.flexible_pcg(A, lambda v: v, b, 1e-10, 2000)
+    Z = [np.zeros_like(w) for w in Ws]
+    _, it_z, h_z = N.flexible_pcg(A, lambda v: N.apply_M(Z, v, sig, Nt, Nx, skip)[0], b, 1e-10, 2000)
+    assert abs(it_z - it_id) <= 1 and np.allclose(h_z[:20], h_id[:20], rtol=1e-8, atol=0)
+
+
 def _params(yk, Nt, Nx, m0, precision):
     return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=m0, wilson_param=1.0,
                              cut_fraction=0.35355339059327373, Nt=Nt, Nx=Nx, cg_tol=1e-10,
