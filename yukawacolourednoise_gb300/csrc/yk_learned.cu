@@ -354,6 +354,16 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Programmatic dependent launch: the kernels of a PCG iteration are launched
+// with programmatic stream serialisation, so a kernel's launch and its
+// independent prologue overlap the previous kernel's tail.  pdl_wait() comes
+// before the first access to memory an earlier kernel of the chain reads or
+// writes (it returns once that kernel has completed and its writes are
+// visible; without a programmatic dependency it returns at once);
+// pdl_trigger() after a block's main work lets the next kernel launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
 {
     const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -391,8 +401,10 @@ __global__ void __launch_bounds__(kNetThreads) net_feat_bf_kernel(const float* _
                                                                   const float* __restrict__ sigma,
                                                                   uint4* __restrict__ X, int V)
 {
+    pdl_wait();
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x)
         X[n] = features_bf(reinterpret_cast<const float4*>(r)[n], sigma[n]);
+    pdl_trigger();
 }
 
 // F^T a + skip r for the BF16 site-major a
@@ -426,19 +438,6 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
     const int tiles_x = (Nx + W - 1) / W;
     const int t0 = (blockIdx.x / tiles_x) * R, x0 = (blockIdx.x % tiles_x) * W;
     const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
-    // stage the tile and its halo: warp w takes the staged rows w, w + 8
-    for (int lr = threadIdx.x >> 5; lr < Rt + 2; lr += kNetThreads / 32) {
-        int t = t0 - 1 + lr;
-        if (t < 0) t += Nt;
-        else if (t >= Nt) t -= Nt;
-        const uint4* src = X + (size_t)t * Nx;
-        for (int lc = lane; lc < Wt + 2; lc += 32) {
-            int x = x0 - 1 + lc;
-            if (x < 0) x += Nx;
-            else if (x >= Nx) x -= Nx;
-            cp_async16(&sm[lr * SW + lc], src + x);
-        }
-    }
     // B fragments of the tap pairs (2p, 2p + 1): K = the pair's 16 inputs, N = 8 outputs
     uint32_t b0[5], b1[5];
 #pragma unroll
@@ -462,6 +461,20 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
         }
         b0[p] = pack_bf2(w[0], w[1]);
         b1[p] = pack_bf2(w[2], w[3]);
+    }
+    pdl_wait();   // the weights above are constant during a solve; X is the previous layer's
+    // stage the tile and its halo: warp w takes the staged rows w, w + 8
+    for (int lr = threadIdx.x >> 5; lr < Rt + 2; lr += kNetThreads / 32) {
+        int t = t0 - 1 + lr;
+        if (t < 0) t += Nt;
+        else if (t >= Nt) t -= Nt;
+        const uint4* src = X + (size_t)t * Nx;
+        for (int lc = lane; lc < Wt + 2; lc += 32) {
+            int x = x0 - 1 + lc;
+            if (x < 0) x += Nx;
+            else if (x >= Nx) x -= Nx;
+            cp_async16(&sm[lr * SW + lc], src + x);
+        }
     }
     cp_async_wait_all();
     __syncthreads();
@@ -505,6 +518,7 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
         if (in0) Yw[(size_t)n0 * 4 + c] = pack_bf2(acc[0], acc[1]);
         if (in1) Yw[(size_t)n1 * 4 + c] = pack_bf2(acc[2], acc[3]);
     }
+    pdl_trigger();
 }
 
 // Several layers in one launch.  A block stages its R x W tile with a halo
@@ -531,6 +545,7 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_fused_kernel(const uint4
                                                                      int Nx, int R, int W)
 {
     extern __shared__ __align__(16) uint4 fsm[];
+    pdl_wait();
     const int H = L.n;
     const int cap = fused_region(R, W, H);
     uint4* bufA = fsm;
@@ -887,6 +902,33 @@ float* dec_of(LearnedNet* n, int l) { return n->dec + (size_t)l * kNetC * n->V; 
 // one block per tile); returns the buffer that holds F^T's input
 size_t fused_smem(int R, int W, int G) { return 2 * sizeof(uint4) * (size_t)fused_region(R, W, G); }
 
+// Launch with programmatic stream serialisation (the kernel calls pdl_wait()
+// before touching its inputs); YK_PDL=0 in the environment: plain launches.
+bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("YK_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+template <typename... K, typename... A>
+void launch_pdl(void (*kern)(K...), int grid, size_t smem, cudaStream_t s, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kNetThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, static_cast<K>(args)...);
+}
+
 uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
 {
     const int L = n->layers, Nt = n->Nt, Nx = n->Nx, R = n->tc_R, W = n->tc_W;
@@ -896,8 +938,8 @@ uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
         int cur = 0;
         auto flush = [&]() {
             if (!seq.n) return;
-            net_conv_fused_kernel<<<grid, kNetThreads, fused_smem(R, W, seq.n), s>>>(n->h16[cur], n->h16[cur ^ 1],
-                                                                                      seq, Nt, Nx, R, W);
+            launch_pdl(net_conv_fused_kernel, grid, fused_smem(R, W, seq.n), s, (const uint4*)n->h16[cur],
+                       n->h16[cur ^ 1], seq, Nt, Nx, R, W);
             cur ^= 1;
             seq.n = 0;
         };
@@ -914,17 +956,13 @@ uint4* net_convs_fast(LearnedNet* n, cudaStream_t s)
     int cur = 0;
     for (int l = 0; l < L; ++l, cur ^= 1) {
         const float* w = n->w + n->woff[l];
-        if (cout_of(n, l) == kNetOut)
-            net_conv_bf_kernel<kNetOut, false><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
-        else
-            net_conv_bf_kernel<kNetC, false><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
+        launch_pdl(cout_of(n, l) == kNetOut ? net_conv_bf_kernel<kNetOut, false> : net_conv_bf_kernel<kNetC, false>,
+                   grid, 0, s, (const uint4*)n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
     }
     for (int l = L - 1; l >= 0; --l, cur ^= 1) {
         const float* w = n->w + n->woff[l];
-        if (cout_of(n, l) == kNetOut)
-            net_conv_bf_kernel<kNetOut, true><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
-        else
-            net_conv_bf_kernel<kNetC, true><<<grid, kNetThreads, 0, s>>>(n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
+        launch_pdl(cout_of(n, l) == kNetOut ? net_conv_bf_kernel<kNetOut, true> : net_conv_bf_kernel<kNetC, true>,
+                   grid, 0, s, (const uint4*)n->h16[cur], n->h16[cur ^ 1], w, Nt, Nx, R, W);
     }
     return n->h16[cur];
 }
@@ -1472,6 +1510,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
                                                              const float* __restrict__ sigma, uint4* __restrict__ X,
                                                              int V)
 {
+    pdl_wait();
     const float2 t = block_totals(part_rz, part_pq, nb);
     const float a = t.y != 0.f ? t.x / t.y : 0.f;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
@@ -1489,6 +1528,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
         reinterpret_cast<float4*>(r)[n] = rv;
         if (X) X[n] = features_bf(rv, sigma[n]);
     }
+    pdl_trigger();
 }
 
 // z = F^T a + skip r (a != null: the network's last transposed layer) or
@@ -1502,6 +1542,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
                                                             float* __restrict__ part, int V)
 {
     __shared__ double red[96];
+    pdl_wait();
     float acc[3] = {0.f, 0.f, 0.f};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         const float4 rv = reinterpret_cast<const float4*>(r)[n];
@@ -1514,6 +1555,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
             acc[2] += fmaf(o.x, qv.x, fmaf(o.y, qv.y, fmaf(o.z, qv.z, o.w * qv.w)));
         }
     }
+    pdl_trigger();
     double tot[3];
     block_sum_f<3>(acc, tot, red);
     const int nb = gridDim.x;
@@ -1546,6 +1588,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __rest
                                                              const float* __restrict__ part_pq, int nb, int Nt,
                                                              int Nx, float rw)
 {
+    pdl_wait();
     const float2 tt = block_totals(part_zq, part_pq, nb);
     const float b = tt.y != 0.f ? -tt.x / tt.y : 0.f;
     const int V = Nt * Nx;
@@ -1563,6 +1606,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __rest
         store_site<float, 1>(t, n, dirac_combine<float, 1, false>(c, tu, td, xu, xd, diag[n], rw, (float)nb.sp,
                                                                   (float)nb.sm));
     }
+    pdl_trigger();
 }
 
 // q = D^dag t and the per-block partials of <p, q> (FP32 per site, FP64
@@ -1574,6 +1618,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __rest
 {
     __shared__ double red[32];
     const int V = Nt * Nx;
+    pdl_wait();
     float acc[1] = {0.f};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         const Nbr nb = neighbours(n, Nt, Nx);
@@ -1584,6 +1629,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __rest
         const Site<float, 1> pv = load_site<float, 1>(p, n);
         acc[0] += fmaf(pv.v[0], o.v[0], fmaf(pv.v[1], o.v[1], fmaf(pv.v[2], o.v[2], pv.v[3] * o.v[3])));
     }
+    pdl_trigger();
     double tot[1];
     block_sum_f<1>(acc, tot, red);
     if (threadIdx.x == 0) part[blockIdx.x] = (float)tot[0];
@@ -1602,10 +1648,11 @@ void pcg_precond(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBufs&
     const int V = n->V, nb = n->grid;
     const uint4* a = nullptr;
     if (use_net) {
-        if (first) net_feat_bf_kernel<<<nb, kNetThreads, 0, s>>>(b.r, n->sig32, n->h16[0], V);
+        if (first) launch_pdl(net_feat_bf_kernel, nb, 0, s, (const float*)b.r, (const float*)n->sig32, n->h16[0], V);
         a = net_convs_fast(n, s);
     }
-    pcg_z_kernel<<<nb, kNetThreads, 0, s>>>(a, n->sig32, b.r, n->skip, b.z, first ? nullptr : b.q, b.part_z, V);
+    launch_pdl(pcg_z_kernel, nb, 0, s, a, (const float*)n->sig32, (const float*)b.r, n->skip, b.z,
+               (const float*)(first ? nullptr : b.q), b.part_z, V);
 }
 
 // `count` iterations from the direction buffer `parity`: p' = z + beta p and
@@ -1619,11 +1666,12 @@ int pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBuf
     for (int it = 0; it < count; ++it, parity ^= 1) {
         float* p = b.p[parity];
         float* pn = b.p[parity ^ 1];
-        pcg_dp_kernel<<<nb, kNetThreads, 0, s>>>(b.z, p, pn, b.tmp, n->diag32, b.part_z + 2 * nb, b.part_pq, nb,
-                                                 d.Nt, d.Nx, rw);
-        pcg_dq_kernel<<<nb, kNetThreads, 0, s>>>(b.tmp, pn, b.q, n->diag32, b.part_pq, d.Nt, d.Nx, rw);
-        pcg_xr_kernel<<<nb, kNetThreads, 0, s>>>(b.x, b.r, pn, b.q, b.part_z, b.part_pq, nb, n->sig32,
-                                                 use_net ? n->h16[0] : nullptr, V);
+        launch_pdl(pcg_dp_kernel, nb, 0, s, (const float*)b.z, (const float*)p, pn, b.tmp, (const float*)n->diag32,
+                   (const float*)(b.part_z + 2 * nb), (const float*)b.part_pq, nb, d.Nt, d.Nx, rw);
+        launch_pdl(pcg_dq_kernel, nb, 0, s, (const float*)b.tmp, (const float*)pn, b.q, (const float*)n->diag32,
+                   b.part_pq, d.Nt, d.Nx, rw);
+        launch_pdl(pcg_xr_kernel, nb, 0, s, b.x, b.r, (const float*)pn, (const float*)b.q, (const float*)b.part_z,
+                   (const float*)b.part_pq, nb, (const float*)n->sig32, use_net ? n->h16[0] : nullptr, V);
         pcg_precond(n, use_net, d, b, false, s);
     }
     return parity;
