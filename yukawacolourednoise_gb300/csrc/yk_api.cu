@@ -1428,6 +1428,20 @@ int yk_set_step(yk_ctx* ctx, int c, int64_t step)
 
 // ---- learned preconditioner ----
 
+// Relative residual reduction of each inner FP32 solve of the preconditioned
+// CG before its FP64 refinement round: 1e-5 (two rounds reach 1e-10; at
+// 512^2, m0 = 0.02 it measured fastest among 1e-4, 1e-5, 3e-6 and 1e-6), or
+// YK_PCG_INNER in the environment
+static double pcg_inner_tol()
+{
+    static const double t = [] {
+        const char* e = getenv("YK_PCG_INNER");
+        const double v = e ? atof(e) : 0.0;
+        return v > 0.0 && v < 1.0 ? v : 1e-5;
+    }();
+    return t;
+}
+
 static int net_ok(yk_ctx* ctx, int c)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
@@ -1686,7 +1700,7 @@ int yk_langevin_step_learned(yk_ctx* ctx, int n_steps, int use_net, yk_solve_sta
                 const SysDev& S = sys[C.sys0 + j];
                 FgcrResult r = {};
                 YK_CK(pcg_solve(net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, S.b, S.x, ctx->tol, ctx->tol_mode,
-                                ctx->max_iter, 1e-4, ctx->stream, &r));
+                                ctx->max_iter, pcg_inner_tol(), ctx->stream, &r));
                 CGState& q = st[C.sys0 + j];
                 std::memset(&q, 0, sizeof(q));
                 q.rr = r.rr;
@@ -1725,7 +1739,7 @@ int yk_pcg_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, int
     }
     Chain& C = ctx->ch[c];
     FgcrResult r = {};
-    YK_CK(pcg_solve(C.net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, b, x, tol, tol_mode, max_iter, 1e-4,
+    YK_CK(pcg_solve(C.net, use_net != 0, C.phi, C.a.m0, C.a.g, C.a.r, b, x, tol, tol_mode, max_iter, pcg_inner_tol(),
                     ctx->stream, &r));
     YK_CK(cudaStreamSynchronize(ctx->stream));
     if (stats) *stats = yk_solve_stats{r.iterations, r.outer, r.rr, r.rr0, r.converged};
