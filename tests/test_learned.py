@@ -176,6 +176,31 @@ def test_trained_network_cuts_iterations(ylib, cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tile", ["8x64x1", "4x16x2", "2x8x4"])
+def test_learned_step_odd_lattice(ylib, cuda, monkeypatch, tile):
+    # a 41 x 25 lattice (odd in both directions: ragged tiles in rows and
+    # columns, a last tile row of one time slice) at three launch shapes of
+    # the 2-layer network: two learned steps agree with the FP64 CG step
+    monkeypatch.setenv("YK_NET_TILE", tile)
+    yk = ylib
+    Nt, Nx = 41, 25
+    fields = []
+    for learned in (False, True):
+        with yk.Context(_params(yk, Nt, Nx, 0.05, yk.YK_FP64)) as ctx:
+            if learned:
+                ctx.net_setup(2, 7)
+                ctx.net_train(n_sources=2, n_levels=3, base_iter=4, steps=60, batch=2, lr=2e-3, seed=3)
+                st = ctx.step_learned(2)
+                assert st.converged == 1
+            else:
+                ctx.step(2)
+            assert ctx.observables().status == 0
+            fields.append(ctx.get_field())
+    err = np.abs(fields[1] - fields[0]).max() / np.abs(fields[0]).max()
+    assert err < 1e-8, err
+
+
+@pytest.mark.gpu
 def test_learned_step_matches_cg_step(ylib, cuda):
     # the same Langevin steps with every fermion solve by the learned PCG
     # (network and identity) and by the step graph's FP64 CG: the fields agree
