@@ -446,6 +446,7 @@ def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_count
             "all_converged": bool(s.converged),
             "conv_tile_rows_cols": [tile.conv_rows, tile.conv_cols],
             "conv_layers_per_launch": tile.conv_layers_per_launch,
+            "pcg_inner_tol": tile.pcg_inner_tol,
             "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4), "loss_after": round(st.loss1, 4),
                          "ms": round(st.ms, 1)},
             "speedup_over_plain_fp64": round((steps / sec) / arms["plain_fp64"]["value"], 3),

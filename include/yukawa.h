@@ -286,6 +286,7 @@ typedef struct yk_tune_result {
     float cg_ms_max;           /* the same at the co-resident maximum                */
     int conv_rows, conv_cols;  /* chain 0 network's convolution tile (0: none yet)   */
     int conv_layers_per_launch; /* its layers per launch (1 .. 2 x layers)           */
+    double pcg_inner_tol;      /* its PCG's inner tolerance, chosen by timing (0: undecided) */
 } yk_tune_result;
 int yk_autotune(yk_ctx* ctx, yk_tune_result* out);
 /* (Environment YK_NET_TILE=RxW or RxWxG, e.g. 8x64x4, fixes the convolution

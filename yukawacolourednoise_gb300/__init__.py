@@ -102,7 +102,7 @@ class SolveStats(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("cg_grid", C.c_int), ("cg_grid_max", C.c_int), ("cg_candidates", C.c_int),
                 ("cg_ms_chosen", C.c_float), ("cg_ms_max", C.c_float), ("conv_rows", C.c_int),
-                ("conv_cols", C.c_int), ("conv_layers_per_launch", C.c_int)]
+                ("conv_cols", C.c_int), ("conv_layers_per_launch", C.c_int), ("pcg_inner_tol", C.c_double)]
 
 
 class NetTrainCfg(C.Structure):

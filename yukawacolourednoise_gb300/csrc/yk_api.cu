@@ -652,6 +652,7 @@ int run_autotune(yk_ctx* ctx)
     for (const Chain& C : ctx->ch)
         if (C.net) {
             net_tile(C.net, &T.conv_rows, &T.conv_cols, &T.conv_layers_per_launch);
+            T.pcg_inner_tol = pcg_inner_choice(C.net);
             break;
         }
     ctx->tuned = true;
@@ -1429,15 +1430,15 @@ int yk_set_step(yk_ctx* ctx, int c, int64_t step)
 // ---- learned preconditioner ----
 
 // Relative residual reduction of each inner FP32 solve of the preconditioned
-// CG before its FP64 refinement round: 1e-5 (two rounds reach 1e-10; at
-// 512^2, m0 = 0.02 it measured fastest among 1e-4, 1e-5, 3e-6 and 1e-6), or
-// YK_PCG_INNER in the environment
+// CG before its FP64 refinement round: YK_PCG_INNER in the environment, else
+// 0 (each network times 1e-4 against 1e-5 on its first solves and keeps the
+// faster)
 static double pcg_inner_tol()
 {
     static const double t = [] {
         const char* e = getenv("YK_PCG_INNER");
         const double v = e ? atof(e) : 0.0;
-        return v > 0.0 && v < 1.0 ? v : 1e-5;
+        return v > 0.0 && v < 1.0 ? v : 0.0;
     }();
     return t;
 }
@@ -1659,6 +1660,7 @@ int yk_tune_report(yk_ctx* ctx, yk_tune_result* out)
     for (const Chain& C : ctx->ch)
         if (C.net) {
             net_tile(C.net, &out->conv_rows, &out->conv_cols, &out->conv_layers_per_launch);
+            out->pcg_inner_tol = pcg_inner_choice(C.net);
             break;
         }
     return YK_OK;

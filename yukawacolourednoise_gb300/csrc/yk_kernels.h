@@ -112,7 +112,10 @@ cudaError_t net_train(LearnedNet* n, const NetOp& op, int steps, int batch, floa
 cudaError_t fgcr_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
                        const double* b, double* x, double tol, int tol_mode, int max_iter, int restart,
                        double inner_tol, cudaStream_t s, FgcrResult* res);
-// preconditioned CG (M SPD) with device-side scalars, inside FP64 refinement
+// preconditioned CG (M SPD) with device-side scalars, inside FP64 refinement;
+// inner_tol <= 0: chosen per network by timing 1e-4 against 1e-5
+// (pcg_inner_choice: the choice with the network, 0 while undecided)
+double pcg_inner_choice(const LearnedNet* n);
 cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
                       const double* b, double* x, double tol, int tol_mode, int max_iter, double inner_tol,
                       cudaStream_t s, FgcrResult* res);

@@ -19,6 +19,7 @@
 // Activations are channel-major float arrays [C][V]; the residual and the
 // output are site-major (4 floats per site, the layout of the CG vectors).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -663,11 +664,20 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_fused_kernel(const uint4
 struct PcgGraph;
 void pcg_graph_destroy(PcgGraph* g);
 
+// the inner tolerance of the preconditioned CG under trial: solves counted,
+// milliseconds of the trial solves, the choice (-1: still trying)
+struct InnerChoice {
+    int tried = 0;
+    double ms[2] = {0.0, 0.0};
+    int chosen = -1;
+};
+
 struct LearnedNet {
     int Nt = 0, Nx = 0, V = 0, layers = 0, nw = 0, nblk = 0, grid = 0;
     int tc_R = 8, tc_W = 64;          // tile of the tensor-core convolutions (rows x columns)
     int tc_G = 1;                     // layers per launch (1: one launch per layer)
     bool tc_tuned = false;            // tile chosen by timing (first solve) or by YK_NET_TILE
+    InnerChoice inner[2];             // the PCG's inner tolerance (identity, network), chosen by timing
     float* sig32 = nullptr;           // FP32 copy of the field of the current solve
     float* diag32 = nullptr;          // FP32 diagonal 2 r + m0 + g sigma of the current solve
     uint4* h16[2] = {nullptr, nullptr};   // BF16 site-major activations of the solvers' M (ping-pong)
@@ -853,6 +863,7 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
 cudaError_t net_weights(LearnedNet* n, float* host, bool set)
 {
     if (set) {
+        n->inner[1] = InnerChoice();
         n->adam_t = 0;
         cudaError_t e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
         if (e == cudaSuccess) e = cudaMemset(n->v, 0, sizeof(float) * n->nw);
@@ -1139,6 +1150,7 @@ cudaError_t net_grad_to_host(LearnedNet* n, float* host, cudaStream_t s)
 // one Adam step on the accumulated gradient of `batch` pairs
 cudaError_t net_adam_step(LearnedNet* n, float lr, int batch, cudaStream_t s)
 {
+    n->inner[1] = InnerChoice();   // new weights: the inner tolerance is chosen again
     n->adam_t += 1;
     const float c1 = 1.f / (1.f - powf(0.9f, (float)n->adam_t)), c2 = 1.f / (1.f - powf(0.999f, (float)n->adam_t));
     net_adam_kernel<<<(n->nw + 255) / 256, 256, 0, s>>>(n->w, n->g, n->m, n->v, n->nw, lr, c1, c2, 1.f / batch);
@@ -1697,9 +1709,9 @@ void pcg_graph_destroy(PcgGraph* g)
     delete g;
 }
 
-cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
-                      const double* b, double* x, double tol, int tol_mode, int max_iter, double inner_tol,
-                      cudaStream_t s, FgcrResult* res)
+static cudaError_t pcg_solve_once(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                                  const double* b, double* x, double tol, int tol_mode, int max_iter,
+                                  double inner_tol, cudaStream_t s, FgcrResult* res)
 {
     const int V4 = 4 * n->V;
     const DiracArgs d = {sigma, n->Nt, n->Nx, m0, g, r};
@@ -1786,7 +1798,14 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
         double rr0 = 0.0;
         e = inner_rr(&rr0);
         double rrc = rr0;
+        // Past the looser 1e-4 reduction a round also ends when a chunk
+        // reduces |r|^2 by less than a third of the round's average (in
+        // logarithm): the FP32 recurrence, with the BF16 preconditioner's
+        // rounding, has stagnated and an FP64 restart is cheaper.
+        const double loose2 = 1e-8 * rr0;
+        int chunks = 0;
         while (e == cudaSuccess && iters < max_iter && rrc > inner_tol * inner_tol * rr0) {
+            const double rr_before = rrc;
             const int cnt = std::min(kPcgChunk, max_iter - iters);
             if (G && cnt == kPcgChunk && parity == 0) {
                 e = cudaGraphLaunch(G->exec, s);
@@ -1797,6 +1816,11 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
             iters += cnt;
             if (e == cudaSuccess) e = inner_rr(&rrc);
             if (!(rrc == rrc)) break;   // NaN: the FP64 check below decides
+            ++chunks;
+            if (rrc < loose2 && rrc > 0.0 && rr_before > 0.0) {
+                const double avg = std::log(rr0 / rrc) / chunks, last = std::log(rr_before / rrc);
+                if (last < avg / 3.0) break;
+            }
         }
         if (e != cudaSuccess) break;
         dvec_add_f_kernel<<<nb, kNetThreads, 0, s>>>(x, B.x, V4);
@@ -1812,6 +1836,39 @@ cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m
     res->rr0 = bb;
     res->converged = rr64 <= stop2 ? 1 : 0;
     return e;
+}
+
+// inner_tol > 0: that tolerance.  inner_tol <= 0: chosen by measurement per
+// network and mode (with or without M): after one warm-up solve, solves
+// alternate between 1e-4 (three FP64 rounds to 1e-10) and 1e-5 (two rounds),
+// kInnerTrials of each (consecutive right-hand sides differ: one solve each
+// would be noise), and later solves take the one with the smaller total.  The better one depends on the
+// problem: a hard system (1024^2, m0 = 0.01) converges more slowly in FP32
+// below 1e-4 than a restart costs, an easier one (512^2, m0 = 0.02) the
+// other way round.  New weights start the choice again.
+cudaError_t pcg_solve(LearnedNet* n, bool use_net, const double* sigma, double m0, double g, double r,
+                      const double* b, double* x, double tol, int tol_mode, int max_iter, double inner_tol,
+                      cudaStream_t s, FgcrResult* res)
+{
+    if (inner_tol > 0.0) return pcg_solve_once(n, use_net, sigma, m0, g, r, b, x, tol, tol_mode, max_iter, inner_tol, s, res);
+    static const double kTols[2] = {1e-4, 1e-5};
+    constexpr int kInnerTrials = 3;
+    InnerChoice& ic = n->inner[use_net ? 1 : 0];
+    const int k = ic.chosen >= 0 ? ic.chosen : ic.tried == 0 ? 1 : (ic.tried - 1) % 2;   // warm-up: 1e-5
+    const auto t0 = std::chrono::steady_clock::now();
+    const cudaError_t e = pcg_solve_once(n, use_net, sigma, m0, g, r, b, x, tol, tol_mode, max_iter, kTols[k], s, res);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (ic.chosen < 0 && e == cudaSuccess) {
+        if (ic.tried >= 1) ic.ms[k] += ms;   // the first solve warms up (tile tuning, graph capture)
+        if (++ic.tried == 1 + 2 * kInnerTrials) ic.chosen = ic.ms[0] <= ic.ms[1] ? 0 : 1;
+    }
+    return e;
+}
+
+double pcg_inner_choice(const LearnedNet* n)
+{
+    const InnerChoice& ic = n->inner[1];
+    return ic.chosen < 0 ? 0.0 : ic.chosen == 0 ? 1e-4 : 1e-5;
 }
 
 }  // namespace yk
