@@ -122,7 +122,8 @@ __device__ __forceinline__ unsigned long long gtimer()
 namespace {
 
 constexpr int kMaxSysPerBlock = 48;
-constexpr int kFinListMax = 1024;   // batched solves whose finisher compacts the active systems
+constexpr int kFinListMax = 1024;
+constexpr int kRuAlign = 10;   // batched solves: iterations at which triggered reliable updates run   // batched solves whose finisher compacts the active systems
 constexpr int kMaxDeps = 64;
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
@@ -653,7 +654,18 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         ar = rr * c * inv_pap;
         ai = -rr * d * inv_pap;
     }
-    if (!isfinite(ar) || !isfinite(ai)) return retire(0, YK_ENAN);
+    bool force_ru = false;
+    if (!isfinite(ar) || !isfinite(ai)) {
+        // a batched system whose convergence candidate waits for its aligned
+        // reliable update can iterate into breakdown (p -> 0): it takes the
+        // update now, without this step (x is unchanged by alpha = 0)
+        if (MIXED && a.sys_count > 1 && !(rr > st.stop2)) {
+            ar = ai = 0.0;
+            force_ru = true;
+        } else {
+            return retire(0, YK_ENAN);
+        }
+    }
     // |r - alpha q|^2 = |r|^2 - 2 Re(alpha <r, q>) + |alpha|^2 |q|^2
     double est = rr - 2.0 * (ar * s[4] - ai * s[5]) + (ar * ar + ai * ai) * s[1];
     if (!(est > 0.0)) est = 0.0;
@@ -671,7 +683,15 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         const bool drop = est < a.reliable_delta * a.reliable_delta * st.rmax2;
         const bool due = a.reliable_every > 0 && (k + 1) % a.reliable_every == 0;
         const bool cap = k + 1 >= a.max_iter;
-        if (cand || drop || due || cap) {
+        // Batched solves: a system's own triggers (convergence candidate,
+        // residual drop) wait for the next iteration divisible by kRuAlign, so
+        // that the systems' FP64 updates share iterations.  An update runs on
+        // the few SMs that own the system's tiles, at the FP64 rate, and every
+        // other block waits for it at the grid barrier.  A candidate far below
+        // its target (the recursion nears breakdown) does not wait.
+        const bool aligned = a.sys_count == 1 || (k + 1) % kRuAlign == 0;
+        const bool deep = est < 1e-6 * st.stop2;
+        if (force_ru || (cand && (aligned || deep)) || (drop && aligned) || due || cap) {
             cv.mode = kRu;
             atomicOr(s_ru, 1);
         }
