@@ -122,8 +122,8 @@ __device__ __forceinline__ unsigned long long gtimer()
 namespace {
 
 constexpr int kMaxSysPerBlock = 48;
-constexpr int kFinListMax = 1024;
-constexpr int kRuAlign = 10;   // batched solves: iterations at which triggered reliable updates run   // batched solves whose finisher compacts the active systems
+constexpr int kFinListMax = 1024;   // batched solves whose finisher compacts the active systems
+constexpr int kRuAlign = 10;        // batched solves: iterations at which triggered reliable updates run
 constexpr int kMaxDeps = 64;
 constexpr long long kWaitCycles = 4000000000LL;   // about 2 s at 2 GHz
 
