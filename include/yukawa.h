@@ -235,10 +235,12 @@ int yk_net_train(yk_ctx* ctx, int chain, const yk_net_train_cfg* cfg, yk_net_tra
  * FP64 refinement rounds. */
 int yk_fgcr_solve(yk_ctx* ctx, int chain, const double* b, double* x, double tol, int tol_mode, int max_iter,
                   int use_net, yk_solve_stats* stats);
-/* As yk_fgcr_solve, by preconditioned CG (the network's M = s I + N^T N is
- * symmetric positive definite, so plain PCG applies): FP32 vectors with the
- * iteration's scalars kept on the device (the host reads |r|^2 every 8
- * iterations), inside FP64 iterative refinement. */
+/* As yk_fgcr_solve, by flexible preconditioned CG (the network's
+ * M = s I + N^T N is symmetric positive definite): FP32 vectors, alpha and
+ * beta computed on the device (the host reads |r|^2 every 8 iterations),
+ * inside FP64 iterative refinement.  Each inner FP32 solve reduces the
+ * residual by 1e-4 or 1e-5, chosen per network by timing its first solves
+ * (environment YK_PCG_INNER fixes it). */
 int yk_pcg_solve(yk_ctx* ctx, int chain, const double* b, double* x, double tol, int tol_mode, int max_iter,
                  int use_net, yk_solve_stats* stats);
 
