@@ -85,6 +85,9 @@ typedef struct yk_params {
                                /*   since the last one (0.001)                  */
     double fixed_dt;           /* > 0: fixed Euler step instead of adaptive eps   */
     int init;                  /* YK_INIT_DRAND48 (reference), YK_INIT_PHILOX     */
+    int learned_layers;        /* yk_run: > 0 trains a network of that many layers */
+                               /*   after thermalisation and runs the measurement  */
+                               /*   steps with yk_langevin_step_learned (0: off)   */
 } yk_params;
 
 /* Parameters after the reference's conversion (main.cu:58-63, 113-170). */

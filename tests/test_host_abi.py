@@ -83,6 +83,7 @@ cg_tol = 1e-10
 reliable_every = 25
 fixed_dt = 0.01
 init = "philox"
+learned_layers = 2
 """)
     p = ylib.Params.from_toml(f)
     assert p.use_mass == 1 and p.mass == -0.5 and p.g == 1.0 and p.cut_fraction == 0.35355339059327373
@@ -90,6 +91,7 @@ init = "philox"
     assert p.seed == 77 and p.yukawa_coupling == 0.5 and p.fermion_mass == 0.1 and p.drift_mode == 1
     assert (p.Nt, p.Nx, p.precision, p.n_rhs, p.cg_tol_mode, p.cg_tol) == (32, 64, ylib.YK_MIXED, 4, 1, 1e-10)
     assert p.reliable_every == 25 and p.fixed_dt == 0.01 and p.init == ylib.YK_INIT_PHILOX
+    assert p.learned_layers == 2 and ylib.Params.default().learned_layers == 0
     with pytest.raises(ylib.YukawaError):
         ylib.Params.from_toml(tmp_path / "missing.toml")
 

@@ -228,3 +228,63 @@ def test_learned_step_matches_cg_step(ylib, cuda):
     for mode in ("identity", "net"):
         err = np.abs(fields[mode] - ref).max() / np.abs(ref).max()
         assert err < 1e-8, (mode, err)
+
+
+@pytest.mark.gpu
+def test_run_protocol_with_learned_solver(ylib, cuda, tmp_path):
+    # the reference's run protocol (yk_run_toml) with [gpu] learned_layers = 2:
+    # a network is trained after thermalisation and the measurement steps
+    # solve with it; the traces agree with the same run by the CG step graph
+    # to the solves' tolerance
+    yk = ylib
+    toml = """
+[physics]
+useMass = "true"
+mass = -0.5
+g = 1.0
+cutFraction = 0.35355339059327373
+
+[langevin]
+averageEpsilon = 0.01
+MaxLangevinTime = 0.5
+ExportTime = 0.05
+burnCount = 2
+MeasureDriftCount = 0
+
+[io]
+configFileName = "cfg.bin"
+export = "false"
+timeSliceFileName = "slice.dat"
+
+[random]
+seed = 11
+
+[fermions]
+yukawa_coupling = 0.5
+fermion_mass = 0.05
+driftMode = 0
+WilsonParam = 1.0
+
+[lattice]
+Nt = 32
+Nx = 32
+
+[gpu]
+precision = "mixed"
+cg_tol_mode = "rel"
+cg_tol = 1e-10
+fixed_dt = 0.01
+init = "philox"
+"""
+    traces = {}
+    for name, extra in (("cg", ""), ("learned", "learned_layers = 2\n")):
+        d = tmp_path / name
+        d.mkdir()
+        (d / "input.toml").write_text(toml + extra)
+        yk.run(d / "input.toml", d)
+        rows = (d / "traces.csv").read_text().strip().splitlines()
+        assert rows[0] == "tr,sigma,phi" and len(rows) > 5
+        traces[name] = np.array([[float(v) for v in r.split(",")] for r in rows[1:]])
+    a, b = traces["cg"], traces["learned"]
+    assert a.shape == b.shape
+    assert np.abs(a - b).max() < 1e-7 * max(1.0, np.abs(a).max())

@@ -56,7 +56,7 @@ class Params(C.Structure):
         ("Nt", C.c_int), ("Nx", C.c_int),
         ("precision", C.c_int), ("n_rhs", C.c_int), ("cg_tol_mode", C.c_int), ("cg_tol", C.c_double),
         ("cg_max_iter", C.c_int), ("reliable_every", C.c_int), ("reliable_delta", C.c_double),
-        ("fixed_dt", C.c_double), ("init", C.c_int),
+        ("fixed_dt", C.c_double), ("init", C.c_int), ("learned_layers", C.c_int),
     ]
 
     @classmethod

@@ -269,6 +269,7 @@ void yk_params_default(yk_params* p)
     p->reliable_delta = 0.001;
     p->fixed_dt = 0.0;
     p->init = YK_INIT_DRAND48;
+    p->learned_layers = 0;
 }
 
 static bool get_d(const std::map<std::string, std::string>& kv, const char* k, double* v)
@@ -342,6 +343,7 @@ int yk_params_from_toml(const char* path, yk_params* p)
         const std::string v = s("gpu.init");
         p->init = (v == "philox") ? YK_INIT_PHILOX : (v == "none" ? YK_INIT_NONE : YK_INIT_DRAND48);
     }
+    get_i(kv, "gpu.learned_layers", &p->learned_layers);
     return YK_OK;
 }
 

@@ -146,10 +146,19 @@ int yk_run_toml(const char* toml_path, const char* out_dir)
     int rc = YK_OK;
     yk_obs obs;
     // one export block: steps until the accumulated eps reaches ExportTime
+    // [gpu] learned_layers > 0: after thermalisation a network of that many
+    // layers is trained on pairs from the chain's own CG, and the steps that
+    // follow solve with it (flexible preconditioned CG in FP64 refinement)
+    bool learned = false;
     auto export_block = [&](double& t_out, double& eps_last) -> int {
         double t = 0.0;
         while (t < p.export_time) {
-            if (int r = yk_langevin_step(ctx, 1)) return r;
+            if (learned) {
+                yk_solve_stats st;
+                if (int r = yk_langevin_step_learned(ctx, 1, 1, &st)) return r;
+            } else if (int r = yk_langevin_step(ctx, 1)) {
+                return r;
+            }
             if (int r = yk_observables(ctx, 0, &obs)) return r;
             if (obs.status == YK_ENAN || obs.status == YK_ETIMEOUT) {
                 yk::set_error("step failed with status %d", obs.status);
@@ -165,6 +174,17 @@ int yk_run_toml(const char* toml_path, const char* out_dir)
     double t_blk = 0.0, eps_last = p.average_epsilon;
     for (int burn = 0; burn < p.burn_count && rc == YK_OK; ++burn) rc = export_block(t_blk, eps_last);
     if (rc == YK_OK) std::printf("Thermalization done!\n");
+    if (rc == YK_OK && p.learned_layers > 0 && p.yukawa_coupling != 0.0) {
+        rc = yk_net_setup(ctx, 0, p.learned_layers, 7, -1.0);
+        yk_net_train_cfg cfg = {4, 5, 4, 400, 4, 2e-3, 3};
+        yk_net_train_stats ts;
+        if (rc == YK_OK) rc = yk_net_train(ctx, 0, &cfg, &ts);
+        if (rc == YK_OK) {
+            std::printf("Learned preconditioner: %d layers, %d pairs, loss %.4f -> %.4f (%.0f ms)\n",
+                        p.learned_layers, ts.pairs, ts.loss0, ts.loss1, ts.ms);
+            learned = true;
+        }
+    }
     double elapsed = 0.0;
     if (rc == YK_OK && p.measure_drift_count > 0) {
         double eps_sum = 0.0;
