@@ -213,3 +213,32 @@ def test_gamma_method():
     assert np.allclose(got, _gamma_py(x), rtol=1e-10, atol=1e-12)
     tau_exact = 0.5 * (1 + rho) / (1 - rho)
     assert abs(got[3] - tau_exact) < 4 * got[4] + 0.3
+
+
+def test_evenodd_schur_solve_matches_direct():
+    # the even-odd Schur complement solve of D^dag chi = eta (the force's
+    # chi = D (D^dag D)^-1 eta) against a dense solve, and its CG iterations
+    # against the reference's CG on D^dag D (the groundwork of an even-odd
+    # solver: half the unknowns, fewer iterations)
+    from oracle import evenodd as E
+    Nt, Nx = 8, 6
+    rng = np.random.default_rng(4)
+    a = O.action(m2=-0.5, lam=1.0, g=0.5, m0=0.05, r=1.0)
+    sigma = rng.uniform(-1, 1, Nt * Nx)
+    eta = rng.normal(size=(Nt * Nx, 4)) + 0j
+    # the diagonal the oracle's D uses
+    unit = np.zeros((Nt * Nx, 4), dtype=np.complex128)
+    unit[5, 2] = 1.0
+    assert abs(O.dirac(Nt, Nx, a, sigma, unit, True)[5, 2] - E.diagonal(a, sigma)[5]) < 1e-14
+    V4 = 4 * Nt * Nx
+    Ddag = np.empty((V4, V4), dtype=np.complex128)
+    for j in range(V4):
+        u = np.zeros(V4, dtype=np.complex128)
+        u[j] = 1.0
+        Ddag[:, j] = O.dirac(Nt, Nx, a, sigma, u.reshape(-1, 4), True).ravel()
+    want = np.linalg.solve(Ddag, eta.ravel()).reshape(-1, 4)
+    chi_eo, it_eo = E.chi_evenodd(Nt, Nx, a, sigma, eta, tol=1e-12)
+    chi_cg, it_cg = E.chi_full(Nt, Nx, a, sigma, eta, tol=1e-12)
+    assert np.abs(chi_eo - want).max() < 1e-9 * np.abs(want).max()
+    assert np.abs(chi_cg - want).max() < 1e-9 * np.abs(want).max()
+    assert it_eo < it_cg, (it_eo, it_cg)
