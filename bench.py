@@ -7,12 +7,17 @@ coloured-noise cutoff Lambda = pi/2 (cutFraction = 1/(2 sqrt 2)), fixed Euler
 step dt = 0.01, one Gaussian stochastic right-hand side per step, CG on
 D^dag D to relative residual 1e-10 with FP32 iterations and FP64 reliable
 updates (every 50 iterations, and each time the FP32 residual drops a
-hundredfold), FP64 field.  Synthetic data: the field starts
-iid Uniform[-1, 1] from seed 1234 and all noise is drawn from Philox.
+hundredfold), FP64 field.  Synthetic data: all noise is drawn from Philox,
+and both arms start from one thermalised field (tests/golden/start_256x256.npz:
+2000 steps of the CPU oracle from iid Uniform[-1, 1], seed 1234), run the
+warm-up steps from it and time the steps that follow, so both time the same
+stretch of the same trajectory and the rate does not depend on --steps.
 
 One step = coloured noise + fermion force (CG) + drift/Euler update +
 per-step observables, replayed as one CUDA graph.  L2 (129 MB) is flushed by a
-256 MiB write between timed steps, outside the timed events.
+256 MiB write between timed steps, outside the timed events.  Every other leg
+of the line (kernel profile, e2e through the C ABI with host buffers, the
+plain FP64 form, the precision errors) replays that same segment.
 
   --impl ours (default): the CUDA path; `value` = steps/s of all ranks.
   --impl reference: the CPU oracle (C restatement of the reference's
@@ -42,6 +47,10 @@ CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (
 BYTES_CG_ITER_MIXED = 200          # unique bytes per site per FP32 CG iteration of cg_kernel (passes A and B)
 BYTES_CG_ITER_HALO = 128           # the same for cg_halo_kernel: D p stays in shared memory, diag is cached
 BYTES_CG_ITER_FP64 = 400
+# the thermalised start of the workload (both arms time the same steps from it)
+START = ROOT / "tests" / "golden" / "start_256x256.npz"
+DATA = ("synthetic: Philox noise; the timed steps continue a chain from tests/golden/start_256x256.npz, "
+        "the CPU oracle's field after 2000 Langevin steps from iid Uniform[-1, 1] (seed 1234)")
 
 
 def workload(precision: str) -> dict:
@@ -137,6 +146,7 @@ def job_value(steps: int, ws: int, t_all: float) -> float:
 
 # ---------------------------------------------------------------- our arm
 def run_ours(args, ws, rank, local):
+    import numpy as np
     import torch
     import yukawacolourednoise_gb300 as yk
 
@@ -166,10 +176,16 @@ def run_ours(args, ws, rank, local):
         if dist is not None:
             dist.barrier()
 
+    phi_start, step_start = start_field()
     ctx = yk.Context(make_params(yk, args.precision, seed=1234 + rank))
     ctx.set_stream(stream.cuda_stream)
+    ctx.set_field(phi_start)
+    ctx.set_step(step_start)
     ctx.step(args.warmup)
     ctx.synchronize()
+    # the timed segment starts here: every other leg of this run replays it
+    phi_seg, step_seg = ctx.get_field(), ctx.get_step()
+    obs_seg = ctx.observables()
 
     barrier()
     clocks = Clocks(local)
@@ -179,77 +195,30 @@ def run_ours(args, ws, rank, local):
     obs = ctx.observables()
     if obs.status not in (0, yk.YK_ENOCONV):
         raise RuntimeError(f"step status {obs.status}")
-    cg_stats = {"iterations_per_step": round(obs.cg_iterations_total / max(obs.steps, 1), 1),
-                "steps_at_iteration_cap": int(obs.noconv_steps), "iteration_cap": 20000}
+    phi_end = ctx.get_field()
+    seg_iters = obs.cg_iterations_total - obs_seg.cg_iterations_total
+    cg_stats = {"iterations_per_step": round(seg_iters / args.steps, 1),
+                "steps_at_iteration_cap": int(obs.noconv_steps - obs_seg.noconv_steps), "iteration_cap": 20000}
     t_all = max_over_ranks(t_sec, dist, "cuda")
     value = job_value(args.steps, ws, t_all)
 
     extras = {}
     if rank == 0 and not args.quick:
-        # kernel timing of the same workload: CUDA events around each kernel class
+        # kernel timing of the same segment: CUDA events around each kernel class
+        ctx.set_field(phi_seg)
+        ctx.set_step(step_seg)
         ctx.profile_begin()
         with torch.cuda.stream(stream):
-            ctx.step(args.profile_steps)
+            ctx.step(args.steps)
         pr = ctx.profile_end()
-        per_launch_ms = pr.cg_ms / max(pr.cg_launches, 1)
-        halo = pr.cg_kernel == 1
-        bpi = (BYTES_CG_ITER_HALO if halo else BYTES_CG_ITER_MIXED) if args.precision == "mixed" else BYTES_CG_ITER_FP64
-        kname = "cg_halo_kernel" if halo else f"cg_kernel<1,{'mixed' if args.precision == 'mixed' else 'fp64'}>"
-        alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
-        pk = peaks()
-        achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
-        tr = ncu_traffic()
-        traffic = None
-        if tr and tr.get("precision") == args.precision and tr.get("kernel", "cg_kernel<1,mixed>") == kname:
-            traffic = tr["dram_bytes_per_iteration"] * pr.cg_iterations / max(pr.cg_launches, 1)
-        extras["roofline"] = {"bound": "hbm", "kernel": kname,
-                              "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
-                              "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
-                              "peak_source": pk["source"],
-                              "bytes_per_site_iteration": bpi,
-                              "cg_iterations_per_step": pr.cg_iterations / max(pr.steps, 1),
-                              "ms_per_launch": round(per_launch_ms, 4)}
-        tot = pr.noise_ms + pr.cg_ms + pr.force_ms + pr.update_ms
-        extras["kernel_share"] = {k: round(v / tot, 4) for k, v in
-                                  (("noise", pr.noise_ms), ("cg", pr.cg_ms), ("force_drift", pr.force_ms),
-                                   ("update", pr.update_ms))}
+        extras["roofline"], extras["kernel_share"] = roofline(pr, args.precision)
         launches_per_step = pr.launches / max(pr.steps, 1)
-
-        # end to end through the C ABI with host buffers (pinned), every step:
-        # H2D of the field, one step, D2H of the field and the observables
-        import numpy as np
-        V = NT * NX
-        host_in = torch.empty(V, dtype=torch.float64).pin_memory()
-        host_out = torch.empty(V, dtype=torch.float64).pin_memory()
-        host_in.copy_(torch.from_numpy(ctx.get_field()))
-        lib = yk.lib()
-        import ctypes as C
-        o = yk.Obs()
-        ke = args.e2e_steps
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            yk._check(lib.yk_set_field_host(ctx.h, 0, C.c_void_p(host_in.data_ptr())))
-            yk._check(lib.yk_langevin_step(ctx.h, 1))
-            yk._check(lib.yk_get_field_host(ctx.h, 0, C.c_void_p(host_out.data_ptr())))
-            yk._check(lib.yk_observables(ctx.h, 0, C.byref(o)))
-            host_in, host_out = host_out, host_in
-        e2e_sec = time.perf_counter() - t0
-        extras["e2e"] = {"value": round(ke / e2e_sec, 2), "unit": "steps/s", "h2d_bytes_per_step": 8 * V,
-                         "d2h_bytes_per_step": 8 * V + C.sizeof(yk.Obs)}
-
-        # plain FP64 CG form of the same workload (the metric's denominator)
+        extras["e2e"] = e2e(yk, torch, ctx, phi_seg, step_seg, args.steps, flush, phi_end)
+        # plain FP64 CG form of the same segment (the metric's denominator)
         if args.precision == "mixed":
-            ctx64 = yk.Context(make_params(yk, "fp64"))
-            ctx64.set_stream(stream.cuda_stream)
-            ctx64.step(args.warmup)
-            ctx64.synchronize()
-            k64 = args.fp64_steps or args.steps   # same trajectory segment as the timed steps
-            t64 = timed_steps(ctx64, k64)
-            extras["plain_fp64"] = {"value": round(k64 / t64, 2), "unit": "steps/s", "steps": k64,
-                                    "speedup_mixed_over_fp64": round(value / ws / (k64 / t64), 3)}
-            ctx64.close()
-
+            extras["plain_fp64"] = plain_fp64(yk, torch, stream, timed_steps, phi_start, step_start, args, value / ws)
+            extras["precision_errors"] = precision_errors(yk, torch, stream, phi_seg, step_seg,
+                                                          min(args.steps, 20))
         # Dirac apply HBM bandwidth on a lattice larger than L2 (complex buffers)
         extras["dirac_hbm"] = dirac_hbm(yk, torch, stream)
         # the batching configuration (many chains of uneven sizes in one graph)
@@ -257,6 +226,9 @@ def run_ours(args, ws, rank, local):
         # the learned-preconditioner configuration (512^2 near the chiral regime)
         if not args.no_learned:
             extras["learned"] = learned(yk, torch, stream, steps=args.learned_steps)
+        # the full form at scale (8 chains of 1024^2, 8 RHS), one timed step per arm
+        if not args.no_full_scale:
+            extras["full_scale"] = full_scale(yk, torch, stream)
         extras["gpu_launches"] = int(round(launches_per_step * args.steps))
 
     ctx.close()
@@ -267,23 +239,179 @@ def run_ours(args, ws, rank, local):
     line = {"metric": METRIC, "value": round(value, 2), "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t_all / args.steps * 1e3, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
-            "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
-            "config": workload(args.precision), "clocks": clk, "cg": cg_stats}
+            "data": DATA, "config": workload(args.precision), "clocks": clk, "cg": cg_stats}
     line.update(extras)
     if "gpu_launches" not in line:
         line["gpu_launches"] = 7 * args.steps
     if not args.no_cpu and ws == 1:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, args.warmup)
     return line
 
 
-def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8):
+def start_field():
+    """The thermalised starting field of the 256^2 workload and the Philox
+    step it continues at (tests/golden/make_start_field.py)."""
+    import numpy as np
+    d = np.load(START)
+    return np.ascontiguousarray(d["phi"], dtype=np.float64), int(d["step"])
+
+
+def roofline(pr, precision):
+    """Roofline of the dominant kernel (the persistent CG) from the profiled
+    steps: algorithmic bytes per launch / CUDA-event launch time."""
+    per_launch_ms = pr.cg_ms / max(pr.cg_launches, 1)
+    halo = pr.cg_kernel == 1
+    bpi = (BYTES_CG_ITER_HALO if halo else BYTES_CG_ITER_MIXED) if precision == "mixed" else BYTES_CG_ITER_FP64
+    kname = "cg_halo_kernel" if halo else f"cg_kernel<1,{'mixed' if precision == 'mixed' else 'fp64'}>"
+    alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
+    pk = peaks()
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    tr = ncu_traffic()
+    traffic = None
+    if tr and tr.get("precision") == precision and tr.get("kernel", "cg_kernel<1,mixed>") == kname:
+        traffic = tr["dram_bytes_per_iteration"] * pr.cg_iterations / max(pr.cg_launches, 1)
+    roof = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+            "peak_source": pk["source"], "bytes_per_site_iteration": bpi,
+            "cg_iterations_per_step": pr.cg_iterations / max(pr.steps, 1),
+            "ms_per_launch": round(per_launch_ms, 4), "profiled_steps": pr.steps}
+    tot = pr.noise_ms + pr.cg_ms + pr.force_ms + pr.update_ms
+    share = {k: round(v / tot, 4) for k, v in (("noise", pr.noise_ms), ("cg", pr.cg_ms),
+                                                ("force_drift", pr.force_ms), ("update", pr.update_ms))}
+    return roof, share
+
+
+def e2e(yk, torch, ctx, phi_seg, step_seg, k, flush, phi_end):
+    """The same k steps as `value` (the timed segment replayed from its first
+    field and Philox step) through the C ABI with host buffers: every step
+    uploads the field from pinned host memory, steps, and reads the field and
+    the observables back.  Wall clock around each step's calls; L2 flushed
+    between steps, outside the timed calls."""
+    import ctypes as C
+    V = NT * NX
+    host_in = torch.empty(V, dtype=torch.float64).pin_memory()
+    host_out = torch.empty(V, dtype=torch.float64).pin_memory()
+    host_in.copy_(torch.from_numpy(phi_seg))
+    ctx.set_step(step_seg)
+    lib = yk.lib()
+    o = yk.Obs()
+    sec = 0.0
+    for i in range(k):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        yk._check(lib.yk_set_field_host(ctx.h, 0, C.c_void_p(host_in.data_ptr())))
+        yk._check(lib.yk_langevin_step(ctx.h, 1))
+        yk._check(lib.yk_get_field_host(ctx.h, 0, C.c_void_p(host_out.data_ptr())))
+        yk._check(lib.yk_observables(ctx.h, 0, C.byref(o)))
+        sec += time.perf_counter() - t0
+        host_in, host_out = host_out, host_in
+    same = bool(torch.equal(host_in, torch.from_numpy(phi_end)))
+    return {"value": round(k / sec, 2), "unit": "steps/s", "h2d_bytes_per_step": 8 * V,
+            "d2h_bytes_per_step": 8 * V + C.sizeof(yk.Obs), "steps": k,
+            "segment": "the steps timed for value, replayed from the segment's first field and step",
+            "same_trajectory_as_value": same, "l2": "flushed between steps (outside the timed calls)"}
+
+
+def plain_fp64(yk, torch, stream, timed_steps, phi_start, step_start, args, value_mixed):
+    """The plain FP64 CG form of the same workload and segment (the metric's
+    denominator): FP64 stencil and CG (cg_kernel, the grid-wide persistent
+    kernel; the halo kernel serves single-system mixed solves)."""
+    ctx64 = yk.Context(make_params(yk, "fp64"))
+    ctx64.set_stream(stream.cuda_stream)
+    ctx64.set_field(phi_start)
+    ctx64.set_step(step_start)
+    ctx64.step(args.warmup)
+    ctx64.synchronize()
+    o0 = ctx64.observables()
+    k64 = args.fp64_steps or args.steps
+    t64 = timed_steps(ctx64, k64)
+    o1 = ctx64.observables()
+    ctx64.close()
+    return {"value": round(k64 / t64, 2), "unit": "steps/s", "steps": k64,
+            "cg_iterations_per_step": round((o1.cg_iterations_total - o0.cg_iterations_total) / k64, 1),
+            "cg_kernel": "cg_kernel<1,fp64> (grid-wide persistent CG)",
+            "speedup_mixed_over_fp64": round(value_mixed / (k64 / t64), 3)}
+
+
+def precision_errors(yk, torch, stream, phi_seg, step_seg, n, n_ops=5):
+    """Errors of the mixed FP32/FP64 path against this library's FP64 path
+    (itself pinned to the CPU oracle to 1e-13 by the tests), at the fields of
+    the timed segment: per step, the max relative error of the FP32 Dirac
+    apply (a Gaussian spinor), of the mixed CG solution (rel-res 1e-10, the
+    same Gaussian right-hand side) and of the step's fermion force (the
+    step's Philox source, the mixed step solver against the FP64 one); and
+    <sigma> of the mixed and FP64 trajectories from the segment's first field
+    with the same Philox streams."""
+    import numpy as np
+    V = NT * NX
+    cm = yk.Context(make_params(yk, "mixed"))
+    c64 = yk.Context(make_params(yk, "fp64"))
+    for c in (cm, c64):
+        c.set_stream(stream.cuda_stream)
+        c.set_field(phi_seg)
+        c.set_step(step_seg)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    d_err, x_err, f_err, sig_m, sig_64 = [], [], [], [], []
+
+    def rel(a, b):
+        return float((a - b).abs().max() / b.abs().max())
+
+    with torch.cuda.stream(stream):
+        for s in range(n):
+            if s < n_ops:
+                c64.set_field(cm.get_field())
+                c64.set_step(step_seg + s)
+                psi = torch.randn(V, 4, dtype=torch.complex128, device="cuda", generator=gen)
+                y64 = torch.empty_like(psi)
+                y32 = torch.empty(V, 4, dtype=torch.complex64, device="cuda")
+                c64.dirac_apply(psi, y64, False, yk.YK_FP64)
+                c64.dirac_apply(psi.to(torch.complex64), y32, False, yk.YK_FP32)
+                x64, xm = torch.zeros_like(psi), torch.zeros_like(psi)
+                c64.cg_solve(psi, x64, yk.YK_DAGGER, 1e-10, yk.YK_TOL_REL, 20000, yk.YK_FP64)
+                c64.cg_solve(psi, xm, yk.YK_DAGGER, 1e-10, yk.YK_TOL_REL, 20000, yk.YK_MIXED)
+                fm = torch.empty(V, dtype=torch.float64, device="cuda")
+                f64 = torch.empty_like(fm)
+                cm.fermion_force(fm)
+                c64.fermion_force(f64)
+                stream.synchronize()
+                d_err.append(rel(y32.to(torch.complex128), y64))
+                x_err.append(rel(xm, x64))
+                f_err.append(rel(fm, f64))
+            cm.step(1)
+            sig_m.append(cm.observables().sum_phi / V)
+        c64.set_field(phi_seg)
+        c64.set_step(step_seg)
+        for s in range(n):
+            c64.step(1)
+            sig_64.append(c64.observables().sum_phi / V)
+        dphi = float(np.abs(cm.get_field() - c64.get_field()).max())
+    cm.close()
+    c64.close()
+    dsig = [abs(a - b) for a, b in zip(sig_m, sig_64)]
+    return {"reference": "this library's FP64 path (pinned to the CPU oracle to 1e-13 in the tests)",
+            "steps_checked": n_ops, "dirac_fp32_max_rel": max(d_err), "cg_mixed_max_rel": max(x_err),
+            "force_mixed_max_rel": max(f_err),
+            "per_step": {"dirac_fp32": [float(f"{v:.3e}") for v in d_err],
+                         "cg_mixed": [float(f"{v:.3e}") for v in x_err],
+                         "force_mixed": [float(f"{v:.3e}") for v in f_err]},
+            "sigma_steps": n, "sigma_mixed_last": sig_m[-1], "sigma_fp64_last": sig_64[-1],
+            "sigma_max_abs_diff": max(dsig), "field_max_abs_diff_last": dphi}
+
+
+
+
+def full_scale(yk, torch, stream, steps=1, L=1024, n_chains=8, n_rhs=8):
     """The full form at scale: 8 chains of 1024^2 (m0 = 0.01, g = 0.6,
     Lambda = pi/4, i.e. cutFraction 0.17678), 8 stochastic right-hand sides
-    per step, mixed CG to rel-res 1e-10, all chains in one step graph, against
-    the plain FP64 CG form of the same step.  `steps` timed steps after
-    `warmup` (a step takes seconds: thousands of CG iterations over 64
-    systems of 2^20 sites)."""
+    per step, all chains in one step, every solve to rel-res 1e-10: the mixed
+    CG step graph, the plain FP64 CG step graph and the learned PCG step
+    (2-layer network trained on chain 0's field, weights shared by the
+    chains; training time reported apart).  Each arm times the first `steps`
+    steps from the same seeded start (a step takes seconds: thousands of
+    iterations over 64 systems of 2^20 sites); the mixed step's grid is tuned
+    before the timed step, the FP64 one runs the co-resident grid untuned."""
     def params(prec, c):
         return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.6, fermion_mass=0.01,
                                  wilson_param=1.0, cut_fraction=0.17677669529663687, Nt=L, Nx=L, fixed_dt=0.01,
@@ -292,13 +420,22 @@ def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8
                                  init=yk.YK_INIT_PHILOX)
 
     out = {"config": f"{n_chains} chains of {L}x{L}, m0 0.01, g 0.6, cutFraction 0.17678, {n_rhs} RHS, "
-                     f"rel-res 1e-10, {steps} timed step(s) after {warmup}", "steps": steps}
+                     f"rel-res 1e-10, the first {steps} step(s) from the seeded start", "steps": steps}
     for name, prec in (("mixed_cg", yk.YK_MIXED), ("plain_fp64", yk.YK_FP64)):
-        ctx = yk.Context([params(prec, c) for c in range(n_chains)])
+        saved = os.environ.get("YK_AUTOTUNE")
+        if prec == yk.YK_FP64:
+            os.environ["YK_AUTOTUNE"] = "0"
+        try:
+            ctx = yk.Context([params(prec, c) for c in range(n_chains)])
+        finally:
+            if saved is None:
+                os.environ.pop("YK_AUTOTUNE", None)
+            else:
+                os.environ["YK_AUTOTUNE"] = saved
         ctx.set_stream(stream.cuda_stream)
-        ctx.step(warmup)
+        if prec == yk.YK_MIXED:
+            ctx.autotune()
         ctx.synchronize()
-        before = sum(ctx.observables(c).cg_iterations_total for c in range(n_chains))
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             a.record(stream)
@@ -307,7 +444,7 @@ def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8
         stream.synchronize()
         sec = a.elapsed_time(b) / 1e3
         obs = [ctx.observables(c) for c in range(n_chains)]
-        its = sum(o.cg_iterations_total for o in obs) - before
+        its = sum(o.cg_iterations_total for o in obs)
         out[name] = {"value": round(steps / sec, 4), "unit": "steps/s (all chains)",
                      "chain_steps_per_s": round(steps * n_chains / sec, 3),
                      "site_steps_per_s": round(steps * n_chains * L * L / sec, 1),
@@ -324,8 +461,6 @@ def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8
     w = ctx.net_get_weights()
     for c in range(1, n_chains):
         ctx.net_set_weights(w, chain=c)
-    ctx.step_learned(warmup)
-    ctx.synchronize()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = ctx.step_learned(steps)
@@ -336,7 +471,9 @@ def full_scale(yk, torch, stream, steps=1, warmup=1, L=1024, n_chains=8, n_rhs=8
                               "solver_iterations_per_system_step": round(s.iterations / (steps * n_chains * n_rhs), 1),
                               "all_converged": bool(s.converged),
                               "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4),
-                                           "loss_after": round(st.loss1, 4), "ms": round(st.ms, 1)}}
+                                           "loss_after": round(st.loss1, 4), "ms": round(st.ms, 1)},
+                              "value_incl_training_over_10000_steps":
+                                  round(10000 / (10000 / (steps / sec) + st.ms / 1e3), 4)}
     ctx.close()
     out["speedup_mixed_over_fp64"] = round(out["mixed_cg"]["value"] / out["plain_fp64"]["value"], 3)
     out["speedup_learned_over_fp64"] = round(out["learned_2layers"]["value"] / out["plain_fp64"]["value"], 3)
@@ -450,7 +587,9 @@ def learned(yk, torch, stream, L=512, m0=0.02, steps=20, burn_in=20, layer_count
             "training": {"pairs": st.pairs, "loss_before": round(st.loss0, 4), "loss_after": round(st.loss1, 4),
                          "ms": round(st.ms, 1)},
             "speedup_over_plain_fp64": round((steps / sec) / arms["plain_fp64"]["value"], 3),
-            "speedup_over_mixed_cg": round((steps / sec) / arms["mixed_cg"]["value"], 3)}
+            "speedup_over_mixed_cg": round((steps / sec) / arms["mixed_cg"]["value"], 3),
+            # the configuration's 5000 steps with this training's time spread over them
+            "value_incl_training_over_5000_steps": round(5000 / (5000 / (steps / sec) + st.ms / 1e3), 2)}
     ctx.close()
     out.update(arms)
     return out
@@ -486,52 +625,58 @@ def dirac_hbm(yk, torch, stream, Nt=4096, Nx=4096, reps=20):
 
 
 # ---------------------------------------------------------------- CPU arms
-def cpu_steps(seconds_budget: float, max_steps: int):
-    """Times full 256x256 Langevin steps of the CPU oracle (all host threads)."""
+def cpu_steps(seconds_budget: float, max_steps: int, warmup: int):
+    """Times full 256x256 Langevin steps of the CPU oracle (all host threads)
+    on the segment the GPU arm times: `warmup` untimed steps from the
+    thermalised start field, then up to `max_steps` steps within the budget."""
     from oracle import oracle as O
     a = O.action(m2=-0.5, lam=1.0, g=0.5, m0=0.1, r=1.0, cut_fraction=CUT)
-    phi = O.uniform_field(1234, 0, NT * NX)
+    phi, step0 = start_field()
+
+    def one(phi, s):
+        return O.langevin_step(NT, NX, a, phi, 1234, 0, step0 + s, tol=1e-10, tol_mode=1, max_iter=20000,
+                               fixed_dt=0.01)[0]
+
+    for s in range(warmup):
+        phi = one(phi, s)
     t0 = time.perf_counter()
-    phi, _ = O.langevin_step(NT, NX, a, phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
-    first = time.perf_counter() - t0
-    n = max(1, min(max_steps, int(seconds_budget / max(first, 1e-6))))
-    t0 = time.perf_counter()
-    for s in range(n):
-        phi, _ = O.langevin_step(NT, NX, a, phi, 1234, 0, s + 1, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    n = 0
+    while n < max_steps and (n == 0 or time.perf_counter() - t0 < seconds_budget):
+        phi = one(phi, warmup + n)
+        n += 1
     dt = time.perf_counter() - t0
     return n, dt, O.threads()
 
 
-def cpu_baseline(seconds: float) -> dict:
-    n, dt, threads = cpu_steps(seconds, 10_000)
+def cpu_baseline(seconds: float, warmup: int) -> dict:
+    n, dt, threads = cpu_steps(seconds, 10_000, warmup)
     return {"value": round(n / dt, 4), "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} full {NT}x{NX} Langevin steps (FP64 CG rel-res 1e-10, OpenMP over sites)"}
+            "sample": f"{n} full {NT}x{NX} Langevin steps from the thermalised start field after {warmup} warm-up "
+                      f"steps (FP64 CG rel-res 1e-10, OpenMP over sites)"}
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
     budget = float(os.environ.get("YK_REF_SECONDS", "120"))
-    per = budget / max(args.steps + args.warmup, 1)
-    # warm-up: one step each (bounded)
-    cpu_steps(per, max(1, min(args.warmup, 3)))
-    n, dt, threads = cpu_steps(max(budget * args.steps / (args.steps + args.warmup), per), args.steps)
+    n, dt, threads = cpu_steps(budget, args.steps, args.warmup)
     v = n / dt
     return {"metric": METRIC, "value": round(v, 4), "unit": "steps/s", "n_gpus": ws, "steps": n,
             "warmup": args.warmup, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic (Philox noise, iid uniform initial field, seed 1234)",
-            "config": workload(args.precision),
+            "data": DATA, "config": workload(args.precision),
             "cpu_baseline": {"value": round(v, 4), "unit": "steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{n} of {args.steps} requested {NT}x{NX} Langevin steps in FP64 "
-                                       f"(CPU restatement of the reference; the reference has no CPU path)"},
+                             "sample": f"{n} of {args.steps} requested {NT}x{NX} Langevin steps in FP64 from the "
+                                       f"thermalised start field after {args.warmup} warm-up steps (the segment "
+                                       f"the GPU arm times; CPU restatement of the reference, which has no CPU "
+                                       f"path)"},
             "e2e": {"value": round(v, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
@@ -547,6 +692,7 @@ def main(argv=None):
     ap.add_argument("--learned-steps", type=int, default=20)
     ap.add_argument("--full-scale", action="store_true",
                     help="only the full form at scale (8 chains of 1024^2, 8 RHS; one JSON object; minutes)")
+    ap.add_argument("--no-full-scale", action="store_true", help="skip the full form at scale in the default run")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

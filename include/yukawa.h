@@ -176,7 +176,8 @@ int yk_cg_solve(yk_ctx* ctx, int chain, const void* b, void* x, int mtype, doubl
  * The scratch is one fixed device array sized for V = Nt*Nx <= 16384 sites;
  * larger lattices return YK_EINVAL.  Calls that overlap in time share that
  * array and race.  Make the first call on a device before any stream capture
- * (it looks the array's address up once per device). */
+ * (it looks the array's address up once per device, and again after a
+ * cudaDeviceReset has replaced the device's context). */
 int yk_cg_solve_static(const double* sigma, int Nt, int Nx, double m0, double g, double r,
                        const void* b, void* x, int mtype, double tol, int tol_mode, int max_iter,
                        void* stream, yk_solve_stats* stats);

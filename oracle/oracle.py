@@ -48,6 +48,10 @@ def lib():
             "yko_drand48_field": (None, [i64, P]),
             "yko_langevin_step": (d, [i, i, A, u64, u32, u64, i, d, i, i, d, P, P]),
             "yko_gamma_method": (None, [P, i64, d, P]),
+            "yko_dirac_pi": (None, [i, i, A, P, P, P, P, i]),
+            "yko_cg_pi": (i, [i, i, A, P, P, P, P, i, d, i, i, C.POINTER(d)]),
+            "yko_force_pi": (i, [i, i, A, P, P, P, i, d, i, i, P]),
+            "yko_langevin_step_pi": (d, [i, i, A, u64, u32, u64, i, d, i, i, d, P, P]),
             "yko_threads": (i, []),
         }
         for name, (res, args) in sig.items():
@@ -222,3 +226,69 @@ def fermion_eta(seed, chain, step, Nt, Nx, n_rhs=1, kind=2):
 
 def threads() -> int:
     return lib().yko_threads()
+
+
+# ---------------------------------------------------------------- pion extension
+def _pi(pi, V):
+    if pi is None:
+        return None, None
+    a = np.ascontiguousarray(pi, dtype=np.float64).reshape(3 * V)
+    return a, _p(a)
+
+
+def dirac_pi(Nt, Nx, a: Action, sigma, pi, psi, dagger=False):
+    """D with the Yukawa term g (sigma + i gamma5 tau.pi); pi: (3, V) or None."""
+    V = Nt * Nx
+    sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(V, 4)
+    keep, pp = _pi(pi, V)
+    out = np.empty_like(psi)
+    lib().yko_dirac_pi(Nt, Nx, C.byref(a), _p(sigma), pp, _p(psi), _p(out), int(bool(dagger)))
+    return out
+
+
+def cg_pi(Nt, Nx, a: Action, sigma, pi, b, mtype=1, tol=1e-8, tol_mode=0, max_iter=1000):
+    V = Nt * Nx
+    sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.complex128).reshape(V, 4)
+    keep, pp = _pi(pi, V)
+    x = np.empty_like(b)
+    rr = C.c_double()
+    it = lib().yko_cg_pi(Nt, Nx, C.byref(a), _p(sigma), pp, _p(b), _p(x), int(mtype), tol, int(tol_mode),
+                         int(max_iter), C.byref(rr))
+    return x, it, rr.value
+
+
+def force_pi(Nt, Nx, a: Action, sigma, pi, eta, tol=1e-8, tol_mode=0, max_iter=1000):
+    """eta: (n_rhs, V, 4) complex.  Returns F (4, V): sigma, pi1, pi2, pi3."""
+    V = Nt * Nx
+    sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+    eta = np.ascontiguousarray(eta, dtype=np.complex128).reshape(-1, V, 4)
+    keep, pp = _pi(pi, V)
+    F = np.empty(4 * V)
+    it = lib().yko_force_pi(Nt, Nx, C.byref(a), _p(sigma), pp, _p(eta), eta.shape[0], tol, int(tol_mode),
+                            int(max_iter), _p(F))
+    return F.reshape(4, V), it
+
+
+@dataclass
+class StepObsPi:
+    eps: float
+    max_drift: float
+    sum_phi: float
+    sum_force: float
+    cg_iters: int
+    sum_phi2: float
+    sum_pi: tuple
+    sum_pi2: float
+
+
+def langevin_step_pi(Nt, Nx, a: Action, phi4, seed, chain, step, n_rhs=1, tol=1e-8, tol_mode=0, max_iter=1000,
+                     fixed_dt=0.0):
+    """One step of the four fields phi4 (4, V) = (sigma, pi1, pi2, pi3)."""
+    phi4 = np.ascontiguousarray(phi4, dtype=np.float64).reshape(4 * Nt * Nx).copy()
+    obs = np.zeros(10)
+    lib().yko_langevin_step_pi(Nt, Nx, C.byref(a), seed, chain, step, n_rhs, tol, int(tol_mode), int(max_iter),
+                               fixed_dt, _p(phi4), _p(obs))
+    return phi4.reshape(4, Nt * Nx), StepObsPi(obs[0], obs[1], obs[2], obs[3], int(obs[4]), obs[5],
+                                               (obs[6], obs[7], obs[8]), obs[9])

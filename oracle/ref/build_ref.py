@@ -21,15 +21,17 @@ prebuilt fatbins through oracle/ref/ref_harness.cpp.
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 import tempfile
 from pathlib import Path
 
-REF_SRC = Path("/root/reference/code/src")
+# the reference's code/src directory (environment YK_REFERENCE_SRC overrides the default)
+REF_SRC = Path(os.environ.get("YK_REFERENCE_SRC", "/root/reference/code/src"))
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-SIZES = [(8, 4), (6, 10), (16, 16)]
+SIZES = [(8, 4), (6, 10), (16, 16), (32, 32)]
 TUS = ["Dirac.cu", "CGsolver.cu", "FermionicDrift.cu", "reductions.cu", "langevin_gpu_v2.cu", "Lattice.cu"]
 KERNELS = ["applyD_gpu", "solve_kernel", "computeDrift", "Run", "gpuMagnetisation", "gpuTimeSlices",
            "gpuTimeSlices_spinors", "gpuTraces", "ApplyMask"]

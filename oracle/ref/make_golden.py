@@ -5,7 +5,7 @@ cuFFT) on the machine it runs on, runs it on a GPU against the reference
 kernels compiled by oracle/ref/build_ref.py (oracle/_ref/*.fatbin), and packs
 each binary dump into an .npz.  Run on a GPU machine:
 
-    python oracle/ref/make_golden.py --out <dir>
+    python oracle/ref/make_golden.py --out <dir> [--sizes 32x32]
 
 TEST INFRASTRUCTURE ONLY.
 """
@@ -20,7 +20,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REF = HERE.parent / "_ref"
-SIZES = [(8, 4), (6, 10), (16, 16)]
+SIZES = [(8, 4), (6, 10), (16, 16), (32, 32)]
 
 
 def build_harness() -> Path:
@@ -49,11 +49,13 @@ def read_dump(path: Path) -> dict[str, np.ndarray]:
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(HERE.parent.parent / "tests" / "golden"))
+    ap.add_argument("--sizes", default=None, help="e.g. 32x32,16x16 (default: every size)")
     args = ap.parse_args(argv)
+    sizes = SIZES if not args.sizes else [tuple(int(v) for v in s.split("x")) for s in args.sizes.split(",")]
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     exe = build_harness()
-    for nt, nx in SIZES:
+    for nt, nx in sizes:
         dump = out / f"ref_{nt}x{nx}.bin"
         subprocess.run([str(exe), str(REF / f"ref_{nt}x{nx}.fatbin"), str(REF / f"symbols_{nt}x{nx}.txt"),
                         str(nt), str(nx), str(dump)], check=True)

@@ -117,6 +117,51 @@ void yko_dirac(int Nt, int Nx, const yko_action* a, const double* sigma,
 }
 
 /* ------------------------------------------------------------------------- */
+/* Pion extension (no reference counterpart: the reference is sigma-only,     */
+/* params.h:25 nVectorComponents = 1, diagonal Dirac.cu:57-69).  The Yukawa   */
+/* term becomes g (sigma + i gamma5 tau.pi) with gamma5 = -i gamma_t gamma_x  */
+/* = sigma_2 on spin (gamma_t = sigma_3, gamma_x = sigma_1 as in Dirac.cu),   */
+/* so i gamma5 = [[0, 1], [-1, 0]], and tau the Pauli matrices on flavour.    */
+/* D^dag carries g (sigma - i gamma5 tau.pi) (i gamma5 tau_a is              */
+/* anti-Hermitian).  pi: 3 fields of V doubles, component-major pi[a*V + n].  */
+/* ------------------------------------------------------------------------- */
+
+/* out += (s1 i gamma5 tau_1 + s2 i gamma5 tau_2 + s3 i gamma5 tau_3) in at one
+   site: in, out = 4 complex [f1s1, f1s2, f2s1, f2s2] as interleaved doubles */
+static void pion_site_add(const double* in, double* out, double s1, double s2, double s3)
+{
+    /* w_f = i sigma_2 psi_f: (w_f)_0 = psi_{f,1}, (w_f)_1 = -psi_{f,0} */
+    double w[2][2][2];
+    for (int f = 0; f < 2; ++f)
+        for (int k = 0; k < 2; ++k) {
+            w[f][0][k] = in[(2 * f + 1) * 2 + k];
+            w[f][1][k] = -in[(2 * f + 0) * 2 + k];
+        }
+    /* tau.s = [[s3, s1 - i s2], [s1 + i s2, -s3]] */
+    for (int sp = 0; sp < 2; ++sp) {
+        const double ar = w[0][sp][0], ai = w[0][sp][1], br = w[1][sp][0], bi = w[1][sp][1];
+        /* flavour 1: s3 a + (s1 - i s2) b */
+        out[(0 + sp) * 2 + 0] += s3 * ar + (s1 * br + s2 * bi);
+        out[(0 + sp) * 2 + 1] += s3 * ai + (s1 * bi - s2 * br);
+        /* flavour 2: (s1 + i s2) a - s3 b */
+        out[(2 + sp) * 2 + 0] += (s1 * ar - s2 * ai) - s3 * br;
+        out[(2 + sp) * 2 + 1] += (s1 * ai + s2 * ar) - s3 * bi;
+    }
+}
+
+void yko_dirac_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi,
+                  const double* in, double* out, int dagger)
+{
+    yko_dirac(Nt, Nx, a, sigma, in, out, dagger);
+    if (!pi) return;
+    const int V = Nt * Nx;
+    const double sg = dagger ? -a->g : a->g;
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n < V; ++n)
+        pion_site_add(in + (int64_t)n * 8, out + (int64_t)n * 8, sg * pi[n], sg * pi[V + n], sg * pi[2 * V + n]);
+}
+
+/* ------------------------------------------------------------------------- */
 /* CG on D^dag D: CGsolver.cu:72-170, gpuSumSpinors :172-177,                 */
 /* gpuDotProduct reductions.cu:145-174.                                        */
 /* ------------------------------------------------------------------------- */
@@ -178,8 +223,24 @@ static void cdiv(double a, double b, double c, double d, double* re, double* im)
     }
 }
 
+static int cg_any(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* b,
+                  double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr);
+
 int yko_cg(int Nt, int Nx, const yko_action* a, const double* sigma, const double* b,
            double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr)
+{
+    return cg_any(Nt, Nx, a, sigma, NULL, b, x, mtype, tol, tol_mode, max_iter, final_rr);
+}
+
+int yko_cg_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* b,
+              double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr)
+{
+    return cg_any(Nt, Nx, a, sigma, pi, b, x, mtype, tol, tol_mode, max_iter, final_rr);
+}
+
+/* pi == NULL: the reference's operator exactly (yko_dirac) */
+static int cg_any(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* b,
+                  double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr)
 {
     const int64_t n = (int64_t)Nt * Nx * 4;   /* complex entries */
     double* r = (double*)malloc(sizeof(double) * 2 * n);
@@ -198,8 +259,8 @@ int yko_cg(int Nt, int Nx, const yko_action* a, const double* sigma, const doubl
     const int second = (mtype == 1) ? 1 : 0;
     int k;
     for (k = 0; k < max_iter && sqrt(rmodsq) > stop; ++k) {
-        yko_dirac(Nt, Nx, a, sigma, p, t2, first);
-        yko_dirac(Nt, Nx, a, sigma, t2, t1, second);
+        yko_dirac_pi(Nt, Nx, a, sigma, pi, p, t2, first);
+        yko_dirac_pi(Nt, Nx, a, sigma, pi, t2, t1, second);
         cdot(n, p, t1, &re, &im);                    /* :133 */
         double ar, ai;
         cdiv(rmodsq, 0.0, re, im, &ar, &ai);         /* :137 alpha = rmodsq / <p,Ap> */
@@ -242,6 +303,49 @@ int yko_force(int Nt, int Nx, const yko_action* a, const double* sigma, const do
     }
     if (n_rhs > 1)
         for (int i = 0; i < V; ++i) F[i] /= (double)n_rhs;
+    free(xs); free(chi);
+    return iters;
+}
+
+/* Pion extension of the force (no reference counterpart; the sigma part is
+   FermionicDrift.cu:83-100 with the pion operator): with chi = D x and
+   x = (D^dag D)^-1 eta, F_sigma(n) = -g Re sum_c conj(chi_{n,c}) eta_{n,c} and
+   F_pi_a(n) = -g Re sum_c conj(chi_{n,c}) (i gamma5 tau_a eta)_{n,c}, the
+   one-noise estimates of -Re tr(D^-1 dD/dphi_a(n)); averaged over the
+   right-hand sides, times cutFraction^2 in rescaled mode.  F4: 4V doubles
+   (sigma, pi_1, pi_2, pi_3).  pi == NULL gives the sigma-only operator (the
+   pion forces are still estimated). */
+int yko_force_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* eta,
+                 int n_rhs, double tol, int tol_mode, int max_iter, double* F4)
+{
+    const int V = Nt * Nx;
+    const int64_t n = (int64_t)V * 4;
+    double* xs = (double*)malloc(sizeof(double) * 2 * n);
+    double* chi = (double*)malloc(sizeof(double) * 2 * n);
+    const double scale = (a->drift_mode == 1) ? a->cut_fraction * a->cut_fraction : 1.0;
+    int iters = 0;
+    for (int64_t i = 0; i < 4 * (int64_t)V; ++i) F4[i] = 0.0;
+    for (int j = 0; j < n_rhs; ++j) {
+        const double* e = eta + (int64_t)j * 2 * n;
+        iters += cg_any(Nt, Nx, a, sigma, pi, e, xs, 1, tol, tol_mode, max_iter, NULL);
+        yko_dirac_pi(Nt, Nx, a, sigma, pi, xs, chi, 0);     /* chi = D x */
+        for (int i = 0; i < V; ++i) {
+            const double* ch = chi + (int64_t)i * 8;
+            const double* es = e + (int64_t)i * 8;
+            double s = 0.0;
+            for (int c = 0; c < 4; ++c) s += ch[2 * c] * es[2 * c] + ch[2 * c + 1] * es[2 * c + 1];
+            F4[i] += -(scale * a->g) * s;
+            for (int q = 0; q < 3; ++q) {
+                double u[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                pion_site_add(es, u, q == 0 ? 1.0 : 0.0, q == 1 ? 1.0 : 0.0, q == 2 ? 1.0 : 0.0);
+                double sq = 0.0;
+                for (int c = 0; c < 4; ++c) sq += ch[2 * c] * u[2 * c] + ch[2 * c + 1] * u[2 * c + 1];
+                F4[(int64_t)(q + 1) * V + i] += -(scale * a->g) * sq;
+            }
+        }
+    }
+    if (n_rhs > 1)
+        for (int64_t i = 0; i < 4 * (int64_t)V; ++i) F4[i] /= (double)n_rhs;
     free(xs); free(chi);
     return iters;
 }
@@ -576,6 +680,77 @@ double yko_langevin_step(int Nt, int Nx, const yko_action* a, uint64_t seed, uin
         for (int i = 0; i < V; ++i) s2 += phi[i] * phi[i];
         obs[0] = eps; obs[1] = maxd; obs[2] = yko_sum(V, phi); obs[3] = yko_sum(V, F);
         obs[4] = (double)iters; obs[5] = s2;
+    }
+    free(w); free(xi); free(F); free(drift);
+    return eps;
+}
+
+/* One Langevin step of the pion extension (no reference counterpart): the
+   four fields phi4 = (sigma, pi_1, pi_2, pi_3), each V doubles, get their own
+   coloured noise (Philox kind 1, rhs 0 for sigma as in the sigma-only step,
+   rhs a for pi_a) and the drift
+     drift_a = F_a + phi_a (m^2 + lambda/6 |phi|^2) - Lap phi_a,
+   |phi|^2 = sigma^2 + pi^2 (the O(4)-symmetric form of PotentialAndMass,
+   langevin_gpu_v2.cu:9-27); max|drift| over all four fields sets the
+   adaptive eps; every field takes the Euler update of langevin_gpu_v2.cu:29-37.
+   At pi = 0 the sigma field moves exactly as in yko_langevin_step.
+   obs[0..9] = {eps, max_drift, sum sigma, sum F_sigma, cg_iters, sum sigma^2,
+   sum pi_1, sum pi_2, sum pi_3, sum |pi|^2}. */
+double yko_langevin_step_pi(int Nt, int Nx, const yko_action* a, uint64_t seed, uint32_t chain,
+                            uint64_t step, int n_rhs, double tol, int tol_mode, int max_iter,
+                            double fixed_dt, double* phi4, double* obs)
+{
+    const int V = Nt * Nx;
+    double* w = (double*)malloc(sizeof(double) * V);
+    double* xi = (double*)malloc(sizeof(double) * 4 * (size_t)V);
+    double* F = (double*)calloc(4 * (size_t)V, sizeof(double));
+    double* drift = (double*)malloc(sizeof(double) * 4 * (size_t)V);
+    for (int q = 0; q < 4; ++q) {
+        yko_normals(seed, chain, step, 1u, (uint32_t)q, V, w);
+        yko_coloured_noise(Nt, Nx, a->cut_fraction, w, xi + (size_t)q * V);
+    }
+    int iters = 0;
+    if (a->g != 0.0) {
+        const int64_t n = (int64_t)V * 4;
+        double* eta = (double*)calloc((size_t)(2 * n * n_rhs), sizeof(double));
+        double* re = (double*)malloc(sizeof(double) * n);
+        for (int j = 0; j < n_rhs; ++j) {
+            yko_normals(seed, chain, step, 2u, (uint32_t)j, n, re);
+            for (int64_t i = 0; i < n; ++i) eta[(int64_t)j * 2 * n + 2 * i] = re[i];
+        }
+        iters = yko_force_pi(Nt, Nx, a, phi4, phi4 + V, eta, n_rhs, tol, tol_mode, max_iter, F);
+        free(eta); free(re);
+    }
+    const double my_lambda = a->lambda / 6.0;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < V; ++i) {
+        const double s0 = phi4[i], p1 = phi4[V + i], p2 = phi4[2 * V + i], p3 = phi4[3 * V + i];
+        const double r2 = s0 * s0 + p1 * p1 + p2 * p2 + p3 * p3;
+        const int t = i / Nx, x = i % Nx;
+        int cols[5] = {i, ((t + 1) % Nt) * Nx + x, ((t - 1 + Nt) % Nt) * Nx + x,
+                       t * Nx + (x + 1) % Nx, t * Nx + (x - 1 + Nx) % Nx};
+        qsort(cols, 5, sizeof(int), cmp_int);
+        for (int q = 0; q < 4; ++q) {
+            const double* f = phi4 + (size_t)q * V;
+            double d = F[(size_t)q * V + i];
+            d += f[i] * (a->m2 + my_lambda * r2);
+            double out = 0.0;
+            for (int j = 0; j < 5; ++j) out += (cols[j] != i ? 1.0 : -4.0) * f[cols[j]];
+            drift[(size_t)q * V + i] = d - out;
+        }
+    }
+    double maxd;
+    const double eps = yko_euler_update(4 * V, a->eps_bar, fixed_dt, phi4, drift, xi, &maxd);
+    if (obs) {
+        double s2 = 0.0, p2 = 0.0;
+        for (int i = 0; i < V; ++i) {
+            s2 += phi4[i] * phi4[i];
+            p2 += phi4[V + i] * phi4[V + i] + phi4[2 * V + i] * phi4[2 * V + i] + phi4[3 * V + i] * phi4[3 * V + i];
+        }
+        obs[0] = eps; obs[1] = maxd; obs[2] = yko_sum(V, phi4); obs[3] = yko_sum(V, F);
+        obs[4] = (double)iters; obs[5] = s2;
+        obs[6] = yko_sum(V, phi4 + V); obs[7] = yko_sum(V, phi4 + 2 * V); obs[8] = yko_sum(V, phi4 + 3 * V);
+        obs[9] = p2;
     }
     free(w); free(xi); free(F); free(drift);
     return eps;

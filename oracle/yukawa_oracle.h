@@ -98,6 +98,22 @@ double yko_langevin_step(int Nt, int Nx, const yko_action* a, uint64_t seed, uin
                          uint64_t step, int n_rhs, double tol, int tol_mode, int max_iter,
                          double fixed_dt, double* phi, double* obs);
 
+/* Pion extension (no reference counterpart; the reference is sigma-only,
+ * params.h:25, Dirac.cu:57-69): Yukawa term g (sigma + i gamma5 tau.pi),
+ * gamma5 = -i gamma_t gamma_x = sigma_2, pi = 3 fields of V doubles
+ * (component-major).  pi == NULL gives the sigma-only operator. */
+void yko_dirac_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi,
+                  const double* in, double* out, int dagger);
+int yko_cg_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* b,
+              double* x, int mtype, double tol, int tol_mode, int max_iter, double* final_rr);
+/* F4: 4V doubles: F_sigma, F_pi1, F_pi2, F_pi3 (see yukawa_oracle.c). */
+int yko_force_pi(int Nt, int Nx, const yko_action* a, const double* sigma, const double* pi, const double* eta,
+                 int n_rhs, double tol, int tol_mode, int max_iter, double* F4);
+/* One step of the four fields phi4 = (sigma, pi1, pi2, pi3); obs[0..9]. */
+double yko_langevin_step_pi(int Nt, int Nx, const yko_action* a, uint64_t seed, uint32_t chain,
+                            uint64_t step, int n_rhs, double tol, int tol_mode, int max_iter,
+                            double fixed_dt, double* phi4, double* obs);
+
 /* Wolff's Gamma-method (U. Wolff, Comput. Phys. Commun. 156 (2004) 143), S_tau = 1.5:
  * out = {mean, error, error_of_error, tau_int, tau_int_error}. */
 void yko_gamma_method(const double* data, int64_t n, double stau, double out[5]);

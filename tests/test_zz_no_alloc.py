@@ -3,8 +3,10 @@
 Collected last on purpose: it must pass both alone and after every other
 test of the session.  Two consecutive calls of the static entry point on the
 same inputs must each agree with the context solve to 1e-12 relative (same
-algorithm, same arithmetic: the results are expected to be identical), and
-a lattice beyond the static scratch is refused with YK_EINVAL.
+algorithm, same arithmetic: the results are expected to be identical).  The
+free device memory (cudaMemGetInfo) must not move across the second call,
+and across the first only by the library's fixed scratch array.  A lattice
+beyond the static scratch is refused with YK_EINVAL.
 """
 import ctypes as C
 
@@ -12,6 +14,10 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+# the static scratch array (6.6 MB) rounded up to the 2 MiB granularity of
+# device memory, plus one more granule for the module that holds it
+STATIC_BYTES_BOUND = 10 << 20
 
 
 def _params(yk, Nt, Nx):
@@ -36,8 +42,11 @@ def test_static_solve_matches_context_solve(ylib, cuda, Nt, Nx, mtype):
         ctx.synchronize()
         want = x_ctx.cpu().numpy()
         stream = torch.cuda.current_stream().cuda_stream
+        outs = [torch.full_like(bd, float("nan")) for _ in range(2)]   # every buffer allocated up front
+        torch.cuda.synchronize()
+        free = [torch.cuda.mem_get_info()[0]]
         for call in range(2):
-            x = torch.full_like(bd, float("nan"))
+            x = outs[call]
             st = yk.SolveStats()
             rc = yk.lib().yk_cg_solve_static(C.c_void_p(ctx.field_ptr()), Nt, Nx, a.m0, a.g, a.r,
                                              C.c_void_p(bd.data_ptr()), C.c_void_p(x.data_ptr()), mtype, 1e-12,
@@ -47,6 +56,13 @@ def test_static_solve_matches_context_solve(ylib, cuda, Nt, Nx, mtype):
             err = np.abs(got - want).max() / np.abs(want).max()
             assert err < 1e-12, (call, err)
             assert st.converged == 1 and st.iterations == st_ctx.iterations, (call, st.iterations)
+            free.append(torch.cuda.mem_get_info()[0])
+        # no device memory taken by the entry point: the second call leaves the
+        # free memory exactly as the first left it; the first may only add the
+        # library's fixed scratch array (about 6.6 MB), when the CUDA loader
+        # brings its module in lazily at that call
+        assert free[2] == free[1], free
+        assert 0 <= free[0] - free[1] <= STATIC_BYTES_BOUND, free
 
 
 def test_static_solve_refuses_large_lattice(ylib, cuda):

@@ -135,6 +135,43 @@ __device__ __forceinline__ Site<R, K> dirac_combine(const Site<R, K>& c, const S
     return o;
 }
 
+// Pion term of the Yukawa coupling (no reference counterpart: the reference is
+// sigma-only, code/src/params.h:25, Dirac.cu:57-69).  With the pions the site
+// term is g (sigma + i gamma5 tau.pi), gamma5 = -i gamma_t gamma_x = sigma_2,
+// so i gamma5 = [[0, 1], [-1, 0]] on spin and tau.s = [[s3, s1 - i s2],
+// [s1 + i s2, -s3]] on flavour:  o += (i gamma5 tau.s) c  for s = +-g pi(n)
+// (D: +g, D^dag: -g).  Complex sites (K = 2) only: tau_2 makes D complex.
+template <typename R>
+__device__ __forceinline__ void pion_add(Site<R, 2>& o, const Site<R, 2>& c, R s1, R s2, R s3)
+{
+#pragma unroll
+    for (int sp = 0; sp < 2; ++sp) {
+        // w_f = i sigma_2 c_f: (w_f)_0 = c_{f,1}, (w_f)_1 = -c_{f,0}
+        const int src = sp == 0 ? 1 : 0;
+        const R sgn = sp == 0 ? R(1) : R(-1);
+        const R ar = sgn * c.v[(0 + src) * 2], ai = sgn * c.v[(0 + src) * 2 + 1];   // w_1 (flavour 1)
+        const R br = sgn * c.v[(2 + src) * 2], bi = sgn * c.v[(2 + src) * 2 + 1];   // w_2 (flavour 2)
+        o.v[(0 + sp) * 2] += s3 * ar + (s1 * br + s2 * bi);
+        o.v[(0 + sp) * 2 + 1] += s3 * ai + (s1 * bi - s2 * br);
+        o.v[(2 + sp) * 2] += (s1 * ar - s2 * ai) - s3 * br;
+        o.v[(2 + sp) * 2 + 1] += (s1 * ai + s2 * ar) - s3 * bi;
+    }
+}
+
+// The pion term at site n of a V-site lattice with pions pi[a * V + n] (a < 3);
+// no-op for real sites or without pions.
+template <typename R, int K>
+__device__ __forceinline__ void pion_term(Site<R, K>& o, const Site<R, K>& c, const double* __restrict__ pi, int n,
+                                          int V, double g, bool dag)
+{
+    if constexpr (K == 2) {
+        if (pi) {
+            const double sg = dag ? -g : g;
+            pion_add<R>(o, c, (R)(sg * pi[n]), (R)(sg * pi[V + n]), (R)(sg * pi[2 * V + n]));
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (J. Salmon et al., "Parallel random numbers: as easy as
 // 1, 2, 3", SC'11) with the framework's counter scheme:

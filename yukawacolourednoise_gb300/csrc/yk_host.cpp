@@ -344,6 +344,12 @@ int yk_params_from_toml(const char* path, yk_params* p)
         p->init = (v == "philox") ? YK_INIT_PHILOX : (v == "none" ? YK_INIT_NONE : YK_INIT_DRAND48);
     }
     get_i(kv, "gpu.learned_layers", &p->learned_layers);
+    // a network has 2..8 layers (yk_net_setup); refuse other values here,
+    // before a run spends its thermalisation on a setting it cannot use
+    if (p->learned_layers != 0 && (p->learned_layers < 2 || p->learned_layers > 8)) {
+        yk::set_error("yk_params_from_toml: gpu.learned_layers = %d (0 for off, or 2..8)", p->learned_layers);
+        return YK_EINVAL;
+    }
     return YK_OK;
 }
 

@@ -44,6 +44,7 @@ struct SysDev {
     int tile0, ntiles;   // tiles of this system in the tile table
     double m0, g, r;     // Dirac parameters of the chain
     const double* sigma; // the chain's scalar field
+    const double* pi;    // the chain's pions (3 x V doubles) on complex systems, or null
     // FP64 vectors (K real planes per spinor entry)
     double* b;           // right-hand side (eta)
     double* x;           // solution

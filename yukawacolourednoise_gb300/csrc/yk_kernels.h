@@ -10,9 +10,10 @@ namespace yk {
 
 // Wilson-Dirac apply on one lattice (K real planes per entry; K = 2 for
 // interleaved complex buffers).  prec YK_FP64 (double) or YK_FP32 (float).
+// pi: the chain's pions (3 x V doubles) or null for the sigma-only operator.
 cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt, int Nx,
                          double m0, double g, double r, int dagger, int prec, int K,
-                         cudaStream_t stream);
+                         cudaStream_t stream, const double* pi = nullptr);
 
 // Batched CG (yk_cg.cu).  Also launches its one-block preparation kernel.
 // grid_out: blocks launched; kernel_out: 0 cg_kernel, 1 cg_halo_kernel (either may be null)

@@ -52,6 +52,37 @@ static __device__ __align__(256) unsigned char g_cg_scratch[kStaticScratchBytes]
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 unsigned char* g_base[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};   // context the address of g_base[dev] belongs to
+
+// Unique id of the calling thread's current context (0 if unavailable).  A
+// cudaDeviceReset() ends the device's primary context; the module is loaded
+// again into the next one, possibly at another address, and that context has
+// a new id.  The driver functions are reached through the runtime, so the
+// library needs no link against libcuda.
+unsigned long long current_context_id()
+{
+    typedef int (*CtxGetCurrent)(void**);
+    typedef int (*CtxGetId)(void*, unsigned long long*);
+    static CtxGetCurrent get_current = nullptr;
+    static CtxGetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetId>(f);
+        looked_up = true;
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 // The system record and tile table of one lattice, written on the device.
 __global__ void static_setup_kernel(unsigned char* base, const double* sigma, const double* b, double* x, int Nt,
@@ -87,7 +118,8 @@ __global__ void static_setup_kernel(unsigned char* base, const double* sigma, co
     }
 }
 
-// Device address of the array on the current device (looked up once per device).
+// Device address of the array on the current device: looked up once per device
+// and again after the device's context changed (a cudaDeviceReset).
 int scratch_base(unsigned char** out)
 {
     int dev = 0;
@@ -100,8 +132,15 @@ int scratch_base(unsigned char** out)
         set_error("yk_cg_solve_static: device %d beyond the %d supported", dev, kMaxDevices);
         return YK_EINVAL;
     }
+    // makes the device's primary context current (creating it if a reset ended it)
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        set_error("yk_cg_solve_static: cudaSetDevice failed: %s", cudaGetErrorString(e));
+        return YK_ECUDA;
+    }
+    const unsigned long long ctx_id = current_context_id();
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_base[dev]) {
+    if (!g_base[dev] || ctx_id != g_ctx_id[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_cg_scratch);
         if (e != cudaSuccess || !p) {
@@ -109,6 +148,7 @@ int scratch_base(unsigned char** out)
             return YK_ECUDA;
         }
         g_base[dev] = static_cast<unsigned char*>(p);
+        g_ctx_id[dev] = ctx_id;
     }
     *out = g_base[dev];
     return YK_OK;

@@ -174,6 +174,9 @@ int yk_run_toml(const char* toml_path, const char* out_dir)
     double t_blk = 0.0, eps_last = p.average_epsilon;
     for (int burn = 0; burn < p.burn_count && rc == YK_OK; ++burn) rc = export_block(t_blk, eps_last);
     if (rc == YK_OK) std::printf("Thermalization done!\n");
+    if (rc == YK_OK && p.learned_layers > 0 && p.yukawa_coupling == 0.0)
+        std::printf("Learned preconditioner: not used (gpu.learned_layers = %d, but yukawa_coupling = 0: "
+                    "no fermion solves)\n", p.learned_layers);
     if (rc == YK_OK && p.learned_layers > 0 && p.yukawa_coupling != 0.0) {
         rc = yk_net_setup(ctx, 0, p.learned_layers, 7, -1.0);
         yk_net_train_cfg cfg = {4, 5, 4, 400, 4, 2e-3, 3};
