@@ -88,6 +88,9 @@ typedef struct yk_params {
     int learned_layers;        /* yk_run: > 0 trains a network of that many layers */
                                /*   after thermalisation and runs the measurement  */
                                /*   steps with yk_langevin_step_learned (0: off)   */
+    int pions;                 /* 1: the pion extension (fields pi_1..3 and the  */
+                               /*   Yukawa term g (sigma + i gamma5 tau.pi));    */
+                               /*   0: the reference's sigma-only model          */
 } yk_params;
 
 /* Parameters after the reference's conversion (main.cu:58-63, 113-170). */
@@ -118,6 +121,8 @@ typedef struct yk_obs {
     int64_t cg_iterations_total; /* CG iterations of all steps of this chain       */
     int64_t noconv_steps;      /* steps whose CG hit its iteration cap            */
     int status;                /* yk_status of the last step                      */
+    double sum_pi[3];          /* pion extension: sum_n pi_a(n) after the step    */
+    double sum_pi2;            /*   sum_n |pi(n)|^2 (zero without pions)          */
 } yk_obs;
 
 typedef struct yk_ctx yk_ctx;
@@ -150,6 +155,31 @@ int yk_set_field_host(yk_ctx* ctx, int chain, const double* phi);
 int yk_get_field_host(yk_ctx* ctx, int chain, double* phi);
 /* Device pointer of the chain's field (V doubles), owned by the context. */
 int yk_field_device(yk_ctx* ctx, int chain, double** phi);
+
+/* Pion extension (no reference counterpart: the reference's model has the one
+ * scalar sigma, code/src/params.h:25, and the real Yukawa diagonal g sigma,
+ * Dirac.cu:57-69).  A context created with params.pions = 1 (every chain)
+ * carries three more fields pi_1..3 per chain, initialised iid
+ * Uniform[-1, 1] from Philox (stream kind 0, rhs a) unless init is
+ * YK_INIT_NONE (zeros), and the Yukawa term becomes
+ * g (sigma + i gamma5 tau.pi) with gamma5 = -i gamma_t gamma_x = sigma_2 on
+ * spin and the Pauli matrices tau on flavour; D^dag carries
+ * g (sigma - i gamma5 tau.pi).  With pions:
+ *   - yk_dirac_apply, yk_cg_solve and yk_correlator use that operator;
+ *   - yk_fermion_force writes 4V doubles: F_sigma, F_pi1, F_pi2, F_pi3,
+ *     F_a(n) = -g Re sum_c conj(chi_c) (dD/dphi_a(n) / g eta)_c;
+ *   - yk_langevin_step moves the four fields, each with its own coloured
+ *     noise (Philox kind 1, rhs a), by the drift
+ *     F_a + phi_a (m^2 + lambda/6 |phi|^2) - Lap phi_a, with max|drift| over
+ *     the four fields in the adaptive step; yk_obs gains sum_pi, sum_pi2;
+ *   - the learned preconditioner, yk_euler_update and the kernel profile
+ *     (real sigma-only operator) return YK_EINVAL.
+ * At pi = 0 the operator is the reference's, bit for bit.
+ * pi: 3V doubles, component-major (pi[a*V + n]); host buffers. */
+int yk_set_pions_host(yk_ctx* ctx, int chain, const double* pi);
+int yk_get_pions_host(yk_ctx* ctx, int chain, double* pi);
+/* Device pointer of the chain's pions (3V doubles), owned by the context. */
+int yk_pions_device(yk_ctx* ctx, int chain, double** pi);
 
 /* ------------------------------------------------------------- operators */
 /* DiracOP<double>::applyD(in, out, MatrixType) (code/src/Dirac.cuh:22,
@@ -367,6 +397,36 @@ int yk_checkpoint_load(yk_ctx* ctx, int chain, const char* path, double* eps_bar
 /* Wolff Gamma-method (analysis/AutoCorrelation/ac.cpp:73-181, Wrapper :183-190):
  * out = {mean, error, error of error, tau_int, tau_int error}; host buffers. */
 int yk_gamma_method(const double* data, int64_t n, double stau, double* out5);
+
+/* Observables of a time series of per-configuration <sigma> values with
+ * Gamma-method errors, computed on the GPU (the reference analyses its
+ * traces.csv offline: analysis/functions.py:42-78 with the Gamma-method of
+ * analysis/AutoCorrelation/ac.cpp:73-181).  Each entry holds {value, error,
+ * error of the error, tau_int, tau_int error}:
+ *   sigma      <s>                                  (functions.py:42-45)
+ *   abs_sigma  <|s|>                                (:47-49)
+ *   chi        V <(s - <s>)^2>, error of that mean  (:54-57)
+ *   binder     1 - <s^4> / (3 <s^2>^2), Wolff's derived-quantity error
+ *              (U. Wolff, Comput. Phys. Commun. 156 (2004) 143)  (:73-78)
+ * Gamma(t) is summed on the device for t <= min(n / 2, 8192). */
+typedef struct yk_series_stats {
+    int64_t n;
+    double sigma[5];
+    double abs_sigma[5];
+    double chi[5];
+    double binder[5];
+} yk_series_stats;
+/* Records <sigma> = sum_n sigma_n / V after every step of the chain (the
+ * update kernel appends it on the device; graph-replayed steps included) into
+ * a new device series of `capacity` values; capacity 0 stops and frees. */
+int yk_series_record(yk_ctx* ctx, int chain, int64_t capacity);
+/* Copies the recorded values (at most cap) to host memory; *n = how many. */
+int yk_series_read(yk_ctx* ctx, int chain, double* host, int64_t cap, int64_t* n);
+/* yk_series_stats of the recorded series (stau: Wolff's S_tau, 1.5). */
+int yk_series_analyse(yk_ctx* ctx, int chain, double stau, yk_series_stats* out);
+/* The same analysis of a host series of n values on a volume-site lattice
+ * (e.g. the sigma column of a traces.csv); runs on the current device. */
+int yk_series_analyse_host(const double* series, int64_t n, int64_t volume, double stau, yk_series_stats* out);
 
 /* The full reference run protocol of main.cu:73-516 (burn-in, epsBar
  * measurement, export loop, slice.dat / data.csv / traces.csv and stdout)

@@ -45,6 +45,7 @@ def lib():
             "yko_philox4x32_10": (None, [P, P, P]),
             "yko_normals": (None, [u64, u32, u64, u32, u32, i64, P]),
             "yko_uniform_field": (None, [u64, u32, i64, P]),
+            "yko_uniform_field_comp": (None, [u64, u32, u32, i64, P]),
             "yko_drand48_field": (None, [i64, P]),
             "yko_langevin_step": (d, [i, i, A, u64, u32, u64, i, d, i, i, d, P, P]),
             "yko_gamma_method": (None, [P, i64, d, P]),
@@ -179,6 +180,14 @@ def normals(seed, chain, step, kind, rhs, n):
 def uniform_field(seed, chain, n):
     out = np.empty(n)
     lib().yko_uniform_field(seed, chain, n, _p(out))
+    return out
+
+
+def uniform_pions(seed, chain, n):
+    """The pion extension's initial pions (3, n): Philox uniform, comp 1..3."""
+    out = np.empty((3, n))
+    for a in range(3):
+        lib().yko_uniform_field_comp(seed, chain, a + 1, n, _p(out[a]))
     return out
 
 

@@ -621,8 +621,14 @@ void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, ui
 
 void yko_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out)
 {
+    yko_uniform_field_comp(seed, chain, 0u, n, out);
+}
+
+/* comp 0: sigma; comp a (1..3): the pion field pi_a of the pion extension */
+void yko_uniform_field_comp(uint64_t seed, uint32_t chain, uint32_t comp, int64_t n, double* out)
+{
     uint32_t key[2], ctr0[4];
-    scheme_key_ctr(seed, chain, 0, 0u, 0u, key, ctr0);
+    scheme_key_ctr(seed, chain, 0, 0u, comp, key, ctr0);
     for (int64_t e = 0; e < (n + 1) / 2; ++e) {
         uint32_t ctr[4] = {(uint32_t)e, ctr0[1], ctr0[2], ctr0[3]}, o[4];
         yko_philox4x32_10(ctr, key, o);

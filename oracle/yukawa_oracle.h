@@ -88,6 +88,7 @@ void yko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
                  int64_t n, double* out);
 void yko_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out);
+void yko_uniform_field_comp(uint64_t seed, uint32_t chain, uint32_t comp, int64_t n, double* out);
 /* The reference's initial field 1 - 2*drand48() from glibc's default drand48 state (main.cu:92-95). */
 void yko_drand48_field(int64_t n, double* out);
 

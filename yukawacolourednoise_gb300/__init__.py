@@ -56,7 +56,7 @@ class Params(C.Structure):
         ("Nt", C.c_int), ("Nx", C.c_int),
         ("precision", C.c_int), ("n_rhs", C.c_int), ("cg_tol_mode", C.c_int), ("cg_tol", C.c_double),
         ("cg_max_iter", C.c_int), ("reliable_every", C.c_int), ("reliable_delta", C.c_double),
-        ("fixed_dt", C.c_double), ("init", C.c_int), ("learned_layers", C.c_int),
+        ("fixed_dt", C.c_double), ("init", C.c_int), ("learned_layers", C.c_int), ("pions", C.c_int),
     ]
 
     @classmethod
@@ -118,7 +118,16 @@ class Obs(C.Structure):
     _fields_ = [("t", C.c_double), ("eps", C.c_double), ("max_drift", C.c_double), ("sum_phi", C.c_double),
                 ("sum_phi2", C.c_double), ("sum_force", C.c_double), ("steps", C.c_int64),
                 ("cg_iterations", C.c_int), ("cg_iterations_total", C.c_int64), ("noconv_steps", C.c_int64),
-                ("status", C.c_int)]
+                ("status", C.c_int), ("sum_pi", C.c_double * 3), ("sum_pi2", C.c_double)]
+
+
+class SeriesStats(C.Structure):
+    """yk_series_stats: each field {value, error, error of error, tau_int, tau_int error}."""
+    _fields_ = [("n", C.c_int64), ("sigma", C.c_double * 5), ("abs_sigma", C.c_double * 5),
+                ("chi", C.c_double * 5), ("binder", C.c_double * 5)]
+
+    def as_dict(self):
+        return {k: list(getattr(self, k)) for k in ("sigma", "abs_sigma", "chi", "binder")} | {"n": self.n}
 
 
 class Profile(C.Structure):
@@ -148,6 +157,9 @@ _SIGS = {
     "yk_set_field_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "yk_get_field_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "yk_field_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "yk_set_pions_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "yk_get_pions_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "yk_pions_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "yk_dirac_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "yk_cg_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
                               C.c_int, C.c_int, C.POINTER(SolveStats)]),
@@ -187,6 +199,10 @@ _SIGS = {
     "yk_checkpoint_load": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.POINTER(C.c_double)]),
     "yk_gamma_method": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
     "yk_run_toml": (C.c_int, [C.c_char_p, C.c_char_p]),
+    "yk_series_record": (C.c_int, [C.c_void_p, C.c_int, C.c_int64]),
+    "yk_series_read": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "yk_series_analyse": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(SeriesStats)]),
+    "yk_series_analyse_host": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.POINTER(SeriesStats)]),
 }
 
 
@@ -282,6 +298,24 @@ class Context:
         a = np.empty(self.volume(chain))
         _check(lib().yk_get_field_host(self.h, chain, a.ctypes.data_as(C.c_void_p)))
         return a
+
+    def set_pions(self, pi, chain=0):
+        """Pion extension: the chain's pi_1..3, shape (3, V)."""
+        import numpy as np
+        a = np.ascontiguousarray(pi, dtype=np.float64)
+        assert a.size == 3 * self.volume(chain)
+        _check(lib().yk_set_pions_host(self.h, chain, a.ctypes.data_as(C.c_void_p)))
+
+    def get_pions(self, chain=0):
+        import numpy as np
+        a = np.empty(3 * self.volume(chain))
+        _check(lib().yk_get_pions_host(self.h, chain, a.ctypes.data_as(C.c_void_p)))
+        return a.reshape(3, -1)
+
+    def pions_ptr(self, chain=0) -> int:
+        p = C.c_void_p()
+        _check(lib().yk_pions_device(self.h, chain, C.byref(p)))
+        return p.value
 
     def field_ptr(self, chain=0) -> int:
         p = C.c_void_p()
@@ -428,6 +462,24 @@ class Context:
     def set_step(self, step, chain=0):
         _check(lib().yk_set_step(self.h, chain, step))
 
+    def series_record(self, capacity, chain=0):
+        """Record <sigma> after every step on the device (capacity 0 stops)."""
+        _check(lib().yk_series_record(self.h, chain, int(capacity)))
+
+    def series_read(self, chain=0, cap=1 << 24):
+        import numpy as np
+        n = C.c_int64()
+        _check(lib().yk_series_read(self.h, chain, None, 0, C.byref(n)))
+        have = C.c_int64()
+        buf = np.empty(max(1, min(cap, 1 << 24)))
+        _check(lib().yk_series_read(self.h, chain, buf.ctypes.data_as(C.c_void_p), buf.size, C.byref(have)))
+        return buf[:have.value].copy()
+
+    def series_analyse(self, stau=1.5, chain=0) -> SeriesStats:
+        st = SeriesStats()
+        _check(lib().yk_series_analyse(self.h, chain, stau, C.byref(st)))
+        return st
+
     def checkpoint_save(self, path, eps_bar, chain=0):
         _check(lib().yk_checkpoint_save(self.h, chain, str(path).encode(), eps_bar))
 
@@ -491,6 +543,15 @@ def gamma_method(data, stau=1.5):
     out = np.zeros(5)
     _check(lib().yk_gamma_method(d.ctypes.data_as(C.c_void_p), d.size, stau, out.ctypes.data_as(C.c_void_p)))
     return tuple(out)
+
+
+def series_stats(series, volume, stau=1.5) -> SeriesStats:
+    """yk_series_analyse_host: <sigma>, <|sigma|>, chi, Binder with Gamma-method errors (GPU)."""
+    import numpy as np
+    a = np.ascontiguousarray(series, dtype=np.float64)
+    st = SeriesStats()
+    _check(lib().yk_series_analyse_host(a.ctypes.data_as(C.c_void_p), a.size, int(volume), stau, C.byref(st)))
+    return st
 
 
 def run(toml_path, out_dir="."):

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -85,6 +86,15 @@ struct Chain {
     Workspace ws;
     LearnedNet* net = nullptr;   // the learned preconditioner (yk_net_setup)
     LearnedNet* pcg_ws = nullptr;   // solver buffers of identity-preconditioned solves without a network
+    // pion extension (params.pions): the fields pi_1..3 (3V), their coloured
+    // and white noise (3V each), the four forces (4V), the pions' drift (3V),
+    // the step's complex sources (n_rhs_pion x 8V) and per-tile sums
+    double* series = nullptr;    // recorded per-step <sigma> (yk_series_record)
+    int64_t series_cap = 0;
+    bool pions = false;
+    int n_rhs_pion = 0;          // complex systems per step (0 when g == 0)
+    double *pi = nullptr, *pi_xi = nullptr, *pi_white = nullptr, *pforce = nullptr, *pdrift = nullptr;
+    double *peta = nullptr, *ptile = nullptr, *ptile_f = nullptr;
 };
 
 }  // namespace
@@ -161,6 +171,12 @@ struct yk_ctx {
     std::vector<cudaEvent_t> pool;
     int prof_steps = 0, prof_launches = 0;
     std::vector<int64_t> prof_iters0;
+    // pion extension: every chain carries pions; the chains' pion buffers and,
+    // per pion field a, a copy of every chain record whose xi is that field's
+    // noise (d_pchains[a * n_chains + c]) for the FFT passes
+    bool pions = false;
+    void* pion_mem = nullptr;
+    ChainDev* d_pchains = nullptr;
 };
 
 namespace {
@@ -215,6 +231,20 @@ int check_params(const yk_params& p, int c)
     }
     if (p.reliable_every < 0 || !(p.reliable_delta > 0.0 && p.reliable_delta < 1.0)) {
         set_error("chain %d: reliable_every must be >= 0 and reliable_delta in (0, 1)", c);
+        return YK_EINVAL;
+    }
+    if (p.pions != 0 && p.pions != 1) {
+        set_error("chain %d: pions must be 0 or 1", c);
+        return YK_EINVAL;
+    }
+    return YK_OK;
+}
+
+// Calls that act on the real sigma-only operator refuse contexts with pions.
+int no_pions(const yk_ctx* ctx, const char* what)
+{
+    if (ctx && ctx->pions) {
+        set_error("%s: not available with pions (it acts on the real sigma-only operator)", what);
         return YK_EINVAL;
     }
     return YK_OK;
@@ -446,6 +476,7 @@ int ensure_ws(yk_ctx* ctx, int c, int R)
         S.g = C.a.g;
         S.r = C.a.r;
         S.sigma = C.phi;
+        S.pi = C.pions ? C.pi : nullptr;
         const size_t* o = &o_vec[(size_t)j * NVEC];
         S.x = ar.at<double>(o[0]);
         S.r64[0] = ar.at<double>(o[1]);
@@ -668,6 +699,111 @@ StepArgs chain_step_args(yk_ctx* ctx, int c)
     return s;
 }
 
+// ---------------------------------------------------------------- pions
+// Buffers of the pion extension (one allocation for every chain), the initial
+// pions (iid Uniform[-1, 1] from Philox stream kind 0, rhs a, or zeros for
+// YK_INIT_NONE) and the per-field chain records of the noise passes.
+int pion_setup(yk_ctx* ctx)
+{
+    const int nch = (int)ctx->ch.size();
+    Arena ar;
+    struct POff {
+        size_t pi, xi, white, force, drift, eta, tile, tilef;
+    };
+    std::vector<POff> po(nch);
+    const size_t o_pch = ar.reserve(sizeof(ChainDev) * 3 * (size_t)nch);
+    for (int c = 0; c < nch; ++c) {
+        const Chain& C = ctx->ch[c];
+        const size_t V = C.V, nt = ntiles_of(C.V);
+        po[c].pi = ar.reserve(8 * 3 * V);
+        po[c].xi = ar.reserve(8 * 3 * V);
+        po[c].white = ar.reserve(8 * 3 * V);
+        po[c].force = ar.reserve(8 * 4 * V);
+        po[c].drift = ar.reserve(8 * 3 * V);
+        po[c].eta = ar.reserve(8 * 8 * V * (size_t)std::max(C.n_rhs_pion, 1));
+        po[c].tile = ar.reserve(8 * 6 * nt);
+        po[c].tilef = ar.reserve(8 * nt);
+    }
+    if (cudaMalloc(&ctx->pion_mem, ar.used) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("pion allocation of %zu bytes failed", ar.used);
+        return YK_ENOMEM;
+    }
+    ar.base = (char*)ctx->pion_mem;
+    YK_CK(cudaMemsetAsync(ctx->pion_mem, 0, ar.used, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    ctx->d_pchains = ar.at<ChainDev>(o_pch);
+    std::vector<ChainDev> pch(3 * (size_t)nch);
+    for (int c = 0; c < nch; ++c) {
+        Chain& C = ctx->ch[c];
+        C.pi = ar.at<double>(po[c].pi);
+        C.pi_xi = ar.at<double>(po[c].xi);
+        C.pi_white = ar.at<double>(po[c].white);
+        C.pforce = ar.at<double>(po[c].force);
+        C.pdrift = ar.at<double>(po[c].drift);
+        C.peta = ar.at<double>(po[c].eta);
+        C.ptile = ar.at<double>(po[c].tile);
+        C.ptile_f = ar.at<double>(po[c].tilef);
+        std::vector<double> pi(3 * (size_t)C.V, 0.0);
+        if (C.p.init != YK_INIT_NONE)
+            for (int a = 0; a < 3; ++a)
+                philox_uniform_field((uint64_t)C.p.seed, (uint32_t)c, C.V, pi.data() + (size_t)a * C.V,
+                                     (uint32_t)(a + 1));
+        YK_CK(cudaMemcpy(C.pi, pi.data(), sizeof(double) * pi.size(), cudaMemcpyHostToDevice));
+        for (int a = 0; a < 3; ++a) {
+            ChainDev H = ctx->h_chains[c];
+            H.xi = C.pi_xi + (size_t)a * C.V;
+            pch[(size_t)a * nch + c] = H;
+        }
+    }
+    YK_CK(cudaMemcpy(ctx->d_pchains, pch.data(), sizeof(ChainDev) * pch.size(), cudaMemcpyHostToDevice));
+    return YK_OK;
+}
+
+// The complex systems of a pion chain: sources eta (device, n_rhs x 8V) or,
+// when null, Philox stream `kind` at the chain's current step; solved with
+// the pion operator on the chain's workspace.
+int pion_solve(yk_ctx* ctx, int c, int kind, const double* eta, int precision, yk_solve_stats* stats)
+{
+    Chain& C = ctx->ch[c];
+    const int R = C.n_rhs_pion;
+    if (R == 0) {
+        if (stats) *stats = yk_solve_stats{0, 0, 0.0, 0.0, 1};
+        return YK_OK;
+    }
+    if (int rc = ensure_ws(ctx, c, R)) return rc;
+    Workspace& w = C.ws;
+    if (!eta) {
+        YK_CK(launch_pion_eta(ctx->d_chains + c, C.peta, R, kind, C.V, ctx->stream));
+        eta = C.peta;
+    }
+    for (int j = 0; j < R; ++j) w.h_sys[j].b = const_cast<double*>(eta) + (size_t)j * 8 * C.V;
+    return ws_solve(ctx, c, R, YK_DAGGER, ctx->tol, ctx->tol_mode, ctx->max_iter, precision, stats);
+}
+
+// One Langevin step of pion chain c: four coloured noises, the complex solves,
+// the four forces, drift and update (yk_pion.cu).  The solves report their
+// statistics to the host, so the step is driven from the host (no graph).
+int pion_step(yk_ctx* ctx, int c)
+{
+    Chain& C = ctx->ch[c];
+    const int nch = (int)ctx->ch.size();
+    const NoiseTables nt = {ctx->d_rows + C.row0, C.nrows, ctx->d_cols + C.col0, C.ncols, ctx->d_white + C.white0,
+                            C.nwhite};
+    YK_CK(launch_noise_tables(ctx->d_chains, nt, ctx->max_nx, ctx->max_cols, nullptr, ctx->stream));
+    YK_CK(launch_pion_white(ctx->d_chains + c, C.pi_white, C.V, ctx->stream));
+    for (int a = 0; a < 3; ++a)
+        YK_CK(launch_noise_tables(ctx->d_pchains + (size_t)a * nch, nt, ctx->max_nx, ctx->max_cols,
+                                  C.pi_white + (size_t)a * C.V, ctx->stream));
+    const int rc = pion_solve(ctx, c, 2, nullptr, ctx->precision, nullptr);
+    if (rc && rc != YK_ENOCONV) return rc;
+    const int R = C.n_rhs_pion;
+    YK_CK(launch_pion_force(ctx->d_chains + c, C.ws.d_sys, R, C.pi, C.pforce, C.V, ctx->stream));
+    YK_CK(launch_pion_drift_update(ctx->d_chains + c, C.pi, C.pforce, C.pdrift, C.pi_xi, C.ptile, C.ptile_f,
+                                   C.ws.d_state, R, C.V, ctx->stream));
+    return YK_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -692,6 +828,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             set_error("chains of one context must share precision and CG settings");
             return YK_EINVAL;
         }
+        if (p.pions != p0.pions) {
+            set_error("chains of one context must all carry pions or none");
+            return YK_EINVAL;
+        }
     }
     std::unique_ptr<yk_ctx> ctx(new yk_ctx());
     YK_CK(cudaGetDevice(&ctx->dev));
@@ -702,6 +842,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
     YK_CK(cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming));
     YK_CK(cudaEventCreateWithFlags(&ctx->join2_ev, cudaEventDisableTiming));
     YK_CK(cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, ctx->dev));
+    ctx->pions = p0.pions != 0;
     ctx->precision = p0.precision;
     ctx->tol_mode = p0.cg_tol_mode;
     ctx->tol = p0.cg_tol;
@@ -749,7 +890,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         C.Nx = C.p.Nx;
         C.V = C.Nt * C.Nx;
         C.filter = all_modes_kept(C.Nt, C.Nx, C.p.cut_fraction) ? 0 : 1;
-        C.n_rhs_step = (C.a.g != 0.0) ? C.p.n_rhs : 0;
+        // with pions the step solves complex systems (the chain's workspace)
+        C.pions = C.p.pions != 0;
+        C.n_rhs_pion = (C.pions && C.a.g != 0.0) ? C.p.n_rhs : 0;
+        C.n_rhs_step = (!C.pions && C.a.g != 0.0) ? C.p.n_rhs : 0;
         const int nt = ntiles_of(C.V);
         C.sys0 = nsys;
         C.cg_tile0 = nsys_tiles;
@@ -1024,6 +1168,11 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         YK_CK(cudaMemcpyAsync(ctx->d_white, white.data(), sizeof(int2) * white.size(), cudaMemcpyHostToDevice,
                               ctx->stream));
     YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->pions)
+        if (int rc = pion_setup(ctx.get())) {
+            yk_ctx_destroy(ctx.release());
+            return rc;
+        }
     *out = ctx.release();
     return YK_OK;
 }
@@ -1040,10 +1189,12 @@ int yk_ctx_destroy(yk_ctx* ctx)
     for (auto e : ctx->pool) cudaEventDestroy(e);
     for (auto& C : ctx->ch) {
         if (C.ws.mem) cudaFree(C.ws.mem);
+        if (C.series) cudaFree(C.series);
         net_destroy(C.net);
         net_destroy(C.pcg_ws);
     }
     if (ctx->mem) cudaFree(ctx->mem);
+    if (ctx->pion_mem) cudaFree(ctx->pion_mem);
     if (ctx->aux) {
         cudaStreamSynchronize(ctx->aux);
         cudaStreamDestroy(ctx->aux);
@@ -1120,6 +1271,120 @@ int yk_get_field_host(yk_ctx* ctx, int c, double* phi)
     return YK_OK;
 }
 
+int yk_series_record(yk_ctx* ctx, int c, int64_t capacity)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (capacity < 0) {
+        set_error("yk_series_record: negative capacity");
+        return YK_EINVAL;
+    }
+    Chain& C = ctx->ch[c];
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (C.series) {
+        YK_CK(cudaFree(C.series));
+        C.series = nullptr;
+        C.series_cap = 0;
+    }
+    if (capacity > 0) {
+        if (cudaMalloc(&C.series, sizeof(double) * (size_t)capacity) != cudaSuccess) {
+            cudaGetLastError();
+            C.series = nullptr;
+            set_error("yk_series_record: allocation of %lld values failed", (long long)capacity);
+            return YK_ENOMEM;
+        }
+        C.series_cap = capacity;
+    }
+    // the update kernels read these three fields of the device record
+    ChainDev& H = ctx->h_chains[c];
+    H.series = C.series;
+    H.series_cap = C.series_cap;
+    H.series_n = 0;
+    const size_t off = offsetof(ChainDev, series);
+    const size_t len = offsetof(ChainDev, series_n) + sizeof(int64_t) - off;
+    YK_CK(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->d_chains + c) + off, reinterpret_cast<const char*>(&H) + off,
+                          len, cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->pions)
+        for (int a = 0; a < 3; ++a)
+            YK_CK(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->d_pchains + (size_t)a * ctx->ch.size() + c) + off,
+                                  reinterpret_cast<const char*>(&H) + off, len, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_series_read(yk_ctx* ctx, int c, double* host, int64_t cap, int64_t* n)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!n || (cap > 0 && !host)) {
+        set_error("yk_series_read: bad arguments");
+        return YK_EINVAL;
+    }
+    const Chain& C = ctx->ch[c];
+    int64_t have = 0;
+    if (C.series)
+        YK_CK(cudaMemcpyAsync(&have, &ctx->d_chains[c].series_n, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    const int64_t k = std::min(have, cap);
+    if (k > 0) {
+        YK_CK(cudaMemcpyAsync(host, C.series, sizeof(double) * (size_t)k, cudaMemcpyDeviceToHost, ctx->stream));
+        YK_CK(cudaStreamSynchronize(ctx->stream));
+    }
+    *n = k;
+    return YK_OK;
+}
+
+int yk_series_analyse(yk_ctx* ctx, int c, double stau, yk_series_stats* out)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    const Chain& C = ctx->ch[c];
+    if (!out || !(stau > 0.0) || !C.series) {
+        set_error("yk_series_analyse: %s", C.series ? "bad arguments" : "no series is recorded (yk_series_record)");
+        return YK_EINVAL;
+    }
+    int64_t have = 0;
+    YK_CK(cudaMemcpyAsync(&have, &ctx->d_chains[c].series_n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return series_analyse(C.series, have, C.V, stau, out, ctx->stream);
+}
+
+int yk_set_pions_host(yk_ctx* ctx, int c, const double* pi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    const Chain& C = ctx->ch[c];
+    if (!C.pions || !pi) {
+        set_error("yk_set_pions_host: %s", C.pions ? "null buffer" : "the context carries no pions");
+        return YK_EINVAL;
+    }
+    YK_CK(cudaMemcpyAsync(C.pi, pi, sizeof(double) * 3 * (size_t)C.V, cudaMemcpyHostToDevice, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_get_pions_host(yk_ctx* ctx, int c, double* pi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    const Chain& C = ctx->ch[c];
+    if (!C.pions || !pi) {
+        set_error("yk_get_pions_host: %s", C.pions ? "null buffer" : "the context carries no pions");
+        return YK_EINVAL;
+    }
+    YK_CK(cudaMemcpyAsync(pi, C.pi, sizeof(double) * 3 * (size_t)C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    YK_CK(cudaStreamSynchronize(ctx->stream));
+    return YK_OK;
+}
+
+int yk_pions_device(yk_ctx* ctx, int c, double** pi)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    if (!ctx->ch[c].pions || !pi) {
+        set_error("yk_pions_device: the context carries no pions");
+        return YK_EINVAL;
+    }
+    *pi = ctx->ch[c].pi;
+    return YK_OK;
+}
+
 int yk_field_device(yk_ctx* ctx, int c, double** phi)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
@@ -1140,7 +1405,7 @@ int yk_dirac_apply(yk_ctx* ctx, int c, const void* in, void* out, int dagger, in
     }
     const Chain& C = ctx->ch[c];
     YK_CK(launch_dirac(in, out, C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r, dagger ? 1 : 0, precision, 2,
-                       ctx->stream));
+                       ctx->stream, C.pions ? C.pi : nullptr));
     return YK_OK;
 }
 
@@ -1170,6 +1435,14 @@ int yk_fermion_force(yk_ctx* ctx, int c, const void* eta, double* F, yk_solve_st
         return YK_EINVAL;
     }
     Chain& C = ctx->ch[c];
+    if (C.pions) {
+        // F: 4V doubles (sigma, pi_1, pi_2, pi_3)
+        int rc = pion_solve(ctx, c, 2, static_cast<const double*>(eta), eta ? YK_FP64 : ctx->precision, stats);
+        if (rc && rc != YK_ENOCONV) return rc;
+        YK_CK(launch_pion_force(ctx->d_chains + c, C.ws.d_sys, C.n_rhs_pion, C.pi, F, C.V, ctx->stream));
+        YK_CK(cudaStreamSynchronize(ctx->stream));
+        return rc;
+    }
     if (eta) {
         const int R = C.p.n_rhs;
         if (int rc = ensure_ws(ctx, c, R)) return rc;
@@ -1224,6 +1497,12 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
         set_error("yk_langevin_step: bad arguments");
         return YK_EINVAL;
     }
+    if (ctx->pions) {
+        for (int i = 0; i < n_steps; ++i)
+            for (int c = 0; c < (int)ctx->ch.size(); ++c)
+                if (int rc = pion_step(ctx, c)) return rc;
+        return YK_OK;
+    }
     if (!ctx->gexec && ctx->autotune && !ctx->tuned && n_steps > 0)
         if (int rc = run_autotune(ctx)) return rc;
     if (!ctx->gexec && !ctx->graph_failed && ctx->stream) {
@@ -1259,6 +1538,7 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
 int yk_euler_update(yk_ctx* ctx, int c, const double* force, const double* xi, yk_obs* obs)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
+    if (int rc = no_pions(ctx, "yk_euler_update")) return rc;
     if (!force || !xi) {
         set_error("yk_euler_update: force and xi are required");
         return YK_EINVAL;
@@ -1275,6 +1555,7 @@ int yk_euler_update(yk_ctx* ctx, int c, const double* force, const double* xi, y
 
 int yk_profile_begin(yk_ctx* ctx)
 {
+    if (int rc = no_pions(ctx, "yk_profile_begin")) return rc;
     if (!ctx) return YK_EINVAL;
     YK_CK(cudaStreamSynchronize(ctx->stream));
     ctx->profiling = true;
@@ -1358,7 +1639,8 @@ int yk_correlator(yk_ctx* ctx, int c, double* corr, yk_solve_stats* stats)
     // CG.solve(in, out, Normal); applyD(out, in, Dagger) (main.cu:456-457)
     int rc = ws_solve(ctx, c, 1, YK_NORMAL, ctx->tol, ctx->tol_mode, ctx->max_iter, ctx->precision, stats);
     if (rc && rc != YK_ENOCONV) return rc;
-    YK_CK(launch_dirac(w.work, w.point, C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r, 1, YK_FP64, 2, ctx->stream));
+    YK_CK(launch_dirac(w.work, w.point, C.phi, C.Nt, C.Nx, C.a.m0, C.a.g, C.a.r, 1, YK_FP64, 2, ctx->stream,
+                       C.pions ? C.pi : nullptr));
     YK_CK(launch_time_slices_spinor(w.point, w.corr, C.Nt, C.Nx, 2, ctx->stream));
     YK_CK(cudaMemcpyAsync(corr, w.corr, sizeof(double) * C.Nt, cudaMemcpyDeviceToHost, ctx->stream));
     YK_CK(cudaStreamSynchronize(ctx->stream));
@@ -1374,12 +1656,21 @@ int yk_condensate(yk_ctx* ctx, int c, double* cond, yk_solve_stats* stats)
         if (stats) *stats = yk_solve_stats{0, 0, 0.0, 0.0, 1};
         return YK_OK;
     }
-    int rc = chain_solve(ctx, c, 3, stats);   // fresh noise: Philox stream kind 3
-    if (rc && rc != YK_ENOCONV) return rc;
-    StepArgs s = chain_step_args(ctx, c);
-    YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
     std::vector<double> F(C.V);
-    YK_CK(cudaMemcpyAsync(F.data(), C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = YK_OK;
+    if (C.pions) {
+        // fresh noise: Philox stream kind 3; the sigma force of the pion operator
+        rc = pion_solve(ctx, c, 3, nullptr, ctx->precision, stats);
+        if (rc && rc != YK_ENOCONV) return rc;
+        YK_CK(launch_pion_force(ctx->d_chains + c, C.ws.d_sys, C.n_rhs_pion, C.pi, C.pforce, C.V, ctx->stream));
+        YK_CK(cudaMemcpyAsync(F.data(), C.pforce, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+        rc = chain_solve(ctx, c, 3, stats);   // fresh noise: Philox stream kind 3
+        if (rc && rc != YK_ENOCONV) return rc;
+        StepArgs s = chain_step_args(ctx, c);
+        YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
+        YK_CK(cudaMemcpyAsync(F.data(), C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    }
     YK_CK(cudaStreamSynchronize(ctx->stream));
     double tr = 0.0;
     for (double f : F) tr += f;
@@ -1445,6 +1736,7 @@ static double pcg_inner_tol()
 
 static int net_ok(yk_ctx* ctx, int c)
 {
+    if (int rc = no_pions(ctx, "the learned preconditioner")) return rc;
     if (int rc = chain_ok(ctx, c)) return rc;
     if (!ctx->ch[c].net) {
         set_error("chain %d has no network (yk_net_setup)", c);
@@ -1456,6 +1748,7 @@ static int net_ok(yk_ctx* ctx, int c)
 int yk_net_setup(yk_ctx* ctx, int c, int layers, uint64_t seed, double skip)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
+    if (int rc = no_pions(ctx, "yk_net_setup")) return rc;
     if (layers < 2 || layers > 8) {
         set_error("yk_net_setup: layers = %d outside [2, 8]", layers);
         return YK_EINVAL;
@@ -1636,6 +1929,7 @@ int yk_fgcr_solve(yk_ctx* ctx, int c, const double* b, double* x, double tol, in
 
 int yk_autotune(yk_ctx* ctx, yk_tune_result* out)
 {
+    if (int rc = no_pions(ctx, "yk_autotune")) return rc;
     if (!ctx) {
         set_error("yk_autotune: null context");
         return YK_EINVAL;
@@ -1668,6 +1962,7 @@ int yk_tune_report(yk_ctx* ctx, yk_tune_result* out)
 
 int yk_langevin_step_learned(yk_ctx* ctx, int n_steps, int use_net, yk_solve_stats* stats)
 {
+    if (int rc = no_pions(ctx, "yk_langevin_step_learned")) return rc;
     if (!ctx || n_steps < 0) {
         set_error("yk_langevin_step_learned: bad arguments");
         return YK_EINVAL;

@@ -1357,8 +1357,10 @@ __device__ __forceinline__ Site<W, K> apply_d(const W* in, int n, const SysDev& 
     const Site<W, K> xu = YK_LD(W, K, in, nb.xu);
     const Site<W, K> xd = YK_LD(W, K, in, nb.xd);
     const W diag = diag_of<W, MIXED>(S, n);
-    return dag ? dirac_combine<W, K, true>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm)
-               : dirac_combine<W, K, false>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm);
+    Site<W, K> o = dag ? dirac_combine<W, K, true>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm)
+                       : dirac_combine<W, K, false>(c, tu, td, xu, xd, diag, (W)S.r, (W)nb.sp, (W)nb.sm);
+    pion_term<W, K>(o, c, S.pi, n, S.V, S.g, dag);
+    return o;
 }
 
 // sum conj(a) b over one site, in the vectors' precision
@@ -1561,9 +1563,10 @@ __device__ bool ru_residual(const CGArgs& a, const SysLocal* sl, const unsigned 
         const Site<double, K> xu = YK_LD(double, K, S.x, nb.xu);
         const Site<double, K> xd = YK_LD(double, K, S.x, nb.xd);
         const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-        const Site<double, K> t = first_dag
+        Site<double, K> t = first_dag
             ? dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
             : dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
+        pion_term<double, K>(t, c, S.pi, n, S.V, S.g, first_dag);
         YK_ST(double, K, S.t64, n, t);
     }
     if (!nsync(a, ++epoch, deps)) return false;
@@ -1584,9 +1587,10 @@ __device__ bool ru_residual(const CGArgs& a, const SysLocal* sl, const unsigned 
             const Site<double, K> xu = YK_LD(double, K, S.t64, nb.xu);
             const Site<double, K> xd = YK_LD(double, K, S.t64, nb.xd);
             const double diag = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
-            const Site<double, K> ax = first_dag
+            Site<double, K> ax = first_dag
                 ? dirac_combine<double, K, false>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm)
                 : dirac_combine<double, K, true>(c, tu, td, xu, xd, diag, S.r, (double)nb.sp, (double)nb.sm);
+            pion_term<double, K>(ax, c, S.pi, n, S.V, S.g, !first_dag);
             const Site<double, K> bv = YK_LD(double, K, S.b, n);
             const Site<float, K> pw = YK_LD(float, K, S.p32[prv], n);
             Site<double, K> rd, pd;
@@ -1806,9 +1810,10 @@ __global__ void __launch_bounds__(cg_threads<K>()) cg_kernel(CGArgs a)
                 }
             }
             const W diag = diag_of<W, MIXED>(S, n);
-            const Site<W, K> t = first_dag
+            Site<W, K> t = first_dag
                 ? dirac_combine<W, K, true>(pn[0], pn[1], pn[2], pn[3], pn[4], diag, (W)S.r, (W)nb.sp, (W)nb.sm)
                 : dirac_combine<W, K, false>(pn[0], pn[1], pn[2], pn[3], pn[4], diag, (W)S.r, (W)nb.sp, (W)nb.sm);
+            pion_term<W, K>(t, pn[0], S.pi, n, S.V, S.g, first_dag);
             YK_ST(W, K, Tv(S), n, t);
             YK_ST(W, K, Pv(S, cur), n, pn[0]);
         }

@@ -338,4 +338,19 @@ __device__ __forceinline__ double block_max(double a, double* scratch)
     return r;
 }
 
+// Block max of non-negative IEEE bit patterns into *word (one atomic per block).
+__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* word)
+{
+    __shared__ unsigned long long s_max;
+    if (threadIdx.x == 0) s_max = 0ull;
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned mh = __reduce_max_sync(full, hi);
+    const unsigned ml = __reduce_max_sync(full, hi == mh ? lo : 0u);
+    if ((threadIdx.x & 31) == 0) atomicMax(&s_max, ((unsigned long long)mh << 32) | ml);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_max) atomicMax(word, s_max);
+}
+
 }  // namespace yk

@@ -170,11 +170,11 @@ static double u52(uint32_t hi, uint32_t lo)
     return ((double)m + 0.5) * 0x1p-52;
 }
 
-void philox_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out)
+void philox_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out, uint32_t word3)
 {
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32) ^ chain;
     for (int64_t e = 0; e < (n + 1) / 2; ++e) {
-        uint32_t c[4] = {(uint32_t)e, 0u, 0u, 0u};
+        uint32_t c[4] = {(uint32_t)e, 0u, 0u, word3};
         philox4x32_10(c, k0, k1);
         out[2 * e] = 1.0 - 2.0 * u52(c[0], c[1]);
         if (2 * e + 1 < n) out[2 * e + 1] = 1.0 - 2.0 * u52(c[2], c[3]);
@@ -199,7 +199,16 @@ void gamma_method(const double* data, int64_t n, double stau, double out[5])
         for (int64_t i = 0; i + t < n; ++i) s += (data[i] - mean) * (data[i + t] - mean);
         gam[(size_t)t] = s / (double)(n - t);
     }
-    if (gam[0] == 0.0) return;
+    gamma_window(gam.data(), tmax, n, stau, out);
+}
+
+// The automatic window and the errors from Gamma(t), t = 0..tmax, of n
+// measurements: fills out[1..4] (error, error of error, tau_int, its error).
+void gamma_window(const double* gam_in, int64_t tmax, int64_t n, double stau, double out[5])
+{
+    out[1] = out[2] = out[3] = out[4] = 0.0;
+    if (n < 2 || tmax < 1 || gam_in[0] == 0.0) return;
+    std::vector<double> gam(gam_in, gam_in + tmax + 1);
     int64_t W = tmax;
     double gint = 0.0;
     for (int64_t t = 1; t <= tmax; ++t) {
@@ -344,6 +353,10 @@ int yk_params_from_toml(const char* path, yk_params* p)
         p->init = (v == "philox") ? YK_INIT_PHILOX : (v == "none" ? YK_INIT_NONE : YK_INIT_DRAND48);
     }
     get_i(kv, "gpu.learned_layers", &p->learned_layers);
+    if (kv.count("gpu.pions")) {
+        const std::string v = s("gpu.pions");
+        p->pions = (v == "true" || v == "1") ? 1 : 0;
+    }
     // a network has 2..8 layers (yk_net_setup); refuse other values here,
     // before a run spends its thermalisation on a setting it cannot use
     if (p->learned_layers != 0 && (p->learned_layers < 2 || p->learned_layers > 8)) {

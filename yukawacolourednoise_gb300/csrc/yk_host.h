@@ -30,9 +30,13 @@ void drand48_field(int64_t skip, int64_t n, double* out);
 
 // 1 - 2u with u from Philox4x32-10 stream kind 0 of (seed, chain), two values
 // per counter (the framework's seeded initial field).
-void philox_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out);
+// word3: the counter's last word (0 for sigma, a for pion field a)
+void philox_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out, uint32_t word3 = 0);
 
 void gamma_method(const double* data, int64_t n, double stau, double out[5]);
+// The automatic window of gamma_method from a given Gamma(t), t = 0..tmax, of
+// n measurements: fills out[1..4] (error, its error, tau_int, its error).
+void gamma_window(const double* gam, int64_t tmax, int64_t n, double stau, double out[5]);
 
 void set_error(const char* fmt, ...);
 

@@ -157,6 +157,10 @@ struct ChainDev {
     unsigned counter2;
     unsigned long long dmax_bits;   // max |drift| of the step as IEEE bits (atomic max; reset by the update)
     int status;
+    // per-step <sigma> = sum sigma / V appended by the update kernels while
+    // series_n < series_cap (series null: not recording)
+    double* series;
+    int64_t series_cap, series_n;
 };
 
 struct StepArgs {

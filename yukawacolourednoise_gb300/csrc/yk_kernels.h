@@ -67,6 +67,23 @@ cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, i
                                const CGState* st = nullptr);
 cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream);
 
+// The pion extension's step (yk_pion.cu): white noise of the three pion
+// fields (3V), the complex sources eta_j of Philox stream `kind` (R x 8V), the
+// forces F4 (4V: sigma, pi_1..3) from the R solved systems, and the drift and
+// Euler update of the four fields with the step's observables.
+cudaError_t launch_pion_white(const ChainDev* C, double* white3, int V, cudaStream_t s);
+cudaError_t launch_pion_eta(const ChainDev* C, double* eta, int R, int kind, int V, cudaStream_t s);
+cudaError_t launch_pion_force(const ChainDev* C, const SysDev* sys, int R, const double* pi, double* F4, int V,
+                              cudaStream_t s);
+cudaError_t launch_pion_drift_update(ChainDev* C, double* pi, const double* F4, double* pdrift, const double* pxi,
+                                     double* tile_part, double* tile_f, const CGState* st, int R, int V,
+                                     cudaStream_t s);
+
+// Gamma-method analysis of a device series of n per-configuration <sigma>
+// values on a `volume`-site lattice (yk_series.cu).  Returns a yk_status.
+int series_analyse(const double* d_series, int64_t n, int64_t volume, double stau, yk_series_stats* out,
+                   cudaStream_t s);
+
 // Point-source / time-slice helpers.
 cudaError_t launch_time_slices_spinor(const double* psi, double* corr, int Nt, int Nx, int K,
                                       cudaStream_t stream);

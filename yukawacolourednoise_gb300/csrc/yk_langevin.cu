@@ -31,21 +31,6 @@ __device__ __forceinline__ void cswap(int& a, int& b)
     b = hi;
 }
 
-// Block max of non-negative IEEE bit patterns into *word (one atomic per block).
-__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* word)
-{
-    __shared__ unsigned long long s_max;
-    if (threadIdx.x == 0) s_max = 0ull;
-    __syncthreads();
-    const unsigned full = 0xffffffffu;
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned mh = __reduce_max_sync(full, hi);
-    const unsigned ml = __reduce_max_sync(full, hi == mh ? lo : 0u);
-    if ((threadIdx.x & 31) == 0) atomicMax(&s_max, ((unsigned long long)mh << 32) | ml);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_max) atomicMax(word, s_max);
-}
-
 template <int K>
 __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const SysDev* __restrict__ sys,
                                                             const CGState* __restrict__ st, int mode)
@@ -187,6 +172,7 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
             if (status == YK_ENOCONV) C.obs.noconv_steps += 1;
             C.obs.status = status;
             C.step += 1;
+            if (C.series && C.series_n < C.series_cap) C.series[C.series_n++] = a / (double)C.V;
             C.counter = 0;
             C.status = 0;
             C.dmax_bits = 0ull;   // every block read it before counting in

@@ -54,12 +54,21 @@ int yk_checkpoint_save(yk_ctx* ctx, int chain, const char* path, double eps_bar)
     h.step = step;
     h.time = obs.t;
     h.eps_bar = eps_bar;
+    // a chain with pions appends pi_1..3 (3V doubles) and marks the header
+    std::vector<double> pi(3 * (size_t)V);
+    double* dpi = nullptr;
+    const bool pions = yk_pions_device(ctx, chain, &dpi) == YK_OK;
+    if (pions) {
+        if (int rc = yk_get_pions_host(ctx, chain, pi.data())) return rc;
+        h.magic[6] = 'P';
+    }
     FILE* f = std::fopen(path, "wb");
     if (!f) {
         yk::set_error("cannot write checkpoint %s", path);
         return YK_EIO;
     }
-    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(phi.data(), sizeof(double), V, f) == (size_t)V;
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(phi.data(), sizeof(double), V, f) == (size_t)V;
+    if (ok && pions) ok = std::fwrite(pi.data(), sizeof(double), pi.size(), f) == pi.size();
     std::fclose(f);
     if (!ok) {
         yk::set_error("short write to %s", path);
@@ -78,15 +87,21 @@ int yk_checkpoint_load(yk_ctx* ctx, int chain, const char* path, double* eps_bar
         return YK_EIO;
     }
     CkptHeader h;
-    std::vector<double> phi(V);
-    const bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, "YKCKPT1", 8) == 0 &&
-                    (int64_t)h.Nt * h.Nx == V && std::fread(phi.data(), sizeof(double), V, f) == (size_t)V;
+    std::vector<double> phi(V), pi(3 * (size_t)V);
+    double* dpi = nullptr;
+    const bool pions = yk_pions_device(ctx, chain, &dpi) == YK_OK;
+    bool ok = std::fread(&h, sizeof(h), 1, f) == 1 &&
+              std::memcmp(h.magic, pions ? "YKCKPTP" : "YKCKPT1", 8) == 0 && (int64_t)h.Nt * h.Nx == V &&
+              std::fread(phi.data(), sizeof(double), V, f) == (size_t)V;
+    if (ok && pions) ok = std::fread(pi.data(), sizeof(double), pi.size(), f) == pi.size();
     std::fclose(f);
     if (!ok) {
-        yk::set_error("checkpoint %s does not match the lattice", path);
+        yk::set_error("checkpoint %s does not match the lattice (or its pions)", path);
         return YK_EIO;
     }
     if (int rc = yk_set_field_host(ctx, chain, phi.data())) return rc;
+    if (pions)
+        if (int rc = yk_set_pions_host(ctx, chain, pi.data())) return rc;
     if (int rc = yk_set_step(ctx, chain, h.step)) return rc;
     if (int rc = yk_set_time(ctx, chain, h.time)) return rc;
     if (eps_bar) *eps_bar = h.eps_bar;
@@ -236,6 +251,12 @@ int yk_run_toml(const char* toml_path, const char* out_dir)
         avg_mag += std::fabs(avg);
         std::printf("abs. mag: %g \t cond: %g \t partial avg: %g\n", std::fabs(avg) / V, std::fabs(trace) / V,
                     avg_mag / nmeas / V);
+        if (p.pions) {
+            // pion extension: |<pi>| = |sum_n pi(n)| / V (not in the reference's output)
+            const double pm = std::sqrt(obs.sum_pi[0] * obs.sum_pi[0] + obs.sum_pi[1] * obs.sum_pi[1] +
+                                        obs.sum_pi[2] * obs.sum_pi[2]);
+            std::printf("#pions: |<pi>|: %g \t <|pi|^2>: %g\n", pm / V, obs.sum_pi2 / V);
+        }
         // fermion correlator from a point source (main.cu:441-469)
         yk_solve_stats st;
         int r2 = yk_correlator(ctx, 0, corr.data(), &st);
