@@ -420,7 +420,8 @@ typedef struct yk_series_stats {
  * update kernel appends it on the device; graph-replayed steps included) into
  * a new device series of `capacity` values; capacity 0 stops and frees. */
 int yk_series_record(yk_ctx* ctx, int chain, int64_t capacity);
-/* Copies the recorded values (at most cap) to host memory; *n = how many. */
+/* Copies the recorded values (at most cap) to host memory; *n = how many.
+ * host == NULL: *n = the number of values recorded so far. */
 int yk_series_read(yk_ctx* ctx, int chain, double* host, int64_t cap, int64_t* n);
 /* yk_series_stats of the recorded series (stau: Wolff's S_tau, 1.5). */
 int yk_series_analyse(yk_ctx* ctx, int chain, double stau, yk_series_stats* out);

@@ -466,12 +466,12 @@ class Context:
         """Record <sigma> after every step on the device (capacity 0 stops)."""
         _check(lib().yk_series_record(self.h, chain, int(capacity)))
 
-    def series_read(self, chain=0, cap=1 << 24):
+    def series_read(self, chain=0):
         import numpy as np
         n = C.c_int64()
         _check(lib().yk_series_read(self.h, chain, None, 0, C.byref(n)))
         have = C.c_int64()
-        buf = np.empty(max(1, min(cap, 1 << 24)))
+        buf = np.empty(max(1, n.value))
         _check(lib().yk_series_read(self.h, chain, buf.ctypes.data_as(C.c_void_p), buf.size, C.byref(have)))
         return buf[:have.value].copy()
 

@@ -1325,6 +1325,10 @@ int yk_series_read(yk_ctx* ctx, int c, double* host, int64_t cap, int64_t* n)
         YK_CK(cudaMemcpyAsync(&have, &ctx->d_chains[c].series_n, sizeof(int64_t), cudaMemcpyDeviceToHost,
                               ctx->stream));
     YK_CK(cudaStreamSynchronize(ctx->stream));
+    if (!host) {   // a query of how many values are recorded
+        *n = have;
+        return YK_OK;
+    }
     const int64_t k = std::min(have, cap);
     if (k > 0) {
         YK_CK(cudaMemcpyAsync(host, C.series, sizeof(double) * (size_t)k, cudaMemcpyDeviceToHost, ctx->stream));
