@@ -31,10 +31,11 @@ from pathlib import Path
 REF_SRC = Path(os.environ.get("YK_REFERENCE_SRC", "/root/reference/code/src"))
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
-SIZES = [(8, 4), (6, 10), (16, 16), (32, 32)]
+SIZES = [(8, 4), (6, 10), (16, 16), (32, 32), (256, 256)]
 TUS = ["Dirac.cu", "CGsolver.cu", "FermionicDrift.cu", "reductions.cu", "langevin_gpu_v2.cu", "Lattice.cu"]
 KERNELS = ["applyD_gpu", "solve_kernel", "computeDrift", "Run", "gpuMagnetisation", "gpuTimeSlices",
-           "gpuTimeSlices_spinors", "gpuTraces", "ApplyMask"]
+           "gpuTimeSlices_spinors", "gpuTraces", "ApplyMask", "DoRNG", "setup_kernel", "random_setup_kernel",
+           "fillNormalRND", "setZero_kernel"]
 FLAGS = ["-arch=sm_103a", "--expt-relaxed-constexpr", "-DUSE_cuFFT", "-O3", "-w"]
 
 

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -333,10 +334,167 @@ static double run_update(CUdeviceptr phi, CUdeviceptr drift, CUdeviceptr noise, 
     return e;
 }
 
+// ------------------------------------------------------------ timing
+static std::vector<double> read_raw(const char* path, size_t n)
+{
+    std::vector<double> v(n);
+    FILE* f = std::fopen(path, "rb");
+    if (!f || std::fread(v.data(), sizeof(double), n, f) != n) {
+        std::fprintf(stderr, "cannot read %zu doubles from %s\n", n, path);
+        std::exit(5);
+    }
+    std::fclose(f);
+    return v;
+}
+
+static double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Times the reference's own kernels on this GPU, launched and synchronised as
+// the reference launches them: the Dirac apply (Dirac.cu:23-35), the CG solve
+// of a given right-hand side (CGsolver.cu:42-59, its occupancy-sized grid)
+// and full Langevin steps (main.cu:370-381: ColouredNoise::operator() with
+// DoRNG, cuFFT and ApplyMask, colouredNoise.cpp:155-178; getForce with
+// fillNormalRND, setZero_kernel, the solve, applyD and computeDrift,
+// FermionicDrift.cu:57-80; Run; the eps copy to the host), from the given
+// field.  Vectors live in device memory (the reference allocates managed
+// memory).  Writes one JSON object.
+static int time_mode(const char* field_path, const char* b_path, int steps, const char* out_path)
+{
+    const double m2 = -0.5, lam = 1.0, g = 0.5, m0 = 0.1, eps_bar = 0.01, cut = 0.35355339059327373;
+    set_params(m2, lam, g, m0, 1.0, cut, 0, eps_bar);
+    const Tables T = make_tables();
+    CGBufs B = make_cg();
+    const size_t SB = 64 * (size_t)V;
+    CUdeviceptr phi = dalloc(8 * (size_t)V), bvec = dalloc(SB), x = dalloc(SB), y = dalloc(SB);
+    const std::vector<double> f0 = read_raw(field_path, V), b = read_raw(b_path, 8 * (size_t)V);
+    h2d(phi, f0.data(), 8 * (size_t)V);
+    h2d(bvec, b.data(), SB);
+    CUevent e0, e1;
+    CK(cuEventCreate(&e0, CU_EVENT_DEFAULT));
+    CK(cuEventCreate(&e1, CU_EVENT_DEFAULT));
+    auto timed = [&](auto&& fn, int reps) {
+        fn();   // warm-up
+        float tot = 0.f;
+        for (int i = 0; i < reps; ++i) {
+            CK(cuEventRecord(e0, nullptr));
+            fn();
+            CK(cuEventRecord(e1, nullptr));
+            CK(cuEventSynchronize(e1));
+            float ms = 0.f;
+            CK(cuEventElapsedTime(&ms, e0, e1));
+            tot += ms;
+        }
+        return tot / reps;
+    };
+    // Dirac apply: occupancy query, cooperative launch, synchronisation
+    const float ms_dirac = timed([&] { applyD(bvec, y, 0, phi, T); }, 20);
+    // CG on D^dag D with the reference's grid (tolerance 1e-8 absolute, 1000 iterations)
+    const float ms_cg = timed([&] { cg_solve_occupancy(bvec, x, 1, phi, T, B); }, 5);
+    // full steps
+    const Kli kr = kli("Run");
+    CUdeviceptr states_noise = dalloc(64 * (size_t)kr.blocks * kr.threads);
+    // fillNormalRND reads state[thread rank] of its whole occupancy-sized grid
+    // (FermionicDrift.cu:104) before its loop over the 4V states, so the
+    // buffer holds max(4V, grid threads) states (64 bytes each, more than a
+    // curandStateXORWOW's 48)
+    int rnd_grid = 0, rnd_block = 0;
+    CK(cuOccupancyMaxPotentialBlockSize(&rnd_grid, &rnd_block, fns.at("fillNormalRND"), nullptr, 0, 0));
+    const size_t n_states_f = std::max((size_t)4 * V, (size_t)rnd_grid * rnd_block);
+    CUdeviceptr states_f = dalloc(64 * n_states_f);
+    int seed = 1234, svol = 4 * V;
+    {
+        CUdeviceptr a1 = states_noise;
+        void* args[] = {&seed, &a1};
+        coop_kli("setup_kernel", kr, args, 0);
+        CUdeviceptr b1 = states_f;
+        void* args2[] = {&seed, &b1, &svol};
+        coop("random_setup_kernel", args2);
+    }
+    const int nfreq = Nt * (Nx / 2 + 1);
+    CUdeviceptr noise = dalloc(8 * (size_t)V), tmp = dalloc(16 * (size_t)nfreq), mask = dalloc(8 * (size_t)nfreq);
+    const std::vector<double> mk = mask_half(cut);
+    h2d(mask, mk.data(), 8 * mk.size());
+    int sizes[2] = {Nt, Nx};
+    cufftHandle pf, pr;
+    CF(cufftPlanMany(&pf, 2, sizes, NULL, 1, V, NULL, 1, V, CUFFT_D2Z, 1));
+    CF(cufftPlanMany(&pr, 2, sizes, NULL, 1, V, NULL, 1, V, CUFFT_Z2D, 1));
+    CUdeviceptr eta = dalloc(SB), buf = dalloc(SB), after = dalloc(SB), drift = dalloc(8 * (size_t)V);
+    CUdeviceptr eps = dalloc(8), md = dalloc(8);
+    h2d(eps, &eps_bar, 8);
+    const Kli km = kli("ApplyMask");
+    const unsigned run_smem = (unsigned)(sizeof(double) * std::max(kr.threads, 32));
+    double export_time = 1.0;
+    int n = V;
+    auto step = [&]() -> double {
+        // ColouredNoise::operator()
+        {
+            CUdeviceptr a0 = noise, a2 = states_noise;
+            void* args[] = {&a0, &n, &a2};
+            coop_kli("DoRNG", kr, args, 0);
+        }
+        CF(cufftExecD2Z(pf, (cufftDoubleReal*)noise, (cufftDoubleComplex*)tmp));
+        CK(cuCtxSynchronize());
+        {
+            CUdeviceptr a0 = tmp, a1 = mask;
+            void* args[] = {&a0, &a1, &n};
+            coop_kli("ApplyMask", km, args, 0);
+        }
+        CF(cufftExecZ2D(pr, (cufftDoubleComplex*)tmp, (cufftDoubleReal*)noise));
+        CK(cuCtxSynchronize());
+        // FermionicDrift::getForce
+        {
+            CUdeviceptr a0 = eta, a1 = states_f;
+            void* args[] = {&a0, &a1, &svol};
+            coop("fillNormalRND", args);
+            CUdeviceptr z0 = after;
+            void* zargs[] = {&z0, &svol};
+            coop("setZero_kernel", zargs);
+        }
+        cg_solve_occupancy(eta, buf, 1, phi, T, B);
+        applyD(buf, after, 0, phi, T);
+        {
+            CUdeviceptr a0 = after, a1 = eta, a2 = drift;
+            void* args[] = {&a0, &a1, &a2};
+            coop("computeDrift", args);
+        }
+        // Run and the host copy of eps
+        {
+            CUdeviceptr a0 = eps, a2 = phi, a3 = drift, a4 = noise, a6 = T.I, a7 = T.J, a8 = T.vals, a9 = md;
+            void* args[] = {&a0, &export_time, &a2, &a3, &a4, &n, &a6, &a7, &a8, &a9};
+            coop_kli("Run", kr, args, run_smem);
+        }
+        double h_eps = 0.0;
+        CK(cuMemcpyDtoH(&h_eps, eps, 8));
+        return h_eps;
+    };
+    for (int i = 0; i < 3; ++i) step();
+    const double t0 = now_s();
+    for (int i = 0; i < steps; ++i) step();
+    const double t1 = now_s();
+    cufftDestroy(pf);
+    cufftDestroy(pr);
+    FILE* f = std::fopen(out_path, "w");
+    if (!f) return 4;
+    std::fprintf(f,
+                 "{\"lattice\": [%d, %d], \"dirac_ms\": %.6f, \"dirac_gbs_136B\": %.2f, \"cg_solve_ms\": %.6f, "
+                 "\"steps\": %d, \"step_ms\": %.6f, \"steps_per_s\": %.4f, \"run_grid\": [%d, %d]}\n",
+                 Nt, Nx, ms_dirac, 136.0 * V / (ms_dirac * 1e-3) / 1e9, ms_cg, steps, (t1 - t0) / steps * 1e3,
+                 steps / (t1 - t0), kr.blocks, kr.threads);
+    std::fclose(f);
+    std::printf("ref_harness timing %dx%d ok\n", Nt, Nx);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s fatbin symbols Nt Nx out.bin\n", argv[0]);
+        std::fprintf(stderr,
+                     "usage: %s fatbin symbols Nt Nx out.bin\n"
+                     "       %s fatbin symbols Nt Nx --time field.raw b.raw steps out.json\n",
+                     argv[0], argv[0]);
         return 1;
     }
     Nt = std::atoi(argv[3]);
@@ -357,6 +515,10 @@ int main(int argc, char** argv)
             CK(cuModuleGetFunction(&f, mod, m.c_str()));
             fns[k] = f;
         }
+    }
+    if (std::string(argv[5]) == "--time") {
+        if (argc < 10) return 1;
+        return time_mode(argv[6], argv[7], std::atoi(argv[8]), argv[9]);
     }
     dump = std::fopen(argv[5], "wb");
     if (!dump) return 4;

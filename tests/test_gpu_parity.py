@@ -120,6 +120,28 @@ def test_cg_mixed_reaches_fp64_residual(ylib, cuda):
         assert st.iterations <= 1.5 * it + 60
 
 
+@pytest.mark.parametrize("scale,tol", [(1e-9, 1e-10), (1.0, 1e-12)])
+def test_cg_mixed_small_residuals(ylib, cuda, scale, tol):
+    # residuals small in absolute terms (a right-hand side of norm ~1e-7, or a
+    # 1e-12 relative target): the FP32 scalar step of the mixed solver stays
+    # finite (|<p, Ap>|^2 would underflow FP32) and converges on the FP64 residual
+    yk = ylib
+    Nt, Nx = 32, 32
+    p = params(yk, Nt, Nx)
+    rng = np.random.default_rng(12)
+    with yk.Context(p) as ctx:
+        sig = rng.uniform(-1, 1, Nt * Nx)
+        ctx.set_field(sig)
+        b = rand_spinor(rng, Nt * Nx) * scale
+        xd = dev(cuda, np.zeros_like(b))
+        st = ctx.cg_solve(dev(cuda, b), xd, tol=tol, tol_mode=yk.YK_TOL_REL, max_iter=5000, precision=yk.YK_MIXED)
+        x = host(xd)
+        a = act(p)
+        r = b - O.dirac(Nt, Nx, a, sig, O.dirac(Nt, Nx, a, sig, x), True)
+        assert st.converged == 1
+        assert np.linalg.norm(r) <= 1.05 * tol * np.linalg.norm(b)
+
+
 def test_cg_iteration_cap_reports_noconv(ylib, cuda):
     yk = ylib
     p = params(yk, 16, 16)

@@ -645,10 +645,14 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
     const double c = s[2], d = s[3];
     double ar, ai;
     if constexpr (MIXED) {
-        const float cf_ = (float)c, df_ = (float)d, rf = (float)rr;
-        const float inv = 1.f / fmaf(cf_, cf_, df_ * df_);
-        ar = (double)(rf * cf_ * inv);
-        ai = (double)(-rf * df_ * inv);
+        // alpha = (c' - i d') / (c'^2 + d'^2) with c' = c / rr, d' = d / rr:
+        // O(1) terms, so no square underflows FP32 when the residual is small
+        // in absolute terms (|r|^2 ~ 1e-21 squares to below FLT_MIN)
+        const float rinv = 1.f / (float)rr;
+        const float cs = (float)c * rinv, ds = (float)d * rinv;
+        const float inv = 1.f / fmaf(cs, cs, ds * ds);
+        ar = (double)(cs * inv);
+        ai = (double)(-ds * inv);
     } else {
         const double inv_pap = 1.0 / fma(c, c, d * d);
         ar = rr * c * inv_pap;
