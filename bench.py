@@ -21,7 +21,9 @@ plain FP64 form, the precision errors) replays that same segment.
 
   --impl ours (default): the CUDA path; `value` = steps/s of all ranks.
   --impl reference: the CPU oracle (C restatement of the reference's
-      algorithm; the reference itself has no CPU path) on the host cores.
+      algorithm; the reference itself has no CPU path) on the host cores;
+      beside it, `reference_gpu`: the reference's own CUDA kernels (compiled
+      from its sources) timed on this GPU.
 
 Multi-GPU: chains are independent, so N GPUs run N replicas (weak scaling,
 no collective on the data path).
@@ -655,12 +657,26 @@ def cpu_baseline(seconds: float, warmup: int) -> dict:
                       f"steps (FP64 CG rel-res 1e-10, OpenMP over sites)"}
 
 
+def reference_gpu(steps=20) -> dict:
+    """The reference's own CUDA kernels on this GPU at the workload's lattice
+    (oracle/ref/time_ref.py: its Dirac apply, CG solve and full Langevin steps,
+    launched and synchronised as the reference does, from the thermalised
+    start field, with the reference's compile-time CG stop |r| <= 1e-8 and its
+    adaptive step).  Reported beside the CPU arm; not the arm's value."""
+    try:
+        from oracle.ref import time_ref
+        return time_ref.time_size(NT, NX, steps)
+    except Exception as e:   # the harness needs the fatbins built from the reference's sources
+        return {"unavailable": f"{type(e).__name__}: {e}"[:300]}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
     budget = float(os.environ.get("YK_REF_SECONDS", "120"))
     n, dt, threads = cpu_steps(budget, args.steps, args.warmup)
     v = n / dt
+    rg = reference_gpu() if not args.no_reference_gpu else {"skipped": "--no-reference-gpu"}
     return {"metric": METRIC, "value": round(v, 4), "unit": "steps/s", "n_gpus": ws, "steps": n,
             "warmup": args.warmup, "ms_per_step": round(dt / n * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
@@ -670,7 +686,8 @@ def run_reference(args, ws, rank):
                                        f"thermalised start field after {args.warmup} warm-up steps (the segment "
                                        f"the GPU arm times; CPU restatement of the reference, which has no CPU "
                                        f"path)"},
-            "e2e": {"value": round(v, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": round(v, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": rg}
 
 
 def main(argv=None):
@@ -693,6 +710,8 @@ def main(argv=None):
     ap.add_argument("--full-scale", action="store_true",
                     help="only the full form at scale (8 chains of 1024^2, 8 RHS; one JSON object; minutes)")
     ap.add_argument("--no-full-scale", action="store_true", help="skip the full form at scale in the default run")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip timing the reference's own CUDA kernels on the GPU")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

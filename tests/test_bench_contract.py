@@ -19,7 +19,7 @@ def _run(*args):
 
 
 def test_reference_arm_prints_one_contract_line():
-    r = _run("--impl", "reference", "--steps", "1", "--warmup", "3")
+    r = _run("--impl", "reference", "--steps", "1", "--warmup", "3", "--no-reference-gpu")
     assert r.returncode == 0, r.stderr
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1

@@ -40,7 +40,11 @@ def rand_spinor(rng, V):
     return rng.normal(size=(V, 4)) + 1j * rng.normal(size=(V, 4))
 
 
-@pytest.mark.parametrize("Nt,Nx,r", [(8, 4, 1.0), (16, 16, 0.5), (6, 10, 1.0), (64, 32, 1.0), (2, 8, 0.0)])
+# rows of a multiple of 32 sites take the column-strip kernel (blocks of 32,
+# 96, 256 threads; bands of 16 rows, the last one partial), the rest the
+# site-per-thread kernel
+@pytest.mark.parametrize("Nt,Nx,r", [(8, 4, 1.0), (16, 16, 0.5), (6, 10, 1.0), (64, 32, 1.0), (2, 8, 0.0),
+                                     (20, 96, 1.0), (3, 256, 0.5), (40, 512, 1.0)])
 def test_dirac_fp64(ylib, cuda, Nt, Nx, r):
     yk = ylib
     p = params(yk, Nt, Nx, wilson_param=r)
@@ -59,9 +63,9 @@ def test_dirac_fp64(ylib, cuda, Nt, Nx, r):
             assert err < 1e-13, (dag, err)
 
 
-def test_dirac_fp32(ylib, cuda):
+@pytest.mark.parametrize("Nt,Nx", [(32, 16), (36, 64), (16, 288)])
+def test_dirac_fp32(ylib, cuda, Nt, Nx):
     yk = ylib
-    Nt, Nx = 32, 16
     p = params(yk, Nt, Nx)
     rng = np.random.default_rng(2)
     with yk.Context(p) as ctx:
@@ -70,10 +74,11 @@ def test_dirac_fp32(ylib, cuda):
         psi = rand_spinor(rng, Nt * Nx).astype(np.complex64)
         x = dev(cuda, psi)
         y = cuda.empty_like(x)
-        ctx.dirac_apply(x, y, dagger=False, precision=yk.YK_FP32)
-        ctx.synchronize()
-        want = O.dirac(Nt, Nx, act(p), sig, psi.astype(np.complex128))
-        assert np.abs(host(y) - want).max() / np.abs(want).max() < 2e-6
+        for dag in (False, True):
+            ctx.dirac_apply(x, y, dagger=dag, precision=yk.YK_FP32)
+            ctx.synchronize()
+            want = O.dirac(Nt, Nx, act(p), sig, psi.astype(np.complex128), dag)
+            assert np.abs(host(y) - want).max() / np.abs(want).max() < 2e-6, dag
 
 
 @pytest.mark.parametrize("mtype", [0, 1])

@@ -52,7 +52,7 @@ def test_pion_initial_fields(ylib, cuda):
             ctx.get_pions()
 
 
-@pytest.mark.parametrize("Nt,Nx,r", [(8, 4, 1.0), (16, 16, 0.5), (6, 10, 1.0)])
+@pytest.mark.parametrize("Nt,Nx,r", [(8, 4, 1.0), (16, 16, 0.5), (6, 10, 1.0), (18, 64, 1.0)])
 def test_pion_dirac_matches_oracle(ylib, cuda, Nt, Nx, r):
     yk = ylib
     p = params(yk, Nt, Nx, wilson_param=r)
