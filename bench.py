@@ -710,6 +710,8 @@ def main(argv=None):
     ap.add_argument("--full-scale", action="store_true",
                     help="only the full form at scale (8 chains of 1024^2, 8 RHS; one JSON object; minutes)")
     ap.add_argument("--no-full-scale", action="store_true", help="skip the full form at scale in the default run")
+    ap.add_argument("--dirac-only", type=int, default=0, metavar="L",
+                    help="only the Dirac apply on an L x L lattice (one JSON object; profiling runs)")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip timing the reference's own CUDA kernels on the GPU")
     args = ap.parse_args(argv)
@@ -720,6 +722,13 @@ def main(argv=None):
         import yukawacolourednoise_gb300 as yk
         stream = torch.cuda.Stream()
         print(json.dumps({"full_scale": full_scale(yk, torch, stream)}), flush=True)
+        return 0
+    if args.dirac_only:
+        import torch
+        import yukawacolourednoise_gb300 as yk
+        stream = torch.cuda.Stream()
+        L = args.dirac_only
+        print(json.dumps({"dirac_hbm": dirac_hbm(yk, torch, stream, Nt=L, Nx=L)}), flush=True)
         return 0
     if args.learned_only:
         import torch
