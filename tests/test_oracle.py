@@ -242,3 +242,24 @@ def test_evenodd_schur_solve_matches_direct():
     assert np.abs(chi_eo - want).max() < 1e-9 * np.abs(want).max()
     assert np.abs(chi_cg - want).max() < 1e-9 * np.abs(want).max()
     assert it_eo < it_cg, (it_eo, it_cg)
+
+
+@pytest.mark.parametrize("Nt,Nx,m0", [(8, 6, 0.05), (16, 16, 0.1), (32, 32, 0.02)])
+def test_evenodd_cgne_stops_on_the_true_residual(Nt, Nx, m0):
+    # CGNE on the Schur complement controls the true residual |eta - D^dag chi|
+    # that the reference's CG on D^dag D controls: at the same rule
+    # (rel-res 1e-10) both meet it, and the even-odd solve takes fewer
+    # iterations (each an S S^dag apply: the stencil work of one D^dag D)
+    from oracle import evenodd as E
+    rng = np.random.default_rng(Nt)
+    a = O.action(m2=-0.5, lam=1.0, g=0.5, m0=m0, r=1.0)
+    sigma = rng.uniform(-1, 1, Nt * Nx)
+    eta = rng.normal(size=(Nt * Nx, 4)) + 0j
+    chi_eo, it_eo = E.chi_evenodd_cgne(Nt, Nx, a, sigma, eta, tol=1e-10)
+    x, it_cg, _ = O.cg(Nt, Nx, a, sigma, eta, mtype=1, tol=1e-10, tol_mode=1, max_iter=20000)
+    chi_cg = O.dirac(Nt, Nx, a, sigma, x)
+    res_eo = E.true_residual(Nt, Nx, a, sigma, eta, chi_eo)
+    res_cg = E.true_residual(Nt, Nx, a, sigma, eta, chi_cg)
+    assert res_eo <= 1.05e-10 and res_cg <= 1.05e-10, (res_eo, res_cg)
+    assert np.abs(chi_eo - chi_cg).max() < 1e-7 * np.abs(chi_cg).max()
+    assert it_eo * 1.5 < it_cg, (it_eo, it_cg)
