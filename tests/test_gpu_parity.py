@@ -66,7 +66,7 @@ def test_dirac_fp64(ylib, cuda, Nt, Nx, r):
 @pytest.mark.parametrize("Nt,Nx", [(32, 16), (36, 64), (16, 288)])
 def test_dirac_fp32(ylib, cuda, Nt, Nx):
     yk = ylib
-    p = params(yk, Nt, Nx)
+    p = params(yk, Nt, Nx, cut_fraction=1.0)   # white noise: any Nx
     rng = np.random.default_rng(2)
     with yk.Context(p) as ctx:
         sig = rng.uniform(-1, 1, Nt * Nx)
