@@ -49,6 +49,7 @@ CUT = 0.35355339059327373          # Lambda = pi/2  ->  cutFraction = Lambda / (
 BYTES_CG_ITER_MIXED = 200          # unique bytes per site per FP32 CG iteration of cg_kernel (passes A and B)
 BYTES_CG_ITER_HALO = 128           # the same for cg_halo_kernel: D p stays in shared memory, diag is cached
 BYTES_CG_ITER_FP64 = 400
+BYTES_CG_ITER_EO = 48              # cg_eo_kernel: r, q, p loaded and stored per compact (even) site, 96 B = 48 B per site
 # the thermalised start of the workload (both arms time the same steps from it)
 START = ROOT / "tests" / "golden" / "start_256x256.npz"
 DATA = ("synthetic: Philox noise; the timed steps continue a chain from tests/golden/start_256x256.npz, "
@@ -262,9 +263,13 @@ def roofline(pr, precision):
     """Roofline of the dominant kernel (the persistent CG) from the profiled
     steps: algorithmic bytes per launch / CUDA-event launch time."""
     per_launch_ms = pr.cg_ms / max(pr.cg_launches, 1)
-    halo = pr.cg_kernel == 1
-    bpi = (BYTES_CG_ITER_HALO if halo else BYTES_CG_ITER_MIXED) if precision == "mixed" else BYTES_CG_ITER_FP64
-    kname = "cg_halo_kernel" if halo else f"cg_kernel<1,{'mixed' if precision == 'mixed' else 'fp64'}>"
+    halo, eo = pr.cg_kernel == 1, pr.cg_kernel == 3
+    if precision != "mixed":
+        bpi = BYTES_CG_ITER_FP64
+    else:
+        bpi = BYTES_CG_ITER_EO if eo else (BYTES_CG_ITER_HALO if halo else BYTES_CG_ITER_MIXED)
+    kname = "cg_eo_kernel" if eo else ("cg_halo_kernel" if halo else
+                                       f"cg_kernel<1,{'mixed' if precision == 'mixed' else 'fp64'}>")
     alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
     pk = peaks()
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9

@@ -269,8 +269,9 @@ def test_langevin_mixed_precision_step(ylib, cuda, monkeypatch, cluster):
         assert ctx.observables().status == 0
 
 
-def _mixed_run(yk, monkeypatch, halo, Nt, Nx, steps):
+def _mixed_run(yk, monkeypatch, halo, Nt, Nx, steps, eo="0"):
     monkeypatch.setenv("YK_CG_HALO", halo)
+    monkeypatch.setenv("YK_CG_EO", eo)
     p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
     with yk.Context(p) as ctx:
         ctx.profile_begin()
@@ -296,6 +297,7 @@ def test_halo_cg_matches_grid_cg(ylib, cuda, monkeypatch, Nt, Nx):
 def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
     # one Langevin step through the halo kernel against the FP64 oracle
     monkeypatch.setenv("YK_CG_HALO", "1")
+    monkeypatch.setenv("YK_CG_EO", "0")
     yk = ylib
     Nt, Nx = 48, 32
     p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
@@ -307,6 +309,66 @@ def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
         want, _ = O.langevin_step(Nt, Nx, act(p), phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
         assert np.abs(ctx.get_field() - want).max() < 1e-8
         assert ctx.observables().status == 0
+
+
+@pytest.mark.parametrize("Nt,Nx", [(32, 32), (256, 256), (64, 128), (128, 64), (48, 32)])
+def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx):
+    # the even-odd Schur-complement solve of the step (CGNE on S S^dag, its
+    # residual the true residual of D^dag chi = eta, the same rule relative to
+    # |eta|) against the FP64 oracle's CG on D^dag D: the fields of three steps
+    # within 1e-8, in fewer iterations than the halo kernel's D^dag D solve
+    yk = ylib
+    monkeypatch.setenv("YK_CG_EO", "1")
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01, reliable_every=50)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        ctx.profile_begin()
+        ctx.step(1)
+        pr = ctx.profile_end()
+        assert pr.cg_kernel == 3, "the step's solve runs the even-odd kernel"
+        got = [ctx.get_field()]
+        ctx.step(2)
+        got.append(ctx.get_field())
+        obs = ctx.observables()
+    assert obs.status == 0
+    a = act(p)
+    want, _ = O.langevin_step(Nt, Nx, a, phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    assert np.abs(got[0] - want).max() < 1e-8
+    w = got[0]
+    for s in (1, 2):
+        w, _ = O.langevin_step(Nt, Nx, a, w, 1234, 0, s, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    assert np.abs(got[1] - w).max() < 1e-8
+    _, k_halo, it_halo, _ = _mixed_run(yk, monkeypatch, "1", Nt, Nx, 1, eo="0")
+    assert pr.cg_iterations < 0.7 * it_halo, (pr.cg_iterations, it_halo)
+
+
+def test_evenodd_force_and_condensate_match_the_full_solve(ylib, cuda, monkeypatch):
+    # yk_fermion_force (the step's Philox source) and yk_condensate through
+    # the even-odd solve against the same calls through the D^dag D solve
+    yk = ylib
+    Nt, Nx = 64, 64
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    res = {}
+    for eo in ("1", "0"):
+        monkeypatch.setenv("YK_CG_EO", eo)
+        with yk.Context(p) as ctx:
+            F = cuda.empty(Nt * Nx, dtype=cuda.float64, device="cuda")
+            ctx.fermion_force(F)
+            cond, _ = ctx.condensate()
+            res[eo] = (F.cpu().numpy(), cond)
+    assert np.abs(res["1"][0] - res["0"][0]).max() < 1e-8 * np.abs(res["0"][0]).max()
+    assert abs(res["1"][1] - res["0"][1]) < 1e-8 * abs(res["0"][1])
+
+
+def test_evenodd_skips_odd_lattices(ylib, cuda, monkeypatch):
+    # odd extents have no checkerboard: the halo kernel's D^dag D solve runs
+    yk = ylib
+    monkeypatch.setenv("YK_CG_EO", "1")
+    p = params(yk, 41, 25, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    with yk.Context(p) as ctx:
+        ctx.profile_begin()
+        ctx.step(1)
+        assert ctx.profile_end().cg_kernel in (0, 1)
 
 
 def test_batched_chains_equal_single_chains(ylib, cuda):

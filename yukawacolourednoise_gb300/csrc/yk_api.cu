@@ -177,6 +177,14 @@ struct yk_ctx {
     bool pions = false;
     void* pion_mem = nullptr;
     ChainDev* d_pchains = nullptr;
+    // even-odd solves of the step (single mixed system on an even lattice;
+    // YK_CG_EO=0 at context creation: never): the systems' compact views and
+    // their tile table (the same tile ids as the full table, fewer of them)
+    bool cg_eo = false;
+    void* eo_mem = nullptr;
+    SysDev* d_sys_eo = nullptr;
+    int2* d_eo_tiles = nullptr;
+    int eo_tile_begin = 0, eo_tile_end = 0;
 };
 
 namespace {
@@ -338,6 +346,8 @@ void prof_end(yk_ctx* ctx, int cls, cudaEvent_t a, int launches)
 // SMs free, the noise passes run on the auxiliary stream beside it, on at
 // most that many blocks, and the update waits for them.  Profiled steps run
 // the kernel classes one after the other.
+void eo_args(const yk_ctx* ctx, CGArgs& a);
+
 int enqueue_step(yk_ctx* ctx)
 {
     cudaEvent_t e = nullptr;
@@ -382,6 +392,7 @@ int enqueue_step(yk_ctx* ctx)
                     a.solo_nt = C.Nt;
                     a.solo_nx = C.Nx;
                 }
+        eo_args(ctx, a);
         if (ctx->cg_cluster) {
             YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles, ctx->n_sys_tiles, 2, ctx->stream));
             YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
@@ -556,7 +567,9 @@ int ws_solve(yk_ctx* ctx, int c, int count, int mtype, double tol, int tol_mode,
 
 // Runs the CG of chain c's step systems (K = 1) with Philox right-hand sides
 // of stream `kind` at the chain's current step.
-int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
+// want_x: the caller reads x (the solution of D^dag D x = b); otherwise the
+// step's even-odd solve may run, which leaves chi = D x in t64 instead.
+int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats, bool want_x = false)
 {
     Chain& C = ctx->ch[c];
     if (C.n_rhs_step == 0) {
@@ -578,6 +591,7 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats)
         a.solo_nt = C.Nt;
         a.solo_nx = C.Nx;
     }
+    if (!want_x) eo_args(ctx, a);
     if (ctx->cg_cluster) {
         YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles + C.cg_tile0, C.cg_tile1 - C.cg_tile0, kind, ctx->stream));
         YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
@@ -758,6 +772,56 @@ int pion_setup(yk_ctx* ctx)
     }
     YK_CK(cudaMemcpy(ctx->d_pchains, pch.data(), sizeof(ChainDev) * pch.size(), cudaMemcpyHostToDevice));
     return YK_OK;
+}
+
+// Compact (even-odd) views of the step's single mixed system: the lattice of
+// one parity class (Nx / 2 columns, V / 2 sites) over the system's buffers --
+// the FP32 vectors compact, x = chi_e followed by rhs_e, t64 the full chi at
+// the end -- and its tile table.
+int eo_setup(yk_ctx* ctx, const std::vector<SysDev>& hs)
+{
+    const char* env = getenv("YK_CG_EO");
+    if (!(env && env[0] == '1') || ctx->nsys != 1 || ctx->precision != YK_MIXED || !ctx->cg_halo || ctx->cg_cluster ||
+        ctx->pions)
+        return YK_OK;
+    const Chain* C = nullptr;
+    for (const Chain& q : ctx->ch)
+        if (q.n_rhs_step == 1) C = &q;
+    if (!C || (C->Nt & 1) || (C->Nx & 1) || C->Nx < 4) return YK_OK;
+    const int Ve = C->V / 2, nte = ntiles_of(Ve);
+    SysDev E = hs[C->sys0];
+    E.Nx = C->Nx / 2;
+    E.V = Ve;
+    E.tile0 = C->cg_tile0;
+    E.ntiles = nte;
+    std::vector<int2> tiles(ctx->n_sys_tiles, make_int2(C->sys0, 0));
+    for (int t = 0; t < nte; ++t) tiles[C->cg_tile0 + t] = make_int2(C->sys0, t * kTile);
+    const size_t o_tiles = ((sizeof(SysDev) * ctx->nsys + 255) / 256) * 256;
+    if (cudaMalloc(&ctx->eo_mem, o_tiles + sizeof(int2) * tiles.size()) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("even-odd view allocation failed");
+        return YK_ENOMEM;
+    }
+    ctx->d_sys_eo = reinterpret_cast<SysDev*>(ctx->eo_mem);
+    ctx->d_eo_tiles = reinterpret_cast<int2*>(static_cast<char*>(ctx->eo_mem) + o_tiles);
+    std::vector<SysDev> views(hs);
+    views[C->sys0] = E;
+    YK_CK(cudaMemcpy(ctx->d_sys_eo, views.data(), sizeof(SysDev) * views.size(), cudaMemcpyHostToDevice));
+    YK_CK(cudaMemcpy(ctx->d_eo_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
+    ctx->eo_tile_begin = C->cg_tile0;
+    ctx->eo_tile_end = C->cg_tile0 + nte;
+    ctx->cg_eo = true;
+    return YK_OK;
+}
+
+// The step CG's even-odd views, when the context has them.
+void eo_args(const yk_ctx* ctx, CGArgs& a)
+{
+    if (!ctx->cg_eo) return;
+    a.sys_eo = ctx->d_sys_eo;
+    a.eo_tiles = ctx->d_eo_tiles;
+    a.eo_tile_begin = ctx->eo_tile_begin;
+    a.eo_tile_end = ctx->eo_tile_end;
 }
 
 // The complex systems of a pion chain: sources eta (device, n_rhs x 8V) or,
@@ -1173,6 +1237,10 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
             yk_ctx_destroy(ctx.release());
             return rc;
         }
+    if (int rc = eo_setup(ctx.get(), hs)) {
+        yk_ctx_destroy(ctx.release());
+        return rc;
+    }
     *out = ctx.release();
     return YK_OK;
 }
@@ -1195,6 +1263,7 @@ int yk_ctx_destroy(yk_ctx* ctx)
     }
     if (ctx->mem) cudaFree(ctx->mem);
     if (ctx->pion_mem) cudaFree(ctx->pion_mem);
+    if (ctx->eo_mem) cudaFree(ctx->eo_mem);
     if (ctx->aux) {
         cudaStreamSynchronize(ctx->aux);
         cudaStreamDestroy(ctx->aux);
@@ -1474,7 +1543,8 @@ int yk_fermion_force(yk_ctx* ctx, int c, const void* eta, double* F, yk_solve_st
     int rc = chain_solve(ctx, c, 2, stats);
     if (rc && rc != YK_ENOCONV) return rc;
     StepArgs s = chain_step_args(ctx, c);
-    YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
+    // the solve's states: chi from t64 where the solve left it there
+    YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream, ctx->d_state));
     YK_CK(cudaMemcpyAsync(F, C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream));
     YK_CK(cudaStreamSynchronize(ctx->stream));
     return rc;
@@ -1672,7 +1742,7 @@ int yk_condensate(yk_ctx* ctx, int c, double* cond, yk_solve_stats* stats)
         rc = chain_solve(ctx, c, 3, stats);   // fresh noise: Philox stream kind 3
         if (rc && rc != YK_ENOCONV) return rc;
         StepArgs s = chain_step_args(ctx, c);
-        YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream));
+        YK_CK(launch_force_drift(s, ctx->d_sys, 1, 1, ctx->stream, ctx->d_state));
         YK_CK(cudaMemcpyAsync(F.data(), C.drift, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
     }
     YK_CK(cudaStreamSynchronize(ctx->stream));
@@ -1880,7 +1950,7 @@ int yk_net_train(yk_ctx* ctx, int c, const yk_net_train_cfg* cfg, yk_net_train_s
     for (int src = 0; src < cfg->n_sources && rc == YK_OK; ++src) {
         const int kind = 100 + src;
         ctx->max_iter = keep_iter;
-        rc = chain_solve(ctx, c, kind, nullptr);
+        rc = chain_solve(ctx, c, kind, nullptr, true);
         if (rc == YK_ENOCONV) rc = YK_OK;
         if (rc) break;
         if (cudaMemcpyAsync(xstar, S.x, sizeof(double) * V4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
@@ -1889,7 +1959,7 @@ int yk_net_train(yk_ctx* ctx, int c, const yk_net_train_cfg* cfg, yk_net_train_s
         }
         for (int lv = 0; lv < cfg->n_levels && rc == YK_OK; ++lv) {
             ctx->max_iter = cfg->base_iter << lv;
-            rc = chain_solve(ctx, c, kind, nullptr);
+            rc = chain_solve(ctx, c, kind, nullptr, true);
             if (rc == YK_ENOCONV) rc = YK_OK;
             if (rc) break;
             const cudaError_t e = net_add_pair(C.net, cap, C.phi, C.a.m0, C.a.g, C.a.r, S.b, xstar, S.x, ctx->stream);

@@ -633,9 +633,11 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         return cv;
     }
     if (k == 0) {
-        st.stop2 = (a.tol_mode == YK_TOL_ABS) ? a.tol * a.tol : a.tol * a.tol * rr;
+        // even-odd solves: relative to |eta|^2 (slot 5), the rule of the full solve
+        const double ref = a.eo ? s[5] : rr;
+        st.stop2 = (a.tol_mode == YK_TOL_ABS) ? a.tol * a.tol : a.tol * a.tol * ref;
         st.rmax2 = rr;
-        st.rr0 = rr;
+        st.rr0 = ref;
     }
     if (!isfinite(rr)) return retire(0, YK_ENAN);
     // mixed: x is exact only at k = 0 and after a reliable update
@@ -2231,6 +2233,476 @@ static size_t halo_smem_bytes(int own, int Nx)
     return (3 * nP + (size_t)own + nT) * sizeof(float4) + nT * sizeof(float);
 }
 
+// ---------------------------------------------------------------------------
+// Even-odd mixed CG of the step's single-system solves (cg_eo_kernel).
+//
+// The force needs chi = (D^dag)^-1 eta, which the reference forms as D x from
+// CG on D^dag D (FermionicDrift.cu:57-80, CGsolver.cu:72-170).  D = A + H with
+// A = 2r + m0 + g sigma per site and H the hops, which join sites of opposite
+// parity (t + x) when Nt and Nx are even.  On the even sites D^dag chi = eta is
+// the Schur system
+//   S chi_e = rhs_e,   S = A_e - H^dag_eo A_o^-1 H^dag_oe,
+//   rhs_e = eta_e - H^dag_eo A_o^-1 eta_o,  chi_o = A_o^-1 (eta_o - H^dag_oe chi_e),
+// solved by CG on S S^dag with chi_e = S^dag y (CGNE), chi_e kept directly:
+// every iteration forms v = S^dag p and q = S v (four half-lattice hops, the
+// stencil work of one D^dag D over half the unknowns), alpha = |r|^2 / |v|^2,
+// chi_e += alpha v, r -= alpha q.  Its residual rhs_e - S chi_e is the true
+// residual of D^dag chi = eta (the odd sites' is zero by construction), the
+// quantity CG on D^dag D controls (there r = eta - D^dag (D x)), so the stop is
+// the same rule relative to |eta|; it takes about 2.3 times fewer iterations.
+//
+// Compact lattices: site (t, x) of parity q is t Nh + x / 2 of its class
+// (Nh = Nx / 2), full site 2 m + ((t + q) & 1).  a.sys are the systems'
+// compact views (Nx = Nh, V = V / 2, tiles over compact sites; the FP32
+// vectors compact; x = chi_e (FP64, compact) followed by rhs_e; t64 the odd
+// hops of the reliable updates and, at the end, chi in the full layout for the
+// force, CGState::chi_ready); a.sys_full the full records (eta in b, sigma).
+// A block owns the compact range [c0, c1), stages p, r, q of the previous
+// iteration on [c0 - 4Nh, c1 + 4Nh) and forms, in shared memory,
+//   w = -A_o^-1 H_oe p      on [c0 - 3Nh, c1 + 3Nh)   (odd)
+//   v = A_e p + H_eo w      on [c0 - 2Nh, c1 + 2Nh)   (even; = S^dag p)
+//   u = -A_o^-1 H^dag_oe v  on [c0 - Nh,  c1 + Nh)    (odd)
+//   q = A_e v + H^dag_eo u  on [c0, c1)               (even; = S v)
+// with the one reducing grid barrier per iteration, the scalar steps and the
+// FP64 reliable updates of cg_halo_kernel (its tile partials: |r|^2, |q|^2,
+// |v|^2 in the <p, Ap> slot, <r, q>).
+
+// Row, x-parity bit and the compact offsets of the x neighbours (opposite
+// class) of compact site m of parity q.
+__device__ __forceinline__ void eo_geom(int m, int q, int Nh, int sh, int& t, int& b, int& dxu, int& dxd)
+{
+    t = sh >= 0 ? (m >> sh) : m / Nh;
+    const int i = m - t * Nh;
+    b = (t + q) & 1;   // x = 2 i + b
+    dxu = b ? ((i == Nh - 1) ? 1 - Nh : 1) : 0;
+    dxd = b ? 0 : ((i == 0) ? Nh - 1 : -1);
+}
+
+// diag c + H (neighbours in `in` at j +- Nh, j + dxu, j + dxd) in FP32 (DAG:
+// the hops of D^dag)
+template <bool DAG>
+__device__ __forceinline__ Site<float, 1> eo_sm(const float4* in, int j, int Nh, int dxu, int dxd,
+                                                const Site<float, 1>& c, float diag, float r, float sp, float sm)
+{
+    return dirac_combine<float, 1, DAG>(c, ld_sm(in, j + Nh), ld_sm(in, j - Nh), ld_sm(in, j + dxu), ld_sm(in, j + dxd),
+                                        diag, r, sp, sm);
+}
+
+// the same in FP64 from a compact global vector (neighbours of compact m)
+template <bool DAG>
+__device__ __forceinline__ Site<double, 1> eo_gl(const double* in, int m, int Ve, int Nh, int dxu, int dxd,
+                                                 const Site<double, 1>& c, double diag, double r, double sp, double sm)
+{
+    const int mu = m + Nh >= Ve ? m + Nh - Ve : m + Nh, md = m - Nh < 0 ? m - Nh + Ve : m - Nh;
+    return dirac_combine<double, 1, DAG>(c, load_site<double, 1>(in, mu), load_site<double, 1>(in, md),
+                                         load_site<double, 1>(in, m + dxu), load_site<double, 1>(in, m + dxd), diag, r,
+                                         sp, sm);
+}
+
+__global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
+{
+    constexpr int K = 1;
+    constexpr int kSkipIm = (1 << 3) | (1 << 5);
+    using W = float;
+    extern __shared__ float4 hsm[];
+    const int hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;
+    __shared__ double red[128];
+    __shared__ SysLocal sl[kMaxSysPerBlock];
+    __shared__ int nsl;
+    __shared__ unsigned char tslot[kMaxTilesPerBlock];
+    __shared__ Deps deps;
+    __shared__ int s_nact, s_anyru;
+    __shared__ int s_cnt[2];
+    __shared__ int s_esc[4], s_fast;
+    __shared__ CGState lst;
+    __shared__ FastShadow fsh;
+    __shared__ SysDev S;    // the compact view
+    __shared__ SysDev SF;   // the full record
+    __shared__ CGArgs sa;
+    const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
+    const int te = min(tb + a.tiles_per_block, a.tile_end);
+    setup_block(a, tb, te, sl, &nsl, tslot, &deps);
+    if (*(volatile int*)a.err) return;
+    if (threadIdx.x == 0) {
+        s_fast = 0;
+        lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
+        lst.active = 1;
+        lst.iters = lst.converged = lst.status = lst.n_ru = lst.chi_ready = 0;
+        lst.mode = kStep;
+        fsh.valid = 0;
+        S = a.sys[a.sys_first];
+        SF = a.sys_full[a.sys_first];
+        sa = a;
+    }
+    __syncthreads();
+    const int Nt = S.Nt, Nh = S.Nx, Ve = S.V;
+    const int sh = (Nh & (Nh - 1)) == 0 ? __ffs(Nh) - 1 : -1;
+    const int c0 = a.tiles[tb].y;
+    const int c1 = min(a.tiles[te - 1].y + kTile, Ve);
+    const int own = c1 - c0;
+    const int nP = own + 8 * Nh;
+    const int cbase = c0 - 4 * Nh;                 // compact site of buffer index 0
+    const int pfirst = wrap_site(cbase, Ve);
+    float4* P_st = hsm;                            // p on [0, nP)
+    float4* R_st = P_st + nP;                      // r there
+    float4* A_st = R_st + nP;                      // q there
+    float4* X_st = A_st + nP;                      // chi_e increment on the own sites
+    float4* V_own = X_st + own;                    // v of the previous iteration on the own sites
+    float4* W_b = V_own + own;                     // w on [Nh, own + 7Nh), later u on [3Nh, own + 5Nh)
+    float4* V_b = W_b + (own + 6 * Nh);            // v on [2Nh, own + 6Nh)
+    float* de_b = reinterpret_cast<float*>(V_b + (own + 4 * Nh));   // A_e on [2Nh, own + 6Nh)
+    float* di_b = de_b + (own + 4 * Nh);                            // 1 / A_o on [Nh, own + 7Nh)
+    float4* Wp = W_b - Nh;                         // buffer-index views
+    float4* Vp = V_b - 2 * Nh;
+    const float* dep = de_b - 2 * Nh;
+    const float* dip = di_b - Nh;
+    const float rw = (float)S.r;
+    const double r64 = S.r;
+    auto diag_at = [&](int m, int q) -> double {
+        int t, b, du, dd;
+        eo_geom(m, q, Nh, sh, t, b, du, dd);
+        return 2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b];
+    };
+    for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads)
+        de_b[j - 2 * Nh] = (float)diag_at(wrap_site(cbase + j, Ve), 0);
+    for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads)
+        di_b[j - Nh] = (float)(1.0 / diag_at(wrap_site(cbase + j, Ve), 1));
+    const double* chi_e = S.x;                      // compact FP64
+    const double* rhs_e = S.x + 4 * (size_t)Ve;
+    unsigned epoch = 0, gen = 0;
+    int staged_k = -1;
+
+    auto stage = [&](int mode, int cur, int prv) {
+        const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
+        const float* Pl = S.p32[prv];
+        const float* Al = prv == 0 ? S.Ap32 : S.t32;
+        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
+            const int m = wrap_site(pfirst + j, Ve);
+            cp_async16(P_st + j, Pl + 4 * (size_t)m);
+            cp_async16(R_st + j, Rl + 4 * (size_t)m);
+            if (mode == kStep) cp_async16(A_st + j, Al + 4 * (size_t)m);
+        }
+        cp_async_commit();
+    };
+
+    // A1: p_k (r_k and the chi_e increment on the own sites) on [0, nP)
+    auto pass_a1 = [&](int mode, int cur, int prv) {
+        const SysLocal& L = sl[0];
+        const W ar = L.f_alpha_re, beta = L.f_beta, cre = L.f_c_re, cim = L.f_c_im;
+        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
+            const int o = j - 4 * Nh;
+            const bool is_own = o >= 0 && o < own;
+            const int m = c0 + o;
+            const Site<W, K> po = ld_sm(P_st, j);
+            Site<W, K> p;
+            if (mode == kStep) {
+                Site<W, K> r = ld_sm(R_st, j);
+                site_axpy<W, K>(r, -ar, W(0), ld_sm(A_st, j));
+#pragma unroll
+                for (int i = 0; i < 4; ++i) p.v[i] = fma(beta, po.v[i], r.v[i]);
+                if (is_own) {
+                    Site<W, K> x = ld_sm(X_st, o);
+                    site_axpy<W, K>(x, ar, W(0), ld_sm(V_own, o));
+                    st_sm(X_st, o, x);
+                    YK_ST(W, K, S.r32[cur], m, r);
+                    YK_ST(W, K, S.p32[cur], m, p);
+                    st_sm(R_st, j, r);
+                }
+            } else if (mode == kRedo) {
+                p = p_next<W, K>(ld_sm(R_st, j), po, beta, cre, cim);
+                if (is_own) YK_ST(W, K, S.p32[cur], m, p);
+            } else {
+                p = po;
+            }
+            st_sm(P_st, j, p);
+        }
+    };
+
+    // w, v, u on their ranges (v of the own sites also to V_own)
+    auto pass_wvu = [&]() {
+        Site<W, K> zero;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) zero.v[i] = W(0);
+        for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads) {
+            int t, b, du, dd;
+            eo_geom(wrap_site(cbase + j, Ve), 1, Nh, sh, t, b, du, dd);
+            const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            Site<W, K> h = eo_sm<false>(P_st, j, Nh, du, dd, zero, W(0), rw, sp, sm);
+            const W s = -dip[j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] *= s;
+            st_sm(Wp, j, h);
+        }
+        __syncthreads();
+        for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads) {
+            int t, b, du, dd;
+            eo_geom(wrap_site(cbase + j, Ve), 0, Nh, sh, t, b, du, dd);
+            const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            const Site<W, K> v = eo_sm<false>(Wp, j, Nh, du, dd, ld_sm(P_st, j), dep[j], rw, sp, sm);
+            st_sm(Vp, j, v);
+            const int o = j - 4 * Nh;
+            if (o >= 0 && o < own) st_sm(V_own, o, v);
+        }
+        __syncthreads();
+        for (int j = 3 * Nh + threadIdx.x; j < own + 5 * Nh; j += kHaloThreads) {
+            int t, b, du, dd;
+            eo_geom(wrap_site(cbase + j, Ve), 1, Nh, sh, t, b, du, dd);
+            const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            Site<W, K> h = eo_sm<true>(Vp, j, Nh, du, dd, zero, W(0), rw, sp, sm);
+            const W s = -dip[j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] *= s;
+            st_sm(Wp, j, h);   // u
+        }
+    };
+
+    // q = S v on the own sites -> A p buffer of iteration cur; the tile partials.
+    // Round 0 adds |eta|^2 of the compact index's two full sites in slot 5.
+    auto pass_q = [&](int cur, bool round0) {
+        float* Ac = cur == 0 ? S.Ap32 : S.t32;
+        for (int base = tb; base < te; base += 2) {
+            const int tile = base + hf;
+            const bool tile_on = tile < te;
+            const int m = tile_on ? c0 + (tile - tb) * kTile + ts : Ve;
+            const bool on = m < Ve;
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+            if (on) {
+                const int j = m - cbase;
+                int t, b, du, dd;
+                eo_geom(m, 0, Nh, sh, t, b, du, dd);
+                const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+                const Site<W, K> v = ld_sm(Vp, j);
+                const Site<W, K> q = eo_sm<true>(Wp, j, Nh, du, dd, v, dep[j], rw, sp, sm);
+                YK_ST(W, K, Ac, m, q);
+                const Site<W, K> r = ld_sm(R_st, j);
+                W rq, dummy;
+                site_dot<W, K>(r, q, rq, dummy);
+                f[0] = FF{site_norm2<W, K>(r), 0.f};
+                f[1] = FF{site_norm2<W, K>(q), 0.f};
+                f[2] = FF{site_norm2<W, K>(v), 0.f};
+                f[4] = FF{rq, 0.f};
+                if (round0) {
+                    const Site<double, K> e0 = load_site<double, K>(SF.b, 2 * m);
+                    const Site<double, K> e1 = load_site<double, K>(SF.b, 2 * m + 1);
+                    f[5] = ff_of(site_norm2<double, K>(e0) + site_norm2<double, K>(e1));
+                }
+            }
+            if (round0)
+                put_partial_ff<(1 << 3), true>(a, tile, tile_on, f, red);
+            else if (s_fast)
+                put_partial_ff<kSkipIm, false>(a, tile, tile_on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
+            else
+                put_partial_ff<kSkipIm, false>(a, tile, tile_on, f, red);
+        }
+    };
+
+    auto reduce = [&](int kk, bool ru) -> bool {
+        auto prefetch = [&]() {
+            if (ru) return;
+            const int k1 = kk + 1;
+            stage(kStep, k1 & 1, (k1 & 1) ^ 1);
+            staged_k = k1;
+        };
+        return solo_reduce_body<K, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh,
+                                         prefetch);
+    };
+
+    // the reliable update of iteration k: fold chi_e += xs + alpha v_{k-1} in
+    // FP64; u = -A_o^-1 H^dag_oe chi_e on the own odd sites (t64, compact);
+    // r = rhs_e - (A_e chi_e + H^dag_eo u) on the own even sites -> r32[cur];
+    // partials |r|^2, <r, p_{k-1}>
+    auto reliable = [&](int cur, int prv) -> bool {
+        const SysLocal& L = sl[0];
+        double* chi = S.x;
+        for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+            const int m = c0 + o;
+            Site<double, K> xv = load_site<double, K>(chi, m);
+            const Site<W, K> xs = ld_sm(X_st, o);
+            const Site<W, K> vv = ld_sm(V_own, o);
+            Site<W, K> zw;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                xv.v[i] += (double)xs.v[i];
+                xv.v[i] = fma(L.alpha_re, (double)vv.v[i], xv.v[i]);
+                zw.v[i] = W(0);
+            }
+            store_site<double, K>(chi, m, xv);
+            st_sm(X_st, o, zw);
+        }
+        if (!nsync(a, ++epoch, deps)) return false;
+        Site<double, K> zero;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
+        for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+            const int m = c0 + o;
+            int t, b, du, dd;
+            eo_geom(m, 1, Nh, sh, t, b, du, dd);
+            const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
+            Site<double, K> h = eo_gl<true>(chi, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
+            const double s = -1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] *= s;
+            store_site<double, K>(S.t64, m, h);
+        }
+        if (!nsync(a, ++epoch, deps)) return false;
+        for (int base = tb; base < te; base += 2) {
+            const int tile = base + hf;
+            const bool tile_on = tile < te;
+            const int m = tile_on ? c0 + (tile - tb) * kTile + ts : Ve;
+            const bool on = m < Ve;
+            double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            if (on) {
+                int t, b, du, dd;
+                eo_geom(m, 0, Nh, sh, t, b, du, dd);
+                const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
+                const double de = 2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b];
+                const Site<double, K> sx =
+                    eo_gl<true>(S.t64, m, Ve, Nh, du, dd, load_site<double, K>(chi, m), de, r64, sp, sm);
+                const Site<double, K> bv = load_site<double, K>(rhs_e, m);
+                const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
+                Site<double, K> rd, pd;
+                Site<W, K> rw32;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    rd.v[i] = bv.v[i] - sx.v[i];
+                    rw32.v[i] = (float)rd.v[i];
+                    pd.v[i] = (double)pw.v[i];
+                }
+                YK_ST(W, K, S.r32[cur], m, rw32);
+                v[0] = site_norm2<double, K>(rd);
+                site_dot<double, K>(rd, pd, v[2], v[3]);
+            }
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+            put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
+        }
+        return true;
+    };
+
+    // ---------------- round 0: eta on the own sites of both classes (kept in
+    // b for the force), chi_e = 0, rhs_e, r_0 = p_0 = rhs_e
+    for (int o = threadIdx.x; o < 2 * own; o += kHaloThreads) {
+        const int m = c0 + (o >> 1), n = 2 * m + (o & 1);   // the compact index's two full sites
+        const Site<double, K> bv = SF.gen_eta ? eta_of_step<K>(SF, n, a.eta_kind) : load_site<double, K>(SF.b, n);
+        if (SF.gen_eta) store_site<double, K>(SF.b, n, bv);
+    }
+    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+        Site<double, K> z;
+        Site<W, K> zw;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            z.v[i] = 0.0;
+            zw.v[i] = W(0);
+        }
+        store_site<double, K>(S.x, c0 + o, z);
+        st_sm(X_st, o, zw);
+        st_sm(V_own, o, zw);
+    }
+    if (!nsync(a, ++epoch, deps)) return;
+    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+        const int m = c0 + o;
+        int t, b, du, dd;
+        eo_geom(m, 0, Nh, sh, t, b, du, dd);
+        const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
+        // the odd neighbours' -A_o^-1 eta_o, formed here from b
+        Site<double, K> nb[4];
+        const int mo[4] = {m + Nh >= Ve ? m + Nh - Ve : m + Nh, m - Nh < 0 ? m - Nh + Ve : m - Nh, m + du, m + dd};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int t2, b2, u2, d2;
+            eo_geom(mo[q], 1, Nh, sh, t2, b2, u2, d2);
+            const int n2 = 2 * mo[q] + b2;
+            nb[q] = load_site<double, K>(SF.b, n2);
+            const double s = -1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n2]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) nb[q].v[i] *= s;
+        }
+        const Site<double, K> e = load_site<double, K>(SF.b, 2 * m + b);
+        // eta_e + H^dag_eo (-A_o^-1 eta_o)
+        const Site<double, K> rh = dirac_combine<double, K, true>(e, nb[0], nb[1], nb[2], nb[3], 1.0, r64, sp, sm);
+        store_site<double, K>(const_cast<double*>(rhs_e), m, rh);
+        Site<W, K> rw32;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rw32.v[i] = (float)rh.v[i];
+        YK_ST(W, K, S.r32[0], m, rw32);
+        YK_ST(W, K, S.p32[0], m, rw32);
+    }
+    if (!nsync(a, ++epoch, deps)) return;
+    stage(kHaloInit, 0, 0);
+    cp_async_wait_all();
+    pass_a1(kHaloInit, 0, 0);
+    __syncthreads();
+    pass_wvu();
+    __syncthreads();
+    pass_q(0, true);
+    if (!reduce(0, false)) return;
+
+    int k = 1;
+    while (k <= a.max_iter) {
+        const int mode = sl[0].mode;
+        if (s_nact == 0 || mode == kRu) {
+            if (staged_k == k) cp_async_wait_all();
+            staged_k = -1;
+        }
+        if (s_nact == 0) break;
+        const int cur = k & 1, prv = cur ^ 1;
+        if (mode == kRu) {
+            if (!reliable(cur, prv)) return;
+            if (!reduce(k, true)) return;
+            continue;
+        }
+        if (!(mode == kStep && staged_k == k)) {
+            if (staged_k == k) cp_async_wait_all();
+            stage(mode, cur, prv);
+        }
+        staged_k = -1;
+        cp_async_wait_all();
+        pass_a1(mode, cur, prv);
+        __syncthreads();
+        pass_wvu();
+        __syncthreads();
+        pass_q(cur, false);
+        if (!reduce(k, false)) return;
+        ++k;
+    }
+    // chi of both classes in the full layout for the force (t64): every
+    // block's final chi_e and its own odd sites' chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
+    if (!nsync(a, ++epoch, deps)) return;
+    Site<double, K> zero;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
+    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+        const int m = c0 + o;
+        int t, b, du, dd;
+        eo_geom(m, 0, Nh, sh, t, b, du, dd);
+        store_site<double, K>(SF.t64, 2 * m + b, load_site<double, K>(S.x, m));
+        eo_geom(m, 1, Nh, sh, t, b, du, dd);
+        const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
+        const Site<double, K> h = eo_gl<true>(S.x, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
+        const int n = 2 * m + b;
+        const Site<double, K> e = load_site<double, K>(SF.b, n);
+        const double inv = 1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n]);
+        Site<double, K> co;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) co.v[i] = (e.v[i] - h.v[i]) * inv;
+        store_site<double, K>(SF.t64, n, co);
+    }
+    // t64 holds chi however the solve ended (also when it retired at k = 0)
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.sys_first].chi_ready = 1;
+}
+
+// Shared memory of cg_eo_kernel for own compact sites per block and Nh.
+static size_t eo_smem_bytes(int own, int Nh)
+{
+    const size_t nP = (size_t)own + 8 * (size_t)Nh;
+    const size_t f4 = 3 * nP + 2 * (size_t)own + ((size_t)own + 6 * Nh) + ((size_t)own + 4 * Nh);
+    const size_t fl = ((size_t)own + 4 * Nh) + ((size_t)own + 6 * Nh);
+    return f4 * sizeof(float4) + fl * sizeof(float);
+}
+
 // Failure detection without a fault: block 0 waits through nsync on block
 // 1's neighbour flag, which block 1 never sets (it returns at once); the
 // bounded wait gives up, records YK_ETIMEOUT in *err and the kernel returns.
@@ -2364,6 +2836,33 @@ static bool halo_takes(int Nt, int Nx, int tpb, size_t* smem)
     return *smem <= kHaloMaxSmem;
 }
 
+// Whether cg_eo_kernel takes the single-system solve of A = D^dag D on an
+// Nt x Nx lattice (both even) whose blocks own tpb compact tiles each: at most
+// 8 tiles per block, the widened compact range within the compact lattice,
+// and its shared memory within kHaloMaxSmem.
+static bool eo_takes(int Nt, int Nx, int tpb, size_t* smem)
+{
+    if (Nt < 2 || Nx < 4 || (Nt & 1) || (Nx & 1) || tpb < 1 || tpb > 8) return false;
+    const long long own = (long long)tpb * kTile, Nh = Nx / 2, Ve = (long long)Nt * Nh;
+    if (own + 8 * Nh > Ve) return false;
+    *smem = eo_smem_bytes((int)own, (int)Nh);
+    return *smem <= kHaloMaxSmem;
+}
+
+static int eo_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        cudaFuncSetAttribute((const void*)cg_eo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHaloMaxSmem);
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel, kHaloThreads, kHaloMaxSmem);
+        maxg = per * nsm;
+    }
+    return maxg;
+}
+
 static int halo_max_grid()
 {
     static int maxg = -1;
@@ -2378,7 +2877,11 @@ static int halo_max_grid()
     return maxg;
 }
 
-void cg_halo_init() { halo_max_grid(); }
+void cg_halo_init()
+{
+    halo_max_grid();
+    eo_max_grid();
+}
 
 static int capped(int maxg, int cap) { return cap > 0 && cap < maxg ? cap : maxg; }
 
@@ -2405,6 +2908,39 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     unsigned threads = cg_threads<K>();
     size_t smem = 0;
     if constexpr (K == 1 && MIXED) {
+        // the even-odd solve of the step's chi (a single system of A = D^dag D
+        // on an even lattice, when the caller gave the compact views)
+        if (a.sys_count == 1 && a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr) {
+            CGArgs e = a;
+            e.sys_full = a.sys;
+            e.sys = a.sys_eo;
+            e.tiles = a.eo_tiles;
+            e.tile_begin = a.eo_tile_begin;
+            e.tile_end = a.eo_tile_end;
+            e.eo = 1;
+            int etpb = 1;
+            const int eg = cg_grid_for(e.tile_end - e.tile_begin, capped(eo_max_grid(), a.grid_cap), &etpb);
+            size_t es = 0;
+            if (eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, etpb, &es)) {
+                e.tiles_per_block = etpb;
+                e.grid = eg;
+                if (grid_out) *grid_out = eg;
+                if (kernel_out) *kernel_out = 3;
+                cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(eg);
+                cfg.blockDim = dim3(kHaloThreads);
+                cfg.dynamicSmemBytes = es;
+                cfg.stream = stream;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeCooperative;
+                attr[0].val.cooperative = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                void* args[] = {&e};
+                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel, args);
+            }
+        }
         // the same tile partition as cg_kernel<1, true>, so the same partials
         size_t hs = 0;
         if (a.sys_count == 1 && halo_takes(a.solo_nt, a.solo_nx, tpb, &hs) && grid <= halo_max_grid()) {

@@ -129,6 +129,18 @@ struct CGArgs {
     // were computed for, [1 + b] = first tile of block b, [1 + grid] = end;
     // used when [0] equals the launch's grid, else the uniform ranges
     const int* balance;
+    // even-odd solve of a single mixed system (the step's chi = (D^dag)^-1 eta):
+    // the systems' compact views and their tile table, given by the caller
+    // (null: not available); launch_cg takes the even-odd kernel when the
+    // lattice qualifies
+    SysDev* sys_eo;
+    const int2* eo_tiles;
+    int eo_tile_begin, eo_tile_end;
+    // inside an even-odd launch: a.sys are the compact views, sys_full the
+    // systems' full records (eta, sigma, t64); the first stopping threshold is
+    // relative to |eta|^2, tile partial slot 5 of round 0
+    const SysDev* sys_full;
+    int eo;
 };
 
 // Per-chain device record of the Langevin step.

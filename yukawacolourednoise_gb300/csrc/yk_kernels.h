@@ -16,7 +16,8 @@ cudaError_t launch_dirac(const void* in, void* out, const double* sigma, int Nt,
                          cudaStream_t stream, const double* pi = nullptr);
 
 // Batched CG (yk_cg.cu).  Also launches its one-block preparation kernel.
-// grid_out: blocks launched; kernel_out: 0 cg_kernel, 1 cg_halo_kernel (either may be null)
+// grid_out: blocks launched; kernel_out: 0 cg_kernel, 1 cg_halo_kernel, 3 cg_eo_kernel
+// (the even-odd solve: a.sys_eo given, chi = (D^dag)^-1 b left in t64) (either may be null)
 cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, int* grid_out, int* kernel_out = nullptr);
 // Work-balanced block ranges (CGArgs::balance) for the next solve of the
 // systems of `a`, from their iteration counts in the solve just finished;
