@@ -51,7 +51,7 @@ def test_c2_headline_steps_from_the_bench_start(ylib, cuda):
         ctx.profile_begin()   # the steps as direct launches: the kernel that ran is reported
         ctx.step(1)
         pr = ctx.profile_end()
-        assert pr.cg_kernel in (1, 3), "the headline step's solve runs the halo or the even-odd CG kernel"
+        assert pr.cg_kernel == 3, "the headline step's solve runs the even-odd CG kernel"
         got = [ctx.get_field()]
         for _ in range(3):
             ctx.step(1)

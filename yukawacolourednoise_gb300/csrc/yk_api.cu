@@ -781,7 +781,7 @@ int pion_setup(yk_ctx* ctx)
 int eo_setup(yk_ctx* ctx, const std::vector<SysDev>& hs)
 {
     const char* env = getenv("YK_CG_EO");
-    if (!(env && env[0] == '1') || ctx->nsys != 1 || ctx->precision != YK_MIXED || !ctx->cg_halo || ctx->cg_cluster ||
+    if ((env && env[0] == '0') || ctx->nsys != 1 || ctx->precision != YK_MIXED || !ctx->cg_halo || ctx->cg_cluster ||
         ctx->pions)
         return YK_OK;
     const Chain* C = nullptr;
