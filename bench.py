@@ -715,6 +715,9 @@ def main(argv=None):
     ap.add_argument("--full-scale", action="store_true",
                     help="only the full form at scale (8 chains of 1024^2, 8 RHS; one JSON object; minutes)")
     ap.add_argument("--no-full-scale", action="store_true", help="skip the full form at scale in the default run")
+    ap.add_argument("--steps-only", type=int, default=0, metavar="L",
+                    help="only --steps mixed Langevin steps of an L x L lattice after --warmup (the workload's "
+                         "couplings, uniform start; one JSON object; profiling runs)")
     ap.add_argument("--dirac-only", type=int, default=0, metavar="L",
                     help="only the Dirac apply on an L x L lattice (one JSON object; profiling runs)")
     ap.add_argument("--no-reference-gpu", action="store_true",
@@ -727,6 +730,27 @@ def main(argv=None):
         import yukawacolourednoise_gb300 as yk
         stream = torch.cuda.Stream()
         print(json.dumps({"full_scale": full_scale(yk, torch, stream)}), flush=True)
+        return 0
+    if args.steps_only:
+        import torch
+        import yukawacolourednoise_gb300 as yk
+        L = args.steps_only
+        stream = torch.cuda.Stream()
+        with yk.Context(make_params(yk, args.precision, Nt=L, Nx=L)) as ctx:
+            ctx.set_stream(stream.cuda_stream)
+            ctx.step(args.warmup)
+            ctx.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                ctx.step(args.steps)
+                b.record(stream)
+            stream.synchronize()
+            o = ctx.observables()
+            print(json.dumps({"steps_only": {"lattice": [L, L], "steps": args.steps,
+                                             "ms_per_step": round(a.elapsed_time(b) / args.steps, 4),
+                                             "cg_iterations_last_step": o.cg_iterations, "status": o.status}}),
+                  flush=True)
         return 0
     if args.dirac_only:
         import torch
