@@ -107,3 +107,28 @@ def test_c3_shaped_batch(ylib, cuda):
                                      max_iter=20000, fixed_dt=0.01)
         err = np.abs(got[c] - phi).max()
         assert err < 1e-8, (c, p.Nt, err)
+
+
+def test_headline_steps_are_reproducible_with_the_auxiliary_stream(ylib, cuda, monkeypatch):
+    # the step's coloured noise and the next step's sources run on an
+    # auxiliary stream beside the CG; whatever their timing, 30 graph-replayed
+    # steps from the bench's start give the same field, bit for bit, as the
+    # same steps with everything on one stream, and as a second run
+    yk = ylib
+    d = np.load(START)
+    phi, step0 = d["phi"].copy(), int(d["step"])
+    p = base(yk, Nt=256, Nx=256, fixed_dt=0.01, precision=yk.YK_MIXED, cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL,
+             cg_max_iter=20000, reliable_every=50, reliable_delta=0.001)
+    fields = []
+    for overlap in ("1", "1", "0"):
+        monkeypatch.setenv("YK_NOISE_OVERLAP", overlap)
+        stream = cuda.cuda.Stream()
+        with yk.Context(p) as ctx:
+            ctx.set_stream(stream.cuda_stream)
+            ctx.set_field(phi)
+            ctx.set_step(step0)
+            ctx.step(30)
+            fields.append(ctx.get_field())
+            assert ctx.observables().status == 0
+    assert np.array_equal(fields[0], fields[1])
+    assert np.array_equal(fields[0], fields[2])

@@ -412,11 +412,15 @@ int enqueue_step(yk_ctx* ctx)
     prof_begin(ctx, &e);
     YK_CK(launch_force_drift(s, ctx->d_sys, 0, 1, ctx->stream, ctx->d_state));
     prof_end(ctx, 2, e, 1);
-    if (overlap) YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));   // xi of this step
+    if (overlap) {
+        YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));   // xi of this step
+        // the next step's eta: its kernel reads the chain's step counter, which
+        // the update advances, so it must be done before the update runs
+        YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join2_ev, 0));
+    }
     prof_begin(ctx, &e);
     YK_CK(launch_update(s, ctx->d_state, ctx->stream));
     prof_end(ctx, 3, e, 1);
-    if (overlap) YK_CK(cudaStreamWaitEvent(ctx->stream, ctx->join2_ev, 0));   // the next step's eta
     if (ctx->profiling) ctx->prof_steps += 1;
     return YK_OK;
 }
