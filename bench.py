@@ -121,9 +121,9 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def ncu_traffic():
-    """DRAM bytes per CG launch from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "cg_halo_kernel_256x256_traffic.json"
+def ncu_traffic(kernel):
+    """DRAM bytes per CG iteration of `kernel` from its committed ncu summary, if any."""
+    f = ROOT / "profiles" / f"{kernel}_256x256_traffic.json"
     if f.exists():
         try:
             return json.loads(f.read_text())
@@ -273,7 +273,7 @@ def roofline(pr, precision):
     alg_bytes = pr.cg_site_iterations * bpi / max(pr.cg_launches, 1)
     pk = peaks()
     achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
-    tr = ncu_traffic()
+    tr = ncu_traffic(kname)
     traffic = None
     if tr and tr.get("precision") == precision and tr.get("kernel", "cg_kernel<1,mixed>") == kname:
         traffic = tr["dram_bytes_per_iteration"] * pr.cg_iterations / max(pr.cg_launches, 1)
