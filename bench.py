@@ -60,7 +60,7 @@ def workload(precision: str) -> dict:
     return {"workload": f"2D {NT}x{NX} Yukawa Langevin step (coloured noise + CG force + Euler), "
                         f"CG rel-res 1e-10, {precision} CG, 1 RHS, fixed dt 0.01",
             "lattice": [NT, NX], "n_rhs": 1, "precision": precision, "cg_tol_rel": 1e-10,
-            "reliable_every": 50, "reliable_delta": 0.001, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
+            "reliable_every": 50, "reliable_delta": 1e-5, "m2": -0.5, "lambda": 1.0, "g": 0.5, "m0": 0.1, "cut_fraction": CUT,
             "l2": "flushed between timed steps (256 MiB write)"}
 
 
@@ -68,7 +68,7 @@ def make_params(yk, precision, seed=1234, Nt=NT, Nx=NX):
     return yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=0.5, fermion_mass=0.1,
                              wilson_param=1.0, cut_fraction=CUT, Nt=Nt, Nx=Nx, fixed_dt=0.01,
                              precision=yk.YK_MIXED if precision == "mixed" else yk.YK_FP64,
-                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=50, reliable_delta=0.001,
+                             cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=50, reliable_delta=1e-5,
                              n_rhs=1, seed=seed, init=yk.YK_INIT_PHILOX)
 
 

@@ -309,8 +309,12 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps);
  * the grid of the step's persistent CG, i.e. how many 256-site tiles each
  * block owns, chosen by timing the step's CG at candidate grids (the
  * co-resident maximum, 3/4 and 1/2 of it, one block per SM, half of that).
- * The learned solver's convolution tile (rows x columns) is chosen by timing
- * candidates on the network's first solve.  Results never depend on either
+ * Where the step's coloured noise and the next step's sources run -- on an
+ * auxiliary stream beside the CG, on the SMs the CG's grid leaves free, or on
+ * the main stream after the CG -- is chosen by timing whole steps of both forms
+ * (the chains' state restored after each).  The learned solver's convolution
+ * tile (rows x columns) is chosen by timing candidates on the network's first
+ * solve.  Results never depend on either
  * choice.  yk_langevin_step tunes automatically before it captures the step
  * graph (environment YK_AUTOTUNE=0 at context creation: not automatically);
  * yk_autotune tunes now (dropping a captured graph) and reports. */
@@ -323,6 +327,9 @@ typedef struct yk_tune_result {
     int conv_rows, conv_cols;  /* chain 0 network's convolution tile (0: none yet)   */
     int conv_layers_per_launch; /* its layers per launch (1 .. 2 x layers)           */
     double pcg_inner_tol;      /* its PCG's inner tolerance, chosen by timing (0: undecided) */
+    int noise_overlap;         /* the step's noise and next sources: 1 on an auxiliary stream */
+                               /*   beside the CG, 0 on the main stream after it, -1 untuned  */
+    float step_ms_overlap, step_ms_serial;   /* two timed steps of each form            */
 } yk_tune_result;
 int yk_autotune(yk_ctx* ctx, yk_tune_result* out);
 /* (Environment YK_NET_TILE=RxW or RxWxG, e.g. 8x64x4, fixes the convolution

@@ -120,8 +120,11 @@ def test_headline_steps_are_reproducible_with_the_auxiliary_stream(ylib, cuda, m
     p = base(yk, Nt=256, Nx=256, fixed_dt=0.01, precision=yk.YK_MIXED, cg_tol=1e-10, cg_tol_mode=yk.YK_TOL_REL,
              cg_max_iter=20000, reliable_every=50, reliable_delta=0.001)
     fields = []
-    for overlap in ("1", "1", "0"):
+    # untuned (the auxiliary stream whenever the CG leaves SMs free), twice;
+    # one stream; and the autotuner's choice between the two
+    for overlap, tune in (("1", "0"), ("1", "0"), ("0", "0"), ("1", "1")):
         monkeypatch.setenv("YK_NOISE_OVERLAP", overlap)
+        monkeypatch.setenv("YK_AUTOTUNE", tune)
         stream = cuda.cuda.Stream()
         with yk.Context(p) as ctx:
             ctx.set_stream(stream.cuda_stream)
@@ -129,6 +132,9 @@ def test_headline_steps_are_reproducible_with_the_auxiliary_stream(ylib, cuda, m
             ctx.set_step(step0)
             ctx.step(30)
             fields.append(ctx.get_field())
-            assert ctx.observables().status == 0
-    assert np.array_equal(fields[0], fields[1])
-    assert np.array_equal(fields[0], fields[2])
+            assert ctx.observables().status == 0 and ctx.get_step() == step0 + 30
+            t = ctx.tune_report()
+            if tune == "1":
+                assert t.noise_overlap in (0, 1) and t.step_ms_overlap > 0 and t.step_ms_serial > 0
+    for f in fields[1:]:
+        assert np.array_equal(fields[0], f)

@@ -102,7 +102,8 @@ class SolveStats(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("cg_grid", C.c_int), ("cg_grid_max", C.c_int), ("cg_candidates", C.c_int),
                 ("cg_ms_chosen", C.c_float), ("cg_ms_max", C.c_float), ("conv_rows", C.c_int),
-                ("conv_cols", C.c_int), ("conv_layers_per_launch", C.c_int), ("pcg_inner_tol", C.c_double)]
+                ("conv_cols", C.c_int), ("conv_layers_per_launch", C.c_int), ("pcg_inner_tol", C.c_double),
+                ("noise_overlap", C.c_int), ("step_ms_overlap", C.c_float), ("step_ms_serial", C.c_float)]
 
 
 class NetTrainCfg(C.Structure):

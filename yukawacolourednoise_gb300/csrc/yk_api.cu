@@ -108,6 +108,7 @@ struct yk_ctx {
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join2_ev = nullptr;
     int n_sm = 0;
     bool noise_overlap = true;   // YK_NOISE_OVERLAP=0 at context creation: never
+    int overlap_choice = -1;     // the autotuner's choice (1 beside the CG, 0 after it; -1 untuned: beside)
     std::vector<Chain> ch;
     void* mem = nullptr;
     // step tables
@@ -359,7 +360,7 @@ int enqueue_step(yk_ctx* ctx)
         g.tile_end = ctx->n_sys_tiles;
         free_sm = ctx->n_sm - cg_predict_grid(g, ctx->precision == YK_MIXED);
     }
-    const bool overlap = free_sm >= 8;
+    const bool overlap = free_sm >= 8 && ctx->overlap_choice != 0;
     if (overlap) {
         YK_CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
         YK_CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
@@ -626,6 +627,79 @@ int chain_solve(yk_ctx* ctx, int c, int kind, yk_solve_stats* stats, bool want_x
     return YK_OK;
 }
 
+// Where the step's coloured noise and the next step's sources run: beside the
+// CG on an auxiliary stream (the SMs its grid leaves free) or after it on the
+// main stream.  A short solve finishes before the auxiliary work on the few
+// free SMs, and the update then waits for it.  Both forms are timed over two
+// steps after one warm-up step, each from the chains' state saved here and
+// restored after (fields and chain records; the steps are deterministic, so
+// tuning changes no result).
+int tune_overlap(yk_ctx* ctx)
+{
+    yk_tune_result& T = ctx->tune;
+    if (!ctx->noise_overlap || ctx->cg_cluster || ctx->nsys == 0 || ctx->nrows == 0 || ctx->pions) return YK_OK;
+    CGArgs g = base_args(ctx);
+    g.tile_begin = 0;
+    g.tile_end = ctx->n_sys_tiles;
+    if (ctx->n_sm - cg_predict_grid(g, ctx->precision == YK_MIXED) < 8) return YK_OK;
+    const int nch = (int)ctx->ch.size();
+    size_t nphi = 0;
+    for (const Chain& C : ctx->ch) nphi += (size_t)C.V;
+    void* save = nullptr;
+    if (cudaMalloc(&save, sizeof(double) * nphi + sizeof(ChainDev) * nch) != cudaSuccess) {
+        cudaGetLastError();
+        return YK_OK;   // no room to save the state: keep the untuned form
+    }
+    double* sphi = static_cast<double*>(save);
+    ChainDev* sch = reinterpret_cast<ChainDev*>(sphi + nphi);
+    auto copy_state = [&](bool to_save) -> cudaError_t {
+        size_t off = 0;
+        cudaError_t e = cudaSuccess;
+        for (const Chain& C : ctx->ch) {
+            e = to_save ? cudaMemcpyAsync(sphi + off, C.phi, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream)
+                        : cudaMemcpyAsync(C.phi, sphi + off, sizeof(double) * C.V, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e != cudaSuccess) return e;
+            off += C.V;
+        }
+        return to_save ? cudaMemcpyAsync(sch, ctx->d_chains, sizeof(ChainDev) * nch, cudaMemcpyDeviceToDevice, ctx->stream)
+                       : cudaMemcpyAsync(ctx->d_chains, sch, sizeof(ChainDev) * nch, cudaMemcpyDeviceToDevice, ctx->stream);
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = YK_OK;
+    float ms[2] = {0.f, 0.f};
+    const bool profiling = ctx->profiling;   // the tuning steps are not profiled steps
+    ctx->profiling = false;
+    cudaError_t e = copy_state(true);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    for (int cand = 1; cand >= 0 && e == cudaSuccess && rc == YK_OK; --cand) {
+        ctx->overlap_choice = cand;
+        rc = enqueue_step(ctx);
+        if (rc == YK_OK) e = cudaEventRecord(e0, ctx->stream);
+        for (int rep = 0; rep < 2 && rc == YK_OK && e == cudaSuccess; ++rep) rc = enqueue_step(ctx);
+        if (rc == YK_OK && e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+        if (rc == YK_OK && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (rc == YK_OK && e == cudaSuccess) e = cudaEventElapsedTime(&ms[cand], e0, e1);
+        if (rc == YK_OK && e == cudaSuccess) rc = status_of_err(ctx);
+        if (rc == YK_OK && e == cudaSuccess) e = copy_state(false);
+    }
+    ctx->profiling = profiling;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(save);
+    if (rc) return rc;
+    if (e != cudaSuccess) {
+        set_error("autotune (noise placement): %s", cudaGetErrorString(e));
+        return YK_ECUDA;
+    }
+    ctx->overlap_choice = ms[1] <= ms[0] ? 1 : 0;
+    T.noise_overlap = ctx->overlap_choice;
+    T.step_ms_overlap = ms[1] / 2.f;
+    T.step_ms_serial = ms[0] / 2.f;
+    return YK_OK;
+}
+
 // The autotuner.  Batched steps (several CG systems in one launch): the grid
 // of the persistent CG, i.e. how many tiles each block owns, by timing the
 // step's CG (sources of Philox kind 100, which no step draws; 48 iterations;
@@ -698,6 +772,8 @@ int run_autotune(yk_ctx* ctx)
         T.cg_grid_max = maxg;
         T.cg_ms_chosen = best_ms;
     }
+    T.noise_overlap = -1;
+    if (int rc = tune_overlap(ctx)) return rc;
     for (const Chain& C : ctx->ch)
         if (C.net) {
             net_tile(C.net, &T.conv_rows, &T.conv_cols, &T.conv_layers_per_launch);
