@@ -44,6 +44,8 @@ def lib():
             "yko_time_slices_spinor": (None, [i, i, P, P]),
             "yko_philox4x32_10": (None, [P, P, P]),
             "yko_normals": (None, [u64, u32, u64, u32, u32, i64, P]),
+            "yko_normals_fp64": (None, [u64, u32, u64, u32, u32, i64, P]),
+            "yko_normal_pair_words": (None, [u32, u32, P]),
             "yko_uniform_field": (None, [u64, u32, i64, P]),
             "yko_uniform_field_comp": (None, [u64, u32, u32, i64, P]),
             "yko_drand48_field": (None, [i64, P]),
@@ -172,8 +174,24 @@ def philox(ctr, key):
 
 
 def normals(seed, chain, step, kind, rhs, n):
+    """Normals 0 .. n-1 of Philox stream (seed, chain; step, kind, rhs): the
+    FP32 Box-Muller of the CUDA generator, bit for bit."""
     out = np.empty(n)
     lib().yko_normals(seed, chain, step, kind, rhs, n, _p(out))
+    return out
+
+
+def normal_pair_words(a, b):
+    """The generator's pair from explicit Philox words: a sets the radius, b the angle."""
+    out = np.empty(2)
+    lib().yko_normal_pair_words(a, b, _p(out))
+    return out
+
+
+def normals_fp64(seed, chain, step, kind, rhs, n):
+    """The same Philox words through an FP64 libm Box-Muller."""
+    out = np.empty(n)
+    lib().yko_normals_fp64(seed, chain, step, kind, rhs, n, _p(out))
     return out
 
 

@@ -602,20 +602,116 @@ static void scheme_key_ctr(uint64_t seed, uint32_t chain, uint64_t step, uint32_
     ctr[3] = (kind << 24) | (rhs & 0xFFFFFFu);
 }
 
+/* Gaussian normals by Box-Muller in FP32 arithmetic: the CUDA generator
+   (yk_common.cuh nm_pair) uses IEEE round-to-nearest intrinsics for every
+   operation, and this file is compiled with -ffp-contract=off, so both give
+   the same bits.  Normals 4e .. 4e+3 of a stream come from Philox counter e:
+   pair 0 from words (0, 1), pair 1 from (2, 3).  A pair (a, b):
+     R = sqrt(2 E), E = -ln u, u = (a + 1/2) 2^-32, angle 2 pi (b + 1/2) 2^-32.
+   ln(1 + f) = 2 atanh(f / (2 + f)) by its Taylor series; sin and cos of
+   2 pi y (|y| <= 1/8 turn) by theirs; u >= 1/2 through w = 1 - u, exact from
+   the complemented word. */
+static float nm_log1p_core(float f)   /* ln(1 + f), f in [-0.293, 0.415] */
+{
+    const float s = f / (2.0f + f);
+    const float t = 2.0f * s;
+    const float z = s * s;
+    float p = fmaf(z, 0x1.c71c72p-4f, 0x1.24924ap-3f);
+    p = fmaf(z, p, 0x1.99999ap-3f);
+    p = fmaf(z, p, 0x1.555556p-2f);
+    return fmaf(t * z, p, t);
+}
+
+static float nm_neglog(uint32_t a)   /* -ln((a + 1/2) 2^-32) */
+{
+    const float ln2hi = 0x1.62e4p-1f, ln2lo = 0x1.7f7d1cp-20f;
+    if (a < 0x80000000u) {
+        const float u = (float)(2u * a + 1u) * 0x1p-33f;
+        uint32_t bits;
+        memcpy(&bits, &u, sizeof bits);
+        int e = (int)(bits >> 23) - 127;
+        bits = (bits & 0x007FFFFFu) | 0x3F800000u;
+        float m;
+        memcpy(&m, &bits, sizeof m);
+        if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+        const float L = nm_log1p_core(m - 1.0f);
+        const float fe = (float)e;
+        return -fmaf(fe, ln2hi, fmaf(fe, ln2lo, L));
+    }
+    const float w = (float)(2u * ~a + 1u) * 0x1p-33f;   /* 1 - u */
+    if (w <= 0x1.2bec34p-2f) return -nm_log1p_core(-w);
+    return (ln2hi - nm_log1p_core(1.0f - 2.0f * w)) + ln2lo;
+}
+
+static void nm_pair(uint32_t a, uint32_t b, float* z0, float* z1)
+{
+    const float R = sqrtf(2.0f * nm_neglog(a));
+    const uint32_t j = (b + 0x20000000u) >> 30;
+    const int32_t d = (int32_t)(b - (j << 30));
+    const float y = (float)(2 * d + 1) * 0x1p-33f;
+    const float y2 = y * y;
+    float sp = fmaf(y2, 0x1.507834p+5f, -0x1.32d2ccp+6f);
+    sp = fmaf(y2, sp, 0x1.466bc6p+6f);
+    sp = fmaf(y2, sp, -0x1.4abbcep+5f);
+    sp = fmaf(y2, sp, 0x1.921fb6p+2f);
+    const float sn = y * sp;
+    float cp = fmaf(y2, -0x1.a6d1f2p+4f, 0x1.e1f506p+5f);
+    cp = fmaf(y2, cp, -0x1.55d3c8p+6f);
+    cp = fmaf(y2, cp, 0x1.03c1f0p+6f);
+    cp = fmaf(y2, cp, -0x1.3bd3ccp+4f);
+    const float cs = fmaf(y2, cp, 1.0f);
+    float c, s;
+    switch (j) {
+    case 0: c = cs; s = sn; break;
+    case 1: c = -sn; s = cs; break;
+    case 2: c = -cs; s = -sn; break;
+    default: c = sn; s = -cs; break;
+    }
+    *z0 = R * c;
+    *z1 = R * s;
+}
+
+/* One pair from explicit words (edge tests of the transform). */
+void yko_normal_pair_words(uint32_t a, uint32_t b, double out[2])
+{
+    float z0, z1;
+    nm_pair(a, b, &z0, &z1);
+    out[0] = z0;
+    out[1] = z1;
+}
+
 void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
                  int64_t n, double* out)
 {
     uint32_t key[2], ctr0[4];
     scheme_key_ctr(seed, chain, step, kind, rhs, key, ctr0);
 #pragma omp parallel for schedule(static)
-    for (int64_t e = 0; e < (n + 1) / 2; ++e) {
+    for (int64_t e = 0; e < (n + 3) / 4; ++e) {
         uint32_t ctr[4] = {(uint32_t)e, ctr0[1], ctr0[2], ctr0[3]}, o[4];
         yko_philox4x32_10(ctr, key, o);
-        const double u1 = u52(o[0], o[1]), u2 = u52(o[2], o[3]);
-        const double R = sqrt(-2.0 * log(u1));
-        const double th = 2.0 * M_PI * u2;
-        out[2 * e] = R * cos(th);
-        if (2 * e + 1 < n) out[2 * e + 1] = R * sin(th);
+        float z[4];
+        nm_pair(o[0], o[1], &z[0], &z[1]);
+        nm_pair(o[2], o[3], &z[2], &z[3]);
+        for (int c = 0; c < 4 && 4 * e + c < n; ++c) out[4 * e + c] = (double)z[c];
+    }
+}
+
+/* Reference transform of the same words in FP64 (libm log, sqrt, cos, sin):
+   the test of the FP32 generator's accuracy. */
+void yko_normals_fp64(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
+                      int64_t n, double* out)
+{
+    uint32_t key[2], ctr0[4];
+    scheme_key_ctr(seed, chain, step, kind, rhs, key, ctr0);
+    for (int64_t e = 0; e < (n + 3) / 4; ++e) {
+        uint32_t ctr[4] = {(uint32_t)e, ctr0[1], ctr0[2], ctr0[3]}, o[4];
+        yko_philox4x32_10(ctr, key, o);
+        for (int p = 0; p < 2; ++p) {
+            const double u = ((double)o[2 * p] + 0.5) * 0x1p-32, t = ((double)o[2 * p + 1] + 0.5) * 0x1p-32;
+            const double R = sqrt(-2.0 * log(u));
+            if (4 * e + 2 * p < n) out[4 * e + 2 * p] = R * cos(2.0 * M_PI * t);
+            if (4 * e + 2 * p + 1 < n) out[4 * e + 2 * p + 1] = R * sin(2.0 * M_PI * t);
+        }
     }
 }
 

@@ -85,8 +85,14 @@ void yko_time_slices_spinor(int Nt, int Nx, const double* psi, double* corr);
 
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the framework's counter scheme. */
 void yko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Normals 0 .. n-1 of a stream: FP32 Box-Muller, normals 4e .. 4e+3 from counter e. */
 void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
                  int64_t n, double* out);
+/* One pair of yko_normals from explicit Philox words a (radius), b (angle). */
+void yko_normal_pair_words(uint32_t a, uint32_t b, double out[2]);
+/* The same words through FP64 libm Box-Muller (accuracy check of yko_normals). */
+void yko_normals_fp64(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
+                      int64_t n, double* out);
 void yko_uniform_field(uint64_t seed, uint32_t chain, int64_t n, double* out);
 void yko_uniform_field_comp(uint64_t seed, uint32_t chain, uint32_t comp, int64_t n, double* out);
 /* The reference's initial field 1 - 2*drand48() from glibc's default drand48 state (main.cu:92-95). */

@@ -214,6 +214,25 @@ def test_coloured_noise(ylib, cuda, Nt, Nx, s):
         assert np.abs(host(xi) - O.coloured_noise(Nt, Nx, s, w0)).max() < 1e-13
 
 
+@pytest.mark.parametrize("Nt,Nx,s", [(16, 16, 1.0), (6, 10, 1.0), (32, 64, 1.0), (16, 16, S_HALF_PI)])
+def test_philox_white_noise_bit_exact(ylib, cuda, Nt, Nx, s):
+    # the GPU's FP32 Box-Muller (IEEE round-to-nearest intrinsics throughout)
+    # and the oracle's C restatement give the same normals, bit for bit: with
+    # cutFraction >= 1 the noise is the white noise itself; with a cutoff the
+    # filter of the oracle's normals matches to rounding
+    yk = ylib
+    p = params(yk, Nt, Nx, cut_fraction=s)
+    with yk.Context(p) as ctx:
+        xi = cuda.empty(Nt * Nx, dtype=cuda.float64, device="cuda")
+        yk.ColouredNoise(ctx, xi)()
+        ctx.synchronize()
+        w = O.normals(1234, 0, 0, 1, 0, Nt * Nx)
+        if s >= 1.0:
+            assert np.array_equal(host(xi), w)
+        else:
+            assert np.abs(host(xi) - O.coloured_noise(Nt, Nx, s, w)).max() < 1e-13
+
+
 def test_euler_update_injected(ylib, cuda):
     yk = ylib
     Nt, Nx = 16, 32

@@ -36,10 +36,39 @@ def test_drand48_matches_libc():
 def test_normals_statistics():
     z = O.normals(1234, 0, 7, 1, 0, 400_000)
     assert abs(z.mean()) < 5e-3 and abs(z.var() - 1.0) < 1e-2
+    stats = pytest.importorskip("scipy.stats")
+    assert stats.kstest(z, "norm").pvalue > 1e-3
+    assert abs(stats.kurtosis(z)) < 0.03 and abs(stats.skew(z)) < 0.02
     # distinct streams are distinct
     assert not np.allclose(z[:100], O.normals(1234, 0, 8, 1, 0, 100))
     assert not np.allclose(z[:100], O.normals(1234, 1, 7, 1, 0, 100))
     assert not np.allclose(z[:100], O.normals(1234, 0, 7, 2, 0, 100))
+
+
+def test_fp32_box_muller_against_fp64():
+    # the FP32 transform of the Philox words is within a few FP32 ulps of the
+    # FP64 libm Box-Muller of the same words
+    z = O.normals(99, 3, 11, 2, 1, 1_000_002)
+    r = O.normals_fp64(99, 3, 11, 2, 1, 1_000_002)
+    ulp = np.spacing(np.abs(r).astype(np.float32)).astype(np.float64)
+    assert (np.abs(z - r) / ulp).max() < 8
+    # every value is an FP32 number
+    assert np.array_equal(z, z.astype(np.float32).astype(np.float64))
+    # normals 4e .. 4e+3 come from counter e: a prefix is a prefix
+    assert np.array_equal(O.normals(99, 3, 11, 2, 1, 7), z[:7])
+
+
+@pytest.mark.parametrize("a", [0, 1, 2**24 + 1, 2**31 - 1, 2**31, 2**31 + 12345, 2**32 - 2, 2**32 - 1])
+@pytest.mark.parametrize("b", [0, 2**29 - 1, 2**29, 2**30 + 7, 2**31, 3 * 2**30 - 1, 2**32 - 1])
+def test_box_muller_edge_words(a, b):
+    # the extreme words: u = 2^-33 (the largest radius, 6.76), u -> 1 (radius
+    # from the complemented word, no collapse to 0) and the quadrant seams
+    z = O.normal_pair_words(a, b)
+    u, t = (a + 0.5) / 2**32, (b + 0.5) / 2**32
+    R = np.sqrt(-2.0 * np.log1p(-(2**32 - 1 - a + 0.5) / 2**32)) if a >= 2**31 else np.sqrt(-2.0 * np.log(u))
+    want = R * np.array([np.cos(2 * np.pi * t), np.sin(2 * np.pi * t)])
+    assert np.abs(z - want).max() <= 1e-6 * max(R, 1e-30)
+    assert np.hypot(*z) > 0.0
 
 
 def _dense(Nt, Nx, a, sig, dagger=False):

@@ -877,13 +877,15 @@ int eo_setup(yk_ctx* ctx, const std::vector<SysDev>& hs)
     std::vector<int2> tiles(ctx->n_sys_tiles, make_int2(C->sys0, 0));
     for (int t = 0; t < nte; ++t) tiles[C->cg_tile0 + t] = make_int2(C->sys0, t * kTile);
     const size_t o_tiles = ((sizeof(SysDev) * ctx->nsys + 255) / 256) * 256;
-    if (cudaMalloc(&ctx->eo_mem, o_tiles + sizeof(int2) * tiles.size()) != cudaSuccess) {
+    const size_t o_dinv = o_tiles + ((sizeof(int2) * tiles.size() + 255) / 256) * 256;
+    if (cudaMalloc(&ctx->eo_mem, o_dinv + sizeof(double) * (size_t)Ve) != cudaSuccess) {
         cudaGetLastError();
         set_error("even-odd view allocation failed");
         return YK_ENOMEM;
     }
     ctx->d_sys_eo = reinterpret_cast<SysDev*>(ctx->eo_mem);
     ctx->d_eo_tiles = reinterpret_cast<int2*>(static_cast<char*>(ctx->eo_mem) + o_tiles);
+    E.dinv = reinterpret_cast<double*>(static_cast<char*>(ctx->eo_mem) + o_dinv);
     std::vector<SysDev> views(hs);
     views[C->sys0] = E;
     YK_CK(cudaMemcpy(ctx->d_sys_eo, views.data(), sizeof(SysDev) * views.size(), cudaMemcpyHostToDevice));

@@ -2365,12 +2365,16 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     };
     for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads)
         de_b[j - 2 * Nh] = (float)diag_at(wrap_site(cbase + j, Ve), 0);
-    for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads)
-        di_b[j - Nh] = (float)(1.0 / diag_at(wrap_site(cbase + j, Ve), 1));
     const double* chi_e = S.x;                      // compact FP64
     const double* rhs_e = S.x + 4 * (size_t)Ve;
     unsigned epoch = 0, gen = 0;
     int staged_k = -1;
+#ifdef YK_CG_TIMING
+    // block 0's cycles: reduce, A1 (with the staging wait), w/v/u, q, reliable
+    // updates, round 0, the reconstruction of chi
+    long long tacc[7] = {0, 0, 0, 0, 0, 0, 0}, tlast = clock64();
+    int tit = 0, tru = 0;
+#endif
 
     auto stage = [&](int mode, int cur, int prv) {
         const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
@@ -2541,7 +2545,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             eo_geom(m, 1, Nh, sh, t, b, du, dd);
             const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
             Site<double, K> h = eo_gl<true>(chi, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
-            const double s = -1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b]);
+            const double s = -S.dinv[m];
 #pragma unroll
             for (int i = 0; i < 4; ++i) h.v[i] *= s;
             store_site<double, K>(S.t64, m, h);
@@ -2583,11 +2587,24 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     };
 
     // ---------------- round 0: eta on the own sites of both classes (kept in
-    // b for the force), chi_e = 0, rhs_e, r_0 = p_0 = rhs_e
+    // b for the force); on the odd ones 1 / A_o (dinv, the one FP64 division
+    // per site of the solve) and -A_o^-1 eta_o (t64, compact); chi_e = 0;
+    // rhs_e; r_0 = p_0 = rhs_e
     for (int o = threadIdx.x; o < 2 * own; o += kHaloThreads) {
-        const int m = c0 + (o >> 1), n = 2 * m + (o & 1);   // the compact index's two full sites
+        const int m = c0 + (o >> 1), q = o & 1;
+        int t, b, du, dd;
+        eo_geom(m, q, Nh, sh, t, b, du, dd);
+        const int n = 2 * m + b;   // the compact index's full site of class q
         const Site<double, K> bv = SF.gen_eta ? eta_of_step<K>(SF, n, a.eta_kind) : load_site<double, K>(SF.b, n);
         if (SF.gen_eta) store_site<double, K>(SF.b, n, bv);
+        if (q) {
+            const double inv = 1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n]);
+            S.dinv[m] = inv;
+            Site<double, K> h;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] = -inv * bv.v[i];
+            store_site<double, K>(S.t64, m, h);
+        }
     }
     for (int o = threadIdx.x; o < own; o += kHaloThreads) {
         Site<double, K> z;
@@ -2602,27 +2619,17 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         st_sm(V_own, o, zw);
     }
     if (!nsync(a, ++epoch, deps)) return;
+    // 1 / A_o in FP32 on the widened range, from the owners' dinv
+    for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads)
+        di_b[j - Nh] = (float)S.dinv[wrap_site(cbase + j, Ve)];
     for (int o = threadIdx.x; o < own; o += kHaloThreads) {
         const int m = c0 + o;
         int t, b, du, dd;
         eo_geom(m, 0, Nh, sh, t, b, du, dd);
         const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
-        // the odd neighbours' -A_o^-1 eta_o, formed here from b
-        Site<double, K> nb[4];
-        const int mo[4] = {m + Nh >= Ve ? m + Nh - Ve : m + Nh, m - Nh < 0 ? m - Nh + Ve : m - Nh, m + du, m + dd};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int t2, b2, u2, d2;
-            eo_geom(mo[q], 1, Nh, sh, t2, b2, u2, d2);
-            const int n2 = 2 * mo[q] + b2;
-            nb[q] = load_site<double, K>(SF.b, n2);
-            const double s = -1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n2]);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) nb[q].v[i] *= s;
-        }
         const Site<double, K> e = load_site<double, K>(SF.b, 2 * m + b);
         // eta_e + H^dag_eo (-A_o^-1 eta_o)
-        const Site<double, K> rh = dirac_combine<double, K, true>(e, nb[0], nb[1], nb[2], nb[3], 1.0, r64, sp, sm);
+        const Site<double, K> rh = eo_gl<true>(S.t64, m, Ve, Nh, du, dd, e, 1.0, r64, sp, sm);
         store_site<double, K>(const_cast<double*>(rhs_e), m, rh);
         Site<W, K> rw32;
 #pragma unroll
@@ -2639,6 +2646,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     __syncthreads();
     pass_q(0, true);
     if (!reduce(0, false)) return;
+    YK_TMARK(5);
 
     int k = 1;
     while (k <= a.max_iter) {
@@ -2652,6 +2660,10 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         if (mode == kRu) {
             if (!reliable(cur, prv)) return;
             if (!reduce(k, true)) return;
+            YK_TMARK(4);
+#ifdef YK_CG_TIMING
+            ++tru;
+#endif
             continue;
         }
         if (!(mode == kStep && staged_k == k)) {
@@ -2662,11 +2674,18 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         cp_async_wait_all();
         pass_a1(mode, cur, prv);
         __syncthreads();
+        YK_TMARK(1);
         pass_wvu();
         __syncthreads();
+        YK_TMARK(2);
         pass_q(cur, false);
+        YK_TMARK(3);
         if (!reduce(k, false)) return;
+        YK_TMARK(0);
         ++k;
+#ifdef YK_CG_TIMING
+        ++tit;
+#endif
     }
     // chi of both classes in the full layout for the force (t64): every
     // block's final chi_e and its own odd sites' chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
@@ -2684,7 +2703,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         const Site<double, K> h = eo_gl<true>(S.x, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
         const int n = 2 * m + b;
         const Site<double, K> e = load_site<double, K>(SF.b, n);
-        const double inv = 1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n]);
+        const double inv = S.dinv[m];
         Site<double, K> co;
 #pragma unroll
         for (int i = 0; i < 4; ++i) co.v[i] = (e.v[i] - h.v[i]) * inv;
@@ -2692,6 +2711,24 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     }
     // t64 holds chi however the solve ended (also when it retired at k = 0)
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.sys_first].chi_ready = 1;
+#ifdef YK_CG_TIMING
+    YK_TMARK(6);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && tit > 0)
+        printf("eo timing (block 0, cycles; %d iterations, %d reliable updates): per iteration reduce %lld  A1 %lld  "
+               "wvu %lld  q %lld | per update %lld | round 0 %lld  reconstruction %lld\n",
+               tit, tru, tacc[0] / tit, tacc[1] / tit, tacc[2] / tit, tacc[3] / tit, tru ? tacc[4] / tru : 0ll, tacc[5],
+               tacc[6]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        volatile unsigned long long* q = g_cg_q;
+        volatile unsigned long long* f = g_cg_f;
+        const unsigned long long nq = f[3] ? f[3] : 1;
+        printf("eo timing (reduction marks over %llu): entry-sync %llu  arrive %llu  wait %llu  sync %llu  "
+               "convert %llu  step %llu  state %llu  end-sync %llu\n",
+               nq, q[0] / nq, q[1] / nq, q[2] / nq, q[3] / nq, q[4] / nq, q[5] / nq, q[6] / nq, q[7] / nq);
+        for (int i = 0; i < 8; ++i) f[i] = 0;
+        for (int i = 0; i < 16; ++i) q[i] = 0;
+    }
+#endif
 }
 
 // Shared memory of cg_eo_kernel for own compact sites per block and Nh.

@@ -100,7 +100,12 @@ __device__ __forceinline__ Nbr neighbours(int n, int Nt, int Nx)
 //  (D psi)(n)   = diag psi(n) - 1/2 sum_mu [ s+ (r - g_mu) psi(n+mu) + s- (r + g_mu) psi(n-mu) ]
 //  (D^+ psi)(n) = diag psi(n) - 1/2 sum_mu [ s+ (r + g_mu) psi(n+mu) + s- (r - g_mu) psi(n-mu) ]
 // with g_t = diag(1,-1), g_x = sigma_1, diag = 2r + m0 + g sigma(n).
-// Both flavours and every real plane see the same real coefficients.
+// Both flavours and every real plane see the same real coefficients.  The
+// space hops are gathered before their coefficients: the up and down
+// neighbours share r / 2 on the same component and take -+1/2 on the other
+// (sigma_1), so each output component costs one multiply, four FMAs and two
+// adds (GB300's FP64 rate is 1/64 of its FP32 rate: the FP64 applications of
+// the reliable updates and the force pay per operation).
 template <typename R, int K, bool DAG>
 __device__ __forceinline__ Site<R, K> dirac_combine(const Site<R, K>& c, const Site<R, K>& tu,
                                                     const Site<R, K>& td, const Site<R, K>& xu,
@@ -113,9 +118,10 @@ __device__ __forceinline__ Site<R, K> dirac_combine(const Site<R, K>& c, const S
     const R cd_up = DAG ? -sp * h * (r - R(1)) : -sp * h * (r + R(1));
     const R cu_dn = DAG ? -sm * h * (r - R(1)) : -sm * h * (r + R(1));
     const R cd_dn = DAG ? -sm * h * (r + R(1)) : -sm * h * (r - R(1));
-    // space hops: up-neighbour uses (r - s1) for D and (r + s1) for D^+
-    const R sx_up = DAG ? R(1) : R(-1);
-    const R sx_dn = -sx_up;
+    // space hops: -1/2 [(r -+ s1) psi(n+x) + (r +- s1) psi(n-x)] (D: upper sign)
+    //   = -r/2 (psi(n+x) + psi(n-x)) + sx/2 s1 (psi(n+x) - psi(n-x)),  sx = +1 for D
+    const R a = -h * r;
+    const R bx = DAG ? -h : h;
 #pragma unroll
     for (int f = 0; f < 2; ++f) {
 #pragma unroll
@@ -123,11 +129,14 @@ __device__ __forceinline__ Site<R, K> dirac_combine(const Site<R, K>& c, const S
             const int iu = (2 * f) * K + k, id = (2 * f + 1) * K + k;
             R ou = diag * c.v[iu];
             R od = diag * c.v[id];
-            ou += cu_up * tu.v[iu] + cu_dn * td.v[iu];
-            od += cd_up * tu.v[id] + cd_dn * td.v[id];
-            // -1/2 (r u +- d), -1/2 (r d +- u)
-            ou -= h * (r * xu.v[iu] + sx_up * xu.v[id]) + h * (r * xd.v[iu] + sx_dn * xd.v[id]);
-            od -= h * (r * xu.v[id] + sx_up * xu.v[iu]) + h * (r * xd.v[id] + sx_dn * xd.v[iu]);
+            ou = fma(cu_up, tu.v[iu], ou);
+            od = fma(cd_up, tu.v[id], od);
+            ou = fma(cu_dn, td.v[iu], ou);
+            od = fma(cd_dn, td.v[id], od);
+            ou = fma(bx, xu.v[id] - xd.v[id], ou);
+            od = fma(bx, xu.v[iu] - xd.v[iu], od);
+            ou = fma(a, xu.v[iu] + xd.v[iu], ou);
+            od = fma(a, xu.v[id] + xd.v[id], od);
             o.v[iu] = ou;
             o.v[id] = od;
         }
@@ -175,8 +184,9 @@ __device__ __forceinline__ void pion_term(Site<R, K>& o, const Site<R, K>& c, co
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (J. Salmon et al., "Parallel random numbers: as easy as
 // 1, 2, 3", SC'11) with the framework's counter scheme:
-//   key = (seed_lo, seed_hi ^ chain), ctr = (pair index, step_lo, step_hi, kind<<24 | rhs)
-// Each counter yields two 52-bit uniforms and, by Box-Muller, two normals.
+//   key = (seed_lo, seed_hi ^ chain), ctr = (index, step_lo, step_hi, kind<<24 | rhs)
+// Each counter yields two 52-bit uniforms (the initial fields) or four
+// normals (the noise and the sources).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
 {
@@ -217,15 +227,106 @@ __device__ __forceinline__ RngStream rng_stream(uint64_t seed, uint32_t chain, u
     return s;
 }
 
-// Normals 2e and 2e+1 of the stream.
-__device__ __forceinline__ double2 normal_pair(const RngStream& s, uint32_t e)
+// ---------------------------------------------------------------------------
+// Gaussian normals: Box-Muller in FP32 arithmetic, every operation an IEEE
+// round-to-nearest intrinsic (no contraction), so that the oracle's C
+// restatement (fmaf, -ffp-contract=off) gives the same bits.  GB300 runs FP64
+// at 1/64 of its FP32 rate, and an FP64 log + sincospi per pair made the
+// sources and the white noise a sizeable part of a step.
+// Normals 4e .. 4e+3 of a stream come from counter e: pair 0 from words
+// (x, y), pair 1 from (z, w); a pair (a, b) is
+//   R = sqrt(2 E), E = -ln u, u = (a + 1/2) 2^-32;   angle 2 pi (b + 1/2) 2^-32;
+//   (R cos, R sin).
+// ln: u < 1/2 is split into 2^e m (m in [sqrt 1/2, sqrt 2)); u >= 1/2 goes
+// through w = 1 - u = (~a + 1/2) 2^-32, exact from the complemented word, so
+// that small radii keep their resolution.  ln(1 + f) = 2 atanh(f / (2 + f))
+// by its Taylor series to s^9 (|s| <= 0.1716: truncation below 2e-9).
+// sin and cos of 2 pi y, |y| <= 1/8 turn, by their Taylor series (to y^9 and
+// y^10, truncation below 3e-9), the quadrant from the word's top bits.
+// Accuracy: a few FP32 ulps against the exact transform of the same words;
+// the largest |normal| is 6.76 (u = 2^-33).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float nm_log1p_core(float f)   // ln(1 + f), f in [-0.293, 0.415]
+{
+    const float s = __fdiv_rn(f, __fadd_rn(2.0f, f));
+    const float t = __fmul_rn(2.0f, s);
+    const float z = __fmul_rn(s, s);
+    float p = __fmaf_rn(z, 0x1.c71c72p-4f, 0x1.24924ap-3f);   // 1/9, 1/7
+    p = __fmaf_rn(z, p, 0x1.99999ap-3f);                       // 1/5
+    p = __fmaf_rn(z, p, 0x1.555556p-2f);                       // 1/3
+    return __fmaf_rn(__fmul_rn(t, z), p, t);
+}
+
+__device__ __forceinline__ float nm_neglog(uint32_t a)   // -ln((a + 1/2) 2^-32)
+{
+    constexpr float kLn2Hi = 0x1.62e4p-1f, kLn2Lo = 0x1.7f7d1cp-20f;   // ln 2 = hi + lo
+    if (a < 0x80000000u) {
+        const float u = __fmul_rn(__uint2float_rn(2u * a + 1u), 0x1p-33f);
+        uint32_t bits = __float_as_uint(u);
+        int e = (int)(bits >> 23) - 127;
+        float m = __uint_as_float((bits & 0x007FFFFFu) | 0x3F800000u);
+        if (m > 0x1.6a09e6p+0f) {
+            m = __fmul_rn(m, 0.5f);
+            e += 1;
+        }
+        const float L = nm_log1p_core(__fsub_rn(m, 1.0f));
+        const float fe = __int2float_rn(e);
+        return -__fmaf_rn(fe, kLn2Hi, __fmaf_rn(fe, kLn2Lo, L));
+    }
+    const float w = __fmul_rn(__uint2float_rn(2u * ~a + 1u), 0x1p-33f);   // 1 - u
+    if (w <= 0x1.2bec34p-2f) return -nm_log1p_core(-w);                  // w <= 1 - sqrt 1/2
+    return __fadd_rn(__fsub_rn(kLn2Hi, nm_log1p_core(__fsub_rn(1.0f, __fmul_rn(2.0f, w)))), kLn2Lo);
+}
+
+__device__ __forceinline__ float2 nm_pair(uint32_t a, uint32_t b)
+{
+    const float R = __fsqrt_rn(__fmul_rn(2.0f, nm_neglog(a)));
+    const uint32_t j = (b + 0x20000000u) >> 30;            // nearest quarter turn
+    const int d = (int)(b - (j << 30));                    // in [-2^29, 2^29)
+    const float y = __fmul_rn(__int2float_rn(2 * d + 1), 0x1p-33f);
+    const float y2 = __fmul_rn(y, y);
+    // (2 pi)^k / k! with alternating signs
+    float sp = __fmaf_rn(y2, 0x1.507834p+5f, -0x1.32d2ccp+6f);
+    sp = __fmaf_rn(y2, sp, 0x1.466bc6p+6f);
+    sp = __fmaf_rn(y2, sp, -0x1.4abbcep+5f);
+    sp = __fmaf_rn(y2, sp, 0x1.921fb6p+2f);
+    const float sn = __fmul_rn(y, sp);
+    float cp = __fmaf_rn(y2, -0x1.a6d1f2p+4f, 0x1.e1f506p+5f);
+    cp = __fmaf_rn(y2, cp, -0x1.55d3c8p+6f);
+    cp = __fmaf_rn(y2, cp, 0x1.03c1f0p+6f);
+    cp = __fmaf_rn(y2, cp, -0x1.3bd3ccp+4f);
+    const float cs = __fmaf_rn(y2, cp, 1.0f);
+    float c, s;
+    if (j == 0) {
+        c = cs;
+        s = sn;
+    } else if (j == 1) {
+        c = -sn;
+        s = cs;
+    } else if (j == 2) {
+        c = -cs;
+        s = -sn;
+    } else {
+        c = sn;
+        s = -cs;
+    }
+    return make_float2(__fmul_rn(R, c), __fmul_rn(R, s));
+}
+
+// Normals 4e .. 4e+3 of the stream.
+__device__ __forceinline__ float4 normal4(const RngStream& s, uint32_t e)
 {
     const uint4 o = philox4x32_10(make_uint4(e, s.c1, s.c2, s.c3), s.key);
-    const double u1 = u52(o.x, o.y), u2 = u52(o.z, o.w);
-    const double R = sqrt(-2.0 * log(u1));
-    double sn, cs;
-    sincospi(2.0 * u2, &sn, &cs);
-    return make_double2(R * cs, R * sn);
+    const float2 p = nm_pair(o.x, o.y), q = nm_pair(o.z, o.w);
+    return make_float4(p.x, p.y, q.x, q.y);
+}
+
+// Normal i of the stream.
+__device__ __forceinline__ double normal_at(const RngStream& s, uint32_t i)
+{
+    const float4 z = normal4(s, i >> 2);
+    const int c = (int)(i & 3u);
+    return (double)(c == 0 ? z.x : c == 1 ? z.y : c == 2 ? z.z : z.w);
 }
 
 // Fermion noise eta of one CG system at site n: real Gaussian entries from the
@@ -235,10 +336,9 @@ template <int K>
 __device__ __forceinline__ Site<double, K> eta_site_at(const SysDev& S, int n, int kind, int64_t step)
 {
     const RngStream rs = rng_stream(S.seed, (uint32_t)S.chain, (uint64_t)step, (uint32_t)kind, (uint32_t)S.rhs);
-    const double2 a = normal_pair(rs, (uint32_t)(2 * n));
-    const double2 b = normal_pair(rs, (uint32_t)(2 * n + 1));
+    const float4 z = normal4(rs, (uint32_t)n);   // normals 4n .. 4n + 3
     Site<double, K> s;
-    const double e[4] = {a.x, a.y, b.x, b.y};
+    const double e[4] = {z.x, z.y, z.z, z.w};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         s.v[i * K] = e[i];

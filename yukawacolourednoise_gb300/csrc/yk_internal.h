@@ -59,6 +59,7 @@ struct SysDev {
     float* Ap32;         // D^dag D p
     float* xs32;         // solution increment since the last reliable update
     float* diag32;       // 2r + m0 + g sigma per site (one float)
+    double* dinv;        // even-odd views: 1 / (2r + m0 + g sigma) on the odd sites (compact)
     // noise generation for b: kind/rhs of the Philox stream, or gen = 0
     int gen_eta;
     uint64_t seed;

@@ -88,8 +88,7 @@ __device__ __forceinline__ double white_at(const ChainDev& C, const double* give
 {
     if (given) return given[n];
     const RngStream rs = rng_stream(C.seed, C.chain_id, (uint64_t)C.step, 1u, 0u);
-    const double2 z = normal_pair(rs, (uint32_t)(n >> 1));
-    return (n & 1) ? z.y : z.x;
+    return normal_at(rs, (uint32_t)n);
 }
 
 // rows t and t + 1 (when t + 1 < Nt) of the white noise, transformed along x
@@ -109,13 +108,16 @@ __global__ void __launch_bounds__(kBlock) noise_rows_fwd(ChainDev* chains, const
     double2* buf = sm;
     double2* tmp = sm + Nx;
     const int base = t * Nx;
-    if (!given && (Nx & 1) == 0) {
+    if (!given && (Nx & 3) == 0) {
+        // four normals of each row per counter
         const RngStream rs = rng_stream(C.seed, C.chain_id, (uint64_t)C.step, 1u, 0u);
-        for (int x2 = threadIdx.x; x2 < Nx / 2; x2 += blockDim.x) {
-            const double2 z = normal_pair(rs, (uint32_t)((base >> 1) + x2));
-            const double2 y = two ? normal_pair(rs, (uint32_t)(((base + Nx) >> 1) + x2)) : make_double2(0.0, 0.0);
-            buf[2 * x2] = make_double2(z.x, y.x);
-            buf[2 * x2 + 1] = make_double2(z.y, y.y);
+        for (int x4 = threadIdx.x; x4 < Nx / 4; x4 += blockDim.x) {
+            const float4 z = normal4(rs, (uint32_t)((base >> 2) + x4));
+            const float4 y = two ? normal4(rs, (uint32_t)(((base + Nx) >> 2) + x4)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            buf[4 * x4] = make_double2(z.x, y.x);
+            buf[4 * x4 + 1] = make_double2(z.y, y.y);
+            buf[4 * x4 + 2] = make_double2(z.z, y.z);
+            buf[4 * x4 + 3] = make_double2(z.w, y.w);
         }
     } else {
         for (int x = threadIdx.x; x < Nx; x += blockDim.x)

@@ -32,8 +32,8 @@
 namespace yk {
 
 // White noise of the three pion fields at the chain's current step: element n
-// of field a is normal 2(n/2) + (n & 1) of Philox stream (kind 1, rhs a), the
-// pairing of the sigma noise (white_at, yk_noise.cu).
+// of field a is normal n of Philox stream (kind 1, rhs a), as the sigma noise
+// (white_at, yk_noise.cu).
 __global__ void __launch_bounds__(kBlock) pion_white_kernel(const ChainDev* __restrict__ C, double* __restrict__ white3)
 {
     const int V = C->V;
@@ -41,8 +41,7 @@ __global__ void __launch_bounds__(kBlock) pion_white_kernel(const ChainDev* __re
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * V; i += gridDim.x * blockDim.x) {
         const int q = i / V, n = i - q * V;
         const RngStream rs = rng_stream(C->seed, C->chain_id, step, 1u, (uint32_t)(q + 1));
-        const double2 z = normal_pair(rs, (uint32_t)(n >> 1));
-        white3[i] = (n & 1) ? z.y : z.x;
+        white3[i] = normal_at(rs, (uint32_t)n);
     }
 }
 
@@ -57,13 +56,12 @@ __global__ void __launch_bounds__(kBlock) pion_eta_kernel(const ChainDev* __rest
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R * V; i += gridDim.x * blockDim.x) {
         const int j = i / V, n = i - j * V;
         const RngStream rs = rng_stream(C->seed, C->chain_id, step, (uint32_t)kind, (uint32_t)j);
-        const double2 a = normal_pair(rs, (uint32_t)(2 * n));
-        const double2 b = normal_pair(rs, (uint32_t)(2 * n + 1));
+        const float4 z = normal4(rs, (uint32_t)n);   // normals 4n .. 4n + 3
         double2* e = reinterpret_cast<double2*>(eta + ((size_t)j * V + n) * 8);
-        e[0] = make_double2(a.x, 0.0);
-        e[1] = make_double2(a.y, 0.0);
-        e[2] = make_double2(b.x, 0.0);
-        e[3] = make_double2(b.y, 0.0);
+        e[0] = make_double2(z.x, 0.0);
+        e[1] = make_double2(z.y, 0.0);
+        e[2] = make_double2(z.z, 0.0);
+        e[3] = make_double2(z.w, 0.0);
     }
 }
 
