@@ -308,36 +308,42 @@ __device__ __forceinline__ bool wait_over(long long t0, int* err)
     return *(volatile int*)err != 0;
 }
 
-// True when the wait gave up (timed out, or another block failed).
+__device__ __forceinline__ unsigned ld_acquire_flag(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// True when the wait gave up (timed out, or another block failed).  The
+// polling load acquires: what the flag's writer released is visible after it.
 __device__ __forceinline__ bool wait_flag(const unsigned* f, unsigned epoch, int* err)
 {
-    const volatile unsigned* q = f;
     const long long t0 = clock64();
-    while ((int)(*q - epoch) < 0)
+    while ((int)(ld_acquire_flag(f) - epoch) < 0)
         if (wait_over(t0, err)) return true;
     return false;
 }
 
 // Neighbour synchronisation: publish this block's epoch, wait until every
-// block in `d` has published it too.  Release: bar.sync + thread 0's fence;
-// acquire: each waiting thread's fence + bar.sync.  False when a wait gave
-// up (the final barrier ORs the waiters' outcomes: no global read of the
-// error flag on the way out).
+// block in `d` has published it too.  Release: bar.sync, then thread 0's
+// release store of the flag (the barrier orders the block's writes before
+// it); acquire: each waiting thread's acquiring poll, then bar.sync.  False
+// when a wait gave up (the final barrier ORs the waiters' outcomes: no global
+// read of the error flag on the way out).
 __device__ bool nsync(const CGArgs& a, unsigned epoch, const Deps& d)
 {
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        *(volatile unsigned*)(a.flags + (size_t)blockIdx.x * kFlagStride) = epoch;
-    }
+    if (threadIdx.x == 0)
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.flags + (size_t)blockIdx.x * kFlagStride),
+                     "r"(epoch)
+                     : "memory");
     int bad = 0;
     if (d.all) {
         for (int b = threadIdx.x; b < (int)gridDim.x && !bad; b += blockDim.x)
             if (b != (int)blockIdx.x) bad = wait_flag(a.flags + (size_t)b * kFlagStride, epoch, a.err);
-        __threadfence();
     } else if ((int)threadIdx.x < d.n) {
         bad = wait_flag(a.flags + (size_t)d.b[threadIdx.x] * kFlagStride, epoch, a.err);
-        __threadfence();
     }
     return __syncthreads_or(bad) == 0;
 }
@@ -2372,7 +2378,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
 #ifdef YK_CG_TIMING
     // block 0's cycles: reduce, A1 (with the staging wait), w/v/u, q, reliable
     // updates, round 0, the reconstruction of chi
-    long long tacc[7] = {0, 0, 0, 0, 0, 0, 0}, tlast = clock64();
+    long long tacc[16] = {}, tlast = clock64();
     int tit = 0, tru = 0;
 #endif
 
@@ -2535,7 +2541,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             store_site<double, K>(chi, m, xv);
             st_sm(X_st, o, zw);
         }
+        YK_TMARK(7);
         if (!nsync(a, ++epoch, deps)) return false;
+        YK_TMARK(8);
         Site<double, K> zero;
 #pragma unroll
         for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
@@ -2550,7 +2558,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             for (int i = 0; i < 4; ++i) h.v[i] *= s;
             store_site<double, K>(S.t64, m, h);
         }
+        YK_TMARK(9);
         if (!nsync(a, ++epoch, deps)) return false;
+        YK_TMARK(10);
         for (int base = tb; base < te; base += 2) {
             const int tile = base + hf;
             const bool tile_on = tile < te;
@@ -2583,6 +2593,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         }
+        YK_TMARK(11);
         return true;
     };
 
@@ -2606,6 +2617,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             store_site<double, K>(S.t64, m, h);
         }
     }
+    YK_TMARK(12);
     for (int o = threadIdx.x; o < own; o += kHaloThreads) {
         Site<double, K> z;
         Site<W, K> zw;
@@ -2619,6 +2631,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         st_sm(V_own, o, zw);
     }
     if (!nsync(a, ++epoch, deps)) return;
+    YK_TMARK(13);
     // 1 / A_o in FP32 on the widened range, from the owners' dinv
     for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads)
         di_b[j - Nh] = (float)S.dinv[wrap_site(cbase + j, Ve)];
@@ -2637,7 +2650,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         YK_ST(W, K, S.r32[0], m, rw32);
         YK_ST(W, K, S.p32[0], m, rw32);
     }
+    YK_TMARK(14);
     if (!nsync(a, ++epoch, deps)) return;
+    YK_TMARK(15);
     stage(kHaloInit, 0, 0);
     cp_async_wait_all();
     pass_a1(kHaloInit, 0, 0);
@@ -2718,6 +2733,11 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
                "wvu %lld  q %lld | per update %lld | round 0 %lld  reconstruction %lld\n",
                tit, tru, tacc[0] / tit, tacc[1] / tit, tacc[2] / tit, tacc[3] / tit, tru ? tacc[4] / tru : 0ll, tacc[5],
                tacc[6]);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && tru > 0)
+        printf("eo timing (per update): fold %lld  nsync %lld  odd %lld  nsync %lld  even %lld  reduce %lld | round 0: "
+               "eta %lld  nsync %lld  rhs %lld  nsync %lld  rest %lld\n",
+               tacc[7] / tru, tacc[8] / tru, tacc[9] / tru, tacc[10] / tru, tacc[11] / tru, tacc[4] / tru, tacc[12],
+               tacc[13], tacc[14], tacc[15], tacc[5]);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         volatile unsigned long long* q = g_cg_q;
         volatile unsigned long long* f = g_cg_f;
