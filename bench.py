@@ -515,11 +515,20 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
     sec = a.elapsed_time(b) / 1e3
     obs = [ctx.observables(c) for c in range(n_chains)]
     t = ctx.tune_report()
+    # two more steps as direct launches: the kernel and its iterations
+    ctx.profile_begin()
+    with torch.cuda.stream(stream):
+        ctx.step(2)
+    pr = ctx.profile_end()
     ctx.close()
     sites = int(sum(int(L) * int(L) for L in Ls))
+    kernels = {0: "cg_kernel (grid-wide D^dag D)", 4: "cg_eob_kernel (batched even-odd)"}
     return {"config": f"{n_chains} chains, L in {{32,64,128,256}} (seed {seed}), 4 RHS, mixed CG rel-res 1e-10",
             "value": round(steps * n_chains / sec, 2), "unit": "chain-steps/s",
             "site_steps_per_s": round(steps * sites / sec, 1), "steps": steps,
+            "ms_per_step": round(sec * 1e3 / steps, 3),
+            "cg_kernel": kernels.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_grid": pr.cg_grid,
+            "cg_iterations_per_system_step": round(pr.cg_iterations / max(pr.steps * n_chains * 4, 1), 1),
             "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs),
             "autotune": {"cg_grid": t.cg_grid, "cg_grid_max": t.cg_grid_max, "candidates": t.cg_candidates,
                          "ms_chosen": round(t.cg_ms_chosen, 3), "ms_at_max": round(t.cg_ms_max, 3)}}
@@ -720,6 +729,8 @@ def main(argv=None):
                          "couplings, uniform start; one JSON object; profiling runs)")
     ap.add_argument("--dirac-only", type=int, default=0, metavar="L",
                     help="only the Dirac apply on an L x L lattice (one JSON object; profiling runs)")
+    ap.add_argument("--batching-only", action="store_true",
+                    help="only the batching configuration (one JSON object; profiling runs)")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip timing the reference's own CUDA kernels on the GPU")
     args = ap.parse_args(argv)
@@ -758,6 +769,12 @@ def main(argv=None):
         stream = torch.cuda.Stream()
         L = args.dirac_only
         print(json.dumps({"dirac_hbm": dirac_hbm(yk, torch, stream, Nt=L, Nx=L)}), flush=True)
+        return 0
+    if args.batching_only:
+        import torch
+        import yukawacolourednoise_gb300 as yk
+        stream = torch.cuda.Stream()
+        print(json.dumps({"batching": batched(yk, torch, stream)}), flush=True)
         return 0
     if args.learned_only:
         import torch

@@ -364,7 +364,8 @@ typedef struct yk_profile {
     int cg_launches;             /* persistent CG launches                        */
     int cg_grid;                 /* blocks of the last CG launch                  */
     int cg_kernel;               /* its kernel: 0 grid-wide, 1 halo, 2 cluster,   */
-                                 /*   3 even-odd (Schur complement)               */
+                                 /*   3 even-odd (Schur complement), 4 batched    */
+                                 /*   even-odd (work dealt out per pass)          */
     double noise_ms, cg_ms, force_ms, update_ms;   /* summed device time          */
     int64_t cg_iterations;       /* CG iterations, summed over systems            */
     int64_t cg_site_iterations;  /* sum over chains of iterations x volume        */

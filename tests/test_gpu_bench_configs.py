@@ -11,8 +11,8 @@ configurations themselves, not only on small lattices.
   steps each, field within 1e-9 (CG rel-res 1e-12).
 * C3-shaped batch: 8 chains with L in {32, 64, 128, 256} (two of each),
   seeded m0 ~ U[0.05, 0.3] and g ~ U[0.3, 0.8], 4 right-hand sides, mixed CG
-  rel-res 1e-10, all chains in one step graph: 2 steps, every chain within
-  1e-8 of its own oracle chain.
+  rel-res 1e-10 (the batched even-odd kernel), all chains in one step graph:
+  2 steps, every chain within 1e-8 of its own oracle chain.
 """
 from pathlib import Path
 
@@ -96,7 +96,10 @@ def test_c3_shaped_batch(ylib, cuda):
                reliable_every=50)
           for L, m0, g in zip(Ls, m0s, gs)]
     with yk.Context(ps) as ctx:
-        ctx.step(2)
+        ctx.profile_begin()
+        ctx.step(1)
+        assert ctx.profile_end().cg_kernel == 4, "the batch's solves run the batched even-odd CG kernel"
+        ctx.step(1)
         got = [ctx.get_field(c) for c in range(len(ps))]
         obs = [ctx.observables(c) for c in range(len(ps))]
     for c, p in enumerate(ps):

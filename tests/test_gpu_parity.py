@@ -454,6 +454,39 @@ def test_batched_block_ranges_keep_results(ylib, cuda, monkeypatch, balance):
         assert np.abs(got[c] - phi).max() < 1e-8, c
 
 
+@pytest.mark.parametrize("specs,kernel", [
+    # even lattices: the batched even-odd CG (work dealt out per pass)
+    ([(40, 24, 0.1, 0.5, S_HALF_PI, 2), (8, 8, 0.25, 0.3, 0.2, 1), (64, 64, 0.05, 0.8, 1.0, 3)], 4),
+    # one odd lattice: the whole batch keeps the D^dag D grid kernel
+    ([(40, 24, 0.1, 0.5, S_HALF_PI, 2), (9, 8, 0.25, 0.3, 1.0, 1)], 0),
+    # a single lattice too wide for the halo kernel's shared memory
+    ([(16, 1024, 0.1, 0.5, S_HALF_PI, 1)], 4),
+], ids=["even_batch", "odd_lattice", "single_wide"])
+def test_batched_even_odd_cg(ylib, cuda, specs, kernel):
+    # the step's solves of every chain and right-hand side through one
+    # even-odd launch; fields within 1e-8 of the FP64 oracle's steps (the
+    # reference's D^dag D solve, FermionicDrift.cu:57-100)
+    yk = ylib
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, cut_fraction=s, n_rhs=nr, precision=yk.YK_MIXED,
+                 cg_tol=1e-10, fixed_dt=0.01)
+          for nt, nx, m0, g, s, nr in specs]
+    with yk.Context(ps) as ctx:
+        ctx.profile_begin()
+        ctx.step(1)
+        pr = ctx.profile_end()
+        assert pr.cg_kernel == kernel
+        ctx.step(2)
+        got = [ctx.get_field(c) for c in range(len(ps))]
+        obs = [ctx.observables(c) for c in range(len(ps))]
+    for c, p in enumerate(ps):
+        assert obs[c].steps == 3 and obs[c].status == 0, c
+        phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+        for step in range(3):
+            phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10, tol_mode=1,
+                                     fixed_dt=0.01)
+        assert np.abs(got[c] - phi).max() < 1e-8, c
+
+
 def test_autotune_keeps_results(ylib, cuda, monkeypatch):
     # batched chains: the tuned CG grid (automatic before the first capture,
     # and again by an explicit call between steps) gives the same fields, bit

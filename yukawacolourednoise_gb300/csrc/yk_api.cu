@@ -402,7 +402,7 @@ int enqueue_step(yk_ctx* ctx)
             prof_end(ctx, 1, e, 2);
         } else {
             // batched: block ranges balanced by the previous step's iterations
-            const bool bal = ctx->nsys > 1 && ctx->cg_balance;
+            const bool bal = ctx->nsys > 1 && ctx->cg_balance && !ctx->cg_eo;
             if (bal) a.balance = ctx->d_balance;
             YK_CK(launch_cg(a, 1, ctx->precision == YK_MIXED, ctx->stream, &ctx->cg_grid, &ctx->cg_kernel));
             if (bal) YK_CK(launch_cg_balance(a, ctx->cg_grid, ctx->d_balance, ctx->stream));
@@ -733,6 +733,7 @@ int run_autotune(yk_ctx* ctx)
         a.st = ctx->d_state;
         a.partial = ctx->d_partial;
         a.coef = ctx->d_coef;
+        eo_args(ctx, a);   // the kernel the step runs
         a.max_iter = std::min(ctx->max_iter, 48);
         int best = 0;
         float best_ms = 0.f;
@@ -860,38 +861,53 @@ int pion_setup(yk_ctx* ctx)
 // the end -- and its tile table.
 int eo_setup(yk_ctx* ctx, const std::vector<SysDev>& hs)
 {
+    // Compact views of the step's systems: a single system (cg_eo_kernel, or
+    // cg_eob_kernel when its lattice is too large for the halo kernel's shared
+    // memory) or every system of a batched step (cg_eob_kernel).  Mixed
+    // precision, sigma-only, every lattice even with Nx >= 4.
     const char* env = getenv("YK_CG_EO");
-    if ((env && env[0] == '0') || ctx->nsys != 1 || ctx->precision != YK_MIXED || !ctx->cg_halo || ctx->cg_cluster ||
-        ctx->pions)
+    if ((env && env[0] == '0') || ctx->nsys < 1 || ctx->nsys > kEobMaxSystems || ctx->precision != YK_MIXED ||
+        ctx->cg_cluster || ctx->pions || (ctx->nsys == 1 && !ctx->cg_halo))
         return YK_OK;
-    const Chain* C = nullptr;
     for (const Chain& q : ctx->ch)
-        if (q.n_rhs_step == 1) C = &q;
-    if (!C || (C->Nt & 1) || (C->Nx & 1) || C->Nx < 4) return YK_OK;
-    const int Ve = C->V / 2, nte = ntiles_of(Ve);
-    SysDev E = hs[C->sys0];
-    E.Nx = C->Nx / 2;
-    E.V = Ve;
-    E.tile0 = C->cg_tile0;
-    E.ntiles = nte;
-    std::vector<int2> tiles(ctx->n_sys_tiles, make_int2(C->sys0, 0));
-    for (int t = 0; t < nte; ++t) tiles[C->cg_tile0 + t] = make_int2(C->sys0, t * kTile);
+        if (q.n_rhs_step > 0 && ((q.Nt & 1) || (q.Nx & 1) || q.Nx < 4)) return YK_OK;
+    std::vector<SysDev> views(hs);
+    std::vector<int2> tiles(ctx->n_sys_tiles, make_int2(0, 0));
+    size_t n_dinv = 0;
+    for (int sidx = 0; sidx < ctx->nsys; ++sidx) n_dinv += (size_t)hs[sidx].V / 2;
     const size_t o_tiles = ((sizeof(SysDev) * ctx->nsys + 255) / 256) * 256;
     const size_t o_dinv = o_tiles + ((sizeof(int2) * tiles.size() + 255) / 256) * 256;
-    if (cudaMalloc(&ctx->eo_mem, o_dinv + sizeof(double) * (size_t)Ve) != cudaSuccess) {
+    if (cudaMalloc(&ctx->eo_mem, o_dinv + sizeof(double) * n_dinv) != cudaSuccess) {
         cudaGetLastError();
         set_error("even-odd view allocation failed");
         return YK_ENOMEM;
     }
+    double* dinv = reinterpret_cast<double*>(static_cast<char*>(ctx->eo_mem) + o_dinv);
+    for (int sidx = 0; sidx < ctx->nsys; ++sidx) {
+        const SysDev& S = hs[sidx];
+        SysDev& E = views[sidx];
+        const int Ve = S.V / 2, nte = ntiles_of(Ve);
+        E.Nx = S.Nx / 2;
+        E.V = Ve;
+        E.tile0 = S.tile0;   // the first nte slots of the system's tile range
+        E.ntiles = nte;
+        E.dinv = dinv;
+        dinv += Ve;
+        E.v32 = S.xs32 + 4 * (size_t)Ve;     // the halves the compact vectors leave free
+        E.w32 = S.r32[1] + 4 * (size_t)Ve;
+        for (int t = 0; t < nte; ++t) tiles[S.tile0 + t] = make_int2(sidx, t * kTile);
+    }
     ctx->d_sys_eo = reinterpret_cast<SysDev*>(ctx->eo_mem);
     ctx->d_eo_tiles = reinterpret_cast<int2*>(static_cast<char*>(ctx->eo_mem) + o_tiles);
-    E.dinv = reinterpret_cast<double*>(static_cast<char*>(ctx->eo_mem) + o_dinv);
-    std::vector<SysDev> views(hs);
-    views[C->sys0] = E;
     YK_CK(cudaMemcpy(ctx->d_sys_eo, views.data(), sizeof(SysDev) * views.size(), cudaMemcpyHostToDevice));
     YK_CK(cudaMemcpy(ctx->d_eo_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
-    ctx->eo_tile_begin = C->cg_tile0;
-    ctx->eo_tile_end = C->cg_tile0 + nte;
+    if (ctx->nsys == 1) {
+        ctx->eo_tile_begin = hs[0].tile0;
+        ctx->eo_tile_end = hs[0].tile0 + views[0].ntiles;
+    } else {
+        ctx->eo_tile_begin = 0;
+        ctx->eo_tile_end = ctx->n_sys_tiles;
+    }
     ctx->cg_eo = true;
     return YK_OK;
 }

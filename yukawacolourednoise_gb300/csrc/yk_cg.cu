@@ -483,6 +483,7 @@ __device__ __forceinline__ float4 ld_sync4f(const void* p)
 struct CoefVals {
     double alpha_re, alpha_im, beta, c_re, c_im;
     int mode;
+    int par;   // batched even-odd solves: the system's buffer parity in the next pass
 };
 
 __device__ __forceinline__ unsigned long long stamp(unsigned payload, unsigned gen)
@@ -526,7 +527,7 @@ __device__ __forceinline__ void publish_coef(CGCoef* c, const CoefVals& v, unsig
         w[2 * i + 1] = stamp((unsigned)(u >> 32), gen);
     }
     w[10] = stamp((unsigned)v.mode, gen);
-    w[11] = stamp(0u, gen);
+    w[11] = stamp((unsigned)v.par, gen);
 #pragma unroll
     for (int i = 0; i < 6; ++i) st_pair(c->w + 2 * i, w[2 * i], w[2 * i + 1]);
 }
@@ -556,6 +557,7 @@ __device__ bool poll_coef(const CGCoef* c, unsigned gen, CoefVals& v, int* err)
             v.c_re = d[3];
             v.c_im = d[4];
             v.mode = (int)(unsigned)(h[10] & 0xffffffffull);
+            v.par = (int)(unsigned)(h[11] & 0xffffffffull);
             return true;
         }
         if (wait_over(t0, err)) return false;
@@ -701,7 +703,9 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         // the few SMs that own the system's tiles, at the FP64 rate, and every
         // other block waits for it at the grid barrier.  A candidate far below
         // its target (the recursion nears breakdown) does not wait.
-        const bool aligned = a.sys_count == 1 || (k + 1) % kRuAlign == 0;
+        // (the batched even-odd kernel runs a system's update inside the
+        // ordinary pass, on every block: no alignment)
+        const bool aligned = a.sys_count == 1 || a.eo || (k + 1) % kRuAlign == 0;
         const bool deep = est < 1e-6 * st.stop2;
         if (force_ru || (cand && (aligned || deep)) || (drop && aligned) || due || cap) {
             cv.mode = kRu;
@@ -972,7 +976,14 @@ __device__ __noinline__ void finish_reduction(const CGArgs& a, int k, bool ru_ro
         const bool writer = have && tg == 0;
         CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
         if (writer && st.mode != kIdle) {
-            if (ru_round && st.mode != kRu) {
+            if (a.eo) {
+                // batched even-odd: every system keeps its own iteration index;
+                // an update ran in this pass for the systems in kRu, at the
+                // index after st.iters, and the pass that redoes its step keeps it
+                const int ks = k == 0 ? 0 : (st.mode == kRedo ? st.iters : st.iters + 1);
+                cv = scalar_step<MIXED>(a, ks, st.mode == kRu, s, st, s_active, s_ru);
+                cv.par = (cv.mode == kRedo ? st.iters : st.iters + 1) & 1;
+            } else if (ru_round && st.mode != kRu) {
                 cv.mode = kWait;
                 atomicAdd(s_active, 1);
             } else {
@@ -2371,8 +2382,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     };
     for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads)
         de_b[j - 2 * Nh] = (float)diag_at(wrap_site(cbase + j, Ve), 0);
-    const double* chi_e = S.x;                      // compact FP64
-    const double* rhs_e = S.x + 4 * (size_t)Ve;
+    const double* rhs_e = S.x + 4 * (size_t)Ve;    // after chi_e (compact FP64)
     unsigned epoch = 0, gen = 0;
     int staged_k = -1;
 #ifdef YK_CG_TIMING
@@ -2751,6 +2761,505 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// Batched even-odd mixed CG (cg_eob_kernel): the Schur-complement CGNE of
+// cg_eo_kernel for every system of a batched step at once (chains of any
+// even lattice, several right-hand sides each), and for single systems too
+// large for cg_eo_kernel's shared memory.  The systems' compact views share
+// one tile table; tile partials, the finisher's per-system scalar steps and
+// the coefficient words are those of cg_kernel (finish_reduction,
+// scalar_step with the even-odd first threshold).
+//
+// Work is dealt out per pass, not per block: each pass takes the tiles of
+// the systems that work in it (a prefix over the systems' tile counts,
+// rebuilt from the published modes every round) and gives every block an
+// equal contiguous share.  A system that converges early leaves no block
+// idle while the slow ones iterate; passes are separated by grid barriers.
+// A round, each system by its mode (kStep, kRedo after an update; kRu):
+//   P1 (even)  r, p, chi increment of the own site; w = -A_o^-1 H_oe p at the
+//              compact index's odd site, the neighbours' p formed from the
+//              previous iteration's r, q, p (the same arithmetic as theirs);
+//              kRu: fold chi_e += xs + alpha v in FP64
+//   P2 (even)  v = A_e p + H_eo w (= S^dag p);  kRu: R2 u = -A_o^-1 H^dag_oe
+//              chi_e in FP64 (t64)
+//   P3 (odd)   u = -A_o^-1 H^dag_oe v;  kRu: R3 r = rhs_e - (A_e chi_e +
+//              H^dag_eo u) in FP64, partials |r|^2, <r, p_{k-1}>
+//   P4 (even)  q = A_e v + H^dag_eo u (= S v), tile partials |r|^2, |q|^2,
+//              |v|^2, <r, q>; the reducing barrier.
+// A system's update thus costs no round of the others: each keeps its own
+// iteration index, and its buffers alternate with that index's parity
+// (published with its coefficients).
+// Round 0: eta (both classes), 1 / A_o (dinv), -A_o^-1 eta_o; rhs_e; then the
+// passes of an ordinary round from p_0 = r_0 = rhs_e (slot 5: |eta|^2).
+// At the end chi in the full layout (t64) for the force.
+// Buffers of a view (compact, Ve = V / 2 sites): x = chi_e then rhs_e (FP64),
+// t64 the odd FP64 hops, r32[2], p32[2], q in Ap32 / t32 by iteration parity,
+// xs32 the chi increment, v32 and w32 (w, later u), diag32 = A_e then 1 / A_o
+// in FP32, dinv 1 / A_o in FP64.
+// ---------------------------------------------------------------------------
+constexpr int kEobMaxSys = kEobMaxSystems;
+
+// Grid barrier without a reduction (the arrival counter of grid_reduce runs on).
+__device__ bool eob_barrier(const CGArgs& a, unsigned& gen)
+{
+    __syncthreads();
+    int bad = 0;
+    if (threadIdx.x == 0) {
+        arrive_release(&a.bar->arrive);
+        const unsigned target = gridDim.x * (gen + 1u);
+        const long long t0 = clock64();
+        while ((int)(ld_acquire(&a.bar->arrive) - target) < 0)
+            if (wait_over(t0, a.err)) {
+                bad = 1;
+                break;
+            }
+    }
+    ++gen;
+    return __syncthreads_or(bad) == 0;
+}
+
+// Exclusive prefix over the systems of the tile counts of those whose mode is
+// in `mask` (bit per mode); s_pre[nsys] = the total.  Two systems per thread
+// (blockDim = 512, nsys <= 1024).
+__device__ void eob_scan(int nsys, const int* s_mode, const int* s_nt, int mask, int* s_pre)
+{
+    __shared__ int ws[kHaloThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int q0 = 2 * t, q1 = 2 * t + 1;
+    const int c0 = (q0 < nsys && ((mask >> s_mode[q0]) & 1)) ? s_nt[q0] : 0;
+    const int c1 = (q1 < nsys && ((mask >> s_mode[q1]) & 1)) ? s_nt[q1] : 0;
+    int v = c0 + c1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) ws[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < kHaloThreads / 32 ? ws[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane < kHaloThreads / 32) ws[lane] = x;
+    }
+    __syncthreads();
+    const int base = (w > 0 ? ws[w - 1] : 0) + v - (c0 + c1);
+    if (q0 < nsys) s_pre[q0] = base;
+    if (q1 < nsys) s_pre[q1] = base + c0;
+    if (t == 0) s_pre[nsys] = ws[kHaloThreads / 32 - 1];
+    __syncthreads();
+}
+
+// The system of entry i of the current prefix: the largest q < nsys with
+// s_pre[q] <= i (systems without tiles in the pass share their successor's start).
+__device__ __forceinline__ int eob_find(int i, int nsys, const int* s_pre)
+{
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pre[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// This block's contiguous share [lo, hi) of `total` entries.
+__device__ __forceinline__ void eob_share(int total, int* lo, int* hi)
+{
+    *lo = (int)(((long long)total * blockIdx.x) / gridDim.x);
+    *hi = (int)(((long long)total * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// Modes of the round from the published coefficient words of every system,
+// and the grid word (systems still iterating, whether any updates reliably).
+__device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_mode, int* s_par, float* s_fa,
+                               float* s_fb, float* s_fc, double* s_da, int* s_nact, int* s_anyru)
+{
+    int bad = 0;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        CoefVals v;
+        if (!poll_coef(a.coef + a.sys_first + q, gen, v, a.err)) {
+            bad = 1;
+        } else {
+            s_mode[q] = v.mode;
+            s_par[q] = v.par;
+            s_fa[q] = (float)v.alpha_re;
+            s_fb[q] = (float)v.beta;
+            s_fc[q] = (float)v.c_re;
+            s_da[q] = v.alpha_re;
+        }
+        __threadfence();   // acquire: the writes before the reducing barrier
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        const long long t0 = clock64();
+        unsigned long long g;
+        while ((unsigned)((g = ld_word(&a.bar->gword)) >> 32) != gen)
+            if (wait_over(t0, a.err)) {
+                bad = 1;
+                break;
+            }
+        *s_nact = (int)(g & 0x7fffffffull);
+        *s_anyru = (int)((g >> 31) & 1ull);
+        __threadfence();
+    }
+    return __syncthreads_or(bad) == 0;
+}
+
+__global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
+{
+    constexpr int K = 1;
+    constexpr int kSkipIm = (1 << 3) | (1 << 5);
+    using W = float;
+    const int hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;
+    __shared__ double red[128];
+    __shared__ int s_mode[kEobMaxSys], s_par[kEobMaxSys], s_nt[kEobMaxSys], s_t0[kEobMaxSys], s_pre[kEobMaxSys + 1];
+    __shared__ float s_fa[kEobMaxSys], s_fb[kEobMaxSys], s_fc[kEobMaxSys];
+    __shared__ double s_da[kEobMaxSys];
+    __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
+    const int nsys = a.sys_count;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        const SysDev& S = a.sys[a.sys_first + q];
+        s_nt[q] = S.ntiles;
+        s_t0[q] = S.tile0;
+        s_mode[q] = kStep;
+        s_par[q] = 0;
+        s_fa[q] = s_fb[q] = s_fc[q] = 0.f;
+        s_da[q] = 0.0;
+    }
+    __syncthreads();
+    if (*(volatile int*)a.err) return;
+    unsigned gen = 0;
+    constexpr int kAll = (1 << kStep) | (1 << kRedo) | (1 << kRu) | (1 << kWait);
+    constexpr int kP1 = (1 << kStep) | (1 << kRedo) | (1 << kRu);
+    constexpr int kP2 = (1 << kStep) | (1 << kRedo);
+    constexpr int kPR = 1 << kRu;
+    constexpr int kInit = -1;   // round 0: p_0 as stored
+
+    // Runs f(S, q, m, tile, on) for every site of this block's share of the
+    // tiles of the systems in `mask`, two tiles at a time (every thread the
+    // same trip count: f may hold block-wide barriers).
+    auto for_sites = [&](int mask, auto&& f) {
+        eob_scan(nsys, s_mode, s_nt, mask, s_pre);
+        int lo, hi;
+        eob_share(s_pre[nsys], &lo, &hi);
+        for (int base = lo; base < hi; base += 2) {
+            const int i = base + hf;
+            const bool tile_on = i < hi;
+            const int q = eob_find(tile_on ? i : lo, nsys, s_pre);
+            const int lt = (tile_on ? i : lo) - s_pre[q];
+            const SysDev& S = a.sys[a.sys_first + q];
+            const int m = lt * kTile + ts;
+            f(S, q, m, s_t0[q] + lt, tile_on, tile_on && m < S.V);
+        }
+    };
+
+    // the compact geometry of site m of class c: row t, time signs
+    struct Geo {
+        int t, b, du, dd, mu, md;
+        float sp, sm;
+    };
+    auto geo = [](const SysDev& S, int m, int c) {
+        Geo g;
+        const int Nh = S.Nx, Ve = S.V;
+        g.t = m / Nh;
+        const int i = m - g.t * Nh;
+        g.b = (g.t + c) & 1;
+        g.du = g.b ? ((i == Nh - 1) ? 1 - Nh : 1) : 0;
+        g.dd = g.b ? 0 : ((i == 0) ? Nh - 1 : -1);
+        g.mu = m + Nh >= Ve ? m + Nh - Ve : m + Nh;
+        g.md = m - Nh < 0 ? m - Nh + Ve : m - Nh;
+        g.sp = (g.t + 1 == S.Nt) ? -1.f : 1.f;
+        g.sm = (g.t == 0) ? -1.f : 1.f;
+        return g;
+    };
+    auto qbuf = [](const SysDev& S, int it) -> float* { return it == 0 ? S.Ap32 : S.t32; };
+
+    // p of iteration `cur` at even compact site n (mode kStep: from r, q, p of
+    // prv; kRedo: from the FP64 residual in r[cur]; round 0: p_0 as stored)
+    auto p_at = [&](const SysDev& S, int q, int n, int mode, int cur, int prv) -> Site<W, K> {
+        if (mode == kStep) {
+            Site<W, K> r = YK_LD(W, K, S.r32[prv], n);
+            site_axpy<W, K>(r, -s_fa[q], W(0), YK_LD(W, K, qbuf(S, prv), n));
+            const Site<W, K> po = YK_LD(W, K, S.p32[prv], n);
+            Site<W, K> p;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) p.v[e] = fma(s_fb[q], po.v[e], r.v[e]);
+            return p;
+        }
+        if (mode == kRedo)
+            return p_next<W, K>(YK_LD(W, K, S.r32[cur], n), YK_LD(W, K, S.p32[prv], n), s_fb[q], s_fc[q], W(0));
+        return YK_LD(W, K, S.p32[cur], n);
+    };
+
+    // P1 of an ordinary round (init: round 0, p_0 as stored) and the fold of
+    // a reliable-update round
+    auto pass_p1 = [&](bool init) {
+        for_sites(init ? kAll : kP1, [&](const SysDev& S, int q, int m, int, bool, bool on) {
+            if (!on) return;
+            const int mode = init ? kInit : s_mode[q];
+            const int cur = s_par[q], prv = cur ^ 1;
+            if (mode == kRu) {
+                Site<double, K> xv = YK_LD(double, K, S.x, m);
+                const Site<W, K> xs = YK_LD(W, K, S.xs32, m);
+                const Site<W, K> vv = YK_LD(W, K, S.v32, m);
+                Site<W, K> zw;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    xv.v[e] += (double)xs.v[e];
+                    xv.v[e] = fma(s_da[q], (double)vv.v[e], xv.v[e]);
+                    zw.v[e] = W(0);
+                }
+                YK_ST(double, K, S.x, m, xv);
+                YK_ST(W, K, S.xs32, m, zw);
+                return;
+            }
+            if (mode == kStep) {
+                Site<W, K> r = YK_LD(W, K, S.r32[prv], m);
+                site_axpy<W, K>(r, -s_fa[q], W(0), YK_LD(W, K, qbuf(S, prv), m));
+                const Site<W, K> po = YK_LD(W, K, S.p32[prv], m);
+                Site<W, K> p;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) p.v[e] = fma(s_fb[q], po.v[e], r.v[e]);
+                Site<W, K> xs = YK_LD(W, K, S.xs32, m);
+                site_axpy<W, K>(xs, s_fa[q], W(0), YK_LD(W, K, S.v32, m));
+                YK_ST(W, K, S.xs32, m, xs);
+                YK_ST(W, K, S.r32[cur], m, r);
+                YK_ST(W, K, S.p32[cur], m, p);
+            } else if (mode == kRedo) {
+                YK_ST(W, K, S.p32[cur], m, (p_at(S, q, m, kRedo, cur, prv)));
+            }
+            // w at the compact index's odd site from the p of its even neighbours
+            const Geo g = geo(S, m, 1);
+            Site<W, K> zero;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) zero.v[e] = W(0);
+            Site<W, K> h = dirac_combine<W, K, false>(zero, p_at(S, q, g.mu, mode, cur, prv),
+                                                      p_at(S, q, g.md, mode, cur, prv),
+                                                      p_at(S, q, m + g.du, mode, cur, prv),
+                                                      p_at(S, q, m + g.dd, mode, cur, prv), W(0), (W)S.r, g.sp, g.sm);
+            const W s = -S.diag32[S.V + m];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) h.v[e] *= s;
+            YK_ST(W, K, S.w32, m, h);
+        });
+    };
+
+    // P2: v = A_e p + H_eo w (even)
+    auto pass_p2 = [&](int mask) {
+        for_sites(mask, [&](const SysDev& S, int q, int m, int, bool, bool on) {
+            if (!on) return;
+            const int cur = s_par[q];
+            const Geo g = geo(S, m, 0);
+            const Site<W, K> v = dirac_combine<W, K, false>(
+                YK_LD(W, K, S.p32[cur], m), YK_LD(W, K, S.w32, g.mu), YK_LD(W, K, S.w32, g.md),
+                YK_LD(W, K, S.w32, m + g.du), YK_LD(W, K, S.w32, m + g.dd), S.diag32[m], (W)S.r, g.sp, g.sm);
+            YK_ST(W, K, S.v32, m, v);
+        });
+    };
+
+    // P3: u = -A_o^-1 H^dag_oe v (odd, into w32)
+    auto pass_p3 = [&](int mask) {
+        for_sites(mask, [&](const SysDev& S, int, int m, int, bool, bool on) {
+            if (!on) return;
+            const Geo g = geo(S, m, 1);
+            Site<W, K> zero;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) zero.v[e] = W(0);
+            Site<W, K> h = dirac_combine<W, K, true>(zero, YK_LD(W, K, S.v32, g.mu), YK_LD(W, K, S.v32, g.md),
+                                                     YK_LD(W, K, S.v32, m + g.du), YK_LD(W, K, S.v32, m + g.dd),
+                                                     W(0), (W)S.r, g.sp, g.sm);
+            const W s = -S.diag32[S.V + m];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) h.v[e] *= s;
+            YK_ST(W, K, S.w32, m, h);
+        });
+    };
+
+    // P4: q = A_e v + H^dag_eo u (even) and the tile partials (round 0 adds
+    // |eta|^2 of the compact index's two full sites in slot 5)
+    auto pass_p4 = [&](int mask, bool round0) {
+        for_sites(mask, [&](const SysDev& S, int q, int m, int tile, bool tile_on, bool on) {
+            const int cur = s_par[q];
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+            if (on) {
+                const Geo g = geo(S, m, 0);
+                const Site<W, K> v = YK_LD(W, K, S.v32, m);
+                const Site<W, K> qv = dirac_combine<W, K, true>(
+                    v, YK_LD(W, K, S.w32, g.mu), YK_LD(W, K, S.w32, g.md), YK_LD(W, K, S.w32, m + g.du),
+                    YK_LD(W, K, S.w32, m + g.dd), S.diag32[m], (W)S.r, g.sp, g.sm);
+                YK_ST(W, K, qbuf(S, cur), m, qv);
+                const Site<W, K> r = YK_LD(W, K, S.r32[cur], m);
+                W rq, dummy;
+                site_dot<W, K>(r, qv, rq, dummy);
+                f[0] = FF{site_norm2<W, K>(r), 0.f};
+                f[1] = FF{site_norm2<W, K>(qv), 0.f};
+                f[2] = FF{site_norm2<W, K>(v), 0.f};
+                f[4] = FF{rq, 0.f};
+                if (round0) {
+                    const Site<double, K> e0 = load_site<double, K>(S.b, 2 * m);
+                    const Site<double, K> e1 = load_site<double, K>(S.b, 2 * m + 1);
+                    f[5] = ff_of(site_norm2<double, K>(e0) + site_norm2<double, K>(e1));
+                }
+            }
+            if (round0)
+                put_partial_ff<(1 << 3), true>(a, tile, tile_on, f, red);
+            else
+                put_partial_ff<kSkipIm, false>(a, tile, tile_on, f, red);
+        });
+    };
+
+    // ---------------- round 0
+    // eta of both classes (b, full layout), A_e and 1 / A_o, -A_o^-1 eta_o (t64),
+    // chi_e = xs = v = 0
+    for_sites(kAll, [&](const SysDev& S, int, int m, int, bool, bool on) {
+        if (!on) return;
+        const int Ve = S.V;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const Geo g = geo(S, m, c);
+            const int n = 2 * m + g.b;
+            const Site<double, K> bv = S.gen_eta ? eta_of_step<K>(S, n, a.eta_kind) : load_site<double, K>(S.b, n);
+            if (S.gen_eta) store_site<double, K>(S.b, n, bv);
+            const double d = 2.0 * S.r + S.m0 + S.g * S.sigma[n];
+            if (c == 0) {
+                S.diag32[m] = (float)d;
+            } else {
+                const double inv = 1.0 / d;
+                S.dinv[m] = inv;
+                S.diag32[Ve + m] = (float)inv;
+                Site<double, K> h;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) h.v[e] = -inv * bv.v[e];
+                store_site<double, K>(S.t64, m, h);
+            }
+        }
+        Site<double, K> z;
+        Site<W, K> zw;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            z.v[e] = 0.0;
+            zw.v[e] = W(0);
+        }
+        store_site<double, K>(S.x, m, z);
+        YK_ST(W, K, S.xs32, m, zw);
+        YK_ST(W, K, S.v32, m, zw);
+    });
+    if (!eob_barrier(a, gen)) return;
+    // rhs_e = eta_e + H^dag_eo (-A_o^-1 eta_o); r_0 = p_0 = rhs_e
+    for_sites(kAll, [&](const SysDev& S, int, int m, int, bool, bool on) {
+        if (!on) return;
+        const Geo g = geo(S, m, 0);
+        const Site<double, K> e = load_site<double, K>(S.b, 2 * m + g.b);
+        const Site<double, K> rh =
+            eo_gl<true>(S.t64, m, S.V, S.Nx, g.du, g.dd, e, 1.0, S.r, (double)g.sp, (double)g.sm);
+        store_site<double, K>(S.x + 4 * (size_t)S.V, m, rh);
+        Site<W, K> rw;
+#pragma unroll
+        for (int e2 = 0; e2 < 4; ++e2) rw.v[e2] = (float)rh.v[e2];
+        YK_ST(W, K, S.r32[0], m, rw);
+        YK_ST(W, K, S.p32[0], m, rw);
+    });
+    if (!eob_barrier(a, gen)) return;
+    pass_p1(true);
+    if (!eob_barrier(a, gen)) return;
+    pass_p2(kAll);
+    if (!eob_barrier(a, gen)) return;
+    pass_p3(kAll);
+    if (!eob_barrier(a, gen)) return;
+    pass_p4(kAll, true);
+    grid_reduce<true>(a, gen, 0, false, &s_flag, &s_active, &s_ru, red);
+
+    // Systems in kRu run their update in the passes of the round (R2 beside P2,
+    // R3 beside P3); every system keeps its own iteration index (the
+    // finisher's), which advances at least every other round.
+    int k = 1;
+    const int kmax = 2 * a.max_iter + 2;
+    while (k <= kmax) {
+        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, s_da, &s_nact, &s_anyru)) return;
+        if (s_nact == 0) break;
+        pass_p1(false);
+        if (!eob_barrier(a, gen)) return;
+        pass_p2(kP2);
+        // R2: u = -A_o^-1 H^dag_oe chi_e (FP64, odd, t64)
+        for_sites(kPR, [&](const SysDev& S, int, int m, int, bool, bool on) {
+            if (!on) return;
+            const Geo g = geo(S, m, 1);
+            Site<double, K> zero;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) zero.v[e] = 0.0;
+            Site<double, K> h =
+                eo_gl<true>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, 0.0, S.r, (double)g.sp, (double)g.sm);
+            const double sc = -S.dinv[m];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) h.v[e] *= sc;
+            store_site<double, K>(S.t64, m, h);
+        });
+        if (!eob_barrier(a, gen)) return;
+        pass_p3(kP2);
+        // R3: r = rhs_e - (A_e chi_e + H^dag_eo u) in FP64; |r|^2, <r, p_{k-1}>
+        for_sites(kPR, [&](const SysDev& S, int q, int m, int tile, bool tile_on, bool on) {
+            const int cur = s_par[q], prv = cur ^ 1;
+            double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            if (on) {
+                const Geo g = geo(S, m, 0);
+                const double de = 2.0 * S.r + S.m0 + S.g * S.sigma[2 * m + g.b];
+                const Site<double, K> sx = eo_gl<true>(S.t64, m, S.V, S.Nx, g.du, g.dd, load_site<double, K>(S.x, m),
+                                                       de, S.r, (double)g.sp, (double)g.sm);
+                const Site<double, K> bv = load_site<double, K>(S.x + 4 * (size_t)S.V, m);
+                const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
+                Site<double, K> rd, pd;
+                Site<W, K> rw;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    rd.v[e] = bv.v[e] - sx.v[e];
+                    rw.v[e] = (float)rd.v[e];
+                    pd.v[e] = (double)pw.v[e];
+                }
+                YK_ST(W, K, S.r32[cur], m, rw);
+                v[0] = site_norm2<double, K>(rd);
+                site_dot<double, K>(rd, pd, v[2], v[3]);
+            }
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+            put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
+        });
+        if (!eob_barrier(a, gen)) return;
+        pass_p4(kP2, false);
+        grid_reduce<true>(a, gen, k, false, &s_flag, &s_active, &s_ru, red);
+        ++k;
+    }
+    // chi of both classes in the full layout (t64) for the force: chi_e, and
+    // chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
+    if (!eob_barrier(a, gen)) return;
+    for_sites(kAll | (1 << kIdle), [&](const SysDev& S, int, int m, int, bool, bool on) {
+        if (!on) return;
+        Geo g = geo(S, m, 0);
+        store_site<double, K>(S.t64, 2 * m + g.b, load_site<double, K>(S.x, m));
+        g = geo(S, m, 1);
+        Site<double, K> zero;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) zero.v[e] = 0.0;
+        const Site<double, K> h =
+            eo_gl<true>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, 0.0, S.r, (double)g.sp, (double)g.sm);
+        const int n = 2 * m + g.b;
+        const Site<double, K> e = load_site<double, K>(S.b, n);
+        const double inv = S.dinv[m];
+        Site<double, K> co;
+#pragma unroll
+        for (int e2 = 0; e2 < 4; ++e2) co.v[e2] = (e.v[e2] - h.v[e2]) * inv;
+        store_site<double, K>(S.t64, n, co);
+    });
+    if (blockIdx.x == 0)
+        for (int q = threadIdx.x; q < nsys; q += blockDim.x) a.st[a.sys_first + q].chi_ready = 1;
+}
+
+
 // Shared memory of cg_eo_kernel for own compact sites per block and Nh.
 static size_t eo_smem_bytes(int own, int Nh)
 {
@@ -2920,6 +3429,20 @@ static int eo_max_grid()
     return maxg;
 }
 
+static int eob_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eob_kernel, kHaloThreads, 0);
+        maxg = per * nsm;
+        if (maxg > kMaxGrid) maxg = kMaxGrid;
+    }
+    return maxg;
+}
+
 static int halo_max_grid()
 {
     static int maxg = -1;
@@ -2938,6 +3461,7 @@ void cg_halo_init()
 {
     halo_max_grid();
     eo_max_grid();
+    eob_max_grid();
 }
 
 static int capped(int maxg, int cap) { return cap > 0 && cap < maxg ? cap : maxg; }
@@ -2967,7 +3491,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
     if constexpr (K == 1 && MIXED) {
         // the even-odd solve of the step's chi (a single system of A = D^dag D
         // on an even lattice, when the caller gave the compact views)
-        if (a.sys_count == 1 && a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr) {
+        if (a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr && a.sys_count <= kEobMaxSys) {
             CGArgs e = a;
             e.sys_full = a.sys;
             e.sys = a.sys_eo;
@@ -2978,7 +3502,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
             int etpb = 1;
             const int eg = cg_grid_for(e.tile_end - e.tile_begin, capped(eo_max_grid(), a.grid_cap), &etpb);
             size_t es = 0;
-            if (eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, etpb, &es)) {
+            if (a.sys_count == 1 && eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, etpb, &es)) {
                 e.tiles_per_block = etpb;
                 e.grid = eg;
                 if (grid_out) *grid_out = eg;
@@ -2997,6 +3521,29 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 void* args[] = {&e};
                 return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel, args);
             }
+            // the batched even-odd kernel: work dealt out per pass, so the
+            // grid does not follow the tiles (at most one block per two tiles)
+            int bg = capped(eob_max_grid(), a.grid_cap);
+            const int want = (a.eo_tile_end - a.eo_tile_begin + 1) / 2;
+            if (bg > want) bg = want;
+            if (bg < 1) bg = 1;
+            e.grid = bg;
+            e.tiles_per_block = 1;
+            if (grid_out) *grid_out = bg;
+            if (kernel_out) *kernel_out = 4;
+            cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(bg);
+            cfg.blockDim = dim3(kHaloThreads);
+            cfg.dynamicSmemBytes = 0;
+            cfg.stream = stream;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            void* args[] = {&e};
+            return cudaLaunchKernelExC(&cfg, (const void*)cg_eob_kernel, args);
         }
         // the same tile partition as cg_kernel<1, true>, so the same partials
         size_t hs = 0;

@@ -21,6 +21,7 @@ constexpr int kMaxFFT = 4096; // longest FFT edge handled in shared memory
 constexpr int kMaxDFT = 256;  // longest non-power-of-two edge (direct DFT)
 constexpr int kMaxTilesPerBlock = 4096;  // tiles one CG block may own
 constexpr int kMaxGrid = 2048;           // blocks of a CG launch (neighbour flags allocated)
+constexpr int kEobMaxSystems = 1024;     // systems of one batched even-odd solve
 constexpr int kFlagStride = 32;          // one 128-byte line per neighbour flag
 
 // Grid barrier of the CG kernel: arrivals are counted (monotonically within a
@@ -60,6 +61,8 @@ struct SysDev {
     float* xs32;         // solution increment since the last reliable update
     float* diag32;       // 2r + m0 + g sigma per site (one float)
     double* dinv;        // even-odd views: 1 / (2r + m0 + g sigma) on the odd sites (compact)
+    float* v32;          // batched even-odd views: v = S^dag p (even, compact)
+    float* w32;          // and w, later u (odd, compact)
     // noise generation for b: kind/rhs of the Philox stream, or gen = 0
     int gen_eta;
     uint64_t seed;
