@@ -2873,12 +2873,44 @@ __device__ __forceinline__ void eob_share(int total, int* lo, int* hi)
     *hi = (int)(((long long)total * (blockIdx.x + 1)) / gridDim.x);
 }
 
-// Modes of the round from the published coefficient words of every system,
-// and the grid word (systems still iterating, whether any updates reliably).
-__device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_mode, int* s_par, float* s_fa,
-                               float* s_fb, float* s_fc, double* s_da, int* s_nact, int* s_anyru)
+// The reducing barrier of a round: after the barrier every block finishes
+// the systems q = blockIdx.x, blockIdx.x + gridDim.x, ...: sums their tile
+// partials (sum_partials: fixed order), runs the scalar step at the system's
+// own iteration index (an update ran in this round for a system in kRu; the
+// round that redoes its step keeps the index) and publishes the coefficients,
+// mode and buffer parity of the next round.  No block finishes for all.
+__device__ bool eob_reduce(const CGArgs& a, unsigned& gen, int k, double* red, int* s_active, int* s_ru)
 {
-    int bad = 0;
+    if (!eob_barrier(a, gen)) return false;
+    for (int q = blockIdx.x; q < a.sys_count; q += gridDim.x) {
+        const int j = a.sys_first + q;
+        const SysDev& S = a.sys[j];
+        double s[6];
+        sum_partials<true>(a, S.tile0, S.ntiles, red, s);
+        if (threadIdx.x == 0) {
+            CGState st;
+            load_state(a.st + j, st);
+            CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
+            if (st.mode != kIdle) {
+                const int ks = k == 0 ? 0 : (st.mode == kRedo ? st.iters : st.iters + 1);
+                cv = scalar_step<true>(a, ks, st.mode == kRu, s, st, s_active, s_ru);
+                cv.par = (cv.mode == kRedo ? st.iters : st.iters + 1) & 1;
+            }
+            st.mode = cv.mode;
+            store_state(a.st + j, st);
+            __threadfence();
+            publish_coef(a.coef + j, cv, gen);
+        }
+    }
+    return true;
+}
+
+// Modes of the round from the published coefficient words of every system;
+// *nact (every thread) = how many threads saw a system still iterating.
+__device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_mode, int* s_par, float* s_fa,
+                               float* s_fb, float* s_fc, double* s_da, int* nact)
+{
+    int bad = 0, act = 0;
     for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
         CoefVals v;
         if (!poll_coef(a.coef + a.sys_first + q, gen, v, a.err)) {
@@ -2890,21 +2922,10 @@ __device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_m
             s_fb[q] = (float)v.beta;
             s_fc[q] = (float)v.c_re;
             s_da[q] = v.alpha_re;
+            act += v.mode != kIdle;
         }
-        __threadfence();   // acquire: the writes before the reducing barrier
     }
-    if (threadIdx.x == blockDim.x - 1) {
-        const long long t0 = clock64();
-        unsigned long long g;
-        while ((unsigned)((g = ld_word(&a.bar->gword)) >> 32) != gen)
-            if (wait_over(t0, a.err)) {
-                bad = 1;
-                break;
-            }
-        *s_nact = (int)(g & 0x7fffffffull);
-        *s_anyru = (int)((g >> 31) & 1ull);
-        __threadfence();
-    }
+    *nact = __syncthreads_count(act > 0);
     return __syncthreads_or(bad) == 0;
 }
 
@@ -2918,7 +2939,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     __shared__ int s_mode[kEobMaxSys], s_par[kEobMaxSys], s_nt[kEobMaxSys], s_t0[kEobMaxSys], s_pre[kEobMaxSys + 1];
     __shared__ float s_fa[kEobMaxSys], s_fb[kEobMaxSys], s_fc[kEobMaxSys];
     __shared__ double s_da[kEobMaxSys];
-    __shared__ int s_flag, s_active, s_ru, s_nact, s_anyru;
+    __shared__ int s_active, s_ru;   // the scalar step's counters (unused here)
     const int nsys = a.sys_count;
     for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
         const SysDev& S = a.sys[a.sys_first + q];
@@ -2932,6 +2953,12 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     __syncthreads();
     if (*(volatile int*)a.err) return;
     unsigned gen = 0;
+#ifdef YK_CG_TIMING
+    // block 0's cycles per round: coefficients, P1, barrier, P2+R2, barrier,
+    // P3+R3, barrier, P4, reduce
+    long long tacc[10] = {}, tlast = clock64();
+    int tit = 0;
+#endif
     constexpr int kAll = (1 << kStep) | (1 << kRedo) | (1 << kRu) | (1 << kWait);
     constexpr int kP1 = (1 << kStep) | (1 << kRedo) | (1 << kRu);
     constexpr int kP2 = (1 << kStep) | (1 << kRedo);
@@ -3172,7 +3199,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     pass_p3(kAll);
     if (!eob_barrier(a, gen)) return;
     pass_p4(kAll, true);
-    grid_reduce<true>(a, gen, 0, false, &s_flag, &s_active, &s_ru, red);
+    if (!eob_reduce(a, gen, 0, red, &s_active, &s_ru)) return;
 
     // Systems in kRu run their update in the passes of the round (R2 beside P2,
     // R3 beside P3); every system keeps its own iteration index (the
@@ -3180,10 +3207,15 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     int k = 1;
     const int kmax = 2 * a.max_iter + 2;
     while (k <= kmax) {
-        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, s_da, &s_nact, &s_anyru)) return;
-        if (s_nact == 0) break;
+        YK_TMARK(8);
+        int nact = 0;
+        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, s_da, &nact)) return;
+        if (nact == 0) break;
+        YK_TMARK(0);
         pass_p1(false);
+        YK_TMARK(1);
         if (!eob_barrier(a, gen)) return;
+        YK_TMARK(2);
         pass_p2(kP2);
         // R2: u = -A_o^-1 H^dag_oe chi_e (FP64, odd, t64)
         for_sites(kPR, [&](const SysDev& S, int, int m, int, bool, bool on) {
@@ -3199,7 +3231,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
             for (int e = 0; e < 4; ++e) h.v[e] *= sc;
             store_site<double, K>(S.t64, m, h);
         });
+        YK_TMARK(3);
         if (!eob_barrier(a, gen)) return;
+        YK_TMARK(4);
         pass_p3(kP2);
         // R3: r = rhs_e - (A_e chi_e + H^dag_eo u) in FP64; |r|^2, <r, p_{k-1}>
         for_sites(kPR, [&](const SysDev& S, int q, int m, int tile, bool tile_on, bool on) {
@@ -3229,11 +3263,24 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
             for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         });
+        YK_TMARK(5);
         if (!eob_barrier(a, gen)) return;
+        YK_TMARK(6);
         pass_p4(kP2, false);
-        grid_reduce<true>(a, gen, k, false, &s_flag, &s_active, &s_ru, red);
+        YK_TMARK(7);
+        if (!eob_reduce(a, gen, k, red, &s_active, &s_ru)) return;
         ++k;
+#ifdef YK_CG_TIMING
+        ++tit;
+#endif
     }
+#ifdef YK_CG_TIMING
+    if (blockIdx.x == 0 && threadIdx.x == 0 && tit > 0)
+        printf("eob timing (block 0 of %d, cycles per round over %d rounds): coefs %lld  P1 %lld  bar %lld  P2+R2 %lld  "
+               "bar %lld  P3+R3 %lld  bar %lld  P4 %lld  reduce %lld\n",
+               (int)gridDim.x, tit, tacc[0] / tit, tacc[1] / tit, tacc[2] / tit, tacc[3] / tit, tacc[4] / tit,
+               tacc[5] / tit, tacc[6] / tit, tacc[7] / tit, tacc[8] / tit);
+#endif
     // chi of both classes in the full layout (t64) for the force: chi_e, and
     // chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
     if (!eob_barrier(a, gen)) return;
