@@ -731,6 +731,9 @@ def main(argv=None):
                     help="only the Dirac apply on an L x L lattice (one JSON object; profiling runs)")
     ap.add_argument("--batching-only", action="store_true",
                     help="only the batching configuration (one JSON object; profiling runs)")
+    ap.add_argument("--batch-case", default="", metavar="L,CHAINS,RHS,STEPS",
+                    help="only STEPS steps of CHAINS chains of L x L with RHS right-hand sides, the batching "
+                         "configuration's couplings, autotuner off (one JSON object; profiling runs)")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip timing the reference's own CUDA kernels on the GPU")
     args = ap.parse_args(argv)
@@ -769,6 +772,26 @@ def main(argv=None):
         stream = torch.cuda.Stream()
         L = args.dirac_only
         print(json.dumps({"dirac_hbm": dirac_hbm(yk, torch, stream, Nt=L, Nx=L)}), flush=True)
+        return 0
+    if args.batch_case:
+        import numpy as np
+        import os as _os
+        _os.environ["YK_AUTOTUNE"] = "0"
+        import yukawacolourednoise_gb300 as yk
+        L, nch, nrhs, nsteps = (int(v) for v in args.batch_case.split(","))
+        rng = np.random.default_rng(1234)
+        ps = [yk.Params.default(use_mass=1, mass=-0.5, g=1.0, yukawa_coupling=float(rng.uniform(0.3, 0.8)),
+                                fermion_mass=float(rng.uniform(0.05, 0.3)), wilson_param=1.0, cut_fraction=CUT,
+                                Nt=L, Nx=L, fixed_dt=0.01, precision=yk.YK_MIXED, cg_tol=1e-10,
+                                cg_tol_mode=yk.YK_TOL_REL, cg_max_iter=20000, reliable_every=50, reliable_delta=0.001,
+                                n_rhs=nrhs, seed=1234, init=yk.YK_INIT_PHILOX) for _ in range(nch)]
+        with yk.Context(ps) as ctx:
+            ctx.step(nsteps)
+            ctx.synchronize()
+            obs = [ctx.observables(c) for c in range(nch)]
+        print(json.dumps({"batch_case": {"lattice": [L, L], "chains": nch, "rhs": nrhs, "steps": nsteps,
+                                         "cg_iterations_last_step": [o.cg_iterations for o in obs],
+                                         "status": [o.status for o in obs]}}), flush=True)
         return 0
     if args.batching_only:
         import torch

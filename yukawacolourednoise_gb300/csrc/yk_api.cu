@@ -701,7 +701,8 @@ int tune_overlap(yk_ctx* ctx)
 }
 
 // The autotuner.  Batched steps (several CG systems in one launch): the grid
-// of the persistent CG, i.e. how many tiles each block owns, by timing the
+// of the persistent CG (the batched even-odd kernel's, or how many tiles
+// each block of cg_kernel owns), by timing the
 // step's CG (sources of Philox kind 100, which no step draws; 48 iterations;
 // two launches after one warm-up) at each candidate: the co-resident maximum,
 // 3/4 and 1/2 of it, one block per SM and half of that.  Fewer blocks own
@@ -715,7 +716,7 @@ int run_autotune(yk_ctx* ctx)
     T = yk_tune_result{};
     const bool mixed = ctx->precision == YK_MIXED;
     if (ctx->nsys > 1 && !ctx->cg_cluster) {
-        const int maxg = cg_max_grid(1, mixed);
+        const int maxg = ctx->cg_eo ? cg_eob_max_grid() : cg_max_grid(1, mixed);
         std::vector<int> cand = {maxg, maxg * 3 / 4, maxg / 2, ctx->n_sm, ctx->n_sm / 2};
         std::sort(cand.begin(), cand.end(), std::greater<int>());
         cand.erase(std::unique(cand.begin(), cand.end()), cand.end());

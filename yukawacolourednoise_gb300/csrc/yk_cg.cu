@@ -3504,6 +3504,8 @@ static int halo_max_grid()
     return maxg;
 }
 
+int cg_eob_max_grid() { return eob_max_grid(); }
+
 void cg_halo_init()
 {
     halo_max_grid();

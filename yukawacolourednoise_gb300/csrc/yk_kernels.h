@@ -25,6 +25,7 @@ cudaError_t launch_cg(const CGArgs& a, int K, bool mixed, cudaStream_t stream, i
 cudaError_t launch_cg_balance(const CGArgs& a, int grid, int* out, cudaStream_t stream);
 // Largest co-resident grid of the CG kernel (cached; call before capturing).
 int cg_max_grid(int K, bool mixed);
+int cg_eob_max_grid();   // co-resident blocks of the batched even-odd CG
 // Kernel attributes and occupancy of the halo CG kernel (call before any stream capture).
 void cg_halo_init();
 // Runs the wait-timeout probe kernel on `stream`; *status = the device status
