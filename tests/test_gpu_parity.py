@@ -330,14 +330,17 @@ def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
         assert ctx.observables().status == 0
 
 
+@pytest.mark.parametrize("patch", ["1", "0"], ids=["patches", "rows"])
 @pytest.mark.parametrize("Nt,Nx", [(32, 32), (256, 256), (64, 128), (128, 64), (48, 32)])
-def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx):
+def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx, patch):
     # the even-odd Schur-complement solve of the step (CGNE on S S^dag, its
     # residual the true residual of D^dag chi = eta, the same rule relative to
     # |eta|) against the FP64 oracle's CG on D^dag D: the fields of three steps
-    # within 1e-8, in fewer iterations than the halo kernel's D^dag D solve
+    # within 1e-8, in fewer iterations than the halo kernel's D^dag D solve;
+    # blocks owning 16 x 16 patches of the compact lattice, or rows of it
     yk = ylib
     monkeypatch.setenv("YK_CG_EO", "1")
+    monkeypatch.setenv("YK_CG_EO_PATCH", patch)
     p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01, reliable_every=50)
     with yk.Context(p) as ctx:
         phi = ctx.get_field()
@@ -459,8 +462,8 @@ def test_batched_block_ranges_keep_results(ylib, cuda, monkeypatch, balance):
     ([(40, 24, 0.1, 0.5, S_HALF_PI, 2), (8, 8, 0.25, 0.3, 0.2, 1), (64, 64, 0.05, 0.8, 1.0, 3)], 4),
     # one odd lattice: the whole batch keeps the D^dag D grid kernel
     ([(40, 24, 0.1, 0.5, S_HALF_PI, 2), (9, 8, 0.25, 0.3, 1.0, 1)], 0),
-    # a single lattice too wide for the halo kernel's shared memory
-    ([(16, 1024, 0.1, 0.5, S_HALF_PI, 1)], 4),
+    # a single lattice neither 16 x 16 patches nor whole rows fit (18 rows)
+    ([(18, 1000, 0.1, 0.5, 1.0, 1)], 4),
 ], ids=["even_batch", "odd_lattice", "single_wide"])
 def test_batched_even_odd_cg(ylib, cuda, specs, kernel):
     # the step's solves of every chain and right-hand side through one

@@ -2283,6 +2283,10 @@ static size_t halo_smem_bytes(int own, int Nx)
 // with the one reducing grid barrier per iteration, the scalar steps and the
 // FP64 reliable updates of cg_halo_kernel (its tile partials: |r|^2, |q|^2,
 // |v|^2 in the <p, Ap> slot, <r, q>).
+// cg_eo_kernel<true> owns 16 x 16 patches of the compact lattice instead of
+// whole rows: the widened patch (24 x 20 cells) holds 480 sites against
+// 1280 for two rows of 128 widened by four rows on each side, and the w, v,
+// u passes compute 1200 sites against 2304 (one partial slot per patch).
 
 // Row, x-parity bit and the compact offsets of the x neighbours (opposite
 // class) of compact site m of parity q.
@@ -2316,6 +2320,16 @@ __device__ __forceinline__ Site<double, 1> eo_gl(const double* in, int m, int Ve
                                          sp, sm);
 }
 
+// Patch geometry of cg_eo_kernel<true>: each block owns kPT rows x kPX compact
+// columns and stages them widened by 4 rows and 2 compact columns (the reach
+// of the four half hops: two compact columns, since consecutive x hops
+// alternate between the compact index's two parities).  Cells at the
+// buffer's column edges get values no own q depends on; their x neighbours
+// stay inside the buffer (the rows of w, v, u exclude the first and last).
+constexpr int kPT = 16, kPX = 16;
+constexpr int kSW = kPX + 4, kSR = kPT + 8, kSN = kSW * kSR;
+
+template <bool PATCH>
 __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
 {
     constexpr int K = 1;
@@ -2340,6 +2354,24 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
     if (*(volatile int*)a.err) return;
+    if constexpr (PATCH) {
+        // the neighbour patches (one hop in t or x) replace the row ranges' neighbours
+        if (threadIdx.x == 0) {
+            const SysDev& V0 = a.sys[a.sys_first];
+            const int npx = V0.Nx / kPX, npt = V0.Nt / kPT;
+            const int pt = blockIdx.x / npx, px = blockIdx.x % npx;
+            const int nb[4] = {((pt + 1) % npt) * npx + px, ((pt + npt - 1) % npt) * npx + px,
+                               pt * npx + (px + 1) % npx, pt * npx + (px + npx - 1) % npx};
+            int n = 0;
+            for (int i = 0; i < 4; ++i) {
+                bool seen = nb[i] == (int)blockIdx.x;
+                for (int j = 0; j < n && !seen; ++j) seen = deps.b[j] == nb[i];
+                if (!seen) deps.b[n++] = nb[i];
+            }
+            deps.n = n;
+            deps.all = 0;
+        }
+    }
     if (threadIdx.x == 0) {
         s_fast = 0;
         lst.rr = lst.rr0 = lst.rr_prev = lst.stop2 = lst.rmax2 = 0.0;
@@ -2354,34 +2386,79 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     __syncthreads();
     const int Nt = S.Nt, Nh = S.Nx, Ve = S.V;
     const int sh = (Nh & (Nh - 1)) == 0 ? __ffs(Nh) - 1 : -1;
-    const int c0 = a.tiles[tb].y;
-    const int c1 = min(a.tiles[te - 1].y + kTile, Ve);
-    const int own = c1 - c0;
-    const int nP = own + 8 * Nh;
-    const int cbase = c0 - 4 * Nh;                 // compact site of buffer index 0
-    const int pfirst = wrap_site(cbase, Ve);
-    float4* P_st = hsm;                            // p on [0, nP)
-    float4* R_st = P_st + nP;                      // r there
-    float4* A_st = R_st + nP;                      // q there
-    float4* X_st = A_st + nP;                      // chi_e increment on the own sites
+    // The staged buffer: rows (PATCH: the kPT x kPX patch at (t0, i0) widened
+    // by 4 rows and 2 compact columns, row stride kSW, wrapped while staging;
+    // else the compact range [c0, c0 + own) widened by 4 rows, stride Nh).
+    // Stencils in the buffer step by +-SB in t and by the x offsets of cell().
+    int c0 = 0, own, t0 = 0, i0 = 0, SB, NB, cbase = 0;
+    if constexpr (PATCH) {
+        const int npx = Nh / kPX;
+        t0 = (blockIdx.x / npx) * kPT;
+        i0 = (blockIdx.x % npx) * kPX;
+        own = kPT * kPX;
+        SB = kSW;
+        NB = kSN;
+    } else {
+        c0 = a.tiles[tb].y;
+        own = min(a.tiles[te - 1].y + kTile, Ve) - c0;
+        SB = Nh;
+        NB = own + 8 * Nh;
+        cbase = c0 - 4 * Nh;                       // compact site of buffer index 0
+    }
+    const int pfirst = PATCH ? 0 : wrap_site(cbase, Ve);
+    // compact site of buffer cell j
+    auto buf_m = [&](int j) -> int {
+        if constexpr (PATCH) {
+            const int r = j / kSW, c = j - r * kSW;
+            int t = t0 - 4 + r, i = i0 - 2 + c;
+            t = t < 0 ? t + Nt : (t >= Nt ? t - Nt : t);
+            i = i < 0 ? i + Nh : (i >= Nh ? i - Nh : i);
+            return t * Nh + i;
+        } else {
+            return wrap_site(pfirst + j, Ve);
+        }
+    };
+    // row, x parity bit and buffer x offsets of cell j's site of class q
+    auto cell = [&](int j, int q, int& t, int& b, int& du, int& dd) {
+        if constexpr (PATCH) {
+            const int r = j / kSW;
+            t = t0 - 4 + r;
+            t = t < 0 ? t + Nt : (t >= Nt ? t - Nt : t);
+            b = (t + q) & 1;
+            du = b;
+            dd = b - 1;
+        } else {
+            eo_geom(wrap_site(pfirst + j, Ve), q, Nh, sh, t, b, du, dd);
+        }
+    };
+    auto own_j = [&](int o) -> int { return PATCH ? (4 + o / kPX) * kSW + 2 + o % kPX : 4 * Nh + o; };
+    auto own_m = [&](int o) -> int { return PATCH ? (t0 + o / kPX) * Nh + i0 + o % kPX : c0 + o; };
+    // own index of buffer cell j, or -1
+    auto own_of = [&](int j) -> int {
+        if constexpr (PATCH) {
+            const int r = j / kSW - 4, c = j % kSW - 2;
+            return (r >= 0 && r < kPT && c >= 0 && c < kPX) ? r * kPX + c : -1;
+        } else {
+            const int o = j - 4 * Nh;
+            return (o >= 0 && o < own) ? o : -1;
+        }
+    };
+    float4* P_st = hsm;                            // p on [0, NB)
+    float4* R_st = P_st + NB;                      // r there
+    float4* A_st = R_st + NB;                      // q there
+    float4* X_st = A_st + NB;                      // chi_e increment on the own sites
     float4* V_own = X_st + own;                    // v of the previous iteration on the own sites
-    float4* W_b = V_own + own;                     // w on [Nh, own + 7Nh), later u on [3Nh, own + 5Nh)
-    float4* V_b = W_b + (own + 6 * Nh);            // v on [2Nh, own + 6Nh)
-    float* de_b = reinterpret_cast<float*>(V_b + (own + 4 * Nh));   // A_e on [2Nh, own + 6Nh)
-    float* di_b = de_b + (own + 4 * Nh);                            // 1 / A_o on [Nh, own + 7Nh)
-    float4* Wp = W_b - Nh;                         // buffer-index views
-    float4* Vp = V_b - 2 * Nh;
-    const float* dep = de_b - 2 * Nh;
-    const float* dip = di_b - Nh;
+    float4* Wp = V_own + own;                      // w on [SB, NB - SB), later u on [3SB, NB - 3SB)
+    float4* Vp = Wp + NB;                          // v on [2SB, NB - 2SB)
+    float* dep = reinterpret_cast<float*>(Vp + NB);   // A_e on [2SB, NB - 2SB)
+    float* dip = dep + NB;                             // 1 / A_o on [SB, NB - SB)
     const float rw = (float)S.r;
     const double r64 = S.r;
-    auto diag_at = [&](int m, int q) -> double {
+    for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += kHaloThreads) {
         int t, b, du, dd;
-        eo_geom(m, q, Nh, sh, t, b, du, dd);
-        return 2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b];
-    };
-    for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads)
-        de_b[j - 2 * Nh] = (float)diag_at(wrap_site(cbase + j, Ve), 0);
+        cell(j, 0, t, b, du, dd);
+        dep[j] = (float)(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * buf_m(j) + b]);
+    }
     const double* rhs_e = S.x + 4 * (size_t)Ve;    // after chi_e (compact FP64)
     unsigned epoch = 0, gen = 0;
     int staged_k = -1;
@@ -2396,8 +2473,8 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
         const float* Pl = S.p32[prv];
         const float* Al = prv == 0 ? S.Ap32 : S.t32;
-        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
-            const int m = wrap_site(pfirst + j, Ve);
+        for (int j = threadIdx.x; j < NB; j += kHaloThreads) {
+            const int m = buf_m(j);
             cp_async16(P_st + j, Pl + 4 * (size_t)m);
             cp_async16(R_st + j, Rl + 4 * (size_t)m);
             if (mode == kStep) cp_async16(A_st + j, Al + 4 * (size_t)m);
@@ -2405,14 +2482,14 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         cp_async_commit();
     };
 
-    // A1: p_k (r_k and the chi_e increment on the own sites) on [0, nP)
+    // A1: p_k (r_k and the chi_e increment on the own sites) on [0, NB)
     auto pass_a1 = [&](int mode, int cur, int prv) {
         const SysLocal& L = sl[0];
         const W ar = L.f_alpha_re, beta = L.f_beta, cre = L.f_c_re, cim = L.f_c_im;
-        for (int j = threadIdx.x; j < nP; j += kHaloThreads) {
-            const int o = j - 4 * Nh;
-            const bool is_own = o >= 0 && o < own;
-            const int m = c0 + o;
+        for (int j = threadIdx.x; j < NB; j += kHaloThreads) {
+            const int o = own_of(j);
+            const bool is_own = o >= 0;
+            const int m = is_own ? own_m(o) : 0;
             const Site<W, K> po = ld_sm(P_st, j);
             Site<W, K> p;
             if (mode == kStep) {
@@ -2443,32 +2520,32 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         Site<W, K> zero;
 #pragma unroll
         for (int i = 0; i < 4; ++i) zero.v[i] = W(0);
-        for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads) {
+        for (int j = SB + threadIdx.x; j < NB - SB; j += kHaloThreads) {
             int t, b, du, dd;
-            eo_geom(wrap_site(cbase + j, Ve), 1, Nh, sh, t, b, du, dd);
+            cell(j, 1, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
-            Site<W, K> h = eo_sm<false>(P_st, j, Nh, du, dd, zero, W(0), rw, sp, sm);
+            Site<W, K> h = eo_sm<false>(P_st, j, SB, du, dd, zero, W(0), rw, sp, sm);
             const W s = -dip[j];
 #pragma unroll
             for (int i = 0; i < 4; ++i) h.v[i] *= s;
             st_sm(Wp, j, h);
         }
         __syncthreads();
-        for (int j = 2 * Nh + threadIdx.x; j < own + 6 * Nh; j += kHaloThreads) {
+        for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += kHaloThreads) {
             int t, b, du, dd;
-            eo_geom(wrap_site(cbase + j, Ve), 0, Nh, sh, t, b, du, dd);
+            cell(j, 0, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
-            const Site<W, K> v = eo_sm<false>(Wp, j, Nh, du, dd, ld_sm(P_st, j), dep[j], rw, sp, sm);
+            const Site<W, K> v = eo_sm<false>(Wp, j, SB, du, dd, ld_sm(P_st, j), dep[j], rw, sp, sm);
             st_sm(Vp, j, v);
-            const int o = j - 4 * Nh;
-            if (o >= 0 && o < own) st_sm(V_own, o, v);
+            const int o = own_of(j);
+            if (o >= 0) st_sm(V_own, o, v);
         }
         __syncthreads();
-        for (int j = 3 * Nh + threadIdx.x; j < own + 5 * Nh; j += kHaloThreads) {
+        for (int j = 3 * SB + threadIdx.x; j < NB - 3 * SB; j += kHaloThreads) {
             int t, b, du, dd;
-            eo_geom(wrap_site(cbase + j, Ve), 1, Nh, sh, t, b, du, dd);
+            cell(j, 1, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
-            Site<W, K> h = eo_sm<true>(Vp, j, Nh, du, dd, zero, W(0), rw, sp, sm);
+            Site<W, K> h = eo_sm<true>(Vp, j, SB, du, dd, zero, W(0), rw, sp, sm);
             const W s = -dip[j];
 #pragma unroll
             for (int i = 0; i < 4; ++i) h.v[i] *= s;
@@ -2483,18 +2560,19 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         for (int base = tb; base < te; base += 2) {
             const int tile = base + hf;
             const bool tile_on = tile < te;
-            const int m = tile_on ? c0 + (tile - tb) * kTile + ts : Ve;
-            const bool on = m < Ve;
+            const int o = (tile - tb) * kTile + ts;
+            const bool on = tile_on && o < own;
+            const int m = on ? own_m(o) : 0;
             FF f[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
             if (on) {
-                const int j = m - cbase;
+                const int j = own_j(o);
                 int t, b, du, dd;
-                eo_geom(m, 0, Nh, sh, t, b, du, dd);
+                cell(j, 0, t, b, du, dd);
                 const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
                 const Site<W, K> v = ld_sm(Vp, j);
-                const Site<W, K> q = eo_sm<true>(Wp, j, Nh, du, dd, v, dep[j], rw, sp, sm);
+                const Site<W, K> q = eo_sm<true>(Wp, j, SB, du, dd, v, dep[j], rw, sp, sm);
                 YK_ST(W, K, Ac, m, q);
                 const Site<W, K> r = ld_sm(R_st, j);
                 W rq, dummy;
@@ -2537,7 +2615,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         const SysLocal& L = sl[0];
         double* chi = S.x;
         for (int o = threadIdx.x; o < own; o += kHaloThreads) {
-            const int m = c0 + o;
+            const int m = own_m(o);
             Site<double, K> xv = load_site<double, K>(chi, m);
             const Site<W, K> xs = ld_sm(X_st, o);
             const Site<W, K> vv = ld_sm(V_own, o);
@@ -2558,7 +2636,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
 #pragma unroll
         for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
         for (int o = threadIdx.x; o < own; o += kHaloThreads) {
-            const int m = c0 + o;
+            const int m = own_m(o);
             int t, b, du, dd;
             eo_geom(m, 1, Nh, sh, t, b, du, dd);
             const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
@@ -2574,8 +2652,9 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         for (int base = tb; base < te; base += 2) {
             const int tile = base + hf;
             const bool tile_on = tile < te;
-            const int m = tile_on ? c0 + (tile - tb) * kTile + ts : Ve;
-            const bool on = m < Ve;
+            const int o = (tile - tb) * kTile + ts;
+            const bool on = tile_on && o < own;
+            const int m = on ? own_m(o) : 0;
             double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
             if (on) {
                 int t, b, du, dd;
@@ -2612,7 +2691,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     // per site of the solve) and -A_o^-1 eta_o (t64, compact); chi_e = 0;
     // rhs_e; r_0 = p_0 = rhs_e
     for (int o = threadIdx.x; o < 2 * own; o += kHaloThreads) {
-        const int m = c0 + (o >> 1), q = o & 1;
+        const int m = own_m(o >> 1), q = o & 1;
         int t, b, du, dd;
         eo_geom(m, q, Nh, sh, t, b, du, dd);
         const int n = 2 * m + b;   // the compact index's full site of class q
@@ -2636,17 +2715,16 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             z.v[i] = 0.0;
             zw.v[i] = W(0);
         }
-        store_site<double, K>(S.x, c0 + o, z);
+        store_site<double, K>(S.x, own_m(o), z);
         st_sm(X_st, o, zw);
         st_sm(V_own, o, zw);
     }
     if (!nsync(a, ++epoch, deps)) return;
     YK_TMARK(13);
     // 1 / A_o in FP32 on the widened range, from the owners' dinv
-    for (int j = Nh + threadIdx.x; j < own + 7 * Nh; j += kHaloThreads)
-        di_b[j - Nh] = (float)S.dinv[wrap_site(cbase + j, Ve)];
+    for (int j = SB + threadIdx.x; j < NB - SB; j += kHaloThreads) dip[j] = (float)S.dinv[buf_m(j)];
     for (int o = threadIdx.x; o < own; o += kHaloThreads) {
-        const int m = c0 + o;
+        const int m = own_m(o);
         int t, b, du, dd;
         eo_geom(m, 0, Nh, sh, t, b, du, dd);
         const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
@@ -2719,7 +2797,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
 #pragma unroll
     for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
     for (int o = threadIdx.x; o < own; o += kHaloThreads) {
-        const int m = c0 + o;
+        const int m = own_m(o);
         int t, b, du, dd;
         eo_geom(m, 0, Nh, sh, t, b, du, dd);
         store_site<double, K>(SF.t64, 2 * m + b, load_site<double, K>(S.x, m));
@@ -3307,13 +3385,12 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
 }
 
 
-// Shared memory of cg_eo_kernel for own compact sites per block and Nh.
-static size_t eo_smem_bytes(int own, int Nh)
+// Shared memory of cg_eo_kernel for `own` compact sites per block and a
+// staged buffer of nb cells: p, r, q, w (then u) and v on the buffer, the chi
+// increment and v on the own sites, A_e and 1 / A_o in FP32 on the buffer.
+static size_t eo_smem_bytes(int own, int nb)
 {
-    const size_t nP = (size_t)own + 8 * (size_t)Nh;
-    const size_t f4 = 3 * nP + 2 * (size_t)own + ((size_t)own + 6 * Nh) + ((size_t)own + 4 * Nh);
-    const size_t fl = ((size_t)own + 4 * Nh) + ((size_t)own + 6 * Nh);
-    return f4 * sizeof(float4) + fl * sizeof(float);
+    return (5 * (size_t)nb + 2 * (size_t)own) * sizeof(float4) + 2 * (size_t)nb * sizeof(float);
 }
 
 // Failure detection without a fault: block 0 waits through nsync on block
@@ -3458,20 +3535,48 @@ static bool eo_takes(int Nt, int Nx, int tpb, size_t* smem)
     if (Nt < 2 || Nx < 4 || (Nt & 1) || (Nx & 1) || tpb < 1 || tpb > 8) return false;
     const long long own = (long long)tpb * kTile, Nh = Nx / 2, Ve = (long long)Nt * Nh;
     if (own + 8 * Nh > Ve) return false;
-    *smem = eo_smem_bytes((int)own, (int)Nh);
+    *smem = eo_smem_bytes((int)own, (int)(own + 8 * Nh));
     return *smem <= kHaloMaxSmem;
+}
+
+// Whether cg_eo_kernel<true> takes it: kPT x kPX patches tile the compact
+// lattice, one block per patch.
+static bool eo_patch_takes(int Nt, int Nx, int* patches, size_t* smem)
+{
+    if (Nt < kPT || Nx < 2 * kPX || (Nt % kPT) || (Nx % (2 * kPX))) return false;
+    *patches = (Nt / kPT) * (Nx / (2 * kPX));
+    *smem = eo_smem_bytes(kPT * kPX, kSN);
+    return true;
 }
 
 static int eo_max_grid()
 {
     static int maxg = -1;
     if (maxg < 0) {
-        cudaFuncSetAttribute((const void*)cg_eo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHaloMaxSmem);
+        cudaFuncSetAttribute((const void*)cg_eo_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kHaloMaxSmem);
         int dev = 0, nsm = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel, kHaloThreads, kHaloMaxSmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<false>, kHaloThreads,
+                                                      kHaloMaxSmem);
         maxg = per * nsm;
+    }
+    return maxg;
+}
+
+static int eo_patch_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        const int smem = (int)eo_smem_bytes(kPT * kPX, kSN);
+        cudaFuncSetAttribute((const void*)cg_eo_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<true>, kHaloThreads, smem);
+        maxg = per * nsm;
+        if (maxg > kMaxGrid) maxg = kMaxGrid;
     }
     return maxg;
 }
@@ -3510,6 +3615,7 @@ void cg_halo_init()
 {
     halo_max_grid();
     eo_max_grid();
+    eo_patch_max_grid();
     eob_max_grid();
 }
 
@@ -3551,6 +3657,30 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
             int etpb = 1;
             const int eg = cg_grid_for(e.tile_end - e.tile_begin, capped(eo_max_grid(), a.grid_cap), &etpb);
             size_t es = 0;
+            // patches first (less halo work per block), then rows of the lattice
+            const char* pe = getenv("YK_CG_EO_PATCH");
+            int np = 0;
+            if (a.sys_count == 1 && !(pe && pe[0] == '0') && eo_patch_takes(a.solo_nt, a.solo_nx, &np, &es) &&
+                np <= eo_patch_max_grid() && e.tile_begin + np <= e.tile_end) {
+                e.tile_end = e.tile_begin + np;   // one partial slot per patch
+                e.tiles_per_block = 1;
+                e.grid = np;
+                if (grid_out) *grid_out = np;
+                if (kernel_out) *kernel_out = 3;
+                cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(np);
+                cfg.blockDim = dim3(kHaloThreads);
+                cfg.dynamicSmemBytes = es;
+                cfg.stream = stream;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeCooperative;
+                attr[0].val.cooperative = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                void* args[] = {&e};
+                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel<true>, args);
+            }
             if (a.sys_count == 1 && eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, etpb, &es)) {
                 e.tiles_per_block = etpb;
                 e.grid = eg;
@@ -3568,7 +3698,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 cfg.attrs = attr;
                 cfg.numAttrs = 1;
                 void* args[] = {&e};
-                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel, args);
+                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel<false>, args);
             }
             // the batched even-odd kernel: work dealt out per pass, so the
             // grid does not follow the tiles (at most one block per two tiles)
