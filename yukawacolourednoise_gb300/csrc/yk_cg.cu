@@ -2355,19 +2355,21 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
     if (*(volatile int*)a.err) return;
     if constexpr (PATCH) {
-        // the neighbour patches (one hop in t or x) replace the row ranges' neighbours
+        // the eight patches around this one replace the row ranges' neighbours:
+        // the widened patch staged after round 0's last neighbour sync reaches
+        // into the diagonal ones too
         if (threadIdx.x == 0) {
             const SysDev& V0 = a.sys[a.sys_first];
             const int npx = V0.Nx / kPX, npt = V0.Nt / kPT;
             const int pt = blockIdx.x / npx, px = blockIdx.x % npx;
-            const int nb[4] = {((pt + 1) % npt) * npx + px, ((pt + npt - 1) % npt) * npx + px,
-                               pt * npx + (px + 1) % npx, pt * npx + (px + npx - 1) % npx};
             int n = 0;
-            for (int i = 0; i < 4; ++i) {
-                bool seen = nb[i] == (int)blockIdx.x;
-                for (int j = 0; j < n && !seen; ++j) seen = deps.b[j] == nb[i];
-                if (!seen) deps.b[n++] = nb[i];
-            }
+            for (int dt = -1; dt <= 1; ++dt)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int nb = ((pt + dt + npt) % npt) * npx + (px + dx + npx) % npx;
+                    bool seen = nb == (int)blockIdx.x;
+                    for (int j = 0; j < n && !seen; ++j) seen = deps.b[j] == nb;
+                    if (!seen) deps.b[n++] = nb;
+                }
             deps.n = n;
             deps.all = 0;
         }
@@ -3628,6 +3630,27 @@ int cg_predict_grid(const CGArgs& a, bool mixed)
                        capped(mixed ? max_grid_t<1, true>() : max_grid_t<1, false>(), a.grid_cap), &tpb);
 }
 
+// The single-system even-odd kernel launch_cg takes for `a` (mixed, K = 1):
+// 2 patches (*grid blocks), 1 rows (*grid blocks of *tpb tiles), 0 neither.
+static int eo_single_variant(const CGArgs& a, int* grid, int* tpb, size_t* smem)
+{
+    if (!(a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr && a.sys_count == 1)) return 0;
+    const char* pe = getenv("YK_CG_EO_PATCH");
+    int np = 0;
+    if (!(pe && pe[0] == '0') && eo_patch_takes(a.solo_nt, a.solo_nx, &np, smem) && np <= eo_patch_max_grid() &&
+        a.eo_tile_begin + np <= a.eo_tile_end) {
+        *grid = np;
+        *tpb = 1;
+        return 2;
+    }
+    const int eg = cg_grid_for(a.eo_tile_end - a.eo_tile_begin, capped(eo_max_grid(), a.grid_cap), tpb);
+    if (eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, *tpb, smem)) {
+        *grid = eg;
+        return 1;
+    }
+    return 0;
+}
+
 template <int K, bool MIXED>
 static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_out, int* kernel_out)
 {
@@ -3654,34 +3677,12 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
             e.tile_begin = a.eo_tile_begin;
             e.tile_end = a.eo_tile_end;
             e.eo = 1;
-            int etpb = 1;
-            const int eg = cg_grid_for(e.tile_end - e.tile_begin, capped(eo_max_grid(), a.grid_cap), &etpb);
-            size_t es = 0;
             // patches first (less halo work per block), then rows of the lattice
-            const char* pe = getenv("YK_CG_EO_PATCH");
-            int np = 0;
-            if (a.sys_count == 1 && !(pe && pe[0] == '0') && eo_patch_takes(a.solo_nt, a.solo_nx, &np, &es) &&
-                np <= eo_patch_max_grid() && e.tile_begin + np <= e.tile_end) {
-                e.tile_end = e.tile_begin + np;   // one partial slot per patch
-                e.tiles_per_block = 1;
-                e.grid = np;
-                if (grid_out) *grid_out = np;
-                if (kernel_out) *kernel_out = 3;
-                cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3(np);
-                cfg.blockDim = dim3(kHaloThreads);
-                cfg.dynamicSmemBytes = es;
-                cfg.stream = stream;
-                cudaLaunchAttribute attr[1];
-                attr[0].id = cudaLaunchAttributeCooperative;
-                attr[0].val.cooperative = 1;
-                cfg.attrs = attr;
-                cfg.numAttrs = 1;
-                void* args[] = {&e};
-                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel<true>, args);
-            }
-            if (a.sys_count == 1 && eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, etpb, &es)) {
+            int eg = 0, etpb = 1;
+            size_t es = 0;
+            const int var = eo_single_variant(a, &eg, &etpb, &es);
+            if (var != 0) {
+                if (var == 2) e.tile_end = e.tile_begin + eg;   // one partial slot per patch
                 e.tiles_per_block = etpb;
                 e.grid = eg;
                 if (grid_out) *grid_out = eg;
@@ -3698,7 +3699,8 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 cfg.attrs = attr;
                 cfg.numAttrs = 1;
                 void* args[] = {&e};
-                return cudaLaunchKernelExC(&cfg, (const void*)cg_eo_kernel<false>, args);
+                return cudaLaunchKernelExC(&cfg, var == 2 ? (const void*)cg_eo_kernel<true> : (const void*)cg_eo_kernel<false>,
+                                           args);
             }
             // the batched even-odd kernel: work dealt out per pass, so the
             // grid does not follow the tiles (at most one block per two tiles)

@@ -453,4 +453,32 @@ __device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned lo
     if (threadIdx.x == 0 && s_max) atomicMax(word, s_max);
 }
 
+// The step's drift at site n of chain C given the fermion force F: F plus
+// the bosonic drift phi (m^2 + lambda/6 phi^2) - Lap phi of
+// langevin_gpu_v2.cu:9-27, the Laplacian summed over its five columns in
+// ascending site order (the reference's CSR rows).
+__device__ __forceinline__ void cswap(int& a, int& b)
+{
+    const int lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+__device__ __forceinline__ double step_drift(const ChainDev& C, int n, double F)
+{
+    const Nbr nb = neighbours(n, C.Nt, C.Nx);
+    const double v = C.phi[n];
+    double d = F;
+    d += v * (C.m2 + (C.lambda / 6.0) * (v * v));
+    int col[5] = {n, (int)nb.tu, (int)nb.td, (int)nb.xu, (int)nb.xd};
+    // 5-input sorting network (9 comparators)
+    cswap(col[0], col[1]); cswap(col[3], col[4]); cswap(col[2], col[4]);
+    cswap(col[2], col[3]); cswap(col[0], col[3]); cswap(col[0], col[2]);
+    cswap(col[1], col[4]); cswap(col[1], col[3]); cswap(col[1], col[2]);
+    double lap = 0.0;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) lap += (col[q] != n ? 1.0 : -4.0) * C.phi[col[q]];
+    return d - lap;
+}
+
 }  // namespace yk

@@ -24,13 +24,6 @@
 
 namespace yk {
 
-__device__ __forceinline__ void cswap(int& a, int& b)
-{
-    const int lo = min(a, b), hi = max(a, b);
-    a = lo;
-    b = hi;
-}
-
 template <int K>
 __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const SysDev* __restrict__ sys,
                                                             const CGState* __restrict__ st, int mode)
@@ -74,18 +67,7 @@ __global__ void __launch_bounds__(kTile) force_drift_kernel(StepArgs s, const Sy
             if (C.n_rhs > 1) F /= (double)C.n_rhs;
         }
         if (mode != 1) {
-            const double v = C.phi[n];
-            d = F;
-            d += v * (C.m2 + (C.lambda / 6.0) * (v * v));
-            int col[5] = {n, (int)nb.tu, (int)nb.td, (int)nb.xu, (int)nb.xd};
-            // 5-input sorting network (9 comparators)
-            cswap(col[0], col[1]); cswap(col[3], col[4]); cswap(col[2], col[4]);
-            cswap(col[2], col[3]); cswap(col[0], col[3]); cswap(col[0], col[2]);
-            cswap(col[1], col[4]); cswap(col[1], col[3]); cswap(col[1], col[2]);
-            double lap = 0.0;
-#pragma unroll
-            for (int q = 0; q < 5; ++q) lap += (col[q] != n ? 1.0 : -4.0) * C.phi[col[q]];
-            d -= lap;
+            d = step_drift(C, n, F);
             C.drift[n] = d;
         } else {
             d = F;
