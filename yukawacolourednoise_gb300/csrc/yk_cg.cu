@@ -1274,6 +1274,13 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
                         }
                     }
                     s_dec = ok ? (done ? 2 : 1) : 0;
+                    if (done) {
+                        // the block's state for the next pass, before the
+                        // barrier that publishes the step
+                        *s_nact = 1;
+                        *s_anyru = lst.mode == kRu;
+                        *s_fast = s_scales == 2 ? 1 : 0;
+                    }
                     YK_QMARK(5);
                 }
             }
@@ -1281,6 +1288,13 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
             __syncthreads();
             fast = s_dec != 0;
             stepped = s_dec == 2;
+            if (stepped) {
+                YK_QMARK(6);
+#ifdef YK_CG_TIMING
+                if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&g_cg_f[3], 1ull);
+#endif
+                return true;   // coefficients, mode and counts published by the barrier above
+            }
         }
     }
     if (!fast) sum_partials<MIXED>(a, a.tile_begin, a.tile_end - a.tile_begin, red, s);
