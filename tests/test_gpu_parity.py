@@ -330,14 +330,14 @@ def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
         assert ctx.observables().status == 0
 
 
-@pytest.mark.parametrize("patch", ["1", "0"], ids=["patches", "rows"])
+@pytest.mark.parametrize("patch", ["16", "8", "0"], ids=["patches16", "patches8", "rows"])
 @pytest.mark.parametrize("Nt,Nx", [(32, 32), (256, 256), (64, 128), (128, 64), (48, 32)])
 def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx, patch):
     # the even-odd Schur-complement solve of the step (CGNE on S S^dag, its
     # residual the true residual of D^dag chi = eta, the same rule relative to
     # |eta|) against the FP64 oracle's CG on D^dag D: the fields of three steps
     # within 1e-8, in fewer iterations than the halo kernel's D^dag D solve;
-    # blocks owning 16 x 16 patches of the compact lattice, or rows of it
+    # blocks owning 16 x 16 or 16 x 8 patches of the compact lattice, or rows
     yk = ylib
     monkeypatch.setenv("YK_CG_EO", "1")
     monkeypatch.setenv("YK_CG_EO_PATCH", patch)

@@ -2334,18 +2334,26 @@ __device__ __forceinline__ Site<double, 1> eo_gl(const double* in, int m, int Ve
                                          sp, sm);
 }
 
-// Patch geometry of cg_eo_kernel<true>: each block owns kPT rows x kPX compact
-// columns and stages them widened by 4 rows and 2 compact columns (the reach
-// of the four half hops: two compact columns, since consecutive x hops
-// alternate between the compact index's two parities).  Cells at the
+// Patch geometry of cg_eo_kernel<PX> (PX > 0): each block owns kPT rows x PX
+// compact columns and stages them widened by 4 rows and 2 compact columns
+// (the reach of the four half hops: two compact columns, since consecutive x
+// hops alternate between the compact index's two parities).  Cells at the
 // buffer's column edges get values no own q depends on; their x neighbours
 // stay inside the buffer (the rows of w, v, u exclude the first and last).
-constexpr int kPT = 16, kPX = 16;
-constexpr int kSW = kPX + 4, kSR = kPT + 8, kSN = kSW * kSR;
+// PX = 16: 512-thread blocks, one per SM; PX = 8: 256-thread blocks, two per
+// SM, so that one block's barrier waits overlap the other's passes.  PX = 0:
+// whole rows (cg_eo_kernel's first form).
+constexpr int kPT = 16, kSR = kPT + 8;
+__host__ __device__ constexpr int eo_threads(int PX) { return PX == 8 ? 256 : kHaloThreads; }
+__host__ __device__ constexpr int eo_sw(int PX) { return (PX > 0 ? PX : 16) + 4; }
 
-template <bool PATCH>
-__global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
+template <int PX>
+__global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
 {
+    constexpr bool PATCH = PX > 0;
+    constexpr int kPX = PATCH ? PX : 16;
+    constexpr int kSW = eo_sw(PX), kSN = kSW * kSR;
+    constexpr int NT = eo_threads(PX);
     constexpr int K = 1;
     constexpr int kSkipIm = (1 << 3) | (1 << 5);
     using W = float;
@@ -2470,7 +2478,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     float* dip = dep + NB;                             // 1 / A_o on [SB, NB - SB)
     const float rw = (float)S.r;
     const double r64 = S.r;
-    for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += kHaloThreads) {
+    for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += NT) {
         int t, b, du, dd;
         cell(j, 0, t, b, du, dd);
         dep[j] = (float)(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * buf_m(j) + b]);
@@ -2489,7 +2497,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         const float* Rl = (mode == kRedo) ? S.r32[cur] : S.r32[prv];
         const float* Pl = S.p32[prv];
         const float* Al = prv == 0 ? S.Ap32 : S.t32;
-        for (int j = threadIdx.x; j < NB; j += kHaloThreads) {
+        for (int j = threadIdx.x; j < NB; j += NT) {
             const int m = buf_m(j);
             cp_async16(P_st + j, Pl + 4 * (size_t)m);
             cp_async16(R_st + j, Rl + 4 * (size_t)m);
@@ -2502,7 +2510,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     auto pass_a1 = [&](int mode, int cur, int prv) {
         const SysLocal& L = sl[0];
         const W ar = L.f_alpha_re, beta = L.f_beta, cre = L.f_c_re, cim = L.f_c_im;
-        for (int j = threadIdx.x; j < NB; j += kHaloThreads) {
+        for (int j = threadIdx.x; j < NB; j += NT) {
             const int o = own_of(j);
             const bool is_own = o >= 0;
             const int m = is_own ? own_m(o) : 0;
@@ -2536,7 +2544,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         Site<W, K> zero;
 #pragma unroll
         for (int i = 0; i < 4; ++i) zero.v[i] = W(0);
-        for (int j = SB + threadIdx.x; j < NB - SB; j += kHaloThreads) {
+        for (int j = SB + threadIdx.x; j < NB - SB; j += NT) {
             int t, b, du, dd;
             cell(j, 1, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
@@ -2547,7 +2555,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             st_sm(Wp, j, h);
         }
         __syncthreads();
-        for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += kHaloThreads) {
+        for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += NT) {
             int t, b, du, dd;
             cell(j, 0, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
@@ -2557,7 +2565,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
             if (o >= 0) st_sm(V_own, o, v);
         }
         __syncthreads();
-        for (int j = 3 * SB + threadIdx.x; j < NB - 3 * SB; j += kHaloThreads) {
+        for (int j = 3 * SB + threadIdx.x; j < NB - 3 * SB; j += NT) {
             int t, b, du, dd;
             cell(j, 1, t, b, du, dd);
             const W sp = (t + 1 == Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
@@ -2630,7 +2638,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     auto reliable = [&](int cur, int prv) -> bool {
         const SysLocal& L = sl[0];
         double* chi = S.x;
-        for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+        for (int o = threadIdx.x; o < own; o += NT) {
             const int m = own_m(o);
             Site<double, K> xv = load_site<double, K>(chi, m);
             const Site<W, K> xs = ld_sm(X_st, o);
@@ -2651,7 +2659,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         Site<double, K> zero;
 #pragma unroll
         for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
-        for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+        for (int o = threadIdx.x; o < own; o += NT) {
             const int m = own_m(o);
             int t, b, du, dd;
             eo_geom(m, 1, Nh, sh, t, b, du, dd);
@@ -2706,7 +2714,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     // b for the force); on the odd ones 1 / A_o (dinv, the one FP64 division
     // per site of the solve) and -A_o^-1 eta_o (t64, compact); chi_e = 0;
     // rhs_e; r_0 = p_0 = rhs_e
-    for (int o = threadIdx.x; o < 2 * own; o += kHaloThreads) {
+    for (int o = threadIdx.x; o < 2 * own; o += NT) {
         const int m = own_m(o >> 1), q = o & 1;
         int t, b, du, dd;
         eo_geom(m, q, Nh, sh, t, b, du, dd);
@@ -2723,7 +2731,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
         }
     }
     YK_TMARK(12);
-    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+    for (int o = threadIdx.x; o < own; o += NT) {
         Site<double, K> z;
         Site<W, K> zw;
 #pragma unroll
@@ -2738,8 +2746,8 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     if (!nsync(a, ++epoch, deps)) return;
     YK_TMARK(13);
     // 1 / A_o in FP32 on the widened range, from the owners' dinv
-    for (int j = SB + threadIdx.x; j < NB - SB; j += kHaloThreads) dip[j] = (float)S.dinv[buf_m(j)];
-    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+    for (int j = SB + threadIdx.x; j < NB - SB; j += NT) dip[j] = (float)S.dinv[buf_m(j)];
+    for (int o = threadIdx.x; o < own; o += NT) {
         const int m = own_m(o);
         int t, b, du, dd;
         eo_geom(m, 0, Nh, sh, t, b, du, dd);
@@ -2812,7 +2820,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eo_kernel(CGArgs a)
     Site<double, K> zero;
 #pragma unroll
     for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
-    for (int o = threadIdx.x; o < own; o += kHaloThreads) {
+    for (int o = threadIdx.x; o < own; o += NT) {
         const int m = own_m(o);
         int t, b, du, dd;
         eo_geom(m, 0, Nh, sh, t, b, du, dd);
@@ -3555,13 +3563,14 @@ static bool eo_takes(int Nt, int Nx, int tpb, size_t* smem)
     return *smem <= kHaloMaxSmem;
 }
 
-// Whether cg_eo_kernel<true> takes it: kPT x kPX patches tile the compact
+// Whether cg_eo_kernel<PX> takes it: kPT x PX patches tile the compact
 // lattice, one block per patch.
+template <int PX>
 static bool eo_patch_takes(int Nt, int Nx, int* patches, size_t* smem)
 {
-    if (Nt < kPT || Nx < 2 * kPX || (Nt % kPT) || (Nx % (2 * kPX))) return false;
-    *patches = (Nt / kPT) * (Nx / (2 * kPX));
-    *smem = eo_smem_bytes(kPT * kPX, kSN);
+    if (Nt < kPT || Nx < 2 * PX || (Nt % kPT) || (Nx % (2 * PX))) return false;
+    *patches = (Nt / kPT) * (Nx / (2 * PX));
+    *smem = eo_smem_bytes(kPT * PX, eo_sw(PX) * kSR);
     return true;
 }
 
@@ -3569,28 +3578,29 @@ static int eo_max_grid()
 {
     static int maxg = -1;
     if (maxg < 0) {
-        cudaFuncSetAttribute((const void*)cg_eo_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute((const void*)cg_eo_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kHaloMaxSmem);
         int dev = 0, nsm = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<false>, kHaloThreads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<0>, kHaloThreads,
                                                       kHaloMaxSmem);
         maxg = per * nsm;
     }
     return maxg;
 }
 
+template <int PX>
 static int eo_patch_max_grid()
 {
     static int maxg = -1;
     if (maxg < 0) {
-        const int smem = (int)eo_smem_bytes(kPT * kPX, kSN);
-        cudaFuncSetAttribute((const void*)cg_eo_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        const int smem = (int)eo_smem_bytes(kPT * PX, eo_sw(PX) * kSR);
+        cudaFuncSetAttribute((const void*)cg_eo_kernel<PX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         int dev = 0, nsm = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<true>, kHaloThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eo_kernel<PX>, eo_threads(PX), smem);
         maxg = per * nsm;
         if (maxg > kMaxGrid) maxg = kMaxGrid;
     }
@@ -3631,7 +3641,8 @@ void cg_halo_init()
 {
     halo_max_grid();
     eo_max_grid();
-    eo_patch_max_grid();
+    eo_patch_max_grid<16>();
+    eo_patch_max_grid<8>();
     eob_max_grid();
 }
 
@@ -3645,24 +3656,38 @@ int cg_predict_grid(const CGArgs& a, bool mixed)
 }
 
 // The single-system even-odd kernel launch_cg takes for `a` (mixed, K = 1):
-// 2 patches (*grid blocks), 1 rows (*grid blocks of *tpb tiles), 0 neither.
-static int eo_single_variant(const CGArgs& a, int* grid, int* tpb, size_t* smem)
+// its patch width (16 or 8; 0 whole rows) in *px, *grid blocks of *tpb tiles
+// (patches: one), false when none takes it.  YK_CG_EO_PATCH=0, 8 or 16 fixes
+// the form.
+static bool eo_single_variant(const CGArgs& a, int* px, int* grid, int* tpb, size_t* smem)
 {
-    if (!(a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr && a.sys_count == 1)) return 0;
+    if (!(a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr && a.sys_count == 1)) return false;
     const char* pe = getenv("YK_CG_EO_PATCH");
+    const int want = pe ? atoi(pe) : -1;
+    // partial slots: one per patch, within the system's tiles (2 per compact tile)
+    const int slots = 2 * (a.eo_tile_end - a.eo_tile_begin);
     int np = 0;
-    if (!(pe && pe[0] == '0') && eo_patch_takes(a.solo_nt, a.solo_nx, &np, smem) && np <= eo_patch_max_grid() &&
-        a.eo_tile_begin + np <= a.eo_tile_end) {
+    if ((want == -1 || want == 16) && eo_patch_takes<16>(a.solo_nt, a.solo_nx, &np, smem) &&
+        np <= eo_patch_max_grid<16>() && np <= slots) {
+        *px = 16;
         *grid = np;
         *tpb = 1;
-        return 2;
+        return true;
+    }
+    if ((want == -1 || want == 8) && eo_patch_takes<8>(a.solo_nt, a.solo_nx, &np, smem) &&
+        np <= eo_patch_max_grid<8>() && np <= slots) {
+        *px = 8;
+        *grid = np;
+        *tpb = 1;
+        return true;
     }
     const int eg = cg_grid_for(a.eo_tile_end - a.eo_tile_begin, capped(eo_max_grid(), a.grid_cap), tpb);
     if (eg <= kMaxGrid && eo_takes(a.solo_nt, a.solo_nx, *tpb, smem)) {
+        *px = 0;
         *grid = eg;
-        return 1;
+        return true;
     }
-    return 0;
+    return false;
 }
 
 template <int K, bool MIXED>
@@ -3692,11 +3717,10 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
             e.tile_end = a.eo_tile_end;
             e.eo = 1;
             // patches first (less halo work per block), then rows of the lattice
-            int eg = 0, etpb = 1;
+            int px = 0, eg = 0, etpb = 1;
             size_t es = 0;
-            const int var = eo_single_variant(a, &eg, &etpb, &es);
-            if (var != 0) {
-                if (var == 2) e.tile_end = e.tile_begin + eg;   // one partial slot per patch
+            if (eo_single_variant(a, &px, &eg, &etpb, &es)) {
+                if (px > 0) e.tile_end = e.tile_begin + eg;   // one partial slot per patch
                 e.tiles_per_block = etpb;
                 e.grid = eg;
                 if (grid_out) *grid_out = eg;
@@ -3704,7 +3728,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
                 cudaLaunchConfig_t cfg = {};
                 cfg.gridDim = dim3(eg);
-                cfg.blockDim = dim3(kHaloThreads);
+                cfg.blockDim = dim3(eo_threads(px));
                 cfg.dynamicSmemBytes = es;
                 cfg.stream = stream;
                 cudaLaunchAttribute attr[1];
@@ -3713,8 +3737,10 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 cfg.attrs = attr;
                 cfg.numAttrs = 1;
                 void* args[] = {&e};
-                return cudaLaunchKernelExC(&cfg, var == 2 ? (const void*)cg_eo_kernel<true> : (const void*)cg_eo_kernel<false>,
-                                           args);
+                const void* fn = px == 16 ? (const void*)cg_eo_kernel<16>
+                               : px == 8  ? (const void*)cg_eo_kernel<8>
+                                          : (const void*)cg_eo_kernel<0>;
+                return cudaLaunchKernelExC(&cfg, fn, args);
             }
             // the batched even-odd kernel: work dealt out per pass, so the
             // grid does not follow the tiles (at most one block per two tiles)
