@@ -630,11 +630,22 @@ __device__ CoefVals scalar_step(const CGArgs& a, int k, bool ru_round, const dou
         if (!isfinite(rr)) return retire(0, YK_ENAN);
         if (!(rr > st.stop2)) return retire(1, 0);
         if (k >= a.max_iter) return retire(0, YK_ENOCONV);
-        // p_k = r + beta (p_{k-1} - gamma r), gamma = <r, p_{k-1}> / |r|^2
-        const double beta = rr / st.rr_prev, inv_rr = 1.0 / rr;
-        cv.beta = beta;
-        cv.c_re = 1.0 - beta * (s[2] * inv_rr);
-        cv.c_im = -beta * (s[3] * inv_rr);
+        // p_k = r + beta (p_{k-1} - gamma r), gamma = <r, p_{k-1}> / |r|^2;
+        // the mixed solver divides in FP32 (its p update is FP32; an FP64
+        // division is ~650 cycles on the path every block waits for)
+        const float rrf = (float)rr, rpf = (float)st.rr_prev;
+        if (MIXED && rrf > FLT_MIN && rpf > FLT_MIN && rrf < FLT_MAX && rpf < FLT_MAX) {
+            const float inv = 1.f / rrf;
+            const float beta = rrf / rpf;
+            cv.beta = (double)beta;
+            cv.c_re = (double)(1.f - beta * ((float)s[2] * inv));
+            cv.c_im = (double)(-beta * ((float)s[3] * inv));
+        } else {
+            const double beta = rr / st.rr_prev, inv_rr = 1.0 / rr;
+            cv.beta = beta;
+            cv.c_re = 1.0 - beta * (s[2] * inv_rr);
+            cv.c_im = -beta * (s[3] * inv_rr);
+        }
         cv.mode = kRedo;
         st.rmax2 = rr;
         atomicAdd(s_active, 1);
@@ -2701,9 +2712,12 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
                 v[0] = site_norm2<double, K>(rd);
                 site_dot<double, K>(rd, pd, v[2], v[3]);
             }
+            // the two reduced slots only (each conversion is FP64 work)
             FF f[6];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+            for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+            f[0] = ff_of(v[0]);
+            f[2] = ff_of(v[2]);
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         }
         YK_TMARK(11);
@@ -3074,11 +3088,14 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
         eob_scan(nsys, s_mode, s_nt, mask, s_pre);
         int lo, hi;
         eob_share(s_pre[nsys], &lo, &hi);
+        int qc = -1;   // the previous tile's system: a contiguous share mostly stays in one
         for (int base = lo; base < hi; base += 2) {
             const int i = base + hf;
             const bool tile_on = i < hi;
-            const int q = eob_find(tile_on ? i : lo, nsys, s_pre);
-            const int lt = (tile_on ? i : lo) - s_pre[q];
+            const int ii = tile_on ? i : lo;
+            const int q = (qc >= 0 && ii >= s_pre[qc] && ii < s_pre[qc + 1]) ? qc : eob_find(ii, nsys, s_pre);
+            qc = q;
+            const int lt = ii - s_pre[q];
             const SysDev& S = a.sys[a.sys_first + q];
             const int m = lt * kTile + ts;
             f(S, q, m, s_t0[q] + lt, tile_on, tile_on && m < S.V);
@@ -3360,9 +3377,12 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
                 v[0] = site_norm2<double, K>(rd);
                 site_dot<double, K>(rd, pd, v[2], v[3]);
             }
+            // the two reduced slots only (each conversion is FP64 work)
             FF f[6];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) f[i] = ff_of(v[i]);
+            for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+            f[0] = ff_of(v[0]);
+            f[2] = ff_of(v[2]);
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         });
         YK_TMARK(5);
