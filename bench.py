@@ -292,8 +292,9 @@ def e2e(yk, torch, ctx, phi_seg, step_seg, k, flush, phi_end):
     """The same k steps as `value` (the timed segment replayed from its first
     field and Philox step) through the C ABI with host buffers: every step
     uploads the field from pinned host memory, steps, and reads the field and
-    the observables back.  Wall clock around each step's calls; L2 flushed
-    between steps, outside the timed calls."""
+    the observables back (yk_langevin_step_io: one call, one synchronisation).
+    Wall clock around each step's call; L2 flushed between steps, outside the
+    timed calls."""
     import ctypes as C
     V = NT * NX
     host_in = torch.empty(V, dtype=torch.float64).pin_memory()
@@ -307,10 +308,8 @@ def e2e(yk, torch, ctx, phi_seg, step_seg, k, flush, phi_end):
         flush.fill_(i & 0xFF)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        yk._check(lib.yk_set_field_host(ctx.h, 0, C.c_void_p(host_in.data_ptr())))
-        yk._check(lib.yk_langevin_step(ctx.h, 1))
-        yk._check(lib.yk_get_field_host(ctx.h, 0, C.c_void_p(host_out.data_ptr())))
-        yk._check(lib.yk_observables(ctx.h, 0, C.byref(o)))
+        yk._check(lib.yk_langevin_step_io(ctx.h, 0, C.c_void_p(host_in.data_ptr()), C.c_void_p(host_out.data_ptr()),
+                                          C.byref(o)))
         sec += time.perf_counter() - t0
         host_in, host_out = host_out, host_in
     same = bool(torch.equal(host_in, torch.from_numpy(phi_end)))

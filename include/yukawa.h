@@ -304,6 +304,15 @@ int yk_coloured_noise(yk_ctx* ctx, int chain, const double* white, double* xi);
  * graph is captured once and replayed. */
 int yk_langevin_step(yk_ctx* ctx, int n_steps);
 
+/* One Langevin step of every chain with chain `chain`'s host I/O in one call
+ * (the per-step host exchange of main.cu:370-381, which copies eps to the host
+ * every step): the field uploaded from phi_in (V doubles, host; NULL keeps the
+ * device field), the step, the field downloaded to phi_out (NULL: not read) and
+ * the observables to obs (NULL: not read), with one synchronisation at the end
+ * (the buffers may be reused when the call returns; pinned buffers take the
+ * copies by DMA). */
+int yk_langevin_step_io(yk_ctx* ctx, int chain, const double* phi_in, double* phi_out, yk_obs* obs);
+
 /* The autotuner (no reference counterpart: the reference's launch shapes are
  * fixed, main.cu:258-266).  Batched contexts (several CG systems per step):
  * the grid of the step's persistent CG, i.e. how many 256-site tiles each

@@ -519,6 +519,35 @@ def test_autotune_keeps_results(ylib, cuda, monkeypatch):
         assert np.array_equal(got[c], want[c]), c
 
 
+def test_step_io_matches_separate_calls(ylib, cuda):
+    # yk_langevin_step_io (upload, step, download, one synchronisation) gives
+    # the fields and observables of set_field + step + get_field + observables
+    yk = ylib
+    p = params(yk, 32, 32, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    phi0 = np.random.default_rng(5).uniform(-1, 1, 32 * 32)
+    want, obs_w = [], []
+    with yk.Context(p) as ctx:
+        ctx.set_field(phi0)
+        for _ in range(3):
+            ctx.step(1)
+            want.append(ctx.get_field())
+            obs_w.append(ctx.observables())
+    with yk.Context(p) as ctx:
+        cur = phi0.copy()
+        out = np.empty_like(cur)
+        for s in range(3):
+            o = ctx.step_io(cur, out)
+            assert np.array_equal(out, want[s]), s
+            assert o.status == 0 and o.steps == s + 1 and o.sum_phi == obs_w[s].sum_phi
+            cur, out = out, cur
+        # no upload: the step continues from the device field; no download
+        o = ctx.step_io(None, None)
+        assert o.steps == 4
+    with pytest.raises(TypeError):
+        with yk.Context(p) as ctx:
+            ctx.step_io(np.zeros(32 * 32, dtype=np.float32))
+
+
 def test_deterministic(ylib, cuda):
     yk = ylib
     p = params(yk, 32, 32)

@@ -185,6 +185,7 @@ _SIGS = {
     "yk_fermion_force": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SolveStats)]),
     "yk_coloured_noise": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "yk_langevin_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "yk_langevin_step_io": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "yk_euler_update": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(Obs)]),
     "yk_observables": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Obs)]),
     "yk_profile_begin": (C.c_int, [C.c_void_p]),
@@ -397,6 +398,28 @@ class Context:
 
     def step(self, n=1):
         _check(lib().yk_langevin_step(self.h, n))
+
+    def step_io(self, phi_in=None, phi_out=None, chain=0) -> "Obs":
+        """One step with chain `chain`'s field uploaded from and downloaded to
+        host arrays (numpy float64 or pinned torch tensors; None: skipped) and
+        its observables returned, one synchronisation."""
+        import numpy as np
+        V = self.volume(chain)
+
+        def host(a, writable):
+            if a is None:
+                return None
+            if isinstance(a, np.ndarray):
+                if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or (writable and not a.flags["WRITEABLE"]):
+                    raise TypeError("step_io: host arrays must be C-contiguous float64 (and writable for phi_out)")
+                if a.size != V:
+                    raise ValueError(f"step_io: {a.size} values for a lattice of {V} sites")
+                return a.ctypes.data
+            return _ptr(a)
+
+        o = Obs()
+        _check(lib().yk_langevin_step_io(self.h, chain, host(phi_in, False), host(phi_out, True), C.byref(o)))
+        return o
 
     def autotune(self) -> TuneResult:
         t = TuneResult()

@@ -1708,6 +1708,19 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
     return YK_OK;
 }
 
+int yk_langevin_step_io(yk_ctx* ctx, int c, const double* phi_in, double* phi_out, yk_obs* obs)
+{
+    if (int rc = chain_ok(ctx, c)) return rc;
+    const Chain& C = ctx->ch[c];
+    if (phi_in)
+        YK_CK(cudaMemcpyAsync(C.phi, phi_in, sizeof(double) * C.V, cudaMemcpyHostToDevice, ctx->stream));
+    if (int rc = yk_langevin_step(ctx, 1)) return rc;
+    if (phi_out)
+        YK_CK(cudaMemcpyAsync(phi_out, C.phi, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream));
+    if (obs) YK_CK(cudaMemcpyAsync(obs, &ctx->d_chains[c].obs, sizeof(yk_obs), cudaMemcpyDeviceToHost, ctx->stream));
+    return status_of_err(ctx);   // the one synchronisation
+}
+
 int yk_euler_update(yk_ctx* ctx, int c, const double* force, const double* xi, yk_obs* obs)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
