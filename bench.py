@@ -408,6 +408,27 @@ def precision_errors(yk, torch, stream, phi_seg, step_seg, n, n_ops=5):
 
 
 
+EOB_BYTES_PER_SITE_ITERATION = 144   # 288 B per compact site and round of cg_eob_kernel
+
+
+def eob_roofline(yk, torch, stream, ctx):
+    """One more step, profiled: the batched even-odd CG's algorithmic bytes
+    (per compact site and round: P1 reads r, q, p, xs, v and writes r, p, xs,
+    w; P2 reads p, w, writes v; P3 reads v, writes u; P4 reads v, u, r, writes
+    q: 288 B, i.e. 144 B per lattice site and iteration) over its CUDA-event
+    time, against the measured HBM copy bandwidth."""
+    ctx.profile_begin()
+    with torch.cuda.stream(stream):
+        ctx.step(1)
+    pr = ctx.profile_end()
+    pk = peaks()
+    kernels = {0: "cg_kernel", 3: "cg_eo_kernel", 4: "cg_eob_kernel"}
+    gbs = pr.cg_site_iterations * EOB_BYTES_PER_SITE_ITERATION / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
+    return {"kernel": kernels.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_ms": round(pr.cg_ms, 3),
+            "bytes_per_site_iteration": EOB_BYTES_PER_SITE_ITERATION, "achieved": round(gbs, 1), "unit": "GB/s",
+            "peak": pk["hbm_gbs"], "frac": round(gbs / pk["hbm_gbs"], 4), "peak_source": pk["source"]}
+
+
 def full_scale(yk, torch, stream, steps=1, L=1024, n_chains=8, n_rhs=8):
     """The full form at scale: 8 chains of 1024^2 (m0 = 0.01, g = 0.6,
     Lambda = pi/4, i.e. cutFraction 0.17678), 8 stochastic right-hand sides
@@ -456,6 +477,8 @@ def full_scale(yk, torch, stream, steps=1, L=1024, n_chains=8, n_rhs=8):
                      "site_steps_per_s": round(steps * n_chains * L * L / sec, 1),
                      "cg_iterations_per_system_step": round(its / (steps * n_chains * n_rhs), 1),
                      "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs)}
+        if prec == yk.YK_MIXED:
+            out[name]["cg_roofline"] = eob_roofline(yk, torch, stream, ctx)
         ctx.close()
     # learned: chain 0's 2-layer network trained at its field, its weights
     # copied to every chain (same couplings; the features adapt to each field)
@@ -520,6 +543,8 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
         ctx.step(2)
     pr = ctx.profile_end()
     ctx.close()
+    pk = peaks()
+    gbs = pr.cg_site_iterations * EOB_BYTES_PER_SITE_ITERATION / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
     sites = int(sum(int(L) * int(L) for L in Ls))
     kernels = {0: "cg_kernel (grid-wide D^dag D)", 4: "cg_eob_kernel (batched even-odd)"}
     return {"config": f"{n_chains} chains, L in {{32,64,128,256}} (seed {seed}), 4 RHS, mixed CG rel-res 1e-10",
@@ -528,6 +553,8 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
             "ms_per_step": round(sec * 1e3 / steps, 3),
             "cg_kernel": kernels.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_grid": pr.cg_grid,
             "cg_iterations_per_system_step": round(pr.cg_iterations / max(pr.steps * n_chains * 4, 1), 1),
+            "cg_roofline": {"bytes_per_site_iteration": EOB_BYTES_PER_SITE_ITERATION, "achieved": round(gbs, 1),
+                            "unit": "GB/s", "peak": pk["hbm_gbs"], "frac": round(gbs / pk["hbm_gbs"], 4)},
             "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs),
             "autotune": {"cg_grid": t.cg_grid, "cg_grid_max": t.cg_grid_max, "candidates": t.cg_candidates,
                          "ms_chosen": round(t.cg_ms_chosen, 3), "ms_at_max": round(t.cg_ms_max, 3)}}
