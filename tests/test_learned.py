@@ -231,6 +231,32 @@ def test_learned_step_matches_cg_step(ylib, cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("lat", [(32, 32), (41, 25)], ids=["32x32", "41x25"])
+def test_persistent_pcg_matches_launched_phases(ylib, cuda, monkeypatch, lat):
+    # the persistent PCG chunk (one cooperative launch, grid barriers between
+    # the phases) against one launch per phase: the same bodies on the same
+    # grid, so the learned steps' fields agree bit for bit, with the network
+    # (per-layer convolutions) and with z = r
+    monkeypatch.setenv("YK_NET_TILE", "8x64x1")
+    yk = ylib
+    Nt, Nx = lat
+    fields = {}
+    for persistent in ("0", "2"):   # off; at most two blocks per SM
+        monkeypatch.setenv("YK_PCG_PERSISTENT", persistent)
+        for use in (False, True):
+            with yk.Context(_params(yk, Nt, Nx, 0.05, yk.YK_FP64)) as ctx:
+                ctx.net_setup(2, 7)
+                ctx.net_train(n_sources=2, n_levels=3, base_iter=4, steps=40, batch=2, lr=2e-3, seed=3)
+                st = ctx.step_learned(2, use_net=use)
+                assert st.converged == 1
+                assert ctx.observables().status == 0
+                fields[persistent, use] = (ctx.get_field(), st.iterations)
+    for use in (False, True):
+        assert fields["0", use][1] == fields["2", use][1]
+        assert np.array_equal(fields["0", use][0], fields["2", use][0]), use
+
+
+@pytest.mark.gpu
 def test_run_protocol_with_learned_solver(ylib, cuda, tmp_path):
     # the reference's run protocol (yk_run_toml) with [gpu] learned_layers = 2:
     # a network is trained after thermalisation and the measurement steps

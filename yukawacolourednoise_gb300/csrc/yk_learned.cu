@@ -36,6 +36,7 @@ namespace yk {
 namespace {
 
 constexpr int kNetThreads = 256;
+constexpr int kPcgMaxConv = 16;   // the persistent PCG's convolutions per iteration (2L)
 constexpr int kNetC = 8;          // feature and hidden channels
 constexpr int kNetOut = 4;        // output channels (spinor components)
 constexpr int kWTile = 64;        // sites per shared-memory tile of the weight gradient
@@ -428,17 +429,17 @@ __global__ void __launch_bounds__(kNetThreads) net_featT_bf_kernel(const uint4* 
 // TRANS = false: Y = conv(X) (a layer of N, 8 -> COUT channels);
 // TRANS = true: Y = conv^T(X) (its transpose in N^T, COUT -> 8: the opposite
 // tap, the same sign, W[k] transposed).  X, Y: BF16 site-major, 8 channels.
-template <int COUT, bool TRANS>
-__global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* __restrict__ X, uint4* __restrict__ Y,
-                                                                  const float* __restrict__ Wl, int Nt, int Nx,
-                                                                  int R, int W)
+// The layer on the tiles blockIdx.x, blockIdx.x + gridDim.x, ... (PDL: the
+// kernel form, one tile per block, with its programmatic-launch wait and
+// trigger; else the persistent PCG's form, tiles in turn).
+template <int COUT, bool TRANS, bool PDL>
+__device__ __forceinline__ void conv_bf_tiles(const uint4* __restrict__ X, uint4* __restrict__ Y,
+                                              const float* __restrict__ Wl, int Nt, int Nx, int R, int W, uint4* sm)
 {
-    __shared__ __align__(16) uint4 sm[(kTcMaxR + 2) * kTcSW];
-    constexpr int SW = kTcSW;
+    constexpr int SW = kTcSW;   // sm: (kTcMaxR + 2) x kTcSW staged sites
     const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
     const int tiles_x = (Nx + W - 1) / W;
-    const int t0 = (blockIdx.x / tiles_x) * R, x0 = (blockIdx.x % tiles_x) * W;
-    const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
+    const int ntiles = ((Nt + R - 1) / R) * tiles_x;
     // B fragments of the tap pairs (2p, 2p + 1): K = the pair's 16 inputs, N = 8 outputs
     uint32_t b0[5], b1[5];
 #pragma unroll
@@ -463,7 +464,11 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
         b0[p] = pack_bf2(w[0], w[1]);
         b1[p] = pack_bf2(w[2], w[3]);
     }
-    pdl_wait();   // the weights above are constant during a solve; X is the previous layer's
+    if (PDL) pdl_wait();   // the weights above are constant during a solve; X is the previous layer's
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    if (tile != (int)blockIdx.x) __syncthreads();   // the previous tile's reads of sm are done
+    const int t0 = (tile / tiles_x) * R, x0 = (tile % tiles_x) * W;
+    const int Rt = min(R, Nt - t0), Wt = min(W, Nx - x0);
     // stage the tile and its halo: warp w takes the staged rows w, w + 8
     for (int lr = threadIdx.x >> 5; lr < Rt + 2; lr += kNetThreads / 32) {
         int t = t0 - 1 + lr;
@@ -519,7 +524,17 @@ __global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* _
         if (in0) Yw[(size_t)n0 * 4 + c] = pack_bf2(acc[0], acc[1]);
         if (in1) Yw[(size_t)n1 * 4 + c] = pack_bf2(acc[2], acc[3]);
     }
-    pdl_trigger();
+    }
+    if (PDL) pdl_trigger();
+}
+
+template <int COUT, bool TRANS>
+__global__ void __launch_bounds__(kNetThreads) net_conv_bf_kernel(const uint4* __restrict__ X, uint4* __restrict__ Y,
+                                                                  const float* __restrict__ Wl, int Nt, int Nx,
+                                                                  int R, int W)
+{
+    __shared__ __align__(16) uint4 sm[(kTcMaxR + 2) * kTcSW];
+    conv_bf_tiles<COUT, TRANS, true>(X, Y, Wl, Nt, Nx, R, W, sm);
 }
 
 // Several layers in one launch.  A block stages its R x W tile with a halo
@@ -705,9 +720,13 @@ struct LearnedNet {
     int restart = 0;
     PcgGraph* pcg = nullptr;          // its captured chunk of iterations
     bool pcg_no_graph = false;        // capture failed once (e.g. the legacy stream)
+    bool persistent = false;          // chunks of iterations as one cooperative launch (grid <= co-resident)
+    unsigned* pbar = nullptr;         // its barrier counter and error word
 };
 
 namespace {
+
+int pcg_chunk_max_grid();
 
 int cout_of(const LearnedNet* n, int l) { return l == n->layers - 1 ? kNetOut : kNetC; }
 
@@ -786,6 +805,7 @@ void net_destroy(LearnedNet* n)
     for (double* p : ds)
         if (p) cudaFree(p);
     if (n->hpart) cudaFreeHost(n->hpart);
+    if (n->pbar) cudaFree(n->pbar);
     pcg_graph_destroy(n->pcg);
     for (uint4* h : n->h16)
         if (h) cudaFree(h);
@@ -818,6 +838,21 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     }
     const size_t V = (size_t)n->V;
     n->grid = (int)std::min<size_t>((V + kNetThreads - 1) / kNetThreads, 4096);
+    // YK_PCG_PERSISTENT=k (opt-in): the PCG chunk as one cooperative launch
+    // of at most k blocks per SM, grid barriers between its phases.  Off by
+    // default: at 512 x 512 its barriers cost more than the PDL launch
+    // boundaries they replace (2-layer network 151 against 178 steps/s).
+    const char* pe = getenv("YK_PCG_PERSISTENT");
+    const int pk = pe ? atoi(pe) : 0;
+    int pg = pk > 0 ? pcg_chunk_max_grid() : 0;
+    if (pg > 0 && 2 * layers <= kPcgMaxConv) {
+        int dev0 = 0, nsm0 = 0;
+        cudaGetDevice(&dev0);
+        cudaDeviceGetAttribute(&nsm0, cudaDevAttrMultiProcessorCount, dev0);
+        pg = std::min(pg, pk * nsm0);
+        n->grid = std::min(n->grid, pg);
+        n->persistent = true;
+    }
     n->nblk = (int)std::min<size_t>((V + kWTile - 1) / kWTile, 512);
     // convolution tiles: 64 columns (or the whole row), rows halved from 8
     // while there are fewer than two tiles per SM
@@ -846,6 +881,7 @@ LearnedNet* net_create(int Nt, int Nx, int layers, cudaError_t* err)
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[0], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMalloc(&n->h16[1], sizeof(uint4) * V);
     if (e == cudaSuccess) e = cudaMallocHost(&n->hpart, sizeof(double) * n->grid);
+    if (e == cudaSuccess) e = cudaMalloc(&n->pbar, 2 * sizeof(unsigned));
     if (e == cudaSuccess) n->hpart_cap = (size_t)n->grid;
     if (e == cudaSuccess) e = cudaMemset(n->m, 0, sizeof(float) * n->nw);
     if (e == cudaSuccess) e = cudaMemset(n->v, 0, sizeof(float) * n->nw);
@@ -1515,14 +1551,13 @@ __device__ __forceinline__ float2 block_totals(const float* a, const float* b, i
 // x += alpha p, r -= alpha q; with X != null also the network's BF16
 // features (r, sigma r) of the new r
 // alpha = <r, z> / <p, q> from the z kernel's and the q kernel's partials
-__global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
-                                                             const float* __restrict__ p, const float* __restrict__ q,
-                                                             const float* __restrict__ part_rz,
-                                                             const float* __restrict__ part_pq, int nb,
-                                                             const float* __restrict__ sigma, uint4* __restrict__ X,
-                                                             int V)
+template <bool PDL>
+__device__ __forceinline__ void pcg_xr_body(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+                                            const float* __restrict__ q, const float* __restrict__ part_rz,
+                                            const float* __restrict__ part_pq, int nb, const float* __restrict__ sigma,
+                                            uint4* __restrict__ X, int V)
 {
-    pdl_wait();
+    if (PDL) pdl_wait();
     const float2 t = block_totals(part_rz, part_pq, nb);
     const float a = t.y != 0.f ? t.x / t.y : 0.f;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
@@ -1540,21 +1575,30 @@ __global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__
         reinterpret_cast<float4*>(r)[n] = rv;
         if (X) X[n] = features_bf(rv, sigma[n]);
     }
-    pdl_trigger();
+    if (PDL) pdl_trigger();
+}
+
+__global__ void __launch_bounds__(kNetThreads) pcg_xr_kernel(float* __restrict__ x, float* __restrict__ r,
+                                                             const float* __restrict__ p, const float* __restrict__ q,
+                                                             const float* __restrict__ part_rz,
+                                                             const float* __restrict__ part_pq, int nb,
+                                                             const float* __restrict__ sigma, uint4* __restrict__ X,
+                                                             int V)
+{
+    pcg_xr_body<true>(x, r, p, q, part_rz, part_pq, nb, sigma, X, V);
 }
 
 // z = F^T a + skip r (a != null: the network's last transposed layer) or
 // z = r (a == null), with the per-block partials of <r, z>, <r, r> and
 // <z, q> (q null: 0) in part[0..nb), part[nb..2nb), part[2nb..3nb) (FP32
 // products of a site, FP64 across warps, stored in FP32).
-__global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restrict__ a,
-                                                            const float* __restrict__ sigma,
-                                                            const float* __restrict__ r, float skip,
-                                                            float* __restrict__ z, const float* __restrict__ q,
-                                                            float* __restrict__ part, int V)
+template <bool PDL>
+__device__ __forceinline__ void pcg_z_body(const uint4* __restrict__ a, const float* __restrict__ sigma,
+                                           const float* __restrict__ r, float skip, float* __restrict__ z,
+                                           const float* __restrict__ q, float* __restrict__ part, int V)
 {
     __shared__ double red[96];
-    pdl_wait();
+    if (PDL) pdl_wait();
     float acc[3] = {0.f, 0.f, 0.f};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         const float4 rv = reinterpret_cast<const float4*>(r)[n];
@@ -1567,7 +1611,7 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
             acc[2] += fmaf(o.x, qv.x, fmaf(o.y, qv.y, fmaf(o.z, qv.z, o.w * qv.w)));
         }
     }
-    pdl_trigger();
+    if (PDL) pdl_trigger();
     double tot[3];
     block_sum_f<3>(acc, tot, red);
     const int nb = gridDim.x;
@@ -1576,6 +1620,15 @@ __global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restr
         part[nb + blockIdx.x] = (float)tot[1];
         part[2 * nb + blockIdx.x] = (float)tot[2];
     }
+}
+
+__global__ void __launch_bounds__(kNetThreads) pcg_z_kernel(const uint4* __restrict__ a,
+                                                            const float* __restrict__ sigma,
+                                                            const float* __restrict__ r, float skip,
+                                                            float* __restrict__ z, const float* __restrict__ q,
+                                                            float* __restrict__ part, int V)
+{
+    pcg_z_body<true>(a, sigma, r, skip, z, q, part, V);
 }
 
 // diag32[n] = 2 r + m0 + g sigma[n] in FP32 (the stencils below run on the
@@ -1593,14 +1646,13 @@ __global__ void diag_f_kernel(const double* __restrict__ sigma, float* __restric
 // beta = -<z', q> / <p, q> (the Polak-Ribiere beta, -alpha <z', q> / <r, z>
 // with alpha = <r, z> / <p, q>) from the partials; 0 when <p, q> = 0 (the
 // round's first direction: the q partials are zeroed)
-__global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __restrict__ z,
-                                                             const float* __restrict__ p, float* __restrict__ p_new,
-                                                             float* __restrict__ t, const float* __restrict__ diag,
-                                                             const float* __restrict__ part_zq,
-                                                             const float* __restrict__ part_pq, int nb, int Nt,
-                                                             int Nx, float rw)
+template <bool PDL>
+__device__ __forceinline__ void pcg_dp_body(const float* __restrict__ z, const float* __restrict__ p,
+                                            float* __restrict__ p_new, float* __restrict__ t,
+                                            const float* __restrict__ diag, const float* __restrict__ part_zq,
+                                            const float* __restrict__ part_pq, int nb, int Nt, int Nx, float rw)
 {
-    pdl_wait();
+    if (PDL) pdl_wait();
     const float2 tt = block_totals(part_zq, part_pq, nb);
     const float b = tt.y != 0.f ? -tt.x / tt.y : 0.f;
     const int V = Nt * Nx;
@@ -1618,19 +1670,29 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __rest
         store_site<float, 1>(t, n, dirac_combine<float, 1, false>(c, tu, td, xu, xd, diag[n], rw, (float)nb.sp,
                                                                   (float)nb.sm));
     }
-    pdl_trigger();
+    if (PDL) pdl_trigger();
+}
+
+__global__ void __launch_bounds__(kNetThreads) pcg_dp_kernel(const float* __restrict__ z,
+                                                             const float* __restrict__ p, float* __restrict__ p_new,
+                                                             float* __restrict__ t, const float* __restrict__ diag,
+                                                             const float* __restrict__ part_zq,
+                                                             const float* __restrict__ part_pq, int nb, int Nt,
+                                                             int Nx, float rw)
+{
+    pcg_dp_body<true>(z, p, p_new, t, diag, part_zq, part_pq, nb, Nt, Nx, rw);
 }
 
 // q = D^dag t and the per-block partials of <p, q> (FP32 per site, FP64
 // across warps)
-__global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __restrict__ t,
-                                                             const float* __restrict__ p, float* __restrict__ q,
-                                                             const float* __restrict__ diag,
-                                                             float* __restrict__ part, int Nt, int Nx, float rw)
+template <bool PDL>
+__device__ __forceinline__ void pcg_dq_body(const float* __restrict__ t, const float* __restrict__ p,
+                                            float* __restrict__ q, const float* __restrict__ diag,
+                                            float* __restrict__ part, int Nt, int Nx, float rw)
 {
     __shared__ double red[32];
     const int V = Nt * Nx;
-    pdl_wait();
+    if (PDL) pdl_wait();
     float acc[1] = {0.f};
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < V; n += gridDim.x * blockDim.x) {
         const Nbr nb = neighbours(n, Nt, Nx);
@@ -1641,10 +1703,18 @@ __global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __rest
         const Site<float, 1> pv = load_site<float, 1>(p, n);
         acc[0] += fmaf(pv.v[0], o.v[0], fmaf(pv.v[1], o.v[1], fmaf(pv.v[2], o.v[2], pv.v[3] * o.v[3])));
     }
-    pdl_trigger();
+    if (PDL) pdl_trigger();
     double tot[1];
     block_sum_f<1>(acc, tot, red);
     if (threadIdx.x == 0) part[blockIdx.x] = (float)tot[0];
+}
+
+__global__ void __launch_bounds__(kNetThreads) pcg_dq_kernel(const float* __restrict__ t,
+                                                             const float* __restrict__ p, float* __restrict__ q,
+                                                             const float* __restrict__ diag,
+                                                             float* __restrict__ part, int Nt, int Nx, float rw)
+{
+    pcg_dq_body<true>(t, p, q, diag, part, Nt, Nx, rw);
 }
 
 struct PcgBufs {
@@ -1652,6 +1722,114 @@ struct PcgBufs {
     float* part_z;    // 3 x grid FP32 partials of the z kernel: <r, z>, <r, r>, <z, q>
     float* part_pq;   // grid FP32 partials of <p, q>
 };
+
+// ---------------------------------------------------------------------------
+// The persistent form of a chunk of PCG iterations: one cooperative launch
+// runs the 4 + 2L phases of every iteration (p' and D p', D^dag, x and r with
+// the features, the network's 2L convolutions, z = M r) with a grid barrier
+// between phases instead of a kernel boundary.  The phases are the kernels'
+// own bodies; the partials stay per block (nb = the launch's blocks, the
+// solver's grid), so every value is the launched kernels' bit for bit.
+// ---------------------------------------------------------------------------
+struct PcgChunk {
+    float *z, *p[2], *tmp, *q, *x, *r;
+    const float *diag, *sig32;
+    float *part_z, *part_pq;
+    uint4* h16[2];
+    const float* w[kPcgMaxConv];   // the convolutions in order: N's layers, then N^T's
+    int cout[kPcgMaxConv];
+    int nconv;
+    int Nt, Nx, V, R, W;
+    float rw, skip;
+    int use_net, count, parity;
+    unsigned* bar;   // arrival counter (zeroed before the launch), then the error word
+};
+
+// Grid barrier of the persistent PCG: release-arrival, acquiring poll,
+// bounded (the error word set and every block leaving when it gives up).
+__device__ bool pcg_sync(unsigned* bar, unsigned& gen)
+{
+    __syncthreads();
+    int bad = 0;
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+        const unsigned target = gridDim.x * (gen + 1u);
+        const long long t0 = clock64();
+        for (;;) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+            if ((int)(v - target) >= 0) break;
+            if (*(volatile unsigned*)(bar + 1) != 0u) {
+                bad = 1;
+                break;
+            }
+            if (clock64() - t0 > 4000000000LL) {   // about 2 s
+                atomicExch(bar + 1, 1u);
+                bad = 1;
+                break;
+            }
+        }
+    }
+    ++gen;
+    return __syncthreads_or(bad) == 0;
+}
+
+__global__ void __launch_bounds__(kNetThreads) pcg_chunk_kernel(PcgChunk P)
+{
+    __shared__ __align__(16) uint4 sm[(kTcMaxR + 2) * kTcSW];
+    unsigned gen = 0;
+    const int nb = gridDim.x;
+    int parity = P.parity;
+    for (int it = 0; it < P.count; ++it, parity ^= 1) {
+        const float* p = P.p[parity];
+        float* pn = P.p[parity ^ 1];
+        pcg_dp_body<false>(P.z, p, pn, P.tmp, P.diag, P.part_z + 2 * nb, P.part_pq, nb, P.Nt, P.Nx, P.rw);
+        if (!pcg_sync(P.bar, gen)) return;
+        pcg_dq_body<false>(P.tmp, pn, P.q, P.diag, P.part_pq, P.Nt, P.Nx, P.rw);
+        if (!pcg_sync(P.bar, gen)) return;
+        pcg_xr_body<false>(P.x, P.r, pn, P.q, P.part_z, P.part_pq, nb, P.sig32, P.use_net ? P.h16[0] : nullptr,
+                           P.V);
+        if (!pcg_sync(P.bar, gen)) return;
+        const uint4* a = nullptr;
+        if (P.use_net) {
+            int cur = 0;
+            for (int l = 0; l < P.nconv; ++l, cur ^= 1) {
+                const uint4* X = P.h16[cur];
+                uint4* Y = P.h16[cur ^ 1];
+                const bool trans = l >= P.nconv / 2, out4 = P.cout[l] == kNetOut;
+                if (!trans) {
+                    if (out4) conv_bf_tiles<kNetOut, false, false>(X, Y, P.w[l], P.Nt, P.Nx, P.R, P.W, sm);
+                    else conv_bf_tiles<kNetC, false, false>(X, Y, P.w[l], P.Nt, P.Nx, P.R, P.W, sm);
+                } else {
+                    if (out4) conv_bf_tiles<kNetOut, true, false>(X, Y, P.w[l], P.Nt, P.Nx, P.R, P.W, sm);
+                    else conv_bf_tiles<kNetC, true, false>(X, Y, P.w[l], P.Nt, P.Nx, P.R, P.W, sm);
+                }
+                if (!pcg_sync(P.bar, gen)) return;
+            }
+            a = P.h16[cur];
+        }
+        pcg_z_body<false>(a, P.sig32, P.r, P.skip, P.z, P.q, P.part_z, P.V);
+        if (!pcg_sync(P.bar, gen)) return;
+    }
+}
+
+// Blocks of pcg_chunk_kernel that fit on the device at once (0: none).
+int pcg_chunk_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)pcg_chunk_kernel, kNetThreads, 0) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            per = 0;
+        }
+        maxg = per * nsm;
+    }
+    return maxg;
+}
 
 // z = M r, its partials and the scalars; X: the features (already written
 // by pcg_xr_kernel, or written here on the first round)
@@ -1675,6 +1853,53 @@ int pcg_iterations(LearnedNet* n, bool use_net, const DiracArgs& d, const PcgBuf
 {
     const int V = n->V, nb = n->grid;
     const float rw = (float)d.r;
+    if (n->persistent && count > 0 && (!use_net || n->tc_G == 1)) {
+        PcgChunk P = {};
+        P.z = b.z;
+        P.p[0] = b.p[0];
+        P.p[1] = b.p[1];
+        P.tmp = b.tmp;
+        P.q = b.q;
+        P.x = b.x;
+        P.r = b.r;
+        P.diag = n->diag32;
+        P.sig32 = n->sig32;
+        P.part_z = b.part_z;
+        P.part_pq = b.part_pq;
+        P.h16[0] = n->h16[0];
+        P.h16[1] = n->h16[1];
+        const int L = n->layers;
+        P.nconv = use_net ? 2 * L : 0;
+        for (int q = 0; q < P.nconv; ++q) {
+            const int l = q < L ? q : 2 * L - 1 - q;   // N's layers, then N^T's in reverse
+            P.w[q] = n->w + n->woff[l];
+            P.cout[q] = cout_of(n, l);
+        }
+        P.Nt = d.Nt;
+        P.Nx = d.Nx;
+        P.V = V;
+        P.R = n->tc_R;
+        P.W = n->tc_W;
+        P.rw = rw;
+        P.skip = n->skip;
+        P.use_net = use_net ? 1 : 0;
+        P.count = count;
+        P.parity = parity;
+        P.bar = n->pbar;
+        cudaMemsetAsync(n->pbar, 0, 2 * sizeof(unsigned), s);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nb);
+        cfg.blockDim = dim3(kNetThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        void* args[] = {&P};
+        cudaLaunchKernelExC(&cfg, (const void*)pcg_chunk_kernel, args);
+        return parity ^ (count & 1);
+    }
     for (int it = 0; it < count; ++it, parity ^= 1) {
         float* p = b.p[parity];
         float* pn = b.p[parity ^ 1];
@@ -1726,8 +1951,13 @@ static cudaError_t pcg_solve_once(LearnedNet* n, bool use_net, const double* sig
     // |r|^2 of the inner solve from the z kernel's partials (host sum)
     auto inner_rr = [&](double* out) -> cudaError_t {
         float* hf = reinterpret_cast<float*>(n->hpart);
+        unsigned* hbad = reinterpret_cast<unsigned*>(hf + n->grid);   // the persistent chunk's error word
+        *hbad = 0u;
         cudaError_t ce = cudaMemcpyAsync(hf, B.part_z + n->grid, sizeof(float) * n->grid, cudaMemcpyDeviceToHost, s);
+        if (ce == cudaSuccess && n->persistent)
+            ce = cudaMemcpyAsync(hbad, n->pbar + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+        if (ce == cudaSuccess && *hbad) ce = cudaErrorLaunchTimeout;   // a barrier wait gave up
         double t = 0.0;
         for (int i = 0; i < n->grid; ++i) t += hf[i];
         *out = t;
