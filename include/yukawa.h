@@ -309,8 +309,11 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps);
  * every step): the field uploaded from phi_in (V doubles, host; NULL keeps the
  * device field), the step, the field downloaded to phi_out (NULL: not read) and
  * the observables to obs (NULL: not read), with one synchronisation at the end
- * (the buffers may be reused when the call returns; pinned buffers take the
- * copies by DMA). */
+ * (the buffers may be reused when the call returns).  With pinned buffers
+ * (or NULL), after the first step, the call is one graph launch: the upload,
+ * the step, the downloads and the error word, the transfers made by kernels
+ * on the mapped buffers; one graph is kept per (chain, phi_in, phi_out), the
+ * last four. */
 int yk_langevin_step_io(yk_ctx* ctx, int chain, const double* phi_in, double* phi_out, yk_obs* obs);
 
 /* The autotuner (no reference counterpart: the reference's launch shapes are

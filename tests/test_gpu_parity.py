@@ -519,33 +519,51 @@ def test_autotune_keeps_results(ylib, cuda, monkeypatch):
         assert np.array_equal(got[c], want[c]), c
 
 
-def test_step_io_matches_separate_calls(ylib, cuda):
+@pytest.mark.parametrize("host", ["pageable", "pinned", "pinned_copies"])
+def test_step_io_matches_separate_calls(ylib, cuda, monkeypatch, host):
     # yk_langevin_step_io (upload, step, download, one synchronisation) gives
-    # the fields and observables of set_field + step + get_field + observables
-    yk = ylib
+    # the fields and observables of set_field + step + get_field + observables;
+    # with pinned fields after the first step it is one graph per pointer pair
+    # (two pairs alternating here, then no upload and no download), its
+    # transfers kernels on the mapped buffers or (YK_IO_KERNEL=0) copies
+    monkeypatch.setenv("YK_IO_KERNEL", "0" if host == "pinned_copies" else "1")
+    yk, torch = ylib, cuda
     p = params(yk, 32, 32, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
-    phi0 = np.random.default_rng(5).uniform(-1, 1, 32 * 32)
+    V = 32 * 32
+    phi0 = np.random.default_rng(5).uniform(-1, 1, V)
     want, obs_w = [], []
     with yk.Context(p) as ctx:
         ctx.set_field(phi0)
-        for _ in range(3):
+        for _ in range(7):
             ctx.step(1)
             want.append(ctx.get_field())
             obs_w.append(ctx.observables())
+
+    def buf(a):
+        if host == "pageable":
+            return a.copy()
+        t = torch.empty(V, dtype=torch.float64).pin_memory()
+        t.copy_(torch.from_numpy(a))
+        return t
+
+    def arr(b):
+        return b if host == "pageable" else b.numpy()
+
     with yk.Context(p) as ctx:
-        cur = phi0.copy()
-        out = np.empty_like(cur)
-        for s in range(3):
+        cur, out = buf(phi0), buf(np.zeros(V))
+        for s in range(6):
             o = ctx.step_io(cur, out)
-            assert np.array_equal(out, want[s]), s
+            assert np.array_equal(arr(out), want[s]), s
             assert o.status == 0 and o.steps == s + 1 and o.sum_phi == obs_w[s].sum_phi
+            assert o.cg_iterations == obs_w[s].cg_iterations
             cur, out = out, cur
         # no upload: the step continues from the device field; no download
         o = ctx.step_io(None, None)
-        assert o.steps == 4
+        assert o.steps == 7 and o.sum_phi == obs_w[6].sum_phi
+        assert np.array_equal(ctx.get_field(), want[6])
     with pytest.raises(TypeError):
         with yk.Context(p) as ctx:
-            ctx.step_io(np.zeros(32 * 32, dtype=np.float32))
+            ctx.step_io(np.zeros(V, dtype=np.float32))
 
 
 def test_deterministic(ylib, cuda):

@@ -142,6 +142,23 @@ struct yk_ctx {
     // step graph
     cudaGraphExec_t gexec = nullptr;
     bool graph_failed = false;
+    // yk_langevin_step_io with pinned host fields: the upload, the step, the
+    // downloads of the field, the observables and the error word as one
+    // graph per (chain, field pointers), the last few kept
+    struct IoGraph {
+        int c;
+        const double* in;
+        double* out;
+        cudaGraphExec_t exec;
+        uint64_t used;
+    };
+    std::vector<IoGraph> io;
+    uint64_t io_clock = 0;
+    bool io_failed = false;
+    void* io_pin = nullptr;   // pinned staging: the observables, then the error word
+    // the transfers as kernels on the mapped host buffers (YK_IO_KERNEL=0 at
+    // context creation: copy-engine copies)
+    bool io_kernel = true;
     int cg_grid = 0;
     int cg_kernel = 0;   // kernel of the last step CG launch (yk_profile.cg_kernel)
     // mixed precision with every step system fitting one 16-CTA cluster and
@@ -1041,6 +1058,8 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         ctx->autotune = !(ae && ae[0] == '0');
         const char* be = getenv("YK_CG_BALANCE");
         ctx->cg_balance = be && be[0] == '1';
+        const char* ie = getenv("YK_IO_KERNEL");
+        ctx->io_kernel = !(ie && ie[0] == '0');
     }
 
     ctx->ch.resize(n_chains);
@@ -1349,6 +1368,8 @@ int yk_ctx_destroy(yk_ctx* ctx)
     if (!ctx) return YK_OK;
     cudaStreamSynchronize(ctx->stream);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (auto& g : ctx->io) cudaGraphExecDestroy(g.exec);
+    if (ctx->io_pin) cudaFreeHost(ctx->io_pin);
     for (auto& r : ctx->recs) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -1708,10 +1729,122 @@ int yk_langevin_step(yk_ctx* ctx, int n_steps)
     return YK_OK;
 }
 
+namespace {
+
+// Pinned host memory (nullptr: no copy), with its device address when it is
+// mapped (else *dev = nullptr).
+bool pinned_host(const void* p, void** dev)
+{
+    *dev = nullptr;
+    if (!p) return true;
+    cudaPointerAttributes at = {};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type != cudaMemoryTypeHost) return false;
+    *dev = at.devicePointer;
+    return true;
+}
+
+static_assert(sizeof(yk_obs) % 8 == 0, "the observables are copied as 8-byte words");
+
+// The io graph of (c, in, out): found, or captured (the least recently used
+// of four replaced); nullptr when capture fails (the calls are then issued
+// one by one).
+yk_ctx::IoGraph* io_graph(yk_ctx* ctx, int c, const double* in, double* out, void* in_dev, void* out_dev)
+{
+    ++ctx->io_clock;
+    for (auto& g : ctx->io)
+        if (g.c == c && g.in == in && g.out == out) {
+            g.used = ctx->io_clock;
+            return &g;
+        }
+    if (ctx->io_failed) return nullptr;
+    if (!ctx->io_pin && cudaMallocHost(&ctx->io_pin, sizeof(yk_obs) + sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->io_pin = nullptr;
+        ctx->io_failed = true;
+        return nullptr;
+    }
+    const Chain& C = ctx->ch[c];
+    yk_obs* hobs = static_cast<yk_obs*>(ctx->io_pin);
+    int* herr = reinterpret_cast<int*>(hobs + 1);
+    void* pin_dev = nullptr;
+    if (cudaHostGetDevicePointer(&pin_dev, ctx->io_pin, 0) != cudaSuccess) {
+        cudaGetLastError();
+        pin_dev = nullptr;
+    }
+    // kernels through the mapped buffers, else copy-engine copies
+    const bool kern = ctx->io_kernel && pin_dev && (!in || in_dev) && (!out || out_dev);
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        bool rec = true;
+        if (in)
+            rec = (kern ? launch_io_load(static_cast<const double*>(in_dev), C.phi, C.V, ctx->stream)
+                        : cudaMemcpyAsync(C.phi, in, sizeof(double) * C.V, cudaMemcpyHostToDevice, ctx->stream)) ==
+                  cudaSuccess;
+        if (rec) rec = enqueue_step(ctx) == YK_OK;
+        if (rec && kern) {
+            yk_obs* dobs = static_cast<yk_obs*>(pin_dev);
+            rec = launch_io_store(C.phi, static_cast<double*>(out_dev), C.V, &ctx->d_chains[c].obs, dobs,
+                                  sizeof(yk_obs), ctx->d_err, reinterpret_cast<int*>(dobs + 1), ctx->stream) ==
+                  cudaSuccess;
+        } else if (rec) {
+            if (out)
+                rec = cudaMemcpyAsync(out, C.phi, sizeof(double) * C.V, cudaMemcpyDeviceToHost, ctx->stream) ==
+                      cudaSuccess;
+            if (rec)
+                rec = cudaMemcpyAsync(hobs, &ctx->d_chains[c].obs, sizeof(yk_obs), cudaMemcpyDeviceToHost,
+                                      ctx->stream) == cudaSuccess;
+            if (rec)
+                rec = cudaMemcpyAsync(herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) ==
+                      cudaSuccess;
+        }
+        const bool end_ok = cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess;
+        ok = rec && end_ok && g && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+    }
+    if (!ok) {
+        cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        ctx->io_failed = true;
+        return nullptr;
+    }
+    if (ctx->io.size() >= 4) {
+        auto lru = std::min_element(ctx->io.begin(), ctx->io.end(),
+                                    [](const yk_ctx::IoGraph& a, const yk_ctx::IoGraph& b) { return a.used < b.used; });
+        cudaGraphExecDestroy(lru->exec);
+        ctx->io.erase(lru);
+    }
+    ctx->io.push_back({c, in, out, exec, ctx->io_clock});
+    return &ctx->io.back();
+}
+
+}  // namespace
+
 int yk_langevin_step_io(yk_ctx* ctx, int c, const double* phi_in, double* phi_out, yk_obs* obs)
 {
     if (int rc = chain_ok(ctx, c)) return rc;
     const Chain& C = ctx->ch[c];
+    // after the first step (autotuning, the step graph): one graph launch and
+    // one synchronisation when the host fields are pinned
+    void *in_dev = nullptr, *out_dev = nullptr;
+    if (ctx->gexec && !ctx->pions && !ctx->profiling && pinned_host(phi_in, &in_dev) && pinned_host(phi_out, &out_dev)) {
+        if (yk_ctx::IoGraph* g = io_graph(ctx, c, phi_in, phi_out, in_dev, out_dev)) {
+            YK_CK(cudaGraphLaunch(g->exec, ctx->stream));
+            YK_CK(cudaStreamSynchronize(ctx->stream));
+            const yk_obs* hobs = static_cast<const yk_obs*>(ctx->io_pin);
+            if (obs) *obs = *hobs;
+            if (const int e = *reinterpret_cast<const int*>(hobs + 1)) {
+                set_error("a bounded device wait gave up (status %d)", e);
+                return YK_ETIMEOUT;
+            }
+            return YK_OK;
+        }
+    }
     if (phi_in)
         YK_CK(cudaMemcpyAsync(C.phi, phi_in, sizeof(double) * C.V, cudaMemcpyHostToDevice, ctx->stream));
     if (int rc = yk_langevin_step(ctx, 1)) return rc;
@@ -2125,6 +2258,8 @@ int yk_autotune(yk_ctx* ctx, yk_tune_result* out)
         cudaGraphExecDestroy(ctx->gexec);
         ctx->gexec = nullptr;
     }
+    for (auto& g : ctx->io) cudaGraphExecDestroy(g.exec);
+    ctx->io.clear();
     if (int rc = run_autotune(ctx)) return rc;
     if (out) *out = ctx->tune;
     return YK_OK;

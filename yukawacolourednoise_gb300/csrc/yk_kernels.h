@@ -68,6 +68,13 @@ int cg_predict_grid(const CGArgs& a, bool mixed);
 cudaError_t launch_force_drift(const StepArgs& s, const SysDev* sys, int mode, int K, cudaStream_t stream,
                                const CGState* st = nullptr);
 cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t stream);
+// yk_langevin_step_io's transfers through mapped pinned host memory (device
+// addresses of the host buffers): the field's upload; the field's download
+// (host null: none) with the observables' bytes (a multiple of 8) and the
+// error word
+cudaError_t launch_io_load(const double* host, double* phi, int V, cudaStream_t stream);
+cudaError_t launch_io_store(const double* phi, double* host, int V, const void* obs, void* hobs, size_t obs_bytes,
+                            const int* err, int* herr, cudaStream_t stream);
 
 // The pion extension's step (yk_pion.cu): white noise of the three pion
 // fields (3V), the complex sources eta_j of Philox stream `kind` (R x 8V), the

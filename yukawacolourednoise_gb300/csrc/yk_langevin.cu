@@ -205,6 +205,66 @@ cudaError_t launch_update(const StepArgs& s, const CGState* st, cudaStream_t str
 }
 
 // ---------------------------------------------------------------------------
+// Field transfers of yk_langevin_step_io through mapped pinned host memory:
+// the copy is a kernel in the step's graph instead of a copy-engine node per
+// buffer (the upload; the download of the field, the observables' words and
+// the error word in one launch).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void io_copy(const double* __restrict__ src, double* __restrict__ dst, int n)
+{
+    const int stride = gridDim.x * blockDim.x;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+        const double2* s2 = reinterpret_cast<const double2*>(src);
+        double2* d2 = reinterpret_cast<double2*>(dst);
+        for (int i = i0; i < n / 2; i += stride) d2[i] = s2[i];
+        if (i0 == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+    } else {
+        for (int i = i0; i < n; i += stride) dst[i] = src[i];
+    }
+}
+
+__global__ void __launch_bounds__(256) io_load_kernel(const double* __restrict__ host, double* __restrict__ phi, int V)
+{
+    io_copy(host, phi, V);
+}
+
+__global__ void __launch_bounds__(256) io_store_kernel(const double* __restrict__ phi, double* __restrict__ host, int V,
+                                                       const double* __restrict__ obs, double* __restrict__ hobs,
+                                                       int obs_words, const int* __restrict__ err, int* herr)
+{
+    if (host) io_copy(phi, host, V);
+    if (blockIdx.x == gridDim.x - 1) {
+        for (int i = threadIdx.x; i < obs_words; i += blockDim.x) hobs[i] = obs[i];
+        if (threadIdx.x == 0) *herr = *err;
+    }
+}
+
+namespace {
+int io_blocks(int V)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(1, std::min((V / 2 + 255) / 256, 2 * nsm));
+}
+}  // namespace
+
+cudaError_t launch_io_load(const double* host, double* phi, int V, cudaStream_t stream)
+{
+    io_load_kernel<<<io_blocks(V), 256, 0, stream>>>(host, phi, V);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_io_store(const double* phi, double* host, int V, const void* obs, void* hobs, size_t obs_bytes,
+                            const int* err, int* herr, cudaStream_t stream)
+{
+    io_store_kernel<<<io_blocks(V), 256, 0, stream>>>(phi, host, V, static_cast<const double*>(obs),
+                                                       static_cast<double*>(hobs), (int)(obs_bytes / 8), err, herr);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Observables used by the export block of main.cu:385-483.
 // ---------------------------------------------------------------------------
 __global__ void time_slices_kernel(const double* __restrict__ phi, double* out, int Nx)
