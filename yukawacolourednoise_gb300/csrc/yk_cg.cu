@@ -185,6 +185,45 @@ __device__ __forceinline__ FF ff_shfl_xor(FF a, int o)
     return FF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
 }
 
+// Float-float products and the reciprocal (Dekker's product with the exact
+// FMA error term; one Newton step from the FP32 reciprocal).  The explicitly
+// rounded intrinsics keep the compiler from contracting the product that the
+// error term subtracts.
+__device__ __forceinline__ FF ff_renorm(float p, float e)
+{
+    const float hi = __fadd_rn(p, e);
+    return FF{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return ff_renorm(p, e);
+}
+
+__device__ __forceinline__ FF ff_mul_f(FF a, float b)
+{
+    const float p = __fmul_rn(a.hi, b);
+    float e = __fmaf_rn(a.hi, b, -p);
+    e = __fmaf_rn(a.lo, b, e);
+    return ff_renorm(p, e);
+}
+
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, FF{-b.hi, -b.lo}); }
+__device__ __forceinline__ double dbl_of(FF a) { return (double)a.hi + (double)a.lo; }
+
+// 1 / d: y = rn(1 / d.hi), then y + y (1 - d y) with d y and the correction in
+// float-float (relative error about 2^-47)
+__device__ __forceinline__ FF ff_rcp(FF d)
+{
+    const float y = __frcp_rn(d.hi);
+    const FF e = ff_sub(FF{1.f, 0.f}, ff_mul_f(d, y));
+    return ff_add(FF{y, 0.f}, ff_mul_f(e, y));
+}
+
 // ---------------------------------------------------------------------------
 // Fixed-point sums (mixed single-system solves, real path).  Each tile adds
 // round(x * 2^e) of its four values (|r|^2, |Ap|^2, <p,Ap>, <r,Ap>) with a
@@ -1103,15 +1142,20 @@ __device__ void sum_partials(const CGArgs& a, int tile0, int ntiles, double* red
 #pragma unroll
             for (int c = 0; c < 6; ++c) red2[w * 6 + c] = make_float2(acc[c].hi, acc[c].lo);
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (w == 0) {
+            // the warps' sums by a fixed tree in warp 0 (the same order in every
+            // block), not a serial chain of float-float additions on thread 0
             FF t[6];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) t[c] = FF{red2[c].x, red2[c].y};
-            for (int u = 1; u < nw; ++u)
+            for (int c = 0; c < 6; ++c) t[c] = lane < nw ? FF{red2[lane * 6 + c].x, red2[lane * 6 + c].y} : FF{0.f, 0.f};
+            int o0 = 1;
+            while (o0 < nw) o0 <<= 1;
+            for (int o = o0 >> 1; o > 0; o >>= 1)
 #pragma unroll
-                for (int c = 0; c < 6; ++c) t[c] = ff_add(t[c], FF{red2[u * 6 + c].x, red2[u * 6 + c].y});
+                for (int c = 0; c < 6; ++c) t[c] = ff_add(t[c], ff_shfl_xor(t[c], o));
+            if (lane == 0)
 #pragma unroll
-            for (int c = 0; c < 6; ++c) s[c] = (double)t[c].hi + (double)t[c].lo;
+                for (int c = 0; c < 6; ++c) s[c] = (double)t[c].hi + (double)t[c].lo;
         }
     } else {
         if (w == 0) {
@@ -2296,18 +2340,20 @@ static size_t halo_smem_bytes(int own, int Nx)
 // Compact lattices: site (t, x) of parity q is t Nh + x / 2 of its class
 // (Nh = Nx / 2), full site 2 m + ((t + q) & 1).  a.sys are the systems'
 // compact views (Nx = Nh, V = V / 2, tiles over compact sites; the FP32
-// vectors compact; x = chi_e (FP64, compact) followed by rhs_e; t64 the odd
-// hops of the reliable updates and, at the end, chi in the full layout for the
+// vectors compact; x = chi_e (compact) followed by rhs_e; t64 the odd hops
+// of the reliable updates and, at the end, chi in the full layout for the
 // force, CGState::chi_ready); a.sys_full the full records (eta in b, sigma).
+// cg_eo_kernel keeps chi_e, rhs_e, the odd hops and dinv in float-float
+// (SiteFF); cg_eob_kernel keeps them in FP64.
 // A block owns the compact range [c0, c1), stages p, r, q of the previous
 // iteration on [c0 - 4Nh, c1 + 4Nh) and forms, in shared memory,
 //   w = -A_o^-1 H_oe p      on [c0 - 3Nh, c1 + 3Nh)   (odd)
 //   v = A_e p + H_eo w      on [c0 - 2Nh, c1 + 2Nh)   (even; = S^dag p)
 //   u = -A_o^-1 H^dag_oe v  on [c0 - Nh,  c1 + Nh)    (odd)
 //   q = A_e v + H^dag_eo u  on [c0, c1)               (even; = S v)
-// with the one reducing grid barrier per iteration, the scalar steps and the
-// FP64 reliable updates of cg_halo_kernel (its tile partials: |r|^2, |q|^2,
-// |v|^2 in the <p, Ap> slot, <r, q>).
+// with the one reducing grid barrier per iteration and the scalar steps of
+// cg_halo_kernel (its tile partials: |r|^2, |q|^2, |v|^2 in the <p, Ap> slot,
+// <r, q>); its reliable updates in float-float on the FP32 pipes.
 // cg_eo_kernel<true> owns 16 x 16 patches of the compact lattice instead of
 // whole rows: the widened patch (24 x 20 cells) holds 480 sites against
 // 1280 for two rows of 128 widened by four rows on each side, and the w, v,
@@ -2343,6 +2389,111 @@ __device__ __forceinline__ Site<double, 1> eo_gl(const double* in, int m, int Ve
     return dirac_combine<double, 1, DAG>(c, load_site<double, 1>(in, mu), load_site<double, 1>(in, md),
                                          load_site<double, 1>(in, m + dxu), load_site<double, 1>(in, m + dxd), diag, r,
                                          sp, sm);
+}
+
+// cg_eo_kernel's reliable updates, round 0 and reconstruction in float-float
+// (about 48 significant bits, on the FP32 pipes: GB300 issues FP64 at 1/64
+// of the FP32 rate and these passes were bound by it).  chi_e, rhs_e and the
+// odd intermediate keep the FP64 vectors' 32 bytes a compact site: four hi
+// words, then four lo words; 1 / A_o keeps its 8 bytes as (hi, lo).  Only the
+// kernel reads them; chi goes out to the force in FP64.
+struct SiteFF {
+    FF v[4];
+};
+
+__device__ __forceinline__ SiteFF ld_ff(const double* base, int m)
+{
+    const float4* p = reinterpret_cast<const float4*>(base) + 2 * (size_t)m;
+    const float4 h = p[0], l = p[1];
+    return SiteFF{{FF{h.x, l.x}, FF{h.y, l.y}, FF{h.z, l.z}, FF{h.w, l.w}}};
+}
+
+__device__ __forceinline__ void st_ff(double* base, int m, const SiteFF& s)
+{
+    float4* p = reinterpret_cast<float4*>(base) + 2 * (size_t)m;
+    p[0] = make_float4(s.v[0].hi, s.v[1].hi, s.v[2].hi, s.v[3].hi);
+    p[1] = make_float4(s.v[0].lo, s.v[1].lo, s.v[2].lo, s.v[3].lo);
+}
+
+__device__ __forceinline__ FF ld_ff1(const double* base, int m)
+{
+    const float2 v = reinterpret_cast<const float2*>(base)[m];
+    return FF{v.x, v.y};
+}
+
+__device__ __forceinline__ void st_ff1(double* base, int m, FF v)
+{
+    reinterpret_cast<float2*>(base)[m] = make_float2(v.hi, v.lo);
+}
+
+// a source vector's site as float-float: the Langevin sources are FP32 normals
+// (exact in FP32) when generated; other right-hand sides are split
+__device__ __forceinline__ SiteFF ff_site_of(const Site<double, 1>& e, bool exact32)
+{
+    SiteFF s;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s.v[i] = exact32 ? FF{(float)e.v[i], 0.f} : ff_of(e.v[i]);
+    return s;
+}
+
+// dirac_combine's hop coefficients in float-float: P = -(r + 1) / 2,
+// M = -(r - 1) / 2, A = -r / 2 (the time hops take +-P and +-M by the
+// antiperiodic signs, the space hops A and +-1/2)
+struct HopFF {
+    FF P, M, A;
+};
+
+__device__ __forceinline__ HopFF hop_ff(double r)
+{
+    return HopFF{ff_of(-0.5 * (r + 1.0)), ff_of(-0.5 * (r - 1.0)), ff_of(-0.5 * r)};
+}
+
+__device__ __forceinline__ FF ff_sign(FF a, float s) { return FF{s * a.hi, s * a.lo}; }
+
+// dirac_combine<float-float, K = 1, DAG> with the same order of terms:
+// MODE 0: H alone; 1: c + H; 2: diag c + H
+template <bool DAG, int MODE>
+__device__ __forceinline__ SiteFF combine_ff(const SiteFF& c, FF diag, const SiteFF& tu, const SiteFF& td,
+                                             const SiteFF& xu, const SiteFF& xd, const HopFF& h, float sp, float sm)
+{
+    const FF cu_up = ff_sign(DAG ? h.P : h.M, sp), cd_up = ff_sign(DAG ? h.M : h.P, sp);
+    const FF cu_dn = ff_sign(DAG ? h.M : h.P, sm), cd_dn = ff_sign(DAG ? h.P : h.M, sm);
+    const float bx = DAG ? -0.5f : 0.5f;
+    SiteFF o;
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+        const int iu = 2 * f, id = 2 * f + 1;
+        FF ou, od;
+        if (MODE == 0) {
+            ou = ff_mul(cu_up, tu.v[iu]);
+            od = ff_mul(cd_up, tu.v[id]);
+        } else {
+            ou = MODE == 1 ? c.v[iu] : ff_mul(diag, c.v[iu]);
+            od = MODE == 1 ? c.v[id] : ff_mul(diag, c.v[id]);
+            ou = ff_add(ou, ff_mul(cu_up, tu.v[iu]));
+            od = ff_add(od, ff_mul(cd_up, tu.v[id]));
+        }
+        ou = ff_add(ou, ff_mul(cu_dn, td.v[iu]));
+        od = ff_add(od, ff_mul(cd_dn, td.v[id]));
+        const FF dfu = ff_sub(xu.v[id], xd.v[id]), dfd = ff_sub(xu.v[iu], xd.v[iu]);
+        ou = ff_add(ou, FF{bx * dfu.hi, bx * dfu.lo});
+        od = ff_add(od, FF{bx * dfd.hi, bx * dfd.lo});
+        ou = ff_add(ou, ff_mul(h.A, ff_add(xu.v[iu], xd.v[iu])));
+        od = ff_add(od, ff_mul(h.A, ff_add(xu.v[id], xd.v[id])));
+        o.v[iu] = ou;
+        o.v[id] = od;
+    }
+    return o;
+}
+
+// eo_gl in float-float: the neighbours of compact m in a float-float vector
+template <bool DAG, int MODE>
+__device__ __forceinline__ SiteFF eo_ff(const double* in, int m, int Ve, int Nh, int dxu, int dxd, const SiteFF& c,
+                                        FF diag, const HopFF& h, float sp, float sm)
+{
+    const int mu = m + Nh >= Ve ? m + Nh - Ve : m + Nh, md = m - Nh < 0 ? m - Nh + Ve : m - Nh;
+    return combine_ff<DAG, MODE>(c, diag, ld_ff(in, mu), ld_ff(in, md), ld_ff(in, m + dxu), ld_ff(in, m + dxd), h, sp,
+                                 sm);
 }
 
 // Patch geometry of cg_eo_kernel<PX> (PX > 0): each block owns kPT rows x PX
@@ -2383,6 +2534,7 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
     __shared__ SysDev S;    // the compact view
     __shared__ SysDev SF;   // the full record
     __shared__ CGArgs sa;
+    __shared__ HopFF s_hop;   // the hop coefficients in float-float (one thread's FP64 work)
     const int tb = a.tile_begin + blockIdx.x * a.tiles_per_block;
     const int te = min(tb + a.tiles_per_block, a.tile_end);
     setup_block(a, tb, te, sl, &nsl, tslot, &deps);
@@ -2417,6 +2569,7 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
         S = a.sys[a.sys_first];
         SF = a.sys_full[a.sys_first];
         sa = a;
+        s_hop = hop_ff(a.sys[a.sys_first].r);
     }
     __syncthreads();
     const int Nt = S.Nt, Nh = S.Nx, Ve = S.V;
@@ -2488,7 +2641,6 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
     float* dep = reinterpret_cast<float*>(Vp + NB);   // A_e on [2SB, NB - 2SB)
     float* dip = dep + NB;                             // 1 / A_o on [SB, NB - SB)
     const float rw = (float)S.r;
-    const double r64 = S.r;
     for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += NT) {
         int t, b, du, dd;
         cell(j, 0, t, b, du, dd);
@@ -2642,44 +2794,46 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
                                          prefetch);
     };
 
-    // the reliable update of iteration k: fold chi_e += xs + alpha v_{k-1} in
-    // FP64; u = -A_o^-1 H^dag_oe chi_e on the own odd sites (t64, compact);
-    // r = rhs_e - (A_e chi_e + H^dag_eo u) on the own even sites -> r32[cur];
-    // partials |r|^2, <r, p_{k-1}>
+    // the reliable update of iteration k, in float-float: fold chi_e += xs +
+    // alpha v_{k-1}; u = -A_o^-1 H^dag_oe chi_e on the own odd sites (t64,
+    // compact); r = rhs_e - (A_e chi_e + H^dag_eo u) on the own even sites ->
+    // r32[cur]; partials |r|^2, <r, p_{k-1}> (FP32 squares of the FP32 r)
     auto reliable = [&](int cur, int prv) -> bool {
-        const SysLocal& L = sl[0];
         double* chi = S.x;
+        const HopFF hop = s_hop;
+        const float al = sl[0].f_alpha_re;
         for (int o = threadIdx.x; o < own; o += NT) {
             const int m = own_m(o);
-            Site<double, K> xv = load_site<double, K>(chi, m);
+            SiteFF xv = ld_ff(chi, m);
             const Site<W, K> xs = ld_sm(X_st, o);
             const Site<W, K> vv = ld_sm(V_own, o);
             Site<W, K> zw;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                xv.v[i] += (double)xs.v[i];
-                xv.v[i] = fma(L.alpha_re, (double)vv.v[i], xv.v[i]);
+                const float pr = __fmul_rn(al, vv.v[i]);   // alpha v exactly: (pr, its FMA error)
+                xv.v[i] = ff_add(xv.v[i], FF{xs.v[i], 0.f});
+                xv.v[i] = ff_add(xv.v[i], FF{pr, __fmaf_rn(al, vv.v[i], -pr)});
                 zw.v[i] = W(0);
             }
-            store_site<double, K>(chi, m, xv);
+            st_ff(chi, m, xv);
             st_sm(X_st, o, zw);
         }
         YK_TMARK(7);
         if (!nsync(a, ++epoch, deps)) return false;
         YK_TMARK(8);
-        Site<double, K> zero;
+        SiteFF zero;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
+        for (int i = 0; i < 4; ++i) zero.v[i] = FF{0.f, 0.f};
         for (int o = threadIdx.x; o < own; o += NT) {
             const int m = own_m(o);
             int t, b, du, dd;
             eo_geom(m, 1, Nh, sh, t, b, du, dd);
-            const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
-            Site<double, K> h = eo_gl<true>(chi, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
-            const double s = -S.dinv[m];
+            const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
+            SiteFF h = eo_ff<true, 0>(chi, m, Ve, Nh, du, dd, zero, FF{0.f, 0.f}, hop, sp, sm);
+            const FF s = ld_ff1(S.dinv, m);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) h.v[i] *= s;
-            store_site<double, K>(S.t64, m, h);
+            for (int i = 0; i < 4; ++i) h.v[i] = ff_mul(FF{-s.hi, -s.lo}, h.v[i]);
+            st_ff(S.t64, m, h);
         }
         YK_TMARK(9);
         if (!nsync(a, ++epoch, deps)) return false;
@@ -2690,34 +2844,28 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
             const int o = (tile - tb) * kTile + ts;
             const bool on = tile_on && o < own;
             const int m = on ? own_m(o) : 0;
-            double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            float v0 = 0.f, v2 = 0.f;
             if (on) {
                 int t, b, du, dd;
                 eo_geom(m, 0, Nh, sh, t, b, du, dd);
-                const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
-                const double de = 2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b];
-                const Site<double, K> sx =
-                    eo_gl<true>(S.t64, m, Ve, Nh, du, dd, load_site<double, K>(chi, m), de, r64, sp, sm);
-                const Site<double, K> bv = load_site<double, K>(rhs_e, m);
+                const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
+                const FF de = ff_of(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b]);
+                const SiteFF sx = eo_ff<true, 2>(S.t64, m, Ve, Nh, du, dd, ld_ff(chi, m), de, hop, sp, sm);
+                const SiteFF bv = ld_ff(rhs_e, m);
                 const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
-                Site<double, K> rd, pd;
                 Site<W, K> rw32;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    rd.v[i] = bv.v[i] - sx.v[i];
-                    rw32.v[i] = (float)rd.v[i];
-                    pd.v[i] = (double)pw.v[i];
-                }
+                for (int i = 0; i < 4; ++i) rw32.v[i] = ff_sub(bv.v[i], sx.v[i]).hi;
                 YK_ST(W, K, S.r32[cur], m, rw32);
-                v[0] = site_norm2<double, K>(rd);
-                site_dot<double, K>(rd, pd, v[2], v[3]);
+                W dummy;
+                v0 = site_norm2<W, K>(rw32);
+                site_dot<W, K>(rw32, pw, v2, dummy);
             }
-            // the two reduced slots only (each conversion is FP64 work)
             FF f[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
-            f[0] = ff_of(v[0]);
-            f[2] = ff_of(v[2]);
+            f[0] = FF{v0, 0.f};
+            f[2] = FF{v2, 0.f};
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         }
         YK_TMARK(11);
@@ -2725,9 +2873,10 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
     };
 
     // ---------------- round 0: eta on the own sites of both classes (kept in
-    // b for the force); on the odd ones 1 / A_o (dinv, the one FP64 division
-    // per site of the solve) and -A_o^-1 eta_o (t64, compact); chi_e = 0;
-    // rhs_e; r_0 = p_0 = rhs_e
+    // b for the force); on the odd ones 1 / A_o (dinv: the float-float
+    // reciprocal of the FP64 diagonal) and -A_o^-1 eta_o (t64, compact);
+    // chi_e = 0; rhs_e; r_0 = p_0 = rhs_e
+    const bool eta32 = SF.gen_eta != 0;   // generated sources are FP32 normals
     for (int o = threadIdx.x; o < 2 * own; o += NT) {
         const int m = own_m(o >> 1), q = o & 1;
         int t, b, du, dd;
@@ -2736,12 +2885,13 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
         const Site<double, K> bv = SF.gen_eta ? eta_of_step<K>(SF, n, a.eta_kind) : load_site<double, K>(SF.b, n);
         if (SF.gen_eta) store_site<double, K>(SF.b, n, bv);
         if (q) {
-            const double inv = 1.0 / (2.0 * S.r + S.m0 + S.g * SF.sigma[n]);
-            S.dinv[m] = inv;
-            Site<double, K> h;
+            const FF inv = ff_rcp(ff_of(2.0 * S.r + S.m0 + S.g * SF.sigma[n]));
+            st_ff1(S.dinv, m, inv);
+            const SiteFF e = ff_site_of(bv, eta32);
+            SiteFF h;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) h.v[i] = -inv * bv.v[i];
-            store_site<double, K>(S.t64, m, h);
+            for (int i = 0; i < 4; ++i) h.v[i] = ff_mul(FF{-inv.hi, -inv.lo}, e.v[i]);
+            st_ff(S.t64, m, h);
         }
     }
     YK_TMARK(12);
@@ -2760,21 +2910,24 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
     if (!nsync(a, ++epoch, deps)) return;
     YK_TMARK(13);
     // 1 / A_o in FP32 on the widened range, from the owners' dinv
-    for (int j = SB + threadIdx.x; j < NB - SB; j += NT) dip[j] = (float)S.dinv[buf_m(j)];
-    for (int o = threadIdx.x; o < own; o += NT) {
-        const int m = own_m(o);
-        int t, b, du, dd;
-        eo_geom(m, 0, Nh, sh, t, b, du, dd);
-        const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
-        const Site<double, K> e = load_site<double, K>(SF.b, 2 * m + b);
-        // eta_e + H^dag_eo (-A_o^-1 eta_o)
-        const Site<double, K> rh = eo_gl<true>(S.t64, m, Ve, Nh, du, dd, e, 1.0, r64, sp, sm);
-        store_site<double, K>(const_cast<double*>(rhs_e), m, rh);
-        Site<W, K> rw32;
+    for (int j = SB + threadIdx.x; j < NB - SB; j += NT) dip[j] = ld_ff1(S.dinv, buf_m(j)).hi;
+    {
+        const HopFF hop = s_hop;
+        for (int o = threadIdx.x; o < own; o += NT) {
+            const int m = own_m(o);
+            int t, b, du, dd;
+            eo_geom(m, 0, Nh, sh, t, b, du, dd);
+            const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
+            const SiteFF e = ff_site_of(load_site<double, K>(SF.b, 2 * m + b), eta32);
+            // eta_e + H^dag_eo (-A_o^-1 eta_o)
+            const SiteFF rh = eo_ff<true, 1>(S.t64, m, Ve, Nh, du, dd, e, FF{1.f, 0.f}, hop, sp, sm);
+            st_ff(const_cast<double*>(rhs_e), m, rh);
+            Site<W, K> rw32;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) rw32.v[i] = (float)rh.v[i];
-        YK_ST(W, K, S.r32[0], m, rw32);
-        YK_ST(W, K, S.p32[0], m, rw32);
+            for (int i = 0; i < 4; ++i) rw32.v[i] = rh.v[i].hi;
+            YK_ST(W, K, S.r32[0], m, rw32);
+            YK_ST(W, K, S.p32[0], m, rw32);
+        }
     }
     YK_TMARK(14);
     if (!nsync(a, ++epoch, deps)) return;
@@ -2831,24 +2984,31 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
     // chi of both classes in the full layout for the force (t64): every
     // block's final chi_e and its own odd sites' chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
     if (!nsync(a, ++epoch, deps)) return;
-    Site<double, K> zero;
+    {
+        const HopFF hop = s_hop;
+        SiteFF zero;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) zero.v[i] = 0.0;
-    for (int o = threadIdx.x; o < own; o += NT) {
-        const int m = own_m(o);
-        int t, b, du, dd;
-        eo_geom(m, 0, Nh, sh, t, b, du, dd);
-        store_site<double, K>(SF.t64, 2 * m + b, load_site<double, K>(S.x, m));
-        eo_geom(m, 1, Nh, sh, t, b, du, dd);
-        const double sp = (t + 1 == Nt) ? -1.0 : 1.0, sm = (t == 0) ? -1.0 : 1.0;
-        const Site<double, K> h = eo_gl<true>(S.x, m, Ve, Nh, du, dd, zero, 0.0, r64, sp, sm);
-        const int n = 2 * m + b;
-        const Site<double, K> e = load_site<double, K>(SF.b, n);
-        const double inv = S.dinv[m];
-        Site<double, K> co;
+        for (int i = 0; i < 4; ++i) zero.v[i] = FF{0.f, 0.f};
+        for (int o = threadIdx.x; o < own; o += NT) {
+            const int m = own_m(o);
+            int t, b, du, dd;
+            eo_geom(m, 0, Nh, sh, t, b, du, dd);
+            const SiteFF xe = ld_ff(S.x, m);
+            Site<double, K> ce;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) co.v[i] = (e.v[i] - h.v[i]) * inv;
-        store_site<double, K>(SF.t64, n, co);
+            for (int i = 0; i < 4; ++i) ce.v[i] = dbl_of(xe.v[i]);
+            store_site<double, K>(SF.t64, 2 * m + b, ce);
+            eo_geom(m, 1, Nh, sh, t, b, du, dd);
+            const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
+            const SiteFF h = eo_ff<true, 0>(S.x, m, Ve, Nh, du, dd, zero, FF{0.f, 0.f}, hop, sp, sm);
+            const int n = 2 * m + b;
+            const SiteFF e = ff_site_of(load_site<double, K>(SF.b, n), eta32);
+            const FF inv = ld_ff1(S.dinv, m);
+            Site<double, K> co;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) co.v[i] = dbl_of(ff_mul(ff_sub(e.v[i], h.v[i]), inv));
+            store_site<double, K>(SF.t64, n, co);
+        }
     }
     // t64 holds chi however the solve ended (also when it retired at k = 0)
     if (blockIdx.x == 0 && threadIdx.x == 0) a.st[a.sys_first].chi_ready = 1;
