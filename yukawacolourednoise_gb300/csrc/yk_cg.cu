@@ -2343,8 +2343,8 @@ static size_t halo_smem_bytes(int own, int Nx)
 // vectors compact; x = chi_e (compact) followed by rhs_e; t64 the odd hops
 // of the reliable updates and, at the end, chi in the full layout for the
 // force, CGState::chi_ready); a.sys_full the full records (eta in b, sigma).
-// cg_eo_kernel keeps chi_e, rhs_e, the odd hops and dinv in float-float
-// (SiteFF); cg_eob_kernel keeps them in FP64.
+// Both even-odd kernels keep chi_e, rhs_e, the odd hops and dinv in
+// float-float (SiteFF).
 // A block owns the compact range [c0, c1), stages p, r, q of the previous
 // iteration on [c0 - 4Nh, c1 + 4Nh) and forms, in shared memory,
 //   w = -A_o^-1 H_oe p      on [c0 - 3Nh, c1 + 3Nh)   (odd)
@@ -2446,6 +2446,14 @@ struct HopFF {
 __device__ __forceinline__ HopFF hop_ff(double r)
 {
     return HopFF{ff_of(-0.5 * (r + 1.0)), ff_of(-0.5 * (r - 1.0)), ff_of(-0.5 * r)};
+}
+
+// the same from r split once (the per-site form: four FP64 operations)
+__device__ __forceinline__ HopFF hop_of_r(double r)
+{
+    const FF rr = ff_of(r);
+    const FF rp = ff_add(rr, FF{1.f, 0.f}), rm = ff_add(rr, FF{-1.f, 0.f});
+    return HopFF{FF{-0.5f * rp.hi, -0.5f * rp.lo}, FF{-0.5f * rm.hi, -0.5f * rm.lo}, FF{-0.5f * rr.hi, -0.5f * rr.lo}};
 }
 
 __device__ __forceinline__ FF ff_sign(FF a, float s) { return FF{s * a.hi, s * a.lo}; }
@@ -3055,11 +3063,11 @@ __global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
 //   P1 (even)  r, p, chi increment of the own site; w = -A_o^-1 H_oe p at the
 //              compact index's odd site, the neighbours' p formed from the
 //              previous iteration's r, q, p (the same arithmetic as theirs);
-//              kRu: fold chi_e += xs + alpha v in FP64
+//              kRu: fold chi_e += xs + alpha v in float-float
 //   P2 (even)  v = A_e p + H_eo w (= S^dag p);  kRu: R2 u = -A_o^-1 H^dag_oe
-//              chi_e in FP64 (t64)
+//              chi_e in float-float (t64)
 //   P3 (odd)   u = -A_o^-1 H^dag_oe v;  kRu: R3 r = rhs_e - (A_e chi_e +
-//              H^dag_eo u) in FP64, partials |r|^2, <r, p_{k-1}>
+//              H^dag_eo u) in float-float, partials |r|^2, <r, p_{k-1}>
 //   P4 (even)  q = A_e v + H^dag_eo u (= S v), tile partials |r|^2, |q|^2,
 //              |v|^2, <r, q>; the reducing barrier.
 // A system's update thus costs no round of the others: each keeps its own
@@ -3184,7 +3192,7 @@ __device__ bool eob_reduce(const CGArgs& a, unsigned& gen, int k, double* red, i
 // Modes of the round from the published coefficient words of every system;
 // *nact (every thread) = how many threads saw a system still iterating.
 __device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_mode, int* s_par, float* s_fa,
-                               float* s_fb, float* s_fc, double* s_da, int* nact)
+                               float* s_fb, float* s_fc, int* nact)
 {
     int bad = 0, act = 0;
     for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
@@ -3197,7 +3205,6 @@ __device__ bool eob_load_coefs(const CGArgs& a, unsigned gen, int nsys, int* s_m
             s_fa[q] = (float)v.alpha_re;
             s_fb[q] = (float)v.beta;
             s_fc[q] = (float)v.c_re;
-            s_da[q] = v.alpha_re;
             act += v.mode != kIdle;
         }
     }
@@ -3214,7 +3221,6 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     __shared__ double red[128];
     __shared__ int s_mode[kEobMaxSys], s_par[kEobMaxSys], s_nt[kEobMaxSys], s_t0[kEobMaxSys], s_pre[kEobMaxSys + 1];
     __shared__ float s_fa[kEobMaxSys], s_fb[kEobMaxSys], s_fc[kEobMaxSys];
-    __shared__ double s_da[kEobMaxSys];
     __shared__ int s_active, s_ru;   // the scalar step's counters (unused here)
     const int nsys = a.sys_count;
     for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
@@ -3224,7 +3230,6 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
         s_mode[q] = kStep;
         s_par[q] = 0;
         s_fa[q] = s_fb[q] = s_fc[q] = 0.f;
-        s_da[q] = 0.0;
     }
     __syncthreads();
     if (*(volatile int*)a.err) return;
@@ -3308,17 +3313,19 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
             const int mode = init ? kInit : s_mode[q];
             const int cur = s_par[q], prv = cur ^ 1;
             if (mode == kRu) {
-                Site<double, K> xv = YK_LD(double, K, S.x, m);
+                SiteFF xv = ld_ff(S.x, m);
                 const Site<W, K> xs = YK_LD(W, K, S.xs32, m);
                 const Site<W, K> vv = YK_LD(W, K, S.v32, m);
+                const float al = s_fa[q];
                 Site<W, K> zw;
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
-                    xv.v[e] += (double)xs.v[e];
-                    xv.v[e] = fma(s_da[q], (double)vv.v[e], xv.v[e]);
+                    const float pr = __fmul_rn(al, vv.v[e]);   // alpha v exactly: (pr, its FMA error)
+                    xv.v[e] = ff_add(xv.v[e], FF{xs.v[e], 0.f});
+                    xv.v[e] = ff_add(xv.v[e], FF{pr, __fmaf_rn(al, vv.v[e], -pr)});
                     zw.v[e] = W(0);
                 }
-                YK_ST(double, K, S.x, m, xv);
+                st_ff(S.x, m, xv);
                 YK_ST(W, K, S.xs32, m, zw);
                 return;
             }
@@ -3435,13 +3442,14 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
             if (c == 0) {
                 S.diag32[m] = (float)d;
             } else {
-                const double inv = 1.0 / d;
-                S.dinv[m] = inv;
-                S.diag32[Ve + m] = (float)inv;
-                Site<double, K> h;
+                const FF inv = ff_rcp(ff_of(d));
+                st_ff1(S.dinv, m, inv);
+                S.diag32[Ve + m] = inv.hi;
+                const SiteFF e = ff_site_of(bv, S.gen_eta != 0);
+                SiteFF h;
 #pragma unroll
-                for (int e = 0; e < 4; ++e) h.v[e] = -inv * bv.v[e];
-                store_site<double, K>(S.t64, m, h);
+                for (int e2 = 0; e2 < 4; ++e2) h.v[e2] = ff_mul(FF{-inv.hi, -inv.lo}, e.v[e2]);
+                st_ff(S.t64, m, h);
             }
         }
         Site<double, K> z;
@@ -3460,13 +3468,13 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     for_sites(kAll, [&](const SysDev& S, int, int m, int, bool, bool on) {
         if (!on) return;
         const Geo g = geo(S, m, 0);
-        const Site<double, K> e = load_site<double, K>(S.b, 2 * m + g.b);
-        const Site<double, K> rh =
-            eo_gl<true>(S.t64, m, S.V, S.Nx, g.du, g.dd, e, 1.0, S.r, (double)g.sp, (double)g.sm);
-        store_site<double, K>(S.x + 4 * (size_t)S.V, m, rh);
+        const SiteFF e = ff_site_of(load_site<double, K>(S.b, 2 * m + g.b), S.gen_eta != 0);
+        const SiteFF rh =
+            eo_ff<true, 1>(S.t64, m, S.V, S.Nx, g.du, g.dd, e, FF{1.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
+        st_ff(S.x + 4 * (size_t)S.V, m, rh);
         Site<W, K> rw;
 #pragma unroll
-        for (int e2 = 0; e2 < 4; ++e2) rw.v[e2] = (float)rh.v[e2];
+        for (int e2 = 0; e2 < 4; ++e2) rw.v[e2] = rh.v[e2].hi;
         YK_ST(W, K, S.r32[0], m, rw);
         YK_ST(W, K, S.p32[0], m, rw);
     });
@@ -3488,7 +3496,7 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     while (k <= kmax) {
         YK_TMARK(8);
         int nact = 0;
-        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, s_da, &nact)) return;
+        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, &nact)) return;
         if (nact == 0) break;
         YK_TMARK(0);
         pass_p1(false);
@@ -3496,53 +3504,48 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
         if (!eob_barrier(a, gen)) return;
         YK_TMARK(2);
         pass_p2(kP2);
-        // R2: u = -A_o^-1 H^dag_oe chi_e (FP64, odd, t64)
+        // R2: u = -A_o^-1 H^dag_oe chi_e (float-float, odd, t64)
         for_sites(kPR, [&](const SysDev& S, int, int m, int, bool, bool on) {
             if (!on) return;
             const Geo g = geo(S, m, 1);
-            Site<double, K> zero;
+            SiteFF zero;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) zero.v[e] = 0.0;
-            Site<double, K> h =
-                eo_gl<true>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, 0.0, S.r, (double)g.sp, (double)g.sm);
-            const double sc = -S.dinv[m];
+            for (int e = 0; e < 4; ++e) zero.v[e] = FF{0.f, 0.f};
+            SiteFF h = eo_ff<true, 0>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, FF{0.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
+            const FF sc = ld_ff1(S.dinv, m);
 #pragma unroll
-            for (int e = 0; e < 4; ++e) h.v[e] *= sc;
-            store_site<double, K>(S.t64, m, h);
+            for (int e = 0; e < 4; ++e) h.v[e] = ff_mul(FF{-sc.hi, -sc.lo}, h.v[e]);
+            st_ff(S.t64, m, h);
         });
         YK_TMARK(3);
         if (!eob_barrier(a, gen)) return;
         YK_TMARK(4);
         pass_p3(kP2);
-        // R3: r = rhs_e - (A_e chi_e + H^dag_eo u) in FP64; |r|^2, <r, p_{k-1}>
+        // R3: r = rhs_e - (A_e chi_e + H^dag_eo u) in float-float; |r|^2,
+        // <r, p_{k-1}> (FP32 squares of the FP32 r)
         for_sites(kPR, [&](const SysDev& S, int q, int m, int tile, bool tile_on, bool on) {
             const int cur = s_par[q], prv = cur ^ 1;
-            double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            float v0 = 0.f, v2 = 0.f;
             if (on) {
                 const Geo g = geo(S, m, 0);
-                const double de = 2.0 * S.r + S.m0 + S.g * S.sigma[2 * m + g.b];
-                const Site<double, K> sx = eo_gl<true>(S.t64, m, S.V, S.Nx, g.du, g.dd, load_site<double, K>(S.x, m),
-                                                       de, S.r, (double)g.sp, (double)g.sm);
-                const Site<double, K> bv = load_site<double, K>(S.x + 4 * (size_t)S.V, m);
+                const FF de = ff_of(2.0 * S.r + S.m0 + S.g * S.sigma[2 * m + g.b]);
+                const SiteFF sx =
+                    eo_ff<true, 2>(S.t64, m, S.V, S.Nx, g.du, g.dd, ld_ff(S.x, m), de, hop_of_r(S.r), g.sp, g.sm);
+                const SiteFF bv = ld_ff(S.x + 4 * (size_t)S.V, m);
                 const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
-                Site<double, K> rd, pd;
                 Site<W, K> rw;
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    rd.v[e] = bv.v[e] - sx.v[e];
-                    rw.v[e] = (float)rd.v[e];
-                    pd.v[e] = (double)pw.v[e];
-                }
+                for (int e = 0; e < 4; ++e) rw.v[e] = ff_sub(bv.v[e], sx.v[e]).hi;
                 YK_ST(W, K, S.r32[cur], m, rw);
-                v[0] = site_norm2<double, K>(rd);
-                site_dot<double, K>(rd, pd, v[2], v[3]);
+                W dummy;
+                v0 = site_norm2<W, K>(rw);
+                site_dot<W, K>(rw, pw, v2, dummy);
             }
-            // the two reduced slots only (each conversion is FP64 work)
             FF f[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
-            f[0] = ff_of(v[0]);
-            f[2] = ff_of(v[2]);
+            f[0] = FF{v0, 0.f};
+            f[2] = FF{v2, 0.f};
             put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         });
         YK_TMARK(5);
@@ -3569,19 +3572,22 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
     for_sites(kAll | (1 << kIdle), [&](const SysDev& S, int, int m, int, bool, bool on) {
         if (!on) return;
         Geo g = geo(S, m, 0);
-        store_site<double, K>(S.t64, 2 * m + g.b, load_site<double, K>(S.x, m));
-        g = geo(S, m, 1);
-        Site<double, K> zero;
+        const SiteFF xe = ld_ff(S.x, m);
+        Site<double, K> ce;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) zero.v[e] = 0.0;
-        const Site<double, K> h =
-            eo_gl<true>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, 0.0, S.r, (double)g.sp, (double)g.sm);
+        for (int e = 0; e < 4; ++e) ce.v[e] = dbl_of(xe.v[e]);
+        store_site<double, K>(S.t64, 2 * m + g.b, ce);
+        g = geo(S, m, 1);
+        SiteFF zero;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) zero.v[e] = FF{0.f, 0.f};
+        const SiteFF h = eo_ff<true, 0>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, FF{0.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
         const int n = 2 * m + g.b;
-        const Site<double, K> e = load_site<double, K>(S.b, n);
-        const double inv = S.dinv[m];
+        const SiteFF e = ff_site_of(load_site<double, K>(S.b, n), S.gen_eta != 0);
+        const FF inv = ld_ff1(S.dinv, m);
         Site<double, K> co;
 #pragma unroll
-        for (int e2 = 0; e2 < 4; ++e2) co.v[e2] = (e.v[e2] - h.v[e2]) * inv;
+        for (int e2 = 0; e2 < 4; ++e2) co.v[e2] = dbl_of(ff_mul(ff_sub(e.v[e2], h.v[e2]), inv));
         store_site<double, K>(S.t64, n, co);
     });
     if (blockIdx.x == 0)
