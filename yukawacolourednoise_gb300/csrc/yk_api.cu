@@ -1310,6 +1310,7 @@ int yk_ctx_create(const yk_params* params, int n_chains, yk_ctx** out)
         H.ntiles = C.nsite_tiles;
         H.m2 = C.a.m2;
         H.lambda = C.a.lambda;
+        H.lambda6 = C.a.lambda / 6.0;
         H.g = C.a.g;
         H.m0 = C.a.m0;
         H.r = C.a.r;

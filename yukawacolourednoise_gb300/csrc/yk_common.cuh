@@ -469,7 +469,7 @@ __device__ __forceinline__ double step_drift(const ChainDev& C, int n, double F)
     const Nbr nb = neighbours(n, C.Nt, C.Nx);
     const double v = C.phi[n];
     double d = F;
-    d += v * (C.m2 + (C.lambda / 6.0) * (v * v));
+    d += v * (C.m2 + C.lambda6 * (v * v));
     int col[5] = {n, (int)nb.tu, (int)nb.td, (int)nb.xu, (int)nb.xd};
     // 5-input sorting network (9 comparators)
     cswap(col[0], col[1]); cswap(col[3], col[4]); cswap(col[2], col[4]);
@@ -477,7 +477,10 @@ __device__ __forceinline__ double step_drift(const ChainDev& C, int n, double F)
     cswap(col[1], col[4]); cswap(col[1], col[3]); cswap(col[1], col[2]);
     double lap = 0.0;
 #pragma unroll
-    for (int q = 0; q < 5; ++q) lap += (col[q] != n ? 1.0 : -4.0) * C.phi[col[q]];
+    for (int q = 0; q < 5; ++q) {
+        const double f = C.phi[col[q]];
+        lap += col[q] != n ? f : -4.0 * f;   // the CSR row's weights 1 and -4 (the product by 1 is exact)
+    }
     return d - lap;
 }
 

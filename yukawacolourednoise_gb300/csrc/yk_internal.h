@@ -154,6 +154,7 @@ struct ChainDev {
     int sys0;            // first CG system of the chain
     int tile0, ntiles;   // site tiles of the chain (force / update kernels)
     double m2, lambda, g, m0, r, cut, eps_bar, fixed_dt;
+    double lambda6;      // lambda / 6 (divided once on the host: the same IEEE quotient)
     int drift_mode;
     int filter;          // 1 if the cutoff removes modes (FFT path), 0 if white
     uint64_t seed;

@@ -159,10 +159,10 @@ __global__ void __launch_bounds__(kTile) pion_drift_kernel(ChainDev* __restrict_
         for (int q = 0; q < 4; ++q) {
             const double* f = q == 0 ? C->phi : pi + (size_t)(q - 1) * V;
             double d = F4[(size_t)q * V + n];
-            d += f[n] * (C->m2 + (C->lambda / 6.0) * r2);
+            d += f[n] * (C->m2 + C->lambda6 * r2);
             double lap = 0.0;
 #pragma unroll
-            for (int k = 0; k < 5; ++k) lap += (col[k] != n ? 1.0 : -4.0) * f[col[k]];
+            for (int k = 0; k < 5; ++k) lap += col[k] != n ? f[col[k]] : -4.0 * f[col[k]];
             d -= lap;
             if (q == 0)
                 C->drift[n] = d;
