@@ -330,14 +330,15 @@ def test_halo_cg_step_against_oracle(ylib, cuda, monkeypatch):
         assert ctx.observables().status == 0
 
 
-@pytest.mark.parametrize("patch", ["16", "8", "0"], ids=["patches16", "patches8", "rows"])
+@pytest.mark.parametrize("patch", ["16", "8", "32", "0"], ids=["patches16", "patches8", "patches32", "rows"])
 @pytest.mark.parametrize("Nt,Nx", [(32, 32), (256, 256), (64, 128), (128, 64), (48, 32)])
 def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx, patch):
     # the even-odd Schur-complement solve of the step (CGNE on S S^dag, its
     # residual the true residual of D^dag chi = eta, the same rule relative to
     # |eta|) against the FP64 oracle's CG on D^dag D: the fields of three steps
     # within 1e-8, in fewer iterations than the halo kernel's D^dag D solve;
-    # blocks owning 16 x 16 or 16 x 8 patches of the compact lattice, or rows
+    # blocks owning 16 x 16, 16 x 8 or 32 x 32 patches of the compact lattice,
+    # or rows (a lattice the asked-for patches do not tile runs rows)
     yk = ylib
     monkeypatch.setenv("YK_CG_EO", "1")
     monkeypatch.setenv("YK_CG_EO_PATCH", patch)
@@ -362,6 +363,26 @@ def test_evenodd_cg_steps_against_oracle(ylib, cuda, monkeypatch, Nt, Nx, patch)
     assert np.abs(got[1] - w).max() < 1e-8
     _, k_halo, it_halo, _ = _mixed_run(yk, monkeypatch, "1", Nt, Nx, 1, eo="0")
     assert pr.cg_iterations < 0.7 * it_halo, (pr.cg_iterations, it_halo)
+
+
+def test_evenodd_512_takes_32x32_patches(ylib, cuda, monkeypatch):
+    # 512 x 512: its 16 x 16 patches (512) are more than the GPU holds at
+    # once, its 32 x 32 patches (128) are not; the single-system kernel takes
+    # them and the step agrees with the FP64 oracle
+    yk = ylib
+    Nt = Nx = 512
+    monkeypatch.delenv("YK_CG_EO_PATCH", raising=False)
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01, reliable_every=50)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        ctx.profile_begin()
+        ctx.step(1)
+        pr = ctx.profile_end()
+        assert pr.cg_kernel == 3 and pr.cg_grid == 128, (pr.cg_kernel, pr.cg_grid)
+        got = ctx.get_field()
+        assert ctx.observables().status == 0
+    want, _ = O.langevin_step(Nt, Nx, act(p), phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    assert np.abs(got - want).max() < 1e-8
 
 
 def test_evenodd_force_and_condensate_match_the_full_solve(ylib, cuda, monkeypatch):

@@ -2504,24 +2504,29 @@ __device__ __forceinline__ SiteFF eo_ff(const double* in, int m, int Ve, int Nh,
                                  sm);
 }
 
-// Patch geometry of cg_eo_kernel<PX> (PX > 0): each block owns kPT rows x PX
+// Patch geometry of cg_eo_kernel<PX> (PX > 0): each block owns eo_pt(PX) rows x PX
 // compact columns and stages them widened by 4 rows and 2 compact columns
 // (the reach of the four half hops: two compact columns, since consecutive x
 // hops alternate between the compact index's two parities).  Cells at the
 // buffer's column edges get values no own q depends on; their x neighbours
 // stay inside the buffer (the rows of w, v, u exclude the first and last).
 // PX = 16: 512-thread blocks, one per SM; PX = 8: 256-thread blocks, two per
-// SM, so that one block's barrier waits overlap the other's passes.  PX = 0:
+// SM, so that one block's barrier waits overlap the other's passes; PX = 32:
+// 32 x 32 patches on 512-thread blocks (156 KB of shared memory), so that a
+// 512 x 512 lattice's 128 patches are co-resident (its 16 x 16 patches are
+// 512).  PX = 0:
 // whole rows (cg_eo_kernel's first form).
-constexpr int kPT = 16, kSR = kPT + 8;
+__host__ __device__ constexpr int eo_pt(int PX) { return PX == 32 ? 32 : 16; }   // patch rows
+__host__ __device__ constexpr int eo_sr(int PX) { return eo_pt(PX) + 8; }        // staged rows
 __host__ __device__ constexpr int eo_threads(int PX) { return PX == 8 ? 256 : kHaloThreads; }
 __host__ __device__ constexpr int eo_sw(int PX) { return (PX > 0 ? PX : 16) + 4; }
 
 template <int PX>
-__global__ void __launch_bounds__(eo_threads(PX)) cg_eo_kernel(CGArgs a)
+__global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(CGArgs a)
 {
     constexpr bool PATCH = PX > 0;
     constexpr int kPX = PATCH ? PX : 16;
+    constexpr int kPT = eo_pt(PX), kSR = eo_sr(PX);
     constexpr int kSW = eo_sw(PX), kSN = kSW * kSR;
     constexpr int NT = eo_threads(PX);
     constexpr int K = 1;
@@ -3754,10 +3759,11 @@ static bool eo_takes(int Nt, int Nx, int tpb, size_t* smem)
 template <int PX>
 static bool eo_patch_takes(int Nt, int Nx, int* patches, size_t* smem)
 {
-    if (Nt < kPT || Nx < 2 * PX || (Nt % kPT) || (Nx % (2 * PX))) return false;
-    *patches = (Nt / kPT) * (Nx / (2 * PX));
-    *smem = eo_smem_bytes(kPT * PX, eo_sw(PX) * kSR);
-    return true;
+    constexpr int PT = eo_pt(PX);
+    if (Nt < PT || Nx < 2 * PX || (Nt % PT) || (Nx % (2 * PX))) return false;
+    *patches = (Nt / PT) * (Nx / (2 * PX));
+    *smem = eo_smem_bytes(PT * PX, eo_sw(PX) * eo_sr(PX));
+    return *smem <= kHaloMaxSmem;
 }
 
 static int eo_max_grid()
@@ -3781,7 +3787,7 @@ static int eo_patch_max_grid()
 {
     static int maxg = -1;
     if (maxg < 0) {
-        const int smem = (int)eo_smem_bytes(kPT * PX, eo_sw(PX) * kSR);
+        const int smem = (int)eo_smem_bytes(eo_pt(PX) * PX, eo_sw(PX) * eo_sr(PX));
         cudaFuncSetAttribute((const void*)cg_eo_kernel<PX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         int dev = 0, nsm = 0, per = 0;
         cudaGetDevice(&dev);
@@ -3829,6 +3835,7 @@ void cg_halo_init()
     eo_max_grid();
     eo_patch_max_grid<16>();
     eo_patch_max_grid<8>();
+    eo_patch_max_grid<32>();
     eob_max_grid();
 }
 
@@ -3865,6 +3872,14 @@ static bool eo_single_variant(const CGArgs& a, int* px, int* grid, int* tpb, siz
         *px = 8;
         *grid = np;
         *tpb = 1;
+        return true;
+    }
+    // 32 x 32 patches: four tiles' partial slots each
+    if ((want == -1 || want == 32) && eo_patch_takes<32>(a.solo_nt, a.solo_nx, &np, smem) &&
+        np <= eo_patch_max_grid<32>() && 4 * np <= slots) {
+        *px = 32;
+        *grid = np;
+        *tpb = 4;
         return true;
     }
     const int eg = cg_grid_for(a.eo_tile_end - a.eo_tile_begin, capped(eo_max_grid(), a.grid_cap), tpb);
@@ -3906,7 +3921,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
             int px = 0, eg = 0, etpb = 1;
             size_t es = 0;
             if (eo_single_variant(a, &px, &eg, &etpb, &es)) {
-                if (px > 0) e.tile_end = e.tile_begin + eg;   // one partial slot per patch
+                if (px > 0) e.tile_end = e.tile_begin + eg * etpb;   // the patches' partial slots
                 e.tiles_per_block = etpb;
                 e.grid = eg;
                 if (grid_out) *grid_out = eg;
@@ -3925,6 +3940,7 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                 void* args[] = {&e};
                 const void* fn = px == 16 ? (const void*)cg_eo_kernel<16>
                                : px == 8  ? (const void*)cg_eo_kernel<8>
+                               : px == 32 ? (const void*)cg_eo_kernel<32>
                                           : (const void*)cg_eo_kernel<0>;
                 return cudaLaunchKernelExC(&cfg, fn, args);
             }
