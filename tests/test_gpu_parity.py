@@ -511,6 +511,33 @@ def test_batched_even_odd_cg(ylib, cuda, specs, kernel):
         assert np.abs(got[c] - phi).max() < 1e-8, c
 
 
+@pytest.mark.parametrize("r", [0.7, 1.3])
+def test_evenodd_wilson_parameter(ylib, cuda, r):
+    # a Wilson parameter r != 1, where the time hops' coefficients -(r -+ 1)/2
+    # are both nonzero (in float-float in the reliable updates, round 0 and the
+    # reconstruction): the single-system kernel (64 x 64) and the batched one
+    # (two chains, one with two right-hand sides) against the FP64 oracle
+    yk = ylib
+    for specs, kernel in (([(64, 64, 0.1, 0.5, 1)], 3), ([(32, 48, 0.1, 0.5, 2), (16, 16, 0.2, 0.7, 1)], 4)):
+        ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, n_rhs=nr, wilson_param=r,
+                     precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+              for nt, nx, m0, g, nr in specs]
+        with yk.Context(ps) as ctx:
+            ctx.profile_begin()
+            ctx.step(1)
+            pr = ctx.profile_end()
+            assert pr.cg_kernel == kernel, (pr.cg_kernel, kernel)
+            ctx.step(1)
+            got = [ctx.get_field(c) for c in range(len(ps))]
+            assert all(ctx.observables(c).status == 0 for c in range(len(ps)))
+        for c, p in enumerate(ps):
+            phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+            for step in range(2):
+                phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10,
+                                         tol_mode=1, fixed_dt=0.01)
+            assert np.abs(got[c] - phi).max() < 1e-8, (c, r)
+
+
 def test_autotune_keeps_results(ylib, cuda, monkeypatch):
     # batched chains: the tuned CG grid (automatic before the first capture,
     # and again by an explicit call between steps) gives the same fields, bit
@@ -585,6 +612,30 @@ def test_step_io_matches_separate_calls(ylib, cuda, monkeypatch, host):
     with pytest.raises(TypeError):
         with yk.Context(p) as ctx:
             ctx.step_io(np.zeros(V, dtype=np.float32))
+
+
+def test_step_io_graph_cache_eviction(ylib, cuda):
+    # six different pinned output buffers, one per step: more pointer pairs
+    # than the four io graphs kept, so older graphs are replaced; each buffer
+    # holds its step's field, as get_field after the same steps
+    yk, torch = ylib, cuda
+    p = params(yk, 32, 32, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
+    V = 32 * 32
+    phi0 = np.random.default_rng(6).uniform(-1, 1, V)
+    want = []
+    with yk.Context(p) as ctx:
+        ctx.set_field(phi0)
+        for _ in range(8):
+            ctx.step(1)
+            want.append(ctx.get_field())
+    outs = [torch.empty(V, dtype=torch.float64).pin_memory() for _ in range(6)]
+    with yk.Context(p) as ctx:
+        ctx.set_field(phi0)
+        for s in range(8):
+            buf = outs[s % 6]
+            o = ctx.step_io(None, buf)
+            assert o.steps == s + 1 and o.status == 0
+            assert np.array_equal(buf.numpy(), want[s]), s
 
 
 def test_deterministic(ylib, cuda):
