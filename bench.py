@@ -408,24 +408,32 @@ def precision_errors(yk, torch, stream, phi_seg, step_seg, n, n_ops=5):
 
 
 
-EOB_BYTES_PER_SITE_ITERATION = 144   # 288 B per compact site and round of cg_eob_kernel
+# Algorithmic bytes per lattice site and iteration of the batched even-odd
+# kernels.  cg_eob_kernel, per compact site and round: P1 reads r, q, p, xs,
+# v and writes r, p, xs, w; P2 reads p, w, writes v; P3 reads v, writes u; P4
+# reads v, u, r, writes q: 288 B, i.e. 144 B per lattice site.
+# cg_eop_kernel: r, q, p, xs, v read and r, p, q, v, xs written per compact
+# site (w and u stay in shared memory; the halo re-reads are not counted):
+# 160 B, i.e. 80 B per lattice site.
+BATCHED_BYTES_PER_SITE_ITERATION = {4: 144, 5: 80}
+BATCHED_KERNELS = {0: "cg_kernel (grid-wide D^dag D)", 3: "cg_eo_kernel (single-system even-odd)",
+                   4: "cg_eob_kernel (batched even-odd, four passes)",
+                   5: "cg_eop_kernel (batched even-odd over 32 x 16 patches)"}
 
 
 def eob_roofline(yk, torch, stream, ctx):
     """One more step, profiled: the batched even-odd CG's algorithmic bytes
-    (per compact site and round: P1 reads r, q, p, xs, v and writes r, p, xs,
-    w; P2 reads p, w, writes v; P3 reads v, writes u; P4 reads v, u, r, writes
-    q: 288 B, i.e. 144 B per lattice site and iteration) over its CUDA-event
-    time, against the measured HBM copy bandwidth."""
+    (BATCHED_BYTES_PER_SITE_ITERATION of the kernel that ran) over its
+    CUDA-event time, against the measured HBM copy bandwidth."""
     ctx.profile_begin()
     with torch.cuda.stream(stream):
         ctx.step(1)
     pr = ctx.profile_end()
     pk = peaks()
-    kernels = {0: "cg_kernel", 3: "cg_eo_kernel", 4: "cg_eob_kernel"}
-    gbs = pr.cg_site_iterations * EOB_BYTES_PER_SITE_ITERATION / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
-    return {"kernel": kernels.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_ms": round(pr.cg_ms, 3),
-            "bytes_per_site_iteration": EOB_BYTES_PER_SITE_ITERATION, "achieved": round(gbs, 1), "unit": "GB/s",
+    bps = BATCHED_BYTES_PER_SITE_ITERATION.get(pr.cg_kernel, 144)
+    gbs = pr.cg_site_iterations * bps / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
+    return {"kernel": BATCHED_KERNELS.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_ms": round(pr.cg_ms, 3),
+            "bytes_per_site_iteration": bps, "achieved": round(gbs, 1), "unit": "GB/s",
             "peak": pk["hbm_gbs"], "frac": round(gbs / pk["hbm_gbs"], 4), "peak_source": pk["source"]}
 
 
@@ -544,16 +552,16 @@ def batched(yk, torch, stream, steps=20, warmup=3, n_chains=64, seed=1234):
     pr = ctx.profile_end()
     ctx.close()
     pk = peaks()
-    gbs = pr.cg_site_iterations * EOB_BYTES_PER_SITE_ITERATION / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
+    bps = BATCHED_BYTES_PER_SITE_ITERATION.get(pr.cg_kernel, 144)
+    gbs = pr.cg_site_iterations * bps / (pr.cg_ms / 1e3) / 1e9 if pr.cg_ms > 0 else 0.0
     sites = int(sum(int(L) * int(L) for L in Ls))
-    kernels = {0: "cg_kernel (grid-wide D^dag D)", 4: "cg_eob_kernel (batched even-odd)"}
     return {"config": f"{n_chains} chains, L in {{32,64,128,256}} (seed {seed}), 4 RHS, mixed CG rel-res 1e-10",
             "value": round(steps * n_chains / sec, 2), "unit": "chain-steps/s",
             "site_steps_per_s": round(steps * sites / sec, 1), "steps": steps,
             "ms_per_step": round(sec * 1e3 / steps, 3),
-            "cg_kernel": kernels.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_grid": pr.cg_grid,
+            "cg_kernel": BATCHED_KERNELS.get(pr.cg_kernel, str(pr.cg_kernel)), "cg_grid": pr.cg_grid,
             "cg_iterations_per_system_step": round(pr.cg_iterations / max(pr.steps * n_chains * 4, 1), 1),
-            "cg_roofline": {"bytes_per_site_iteration": EOB_BYTES_PER_SITE_ITERATION, "achieved": round(gbs, 1),
+            "cg_roofline": {"bytes_per_site_iteration": bps, "achieved": round(gbs, 1),
                             "unit": "GB/s", "peak": pk["hbm_gbs"], "frac": round(gbs / pk["hbm_gbs"], 4)},
             "status_ok": all(o.status in (0, yk.YK_ENOCONV) for o in obs),
             "autotune": {"cg_grid": t.cg_grid, "cg_grid_max": t.cg_grid_max, "candidates": t.cg_candidates,

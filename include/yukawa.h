@@ -377,7 +377,8 @@ typedef struct yk_profile {
     int cg_grid;                 /* blocks of the last CG launch                  */
     int cg_kernel;               /* its kernel: 0 grid-wide, 1 halo, 2 cluster,   */
                                  /*   3 even-odd (Schur complement), 4 batched    */
-                                 /*   even-odd (work dealt out per pass)          */
+                                 /*   even-odd (work dealt out per pass), 5       */
+                                 /*   batched even-odd over 32 x 16 patches       */
     double noise_ms, cg_ms, force_ms, update_ms;   /* summed device time          */
     int64_t cg_iterations;       /* CG iterations, summed over systems            */
     int64_t cg_site_iterations;  /* sum over chains of iterations x volume        */

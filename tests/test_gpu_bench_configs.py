@@ -98,7 +98,7 @@ def test_c3_shaped_batch(ylib, cuda):
     with yk.Context(ps) as ctx:
         ctx.profile_begin()
         ctx.step(1)
-        assert ctx.profile_end().cg_kernel == 4, "the batch's solves run the batched even-odd CG kernel"
+        assert ctx.profile_end().cg_kernel == 5, "the batch's solves run the batched even-odd patch kernel"
         ctx.step(1)
         got = [ctx.get_field(c) for c in range(len(ps))]
         obs = [ctx.observables(c) for c in range(len(ps))]

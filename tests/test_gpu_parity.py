@@ -515,10 +515,12 @@ def test_batched_even_odd_cg(ylib, cuda, specs, kernel):
 def test_evenodd_wilson_parameter(ylib, cuda, r):
     # a Wilson parameter r != 1, where the time hops' coefficients -(r -+ 1)/2
     # are both nonzero (in float-float in the reliable updates, round 0 and the
-    # reconstruction): the single-system kernel (64 x 64) and the batched one
-    # (two chains, one with two right-hand sides) against the FP64 oracle
+    # reconstruction): the single-system kernel (64 x 64), the batched one
+    # (two chains, one with two right-hand sides) and the batched patch
+    # kernel against the FP64 oracle
     yk = ylib
-    for specs, kernel in (([(64, 64, 0.1, 0.5, 1)], 3), ([(32, 48, 0.1, 0.5, 2), (16, 16, 0.2, 0.7, 1)], 4)):
+    for specs, kernel in (([(64, 64, 0.1, 0.5, 1)], 3), ([(32, 48, 0.1, 0.5, 2), (16, 16, 0.2, 0.7, 1)], 4),
+                          ([(32, 64, 0.1, 0.5, 2), (32, 32, 0.2, 0.7, 1)], 5)):
         ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, n_rhs=nr, wilson_param=r,
                      precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01)
               for nt, nx, m0, g, nr in specs]
@@ -536,6 +538,36 @@ def test_evenodd_wilson_parameter(ylib, cuda, r):
                 phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10,
                                          tol_mode=1, fixed_dt=0.01)
             assert np.abs(got[c] - phi).max() < 1e-8, (c, r)
+
+
+@pytest.mark.parametrize("eop", ["1", "0"], ids=["patch_kernel", "four_pass_kernel"])
+def test_batched_patch_kernel(ylib, cuda, monkeypatch, eop):
+    # a batch whose compact lattices 32 x 16 patches tile (32 x 32 and 64 x 32:
+    # the staged buffer wraps across the whole compact row; 64 x 64 with three
+    # right-hand sides; 32 x 96; different masses, so the systems converge and
+    # run their reliable updates in different rounds): the batched patch
+    # kernel, and the four-pass kernel, against the FP64 oracle
+    monkeypatch.setenv("YK_CG_EOP", eop)
+    yk = ylib
+    specs = [(32, 32, 0.1, 0.5, 2), (64, 32, 0.3, 0.4, 1), (64, 64, 0.05, 0.8, 3), (32, 96, 0.2, 0.6, 1)]
+    ps = [params(yk, nt, nx, fermion_mass=m0, yukawa_coupling=g, n_rhs=nr, precision=yk.YK_MIXED, cg_tol=1e-10,
+                 fixed_dt=0.01, reliable_every=50)
+          for nt, nx, m0, g, nr in specs]
+    with yk.Context(ps) as ctx:
+        ctx.profile_begin()
+        ctx.step(1)
+        pr = ctx.profile_end()
+        assert pr.cg_kernel == (5 if eop == "1" else 4), pr.cg_kernel
+        ctx.step(2)
+        got = [ctx.get_field(c) for c in range(len(ps))]
+        obs = [ctx.observables(c) for c in range(len(ps))]
+    for c, p in enumerate(ps):
+        assert obs[c].steps == 3 and obs[c].status == 0, c
+        phi = O.uniform_field(1234, c, p.Nt * p.Nx)
+        for step in range(3):
+            phi, _ = O.langevin_step(p.Nt, p.Nx, act(p), phi, 1234, c, step, n_rhs=p.n_rhs, tol=1e-10, tol_mode=1,
+                                     fixed_dt=0.01)
+        assert np.abs(got[c] - phi).max() < 1e-8, c
 
 
 def test_autotune_keeps_results(ylib, cuda, monkeypatch):

@@ -203,6 +203,7 @@ struct yk_ctx {
     SysDev* d_sys_eo = nullptr;
     int2* d_eo_tiles = nullptr;
     int eo_tile_begin = 0, eo_tile_end = 0;
+    bool eo_patches = false;   // every system tiled by 32 x 16 patches of its compact lattice
 };
 
 namespace {
@@ -926,6 +927,11 @@ int eo_setup(yk_ctx* ctx, const std::vector<SysDev>& hs)
         ctx->eo_tile_begin = 0;
         ctx->eo_tile_end = ctx->n_sys_tiles;
     }
+    // every step system's compact lattice tiled by 32 x 16 patches: batches may
+    // take the patch kernel
+    ctx->eo_patches = true;
+    for (const Chain& q : ctx->ch)
+        if (q.n_rhs_step > 0 && ((q.Nt % 32) || ((q.Nx / 2) % 16))) ctx->eo_patches = false;
     ctx->cg_eo = true;
     return YK_OK;
 }
@@ -938,6 +944,7 @@ void eo_args(const yk_ctx* ctx, CGArgs& a)
     a.eo_tiles = ctx->d_eo_tiles;
     a.eo_tile_begin = ctx->eo_tile_begin;
     a.eo_tile_end = ctx->eo_tile_end;
+    a.eo_patches = ctx->eo_patches ? 1 : 0;
 }
 
 // The complex systems of a pion chain: sources eta (device, n_rhs x 8V) or,

@@ -134,6 +134,8 @@ enum CGMode {
     kRu = 2,     // reliable update (mixed): fold x, then r = b - A x in FP64
     kRedo = 3,   // after a reliable update: p = c r + beta p from the FP64 residual
     kWait = 4,   // another system's reliable update runs; this one already stepped
+    kRu2 = 5,    // the patch kernel's update, second round: the odd hop of chi
+    kRu3 = 6,    // and third round: the residual and its partials
 };
 
 // Per-block copy of the coefficients of one system whose tiles it owns (FP64,
@@ -3600,6 +3602,502 @@ __global__ void __launch_bounds__(kHaloThreads) cg_eob_kernel(CGArgs a)
 }
 
 
+// ---------------------------------------------------------------------------
+// Batched even-odd CG over patches (cg_eop_kernel): the iteration of
+// cg_eo_kernel for every system of a batch whose compact lattices 32 x 16
+// patches tile (Nt a multiple of 32, Nx / 2 of 16).  The patches of the systems
+// that iterate are dealt out to the blocks every round, as cg_eob_kernel
+// deals out tiles, and a block takes its share one patch after another: it
+// stages the patch's p, r and q of the previous iteration widened by 4 rows
+// and 2 compact columns, with A_e and 1 / A_o (the next patch's copies in
+// flight while it works on this one), forms p, r, w, v, u and q in shared
+// memory, and writes r, p, q, v, the chi increment and the patch's tile
+// partials.  w and u never leave the SM, so a round moves fewer bytes than
+// cg_eob_kernel's four passes, and it has one grid barrier, the reducing
+// one, where cg_eob_kernel has four.  A system's reliable update takes three
+// rounds of its own (kRu: the fold; kRu2: the odd hop; kRu3: the residual and
+// its partials), run site by site beside the other systems' patches, in
+// float-float as in the other even-odd kernels.
+// ---------------------------------------------------------------------------
+constexpr int kEopPT = 32, kEopPX = 16, kEopSW = kEopPX + 4, kEopNB = kEopSW * (kEopPT + 8),
+              kEopOwn = kEopPT * kEopPX;
+static_assert(kEopOwn == 2 * kTile, "a patch fills two tiles' partial slots (rows 0-15, 16-31)");
+
+// Shared memory of cg_eop_kernel: two staging sets (p, r, q, A_e, 1 / A_o on
+// the widened patch; the chi increment and v on the own sites), w (then u)
+// and v.
+constexpr size_t kEopSet = 3 * (size_t)kEopNB * sizeof(float4) + 2 * (size_t)kEopNB * sizeof(float) +
+                           2 * (size_t)kEopOwn * sizeof(float4);
+static size_t eop_smem_bytes() { return 2 * kEopSet + 2 * (size_t)kEopNB * sizeof(float4); }
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// The reducing barrier of cg_eop_kernel: eob_reduce, with the update's first
+// two rounds (kRu, kRu2: no partials) moving the system to its next round.
+__device__ bool eop_reduce(const CGArgs& a, unsigned& gen, int k, double* red, int* s_active, int* s_ru,
+                           const int* s_mode, const int* s_par)
+{
+    if (!eob_barrier(a, gen)) return false;
+    for (int q = blockIdx.x; q < a.sys_count; q += gridDim.x) {
+        const int j = a.sys_first + q;
+        const SysDev& S = a.sys[j];
+        const int mode = s_mode[q];   // this round's (the block's copy: uniform)
+        double s[6];
+        if (mode != kRu && mode != kRu2 && mode != kIdle) sum_partials<true>(a, S.tile0, S.ntiles, red, s);
+        if (threadIdx.x == 0) {
+            CGState st;
+            load_state(a.st + j, st);
+            CoefVals cv = {0.0, 0.0, 0.0, 1.0, 0.0, kIdle};
+            cv.par = s_par[q];
+            if (st.mode == kRu || st.mode == kRu2) {
+                cv.mode = st.mode == kRu ? kRu2 : kRu3;
+            } else if (st.mode != kIdle) {
+                const int ks = k == 0 ? 0 : (st.mode == kRedo ? st.iters : st.iters + 1);
+                cv = scalar_step<true>(a, ks, st.mode == kRu3, s, st, s_active, s_ru);
+                cv.par = (cv.mode == kRedo ? st.iters : st.iters + 1) & 1;
+            }
+            st.mode = cv.mode;
+            store_state(a.st + j, st);
+            __threadfence();
+            publish_coef(a.coef + j, cv, gen);
+        }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kHaloThreads, 1) cg_eop_kernel(CGArgs a)
+{
+    constexpr int K = 1;
+    constexpr int kSkipIm = (1 << 3) | (1 << 5);
+    constexpr int SB = kEopSW, NB = kEopNB, NT = kHaloThreads;
+    using W = float;
+    extern __shared__ float4 hsm[];
+    // staging set s at hsm + s * kEopSet bytes: p, r, q (NB each), xs, v
+    // (own), then A_e, 1 / A_o (NB floats each)
+    auto set_base = [&](int set) -> float4* { return reinterpret_cast<float4*>(reinterpret_cast<char*>(hsm) + set * kEopSet); };
+    float4* Wp = set_base(2);    // w, later u
+    float4* Vp = Wp + NB;        // v
+    const int hf = threadIdx.x / kTile, ts = threadIdx.x % kTile;
+    __shared__ double red[128];
+    __shared__ int s_mode[kEobMaxSys], s_par[kEobMaxSys], s_nt[kEobMaxSys], s_t0[kEobMaxSys], s_pre[kEobMaxSys + 1];
+    __shared__ int s_np[kEobMaxSys];   // patches of each system (two tiles each)
+    __shared__ float s_fa[kEobMaxSys], s_fb[kEobMaxSys], s_fc[kEobMaxSys];
+    __shared__ int s_active, s_ru;   // the scalar step's counters (unused here)
+    const int nsys = a.sys_count;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        const SysDev& S = a.sys[a.sys_first + q];
+        s_nt[q] = S.ntiles;
+        s_np[q] = S.ntiles / 2;
+        s_t0[q] = S.tile0;
+        s_mode[q] = kStep;
+        s_par[q] = 0;
+        s_fa[q] = s_fb[q] = s_fc[q] = 0.f;
+    }
+    __syncthreads();
+    if (*(volatile int*)a.err) return;
+    unsigned gen = 0;
+    constexpr int kAll = (1 << kStep) | (1 << kRedo) | (1 << kRu) | (1 << kRu2) | (1 << kRu3);
+    constexpr int kPass = (1 << kStep) | (1 << kRedo);
+    constexpr int kInit = -1;   // round 0: p_0 and r_0 as stored
+
+    // a patch of the current prefix: its system, index and place
+    struct Patch {
+        int q, lp, t0, i0, Nt, Nh, Ve;
+    };
+    auto patch_of = [&](int i, int& qc) -> Patch {
+        const int q = (qc >= 0 && i >= s_pre[qc] && i < s_pre[qc + 1]) ? qc : eob_find(i, nsys, s_pre);
+        qc = q;
+        const SysDev& S = a.sys[a.sys_first + q];
+        Patch P;
+        P.q = q;
+        P.lp = i - s_pre[q];
+        P.Nt = S.Nt;
+        P.Nh = S.Nx;
+        P.Ve = S.V;
+        const int npx = P.Nh / kEopPX;
+        P.t0 = (P.lp / npx) * kEopPT;
+        P.i0 = (P.lp % npx) * kEopPX;
+        return P;
+    };
+    // compact site of buffer cell j (the widened patch, wrapped)
+    auto buf_m = [](const Patch& P, int j) -> int {
+        const int r = j / SB, c = j - r * SB;
+        int t = P.t0 - 4 + r, i = P.i0 - 2 + c;
+        t = t < 0 ? t + P.Nt : (t >= P.Nt ? t - P.Nt : t);
+        i = i < 0 ? i + P.Nh : (i >= P.Nh ? i - P.Nh : i);
+        return t * P.Nh + i;
+    };
+    auto cell_t = [](const Patch& P, int j) -> int {
+        const int t = P.t0 - 4 + j / SB;
+        return t < 0 ? t + P.Nt : (t >= P.Nt ? t - P.Nt : t);
+    };
+    auto own_j = [](int o) -> int { return (4 + o / kEopPX) * SB + 2 + o % kEopPX; };
+    auto own_m = [](const Patch& P, int o) -> int { return (P.t0 + o / kEopPX) * P.Nh + P.i0 + o % kEopPX; };
+    auto own_of = [](int j) -> int {
+        const int r = j / SB - 4, c = j % SB - 2;
+        return (r >= 0 && r < kEopPT && c >= 0 && c < kEopPX) ? r * kEopPX + c : -1;
+    };
+
+    // stage patch P (mode: its system's; kInit: round 0) into set `set`
+    auto stage = [&](const Patch& P, int mode, int set) {
+        const SysDev& S = a.sys[a.sys_first + P.q];
+        const int cur = s_par[P.q], prv = cur ^ 1;
+        const float* Rl = (mode == kRedo || mode == kInit) ? S.r32[cur] : S.r32[prv];
+        const float* Pl = mode == kInit ? S.p32[cur] : S.p32[prv];
+        const float* Al = prv == 0 ? S.Ap32 : S.t32;
+        float4* B = set_base(set);
+        float4* X = B + 3 * NB;
+        float* D = reinterpret_cast<float*>(X + 2 * kEopOwn);
+        for (int j = threadIdx.x; j < NB; j += NT) {
+            const int m = buf_m(P, j);
+            cp_async16(B + j, Pl + 4 * (size_t)m);
+            cp_async16(B + NB + j, Rl + 4 * (size_t)m);
+            if (mode == kStep) cp_async16(B + 2 * NB + j, Al + 4 * (size_t)m);
+            cp_async4(D + j, S.diag32 + m);               // A_e (even)
+            cp_async4(D + NB + j, S.diag32 + P.Ve + m);   // 1 / A_o (odd)
+        }
+        if (mode == kStep)   // the chi increment and v of the own sites
+            for (int o = threadIdx.x; o < kEopOwn; o += NT) {
+                const int m = own_m(P, o);
+                cp_async16(X + o, S.xs32 + 4 * (size_t)m);
+                cp_async16(X + kEopOwn + o, S.v32 + 4 * (size_t)m);
+            }
+        cp_async_commit();
+    };
+
+    // the iteration at patch P from staging set `set`
+    auto body = [&](const Patch& P, int mode, int set, bool round0) {
+        const SysDev& S = a.sys[a.sys_first + P.q];
+        float4* P_st = set_base(set);
+        float4* R_st = P_st + NB;
+        const float4* A_st = R_st + NB;
+        const float4* X_st = A_st + NB;
+        const float4* Vo_st = X_st + kEopOwn;
+        const float* dep = reinterpret_cast<const float*>(Vo_st + kEopOwn);
+        const float* dip = dep + NB;
+        const int cur = s_par[P.q];
+        const W rw = (W)S.r;
+        const W ar = s_fa[P.q], beta = s_fb[P.q], cre = s_fc[P.q];
+        // A1: p (and r, the chi increment on the own sites) on the buffer
+        for (int j = threadIdx.x; j < NB; j += NT) {
+            const int o = own_of(j);
+            const Site<W, K> po = ld_sm(P_st, j);
+            Site<W, K> p;
+            if (mode == kStep) {
+                Site<W, K> r = ld_sm(R_st, j);
+                site_axpy<W, K>(r, -ar, W(0), ld_sm(A_st, j));
+#pragma unroll
+                for (int i = 0; i < 4; ++i) p.v[i] = fma(beta, po.v[i], r.v[i]);
+                if (o >= 0) {
+                    const int m = own_m(P, o);
+                    Site<W, K> x = ld_sm(X_st, o);
+                    site_axpy<W, K>(x, ar, W(0), ld_sm(Vo_st, o));
+                    YK_ST(W, K, S.xs32, m, x);
+                    YK_ST(W, K, S.r32[cur], m, r);
+                    YK_ST(W, K, S.p32[cur], m, p);
+                    st_sm(R_st, j, r);
+                }
+            } else if (mode == kRedo) {
+                p = p_next<W, K>(ld_sm(R_st, j), po, beta, cre, W(0));
+                if (o >= 0) YK_ST(W, K, S.p32[cur], own_m(P, o), p);
+            } else {
+                p = po;
+            }
+            st_sm(P_st, j, p);
+        }
+        __syncthreads();
+        Site<W, K> zero;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) zero.v[i] = W(0);
+        // w = -A_o^-1 H_oe p (odd) on [SB, NB - SB)
+        for (int j = SB + threadIdx.x; j < NB - SB; j += NT) {
+            const int t = cell_t(P, j), b = (t + 1) & 1;
+            const W sp = (t + 1 == P.Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            Site<W, K> h = eo_sm<false>(P_st, j, SB, b, b - 1, zero, W(0), rw, sp, sm);
+            const W sc = -dip[j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] *= sc;
+            st_sm(Wp, j, h);
+        }
+        __syncthreads();
+        // v = A_e p + H_eo w (even) on [2SB, NB - 2SB); the own sites' to v32
+        for (int j = 2 * SB + threadIdx.x; j < NB - 2 * SB; j += NT) {
+            const int t = cell_t(P, j), b = t & 1;
+            const W sp = (t + 1 == P.Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            const Site<W, K> v = eo_sm<false>(Wp, j, SB, b, b - 1, ld_sm(P_st, j), dep[j], rw, sp, sm);
+            st_sm(Vp, j, v);
+            const int o = own_of(j);
+            if (o >= 0) YK_ST(W, K, S.v32, own_m(P, o), v);
+        }
+        __syncthreads();
+        // u = -A_o^-1 H^dag_oe v (odd) on [3SB, NB - 3SB)
+        for (int j = 3 * SB + threadIdx.x; j < NB - 3 * SB; j += NT) {
+            const int t = cell_t(P, j), b = (t + 1) & 1;
+            const W sp = (t + 1 == P.Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            Site<W, K> h = eo_sm<true>(Vp, j, SB, b, b - 1, zero, W(0), rw, sp, sm);
+            const W sc = -dip[j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) h.v[i] *= sc;
+            st_sm(Wp, j, h);
+        }
+        __syncthreads();
+        // q = A_e v + H^dag_eo u on the own sites and the patch's partials
+        // (round 0 adds |eta|^2 of the compact index's two full sites)
+        FF f[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+        const bool on = true;   // rows 0-15 of the patch in threads 0-255, rows 16-31 in 256-511
+        {
+            const int o = hf * kTile + ts;
+            const int j = own_j(o), m = own_m(P, o);
+            const int t = cell_t(P, j), b = t & 1;
+            const W sp = (t + 1 == P.Nt) ? W(-1) : W(1), sm = (t == 0) ? W(-1) : W(1);
+            const Site<W, K> v = ld_sm(Vp, j);
+            const Site<W, K> qv = eo_sm<true>(Wp, j, SB, b, b - 1, v, dep[j], rw, sp, sm);
+            YK_ST(W, K, cur == 0 ? S.Ap32 : S.t32, m, qv);
+            const Site<W, K> r = ld_sm(R_st, j);
+            W rq, dummy;
+            site_dot<W, K>(r, qv, rq, dummy);
+            f[0] = FF{site_norm2<W, K>(r), 0.f};
+            f[1] = FF{site_norm2<W, K>(qv), 0.f};
+            f[2] = FF{site_norm2<W, K>(v), 0.f};
+            f[4] = FF{rq, 0.f};
+            if (round0) {
+                const SysDev& SF = a.sys_full[a.sys_first + P.q];
+                const Site<double, K> e0 = load_site<double, K>(SF.b, 2 * m);
+                const Site<double, K> e1 = load_site<double, K>(SF.b, 2 * m + 1);
+                f[5] = ff_of(site_norm2<double, K>(e0) + site_norm2<double, K>(e1));
+            }
+        }
+        const int tile = s_t0[P.q] + 2 * P.lp + hf;
+        if (round0)
+            put_partial_ff<(1 << 3), true>(a, tile, on, f, red);
+        else
+            put_partial_ff<kSkipIm, false>(a, tile, on, f, red);
+    };
+
+    // this block's share of the patches of the systems in the pass modes
+    // (round 0: of every system), the next patch's staging in flight
+    auto pass = [&](bool init) {
+        eob_scan(nsys, s_mode, s_np, init ? kAll : kPass, s_pre);
+        int lo, hi;
+        eob_share(s_pre[nsys], &lo, &hi);
+        int qc = -1, qn = -1;
+        if (lo < hi) {
+            const Patch P0 = patch_of(lo, qn);
+            stage(P0, init ? kInit : s_mode[P0.q], 0);
+        }
+        for (int i = lo; i < hi; ++i) {
+            const int set = (i - lo) & 1;
+            const Patch P = patch_of(i, qc);
+            if (i + 1 < hi) {
+                const Patch Pn = patch_of(i + 1, qn);
+                stage(Pn, init ? kInit : s_mode[Pn.q], set ^ 1);
+                cp_async_wait_one();
+            } else {
+                cp_async_wait_all();
+            }
+            __syncthreads();
+            body(P, init ? kInit : s_mode[P.q], set, init);
+        }
+    };
+
+    // Runs f(S, q, m, tile, tile_on, on) for every site of this block's share
+    // of the tiles of the systems in `mask`, two tiles at a time.
+    auto for_sites = [&](int mask, auto&& f) {
+        eob_scan(nsys, s_mode, s_nt, mask, s_pre);
+        int lo, hi;
+        eob_share(s_pre[nsys], &lo, &hi);
+        int qc = -1;
+        for (int base = lo; base < hi; base += 2) {
+            const int i = base + hf;
+            const bool tile_on = i < hi;
+            const int ii = tile_on ? i : lo;
+            const int q = (qc >= 0 && ii >= s_pre[qc] && ii < s_pre[qc + 1]) ? qc : eob_find(ii, nsys, s_pre);
+            qc = q;
+            const int lt = ii - s_pre[q];
+            const SysDev& S = a.sys[a.sys_first + q];
+            const int m = lt * kTile + ts;
+            f(S, q, m, s_t0[q] + lt, tile_on, tile_on && m < S.V);
+        }
+    };
+    struct Geo {
+        int b, du, dd;
+        float sp, sm;
+    };
+    auto geo = [](const SysDev& S, int m, int c) {
+        Geo g;
+        const int Nh = S.Nx;
+        const int t = m / Nh, i = m - t * Nh;
+        g.b = (t + c) & 1;
+        g.du = g.b ? ((i == Nh - 1) ? 1 - Nh : 1) : 0;
+        g.dd = g.b ? 0 : ((i == 0) ? Nh - 1 : -1);
+        g.sp = (t + 1 == S.Nt) ? -1.f : 1.f;
+        g.sm = (t == 0) ? -1.f : 1.f;
+        return g;
+    };
+
+    // ---------------- round 0: eta of both classes (b, full layout), A_e and
+    // 1 / A_o, -A_o^-1 eta_o (t64), chi_e = xs = v = 0; then rhs_e, r_0 = p_0
+    for_sites(kAll, [&](const SysDev& S, int q, int m, int, bool, bool on) {
+        if (!on) return;
+        const SysDev& SF = a.sys_full[a.sys_first + q];
+        const int Ve = S.V;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const Geo g = geo(S, m, c);
+            const int n = 2 * m + g.b;
+            const Site<double, K> bv =
+                SF.gen_eta ? eta_of_step<K>(SF, n, a.eta_kind) : load_site<double, K>(SF.b, n);
+            if (SF.gen_eta) store_site<double, K>(SF.b, n, bv);
+            const double d = 2.0 * S.r + S.m0 + S.g * SF.sigma[n];
+            if (c == 0) {
+                S.diag32[m] = (float)d;
+            } else {
+                const FF inv = ff_rcp(ff_of(d));
+                st_ff1(S.dinv, m, inv);
+                S.diag32[Ve + m] = inv.hi;
+                const SiteFF e = ff_site_of(bv, SF.gen_eta != 0);
+                SiteFF h;
+#pragma unroll
+                for (int e2 = 0; e2 < 4; ++e2) h.v[e2] = ff_mul(FF{-inv.hi, -inv.lo}, e.v[e2]);
+                st_ff(S.t64, m, h);
+            }
+        }
+        Site<double, K> z;
+        Site<W, K> zw;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            z.v[e] = 0.0;
+            zw.v[e] = W(0);
+        }
+        store_site<double, K>(S.x, m, z);
+        YK_ST(W, K, S.xs32, m, zw);
+        YK_ST(W, K, S.v32, m, zw);
+    });
+    if (!eob_barrier(a, gen)) return;
+    for_sites(kAll, [&](const SysDev& S, int q, int m, int, bool, bool on) {
+        if (!on) return;
+        const SysDev& SF = a.sys_full[a.sys_first + q];
+        const Geo g = geo(S, m, 0);
+        const SiteFF e = ff_site_of(load_site<double, K>(SF.b, 2 * m + g.b), SF.gen_eta != 0);
+        const SiteFF rh =
+            eo_ff<true, 1>(S.t64, m, S.V, S.Nx, g.du, g.dd, e, FF{1.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
+        st_ff(S.x + 4 * (size_t)S.V, m, rh);
+        Site<W, K> rw;
+#pragma unroll
+        for (int e2 = 0; e2 < 4; ++e2) rw.v[e2] = rh.v[e2].hi;
+        YK_ST(W, K, S.r32[0], m, rw);
+        YK_ST(W, K, S.p32[0], m, rw);
+    });
+    if (!eob_barrier(a, gen)) return;
+    pass(true);
+    if (!eop_reduce(a, gen, 0, red, &s_active, &s_ru, s_mode, s_par)) return;
+
+    // every round: the patches of the systems that iterate, and the update
+    // rounds of the others (each system keeps its own iteration index)
+    int k = 1;
+    const int kmax = 4 * a.max_iter + 4;
+    while (k <= kmax) {
+        int nact = 0;
+        if (!eob_load_coefs(a, gen, nsys, s_mode, s_par, s_fa, s_fb, s_fc, &nact)) return;
+        if (nact == 0) break;
+        pass(false);
+        // kRu: fold chi_e += xs + alpha v (float-float); xs = 0
+        for_sites(1 << kRu, [&](const SysDev& S, int q, int m, int, bool, bool on) {
+            if (!on) return;
+            SiteFF xv = ld_ff(S.x, m);
+            const Site<W, K> xs = YK_LD(W, K, S.xs32, m);
+            const Site<W, K> vv = YK_LD(W, K, S.v32, m);
+            const float al = s_fa[q];
+            Site<W, K> zw;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float pr = __fmul_rn(al, vv.v[e]);   // alpha v exactly: (pr, its FMA error)
+                xv.v[e] = ff_add(xv.v[e], FF{xs.v[e], 0.f});
+                xv.v[e] = ff_add(xv.v[e], FF{pr, __fmaf_rn(al, vv.v[e], -pr)});
+                zw.v[e] = W(0);
+            }
+            st_ff(S.x, m, xv);
+            YK_ST(W, K, S.xs32, m, zw);
+        });
+        // kRu2: u = -A_o^-1 H^dag_oe chi_e (odd, t64)
+        for_sites(1 << kRu2, [&](const SysDev& S, int, int m, int, bool, bool on) {
+            if (!on) return;
+            const Geo g = geo(S, m, 1);
+            SiteFF zero;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) zero.v[e] = FF{0.f, 0.f};
+            SiteFF h = eo_ff<true, 0>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, FF{0.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
+            const FF sc = ld_ff1(S.dinv, m);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) h.v[e] = ff_mul(FF{-sc.hi, -sc.lo}, h.v[e]);
+            st_ff(S.t64, m, h);
+        });
+        // kRu3: r = rhs_e - (A_e chi_e + H^dag_eo u); |r|^2, <r, p_{k-1}>
+        for_sites(1 << kRu3, [&](const SysDev& S, int q, int m, int tile, bool tile_on, bool on) {
+            const int cur = s_par[q], prv = cur ^ 1;
+            float v0 = 0.f, v2 = 0.f;
+            if (on) {
+                const SysDev& SF = a.sys_full[a.sys_first + q];
+                const Geo g = geo(S, m, 0);
+                const FF de = ff_of(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + g.b]);
+                const SiteFF sx =
+                    eo_ff<true, 2>(S.t64, m, S.V, S.Nx, g.du, g.dd, ld_ff(S.x, m), de, hop_of_r(S.r), g.sp, g.sm);
+                const SiteFF bv = ld_ff(S.x + 4 * (size_t)S.V, m);
+                const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
+                Site<W, K> rw;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) rw.v[e] = ff_sub(bv.v[e], sx.v[e]).hi;
+                YK_ST(W, K, S.r32[cur], m, rw);
+                W dummy;
+                v0 = site_norm2<W, K>(rw);
+                site_dot<W, K>(rw, pw, v2, dummy);
+            }
+            FF f[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
+            f[0] = FF{v0, 0.f};
+            f[2] = FF{v2, 0.f};
+            put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
+        });
+        if (!eop_reduce(a, gen, k, red, &s_active, &s_ru, s_mode, s_par)) return;
+        ++k;
+    }
+    // chi of both classes in the full layout (t64) for the force
+    if (!eob_barrier(a, gen)) return;
+    for_sites(kAll | (1 << kIdle), [&](const SysDev& S, int q, int m, int, bool, bool on) {
+        if (!on) return;
+        const SysDev& SF = a.sys_full[a.sys_first + q];
+        Geo g = geo(S, m, 0);
+        const SiteFF xe = ld_ff(S.x, m);
+        Site<double, K> ce;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ce.v[e] = dbl_of(xe.v[e]);
+        store_site<double, K>(SF.t64, 2 * m + g.b, ce);
+        g = geo(S, m, 1);
+        SiteFF zero;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) zero.v[e] = FF{0.f, 0.f};
+        const SiteFF h = eo_ff<true, 0>(S.x, m, S.V, S.Nx, g.du, g.dd, zero, FF{0.f, 0.f}, hop_of_r(S.r), g.sp, g.sm);
+        const int n = 2 * m + g.b;
+        const SiteFF e = ff_site_of(load_site<double, K>(SF.b, n), SF.gen_eta != 0);
+        const FF inv = ld_ff1(S.dinv, m);
+        Site<double, K> co;
+#pragma unroll
+        for (int e2 = 0; e2 < 4; ++e2) co.v[e2] = dbl_of(ff_mul(ff_sub(e.v[e2], h.v[e2]), inv));
+        store_site<double, K>(SF.t64, n, co);
+    });
+    if (blockIdx.x == 0)
+        for (int q = threadIdx.x; q < nsys; q += blockDim.x) a.st[a.sys_first + q].chi_ready = 1;
+}
+
+
 // Shared memory of cg_eo_kernel for `own` compact sites per block and a
 // staged buffer of nb cells: p, r, q, w (then u) and v on the buffer, the chi
 // increment and v on the own sites, A_e and 1 / A_o in FP32 on the buffer.
@@ -3813,6 +4311,26 @@ static int eob_max_grid()
     return maxg;
 }
 
+static int eop_max_grid()
+{
+    static int maxg = -1;
+    if (maxg < 0) {
+        const int smem = (int)eop_smem_bytes();
+        cudaFuncSetAttribute((const void*)cg_eop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)cg_eop_kernel, kHaloThreads, smem) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            per = 0;
+        }
+        maxg = per * nsm;
+        if (maxg > kMaxGrid) maxg = kMaxGrid;
+    }
+    return maxg;
+}
+
 static int halo_max_grid()
 {
     static int maxg = -1;
@@ -3837,6 +4355,7 @@ void cg_halo_init()
     eo_patch_max_grid<8>();
     eo_patch_max_grid<32>();
     eob_max_grid();
+    eop_max_grid();
 }
 
 static int capped(int maxg, int cap) { return cap > 0 && cap < maxg ? cap : maxg; }
@@ -3943,6 +4462,32 @@ static cudaError_t launch_cg_t(const CGArgs& a0, cudaStream_t stream, int* grid_
                                : px == 32 ? (const void*)cg_eo_kernel<32>
                                           : (const void*)cg_eo_kernel<0>;
                 return cudaLaunchKernelExC(&cfg, fn, args);
+            }
+            // lattices that 16 x 16 patches tile: the batched patch kernel
+            // (YK_CG_EOP=0: the four-pass kernel below), one block per SM
+            const char* pe = getenv("YK_CG_EOP");
+            if (a.eo_patches && !(pe && pe[0] == '0') && eop_max_grid() > 0) {
+                int pg = capped(eop_max_grid(), a.grid_cap);
+                const int want = a.eo_tile_end - a.eo_tile_begin;   // patches (one tile each)
+                if (pg > want) pg = want;
+                if (pg < 1) pg = 1;
+                e.grid = pg;
+                e.tiles_per_block = 1;
+                if (grid_out) *grid_out = pg;
+                if (kernel_out) *kernel_out = 5;
+                cg_prepare_kernel<<<1, 256, 0, stream>>>(e);
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(pg);
+                cfg.blockDim = dim3(kHaloThreads);
+                cfg.dynamicSmemBytes = eop_smem_bytes();
+                cfg.stream = stream;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeCooperative;
+                attr[0].val.cooperative = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                void* args[] = {&e};
+                return cudaLaunchKernelExC(&cfg, (const void*)cg_eop_kernel, args);
             }
             // the batched even-odd kernel: work dealt out per pass, so the
             // grid does not follow the tiles (at most one block per two tiles)

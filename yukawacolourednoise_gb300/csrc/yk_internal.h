@@ -140,6 +140,9 @@ struct CGArgs {
     SysDev* sys_eo;
     const int2* eo_tiles;
     int eo_tile_begin, eo_tile_end;
+    // every system's compact lattice is tiled by 32 x 16 patches (Nt a multiple
+    // of 32, Nx / 2 of 16): batches may take the patch kernel (cg_eop_kernel)
+    int eo_patches;
     // inside an even-odd launch: a.sys are the compact views, sys_full the
     // systems' full records (eta, sigma, t64); the first stopping threshold is
     // relative to |eta|^2, tile partial slot 5 of round 0
