@@ -149,6 +149,7 @@ struct yk_ctx {
         int c;
         const double* in;
         double* out;
+        const void *in_dev, *out_dev;   // their mapped device addresses when captured
         cudaGraphExec_t exec;
         uint64_t used;
     };
@@ -1764,7 +1765,7 @@ yk_ctx::IoGraph* io_graph(yk_ctx* ctx, int c, const double* in, double* out, voi
 {
     ++ctx->io_clock;
     for (auto& g : ctx->io)
-        if (g.c == c && g.in == in && g.out == out) {
+        if (g.c == c && g.in == in && g.out == out && g.in_dev == in_dev && g.out_dev == out_dev) {
             g.used = ctx->io_clock;
             return &g;
         }
@@ -1827,7 +1828,7 @@ yk_ctx::IoGraph* io_graph(yk_ctx* ctx, int c, const double* in, double* out, voi
         cudaGraphExecDestroy(lru->exec);
         ctx->io.erase(lru);
     }
-    ctx->io.push_back({c, in, out, exec, ctx->io_clock});
+    ctx->io.push_back({c, in, out, in_dev, out_dev, exec, ctx->io_clock});
     return &ctx->io.back();
 }
 

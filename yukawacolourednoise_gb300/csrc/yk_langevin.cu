@@ -90,6 +90,15 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
     __shared__ int s_last;
     const int2 ct = s.tiles[blockIdx.x];
     ChainDev& C = s.ch[ct.x];
+    const int n = ct.y + threadIdx.x;
+    // the site's operands first: their loads overlap thread 0's FP64 division
+    // and square root below
+    double v = 0.0, dr = 0.0, xn = 0.0;
+    if (n < C.V) {
+        v = C.phi[n];
+        dr = C.drift[n];
+        xn = C.xi[n];
+    }
     if (threadIdx.x == 0) {
         double m = __longlong_as_double((long long)*(volatile unsigned long long*)&C.dmax_bits);
         if (m > 1e5) m = 1e5;               // langevin_gpu_v2.cu:83-91
@@ -102,11 +111,9 @@ __global__ void __launch_bounds__(kTile) update_kernel(StepArgs s, const CGState
     __syncthreads();
     const double eps = s_eps;
     const double fact = s_fact;
-    const int n = ct.y + threadIdx.x;
     double p1 = 0.0, p2 = 0.0;
     if (n < C.V) {
-        double v = C.phi[n];
-        v -= eps * C.drift[n] + fact * C.xi[n];
+        v -= eps * dr + fact * xn;
         C.phi[n] = v;
         p1 = v;
         p2 = v * v;
