@@ -368,17 +368,37 @@ void prof_end(yk_ctx* ctx, int cls, cudaEvent_t a, int launches)
 // the kernel classes one after the other.
 void eo_args(const yk_ctx* ctx, CGArgs& a);
 
+// The arguments of the step's CG launch (every system, Philox sources).
+CGArgs step_cg_args(yk_ctx* ctx)
+{
+    CGArgs a = base_args(ctx);
+    a.sys = ctx->d_sys;
+    a.sys_first = 0;
+    a.sys_count = ctx->nsys;
+    a.tiles = ctx->d_sys_tiles;
+    a.tile_begin = 0;
+    a.tile_end = ctx->n_sys_tiles;
+    a.eta_kind = 2;
+    a.st = ctx->d_state;
+    a.partial = ctx->d_partial;
+    a.coef = ctx->d_coef;
+    if (ctx->nsys == 1 && ctx->cg_halo)
+        for (const Chain& C : ctx->ch)
+            if (C.n_rhs_step > 0) {
+                a.solo_nt = C.Nt;
+                a.solo_nx = C.Nx;
+            }
+    eo_args(ctx, a);
+    return a;
+}
+
 int enqueue_step(yk_ctx* ctx)
 {
     cudaEvent_t e = nullptr;
     NoiseTables nt = {ctx->d_rows, ctx->nrows, ctx->d_cols, ctx->ncols, ctx->d_white, ctx->nwhite};
     int free_sm = 0;
-    if (ctx->noise_overlap && !ctx->profiling && !ctx->cg_cluster && ctx->nsys > 0 && ctx->nrows > 0) {
-        CGArgs g = base_args(ctx);
-        g.tile_begin = 0;
-        g.tile_end = ctx->n_sys_tiles;
-        free_sm = ctx->n_sm - cg_predict_grid(g, ctx->precision == YK_MIXED);
-    }
+    if (ctx->noise_overlap && !ctx->profiling && !ctx->cg_cluster && ctx->nsys > 0 && ctx->nrows > 0)
+        free_sm = ctx->n_sm - cg_predict_grid(step_cg_args(ctx), ctx->precision == YK_MIXED);
     const bool overlap = free_sm >= 8 && ctx->overlap_choice != 0;
     if (overlap) {
         YK_CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
@@ -395,24 +415,7 @@ int enqueue_step(yk_ctx* ctx)
     }
     if (ctx->nsys > 0) {
         prof_begin(ctx, &e);
-        CGArgs a = base_args(ctx);
-        a.sys = ctx->d_sys;
-        a.sys_first = 0;
-        a.sys_count = ctx->nsys;
-        a.tiles = ctx->d_sys_tiles;
-        a.tile_begin = 0;
-        a.tile_end = ctx->n_sys_tiles;
-        a.eta_kind = 2;
-        a.st = ctx->d_state;
-        a.partial = ctx->d_partial;
-        a.coef = ctx->d_coef;
-        if (ctx->nsys == 1 && ctx->cg_halo)
-            for (const Chain& C : ctx->ch)
-                if (C.n_rhs_step > 0) {
-                    a.solo_nt = C.Nt;
-                    a.solo_nx = C.Nx;
-                }
-        eo_args(ctx, a);
+        CGArgs a = step_cg_args(ctx);
         if (ctx->cg_cluster) {
             YK_CK(launch_eta(ctx->d_sys, ctx->d_sys_tiles, ctx->n_sys_tiles, 2, ctx->stream));
             YK_CK(launch_cg_cluster(a, ctx->cluster_sites, ctx->stream));
@@ -657,10 +660,7 @@ int tune_overlap(yk_ctx* ctx)
 {
     yk_tune_result& T = ctx->tune;
     if (!ctx->noise_overlap || ctx->cg_cluster || ctx->nsys == 0 || ctx->nrows == 0 || ctx->pions) return YK_OK;
-    CGArgs g = base_args(ctx);
-    g.tile_begin = 0;
-    g.tile_end = ctx->n_sys_tiles;
-    if (ctx->n_sm - cg_predict_grid(g, ctx->precision == YK_MIXED) < 8) return YK_OK;
+    if (ctx->n_sm - cg_predict_grid(step_cg_args(ctx), ctx->precision == YK_MIXED) < 8) return YK_OK;
     const int nch = (int)ctx->ch.size();
     size_t nphi = 0;
     for (const Chain& C : ctx->ch) nphi += (size_t)C.V;

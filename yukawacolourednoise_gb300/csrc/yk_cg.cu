@@ -4360,8 +4360,22 @@ void cg_halo_init()
 
 static int capped(int maxg, int cap) { return cap > 0 && cap < maxg ? cap : maxg; }
 
+static bool eo_single_variant(const CGArgs& a, int* px, int* grid, int* tpb, size_t* smem);
+
+// The grid launch_cg would use for `a` (the even-odd kernels' when the caller
+// gave the compact views, as launch_cg_t picks them).
 int cg_predict_grid(const CGArgs& a, bool mixed)
 {
+    if (mixed && a.sys_eo && a.eo_tiles && a.mtype == YK_DAGGER && a.balance == nullptr &&
+        a.sys_count <= kEobMaxSys) {
+        int px = 0, eg = 0, etpb = 1;
+        size_t es = 0;
+        if (eo_single_variant(a, &px, &eg, &etpb, &es)) return eg;
+        const int nt = a.eo_tile_end - a.eo_tile_begin;
+        const char* pe = getenv("YK_CG_EOP");
+        if (a.eo_patches && !(pe && pe[0] == '0') && eop_max_grid() > 0) return std::min(capped(eop_max_grid(), a.grid_cap), std::max(nt, 1));
+        return std::min(capped(eob_max_grid(), a.grid_cap), std::max((nt + 1) / 2, 1));
+    }
     int tpb = 1;
     return cg_grid_for(a.tile_end - a.tile_begin,
                        capped(mixed ? max_grid_t<1, true>() : max_grid_t<1, false>(), a.grid_cap), &tpb);
