@@ -2382,23 +2382,12 @@ __device__ __forceinline__ Site<float, 1> eo_sm(const float4* in, int j, int Nh,
                                         diag, r, sp, sm);
 }
 
-// the same in FP64 from a compact global vector (neighbours of compact m)
-template <bool DAG>
-__device__ __forceinline__ Site<double, 1> eo_gl(const double* in, int m, int Ve, int Nh, int dxu, int dxd,
-                                                 const Site<double, 1>& c, double diag, double r, double sp, double sm)
-{
-    const int mu = m + Nh >= Ve ? m + Nh - Ve : m + Nh, md = m - Nh < 0 ? m - Nh + Ve : m - Nh;
-    return dirac_combine<double, 1, DAG>(c, load_site<double, 1>(in, mu), load_site<double, 1>(in, md),
-                                         load_site<double, 1>(in, m + dxu), load_site<double, 1>(in, m + dxd), diag, r,
-                                         sp, sm);
-}
-
-// cg_eo_kernel's reliable updates, round 0 and reconstruction in float-float
-// (about 48 significant bits, on the FP32 pipes: GB300 issues FP64 at 1/64
-// of the FP32 rate and these passes were bound by it).  chi_e, rhs_e and the
-// odd intermediate keep the FP64 vectors' 32 bytes a compact site: four hi
-// words, then four lo words; 1 / A_o keeps its 8 bytes as (hi, lo).  Only the
-// kernel reads them; chi goes out to the force in FP64.
+// The even-odd kernels' reliable updates, round 0 and reconstruction in
+// float-float (about 48 significant bits, on the FP32 pipes: GB300 issues
+// FP64 at 1/64 of the FP32 rate and these passes were bound by it).  chi_e,
+// rhs_e and the odd intermediate keep the FP64 vectors' 32 bytes a compact
+// site: four hi words, then four lo words; 1 / A_o keeps its 8 bytes as (hi,
+// lo).  Only the kernels read them; chi goes out to the force in FP64.
 struct SiteFF {
     FF v[4];
 };
@@ -2496,7 +2485,8 @@ __device__ __forceinline__ SiteFF combine_ff(const SiteFF& c, FF diag, const Sit
     return o;
 }
 
-// eo_gl in float-float: the neighbours of compact m in a float-float vector
+// the odd/even half hop of compact m from a float-float vector (its four
+// neighbours at m +- Nh, m + dxu, m + dxd)
 template <bool DAG, int MODE>
 __device__ __forceinline__ SiteFF eo_ff(const double* in, int m, int Ve, int Nh, int dxu, int dxd, const SiteFF& c,
                                         FF diag, const HopFF& h, float sp, float sm)
