@@ -1586,10 +1586,18 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool w
         for (int i = 0; i < 6; ++i) red2[w * 6 + i] = make_float2(v[i].hi, v[i].lo);
     __syncthreads();
     const int ts = threadIdx.x % kTile, w0 = (threadIdx.x / kTile) * hw;
-    if (write && ts < 6) {
-        const int i = ts;
-        FF t{red2[w0 * 6 + i].x, red2[w0 * 6 + i].y};
-        for (int u = 1; u < hw; ++u) t = ff_add(t, FF{red2[(w0 + u) * 6 + i].x, red2[(w0 + u) * 6 + i].y});
+    // the tile's hw warp sums of slot i by a fixed tree over an aligned group
+    // of hw lanes (thread ts < 6 hw: slot ts / hw, warp ts % hw; the groups of
+    // slots 0-3 fill the tile's first warp, those of 4-5 half its second)
+    static_assert(6 * hw <= 64 && (hw & (hw - 1)) == 0, "six slots' groups in two warps");
+    if (ts < 6 * hw) {
+        const int i = ts / hw, u = ts % hw;
+        const unsigned mask = ts < 32 ? 0xffffffffu : (unsigned)((1ull << (6 * hw - 32)) - 1ull);
+        FF t{red2[(w0 + u) * 6 + i].x, red2[(w0 + u) * 6 + i].y};
+#pragma unroll
+        for (int o = hw / 2; o > 0; o >>= 1)
+            t = ff_add(t, FF{__shfl_xor_sync(mask, t.hi, o), __shfl_xor_sync(mask, t.lo, o)});
+        if (!write || u != 0) return;
 #ifdef YK_CG_CHECKED
         if (tile < a.tile_begin || tile >= a.tile_end) {
             if (atomicCAS(&g_cg_bad, 0, __LINE__) == 0) printf("cg check: bad partial tile %d\n", tile);
