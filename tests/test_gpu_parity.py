@@ -385,6 +385,26 @@ def test_evenodd_512_takes_32x32_patches(ylib, cuda, monkeypatch):
     assert np.abs(got - want).max() < 1e-8
 
 
+def test_evenodd_1024_single_chain_takes_the_patch_kernel(ylib, cuda, monkeypatch):
+    # 1024 x 1024, one chain: no single-system form fits (its 32 x 32 patches
+    # are 512), so the batched patch kernel runs with one system; the step
+    # agrees with the FP64 oracle
+    yk = ylib
+    Nt = Nx = 1024
+    monkeypatch.delenv("YK_CG_EOP", raising=False)
+    p = params(yk, Nt, Nx, precision=yk.YK_MIXED, cg_tol=1e-10, fixed_dt=0.01, reliable_every=50)
+    with yk.Context(p) as ctx:
+        phi = ctx.get_field()
+        ctx.profile_begin()
+        ctx.step(1)
+        pr = ctx.profile_end()
+        assert pr.cg_kernel == 5, pr.cg_kernel
+        got = ctx.get_field()
+        assert ctx.observables().status == 0
+    want, _ = O.langevin_step(Nt, Nx, act(p), phi, 1234, 0, 0, tol=1e-10, tol_mode=1, fixed_dt=0.01)
+    assert np.abs(got - want).max() < 1e-8
+
+
 def test_evenodd_force_and_condensate_match_the_full_solve(ylib, cuda, monkeypatch):
     # yk_fermion_force (the step's Philox source) and yk_condensate through
     # the even-odd solve against the same calls through the D^dag D solve
