@@ -46,6 +46,8 @@ def lib():
             "yko_normals": (None, [u64, u32, u64, u32, u32, i64, P]),
             "yko_normals_fp64": (None, [u64, u32, u64, u32, u32, i64, P]),
             "yko_normal_pair_words": (None, [u32, u32, P]),
+            "yko_ff_ops": (None, [i64, P, P, P, P, P]),
+            "yko_ff_hop": (None, [i, i, d, P, d, P, P, P, P, d, d, P]),
             "yko_uniform_field": (None, [u64, u32, i64, P]),
             "yko_uniform_field_comp": (None, [u64, u32, u32, i64, P]),
             "yko_drand48_field": (None, [i64, P]),
@@ -185,6 +187,25 @@ def normal_pair_words(a, b):
     """The generator's pair from explicit Philox words: a sets the radius, b the angle."""
     out = np.empty(2)
     lib().yko_normal_pair_words(a, b, _p(out))
+    return out
+
+
+def ff_ops(a, b):
+    """The GPU even-odd kernels' float-float sum, product and reciprocal of the
+    float-float splits of a and b (accuracy tests)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    s, p, r = np.empty_like(a), np.empty_like(a), np.empty_like(a)
+    lib().yko_ff_ops(a.size, _p(a), _p(b), _p(s), _p(p), _p(r))
+    return s, p, r
+
+
+def ff_hop(dag, mode, r, c, diag, tu, td, xu, xd, sp, sm):
+    """One real site of the kernels' float-float half hop (four components)."""
+    arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (c, tu, td, xu, xd)]
+    out = np.empty(4)
+    lib().yko_ff_hop(int(dag), int(mode), float(r), _p(arrs[0]), float(diag), _p(arrs[1]), _p(arrs[2]),
+                     _p(arrs[3]), _p(arrs[4]), float(sp), float(sm), _p(out))
     return out
 
 

@@ -899,3 +899,131 @@ void yko_gamma_method(const double* data, int64_t n, double stau, double out[5])
     out[4] = tau * 2.0 * sqrt(((double)W - tau + 0.5) / (double)n);
     free(gam);
 }
+
+/* ------------------------------------------------------------------------
+   Float-float arithmetic of the GPU's even-odd reliable updates, round 0 and
+   reconstruction of chi, restated for the accuracy tests (test
+   infrastructure: tests/test_oracle.py measures it against long-double
+   arithmetic; the kernels hold their own copy in csrc/yk_cg.cu).  A value is
+   hi + lo, two floats.  Sums use Knuth's two-sum of the high words with the
+   low words added; products use Dekker's product with the error term from
+   fmaf; the reciprocal takes one Newton step from the correctly rounded float
+   reciprocal.  The file is compiled with -ffp-contract=off, so the only
+   fused operations are the explicit fmaf calls, as in the kernels. */
+typedef struct {
+    float hi, lo;
+} yko_ff;
+
+static yko_ff ff_add(yko_ff a, yko_ff b)
+{
+    const float s = a.hi + b.hi;
+    const float bp = s - a.hi;
+    float e = (a.hi - (s - bp)) + (b.hi - bp);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    yko_ff r = {hi, e - (hi - s)};
+    return r;
+}
+
+static yko_ff ff_renorm(float p, float e)
+{
+    const float hi = p + e;
+    yko_ff r = {hi, e - (hi - p)};
+    return r;
+}
+
+static yko_ff ff_mul(yko_ff a, yko_ff b)
+{
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return ff_renorm(p, e);
+}
+
+static yko_ff ff_mul_f(yko_ff a, float b)
+{
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return ff_renorm(p, e);
+}
+
+static yko_ff ff_of(double x)
+{
+    const float hi = (float)x;
+    yko_ff r = {hi, (float)(x - (double)hi)};
+    return r;
+}
+
+static yko_ff ff_neg(yko_ff a)
+{
+    yko_ff r = {-a.hi, -a.lo};
+    return r;
+}
+
+static double ff_dbl(yko_ff a) { return (double)a.hi + (double)a.lo; }
+
+static yko_ff ff_rcp(yko_ff d)
+{
+    const float y = 1.0f / d.hi;
+    const yko_ff one = {1.0f, 0.0f}, y0 = {y, 0.0f};
+    const yko_ff e = ff_add(one, ff_neg(ff_mul_f(d, y)));
+    return ff_add(y0, ff_mul_f(e, y));
+}
+
+void yko_ff_ops(int64_t n, const double* a, const double* b, double* sum, double* prod, double* rcp)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        const yko_ff A = ff_of(a[i]), B = ff_of(b[i]);
+        sum[i] = ff_dbl(ff_add(A, B));
+        prod[i] = ff_dbl(ff_mul(A, B));
+        rcp[i] = ff_dbl(ff_rcp(A));
+    }
+}
+
+/* One site of the half hop in float-float, in the kernels' order of terms
+   (csrc/yk_cg.cu combine_ff, DAG 0 or 1; mode 0: H alone, 1: c + H, 2:
+   diag c + H) for a real site of four components (flavour f: upper 2f, lower
+   2f + 1); the coefficients from r as the kernels' hop_of_r forms them. */
+void yko_ff_hop(int dag, int mode, double r, const double* c, double diag, const double* tu, const double* td,
+                const double* xu, const double* xd, double sp, double sm, double* out)
+{
+    const yko_ff rr = ff_of(r), one = {1.0f, 0.0f}, mone = {-1.0f, 0.0f};
+    const yko_ff rp = ff_add(rr, one), rm = ff_add(rr, mone);
+    const yko_ff P = {-0.5f * rp.hi, -0.5f * rp.lo}, M = {-0.5f * rm.hi, -0.5f * rm.lo},
+                 A = {-0.5f * rr.hi, -0.5f * rr.lo};
+    const float fsp = (float)sp, fsm = (float)sm;
+    const yko_ff Pp = {fsp * (dag ? P : M).hi, fsp * (dag ? P : M).lo};
+    const yko_ff Mp = {fsp * (dag ? M : P).hi, fsp * (dag ? M : P).lo};
+    const yko_ff Mm = {fsm * (dag ? M : P).hi, fsm * (dag ? M : P).lo};
+    const yko_ff Pm = {fsm * (dag ? P : M).hi, fsm * (dag ? P : M).lo};
+    const float bx = dag ? -0.5f : 0.5f;
+    const yko_ff dg = ff_of(diag);
+    for (int f = 0; f < 2; ++f) {
+        const int iu = 2 * f, id = 2 * f + 1;
+        yko_ff ou, od;
+        const yko_ff tuu = ff_of(tu[iu]), tud = ff_of(tu[id]), tdu = ff_of(td[iu]), tdd = ff_of(td[id]);
+        const yko_ff xuu = ff_of(xu[iu]), xud = ff_of(xu[id]), xdu = ff_of(xd[iu]), xdd = ff_of(xd[id]);
+        if (mode == 0) {
+            ou = ff_mul(Pp, tuu);
+            od = ff_mul(Mp, tud);
+        } else {
+            const yko_ff cu = ff_of(c[iu]), cd = ff_of(c[id]);
+            ou = mode == 1 ? cu : ff_mul(dg, cu);
+            od = mode == 1 ? cd : ff_mul(dg, cd);
+            ou = ff_add(ou, ff_mul(Pp, tuu));
+            od = ff_add(od, ff_mul(Mp, tud));
+        }
+        ou = ff_add(ou, ff_mul(Mm, tdu));
+        od = ff_add(od, ff_mul(Pm, tdd));
+        const yko_ff dfu = ff_add(xud, ff_neg(xdd)), dfd = ff_add(xuu, ff_neg(xdu));
+        const yko_ff bu = {bx * dfu.hi, bx * dfu.lo}, bd = {bx * dfd.hi, bx * dfd.lo};
+        ou = ff_add(ou, bu);
+        od = ff_add(od, bd);
+        ou = ff_add(ou, ff_mul(A, ff_add(xuu, xdu)));
+        od = ff_add(od, ff_mul(A, ff_add(xud, xdd)));
+        out[iu] = ff_dbl(ou);
+        out[id] = ff_dbl(od);
+    }
+}

@@ -90,6 +90,12 @@ void yko_normals(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, ui
                  int64_t n, double* out);
 /* One pair of yko_normals from explicit Philox words a (radius), b (angle). */
 void yko_normal_pair_words(uint32_t a, uint32_t b, double out[2]);
+/* The GPU even-odd kernels' float-float arithmetic (accuracy tests only):
+   sum, product and reciprocal of float-float splits of a[i], b[i]; one site
+   of the half hop in float-float. */
+void yko_ff_ops(int64_t n, const double* a, const double* b, double* sum, double* prod, double* rcp);
+void yko_ff_hop(int dag, int mode, double r, const double* c, double diag, const double* tu, const double* td,
+                const double* xu, const double* xd, double sp, double sm, double* out);
 /* The same words through FP64 libm Box-Muller (accuracy check of yko_normals). */
 void yko_normals_fp64(uint64_t seed, uint32_t chain, uint64_t step, uint32_t kind, uint32_t rhs,
                       int64_t n, double* out);

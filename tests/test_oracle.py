@@ -292,3 +292,64 @@ def test_evenodd_cgne_stops_on_the_true_residual(Nt, Nx, m0):
     assert res_eo <= 1.05e-10 and res_cg <= 1.05e-10, (res_eo, res_cg)
     assert np.abs(chi_eo - chi_cg).max() < 1e-7 * np.abs(chi_cg).max()
     assert it_eo * 1.5 < it_cg, (it_eo, it_cg)
+
+
+def _ff_split(x):
+    hi = x.astype(np.float32)
+    lo = (x - hi.astype(np.float64)).astype(np.float32)
+    return np.longdouble(1) * hi + np.longdouble(1) * lo
+
+
+def test_float_float_arithmetic_accuracy():
+    # the GPU even-odd kernels' float-float sum, product and reciprocal
+    # (restated in the oracle: two-sum with the low words added, Dekker's
+    # product through fmaf, one Newton step for 1/d) against long double on
+    # the same float-float inputs: within 2^-45 of the exact result, relative
+    # to |a| + |b| for sums and to the result for products and reciprocals
+    rng = np.random.default_rng(21)
+    n = 200000
+    a = rng.normal(size=n) * 10.0 ** rng.uniform(-6, 6, n)
+    b = rng.normal(size=n) * 10.0 ** rng.uniform(-6, 6, n)
+    b[: n // 4] = -a[: n // 4] * (1 + rng.normal(size=n // 4) * 1e-9)   # near-cancelling sums
+    s, p, r = O.ff_ops(a, b)
+    A, B = _ff_split(a), _ff_split(b)
+    tol = 2.0 ** -45
+    assert np.max(np.abs(np.longdouble(1) * s - (A + B)) / (np.abs(A) + np.abs(B))) < tol
+    assert np.max(np.abs((np.longdouble(1) * p - A * B) / (A * B))) < tol
+    assert np.max(np.abs((np.longdouble(1) * r - 1 / A) * A)) < tol
+
+
+@pytest.mark.parametrize("r", [1.0, 0.7])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("dag", [0, 1])
+def test_float_float_half_hop_accuracy(dag, mode, r):
+    # one site of the kernels' float-float half hop (reliable updates: H chi,
+    # A_e chi + H u; round 0: eta_e + H t) against the Wilson-Dirac site
+    # formula in long double on the same float-float inputs: the error stays
+    # within 2^-44 of the sum of the terms' magnitudes, so a true residual
+    # r = rhs - S chi formed from it is off by about 1e-13 |rhs| at most
+    rng = np.random.default_rng(22 + 7 * dag + mode)
+    L = np.longdouble
+    worst = 0.0
+    for _ in range(400):
+        c, tu, td, xu, xd = (rng.normal(size=4) * 10.0 ** rng.uniform(-3, 3) for _ in range(5))
+        diag = rng.uniform(1.0, 4.0)
+        sp, sm = rng.choice([-1.0, 1.0], size=2)
+        got = O.ff_hop(dag, mode, r, c, diag, tu, td, xu, xd, sp, sm)
+        C_, TU, TD, XU, XD = (_ff_split(v) for v in (c, tu, td, xu, xd))
+        R, D = _ff_split(np.array([r]))[0], _ff_split(np.array([diag]))[0]
+        P, M, A = -(R + 1) / 2, -(R - 1) / 2, -R / 2
+        cu_up, cd_up = sp * (P if dag else M), sp * (M if dag else P)
+        cu_dn, cd_dn = sm * (M if dag else P), sm * (P if dag else M)
+        bx = L(-0.5) if dag else L(0.5)
+        for f in range(2):
+            iu, id_ = 2 * f, 2 * f + 1
+            base_u = L(0) if mode == 0 else (C_[iu] if mode == 1 else D * C_[iu])
+            base_d = L(0) if mode == 0 else (C_[id_] if mode == 1 else D * C_[id_])
+            tu_terms = [base_u, cu_up * TU[iu], cu_dn * TD[iu], bx * (XU[id_] - XD[id_]), A * (XU[iu] + XD[iu])]
+            td_terms = [base_d, cd_up * TU[id_], cd_dn * TD[id_], bx * (XU[iu] - XD[iu]), A * (XU[id_] + XD[id_])]
+            for k, terms in ((iu, tu_terms), (id_, td_terms)):
+                want = sum(terms)
+                scale = sum(abs(t) for t in terms) + abs(XU[iu]) + abs(XD[iu]) + abs(XU[id_]) + abs(XD[id_])
+                worst = max(worst, float(abs(L(got[k]) - want) / scale))
+    assert worst < 2.0 ** -44, worst
