@@ -2659,7 +2659,12 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
         cell(j, 0, t, b, du, dd);
         dep[j] = (float)(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * buf_m(j) + b]);
     }
-    const double* rhs_e = S.x + 4 * (size_t)Ve;    // after chi_e (compact FP64)
+    const double* rhs_e = S.x + 4 * (size_t)Ve;    // after chi_e (compact float-float)
+    // the odd hops of the updates and round 0 (compact float-float, 32 bytes a
+    // site) in xs32, which this kernel leaves unused (its chi increment lives
+    // in shared memory): t64 is the output, so the last update's u survives
+    // the reconstruction of chi
+    double* const T = reinterpret_cast<double*>(S.xs32);
     unsigned epoch = 0, gen = 0;
     int staged_k = -1;
 #ifdef YK_CG_TIMING
@@ -2846,7 +2851,7 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             const FF s = ld_ff1(S.dinv, m);
 #pragma unroll
             for (int i = 0; i < 4; ++i) h.v[i] = ff_mul(FF{-s.hi, -s.lo}, h.v[i]);
-            st_ff(S.t64, m, h);
+            st_ff(T, m, h);
         }
         YK_TMARK(9);
         if (!nsync(a, ++epoch, deps)) return false;
@@ -2863,7 +2868,7 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
                 eo_geom(m, 0, Nh, sh, t, b, du, dd);
                 const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
                 const FF de = ff_of(2.0 * S.r + S.m0 + S.g * SF.sigma[2 * m + b]);
-                const SiteFF sx = eo_ff<true, 2>(S.t64, m, Ve, Nh, du, dd, ld_ff(chi, m), de, hop, sp, sm);
+                const SiteFF sx = eo_ff<true, 2>(T, m, Ve, Nh, du, dd, ld_ff(chi, m), de, hop, sp, sm);
                 const SiteFF bv = ld_ff(rhs_e, m);
                 const Site<W, K> pw = YK_LD(W, K, S.p32[prv], m);
                 Site<W, K> rw32;
@@ -2904,7 +2909,7 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             SiteFF h;
 #pragma unroll
             for (int i = 0; i < 4; ++i) h.v[i] = ff_mul(FF{-inv.hi, -inv.lo}, e.v[i]);
-            st_ff(S.t64, m, h);
+            st_ff(T, m, h);
         }
     }
     YK_TMARK(12);
@@ -2933,7 +2938,7 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
             const SiteFF e = ff_site_of(load_site<double, K>(SF.b, 2 * m + b), eta32);
             // eta_e + H^dag_eo (-A_o^-1 eta_o)
-            const SiteFF rh = eo_ff<true, 1>(S.t64, m, Ve, Nh, du, dd, e, FF{1.f, 0.f}, hop, sp, sm);
+            const SiteFF rh = eo_ff<true, 1>(T, m, Ve, Nh, du, dd, e, FF{1.f, 0.f}, hop, sp, sm);
             st_ff(const_cast<double*>(rhs_e), m, rh);
             Site<W, K> rw32;
 #pragma unroll
@@ -2995,9 +3000,33 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
 #endif
     }
     // chi of both classes in the full layout for the force (t64): every
-    // block's final chi_e and its own odd sites' chi_o = A_o^-1 (eta_o - H^dag_oe chi_e)
-    if (!nsync(a, ++epoch, deps)) return;
-    {
+    // block's final chi_e and its own odd sites' chi_o = A_o^-1 (eta_o - H^dag_oe chi_e).
+    // A solve that retired converged in an update round (the block's copy of
+    // the replicated state says so, alike in every block) has u = -A_o^-1
+    // H^dag_oe chi_e of its final chi_e in T already: chi_o = A_o^-1 eta_o + u,
+    // own sites only, no neighbour sync
+    if (lst.chi_ready && lst.converged) {
+        for (int o = threadIdx.x; o < own; o += NT) {
+            const int m = own_m(o);
+            int t, b, du, dd;
+            eo_geom(m, 0, Nh, sh, t, b, du, dd);
+            const SiteFF xe = ld_ff(S.x, m);
+            Site<double, K> ce;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) ce.v[i] = dbl_of(xe.v[i]);
+            store_site<double, K>(SF.t64, 2 * m + b, ce);
+            eo_geom(m, 1, Nh, sh, t, b, du, dd);
+            const int n = 2 * m + b;
+            const SiteFF e = ff_site_of(load_site<double, K>(SF.b, n), eta32);
+            const SiteFF u = ld_ff(T, m);
+            const FF inv = ld_ff1(S.dinv, m);
+            Site<double, K> co;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) co.v[i] = dbl_of(ff_add(ff_mul(e.v[i], inv), u.v[i]));
+            store_site<double, K>(SF.t64, n, co);
+        }
+    } else {
+        if (!nsync(a, ++epoch, deps)) return;
         const HopFF hop = s_hop;
         SiteFF zero;
 #pragma unroll
