@@ -837,6 +837,37 @@ __device__ bool fast_step(const CGArgs& a, int k, FF rr, FF apap, FF pap, FF rap
     return true;
 }
 
+// The scalar step of a reliable update on the FP32 pipes (scalar_step's
+// update branch, the mixed solver's FP32 restart coefficients) for an update
+// that leaves the solve running: p_k = r + beta (p_{k-1} - gamma r), beta =
+// |r|^2 / |r_{k-1}|^2, gamma = <r, p_{k-1}> / |r|^2.  An update near or below
+// the stop (the FP64 comparison decides), at the iteration cap, or with a
+// value outside FP32's range takes the FP64 step, which also stores the
+// host-visible state.
+__device__ bool fast_ru_step(const CGArgs& a, int k, FF rr, FF rp, CGState& st, SysLocal& L)
+{
+    const float rrf = rr.hi + rr.lo, rpf = (float)st.rr_prev, stop2f = (float)st.stop2;
+    if (!(rrf > FLT_MIN) || !(rrf < FLT_MAX) || !(rpf > FLT_MIN) || !(rpf < FLT_MAX)) return false;
+    if (!(rrf > 1.001f * stop2f) || k >= a.max_iter) return false;
+    const float inv = 1.f / rrf, beta = rrf / rpf;
+    const float c_re = 1.f - beta * ((rp.hi + rp.lo) * inv);
+    st.n_ru += 1;
+    st.rr = (double)rrf;
+    st.iters = k;
+    st.rmax2 = st.rr;
+    st.mode = kRedo;
+    L.mode = kRedo;
+    L.alpha_re = L.alpha_im = 0.0;
+    L.beta = (double)beta;
+    L.c_re = (double)c_re;
+    L.c_im = 0.0;
+    L.f_alpha_re = L.f_alpha_im = 0.f;
+    L.f_beta = beta;
+    L.f_c_re = c_re;
+    L.f_c_im = 0.f;
+    return true;
+}
+
 __device__ __forceinline__ void load_state(const CGState* p, CGState& st)
 {
     const volatile CGState& v = *p;
@@ -1212,7 +1243,10 @@ struct NoHook {
     __device__ void operator()() const {}
 };
 
-template <int K, bool MIXED, typename Hook = NoHook>
+// RUFIX: the caller's reliable updates add their partials to the fixed-point
+// totals too (put_partial_ff RU_SCALE), so an update round may take the fast
+// path (fast_ru_step) like an ordinary one.
+template <int K, bool MIXED, bool RUFIX = false, typename Hook = NoHook>
 __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen, int k, bool ru_round, double* red,
                                                  CGState& lst, SysLocal& L, int* s_nact, int* s_anyru, int* s_cnt,
                                                  int* esc, int* s_fast, FastShadow& fs, Hook after_barrier = Hook())
@@ -1253,7 +1287,7 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
     if (__syncthreads_or(bad)) return false;
     // the fixed-point totals of this barrier, if the tiles added them: lanes
     // 0-3 load one each, lane 4 the overflow flag -- ahead of the hook's loads
-    const bool fix_now = kFix && !ru_round && *s_fast;
+    const bool fix_now = kFix && (!ru_round || RUFIX) && *s_fast;
     long long Sv = 0;
     unsigned long long over_v = 0ull;
     if (fix_now && threadIdx.x < 5) {
@@ -1284,10 +1318,12 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
                 bool okl = true, conv = true;
                 FF fv = {0.f, 0.f};
                 int er = 0, due = 0;
+                // an update's <r, p> (lane 2) is at the scale of |r|^2
+                const int el = (ru_round && lane == 2) ? esc[0] : (lane < 4 ? esc[lane] : 0);
                 if (lane < 4) {
                     okl = Sv < kFixLimit && Sv > -kFixLimit;
-                    conv = okl && fix_to_ff(Sv, esc[lane], fv);
-                    if (lane < 3 && Sv > 0) er = fix_rescale(Sv, esc[lane]);
+                    conv = okl && fix_to_ff(Sv, el, fv);
+                    if (lane < 3 && Sv > 0) er = fix_rescale(Sv, el);
                 } else if (lane == 4) {
                     okl = over_v == 0ull;
                 } else if (lane == 5) {
@@ -1295,7 +1331,7 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
                 }
                 const bool ok = __all_sync(full, okl);
                 const bool convall = __all_sync(full, conv);
-                const bool pos = __all_sync(full, lane >= 3 || Sv > 0);
+                const bool pos = __all_sync(full, (ru_round ? lane != 0 : lane >= 3) || Sv > 0);
                 FF v[4];
                 long long S[4];
 #pragma unroll
@@ -1311,20 +1347,25 @@ __device__ __forceinline__ bool solo_reduce_body(const CGArgs& a, unsigned& gen,
                     bool done = false;
                     if (ok) {
                         // the ordinary step on the FP32 pipes; the FP64 one otherwise
-                        done = convall && lst.mode != kIdle && fast_step(a, k, v[0], v[1], v[2], v[3], due != 0, lst, fs, L);
+                        done = convall && lst.mode != kIdle &&
+                               (ru_round ? fast_ru_step(a, k, v[0], v[2], lst, L)
+                                         : fast_step(a, k, v[0], v[1], v[2], v[3], due != 0, lst, fs, L));
                         if (!done) {
                             s[0] = scalbn((double)S[0], -esc[0]);
                             s[1] = scalbn((double)S[1], -esc[1]);
-                            s[2] = scalbn((double)S[2], -esc[2]);
+                            s[2] = scalbn((double)S[2], -(ru_round ? esc[0] : esc[2]));
                             s[4] = scalbn((double)S[3], -esc[3]);
                             s[3] = s[5] = 0.0;
                         }
-                        // next scales straight from the integer totals
+                        // next scales straight from the integer totals (an
+                        // update's round renews the |r|^2 scale only)
                         if (pos) {
                             esc[0] = e0;
-                            esc[1] = e1;
-                            esc[2] = e2;
-                            esc[3] = (e0 + e1) / 2 - 1;   // |<r, Ap>| <= |r| |Ap|
+                            if (!ru_round) {
+                                esc[1] = e1;
+                                esc[2] = e2;
+                                esc[3] = (e0 + e1) / 2 - 1;   // |<r, Ap>| <= |r| |Ap|
+                            }
                             s_scales = 2;   // scales already set
                         } else {
                             s_scales = 3;   // no usable scales: the next sums go through the tile partials
@@ -1562,7 +1603,9 @@ __device__ __forceinline__ void put_partial(const CGArgs& a, int tile, bool writ
 // the warp butterfly runs in float-float; otherwise the warp sums are plain
 // FP32 (the per-site values are FP32 products).  The warps' sums are added in
 // warp order by one thread per value.
-template <int SKIP_MASK, bool WARP_FF>
+// RU_SCALE: a reliable update's partials (|r|^2 in slot 0, <r, p> in slot 2)
+// go into the fixed-point totals both at the scale of |r|^2.
+template <int SKIP_MASK, bool WARP_FF, bool RU_SCALE = false>
 __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool write, FF (&v)[6], double* red,
                                                long long (*fsum)[16] = nullptr, const int* esc = nullptr)
 {
@@ -1608,7 +1651,8 @@ __device__ __forceinline__ void put_partial_ff(const CGArgs& a, int tile, bool w
         if (fsum) {
             const int c = fix_value_of_slot(i);
             if (c >= 0) {
-                const long long v = to_fixed(t, esc[c]), lim = fix_tile_limit(a.tile_end - a.tile_begin);
+                const long long v = to_fixed(t, esc[(RU_SCALE && c == 2) ? 0 : c]),
+                                lim = fix_tile_limit(a.tile_end - a.tile_begin);
                 if (v < lim && v > -lim)
                     atomicAdd(reinterpret_cast<unsigned long long*>(&fsum[c][0]), (unsigned long long)v);
                 else
@@ -2808,7 +2852,7 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             stage(kStep, k1 & 1, (k1 & 1) ^ 1);
             staged_k = k1;
         };
-        return solo_reduce_body<K, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh,
+        return solo_reduce_body<K, true, true>(sa, gen, kk, ru, red, lst, sl[0], &s_nact, &s_anyru, s_cnt, s_esc, &s_fast, fsh,
                                          prefetch);
     };
 
@@ -2884,7 +2928,11 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             for (int i = 0; i < 6; ++i) f[i] = FF{0.f, 0.f};
             f[0] = FF{v0, 0.f};
             f[2] = FF{v2, 0.f};
-            put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
+            if (s_fast)   // the fixed-point totals too, at the scale of |r|^2
+                put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true, true>(
+                    a, tile, tile_on, f, red, a.bar->fsum[(gen + 1u) % 3u], s_esc);
+            else
+                put_partial_ff<(1 << 1) | (1 << 4) | (1 << 5) | kSkipIm, true>(a, tile, tile_on, f, red);
         }
         YK_TMARK(11);
         return true;
