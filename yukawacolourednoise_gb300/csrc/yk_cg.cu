@@ -2977,7 +2977,37 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
     YK_TMARK(13);
     // 1 / A_o in FP32 on the widened range, from the owners' dinv
     for (int j = SB + threadIdx.x; j < NB - SB; j += NT) dip[j] = ld_ff1(S.dinv, buf_m(j)).hi;
-    {
+    if constexpr (PATCH) {
+        // r_0 = p_0 = rhs_e on the whole widened patch, formed here: the odd
+        // values it reads (T, eta) lie in the eight surrounding patches, which
+        // the neighbour sync above waited for, so neither a second sync nor a
+        // staging of the neighbours' r_0 and p_0 is needed.  Every block forms
+        // a cell's value with the same operations, so the copies agree bit for
+        // bit; the own cells also go to rhs_e, r32[0] and p32[0].  Each thread
+        // writes the cells that pass_a1 reads in the same thread.
+        const HopFF hop = s_hop;
+        for (int j = threadIdx.x; j < NB; j += NT) {
+            const int m = buf_m(j);
+            int t, b, du, dd;
+            eo_geom(m, 0, Nh, sh, t, b, du, dd);
+            const float sp = (t + 1 == Nt) ? -1.f : 1.f, sm = (t == 0) ? -1.f : 1.f;
+            const SiteFF e = ff_site_of(load_site<double, K>(SF.b, 2 * m + b), eta32);
+            // eta_e + H^dag_eo (-A_o^-1 eta_o)
+            const SiteFF rh = eo_ff<true, 1>(T, m, Ve, Nh, du, dd, e, FF{1.f, 0.f}, hop, sp, sm);
+            Site<W, K> rw32;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) rw32.v[i] = rh.v[i].hi;
+            st_sm(P_st, j, rw32);
+            st_sm(R_st, j, rw32);
+            if (own_of(j) >= 0) {
+                st_ff(const_cast<double*>(rhs_e), m, rh);
+                YK_ST(W, K, S.r32[0], m, rw32);
+                YK_ST(W, K, S.p32[0], m, rw32);
+            }
+        }
+        YK_TMARK(14);
+        YK_TMARK(15);
+    } else {
         const HopFF hop = s_hop;
         for (int o = threadIdx.x; o < own; o += NT) {
             const int m = own_m(o);
@@ -2994,12 +3024,12 @@ __global__ void __launch_bounds__(eo_threads(PX), PX == 8 ? 2 : 1) cg_eo_kernel(
             YK_ST(W, K, S.r32[0], m, rw32);
             YK_ST(W, K, S.p32[0], m, rw32);
         }
+        YK_TMARK(14);
+        if (!nsync(a, ++epoch, deps)) return;
+        YK_TMARK(15);
+        stage(kHaloInit, 0, 0);
+        cp_async_wait_all();
     }
-    YK_TMARK(14);
-    if (!nsync(a, ++epoch, deps)) return;
-    YK_TMARK(15);
-    stage(kHaloInit, 0, 0);
-    cp_async_wait_all();
     pass_a1(kHaloInit, 0, 0);
     __syncthreads();
     pass_wvu();
